@@ -1,0 +1,385 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 feature front-end on the batched-uniform workload:
+64 consecutive 752x480 u8 frames of a seeded camera trajectory over a
+textured plane, each frame detected + described and matched against the
+previous one (63 pairs).  A step is one pass over the 64-frame batch.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints one JSON line (rank 0).  ``value`` = frames/s with inputs resident in
+HBM (graph replay of the 5-kernel batch, L2 flushed between steps);
+``e2e`` = the same through the C ABI with pinned-host H2D of the frames and
+D2H of every feature record and match list inside the timed region;
+``plain_fps`` = the plain per-frame form (one frame per launch sequence,
+synchronous per frame).  ``--impl reference`` times the CPU restatement of
+the reference's path (oracle port) on all host cores, on the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import multiprocessing as mp
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+W, H, LEVELS = 752, 480, 6
+METRIC = "frames/s detect+describe+match @752x480 (batched, 64-frame graph)"
+WORKLOAD = "batched-uniform: 64 consecutive 752x480 u8 frames, plane trajectory, consecutive-pair matching"
+
+
+def _args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--frames", type=int, default=64)
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--cpu-seconds", type=float, default=12.0, help="bounded CPU-baseline sample")
+    return ap.parse_args()
+
+
+def _dist():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+# ------------------------------------------------------------------ clocks
+
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons during a region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (OSError, ValueError):
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if self.proc is not None:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            if self.thread:
+                self.thread.join(timeout=2)
+        return summarize_clocks(self.lines)
+
+
+def summarize_clocks(lines: list[str]) -> dict:
+    sm, smax, reasons = [], [], set()
+    names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+    for ln in lines:
+        parts = [p.strip() for p in ln.split(",")]
+        if len(parts) < 7:
+            continue
+        try:
+            sm.append(float(parts[0]))
+            smax.append(float(parts[1]))
+        except ValueError:
+            continue
+        for name, flag in zip(names, parts[3:7]):
+            if flag.lower().startswith("active"):
+                reasons.add(name)
+    return {
+        "sm_mhz": statistics.median(sm) if sm else None,
+        "sm_max_mhz": max(smax) if smax else None,
+        "reasons": sorted(reasons),
+        "samples": len(sm),
+    }
+
+
+# ------------------------------------------------------------------ bytes
+
+def algorithmic_bytes(kept_per_frame: list[int], matches_per_pair: list[int], frames: int) -> dict:
+    """Per-frame algorithmic bytes of the path:
+    W*H (u8 LOD0 read) + 4*(P - W*H) (f32 levels written) + 48*N (feature
+    records written) + 32*(N + M) (descriptors read for matching, current +
+    reference) + 8*K (match index pairs written)."""
+    from uni_slam_gb300 import level_dims
+
+    dims = level_dims(W, H, LEVELS)
+    P = sum(w * h for w, h in dims)
+    wh = W * H
+    N = sum(kept_per_frame)
+    M = sum(kept_per_frame[:-1])  # each pair's reference set is the previous frame
+    K = sum(matches_per_pair)
+    total = frames * (wh + 4 * (P - wh)) + 48 * N + 32 * (N + M) + 8 * K
+    return {
+        "pyramid_per_frame": wh + 4 * (P - wh),
+        "describe_total": 48 * N,
+        "match_total": 32 * (N + M) + 8 * K,
+        "total_per_step": total,
+    }
+
+
+# ------------------------------------------------------------------ CPU side
+
+def _cpu_frame(args):
+    img, pattern = args
+    import oracle
+
+    return oracle.frame(img, pattern)
+
+
+def _cpu_match(args):
+    fa, fb = args
+    import oracle
+
+    return len(oracle.match(fa[0], fa[1], fb[0], fb[1], W, H))
+
+
+def cpu_baseline_sample(frames, pattern, seconds: float) -> dict:
+    """Single-threaded oracle port on a time-bounded prefix of the workload."""
+    import oracle
+
+    t0 = time.perf_counter()
+    prev = None
+    n = 0
+    for img in frames:
+        cur = oracle.frame(img, pattern)
+        if prev is not None:
+            oracle.match(prev[0], prev[1], cur[0], cur[1], W, H)
+        prev = cur
+        n += 1
+        if time.perf_counter() - t0 >= seconds and n >= 2:
+            break
+    dt = time.perf_counter() - t0
+    return {"value": n / dt, "unit": "frames/s", "cores": 1, "kind": "port",
+            "sample": f"first {n} frames of the workload (detect+describe each, match each against the previous), "
+                      f"CPU restatement of the reference path, 1 thread, {dt:.1f} s"}
+
+
+def run_reference(a):
+    rank, world, _ = _dist()
+    if rank != 0:
+        return
+    from uni_slam_gb300 import pattern as patmod
+    from uni_slam_gb300 import synth
+
+    pat = patmod.load()
+    frames = synth.config1_sequence(a.seed, n=a.frames)
+    cores = os.cpu_count() or 1
+    ctx = mp.get_context("spawn")
+    times = []
+    with ctx.Pool(cores) as pool:
+        for step in range(a.warmup + a.steps):
+            t0 = time.perf_counter()
+            feats = pool.map(_cpu_frame, [(f, pat) for f in frames])
+            pool.map(_cpu_match, [(feats[i], feats[i + 1]) for i in range(len(feats) - 1)])
+            dt = time.perf_counter() - t0
+            if step >= a.warmup:
+                times.append(dt)
+    step_s = statistics.mean(times)
+    value = a.frames / step_s
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "frames/s", "n_gpus": a.gpus,
+        "steps": a.steps, "warmup": a.warmup, "ms_per_step": step_s * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32+u32", "data": "synthetic (seeded; EuRoC absent)",
+        "config": {"workload": WORKLOAD, "frames": a.frames, "levels": LEVELS, "seed": a.seed},
+        "cpu_baseline": {"value": value, "unit": "frames/s", "cores": cores, "kind": "port",
+                         "sample": f"the full {a.frames}-frame step on a {cores}-process pool (CPU restatement of "
+                                   "the reference's WGSL passes + matcher; the WGSL passes cannot run through Dawn "
+                                   "on this box)"},
+        "e2e": {"value": value, "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ------------------------------------------------------------------ GPU side
+
+def run_ours(a):
+    rank, world, local = _dist()
+    import numpy as np
+    import torch
+
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    from uni_slam_gb300 import Batch, Context, Frontend
+    from uni_slam_gb300 import pattern as patmod
+    from uni_slam_gb300 import synth
+
+    pat = patmod.load()
+    frames = synth.config1_sequence(a.seed + rank, n=a.frames)
+    n = len(frames)
+    ctx = Context(pat, levels=LEVELS, max_width=W, max_height=H, device=local)
+    batch = Batch(ctx, [(W, H)] * n, [(i, i + 1) for i in range(n - 1)])
+    for i, f in enumerate(frames):
+        batch.set_frame(i, f)
+    batch.upload()
+    batch.sync()
+
+    stream = torch.cuda.Stream()
+    batch.set_stream(stream.cuda_stream)
+    l2_flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+
+    # ---- resident-input form (value)
+    for _ in range(a.warmup):
+        batch.run()
+    stream.synchronize()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(a.steps)]
+    clocks = ClockSampler(local)
+    barrier()
+    clocks.start()
+    t_wall = time.perf_counter()
+    with torch.cuda.stream(stream):
+        for e0, e1 in evs:
+            l2_flush.zero_()
+            e0.record(stream)
+            batch.run()
+            e1.record(stream)
+    stream.synchronize()
+    barrier()
+    wall_s = time.perf_counter() - t_wall
+    clk = clocks.stop()
+    step_ms = sum(e0.elapsed_time(e1) for e0, e1 in evs) / a.steps
+    step_ms_max = step_ms
+    if dist is not None:
+        t = torch.tensor([step_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        step_ms_max = float(t.item())
+    value = n * world / (step_ms_max / 1e3)
+
+    # ---- results of one step (counts for the byte model)
+    batch.download()
+    batch.sync()
+    kept = [int(batch.features(i)[1].sum()) for i in range(n)]
+    nmatch = [len(batch.matches(p)) for p in range(n - 1)]
+    nbytes = algorithmic_bytes(kept, nmatch, n)
+
+    # ---- per-kernel timing for the roofline (events on the launching stream)
+    prof = batch.profile(iters=5)
+    dom = max(prof, key=prof.get)
+    kernel_bytes = {
+        "k_detect": nbytes["pyramid_per_frame"] * n,
+        "k_describe": nbytes["describe_total"],
+        "k_match": nbytes["match_total"],
+    }
+    peaks = json.load(open(os.path.join(REPO, "MEASURED_PEAKS.json"))) if os.path.exists(
+        os.path.join(REPO, "MEASURED_PEAKS.json")) else None
+    peak = peaks["hbm_gbs"] if peaks else 6800.0
+    dom_bytes = kernel_bytes.get(dom)
+    achieved = (dom_bytes / (prof[dom] / 1e3) / 1e9) if dom_bytes else None
+    roofline = {
+        "bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
+        "frac": (achieved / peak) if achieved else None, "traffic": None,
+        "peak_source": "measured" if peaks else "fallback",
+        "kernel_ms": prof, "algorithmic_bytes_per_launch": dom_bytes,
+        "path_achieved": nbytes["total_per_step"] / (step_ms / 1e3) / 1e9,
+        "path_frac": nbytes["total_per_step"] / (step_ms / 1e3) / 1e9 / peak,
+    }
+
+    # ---- end to end through the C ABI: pinned H2D + graph + D2H every step
+    for _ in range(a.warmup):
+        batch.upload()
+        batch.run()
+        batch.download()
+        stream.synchronize()
+    barrier()
+    e2e_times = []
+    for _ in range(a.steps):
+        t0 = time.perf_counter()
+        batch.upload()
+        batch.run()
+        batch.download()
+        batch.sync()
+        e2e_times.append(time.perf_counter() - t0)
+    barrier()
+    e2e_s = statistics.mean(e2e_times)
+    if dist is not None:
+        t = torch.tensor([e2e_s], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    h2d, d2h = batch.io_bytes()
+
+    # ---- plain per-frame form: one frame per launch sequence, synchronous
+    fe = Frontend(ctx, W, H)
+    dev_frames = torch.from_numpy(np.stack(frames)).to("cuda")
+    torch.cuda.synchronize()
+    base = dev_frames.data_ptr()
+    for i in range(min(4, n)):
+        fe.enqueue(base + i * W * H, W, advance_reference=True)
+        fe.sync()
+    t0 = time.perf_counter()
+    for i in range(n):
+        fe.enqueue(base + i * W * H, W, advance_reference=True)
+        fe.sync()
+    plain_s = time.perf_counter() - t0
+    plain_fps = n / plain_s
+    fe.close()
+
+    cpu = None
+    if rank == 0:
+        cpu = cpu_baseline_sample(frames, pat, a.cpu_seconds)
+
+    batch.close()
+    ctx.close()
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "frames/s", "n_gpus": world, "steps": a.steps,
+            "warmup": a.warmup, "ms_per_step": step_ms_max, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32+u32", "data": "synthetic (seeded plane trajectory; EuRoC absent)",
+            "config": {"workload": WORKLOAD, "frames": n, "pairs": n - 1, "levels": LEVELS, "seed": a.seed,
+                       "l2": "flushed (256 MiB write) between timed steps", "parallelism": f"replicas x{world}"},
+            "plain_fps": plain_fps, "batched_over_plain": value / world / plain_fps,
+            "e2e": {"value": n * world / e2e_s, "unit": "frames/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h},
+            "gpu_launches": 5 * a.steps, "roofline": roofline, "cpu_baseline": cpu, "clocks": clk,
+            "features_per_frame": sum(kept) / n, "matches_per_pair": sum(nmatch) / max(1, n - 1),
+            "wall_s_timed": wall_s,
+        }
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def main():
+    a = _args()
+    if a.impl == "reference":
+        run_reference(a)
+    else:
+        run_ours(a)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,174 @@
+/*
+ * uslam.h — C ABI of the GB300 feature front-end (pyramid, FAST-style detect,
+ * cull, rotated BRIEF, windowed mutual Hamming matching).
+ *
+ * It replaces, for the reference uni_slam:
+ *   - the four GPU passes of the feature-detect stage
+ *     (wslam/src/feature_detect/feature_detect.cpp:54-67: FillPyramidPass,
+ *     PassDetectCorners, CullCornersPass, GenerateFeaturesPass),
+ *   - the feature readback/decode of LoadDataCPUPass
+ *     (wslam/src/pose_estimate_cpu/load_features_cpu.cpp:54-187),
+ *   - the CPU matcher MatchFeaturesCPU
+ *     (wslam/src/pose_estimate_cpu/match_features_cpu.cpp:152-268).
+ *
+ * Plain pointers and sizes only.  Every call returns a uslam_status; on
+ * failure uslam_last_error(ctx) holds a message.  No call throws.  A context
+ * and everything created from it belong to one host thread at a time.
+ */
+#ifndef USLAM_H
+#define USLAM_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum uslam_status {
+    USLAM_OK = 0,
+    USLAM_INVALID_ARG = 1, /* bad size, null pointer, out-of-range index */
+    USLAM_OOM = 2,         /* device or pinned-host allocation refused */
+    USLAM_TIMEOUT = 3,     /* a bounded wait ran out (uslam_*_sync with timeout) */
+    USLAM_CUDA_ERROR = 4,  /* a CUDA runtime call failed */
+    USLAM_CAPACITY = 5,    /* caller buffer or admission budget too small */
+    USLAM_NOT_READY = 6,   /* no reference feature set yet (the reference's STAGE_STOP) */
+    USLAM_KERNEL_CHECK = 7 /* a kernel's own bounds check tripped (error word set) */
+} uslam_status;
+
+typedef struct uslam_ctx uslam_ctx;
+typedef struct uslam_batch uslam_batch;
+typedef struct uslam_frontend uslam_frontend;
+
+/* Same 48-byte layout as the reference's gpumodels::Feature
+ * (wslam/src/models.hpp:31-69): coords, FAST strength, orientation (rad),
+ * 256-bit descriptor (bit i of the BRIEF test i is word i/32, bit i%32). */
+typedef struct uslam_feature {
+    float x;
+    float y;
+    uint32_t strength;
+    float orientation;
+    uint32_t descriptor[8];
+} uslam_feature;
+
+/* One mutual match: feature idx_a of level lod_a of the previous (reference)
+ * set and feature idx_b of level lod_b of the current set.  The reference
+ * keeps these in MatchResult[lod_a] keyed by the current feature
+ * (match_features_cpu.cpp:195-205). */
+typedef struct uslam_match {
+    int32_t lod_a;
+    int32_t idx_a;
+    int32_t lod_b;
+    int32_t idx_b;
+} uslam_match;
+
+typedef struct uslam_params {
+    int device;          /* CUDA device ordinal */
+    int levels;          /* pyramid levels; reference: 6 (wslam/include/wslam/common.hpp:43) */
+    int max_width;       /* largest accepted frame width (<= 8192) */
+    int max_height;      /* largest accepted frame height */
+    int cap_per_level;   /* features kept per level; 0 = W0*H0/250 (common.hpp:47) */
+    /* 256 BRIEF tests, (ax, ay, bx, by) int32 each: the reference's
+     * gpumodels::BRIEFTestSet uploaded by GenerateFeaturesPass::writeConstantValues
+     * (wslam/src/feature_detect/generate_features.cpp:450-493). */
+    const int32_t* brief_pattern;
+} uslam_params;
+
+/* ---- context ---------------------------------------------------------- */
+
+/* Replaces the Dawn device + pass initialisation (compute/src/gpu.cpp:284-553,
+ * every Pass::initialize of the feature-detect stage). */
+uslam_status uslam_create(const uslam_params* params, uslam_ctx** out);
+void uslam_destroy(uslam_ctx* ctx);
+const char* uslam_last_error(const uslam_ctx* ctx);
+const char* uslam_status_string(uslam_status s);
+/* Level dimensions w_l = (uint32)(W0 / pow(1.2, l)) (wslam/src/common.cpp:41-45). */
+uslam_status uslam_level_dims(int width, int height, int levels, int* w_out, int* h_out);
+
+/* Host-only: the data-independent coverage of the reference's two cull
+ * dispatches for a level of size w x h of a W0 x H0 frame
+ * (resources/cull_corners.wgsl:22-109 with the dispatch of
+ * wslam/src/feature_detect/cull_corners.cpp:332-353), as a bitmap of
+ * ceil(w*h/32) words: bit p set iff pixel p survives culling whenever its
+ * response is > 0 (row 0 additionally needs the 1x3 first arg-max, applied
+ * on the device).  Needs no GPU. */
+uslam_status uslam_cull_coverage(int W0, int H0, int w, int h, uint32_t* bits_out);
+
+/* ---- batched form: a work table over many frames and frame pairs -------- */
+
+/* Plan a batch of n_frames frames (any mix of sizes) and n_pairs matches
+ * (pair k matches frame pair_prev[k] (reference set) against frame
+ * pair_curr[k]).  Allocates every device buffer up front. */
+uslam_status uslam_batch_create(uslam_ctx* ctx, int n_frames, const int* widths, const int* heights,
+                                int n_pairs, const int* pair_prev, const int* pair_curr, uslam_batch** out);
+void uslam_batch_destroy(uslam_batch* b);
+/* Device address and row pitch of a frame's LOD0 input buffer (u8), for
+ * callers that keep frames resident in HBM. */
+uslam_status uslam_batch_input_device(uslam_batch* b, int frame, uint8_t** dev_ptr, int* pitch);
+/* Pinned host staging buffer of a frame's input (row pitch as above). */
+uslam_status uslam_batch_input_host(uslam_batch* b, int frame, uint8_t** host_ptr, int* pitch);
+/* Asynchronous host->device copy of every frame from the pinned staging. */
+uslam_status uslam_batch_upload(uslam_batch* b);
+/* Copy caller frames (any host memory, given pitch) into the pinned staging. */
+uslam_status uslam_batch_set_frame(uslam_batch* b, int frame, const uint8_t* img, int pitch);
+/* Launch detect + describe of every frame and match of every pair (one CUDA
+ * graph replay: five kernel launches for the whole batch). Asynchronous. */
+uslam_status uslam_batch_run(uslam_batch* b);
+/* Asynchronous device->host copy of every frame's features and every pair's
+ * matches into pinned staging (read them with the getters below). */
+uslam_status uslam_batch_download(uslam_batch* b);
+/* Wait for the batch (timeout_ms <= 0: no limit); checks kernel error words. */
+uslam_status uslam_batch_sync(uslam_batch* b, int timeout_ms);
+/* Features of a frame, level by level in (y, x) order, from the staging
+ * (after download + sync).  kept/raw receive `levels` counts each. */
+uslam_status uslam_batch_features(uslam_batch* b, int frame, uslam_feature* out, int max_out, int* kept,
+                                  int* raw);
+uslam_status uslam_batch_matches(uslam_batch* b, int pair, uslam_match* out, int max_out, int* n_out);
+/* Parity getters (synchronous, read device memory directly). */
+uslam_status uslam_batch_pyramid_level(uslam_batch* b, int frame, int level, float* out);
+uslam_status uslam_batch_keypoint_map(uslam_batch* b, int frame, int level, uint8_t* out);
+uslam_status uslam_batch_blur_level(uslam_batch* b, int frame, int level, float* out);
+/* Issue later upload/run/download calls on a caller's cudaStream_t (NULL:
+ * the batch's own stream), so callers can record their own events around them. */
+uslam_status uslam_batch_set_stream(uslam_batch* b, void* cuda_stream);
+/* Per-kernel timing: launch the batch's five kernels `iters` times without
+ * the graph, with CUDA events between them on the batch stream, and return
+ * the mean milliseconds per launch of detect, compact, describe, match and
+ * mutual in kernel_ms[0..4].  Synchronous. */
+uslam_status uslam_batch_profile(uslam_batch* b, int iters, float* kernel_ms);
+/* Bytes moved by upload and download per call (for end-to-end accounting). */
+uslam_status uslam_batch_io_bytes(uslam_batch* b, size_t* h2d, size_t* d2h);
+
+/* ---- plain per-frame form: the reference's pass sequence ---------------- */
+
+/* One camera stream of fixed frame size holding FeatureSet(0) (current) and
+ * FeatureSet(1) (reference) on the device, with the reference's rotation rule
+ * (LoadDataCPUPass::shiftFeatureSets, load_features_cpu.cpp:111-142). */
+uslam_status uslam_frontend_create(uslam_ctx* ctx, int width, int height, uslam_frontend** out);
+void uslam_frontend_destroy(uslam_frontend* fe);
+/* Process one frame: upload (img == NULL: the frame is already in the input
+ * buffer returned by uslam_frontend_input_device), detect + describe into
+ * FeatureSet(0) and, when a reference set exists, match FeatureSet(1) ->
+ * FeatureSet(0).  advance_reference mirrors the "gen:feat:refadv" marker:
+ * the previous current set becomes the reference before this frame is
+ * stored.  Returns USLAM_NOT_READY (features computed, no matching) when no
+ * reference exists yet.  Synchronous. */
+uslam_status uslam_frontend_process(uslam_frontend* fe, const uint8_t* img, int pitch, int advance_reference);
+uslam_status uslam_frontend_input_device(uslam_frontend* fe, uint8_t** dev_ptr, int* pitch);
+/* which = 0: current set, 1: reference set. */
+uslam_status uslam_frontend_features(uslam_frontend* fe, int which, uslam_feature* out, int max_out, int* kept,
+                                     int* raw);
+uslam_status uslam_frontend_matches(uslam_frontend* fe, uslam_match* out, int max_out, int* n_out);
+/* Asynchronous form of uslam_frontend_process for a frame already in device
+ * memory (dev_img, row pitch; NULL: the frontend's input buffer): enqueue the
+ * copy and the frame's work and return.  *matched tells whether a match was
+ * enqueued.  Wait with uslam_frontend_sync. */
+uslam_status uslam_frontend_enqueue(uslam_frontend* fe, const uint8_t* dev_img, int pitch, int advance_reference,
+                                    int* matched);
+uslam_status uslam_frontend_sync(uslam_frontend* fe);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* USLAM_H */

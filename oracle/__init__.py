@@ -1,0 +1,185 @@
+"""CPU oracle of the feature front-end — TEST INFRASTRUCTURE ONLY.
+
+Only tests/, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
+``bench.py`` load this package; the product library never calls it.  See
+oracle.h for what each function restates and the parity status (matcher
+pinned against the reference's own compiled source; WGSL stages unpinned).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import glob
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "liboracle.so")
+REF_DIR = os.path.join(HERE, "_ref")
+
+FEATURE_DTYPE = np.dtype([
+    ("x", "<f4"), ("y", "<f4"), ("strength", "<u4"), ("orientation", "<f4"), ("descriptor", "<u4", (8,)),
+])
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB):
+            raise RuntimeError(f"{LIB} missing: run `make -C oracle`")
+        L = C.CDLL(LIB)
+        vp = C.c_void_p
+        L.orc_level_dims.argtypes = [C.c_int, C.c_int, C.c_int, vp, vp]
+        L.orc_pyramid_level.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.c_uint32, C.c_uint32, C.c_int, vp]
+        L.orc_detect.argtypes = [vp, C.c_uint32, C.c_uint32, vp]
+        L.orc_cull.argtypes = [vp, C.c_uint32, C.c_uint32, C.c_int, C.c_int, vp]
+        L.orc_describe.argtypes = [vp, C.c_uint32, C.c_uint32, C.c_int, C.c_int, vp, vp, vp]
+        L.orc_blur_level.argtypes = [vp, C.c_uint32, C.c_uint32, vp]
+        L.orc_gauss_tap9.argtypes = [vp, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32]
+        L.orc_gauss_tap9.restype = C.c_float
+        L.orc_frame.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, vp, vp, C.c_int, vp, vp]
+        L.orc_frame.restype = C.c_int
+        L.orc_match.argtypes = [vp, vp, vp, vp, C.c_int, C.c_int, C.c_int, vp, C.c_int]
+        L.orc_match.restype = C.c_int
+        L.orc_atan2f.argtypes = [C.c_float, C.c_float]
+        L.orc_atan2f.restype = C.c_float
+        L.orc_sincosf.argtypes = [C.c_float, vp, vp]
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+def level_dims(W0: int, H0: int, levels: int = 6):
+    w = np.zeros(levels, np.uint32)
+    h = np.zeros(levels, np.uint32)
+    lib().orc_level_dims(W0, H0, levels, _p(w), _p(h))
+    return [(int(a), int(b)) for a, b in zip(w, h)]
+
+
+def pyramid_level(img: np.ndarray, level: int, levels: int = 6) -> np.ndarray:
+    img = np.ascontiguousarray(img, np.uint8)
+    H0, W0 = img.shape
+    w, h = level_dims(W0, H0, levels)[level]
+    out = np.zeros((h, w), np.float32)
+    lib().orc_pyramid_level(_p(img), W0, H0, W0, w, h, int(level == 0), _p(out))
+    return out
+
+
+def detect(lvl: np.ndarray) -> np.ndarray:
+    lvl = np.ascontiguousarray(lvl, np.float32)
+    h, w = lvl.shape
+    out = np.zeros((h, w), np.uint32)
+    lib().orc_detect(_p(lvl), w, h, _p(out))
+    return out
+
+
+def cull(resp: np.ndarray, W0: int, H0: int) -> np.ndarray:
+    resp = np.ascontiguousarray(resp, np.uint32)
+    h, w = resp.shape
+    out = np.zeros((h, w), np.uint32)
+    lib().orc_cull(_p(resp), w, h, W0, H0, _p(out))
+    return out
+
+
+def gauss_tap9(lvl: np.ndarray, px: int, py: int) -> float:
+    lvl = np.ascontiguousarray(lvl, np.float32)
+    h, w = lvl.shape
+    return float(lib().orc_gauss_tap9(_p(lvl), w, h, px & 0xffffffff, py & 0xffffffff))
+
+
+def blur_level(lvl: np.ndarray) -> np.ndarray:
+    lvl = np.ascontiguousarray(lvl, np.float32)
+    h, w = lvl.shape
+    out = np.zeros((h, w), np.float32)
+    lib().orc_blur_level(_p(lvl), w, h, _p(out))
+    return out
+
+
+def describe(lvl: np.ndarray, x: int, y: int, pattern: np.ndarray):
+    lvl = np.ascontiguousarray(lvl, np.float32)
+    pat = np.ascontiguousarray(pattern, np.int32).reshape(-1)
+    h, w = lvl.shape
+    th = np.zeros(1, np.float32)
+    d = np.zeros(8, np.uint32)
+    lib().orc_describe(_p(lvl), w, h, x, y, _p(pat), _p(th), _p(d))
+    return float(th[0]), d
+
+
+def frame(img: np.ndarray, pattern: np.ndarray, levels: int = 6, cap: int | None = None):
+    """Features of one frame: (features[FEATURE_DTYPE], kept[levels], raw[levels])."""
+    img = np.ascontiguousarray(img, np.uint8)
+    H0, W0 = img.shape
+    if cap is None:
+        cap = W0 * H0 // 250
+    pat = np.ascontiguousarray(pattern, np.int32).reshape(-1)
+    dims = level_dims(W0, H0, levels)
+    max_feats = max(1, sum(min(cap, w * h) for w, h in dims))
+    feats = np.zeros(max_feats, FEATURE_DTYPE)
+    kept = np.zeros(levels, np.int32)
+    raw = np.zeros(levels, np.int32)
+    n = lib().orc_frame(_p(img), W0, H0, W0, levels, cap, _p(pat), _p(feats), max_feats, _p(kept), _p(raw))
+    if n < 0:
+        raise RuntimeError("orc_frame: feature buffer too small")
+    return feats[:n].copy(), kept, raw
+
+
+def match(feats_a, kept_a, feats_b, kept_b, W0: int, H0: int) -> np.ndarray:
+    """Mutual matches (lod_a, idx_a, lod_b, idx_b) of prev=a against curr=b."""
+    levels = len(kept_a)
+    a = np.ascontiguousarray(feats_a, FEATURE_DTYPE)
+    b = np.ascontiguousarray(feats_b, FEATURE_DTYPE)
+    a_off = np.concatenate([[0], np.cumsum(kept_a)]).astype(np.int32)
+    b_off = np.concatenate([[0], np.cumsum(kept_b)]).astype(np.int32)
+    max_out = max(1, int(min(a_off[-1], b_off[-1])))
+    out = np.zeros((max_out, 4), np.int32)
+    n = lib().orc_match(_p(a), _p(a_off), _p(b), _p(b_off), levels, W0, H0, _p(out), max_out)
+    if n < 0:
+        raise RuntimeError("orc_match: output buffer too small")
+    return out[:n].copy()
+
+
+def atan2f(y: float, x: float) -> float:
+    return float(lib().orc_atan2f(y, x))
+
+
+def sincosf(a: float) -> tuple[float, float]:
+    s = np.zeros(1, np.float32)
+    c = np.zeros(1, np.float32)
+    lib().orc_sincosf(a, _p(s), _p(c))
+    return float(s[0]), float(c[0])
+
+
+# --------------------------------------------------- compiled reference matcher
+
+def ref_matcher(W0: int = 752, H0: int = 480):
+    """The reference's own match_features_cpu.cpp (compiled by oracle/Makefile), or None."""
+    path = os.path.join(REF_DIR, f"libref_matcher_{W0}x{H0}.so")
+    if not os.path.exists(path):
+        return None
+    L = C.CDLL(path)
+    vp = C.c_void_p
+    L.ref_find_matches.argtypes = [vp, vp, vp, vp, vp, C.c_int]
+    L.ref_find_matches.restype = C.c_int
+
+    def run(feats_a, kept_a, feats_b, kept_b):
+        a = np.ascontiguousarray(feats_a, FEATURE_DTYPE)
+        b = np.ascontiguousarray(feats_b, FEATURE_DTYPE)
+        a_off = np.concatenate([[0], np.cumsum(kept_a)]).astype(np.int32)
+        b_off = np.concatenate([[0], np.cumsum(kept_b)]).astype(np.int32)
+        max_out = max(1, int(min(a_off[-1], b_off[-1])))
+        out = np.zeros((max_out, 4), np.int32)
+        n = L.ref_find_matches(_p(a), _p(a_off), _p(b), _p(b_off), _p(out), max_out)
+        if n < 0:
+            raise RuntimeError("ref_find_matches: output buffer too small")
+        return out[:n].copy()
+
+    return run
+
+
+def ref_matcher_sizes():
+    return sorted(os.path.basename(p)[len("libref_matcher_"):-3] for p in glob.glob(os.path.join(REF_DIR, "*.so")))

@@ -1,0 +1,195 @@
+"""Parity of the CUDA path (through the C ABI) with the CPU oracle: bit-exact
+pyramid levels, blur cache, culled keypoint maps, feature records
+(coordinates, strength, orientation, 256-bit descriptors), raw/kept counts
+and mutual match lists, on seeded synthetic frames and edge cases."""
+import numpy as np
+import pytest
+
+import oracle
+from uni_slam_gb300 import Batch, Context, Frontend, synth
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def ctx(brief_pattern):
+    c = Context(brief_pattern, levels=6, max_width=1280, max_height=720)
+    yield c
+    c.close()
+
+
+def _run(ctx, frames, pairs=()):
+    b = Batch(ctx, [(f.shape[1], f.shape[0]) for f in frames], list(pairs))
+    b.process(frames)
+    return b
+
+
+def _mm(m):
+    if len(m) == 0:
+        return np.zeros((0, 4), np.int32)
+    return np.stack([m["lod_a"], m["idx_a"], m["lod_b"], m["idx_b"]], 1)
+
+
+def _assert_features_equal(got, exp):
+    gf, gk, gr = got
+    ef, ek, er = exp
+    assert np.array_equal(gr, er), (gr, er)
+    assert np.array_equal(gk, ek), (gk, ek)
+    assert gf.shape == ef.shape
+    if gf.tobytes() != ef.tobytes():
+        gb = gf.view(np.uint8).reshape(len(gf), 48)
+        eb = ef.view(np.uint8).reshape(len(ef), 48)
+        bad = np.nonzero((gb != eb).any(1))[0]
+        i = int(bad[0])
+        raise AssertionError(f"{len(bad)} feature records differ; first #{i}: gpu={gf[i]} oracle={ef[i]}")
+
+
+def test_pyramid_levels_bit_exact(ctx):
+    f1, _ = synth.config0_pair(0)
+    b = _run(ctx, [f1])
+    try:
+        for l in range(1, 6):
+            assert np.array_equal(b.pyramid_level(0, l).view(np.uint32),
+                                  oracle.pyramid_level(f1, l).view(np.uint32)), f"level {l}"
+    finally:
+        b.close()
+
+
+def test_blur_cache_bit_exact(ctx):
+    f1, _ = synth.config0_pair(1)
+    b = _run(ctx, [f1])
+    try:
+        for l in range(6):
+            exp = oracle.blur_level(oracle.pyramid_level(f1, l))
+            assert np.array_equal(b.blur_level(0, l).view(np.uint32), exp.view(np.uint32)), f"level {l}"
+    finally:
+        b.close()
+
+
+def test_keypoint_maps_bit_exact(ctx):
+    for seed in (0, 3):
+        f1, _ = synth.config0_pair(seed)
+        b = _run(ctx, [f1])
+        try:
+            for l in range(6):
+                lvl = oracle.pyramid_level(f1, l)
+                exp = oracle.cull(oracle.detect(lvl), 752, 480)
+                assert np.array_equal(b.keypoint_map(0, l).astype(np.uint32), exp), f"seed {seed} level {l}"
+        finally:
+            b.close()
+
+
+@pytest.mark.parametrize("seed", [0, 1, 2])
+def test_features_and_matches_bit_exact(ctx, brief_pattern, seed):
+    f1, f2 = synth.config0_pair(seed)
+    b = _run(ctx, [f1, f2], [(0, 1)])
+    try:
+        got = [b.features(i) for i in range(2)]
+        exp = [oracle.frame(f, brief_pattern) for f in (f1, f2)]
+        for g, e in zip(got, exp):
+            _assert_features_equal(g, e)
+        em = oracle.match(exp[0][0], exp[0][1], exp[1][0], exp[1][1], 752, 480)
+        gm = _mm(b.matches(0))
+        assert len(em) > 100
+        assert np.array_equal(gm, em)
+        ref = oracle.ref_matcher(752, 480)
+        if ref is not None:  # the reference's own compiled matcher, where available
+            assert np.array_equal(gm, ref(exp[0][0], exp[0][1], exp[1][0], exp[1][1]))
+    finally:
+        b.close()
+
+
+def test_uneven_batch_equals_oracle_and_alone(ctx, brief_pattern):
+    sizes = [(640, 480), (752, 480), (1280, 720), (97, 61), (333, 211)]
+    frames, pairs = [], []
+    for k, (w, h) in enumerate(sizes):
+        a, c = synth.config0_pair(100 + k, w, h)
+        frames += [a, c]
+        pairs.append((2 * k, 2 * k + 1))
+    b = _run(ctx, frames, pairs)
+    try:
+        for k, (w, h) in enumerate(sizes):
+            exp = [oracle.frame(frames[2 * k + j], brief_pattern) for j in range(2)]
+            for j in range(2):
+                _assert_features_equal(b.features(2 * k + j), exp[j])
+            em = oracle.match(exp[0][0], exp[0][1], exp[1][0], exp[1][1], w, h)
+            assert np.array_equal(_mm(b.matches(k)), em), f"pair {k} {w}x{h}"
+        # the same pair alone in its own batch gives the same bytes
+        alone = _run(ctx, frames[4:6], [(0, 1)])
+        try:
+            assert alone.features(1)[0].tobytes() == b.features(5)[0].tobytes()
+            assert np.array_equal(_mm(alone.matches(0)), _mm(b.matches(2)))
+        finally:
+            alone.close()
+    finally:
+        b.close()
+
+
+def test_repeat_runs_are_identical(ctx):
+    frames = synth.config1_sequence(5, n=4)
+    b = Batch(ctx, [(752, 480)] * 4, [(0, 1), (1, 2), (2, 3)])
+    try:
+        b.process(frames)
+        first = [b.features(i)[0].tobytes() for i in range(4)] + [_mm(b.matches(p)).tobytes() for p in range(3)]
+        b.run()
+        b.download()
+        b.sync()
+        again = [b.features(i)[0].tobytes() for i in range(4)] + [_mm(b.matches(p)).tobytes() for p in range(3)]
+        assert first == again
+    finally:
+        b.close()
+
+
+def test_constant_and_tiny_frames(brief_pattern):
+    with Context(brief_pattern, levels=6, max_width=64, max_height=64, cap_per_level=50) as c:
+        flat = np.full((48, 64), 77, np.uint8)
+        tiny = synth.config_frame(9, 10, 10)
+        odd = synth.config_frame(11, 37, 23)
+        frames = [flat, flat, tiny, tiny, odd]
+        b = _run(c, frames, [(0, 1), (2, 3)])
+        try:
+            f, kept, raw = b.features(0)
+            assert len(f) == 0 and not raw.any()
+            assert len(b.matches(0)) == 0
+            for i in (2, 4):
+                _assert_features_equal(b.features(i), oracle.frame(frames[i], brief_pattern, cap=50))
+        finally:
+            b.close()
+
+
+def test_cap_keeps_first_in_yx_order(brief_pattern):
+    f1, _ = synth.config0_pair(4)
+    with Context(brief_pattern, levels=6, max_width=752, max_height=480, cap_per_level=100) as c:
+        b = _run(c, [f1])
+        try:
+            got = b.features(0)
+            exp = oracle.frame(f1, brief_pattern, cap=100)
+            _assert_features_equal(got, exp)
+            assert (got[1] == 100).all() and (got[2] > 100).all()
+        finally:
+            b.close()
+
+
+def test_frontend_rotation_matches_reference_rule(ctx, brief_pattern):
+    """FeatureSet(1) advances on the marker or when absent
+    (load_features_cpu.cpp:111-142); matching is FeatureSet(1) -> FeatureSet(0)."""
+    frames = synth.config1_sequence(7, n=6)
+    advance = [False, False, False, True, False, True]
+    fe = Frontend(ctx, 752, 480)
+    try:
+        ref_set = None
+        cur_set = None
+        for i, (img, adv) in enumerate(zip(frames, advance)):
+            matched = fe.process(img, advance_reference=adv)
+            exp = oracle.frame(img, brief_pattern)
+            if cur_set is not None and (ref_set is None or adv):
+                ref_set = cur_set
+            cur_set = exp
+            assert matched == (ref_set is not None)
+            _assert_features_equal(fe.features(0), exp)
+            if ref_set is not None:
+                _assert_features_equal(fe.features(1), ref_set)
+                em = oracle.match(ref_set[0], ref_set[1], exp[0], exp[1], 752, 480)
+                assert np.array_equal(_mm(fe.matches()), em), f"frame {i}"
+    finally:
+        fe.close()

@@ -1,0 +1,69 @@
+"""Pins of the CPU oracle against the reference itself.
+
+The matcher restatement (oracle/oracle.c: orc_match) must reproduce the
+reference's own wslam/src/pose_estimate_cpu/match_features_cpu.cpp exactly:
+against golden vectors that the compiled reference produced
+(tests/golden/make_golden.py) and, where the reference checkout is present,
+against the compiled reference live on fresh random cases.
+"""
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden", "matcher_cases.npz")
+
+
+def _cases():
+    z = np.load(GOLDEN)
+    for k in range(int(z["n_cases"][0])):
+        W, H = (int(v) for v in z[f"c{k}_size"])
+        yield (k, W, H, z[f"c{k}_a"].view(oracle.FEATURE_DTYPE), z[f"c{k}_ka"],
+               z[f"c{k}_b"].view(oracle.FEATURE_DTYPE), z[f"c{k}_kb"], z[f"c{k}_matches"])
+
+
+@pytest.mark.parametrize("case", list(_cases()), ids=lambda c: f"case{c[0]}")
+def test_matcher_against_reference_golden(case):
+    _, W, H, fa, ka, fb, kb, expected = case
+    got = oracle.match(fa, ka, fb, kb, W, H)
+    assert got.shape == expected.shape
+    assert np.array_equal(got, expected)
+
+
+def _random_sets(rs, W, H, per_level, flip_p):
+    dims = oracle.level_dims(W, H, 6)
+    a, b = [], []
+    for (w, h) in dims:
+        n = int(rs.randint(0, per_level))
+        f = np.zeros(n, oracle.FEATURE_DTYPE)
+        idx = np.sort(rs.choice(w * h, size=n, replace=False))
+        f["x"], f["y"] = idx % w, idx // w
+        f["descriptor"] = rs.randint(0, 2**32, size=(n, 8), dtype=np.uint64).astype(np.uint32)
+        g = f.copy()
+        g["x"] = np.clip(g["x"] + rs.randint(-3, 4, size=n), 0, w - 1)
+        bits = rs.uniform(size=(n, 256)) < flip_p
+        g["descriptor"] ^= np.packbits(bits, axis=1, bitorder="little").view("<u4")
+        key = g["y"].astype(np.int64) * w + g["x"]
+        _, first = np.unique(key, return_index=True)
+        g = g[np.sort(first)]
+        g = g[np.argsort(g["y"].astype(np.int64) * w + g["x"], kind="stable")]
+        a.append(f)
+        b.append(g)
+    ka = np.array([len(x) for x in a], np.int32)
+    kb = np.array([len(x) for x in b], np.int32)
+    return np.concatenate(a), ka, np.concatenate(b), kb
+
+
+@pytest.mark.parametrize("size", [(752, 480), (1280, 720)])
+def test_matcher_against_compiled_reference_live(size):
+    ref = oracle.ref_matcher(*size)
+    if ref is None:
+        pytest.skip("reference checkout not present: compiled reference matcher unavailable (golden pins still run)")
+    rs = np.random.RandomState(size[0])
+    for trial in range(12):
+        fa, ka, fb, kb = _random_sets(rs, size[0], size[1], per_level=120, flip_p=[0.0, 0.05, 0.2][trial % 3])
+        exp = ref(fa, ka, fb, kb)
+        got = oracle.match(fa, ka, fb, kb, *size)
+        assert np.array_equal(got, exp), f"trial {trial}"

@@ -1,0 +1,718 @@
+// kernels.cu — sm_103a kernels of the GB300 feature front-end.
+//
+//   k_detect   (K1) pyramid level tile + FAST response + cull + blur cache
+//   k_compact       per (frame, level): ordered keypoint compaction, cap, x-sort
+//   k_describe (K2) orientation + 256-bit rotated BRIEF, one warp per keypoint
+//   k_match    (K3) windowed top-2 Hamming search, one warp per query
+//   k_mutual        mutual cross-check and ordered match output
+//
+// Arithmetic contract: binary32, round-to-nearest-even, no FMA contraction
+// (the library is compiled with --fmad=false), evaluation order as in the
+// reference shaders.  Every kernel is bit-exact against the CPU oracle.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/uslam_canon.h"
+#include "uslam_internal.h"
+
+namespace uslam {
+
+// K1 tile geometry: TW x TH output pixels, halo HX columns / HY rows.
+constexpr int TW = 64;
+constexpr int TH = 16;
+constexpr int HX = 5;
+constexpr int HY = 3;
+constexpr int SW = TW + 2 * HX;
+constexpr int SH = TH + 2 * HY;
+constexpr int K1_THREADS = 256;
+
+// Bresenham circle of radius 3 (resources/detect_corners.wgsl:31-32).
+__constant__ int8_t c_circle_x[16] = {0, 1, 2, 3, 3, 3, 2, 1, 0, -1, -2, -3, -3, -3, -2, -1};
+__constant__ int8_t c_circle_y[16] = {-3, -3, -2, -1, 0, 1, 2, 3, 3, 3, 2, 1, 0, -1, -2, -3};
+
+// Orientation disc r = 3 in (dy outer, dx inner) order (generate_features.wgsl:87-97).
+__constant__ int8_t c_disc_x[32];
+__constant__ int8_t c_disc_y[32];
+
+// Tint robustness clamp of textureLoad coordinates: min(u32(c), n - 1).
+__device__ __forceinline__ int tint_clamp(int c, int n) {
+    const unsigned u = (unsigned)c;
+    return u < (unsigned)n ? (int)u : n - 1;
+}
+
+// Clamp-to-edge index of an integer-valued float (may be huge or negative).
+__device__ __forceinline__ int edge_index(float f, int n) {
+    if (f <= 0.0f) return 0;
+    if (f >= (float)(n - 1)) return n - 1;
+    return (int)f;
+}
+
+__device__ __forceinline__ float lod0_texel(const FrameDev& F, int x, int y) {
+    return (float)__ldg(F.img + (size_t)y * (size_t)F.img_pitch + x) / 255.0f;
+}
+
+// Level pixel (x, y) of level l: LOD0 = u8/255, l >= 1 = one canonical
+// bilinear tap of LOD0 at the texel centre (resources/create_pyramid.wgsl:11-12).
+__device__ float pyramid_pixel(const FrameDev& F, int l, int x, int y) {
+    if (l == 0) return lod0_texel(F, x, y);
+    const float uvx = ((float)x + 0.5f) / (float)F.w[l];
+    const float uvy = ((float)y + 0.5f) / (float)F.h[l];
+    const float u = uvx * (float)F.W0 - 0.5f;
+    const float v = uvy * (float)F.H0 - 0.5f;
+    const float fi = floorf(u);
+    const float fj = floorf(v);
+    const float a = u - fi;
+    const float b = v - fj;
+    const int i0 = edge_index(fi, F.W0), i1 = edge_index(fi + 1.0f, F.W0);
+    const int j0 = edge_index(fj, F.H0), j1 = edge_index(fj + 1.0f, F.H0);
+    const float t00 = lod0_texel(F, i0, j0), t10 = lod0_texel(F, i1, j0);
+    const float t01 = lod0_texel(F, i0, j1), t11 = lod0_texel(F, i1, j1);
+    const float na = 1.0f - a, nb = 1.0f - b;
+    float r = (na * nb) * t00;
+    r = r + (a * nb) * t10;
+    r = r + (na * b) * t01;
+    r = r + (a * b) * t11;
+    return r;
+}
+
+// Level texel for describe-time reads (level 0 from the u8 frame).
+__device__ __forceinline__ float level_texel(const FrameDev& F, int l, int x, int y) {
+    if (l == 0) return lod0_texel(F, x, y);
+    return __ldg(F.lvl[l] + (size_t)y * (size_t)F.w[l] + x);
+}
+
+// FAST response at smem cell (r, c): 1 + longest non-wrapping run of
+// |centre - p_i| > 0.15, kept iff > 9 (detect_corners.wgsl:58-81).
+__device__ __forceinline__ uint32_t fast_response(const float (*sm)[SW], int r, int c) {
+    const float center = sm[r][c];
+    uint32_t m = 0;
+#pragma unroll
+    for (int i = 0; i < 16; ++i) {
+        const float p = sm[r + c_circle_y[i]][c + c_circle_x[i]];
+        m |= (fabsf(center - p) > 0.15f ? 1u : 0u) << i;
+    }
+    // run >= 9 test: AND of the mask shifted by 0..8
+    uint32_t t = m & (m >> 1);
+    t &= t >> 2;
+    t &= t >> 4;
+    t &= t >> 1;
+    if (t == 0u) return 0u;
+    uint32_t run = 0;
+    while (m) {
+        m &= m << 1;
+        ++run;
+    }
+    return run + 1u;
+}
+
+__device__ __forceinline__ bool mask_bit(const uint32_t* mask, int p) {
+    return (__ldg(mask + (p >> 5)) >> (p & 31)) & 1u;
+}
+
+// ---------------------------------------------------------------- K1 ----
+__global__ void __launch_bounds__(K1_THREADS)
+k_detect(const FrameDev* __restrict__ frames, const TileItem* __restrict__ tiles, uint32_t* err) {
+    __shared__ float sm[SH][SW];
+    const TileItem it = tiles[blockIdx.x];
+    const FrameDev& F = frames[it.frame];
+    const int l = it.level;
+    const int w = F.w[l], h = F.h[l];
+    const int X0 = it.tx * TW, Y0 = it.ty * TH;
+
+    // 1. level tile + halo; halo cells follow the Tint clamp (far edge for < 0)
+    for (int idx = threadIdx.x; idx < SH * SW; idx += K1_THREADS) {
+        const int r = idx / SW, c = idx - r * SW;
+        const int gy = tint_clamp(Y0 - HY + r, h);
+        const int gx = tint_clamp(X0 - HX + c, w);
+        sm[r][c] = pyramid_pixel(F, l, gx, gy);
+    }
+    __syncthreads();
+
+    const float tex_x = 1.0f / (float)w;
+    const float tex_y = 1.0f / (float)h;
+    const int tx = threadIdx.x % TW;
+    const int x = X0 + tx;
+    const uint32_t* mask = F.mask[l];
+    for (int ty = threadIdx.x / TW; ty < TH; ty += K1_THREADS / TW) {
+        const int y = Y0 + ty;
+        if (x >= w || y >= h) continue;
+        const int r = ty + HY, c = tx + HX;
+        const size_t p = (size_t)y * (size_t)w + (size_t)x;
+
+        // 2. FAST response + cull (resources/cull_corners.wgsl; see mask_bit)
+        const uint32_t S = fast_response(sm, r, c);
+        uint32_t keep = 0;
+        if (S > 0u && mask_bit(mask, (int)p)) {
+            keep = S;
+            if (y == 0) {
+                // row 0: first arg-max of the 1x3 region [9k, min(9k+3, w))
+                const int start = x - x % 9;
+                const int end = min(start + 3, w);
+                for (int q = start; q < end; ++q) {
+                    if (q == x) continue;
+                    const uint32_t Sq = fast_response(sm, r, c + (q - x));
+                    if ((q < x && Sq >= S) || (q > x && Sq > S)) keep = 0;
+                }
+            }
+        }
+        F.kpmap[l][(size_t)y * F.kp_pitch[l] + x] = (uint8_t)keep;
+        if (l > 0) F.lvl[l][p] = sm[r][c];
+
+        // 3. blur cache: G(x, y) of generate_features.wgsl:149-172 for this pixel
+        const float uvx = ((float)x + 0.5f) * tex_x;
+        const float uvy = ((float)y + 0.5f) * tex_y;
+        int ix0[3], ix1[3], iy0[3], iy1[3];
+        float ax[3], by[3];
+        const float off[3] = {-1.2f, 0.0f, 1.2f};
+        bool ok = true;
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const float u = (uvx + off[k] * tex_x) * (float)w - 0.5f;
+            const float v = (uvy + off[k] * tex_y) * (float)h - 0.5f;
+            const float fi = floorf(u), fj = floorf(v);
+            ax[k] = u - fi;
+            by[k] = v - fj;
+            ix0[k] = edge_index(fi, w) - (X0 - HX);
+            ix1[k] = edge_index(fi + 1.0f, w) - (X0 - HX);
+            iy0[k] = edge_index(fj, h) - (Y0 - HY);
+            iy1[k] = edge_index(fj + 1.0f, h) - (Y0 - HY);
+            ok = ok && ix0[k] >= 0 && ix1[k] < SW && iy0[k] >= 0 && iy1[k] < SH;
+        }
+        float sum = 0.0f;
+        if (ok) {
+            const float wt[3] = {0.3125f, 0.375f, 0.3125f};
+#pragma unroll
+            for (int j = 0; j < 3; ++j) {
+#pragma unroll
+                for (int i = 0; i < 3; ++i) {
+                    const float a = ax[i], b = by[j];
+                    const float na = 1.0f - a, nb = 1.0f - b;
+                    float s = (na * nb) * sm[iy0[j]][ix0[i]];
+                    s = s + (a * nb) * sm[iy0[j]][ix1[i]];
+                    s = s + (na * b) * sm[iy1[j]][ix0[i]];
+                    s = s + (a * b) * sm[iy1[j]][ix1[i]];
+                    sum = sum + (s * wt[i]) * wt[j];
+                }
+            }
+        } else {
+            atomicOr(err, USLAM_ERR_SMEM_RANGE);
+        }
+        F.blur[l][p] = sum;
+    }
+}
+
+// ------------------------------------------------------------ compact ----
+constexpr int KC_THREADS = 1024;
+
+__device__ __forceinline__ int nonzero_bytes(uint32_t v) {
+    return __popc(__vcmpne4(v, 0u)) >> 3;
+}
+
+// Block-wide exclusive scan of one value per thread; returns the prefix and
+// writes the block total to *total.
+__device__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* s_warp, uint32_t* total) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int nwarps = (blockDim.x + 31) >> 5;
+    uint32_t incl = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += t;
+    }
+    if (lane == 31) s_warp[warp] = incl;
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t wv = lane < nwarps ? s_warp[lane] : 0u;
+        uint32_t wi = wv;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t t = __shfl_up_sync(0xffffffffu, wi, o);
+            if (lane >= o) wi += t;
+        }
+        if (lane < nwarps) s_warp[lane] = wi - wv;
+        if (lane == 31) s_warp[32] = wi;
+    }
+    __syncthreads();
+    const uint32_t res = s_warp[warp] + incl - v;
+    *total = s_warp[32];
+    __syncthreads();
+    return res;
+}
+
+// One CTA per (frame, level): keypoints in (y, x) order from the culled
+// strength map, cap applied to the first `cap`, then a counting sort of the
+// kept features by x for the matcher's window lookup.
+__global__ void __launch_bounds__(KC_THREADS)
+k_compact(const FrameDev* __restrict__ frames, const SegDev* __restrict__ segs) {
+    extern __shared__ uint32_t s_hist[];  // [w + 1]
+    __shared__ uint32_t s_warp[33];
+    __shared__ uint32_t s_base[32];
+    const SegDev sg = segs[blockIdx.x];
+    const FrameDev& F = frames[sg.frame];
+    const int l = sg.level;
+    const int w = F.w[l], h = F.h[l], kpitch = F.kp_pitch[l];
+    const uint8_t* kp = F.kpmap[l];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int rows_per = (h + 31) / 32;
+    const int r0 = warp * rows_per, r1 = min(h, r0 + rows_per);
+    const uint32_t cap = (uint32_t)F.cap;
+
+    // pass 1: count per warp
+    uint32_t cnt = 0;
+    for (int y = r0; y < r1; ++y) {
+        const uint32_t* row = reinterpret_cast<const uint32_t*>(kp + (size_t)y * kpitch);
+        for (int x4 = lane; x4 * 4 < w; x4 += 32) cnt += nonzero_bytes(row[x4]);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+    if (lane == 0) s_base[warp] = cnt;
+    __syncthreads();
+    if (warp == 0) {
+        const uint32_t v = s_base[lane];
+        uint32_t incl = v;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += t;
+        }
+        s_base[lane] = incl - v;
+        if (lane == 31) s_warp[32] = incl;
+    }
+    __syncthreads();
+    const uint32_t total = s_warp[32];
+
+    // pass 2: ordered write of (x, y, strength) headers
+    uint32_t running = s_base[warp];
+    uint32_t* feats = F.feats[l];
+    for (int y = r0; y < r1; ++y) {
+        const uint32_t* row = reinterpret_cast<const uint32_t*>(kp + (size_t)y * kpitch);
+        for (int base = 0; base < w; base += 128) {
+            const int x4 = base / 4 + lane;
+            const uint32_t v = (x4 * 4 < w) ? row[x4] : 0u;
+            const uint32_t n = (uint32_t)nonzero_bytes(v);
+            uint32_t incl = n;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o) incl += t;
+            }
+            uint32_t pos = running + incl - n;
+            for (int b = 0; b < 4; ++b) {
+                const uint32_t s = (v >> (8 * b)) & 0xffu;
+                if (s == 0u) continue;
+                if (pos < cap) {
+                    uint32_t* rec = feats + (size_t)pos * 12u;
+                    rec[0] = __float_as_uint((float)(x4 * 4 + b));
+                    rec[1] = __float_as_uint((float)y);
+                    rec[2] = s;
+                }
+                ++pos;
+            }
+            running += __shfl_sync(0xffffffffu, incl, 31);
+        }
+    }
+    const uint32_t kept = total < cap ? total : cap;
+    if (threadIdx.x == 0) {
+        F.raw[l] = total;
+        F.kept[l] = kept;
+    }
+
+    // counting sort of kept features by x
+    for (int i = threadIdx.x; i <= w; i += KC_THREADS) s_hist[i] = 0u;
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < kept; i += KC_THREADS) {
+        const int fx = (int)__uint_as_float(feats[(size_t)i * 12u]);
+        atomicAdd(&s_hist[fx], 1u);
+    }
+    __syncthreads();
+    const int per = (w + KC_THREADS) / KC_THREADS;  // bins per thread over w + 1 bins
+    const int b0 = threadIdx.x * per;
+    uint32_t local = 0;
+    for (int k = 0; k < per; ++k) {
+        const int b = b0 + k;
+        if (b < w) local += s_hist[b];
+    }
+    uint32_t tot;
+    uint32_t run = block_exclusive_scan(local, s_warp, &tot);
+    uint32_t* colstart = F.colstart[l];
+    for (int k = 0; k < per; ++k) {
+        const int b = b0 + k;
+        if (b <= w) {
+            const uint32_t c = b < w ? s_hist[b] : 0u;
+            colstart[b] = run;
+            s_hist[b] = run;  // becomes the fill cursor
+            run += c;
+        }
+    }
+    __syncthreads();
+    uint32_t* xorder = F.xorder[l];
+    for (uint32_t i = threadIdx.x; i < kept; i += KC_THREADS) {
+        const int fx = (int)__uint_as_float(feats[(size_t)i * 12u]);
+        const uint32_t slot = atomicAdd(&s_hist[fx], 1u);
+        xorder[slot] = i;
+    }
+}
+
+// ------------------------------------------------------------- K2 ----
+constexpr int KD_THREADS = 256;
+constexpr int MAX_SEGS = 4096;
+
+// Prefix over per-segment counts, shared by the persistent kernels.
+template <typename CountFn>
+__device__ uint32_t segment_prefix(int nseg, uint32_t* s_pref, uint32_t* s_warp, CountFn count) {
+    const int per = (nseg + blockDim.x - 1) / blockDim.x;
+    const int b0 = threadIdx.x * per;
+    uint32_t local = 0;
+    for (int k = 0; k < per; ++k)
+        if (b0 + k < nseg) local += count(b0 + k);
+    uint32_t tot;
+    uint32_t run = block_exclusive_scan(local, s_warp, &tot);
+    for (int k = 0; k < per; ++k) {
+        if (b0 + k < nseg) {
+            s_pref[b0 + k] = run;
+            run += count(b0 + k);
+        }
+    }
+    if (threadIdx.x == 0) s_pref[nseg] = tot;
+    __syncthreads();
+    return tot;
+}
+
+__device__ __forceinline__ int find_segment(const uint32_t* s_pref, int nseg, uint32_t g) {
+    int lo = 0, hi = nseg - 1;  // largest s with s_pref[s] <= g
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (s_pref[mid] <= g) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+// G(P) evaluated directly (points outside the level; the sampler clamps).
+__device__ float gauss_tap9_direct(const FrameDev& F, int l, uint32_t px, uint32_t py) {
+    const int w = F.w[l], h = F.h[l];
+    const float tex_x = 1.0f / (float)w;
+    const float tex_y = 1.0f / (float)h;
+    const float uvx = ((float)px + 0.5f) * tex_x;
+    const float uvy = ((float)py + 0.5f) * tex_y;
+    const float off[3] = {-1.2f, 0.0f, 1.2f};
+    const float wt[3] = {0.3125f, 0.375f, 0.3125f};
+    float sum = 0.0f;
+    for (int j = 0; j < 3; ++j) {
+        for (int i = 0; i < 3; ++i) {
+            const float u = (uvx + off[i] * tex_x) * (float)w - 0.5f;
+            const float v = (uvy + off[j] * tex_y) * (float)h - 0.5f;
+            const float fi = floorf(u), fj = floorf(v);
+            const float a = u - fi, b = v - fj;
+            const int i0 = edge_index(fi, w), i1 = edge_index(fi + 1.0f, w);
+            const int j0 = edge_index(fj, h), j1 = edge_index(fj + 1.0f, h);
+            const float na = 1.0f - a, nb = 1.0f - b;
+            float s = (na * nb) * level_texel(F, l, i0, j0);
+            s = s + (a * nb) * level_texel(F, l, i1, j0);
+            s = s + (na * b) * level_texel(F, l, i0, j1);
+            s = s + (a * b) * level_texel(F, l, i1, j1);
+            sum = sum + (s * wt[i]) * wt[j];
+        }
+    }
+    return sum;
+}
+
+__device__ __forceinline__ float gauss_tap9(const FrameDev& F, int l, uint32_t px, uint32_t py) {
+    if (px < (uint32_t)F.w[l] && py < (uint32_t)F.h[l])
+        return __ldg(F.blur[l] + (size_t)py * (size_t)F.w[l] + px);
+    return gauss_tap9_direct(F, l, px, py);
+}
+
+__global__ void __launch_bounds__(KD_THREADS)
+k_describe(const FrameDev* __restrict__ frames, const SegDev* __restrict__ segs, int nseg,
+           const int32_t* __restrict__ pattern) {
+    __shared__ int4 s_pat[256];
+    __shared__ uint32_t s_pref[MAX_SEGS + 1];
+    __shared__ uint32_t s_warp[33];
+    for (int i = threadIdx.x; i < 256; i += KD_THREADS)
+        s_pat[i] = make_int4(pattern[4 * i], pattern[4 * i + 1], pattern[4 * i + 2], pattern[4 * i + 3]);
+    const uint32_t total = segment_prefix(nseg, s_pref, s_warp, [&](int s) {
+        return frames[segs[s].frame].kept[segs[s].level];
+    });
+    const int lane = threadIdx.x & 31;
+    const int gw = blockIdx.x * (KD_THREADS / 32) + (threadIdx.x >> 5);
+    const int nw = gridDim.x * (KD_THREADS / 32);
+    for (uint32_t g = gw; g < total; g += nw) {
+        const int sidx = find_segment(s_pref, nseg, g);
+        const uint32_t i = g - s_pref[sidx];
+        const FrameDev& F = frames[segs[sidx].frame];
+        const int l = segs[sidx].level;
+        const int w = F.w[l], h = F.h[l];
+        uint32_t* rec = F.feats[l] + (size_t)i * 12u;
+        const int x = (int)__uint_as_float(rec[0]);
+        const int y = (int)__uint_as_float(rec[1]);
+
+        // orientation: intensity moments over the r = 3 disc, summed in order
+        float p = 0.0f;
+        if (lane < 29) {
+            const int cx = tint_clamp(x + c_disc_x[lane], w);
+            const int cy = tint_clamp(y + c_disc_y[lane], h);
+            p = level_texel(F, l, cx, cy);
+        }
+        float m10 = 0.0f, m01 = 0.0f;
+#pragma unroll
+        for (int k = 0; k < 29; ++k) {
+            const float v = __shfl_sync(0xffffffffu, p, k);
+            m10 = m10 + (float)c_disc_x[k] * v;
+            m01 = m01 + (float)c_disc_y[k] * v;
+        }
+        const float theta = uslam_atan2f(m01, m10);
+        float s, c;
+        uslam_sincosf(theta, &s, &c);
+
+        // 256 tests, lane j owns tests j, j + 32, ..., j + 224
+        uint32_t words[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            const int4 t = s_pat[lane + 32 * k];
+            const float fax = (float)t.x, fay = (float)t.y, fbx = (float)t.z, fby = (float)t.w;
+            const int rax = (int)rintf(fax * c - fay * s);
+            const int ray = (int)rintf(fax * s + fay * c);
+            const int rbx = (int)rintf(fbx * c - fby * s);
+            const int rby = (int)rintf(fbx * s + fby * c);
+            const float ga = gauss_tap9(F, l, (uint32_t)(x + rax), (uint32_t)(y + ray));
+            const float gb = gauss_tap9(F, l, (uint32_t)(x + rbx), (uint32_t)(y + rby));
+            words[k] = __ballot_sync(0xffffffffu, ga > gb);
+        }
+        uint32_t out = __float_as_uint(theta);
+#pragma unroll
+        for (int k = 0; k < 8; ++k)
+            if (lane == 4 + k) out = words[k];
+        if (lane >= 3 && lane < 12) rec[lane] = out;
+    }
+}
+
+// ------------------------------------------------------------- K3 ----
+constexpr int KM_THREADS = 256;
+
+struct MatchSegDev {
+    int pair;
+    int dir;    // 0: queries = curr (b), pool = prev (a); 1: the reverse
+    int level;
+};
+
+__device__ __forceinline__ float lod_scale(int lod) {
+    float s = 1.0f;  // match_features_cpu.cpp:58-64
+    for (int i = 0; i < lod; ++i) s = s * 1.2f;
+    return s;
+}
+
+// First xb in [0, w] with (float)xb * s >= lo (w if none).
+__device__ int first_col_ge(float lo, float s, int w) {
+    int xb = (int)fminf(fmaxf(floorf(lo / s) - 1.0f, 0.0f), (float)w);
+    while (xb > 0 && (float)(xb - 1) * s >= lo) --xb;
+    while (xb < w && !((float)xb * s >= lo)) ++xb;
+    return xb;
+}
+
+// Last xb in [-1, w - 1] with (float)xb * s <= hi (-1 if none).
+__device__ int last_col_le(float hi, float s, int w) {
+    int xb = (int)fminf(fmaxf(floorf(hi / s) + 1.0f, -1.0f), (float)(w - 1));
+    while (xb < w - 1 && (float)(xb + 1) * s <= hi) ++xb;
+    while (xb >= 0 && !((float)xb * s <= hi)) --xb;
+    return xb;
+}
+
+__global__ void __launch_bounds__(KM_THREADS)
+k_match(const FrameDev* __restrict__ frames, const PairDev* __restrict__ pairs,
+        const MatchSegDev* __restrict__ segs, int nseg) {
+    __shared__ uint32_t s_pref[MAX_SEGS + 1];
+    __shared__ uint32_t s_warp[33];
+    const uint32_t total = segment_prefix(nseg, s_pref, s_warp, [&](int s) {
+        const PairDev& P = pairs[segs[s].pair];
+        const int qf = segs[s].dir == 0 ? P.curr : P.prev;
+        return frames[qf].kept[segs[s].level];
+    });
+    const int lane = threadIdx.x & 31;
+    const int gw = blockIdx.x * (KM_THREADS / 32) + (threadIdx.x >> 5);
+    const int nw = gridDim.x * (KM_THREADS / 32);
+    for (uint32_t g = gw; g < total; g += nw) {
+        const int sidx = find_segment(s_pref, nseg, g);
+        const uint32_t i = g - s_pref[sidx];
+        const MatchSegDev sg = segs[sidx];
+        const PairDev& P = pairs[sg.pair];
+        const FrameDev& Q = frames[sg.dir == 0 ? P.curr : P.prev];
+        const FrameDev& B = frames[sg.dir == 0 ? P.prev : P.curr];
+        const int l = sg.level;
+        const uint32_t* qrec = Q.feats[l] + (size_t)i * 12u;
+        const float ql = lod_scale(l);
+        const float cx = (float)(uint32_t)__uint_as_float(qrec[0]) * ql;
+        const float cy = (float)(uint32_t)__uint_as_float(qrec[1]) * ql;
+        const uint4 qd0 = *reinterpret_cast<const uint4*>(qrec + 4);
+        const uint4 qd1 = *reinterpret_cast<const uint4*>(qrec + 8);
+
+        uint32_t best = 0xffffffffu, second = 0xffffffffu;
+        int32_t bidx = -1;
+        const int L = B.levels;
+        uint32_t pool = B.kept[l];
+        if (l > 0) pool += B.kept[l - 1];
+        if (l + 1 < L) pool += B.kept[l + 1];
+        if (pool >= 2u) {
+            const float lo = cx - P.max_dx, hi = cx + P.max_dx;
+            for (int k = 0; k < 3; ++k) {
+                const int pl = k == 0 ? l : (k == 1 ? l - 1 : l + 1);
+                if (pl < 0 || pl >= L) continue;
+                const float ps = lod_scale(pl);
+                const int wpl = B.w[pl];
+                const int xlo = first_col_ge(lo, ps, wpl);
+                const int xhi = last_col_le(hi, ps, wpl);
+                if (xlo > xhi) continue;
+                const uint32_t c0 = B.colstart[pl][xlo], c1 = B.colstart[pl][xhi + 1];
+                const uint32_t* xorder = B.xorder[pl];
+                const uint32_t* feats = B.feats[pl];
+                for (uint32_t kk = c0 + lane; kk < c1; kk += 32) {
+                    const uint32_t j = __ldg(xorder + kk);
+                    const uint32_t* rec = feats + (size_t)j * 12u;
+                    const float by = (float)(uint32_t)__uint_as_float(__ldg(rec + 1)) * ps;
+                    if (fabsf(cy - by) > P.max_dy) continue;
+                    const uint4 d0 = __ldg(reinterpret_cast<const uint4*>(rec + 4));
+                    const uint4 d1 = __ldg(reinterpret_cast<const uint4*>(rec + 8));
+                    const uint32_t d = __popc(d0.x ^ qd0.x) + __popc(d0.y ^ qd0.y) + __popc(d0.z ^ qd0.z) +
+                                       __popc(d0.w ^ qd0.w) + __popc(d1.x ^ qd1.x) + __popc(d1.y ^ qd1.y) +
+                                       __popc(d1.z ^ qd1.z) + __popc(d1.w ^ qd1.w);
+                    if (d < best) {
+                        second = best;
+                        best = d;
+                        bidx = USLAM_PACK(pl, j);
+                    } else if (d < second) {
+                        second = d;
+                    }
+                }
+            }
+        }
+        // warp merge of (best, second, idx)
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const uint32_t ob = __shfl_xor_sync(0xffffffffu, best, o);
+            const uint32_t os = __shfl_xor_sync(0xffffffffu, second, o);
+            const int32_t oi = __shfl_xor_sync(0xffffffffu, bidx, o);
+            if (ob < best || (ob == best && oi > bidx)) {
+                second = min(best, os);
+                best = ob;
+                bidx = oi;
+            } else {
+                second = min(second, ob);
+            }
+        }
+        if (lane == 0) {
+            int32_t res = -1;
+            if (bidx >= 0 && (float)best < 0.85f * (float)second) res = bidx;
+            const int capq = Q.cap;
+            if (sg.dir == 0) P.b2a[(size_t)l * capq + i] = res;
+            else P.a2b[(size_t)l * capq + i] = res;
+        }
+    }
+}
+
+// ---------------------------------------------------------- mutual ----
+constexpr int KU_THREADS = 256;
+
+// One CTA per (pair, level of a): keep (a, b) iff b2a[b] == a, in a order
+// (match_features_cpu.cpp:196-205).
+__global__ void __launch_bounds__(KU_THREADS)
+k_mutual(const FrameDev* __restrict__ frames, const PairDev* __restrict__ pairs, const SegDev* __restrict__ segs,
+         uint32_t* err) {
+    __shared__ uint32_t s_warp[33];
+    const int pi = segs[blockIdx.x].frame;  // pair index
+    const int l = segs[blockIdx.x].level;
+    const PairDev& P = pairs[pi];
+    const FrameDev& A = frames[P.prev];
+    const FrameDev& B = frames[P.curr];
+    const uint32_t n = A.kept[l];
+    uint32_t base = 0;
+    for (uint32_t c0 = 0; c0 < n; c0 += KU_THREADS) {
+        const uint32_t i = c0 + threadIdx.x;
+        int32_t m = -1;
+        bool ok = false;
+        if (i < n) {
+            m = P.a2b[(size_t)l * A.cap + i];
+            if (m >= 0) {
+                const int bl = USLAM_PACK_LEVEL(m), bi = USLAM_PACK_INDEX(m);
+                ok = P.b2a[(size_t)bl * B.cap + bi] == USLAM_PACK(l, i);
+            }
+        }
+        uint32_t tot;
+        const uint32_t pos = base + block_exclusive_scan(ok ? 1u : 0u, s_warp, &tot);
+        if (ok) {
+            if (pos < (uint32_t)P.max_matches_per_level) {
+                int32_t* o = P.matches + ((size_t)l * P.max_matches_per_level + pos) * 4;
+                o[0] = l;
+                o[1] = (int32_t)i;
+                o[2] = USLAM_PACK_LEVEL(m);
+                o[3] = USLAM_PACK_INDEX(m);
+            } else {
+                atomicOr(err, USLAM_ERR_MATCH_OVERFLOW);
+            }
+        }
+        base += tot;
+    }
+    if (threadIdx.x == 0) P.match_count[l] = base;
+}
+
+}  // namespace uslam
+
+// ------------------------------------------------------------ launch ----
+namespace uslam {
+
+cudaError_t init_constants() {
+    int8_t dx[32] = {0}, dy[32] = {0};
+    int n = 0;
+    for (int y = -3; y <= 3; ++y)
+        for (int x = -3; x <= 3; ++x)
+            if (x * x + y * y <= 9) {
+                dx[n] = (int8_t)x;
+                dy[n] = (int8_t)y;
+                ++n;
+            }
+    cudaError_t e = cudaMemcpyToSymbol(c_disc_x, dx, sizeof(dx));
+    if (e != cudaSuccess) return e;
+    return cudaMemcpyToSymbol(c_disc_y, dy, sizeof(dy));
+}
+
+cudaError_t launch_detect(const FrameDev* frames, const TileItem* tiles, int ntiles, uint32_t* err,
+                          cudaStream_t st) {
+    if (ntiles <= 0) return cudaSuccess;
+    k_detect<<<ntiles, K1_THREADS, 0, st>>>(frames, tiles, err);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_compact(const FrameDev* frames, const SegDev* segs, int nseg, int max_w, cudaStream_t st) {
+    if (nseg <= 0) return cudaSuccess;
+    const size_t smem = (size_t)(max_w + 1) * sizeof(uint32_t);
+    k_compact<<<nseg, KC_THREADS, smem, st>>>(frames, segs);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_describe(const FrameDev* frames, const SegDev* segs, int nseg, const int32_t* pattern,
+                            int grid, cudaStream_t st) {
+    if (nseg <= 0) return cudaSuccess;
+    k_describe<<<grid, KD_THREADS, 0, st>>>(frames, segs, nseg, pattern);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_match(const FrameDev* frames, const PairDev* pairs, const void* segs, int nseg, int grid,
+                         cudaStream_t st) {
+    if (nseg <= 0) return cudaSuccess;
+    k_match<<<grid, KM_THREADS, 0, st>>>(frames, pairs, static_cast<const MatchSegDev*>(segs), nseg);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_mutual(const FrameDev* frames, const PairDev* pairs, const SegDev* segs, int nseg,
+                          uint32_t* err, cudaStream_t st) {
+    if (nseg <= 0) return cudaSuccess;
+    k_mutual<<<nseg, KU_THREADS, 0, st>>>(frames, pairs, segs, err);
+    return cudaGetLastError();
+}
+
+cudaError_t set_compact_smem(int max_w) {
+    const size_t smem = (size_t)(max_w + 1) * sizeof(uint32_t);
+    if (smem <= 48 * 1024) return cudaSuccess;
+    return cudaFuncSetAttribute(k_compact, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+}
+
+}  // namespace uslam

@@ -1,0 +1,984 @@
+// runtime.cu — host runtime and C ABI of the GB300 feature front-end.
+//
+// A context (uslam_ctx) owns the device, the BRIEF table and the per-
+// resolution cull coverage masks.  A batch (uslam_batch) is a work table over
+// frames and frame pairs with every buffer carved out of one arena:
+//   [inputs: LOD0 u8 of every frame][outputs: counts + features of every
+//   frame, counts + matches of every pair][scratch: pyramid, blur cache,
+//   keypoint maps, x-sort tables, match directions, error word]
+// so one H2D copy feeds the whole batch and one D2H copy returns it.  The
+// batch's launch sequence (5 kernels) is captured once into a CUDA graph.
+// A frontend (uslam_frontend) is a 2-slot batch driven frame by frame with
+// the reference's FeatureSet(0)/(1) rotation.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <string>
+#include <thread>
+#include <utility>
+#include <vector>
+
+#include "../../include/uslam.h"
+#include "uslam_internal.h"
+
+namespace uslam {
+struct MatchSegDev {
+    int pair;
+    int dir;
+    int level;
+};
+cudaError_t init_constants();
+cudaError_t launch_detect(const FrameDev*, const TileItem*, int, uint32_t*, cudaStream_t);
+cudaError_t launch_compact(const FrameDev*, const SegDev*, int, int, cudaStream_t);
+cudaError_t launch_describe(const FrameDev*, const SegDev*, int, const int32_t*, int, cudaStream_t);
+cudaError_t launch_match(const FrameDev*, const PairDev*, const void*, int, int, cudaStream_t);
+cudaError_t launch_mutual(const FrameDev*, const PairDev*, const SegDev*, int, uint32_t*, cudaStream_t);
+cudaError_t set_compact_smem(int max_w);
+constexpr int kTileW = 64;
+constexpr int kTileH = 16;
+constexpr int kMaxSegs = 4096;
+constexpr int kMaxWidth = 8192;
+}  // namespace uslam
+
+using namespace uslam;
+
+namespace {
+
+size_t round_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+
+uslam_status set_err(std::string* dst, uslam_status s, const std::string& msg) {
+    if (dst) *dst = msg;
+    return s;
+}
+
+// Level dims (wslam/src/common.cpp:41-45).
+void level_dims(int W0, int H0, int levels, int* w, int* h) {
+    for (int l = 0; l < levels; ++l) {
+        const double factor = l == 0 ? 1.0 : std::pow(1.2, static_cast<double>(l));
+        w[l] = static_cast<int>(static_cast<uint32_t>(static_cast<double>(W0) / factor));
+        h[l] = static_cast<int>(static_cast<uint32_t>(static_cast<double>(H0) / factor));
+    }
+}
+
+uint32_t ceil_div_u(uint32_t n, uint32_t d) { return (n + d - 1u) / d; }
+
+// Coverage of the reference's cull passes for one level, as a bitmap.
+// main_horizontal (resources/cull_corners.wgsl:22-57) with dispatch
+// ceil(ceil(W0/3)/64) x H0 x levels workgroups of 64 (cull_corners.cpp:332-341)
+// writes H[9*gx + y*w] = S for every start >= w (the regional loop is empty
+// there because end = min(start+3, w) <= start); in row 0 it keeps the first
+// arg-max of [9k, min(9k+3, w)).  main_vertical (:60-109) with dispatch
+// ceil(W0/64) x ceil(H0/3) copies H at start + k*w, k < min((W0*H0 - start)/w, 3),
+// start = 3*gx + 3*gy*w, and at start itself in every case.  A keypoint is a pixel whose final value is > 0, so:
+//   bit(p) = V(p) && (p < w ? p % 9 < 3 : H(p)),
+// with the row-0 arg-max applied in the kernel.
+std::vector<uint32_t> build_cull_mask(int W0, int H0, int w, int h) {
+    const uint64_t n = static_cast<uint64_t>(w) * static_cast<uint64_t>(h);
+    const uint64_t blk = static_cast<uint64_t>(W0) * static_cast<uint64_t>(H0);
+    std::vector<uint8_t> mh(n, 0), mv(n, 0);
+    const uint32_t gx_h = ceil_div_u(ceil_div_u(W0, 3), 64) * 64;
+    const uint32_t gy_h = static_cast<uint32_t>(H0);
+    const uint32_t gx_v = ceil_div_u(W0, 64) * 64;
+    const uint32_t gy_v = ceil_div_u(H0, 3);
+    for (uint32_t y = 0; y < gy_h; ++y)
+        for (uint32_t gx = 0; gx < gx_h; ++gx) {
+            const uint64_t s = 9ull * gx + static_cast<uint64_t>(y) * w;
+            if (s < n && s >= static_cast<uint64_t>(w)) mh[s] = 1;
+        }
+    for (uint32_t gy = 0; gy < gy_v; ++gy)
+        for (uint32_t gx = 0; gx < gx_v; ++gx) {
+            const uint64_t s = 3ull * gx + 3ull * gy * static_cast<uint64_t>(w);
+            if (s >= n) continue;
+            // didFindMax starts as src[start] > 0, so V[start] = H[start] even
+            // when the loop below is empty (cull_corners.wgsl:83-97)
+            mv[s] = 1;
+            uint64_t cnt = (blk - s) / static_cast<uint64_t>(w);
+            if (cnt > 3) cnt = 3;
+            for (uint64_t k = 0; k < cnt; ++k) {
+                const uint64_t i = s + k * static_cast<uint64_t>(w);
+                if (i < n) mv[i] = 1;
+            }
+        }
+    std::vector<uint32_t> bits((n + 31) / 32, 0u);
+    for (uint64_t p = 0; p < n; ++p) {
+        const bool keep = mv[p] && (p < static_cast<uint64_t>(w) ? (p % 9) < 3 : mh[p] != 0);
+        if (keep) bits[p >> 5] |= 1u << (p & 31);
+    }
+    return bits;
+}
+
+struct ResClass {
+    int W0 = 0, H0 = 0;
+    std::vector<uint32_t*> d_mask;
+};
+
+}  // namespace
+
+struct uslam_ctx {
+    int device = 0;
+    int levels = 6;
+    int max_w = 0, max_h = 0;
+    int cap_override = 0;
+    int num_sms = 0;
+    int32_t* d_pattern = nullptr;
+    std::string err;
+    std::map<std::pair<int, int>, ResClass> classes;
+
+    uslam_status cuda_fail(cudaError_t e, const char* what) {
+        err = std::string(what) + ": " + cudaGetErrorString(e);
+        return USLAM_CUDA_ERROR;
+    }
+    // Masks of a resolution class, built and uploaded on first use.
+    uslam_status masks_for(int W0, int H0, const int* w, const int* h, std::vector<uint32_t*>* out) {
+        auto key = std::make_pair(W0, H0);
+        auto it = classes.find(key);
+        if (it == classes.end()) {
+            ResClass rc;
+            rc.W0 = W0;
+            rc.H0 = H0;
+            for (int l = 0; l < levels; ++l) {
+                const std::vector<uint32_t> bits = build_cull_mask(W0, H0, w[l], h[l]);
+                uint32_t* d = nullptr;
+                cudaError_t e = cudaMalloc(&d, bits.size() * sizeof(uint32_t));
+                if (e != cudaSuccess) {
+                    for (auto* p : rc.d_mask) cudaFree(p);
+                    err = std::string("cull mask allocation: ") + cudaGetErrorString(e);
+                    return e == cudaErrorMemoryAllocation ? USLAM_OOM : USLAM_CUDA_ERROR;
+                }
+                e = cudaMemcpy(d, bits.data(), bits.size() * sizeof(uint32_t), cudaMemcpyHostToDevice);
+                if (e != cudaSuccess) {
+                    cudaFree(d);
+                    for (auto* p : rc.d_mask) cudaFree(p);
+                    return cuda_fail(e, "cull mask upload");
+                }
+                rc.d_mask.push_back(d);
+            }
+            it = classes.emplace(key, std::move(rc)).first;
+        }
+        *out = it->second.d_mask;
+        return USLAM_OK;
+    }
+};
+
+namespace {
+
+// Launch tables of one program (a subset of the batch's frames and pairs).
+struct Program {
+    int ntiles = 0, nfsegs = 0, nmsegs = 0, nusegs = 0;
+    TileItem* tiles = nullptr;
+    SegDev* fsegs = nullptr;
+    MatchSegDev* msegs = nullptr;
+    SegDev* usegs = nullptr;
+    std::vector<char> host;  // host image of the tables
+    cudaGraphExec_t graph = nullptr;
+};
+
+}  // namespace
+
+struct uslam_batch {
+    uslam_ctx* ctx = nullptr;
+    int levels = 0;
+    int max_w = 0;
+    std::vector<FrameDev> frames;
+    std::vector<PairDev> pairs;
+    std::vector<size_t> in_off;    // per frame, offset of the input in the inputs region
+    std::vector<size_t> feat_off;  // per frame, offset of its outputs in the outputs region
+    std::vector<size_t> pair_off;  // per pair, offset of its outputs in the outputs region
+    char* arena = nullptr;
+    size_t in_bytes = 0, out_bytes = 0, arena_bytes = 0;
+    char* h_in = nullptr;   // pinned
+    char* h_out = nullptr;  // pinned
+    FrameDev* d_frames = nullptr;
+    PairDev* d_pairs = nullptr;
+    uint32_t* d_err = nullptr;
+    char* d_tables = nullptr;
+    cudaStream_t stream = nullptr;      // stream in use (own or caller's)
+    cudaStream_t own_stream = nullptr;  // created with the batch
+    Program full;
+    std::vector<Program> frame_prog;  // per frame: detect+describe only
+    std::vector<Program> pair_prog;   // per pair: match only
+    std::string* err() { return &ctx->err; }
+};
+
+namespace {
+
+uslam_status build_program(uslam_batch* b, const std::vector<int>& fr, const std::vector<int>& pr, Program* P) {
+    std::vector<TileItem> tiles;
+    std::vector<SegDev> fsegs, usegs;
+    std::vector<MatchSegDev> msegs;
+    for (int f : fr) {
+        const FrameDev& F = b->frames[f];
+        for (int l = 0; l < F.levels; ++l) {
+            const int nx = (F.w[l] + kTileW - 1) / kTileW, ny = (F.h[l] + kTileH - 1) / kTileH;
+            for (int ty = 0; ty < ny; ++ty)
+                for (int tx = 0; tx < nx; ++tx) {
+                    TileItem t{};
+                    t.frame = static_cast<uint16_t>(f);
+                    t.level = static_cast<uint8_t>(l);
+                    t.tx = static_cast<uint16_t>(tx);
+                    t.ty = static_cast<uint16_t>(ty);
+                    tiles.push_back(t);
+                }
+            fsegs.push_back(SegDev{f, l});
+        }
+    }
+    for (int p : pr) {
+        for (int l = 0; l < b->levels; ++l) {
+            msegs.push_back(MatchSegDev{p, 0, l});
+            msegs.push_back(MatchSegDev{p, 1, l});
+            usegs.push_back(SegDev{p, l});
+        }
+    }
+    if (static_cast<int>(fsegs.size()) > kMaxSegs || static_cast<int>(msegs.size()) > kMaxSegs)
+        return set_err(b->err(), USLAM_CAPACITY, "batch exceeds 4096 (frame, level) or (pair, dir, level) segments");
+    P->ntiles = static_cast<int>(tiles.size());
+    P->nfsegs = static_cast<int>(fsegs.size());
+    P->nmsegs = static_cast<int>(msegs.size());
+    P->nusegs = static_cast<int>(usegs.size());
+    const size_t t_bytes = round_up(tiles.size() * sizeof(TileItem), 256);
+    const size_t f_bytes = round_up(fsegs.size() * sizeof(SegDev), 256);
+    const size_t m_bytes = round_up(msegs.size() * sizeof(MatchSegDev), 256);
+    const size_t u_bytes = round_up(usegs.size() * sizeof(SegDev), 256);
+    P->host.assign(t_bytes + f_bytes + m_bytes + u_bytes, 0);
+    std::memcpy(P->host.data(), tiles.data(), tiles.size() * sizeof(TileItem));
+    std::memcpy(P->host.data() + t_bytes, fsegs.data(), fsegs.size() * sizeof(SegDev));
+    std::memcpy(P->host.data() + t_bytes + f_bytes, msegs.data(), msegs.size() * sizeof(MatchSegDev));
+    std::memcpy(P->host.data() + t_bytes + f_bytes + m_bytes, usegs.data(), usegs.size() * sizeof(SegDev));
+    return USLAM_OK;
+}
+
+// Enqueue a program's launch sequence on the batch stream.
+cudaError_t enqueue_program(uslam_batch* b, const Program& P) {
+    uslam_ctx* c = b->ctx;
+    cudaError_t e = cudaSuccess;
+    if (P.ntiles > 0) {
+        if ((e = launch_detect(b->d_frames, P.tiles, P.ntiles, b->d_err, b->stream)) != cudaSuccess) return e;
+        if ((e = launch_compact(b->d_frames, P.fsegs, P.nfsegs, b->max_w, b->stream)) != cudaSuccess) return e;
+        const int grid = c->num_sms * 4;
+        if ((e = launch_describe(b->d_frames, P.fsegs, P.nfsegs, c->d_pattern, grid, b->stream)) != cudaSuccess)
+            return e;
+    }
+    if (P.nmsegs > 0) {
+        const int grid = c->num_sms * 4;
+        if ((e = launch_match(b->d_frames, b->d_pairs, P.msegs, P.nmsegs, grid, b->stream)) != cudaSuccess) return e;
+        if ((e = launch_mutual(b->d_frames, b->d_pairs, P.usegs, P.nusegs, b->d_err, b->stream)) != cudaSuccess)
+            return e;
+    }
+    return cudaSuccess;
+}
+
+uslam_status capture_graph(uslam_batch* b, Program* P) {
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return b->ctx->cuda_fail(e, "begin capture");
+    e = cudaMemsetAsync(b->d_err, 0, sizeof(uint32_t), b->stream);
+    cudaError_t e2 = e == cudaSuccess ? enqueue_program(b, *P) : e;
+    e = cudaStreamEndCapture(b->stream, &g);
+    if (e2 != cudaSuccess) {
+        if (g) cudaGraphDestroy(g);
+        return b->ctx->cuda_fail(e2, "capture launches");
+    }
+    if (e != cudaSuccess) return b->ctx->cuda_fail(e, "end capture");
+    e = cudaGraphInstantiate(&P->graph, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return b->ctx->cuda_fail(e, "graph instantiate");
+    return USLAM_OK;
+}
+
+void free_batch(uslam_batch* b) {
+    if (!b) return;
+    auto drop = [](Program& P) {
+        if (P.graph) cudaGraphExecDestroy(P.graph);
+        P.graph = nullptr;
+    };
+    drop(b->full);
+    for (auto& P : b->frame_prog) drop(P);
+    for (auto& P : b->pair_prog) drop(P);
+    if (b->own_stream) cudaStreamDestroy(b->own_stream);
+    if (b->arena) cudaFree(b->arena);
+    if (b->d_tables) cudaFree(b->d_tables);
+    if (b->h_in) cudaFreeHost(b->h_in);
+    if (b->h_out) cudaFreeHost(b->h_out);
+    delete b;
+}
+
+uslam_status create_batch(uslam_ctx* ctx, int n_frames, const int* widths, const int* heights, int n_pairs,
+                          const int* pair_prev, const int* pair_curr, bool per_item_programs, uslam_batch** out) {
+    if (!ctx || !out || n_frames <= 0 || !widths || !heights || n_pairs < 0 || (n_pairs > 0 && (!pair_prev || !pair_curr)))
+        return set_err(ctx ? &ctx->err : nullptr, USLAM_INVALID_ARG, "batch_create: bad arguments");
+    if (n_frames > 65535) return set_err(&ctx->err, USLAM_INVALID_ARG, "batch_create: more than 65535 frames");
+    cudaError_t e = cudaSetDevice(ctx->device);
+    if (e != cudaSuccess) return ctx->cuda_fail(e, "cudaSetDevice");
+    auto* b = new uslam_batch();
+    b->ctx = ctx;
+    b->levels = ctx->levels;
+    const int L = ctx->levels;
+    b->frames.resize(n_frames);
+    b->in_off.resize(n_frames);
+    b->feat_off.resize(n_frames);
+    // ---- layout pass: offsets relative to region starts
+    size_t in_bytes = 0, out_bytes = 0, scratch = 0;
+    auto take = [](size_t* cur, size_t n) {
+        const size_t o = round_up(*cur, 256);
+        *cur = o + n;
+        return o;
+    };
+    struct FrameLayout {
+        size_t lvl[USLAM_MAX_LEVELS], blur[USLAM_MAX_LEVELS], kpmap[USLAM_MAX_LEVELS], feats[USLAM_MAX_LEVELS],
+            xorder[USLAM_MAX_LEVELS], colstart[USLAM_MAX_LEVELS], counts;
+    };
+    std::vector<FrameLayout> fl(n_frames);
+    for (int f = 0; f < n_frames; ++f) {
+        const int W0 = widths[f], H0 = heights[f];
+        if (W0 <= 0 || H0 <= 0 || W0 > ctx->max_w || H0 > ctx->max_h) {
+            free_batch(b);
+            return set_err(&ctx->err, USLAM_INVALID_ARG,
+                           "batch_create: frame " + std::to_string(f) + " size " + std::to_string(W0) + "x" +
+                               std::to_string(H0) + " outside 1.." + std::to_string(ctx->max_w) + "x" +
+                               std::to_string(ctx->max_h));
+        }
+        FrameDev& F = b->frames[f];
+        std::memset(&F, 0, sizeof(F));
+        F.W0 = W0;
+        F.H0 = H0;
+        F.levels = L;
+        F.img_pitch = static_cast<int>(round_up(static_cast<size_t>(W0), 16));
+        level_dims(W0, H0, L, F.w, F.h);
+        for (int l = 0; l < L; ++l) {
+            if (F.w[l] < 1 || F.h[l] < 1) {
+                free_batch(b);
+                return set_err(&ctx->err, USLAM_INVALID_ARG,
+                               "batch_create: frame " + std::to_string(f) + " has an empty pyramid level " +
+                                   std::to_string(l));
+            }
+        }
+        const long long cap_ll = ctx->cap_override > 0 ? ctx->cap_override
+                                                       : static_cast<long long>(W0) * H0 / 250;
+        F.cap = static_cast<int>(cap_ll);
+        const size_t capa = static_cast<size_t>(F.cap > 0 ? F.cap : 1);
+        b->in_off[f] = take(&in_bytes, static_cast<size_t>(H0) * F.img_pitch);
+        b->feat_off[f] = take(&out_bytes, 2 * sizeof(uint32_t) * L);
+        FrameLayout& Ly = fl[f];
+        Ly.counts = b->feat_off[f];
+        for (int l = 0; l < L; ++l) {
+            const size_t n = static_cast<size_t>(F.w[l]) * F.h[l];
+            F.kp_pitch[l] = static_cast<int>(round_up(static_cast<size_t>(F.w[l]), 16));
+            Ly.feats[l] = take(&out_bytes, capa * 48);
+            Ly.lvl[l] = l > 0 ? take(&scratch, n * 4) : 0;
+            Ly.blur[l] = take(&scratch, n * 4);
+            Ly.kpmap[l] = take(&scratch, static_cast<size_t>(F.h[l]) * F.kp_pitch[l]);
+            Ly.xorder[l] = take(&scratch, capa * 4);
+            Ly.colstart[l] = take(&scratch, (static_cast<size_t>(F.w[l]) + 1) * 4);
+        }
+        b->max_w = std::max(b->max_w, F.w[0]);
+    }
+    b->pairs.resize(n_pairs);
+    b->pair_off.resize(n_pairs);
+    std::vector<std::pair<size_t, size_t>> dirs(n_pairs);
+    for (int p = 0; p < n_pairs; ++p) {
+        const int a = pair_prev[p], c = pair_curr[p];
+        if (a < 0 || a >= n_frames || c < 0 || c >= n_frames || a == c) {
+            free_batch(b);
+            return set_err(&ctx->err, USLAM_INVALID_ARG, "batch_create: pair " + std::to_string(p) + " has bad frame indices");
+        }
+        if (b->frames[a].W0 != b->frames[c].W0 || b->frames[a].H0 != b->frames[c].H0) {
+            free_batch(b);
+            return set_err(&ctx->err, USLAM_INVALID_ARG, "batch_create: pair " + std::to_string(p) + " mixes frame sizes");
+        }
+        PairDev& P = b->pairs[p];
+        std::memset(&P, 0, sizeof(P));
+        P.prev = a;
+        P.curr = c;
+        const int capa = std::max(b->frames[a].cap, 1), capc = std::max(b->frames[c].cap, 1);
+        P.max_matches_per_level = capa;
+        // match_features_cpu.cpp:76-77: 0.1F * frame size, in f32
+        P.max_dx = 0.1f * static_cast<float>(static_cast<uint32_t>(b->frames[a].W0));
+        P.max_dy = 0.1f * static_cast<float>(static_cast<uint32_t>(b->frames[a].H0));
+        b->pair_off[p] = take(&out_bytes, round_up(sizeof(uint32_t) * L, 16) + static_cast<size_t>(L) * capa * 16);
+        dirs[p].first = take(&scratch, static_cast<size_t>(L) * capa * 4);
+        dirs[p].second = take(&scratch, static_cast<size_t>(L) * capc * 4);
+    }
+    const size_t err_off = take(&scratch, 256);
+    const size_t frames_off = take(&scratch, sizeof(FrameDev) * n_frames);
+    const size_t pairs_off = take(&scratch, sizeof(PairDev) * std::max(n_pairs, 1));
+    in_bytes = round_up(in_bytes, 256);
+    out_bytes = round_up(out_bytes, 256);
+    b->in_bytes = in_bytes;
+    b->out_bytes = out_bytes;
+    b->arena_bytes = in_bytes + out_bytes + round_up(scratch, 256);
+
+    e = cudaMalloc(&b->arena, b->arena_bytes);
+    if (e != cudaSuccess) {
+        const std::string m = std::string("arena of ") + std::to_string(b->arena_bytes) + " bytes: " + cudaGetErrorString(e);
+        free_batch(b);
+        cudaGetLastError();
+        return set_err(&ctx->err, USLAM_OOM, m);
+    }
+    e = cudaHostAlloc(&b->h_in, in_bytes, cudaHostAllocDefault);
+    if (e == cudaSuccess) e = cudaHostAlloc(&b->h_out, out_bytes, cudaHostAllocDefault);
+    if (e != cudaSuccess) {
+        free_batch(b);
+        cudaGetLastError();
+        return set_err(&ctx->err, USLAM_OOM, "pinned staging allocation refused");
+    }
+    std::memset(b->h_in, 0, in_bytes);
+    std::memset(b->h_out, 0, out_bytes);
+    e = cudaMemset(b->arena, 0, b->arena_bytes);
+    if (e != cudaSuccess) {
+        free_batch(b);
+        return ctx->cuda_fail(e, "arena clear");
+    }
+    e = cudaStreamCreateWithFlags(&b->own_stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        free_batch(b);
+        return ctx->cuda_fail(e, "stream create");
+    }
+    b->stream = b->own_stream;
+    char* in_base = b->arena;
+    char* out_base = b->arena + in_bytes;
+    char* sc_base = b->arena + in_bytes + out_bytes;
+    for (int f = 0; f < n_frames; ++f) {
+        FrameDev& F = b->frames[f];
+        const FrameLayout& Ly = fl[f];
+        F.img = reinterpret_cast<const uint8_t*>(in_base + b->in_off[f]);
+        F.kept = reinterpret_cast<uint32_t*>(out_base + Ly.counts);
+        F.raw = F.kept + L;
+        std::vector<uint32_t*> masks;
+        uslam_status s = ctx->masks_for(F.W0, F.H0, F.w, F.h, &masks);
+        if (s != USLAM_OK) {
+            free_batch(b);
+            return s;
+        }
+        for (int l = 0; l < L; ++l) {
+            F.lvl[l] = l > 0 ? reinterpret_cast<float*>(sc_base + Ly.lvl[l]) : nullptr;
+            F.blur[l] = reinterpret_cast<float*>(sc_base + Ly.blur[l]);
+            F.kpmap[l] = reinterpret_cast<uint8_t*>(sc_base + Ly.kpmap[l]);
+            F.feats[l] = reinterpret_cast<uint32_t*>(out_base + Ly.feats[l]);
+            F.xorder[l] = reinterpret_cast<uint32_t*>(sc_base + Ly.xorder[l]);
+            F.colstart[l] = reinterpret_cast<uint32_t*>(sc_base + Ly.colstart[l]);
+            F.mask[l] = masks[l];
+        }
+    }
+    for (int p = 0; p < n_pairs; ++p) {
+        PairDev& P = b->pairs[p];
+        P.match_count = reinterpret_cast<uint32_t*>(out_base + b->pair_off[p]);
+        P.matches = reinterpret_cast<int32_t*>(out_base + b->pair_off[p] + round_up(sizeof(uint32_t) * L, 16));
+        P.a2b = reinterpret_cast<int32_t*>(sc_base + dirs[p].first);
+        P.b2a = reinterpret_cast<int32_t*>(sc_base + dirs[p].second);
+    }
+    b->d_err = reinterpret_cast<uint32_t*>(sc_base + err_off);
+    b->d_frames = reinterpret_cast<FrameDev*>(sc_base + frames_off);
+    b->d_pairs = reinterpret_cast<PairDev*>(sc_base + pairs_off);
+    e = cudaMemcpy(b->d_frames, b->frames.data(), sizeof(FrameDev) * n_frames, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && n_pairs > 0)
+        e = cudaMemcpy(b->d_pairs, b->pairs.data(), sizeof(PairDev) * n_pairs, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        free_batch(b);
+        return ctx->cuda_fail(e, "frame table upload");
+    }
+    e = set_compact_smem(b->max_w);
+    if (e != cudaSuccess) {
+        free_batch(b);
+        return ctx->cuda_fail(e, "compact smem attribute");
+    }
+    // ---- programs
+    std::vector<int> all_f(n_frames), all_p(n_pairs);
+    for (int f = 0; f < n_frames; ++f) all_f[f] = f;
+    for (int p = 0; p < n_pairs; ++p) all_p[p] = p;
+    std::vector<Program*> progs;
+    uslam_status s = build_program(b, all_f, all_p, &b->full);
+    if (s != USLAM_OK) {
+        free_batch(b);
+        return s;
+    }
+    progs.push_back(&b->full);
+    if (per_item_programs) {
+        b->frame_prog.resize(n_frames);
+        b->pair_prog.resize(n_pairs);
+        for (int f = 0; f < n_frames; ++f) {
+            if ((s = build_program(b, {f}, {}, &b->frame_prog[f])) != USLAM_OK) {
+                free_batch(b);
+                return s;
+            }
+            progs.push_back(&b->frame_prog[f]);
+        }
+        for (int p = 0; p < n_pairs; ++p) {
+            if ((s = build_program(b, {}, {p}, &b->pair_prog[p])) != USLAM_OK) {
+                free_batch(b);
+                return s;
+            }
+            progs.push_back(&b->pair_prog[p]);
+        }
+    }
+    size_t tbytes = 0;
+    for (Program* P : progs) tbytes += P->host.size();
+    e = cudaMalloc(&b->d_tables, std::max<size_t>(tbytes, 256));
+    if (e != cudaSuccess) {
+        free_batch(b);
+        cudaGetLastError();
+        return set_err(&ctx->err, USLAM_OOM, "work table allocation refused");
+    }
+    size_t cur = 0;
+    for (Program* P : progs) {
+        char* base = b->d_tables + cur;
+        const size_t t_bytes = round_up(P->ntiles * sizeof(TileItem), 256);
+        const size_t f_bytes = round_up(P->nfsegs * sizeof(SegDev), 256);
+        const size_t m_bytes = round_up(P->nmsegs * sizeof(MatchSegDev), 256);
+        P->tiles = reinterpret_cast<TileItem*>(base);
+        P->fsegs = reinterpret_cast<SegDev*>(base + t_bytes);
+        P->msegs = reinterpret_cast<MatchSegDev*>(base + t_bytes + f_bytes);
+        P->usegs = reinterpret_cast<SegDev*>(base + t_bytes + f_bytes + m_bytes);
+        if (!P->host.empty()) {
+            e = cudaMemcpy(base, P->host.data(), P->host.size(), cudaMemcpyHostToDevice);
+            if (e != cudaSuccess) {
+                free_batch(b);
+                return ctx->cuda_fail(e, "work table upload");
+            }
+        }
+        cur += P->host.size();
+    }
+    if ((s = capture_graph(b, &b->full)) != USLAM_OK) {
+        free_batch(b);
+        return s;
+    }
+    *out = b;
+    return USLAM_OK;
+}
+
+uslam_status check_err_word(uslam_batch* b) {
+    uint32_t word = 0;
+    cudaError_t e = cudaMemcpy(&word, b->d_err, sizeof(word), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return b->ctx->cuda_fail(e, "error word readback");
+    if (word != 0u) {
+        std::string m = "kernel bounds check tripped:";
+        if (word & USLAM_ERR_SMEM_RANGE) m += " blur tap outside the staged tile;";
+        if (word & USLAM_ERR_MATCH_OVERFLOW) m += " match list overflow;";
+        return set_err(b->err(), USLAM_KERNEL_CHECK, m);
+    }
+    return USLAM_OK;
+}
+
+uslam_status sync_stream(uslam_batch* b, int timeout_ms) {
+    cudaError_t e;
+    if (timeout_ms <= 0) {
+        e = cudaStreamSynchronize(b->stream);
+    } else {
+        // host watchdog: poll with a deadline instead of blocking forever
+        const auto deadline = std::chrono::steady_clock::now() + std::chrono::milliseconds(timeout_ms);
+        while ((e = cudaStreamQuery(b->stream)) == cudaErrorNotReady) {
+            if (std::chrono::steady_clock::now() >= deadline)
+                return set_err(b->err(), USLAM_TIMEOUT, "batch did not finish within " + std::to_string(timeout_ms) + " ms");
+            std::this_thread::sleep_for(std::chrono::microseconds(50));
+        }
+    }
+    if (e != cudaSuccess) return b->ctx->cuda_fail(e, "stream synchronize");
+    return check_err_word(b);
+}
+
+uslam_status copy_features(uslam_batch* b, const char* out_base, int frame, uslam_feature* out, int max_out, int* kept,
+                           int* raw) {
+    const FrameDev& F = b->frames[frame];
+    const int L = b->levels;
+    const uint32_t* counts = reinterpret_cast<const uint32_t*>(out_base + b->feat_off[frame]);
+    int total = 0;
+    for (int l = 0; l < L; ++l) {
+        if (kept) kept[l] = static_cast<int>(counts[l]);
+        if (raw) raw[l] = static_cast<int>(counts[L + l]);
+        total += static_cast<int>(counts[l]);
+    }
+    if (!out) return USLAM_OK;
+    if (total > max_out) return set_err(b->err(), USLAM_CAPACITY, "features: output buffer holds " + std::to_string(max_out) + " < " + std::to_string(total));
+    int n = 0;
+    const char* arena_out = reinterpret_cast<const char*>(b->arena + b->in_bytes);
+    for (int l = 0; l < L; ++l) {
+        const size_t off = reinterpret_cast<const char*>(F.feats[l]) - arena_out;
+        std::memcpy(out + n, out_base + off, counts[l] * sizeof(uslam_feature));
+        n += static_cast<int>(counts[l]);
+    }
+    return USLAM_OK;
+}
+
+uslam_status copy_matches(uslam_batch* b, const char* out_base, int pair, uslam_match* out, int max_out, int* n_out) {
+    const PairDev& P = b->pairs[pair];
+    const int L = b->levels;
+    const char* arena_out = reinterpret_cast<const char*>(b->arena + b->in_bytes);
+    const uint32_t* counts = reinterpret_cast<const uint32_t*>(out_base + b->pair_off[pair]);
+    const int32_t* m = reinterpret_cast<const int32_t*>(out_base + (reinterpret_cast<const char*>(P.matches) - arena_out));
+    int total = 0;
+    for (int l = 0; l < L; ++l) total += static_cast<int>(std::min<uint32_t>(counts[l], P.max_matches_per_level));
+    if (n_out) *n_out = total;
+    if (!out) return USLAM_OK;
+    if (total > max_out) return set_err(b->err(), USLAM_CAPACITY, "matches: output buffer too small");
+    int n = 0;
+    for (int l = 0; l < L; ++l) {
+        const int c = static_cast<int>(std::min<uint32_t>(counts[l], P.max_matches_per_level));
+        std::memcpy(out + n, m + static_cast<size_t>(l) * P.max_matches_per_level * 4, c * sizeof(uslam_match));
+        n += c;
+    }
+    return USLAM_OK;
+}
+
+}  // namespace
+
+// ====================================================================== ABI
+
+extern "C" {
+
+const char* uslam_status_string(uslam_status s) {
+    switch (s) {
+        case USLAM_OK: return "ok";
+        case USLAM_INVALID_ARG: return "invalid argument";
+        case USLAM_OOM: return "out of memory";
+        case USLAM_TIMEOUT: return "timeout";
+        case USLAM_CUDA_ERROR: return "cuda error";
+        case USLAM_CAPACITY: return "capacity";
+        case USLAM_NOT_READY: return "not ready";
+        case USLAM_KERNEL_CHECK: return "kernel check";
+    }
+    return "unknown";
+}
+
+uslam_status uslam_level_dims(int width, int height, int levels, int* w_out, int* h_out) {
+    if (width <= 0 || height <= 0 || levels <= 0 || levels > USLAM_MAX_LEVELS || !w_out || !h_out)
+        return USLAM_INVALID_ARG;
+    level_dims(width, height, levels, w_out, h_out);
+    return USLAM_OK;
+}
+
+uslam_status uslam_cull_coverage(int W0, int H0, int w, int h, uint32_t* bits_out) {
+    if (W0 <= 0 || H0 <= 0 || w <= 0 || h <= 0 || w > W0 || h > H0 || !bits_out) return USLAM_INVALID_ARG;
+    const std::vector<uint32_t> bits = build_cull_mask(W0, H0, w, h);
+    std::memcpy(bits_out, bits.data(), bits.size() * sizeof(uint32_t));
+    return USLAM_OK;
+}
+
+uslam_status uslam_create(const uslam_params* params, uslam_ctx** out) {
+    if (!params || !out) return USLAM_INVALID_ARG;
+    *out = nullptr;
+    if (params->levels < 1 || params->levels > USLAM_MAX_LEVELS || params->max_width < 1 ||
+        params->max_width > kMaxWidth || params->max_height < 1 || params->max_height > 65535 ||
+        params->cap_per_level < 0 || params->cap_per_level >= (1 << 24) || !params->brief_pattern)
+        return USLAM_INVALID_ARG;
+    auto* c = new uslam_ctx();
+    c->device = params->device;
+    c->levels = params->levels;
+    c->max_w = params->max_width;
+    c->max_h = params->max_height;
+    c->cap_override = params->cap_per_level;
+    cudaError_t e = cudaSetDevice(c->device);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, c->device);
+    if (e == cudaSuccess) e = init_constants();
+    if (e == cudaSuccess) e = cudaMalloc(&c->d_pattern, 1024 * sizeof(int32_t));
+    if (e == cudaSuccess)
+        e = cudaMemcpy(c->d_pattern, params->brief_pattern, 1024 * sizeof(int32_t), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        if (c->d_pattern) cudaFree(c->d_pattern);
+        delete c;
+        return e == cudaErrorMemoryAllocation ? USLAM_OOM : USLAM_CUDA_ERROR;
+    }
+    *out = c;
+    return USLAM_OK;
+}
+
+void uslam_destroy(uslam_ctx* c) {
+    if (!c) return;
+    cudaSetDevice(c->device);
+    for (auto& kv : c->classes)
+        for (auto* p : kv.second.d_mask) cudaFree(p);
+    if (c->d_pattern) cudaFree(c->d_pattern);
+    delete c;
+}
+
+const char* uslam_last_error(const uslam_ctx* c) { return c ? c->err.c_str() : "null context"; }
+
+uslam_status uslam_batch_create(uslam_ctx* ctx, int n_frames, const int* widths, const int* heights, int n_pairs,
+                                const int* pair_prev, const int* pair_curr, uslam_batch** out) {
+    return create_batch(ctx, n_frames, widths, heights, n_pairs, pair_prev, pair_curr, false, out);
+}
+
+void uslam_batch_destroy(uslam_batch* b) {
+    if (!b) return;
+    cudaSetDevice(b->ctx->device);
+    free_batch(b);
+}
+
+uslam_status uslam_batch_input_device(uslam_batch* b, int frame, uint8_t** dev_ptr, int* pitch) {
+    if (!b || frame < 0 || frame >= static_cast<int>(b->frames.size()) || !dev_ptr) return USLAM_INVALID_ARG;
+    *dev_ptr = const_cast<uint8_t*>(b->frames[frame].img);
+    if (pitch) *pitch = b->frames[frame].img_pitch;
+    return USLAM_OK;
+}
+
+uslam_status uslam_batch_input_host(uslam_batch* b, int frame, uint8_t** host_ptr, int* pitch) {
+    if (!b || frame < 0 || frame >= static_cast<int>(b->frames.size()) || !host_ptr) return USLAM_INVALID_ARG;
+    *host_ptr = reinterpret_cast<uint8_t*>(b->h_in + b->in_off[frame]);
+    if (pitch) *pitch = b->frames[frame].img_pitch;
+    return USLAM_OK;
+}
+
+uslam_status uslam_batch_set_frame(uslam_batch* b, int frame, const uint8_t* img, int pitch) {
+    if (!b || frame < 0 || frame >= static_cast<int>(b->frames.size()) || !img) return USLAM_INVALID_ARG;
+    const FrameDev& F = b->frames[frame];
+    if (pitch < F.W0) return set_err(b->err(), USLAM_INVALID_ARG, "set_frame: pitch smaller than the frame width");
+    char* dst = b->h_in + b->in_off[frame];
+    for (int y = 0; y < F.H0; ++y) std::memcpy(dst + static_cast<size_t>(y) * F.img_pitch, img + static_cast<size_t>(y) * pitch, F.W0);
+    return USLAM_OK;
+}
+
+uslam_status uslam_batch_upload(uslam_batch* b) {
+    if (!b) return USLAM_INVALID_ARG;
+    cudaError_t e = cudaMemcpyAsync(b->arena, b->h_in, b->in_bytes, cudaMemcpyHostToDevice, b->stream);
+    if (e != cudaSuccess) return b->ctx->cuda_fail(e, "batch upload");
+    return USLAM_OK;
+}
+
+uslam_status uslam_batch_run(uslam_batch* b) {
+    if (!b) return USLAM_INVALID_ARG;
+    cudaError_t e = cudaGraphLaunch(b->full.graph, b->stream);
+    if (e != cudaSuccess) return b->ctx->cuda_fail(e, "graph launch");
+    return USLAM_OK;
+}
+
+uslam_status uslam_batch_download(uslam_batch* b) {
+    if (!b) return USLAM_INVALID_ARG;
+    cudaError_t e = cudaMemcpyAsync(b->h_out, b->arena + b->in_bytes, b->out_bytes, cudaMemcpyDeviceToHost, b->stream);
+    if (e != cudaSuccess) return b->ctx->cuda_fail(e, "batch download");
+    return USLAM_OK;
+}
+
+uslam_status uslam_batch_sync(uslam_batch* b, int timeout_ms) {
+    if (!b) return USLAM_INVALID_ARG;
+    return sync_stream(b, timeout_ms);
+}
+
+uslam_status uslam_batch_features(uslam_batch* b, int frame, uslam_feature* out, int max_out, int* kept, int* raw) {
+    if (!b || frame < 0 || frame >= static_cast<int>(b->frames.size())) return USLAM_INVALID_ARG;
+    return copy_features(b, b->h_out, frame, out, max_out, kept, raw);
+}
+
+uslam_status uslam_batch_matches(uslam_batch* b, int pair, uslam_match* out, int max_out, int* n_out) {
+    if (!b || pair < 0 || pair >= static_cast<int>(b->pairs.size())) return USLAM_INVALID_ARG;
+    return copy_matches(b, b->h_out, pair, out, max_out, n_out);
+}
+
+uslam_status uslam_batch_pyramid_level(uslam_batch* b, int frame, int level, float* out) {
+    if (!b || !out || frame < 0 || frame >= static_cast<int>(b->frames.size()) || level < 1 || level >= b->levels)
+        return USLAM_INVALID_ARG;
+    const FrameDev& F = b->frames[frame];
+    cudaError_t e = cudaMemcpy(out, F.lvl[level], sizeof(float) * F.w[level] * F.h[level], cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return b->ctx->cuda_fail(e, "pyramid readback");
+    return USLAM_OK;
+}
+
+uslam_status uslam_batch_blur_level(uslam_batch* b, int frame, int level, float* out) {
+    if (!b || !out || frame < 0 || frame >= static_cast<int>(b->frames.size()) || level < 0 || level >= b->levels)
+        return USLAM_INVALID_ARG;
+    const FrameDev& F = b->frames[frame];
+    cudaError_t e = cudaMemcpy(out, F.blur[level], sizeof(float) * F.w[level] * F.h[level], cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return b->ctx->cuda_fail(e, "blur readback");
+    return USLAM_OK;
+}
+
+uslam_status uslam_batch_keypoint_map(uslam_batch* b, int frame, int level, uint8_t* out) {
+    if (!b || !out || frame < 0 || frame >= static_cast<int>(b->frames.size()) || level < 0 || level >= b->levels)
+        return USLAM_INVALID_ARG;
+    const FrameDev& F = b->frames[frame];
+    cudaError_t e = cudaMemcpy2D(out, F.w[level], F.kpmap[level], F.kp_pitch[level], F.w[level], F.h[level],
+                                 cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return b->ctx->cuda_fail(e, "keypoint map readback");
+    return USLAM_OK;
+}
+
+uslam_status uslam_batch_set_stream(uslam_batch* b, void* cuda_stream) {
+    if (!b) return USLAM_INVALID_ARG;
+    b->stream = cuda_stream ? static_cast<cudaStream_t>(cuda_stream) : b->own_stream;
+    return USLAM_OK;
+}
+
+uslam_status uslam_batch_profile(uslam_batch* b, int iters, float* kernel_ms) {
+    if (!b || iters <= 0 || !kernel_ms) return USLAM_INVALID_ARG;
+    uslam_ctx* c = b->ctx;
+    const Program& P = b->full;
+    cudaEvent_t ev[6];
+    for (auto& x : ev) x = nullptr;
+    cudaError_t e = cudaSuccess;
+    for (int i = 0; i < 6 && e == cudaSuccess; ++i) e = cudaEventCreate(&ev[i]);
+    double acc[5] = {0, 0, 0, 0, 0};
+    const int grid = c->num_sms * 4;
+    for (int it = 0; it < iters && e == cudaSuccess; ++it) {
+        e = cudaEventRecord(ev[0], b->stream);
+        if (e == cudaSuccess) e = launch_detect(b->d_frames, P.tiles, P.ntiles, b->d_err, b->stream);
+        if (e == cudaSuccess) e = cudaEventRecord(ev[1], b->stream);
+        if (e == cudaSuccess) e = launch_compact(b->d_frames, P.fsegs, P.nfsegs, b->max_w, b->stream);
+        if (e == cudaSuccess) e = cudaEventRecord(ev[2], b->stream);
+        if (e == cudaSuccess) e = launch_describe(b->d_frames, P.fsegs, P.nfsegs, c->d_pattern, grid, b->stream);
+        if (e == cudaSuccess) e = cudaEventRecord(ev[3], b->stream);
+        if (e == cudaSuccess) e = launch_match(b->d_frames, b->d_pairs, P.msegs, P.nmsegs, grid, b->stream);
+        if (e == cudaSuccess) e = cudaEventRecord(ev[4], b->stream);
+        if (e == cudaSuccess) e = launch_mutual(b->d_frames, b->d_pairs, P.usegs, P.nusegs, b->d_err, b->stream);
+        if (e == cudaSuccess) e = cudaEventRecord(ev[5], b->stream);
+        if (e == cudaSuccess) e = cudaEventSynchronize(ev[5]);
+        for (int k = 0; k < 5 && e == cudaSuccess; ++k) {
+            float ms = 0.0f;
+            e = cudaEventElapsedTime(&ms, ev[k], ev[k + 1]);
+            acc[k] += ms;
+        }
+    }
+    for (auto& x : ev)
+        if (x) cudaEventDestroy(x);
+    if (e != cudaSuccess) return c->cuda_fail(e, "profile");
+    for (int k = 0; k < 5; ++k) kernel_ms[k] = static_cast<float>(acc[k] / iters);
+    return check_err_word(b);
+}
+
+uslam_status uslam_batch_io_bytes(uslam_batch* b, size_t* h2d, size_t* d2h) {
+    if (!b) return USLAM_INVALID_ARG;
+    if (h2d) *h2d = b->in_bytes;
+    if (d2h) *d2h = b->out_bytes;
+    return USLAM_OK;
+}
+
+}  // extern "C"
+
+// ================================================================= frontend
+
+struct uslam_frontend {
+    uslam_batch* b = nullptr;
+    uint8_t* incoming = nullptr;  // device buffer for caller-written frames
+    int cur = -1;                 // slot holding FeatureSet(0)
+    int ref = -1;                 // slot holding FeatureSet(1)
+    bool matched = false;
+};
+
+namespace {
+
+// Choose the slot of the next frame and enqueue its copy and work.
+// src_host != NULL: H2D from caller memory; else src_dev != NULL: D2D from
+// caller device memory; else D2D from `incoming`.
+uslam_status frontend_enqueue(uslam_frontend* fe, const uint8_t* src_host, const uint8_t* src_dev, int pitch,
+                              int advance_reference, int* matched) {
+    uslam_batch* b = fe->b;
+    const FrameDev& F0 = b->frames[0];
+    // LoadDataCPUPass::shiftFeatureSets (load_features_cpu.cpp:111-142): the
+    // current set becomes the reference when asked or when none exists yet;
+    // otherwise the reference is kept and the current set is replaced.
+    int slot;
+    if (fe->cur < 0) {
+        slot = 0;
+    } else {
+        if (fe->ref < 0 || advance_reference) fe->ref = fe->cur;
+        slot = 1 - fe->ref;
+    }
+    uint8_t* dst = const_cast<uint8_t*>(b->frames[slot].img);
+    cudaError_t e;
+    if (src_host) {
+        if (pitch < F0.W0) return set_err(b->err(), USLAM_INVALID_ARG, "process: pitch smaller than the frame width");
+        e = cudaMemcpy2DAsync(dst, F0.img_pitch, src_host, pitch, F0.W0, F0.H0, cudaMemcpyHostToDevice, b->stream);
+    } else if (src_dev) {
+        if (pitch < F0.W0) return set_err(b->err(), USLAM_INVALID_ARG, "enqueue: pitch smaller than the frame width");
+        e = cudaMemcpy2DAsync(dst, F0.img_pitch, src_dev, pitch, F0.W0, F0.H0, cudaMemcpyDeviceToDevice, b->stream);
+    } else {
+        e = cudaMemcpyAsync(dst, fe->incoming, static_cast<size_t>(F0.H0) * F0.img_pitch, cudaMemcpyDeviceToDevice,
+                            b->stream);
+    }
+    if (e == cudaSuccess) e = cudaMemsetAsync(b->d_err, 0, sizeof(uint32_t), b->stream);
+    if (e == cudaSuccess) e = enqueue_program(b, b->frame_prog[slot]);
+    fe->cur = slot;
+    fe->matched = false;
+    if (e == cudaSuccess && fe->ref >= 0) {
+        const int pair = slot == 0 ? 0 : 1;  // pair 0 = slot1 -> slot0, pair 1 = slot0 -> slot1
+        e = enqueue_program(b, b->pair_prog[pair]);
+        fe->matched = true;
+    }
+    if (e != cudaSuccess) return b->ctx->cuda_fail(e, "frontend launch");
+    if (matched) *matched = fe->matched ? 1 : 0;
+    return USLAM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+uslam_status uslam_frontend_create(uslam_ctx* ctx, int width, int height, uslam_frontend** out) {
+    if (!ctx || !out) return USLAM_INVALID_ARG;
+    const int ws[2] = {width, width}, hs[2] = {height, height};
+    const int prev[2] = {1, 0}, curr[2] = {0, 1};  // pair 0: slot1 -> slot0, pair 1: slot0 -> slot1
+    uslam_batch* b = nullptr;
+    uslam_status s = create_batch(ctx, 2, ws, hs, 2, prev, curr, true, &b);
+    if (s != USLAM_OK) return s;
+    auto* fe = new uslam_frontend();
+    fe->b = b;
+    cudaError_t e = cudaMalloc(&fe->incoming, static_cast<size_t>(b->frames[0].H0) * b->frames[0].img_pitch);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        uslam_batch_destroy(b);
+        delete fe;
+        return set_err(&ctx->err, USLAM_OOM, "frontend input buffer allocation refused");
+    }
+    *out = fe;
+    return USLAM_OK;
+}
+
+void uslam_frontend_destroy(uslam_frontend* fe) {
+    if (!fe) return;
+    cudaSetDevice(fe->b->ctx->device);
+    if (fe->incoming) cudaFree(fe->incoming);
+    uslam_batch_destroy(fe->b);
+    delete fe;
+}
+
+uslam_status uslam_frontend_input_device(uslam_frontend* fe, uint8_t** dev_ptr, int* pitch) {
+    if (!fe || !dev_ptr) return USLAM_INVALID_ARG;
+    *dev_ptr = fe->incoming;
+    if (pitch) *pitch = fe->b->frames[0].img_pitch;
+    return USLAM_OK;
+}
+
+uslam_status uslam_frontend_enqueue(uslam_frontend* fe, const uint8_t* dev_img, int pitch, int advance_reference,
+                                    int* matched) {
+    if (!fe) return USLAM_INVALID_ARG;
+    return frontend_enqueue(fe, nullptr, dev_img, pitch, advance_reference, matched);
+}
+
+uslam_status uslam_frontend_sync(uslam_frontend* fe) {
+    if (!fe) return USLAM_INVALID_ARG;
+    return sync_stream(fe->b, 0);
+}
+
+uslam_status uslam_frontend_process(uslam_frontend* fe, const uint8_t* img, int pitch, int advance_reference) {
+    if (!fe) return USLAM_INVALID_ARG;
+    int matched = 0;
+    uslam_status s = frontend_enqueue(fe, img, nullptr, pitch, advance_reference, &matched);
+    if (s != USLAM_OK) return s;
+    s = sync_stream(fe->b, 0);
+    if (s != USLAM_OK) return s;
+    return matched ? USLAM_OK : USLAM_NOT_READY;
+}
+
+uslam_status uslam_frontend_features(uslam_frontend* fe, int which, uslam_feature* out, int max_out, int* kept,
+                                     int* raw) {
+    if (!fe || (which != 0 && which != 1)) return USLAM_INVALID_ARG;
+    const int slot = which == 0 ? fe->cur : fe->ref;
+    if (slot < 0) return set_err(fe->b->err(), USLAM_NOT_READY, "features: that feature set does not exist yet");
+    uslam_batch* b = fe->b;
+    cudaError_t e = cudaMemcpy(b->h_out, b->arena + b->in_bytes, b->out_bytes, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return b->ctx->cuda_fail(e, "features readback");
+    return copy_features(b, b->h_out, slot, out, max_out, kept, raw);
+}
+
+uslam_status uslam_frontend_matches(uslam_frontend* fe, uslam_match* out, int max_out, int* n_out) {
+    if (!fe) return USLAM_INVALID_ARG;
+    if (!fe->matched) return set_err(fe->b->err(), USLAM_NOT_READY, "matches: no reference feature set yet");
+    uslam_batch* b = fe->b;
+    cudaError_t e = cudaMemcpy(b->h_out, b->arena + b->in_bytes, b->out_bytes, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return b->ctx->cuda_fail(e, "matches readback");
+    const int pair = fe->cur == 0 ? 0 : 1;
+    return copy_matches(b, b->h_out, pair, out, max_out, n_out);
+}
+
+}  // extern "C"

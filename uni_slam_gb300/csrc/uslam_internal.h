@@ -1,0 +1,69 @@
+// uslam_internal.h — device-side data layout shared by the kernels and the
+// host runtime of the GB300 feature front-end.
+//
+// HBM layout of one frame slot (all sub-buffers 256-byte aligned, carved out
+// of one arena allocation per batch):
+//   img      u8   [H0][img_pitch]          LOD0 input (the H2D boundary)
+//   lvl[l]   f32  [h_l][w_l]   (l >= 1)    pyramid level l (parity output)
+//   blur[l]  f32  [h_l][w_l]               9-tap blurred sample G(x, y) of level l
+//   kpmap[l] u8   [h_l][kp_pitch_l]        culled FAST strength (0 = no keypoint)
+//   feats[l] Feature[cap]                  gpumodels::Feature records, (y, x) order
+//   xorder[l] u32 [cap]                    feature indices sorted by x (matching)
+//   colstart[l] u32 [w_l + 1]              first xorder slot of each column
+//   counts   u32  [2][levels]              kept (<= cap) and raw keypoint counts
+#pragma once
+
+#include <stdint.h>
+
+#define USLAM_MAX_LEVELS 12
+
+// Device copy of one frame's geometry and buffer addresses.
+struct FrameDev {
+    const uint8_t* img;
+    int W0, H0, img_pitch, levels, cap;
+    int w[USLAM_MAX_LEVELS];
+    int h[USLAM_MAX_LEVELS];
+    int kp_pitch[USLAM_MAX_LEVELS];
+    float* lvl[USLAM_MAX_LEVELS];
+    float* blur[USLAM_MAX_LEVELS];
+    uint8_t* kpmap[USLAM_MAX_LEVELS];
+    const uint32_t* mask[USLAM_MAX_LEVELS];  // combined cull coverage bitmap
+    uint32_t* feats[USLAM_MAX_LEVELS];       // 12 u32 (48 B) per feature
+    uint32_t* xorder[USLAM_MAX_LEVELS];
+    uint32_t* colstart[USLAM_MAX_LEVELS];
+    uint32_t* kept;  // [levels]
+    uint32_t* raw;   // [levels]
+};
+
+// One frame pair to match: prev = reference set (a), curr = current set (b).
+struct PairDev {
+    int prev, curr;         // frame indices in the batch
+    int32_t* a2b;           // [levels * cap_prev]: prev feature -> packed curr feature or -1
+    int32_t* b2a;           // [levels * cap_curr]
+    int32_t* matches;       // 4 ints per match (lod_a, idx_a, lod_b, idx_b)
+    uint32_t* match_count;  // [levels] matches whose a lies in that level
+    int max_matches_per_level;
+    float max_dx, max_dy;   // 0.1f * W0, 0.1f * H0 of the frame size
+};
+
+// K1 work item: one TW x TH tile of one level of one frame.
+struct TileItem {
+    uint16_t frame;
+    uint8_t level;
+    uint8_t pad;
+    uint16_t tx, ty;
+};
+
+// Segment tables for the persistent describe / match kernels.
+struct SegDev {
+    int frame;
+    int level;
+};
+
+#define USLAM_ERR_SMEM_RANGE 1u
+#define USLAM_ERR_MATCH_OVERFLOW 2u
+
+// Packed match-partner encoding: level in the top 8 bits, index in the low 24.
+#define USLAM_PACK(l, i) (((int32_t)(l) << 24) | (int32_t)(i))
+#define USLAM_PACK_LEVEL(p) ((int)((uint32_t)(p) >> 24))
+#define USLAM_PACK_INDEX(p) ((int)((uint32_t)(p) & 0xffffffu))

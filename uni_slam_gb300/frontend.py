@@ -1,0 +1,236 @@
+"""Python handles over the C ABI: Context, Batch (work-table form) and
+Frontend (the reference's per-frame pass sequence with FeatureSet rotation).
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import capi
+from .capi import FEATURE_DTYPE, MATCH_DTYPE, USlamError, iptr, ptr
+
+
+KERNELS = ("k_detect", "k_compact", "k_describe", "k_match", "k_mutual")
+
+
+def level_dims(width: int, height: int, levels: int = 6) -> list[tuple[int, int]]:
+    lib = capi.load()
+    w = np.zeros(levels, np.int32)
+    h = np.zeros(levels, np.int32)
+    st = lib.uslam_level_dims(width, height, levels, iptr(w), iptr(h))
+    if st != capi.OK:
+        raise USlamError(st, "level_dims")
+    return [(int(a), int(b)) for a, b in zip(w, h)]
+
+
+class Context:
+    """Device context: BRIEF table, level count, cap, size limits."""
+
+    def __init__(self, pattern: np.ndarray, levels: int = 6, max_width: int = 4096, max_height: int = 4096,
+                 cap_per_level: int = 0, device: int = 0):
+        self.lib = capi.load()
+        self._pattern = np.ascontiguousarray(pattern, dtype=np.int32).reshape(-1)
+        if self._pattern.size != 1024:
+            raise ValueError("pattern must hold 256 x (ax, ay, bx, by)")
+        p = capi.Params(device, levels, max_width, max_height, cap_per_level,
+                        self._pattern.ctypes.data_as(C.POINTER(C.c_int32)))
+        h = C.c_void_p()
+        st = self.lib.uslam_create(C.byref(p), C.byref(h))
+        if st != capi.OK:
+            raise USlamError(st, "uslam_create failed")
+        self.h = h
+        self.levels = levels
+
+    def error(self) -> str:
+        return self.lib.uslam_last_error(self.h).decode()
+
+    def check(self, st: int, what: str, ok=(capi.OK,)):
+        if st not in ok:
+            raise USlamError(st, f"{what}: {self.error()}")
+        return st
+
+    def close(self):
+        if self.h:
+            self.lib.uslam_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+
+class Batch:
+    """Work table over frames of any sizes plus frame pairs to match."""
+
+    def __init__(self, ctx: Context, sizes: list[tuple[int, int]], pairs: list[tuple[int, int]] = ()):
+        self.ctx = ctx
+        self.lib = ctx.lib
+        self.sizes = list(sizes)
+        self.pairs = list(pairs)
+        w = np.array([s[0] for s in sizes], np.int32)
+        h = np.array([s[1] for s in sizes], np.int32)
+        pp = np.array([p[0] for p in pairs] or [0], np.int32)
+        pc = np.array([p[1] for p in pairs] or [0], np.int32)
+        hb = C.c_void_p()
+        ctx.check(self.lib.uslam_batch_create(ctx.h, len(sizes), iptr(w), iptr(h), len(self.pairs), iptr(pp),
+                                              iptr(pc), C.byref(hb)), "batch_create")
+        self.h = hb
+        self.caps = []
+
+    def set_frame(self, i: int, img: np.ndarray):
+        img = np.ascontiguousarray(img, dtype=np.uint8)
+        self.ctx.check(self.lib.uslam_batch_set_frame(self.h, i, ptr(img), img.shape[1]), "set_frame")
+
+    def input_device(self, i: int) -> tuple[int, int]:
+        p = C.POINTER(C.c_uint8)()
+        pitch = C.c_int()
+        self.ctx.check(self.lib.uslam_batch_input_device(self.h, i, C.byref(p), C.byref(pitch)), "input_device")
+        return C.cast(p, C.c_void_p).value, pitch.value
+
+    def input_host(self, i: int) -> np.ndarray:
+        """Pinned staging view (H0 x pitch) of frame i's input."""
+        p = C.POINTER(C.c_uint8)()
+        pitch = C.c_int()
+        self.ctx.check(self.lib.uslam_batch_input_host(self.h, i, C.byref(p), C.byref(pitch)), "input_host")
+        h0 = self.sizes[i][1]
+        return np.ctypeslib.as_array(p, shape=(h0 * pitch.value,)).reshape(h0, pitch.value)
+
+    def upload(self):
+        self.ctx.check(self.lib.uslam_batch_upload(self.h), "upload")
+
+    def run(self):
+        self.ctx.check(self.lib.uslam_batch_run(self.h), "run")
+
+    def download(self):
+        self.ctx.check(self.lib.uslam_batch_download(self.h), "download")
+
+    def sync(self, timeout_ms: int = 0):
+        self.ctx.check(self.lib.uslam_batch_sync(self.h, timeout_ms), "sync")
+
+    def process(self, frames: list[np.ndarray]):
+        for i, f in enumerate(frames):
+            self.set_frame(i, f)
+        self.upload()
+        self.run()
+        self.download()
+        self.sync()
+
+    def features(self, i: int):
+        L = self.ctx.levels
+        kept = np.zeros(L, np.int32)
+        raw = np.zeros(L, np.int32)
+        self.ctx.check(self.lib.uslam_batch_features(self.h, i, None, 0, iptr(kept), iptr(raw)), "features")
+        out = np.zeros(int(kept.sum()), FEATURE_DTYPE)
+        self.ctx.check(self.lib.uslam_batch_features(self.h, i, ptr(out), out.size, iptr(kept), iptr(raw)),
+                       "features")
+        return out, kept, raw
+
+    def matches(self, p: int) -> np.ndarray:
+        n = C.c_int()
+        self.ctx.check(self.lib.uslam_batch_matches(self.h, p, None, 0, C.byref(n)), "matches")
+        out = np.zeros(n.value, MATCH_DTYPE)
+        self.ctx.check(self.lib.uslam_batch_matches(self.h, p, ptr(out), out.size, C.byref(n)), "matches")
+        return out
+
+    def _dims(self, i: int, level: int):
+        return level_dims(self.sizes[i][0], self.sizes[i][1], self.ctx.levels)[level]
+
+    def pyramid_level(self, i: int, level: int) -> np.ndarray:
+        w, h = self._dims(i, level)
+        out = np.zeros((h, w), np.float32)
+        self.ctx.check(self.lib.uslam_batch_pyramid_level(self.h, i, level, ptr(out)), "pyramid_level")
+        return out
+
+    def blur_level(self, i: int, level: int) -> np.ndarray:
+        w, h = self._dims(i, level)
+        out = np.zeros((h, w), np.float32)
+        self.ctx.check(self.lib.uslam_batch_blur_level(self.h, i, level, ptr(out)), "blur_level")
+        return out
+
+    def keypoint_map(self, i: int, level: int) -> np.ndarray:
+        w, h = self._dims(i, level)
+        out = np.zeros((h, w), np.uint8)
+        self.ctx.check(self.lib.uslam_batch_keypoint_map(self.h, i, level, ptr(out)), "keypoint_map")
+        return out
+
+    def set_stream(self, cuda_stream: int | None):
+        self.ctx.check(self.lib.uslam_batch_set_stream(self.h, C.c_void_p(cuda_stream or 0)), "set_stream")
+
+    def profile(self, iters: int = 5) -> dict[str, float]:
+        ms = np.zeros(5, np.float32)
+        self.ctx.check(self.lib.uslam_batch_profile(self.h, iters, ptr(ms)), "profile")
+        return dict(zip(KERNELS, (float(v) for v in ms)))
+
+    def io_bytes(self) -> tuple[int, int]:
+        a = C.c_size_t()
+        b = C.c_size_t()
+        self.ctx.check(self.lib.uslam_batch_io_bytes(self.h, C.byref(a), C.byref(b)), "io_bytes")
+        return a.value, b.value
+
+    def close(self):
+        if self.h:
+            self.lib.uslam_batch_destroy(self.h)
+            self.h = None
+
+
+class Frontend:
+    """One camera stream: FeatureSet(0)/(1) on the device, matched per frame."""
+
+    def __init__(self, ctx: Context, width: int, height: int):
+        self.ctx = ctx
+        self.lib = ctx.lib
+        self.width, self.height = width, height
+        h = C.c_void_p()
+        ctx.check(self.lib.uslam_frontend_create(ctx.h, width, height, C.byref(h)), "frontend_create")
+        self.h = h
+
+    def process(self, img: np.ndarray | None, advance_reference: bool = False) -> bool:
+        """Returns True when the frame was matched against a reference set."""
+        if img is None:
+            st = self.lib.uslam_frontend_process(self.h, None, 0, int(advance_reference))
+        else:
+            img = np.ascontiguousarray(img, dtype=np.uint8)
+            st = self.lib.uslam_frontend_process(self.h, ptr(img), img.shape[1], int(advance_reference))
+        self.ctx.check(st, "frontend_process", ok=(capi.OK, capi.NOT_READY))
+        return st == capi.OK
+
+    def input_device(self) -> tuple[int, int]:
+        p = C.POINTER(C.c_uint8)()
+        pitch = C.c_int()
+        self.ctx.check(self.lib.uslam_frontend_input_device(self.h, C.byref(p), C.byref(pitch)), "input_device")
+        return C.cast(p, C.c_void_p).value, pitch.value
+
+    def enqueue(self, dev_ptr: int | None = None, pitch: int = 0, advance_reference: bool = False) -> bool:
+        """Enqueue a frame already in device memory (None: the input buffer)."""
+        m = C.c_int()
+        self.ctx.check(self.lib.uslam_frontend_enqueue(self.h, C.c_void_p(dev_ptr or 0), pitch,
+                                                       int(advance_reference), C.byref(m)), "enqueue")
+        return bool(m.value)
+
+    def sync(self):
+        self.ctx.check(self.lib.uslam_frontend_sync(self.h), "frontend_sync")
+
+    def features(self, which: int = 0):
+        L = self.ctx.levels
+        kept = np.zeros(L, np.int32)
+        raw = np.zeros(L, np.int32)
+        self.ctx.check(self.lib.uslam_frontend_features(self.h, which, None, 0, iptr(kept), iptr(raw)), "features")
+        out = np.zeros(int(kept.sum()), FEATURE_DTYPE)
+        self.ctx.check(self.lib.uslam_frontend_features(self.h, which, ptr(out), out.size, iptr(kept), iptr(raw)),
+                       "features")
+        return out, kept, raw
+
+    def matches(self) -> np.ndarray:
+        n = C.c_int()
+        self.ctx.check(self.lib.uslam_frontend_matches(self.h, None, 0, C.byref(n)), "matches")
+        out = np.zeros(n.value, MATCH_DTYPE)
+        self.ctx.check(self.lib.uslam_frontend_matches(self.h, ptr(out), out.size, C.byref(n)), "matches")
+        return out
+
+    def close(self):
+        if self.h:
+            self.lib.uslam_frontend_destroy(self.h)
+            self.h = None
