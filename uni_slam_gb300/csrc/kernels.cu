@@ -3,7 +3,7 @@
 //   k_detect   (K1) pyramid level tile + FAST response + cull + blur cache
 //   k_compact       per (frame, level): ordered keypoint compaction, cap, x-sort
 //   k_describe (K2) orientation + 256-bit rotated BRIEF, one warp per keypoint
-//   k_match    (K3) windowed top-2 Hamming search, one warp per query
+//   k_match    (K3) windowed top-2 Hamming search, 32 x-adjacent queries per warp
 //   k_mutual        mutual cross-check and ordered match output
 //
 // Arithmetic contract: binary32, round-to-nearest-even, no FMA contraction
@@ -110,32 +110,114 @@ __device__ __forceinline__ bool mask_bit(const uint32_t* mask, int p) {
 }
 
 // ---------------------------------------------------------------- K1 ----
+// One TW x TH tile of one level: stage the level pixels (+ halo) in shared
+// memory, then per pixel the FAST response, the cull decision, the level
+// value and the blur-cache value G(x, y).  Sampling coordinates depend only
+// on the row or only on the column, so they are computed once per tile row /
+// column (same operations as the per-pixel formula, hence the same bits).
 __global__ void __launch_bounds__(K1_THREADS)
 k_detect(const FrameDev* __restrict__ frames, const TileItem* __restrict__ tiles, uint32_t* err) {
     __shared__ float sm[SH][SW];
+    __shared__ float s_lut[256];                 // f32(u8) / 255
+    __shared__ int s_fx0[SW], s_fx1[SW];         // LOD0 source columns per staged column
+    __shared__ float s_fa[SW];
+    __shared__ int s_fy0[SH], s_fy1[SH];         // LOD0 source rows per staged row
+    __shared__ float s_fb[SH];
+    __shared__ int s_by0[3][TH], s_by1[3][TH];   // blur taps: staged rows per output row
+    __shared__ float s_bb[3][TH];
     const TileItem it = tiles[blockIdx.x];
     const FrameDev& F = frames[it.frame];
     const int l = it.level;
     const int w = F.w[l], h = F.h[l];
     const int X0 = it.tx * TW, Y0 = it.ty * TH;
+    const int t = threadIdx.x;
+    const float tex_x = 1.0f / (float)w;
+    const float tex_y = 1.0f / (float)h;
+    const float off[3] = {-1.2f, 0.0f, 1.2f};
+    const uint8_t* img = F.img;
+    const int pitch = F.img_pitch;
 
-    // 1. level tile + halo; halo cells follow the Tint clamp (far edge for < 0)
-    for (int idx = threadIdx.x; idx < SH * SW; idx += K1_THREADS) {
-        const int r = idx / SW, c = idx - r * SW;
+    // 0. per-tile tables
+    s_lut[t] = (float)t / 255.0f;
+    if (l > 0 && t < SW) {
+        // create_pyramid.wgsl:11-12 + canonical bilinear, x part
+        const int gx = tint_clamp(X0 - HX + t, w);
+        const float u = (((float)gx + 0.5f) / (float)w) * (float)F.W0 - 0.5f;
+        const float fi = floorf(u);
+        s_fa[t] = u - fi;
+        s_fx0[t] = edge_index(fi, F.W0);
+        s_fx1[t] = edge_index(fi + 1.0f, F.W0);
+    } else if (l > 0 && t >= 96 && t < 96 + SH) {
+        const int r = t - 96;
         const int gy = tint_clamp(Y0 - HY + r, h);
-        const int gx = tint_clamp(X0 - HX + c, w);
-        sm[r][c] = pyramid_pixel(F, l, gx, gy);
+        const float v = (((float)gy + 0.5f) / (float)h) * (float)F.H0 - 0.5f;
+        const float fj = floorf(v);
+        s_fb[r] = v - fj;
+        s_fy0[r] = edge_index(fj, F.H0);
+        s_fy1[r] = edge_index(fj + 1.0f, F.H0);
+    } else if (t >= 160 && t < 160 + 3 * TH) {
+        // generate_features.wgsl:153-169, y part of the 9 taps
+        const int ty = (t - 160) / 3, k = (t - 160) % 3;
+        const float uvy = ((float)(Y0 + ty) + 0.5f) * tex_y;
+        const float offk = k == 0 ? -1.2f : (k == 1 ? 0.0f : 1.2f);
+        const float v = (uvy + offk * tex_y) * (float)h - 0.5f;
+        const float fj = floorf(v);
+        int r0 = edge_index(fj, h) - (Y0 - HY), r1 = edge_index(fj + 1.0f, h) - (Y0 - HY);
+        if (Y0 + ty < h && (r0 < 0 || r1 >= SH)) atomicOr(err, USLAM_ERR_SMEM_RANGE);
+        s_bb[k][ty] = v - fj;
+        s_by0[k][ty] = min(max(r0, 0), SH - 1);
+        s_by1[k][ty] = min(max(r1, 0), SH - 1);
     }
     __syncthreads();
 
-    const float tex_x = 1.0f / (float)w;
-    const float tex_y = 1.0f / (float)h;
-    const int tx = threadIdx.x % TW;
+    // 1. level tile + halo; halo cells follow the Tint clamp (far edge for < 0)
+    for (int idx = t; idx < SH * SW; idx += K1_THREADS) {
+        const int r = idx / SW, c = idx - r * SW;
+        float val;
+        if (l == 0) {
+            const int gy = tint_clamp(Y0 - HY + r, h);
+            const int gx = tint_clamp(X0 - HX + c, w);
+            val = s_lut[__ldg(img + (size_t)gy * pitch + gx)];
+        } else {
+            const float a = s_fa[c], b = s_fb[r];
+            const uint8_t* r0 = img + (size_t)s_fy0[r] * pitch;
+            const uint8_t* r1 = img + (size_t)s_fy1[r] * pitch;
+            const float t00 = s_lut[__ldg(r0 + s_fx0[c])], t10 = s_lut[__ldg(r0 + s_fx1[c])];
+            const float t01 = s_lut[__ldg(r1 + s_fx0[c])], t11 = s_lut[__ldg(r1 + s_fx1[c])];
+            const float na = 1.0f - a, nb = 1.0f - b;
+            val = (na * nb) * t00;
+            val = val + (a * nb) * t10;
+            val = val + (na * b) * t01;
+            val = val + (a * b) * t11;
+        }
+        sm[r][c] = val;
+    }
+    __syncthreads();
+
+    const int tx = t % TW;
     const int x = X0 + tx;
+    if (x >= w) return;
+    // blur taps, x part (this thread's column is fixed)
+    int ix0[3], ix1[3];
+    float ax[3];
+    {
+        const float uvx = ((float)x + 0.5f) * tex_x;
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const float u = (uvx + off[k] * tex_x) * (float)w - 0.5f;
+            const float fi = floorf(u);
+            ax[k] = u - fi;
+            int c0 = edge_index(fi, w) - (X0 - HX), c1 = edge_index(fi + 1.0f, w) - (X0 - HX);
+            if (c0 < 0 || c1 >= SW) atomicOr(err, USLAM_ERR_SMEM_RANGE);
+            ix0[k] = min(max(c0, 0), SW - 1);
+            ix1[k] = min(max(c1, 0), SW - 1);
+        }
+    }
     const uint32_t* mask = F.mask[l];
-    for (int ty = threadIdx.x / TW; ty < TH; ty += K1_THREADS / TW) {
+    const float wt[3] = {0.3125f, 0.375f, 0.3125f};
+    for (int ty = t / TW; ty < TH; ty += K1_THREADS / TW) {
         const int y = Y0 + ty;
-        if (x >= w || y >= h) continue;
+        if (y >= h) break;
         const int r = ty + HY, c = tx + HX;
         const size_t p = (size_t)y * (size_t)w + (size_t)x;
 
@@ -158,44 +240,24 @@ k_detect(const FrameDev* __restrict__ frames, const TileItem* __restrict__ tiles
         F.kpmap[l][(size_t)y * F.kp_pitch[l] + x] = (uint8_t)keep;
         if (l > 0) F.lvl[l][p] = sm[r][c];
 
-        // 3. blur cache: G(x, y) of generate_features.wgsl:149-172 for this pixel
-        const float uvx = ((float)x + 0.5f) * tex_x;
-        const float uvy = ((float)y + 0.5f) * tex_y;
-        int ix0[3], ix1[3], iy0[3], iy1[3];
-        float ax[3], by[3];
-        const float off[3] = {-1.2f, 0.0f, 1.2f};
-        bool ok = true;
-#pragma unroll
-        for (int k = 0; k < 3; ++k) {
-            const float u = (uvx + off[k] * tex_x) * (float)w - 0.5f;
-            const float v = (uvy + off[k] * tex_y) * (float)h - 0.5f;
-            const float fi = floorf(u), fj = floorf(v);
-            ax[k] = u - fi;
-            by[k] = v - fj;
-            ix0[k] = edge_index(fi, w) - (X0 - HX);
-            ix1[k] = edge_index(fi + 1.0f, w) - (X0 - HX);
-            iy0[k] = edge_index(fj, h) - (Y0 - HY);
-            iy1[k] = edge_index(fj + 1.0f, h) - (Y0 - HY);
-            ok = ok && ix0[k] >= 0 && ix1[k] < SW && iy0[k] >= 0 && iy1[k] < SH;
-        }
+        // 3. blur cache: G(x, y) of generate_features.wgsl:149-172
         float sum = 0.0f;
-        if (ok) {
-            const float wt[3] = {0.3125f, 0.375f, 0.3125f};
 #pragma unroll
-            for (int j = 0; j < 3; ++j) {
+        for (int j = 0; j < 3; ++j) {
+            const float b = s_bb[j][ty];
+            const float* row0 = sm[s_by0[j][ty]];
+            const float* row1 = sm[s_by1[j][ty]];
+            const float nb = 1.0f - b;
 #pragma unroll
-                for (int i = 0; i < 3; ++i) {
-                    const float a = ax[i], b = by[j];
-                    const float na = 1.0f - a, nb = 1.0f - b;
-                    float s = (na * nb) * sm[iy0[j]][ix0[i]];
-                    s = s + (a * nb) * sm[iy0[j]][ix1[i]];
-                    s = s + (na * b) * sm[iy1[j]][ix0[i]];
-                    s = s + (a * b) * sm[iy1[j]][ix1[i]];
-                    sum = sum + (s * wt[i]) * wt[j];
-                }
+            for (int i = 0; i < 3; ++i) {
+                const float a = ax[i];
+                const float na = 1.0f - a;
+                float sv = (na * nb) * row0[ix0[i]];
+                sv = sv + (a * nb) * row0[ix1[i]];
+                sv = sv + (na * b) * row1[ix0[i]];
+                sv = sv + (a * b) * row1[ix1[i]];
+                sum = sum + (sv * wt[i]) * wt[j];
             }
-        } else {
-            atomicOr(err, USLAM_ERR_SMEM_RANGE);
         }
         F.blur[l][p] = sum;
     }
@@ -389,7 +451,9 @@ __device__ __forceinline__ int find_segment(const uint32_t* s_pref, int nseg, ui
 }
 
 // G(P) evaluated directly (points outside the level; the sampler clamps).
-__device__ float gauss_tap9_direct(const FrameDev& F, int l, uint32_t px, uint32_t py) {
+// Rare (keypoints within ~18 px of a border): kept out of line so the hot
+// loop of k_describe stays small in the instruction cache.
+__device__ __noinline__ float gauss_tap9_direct(const FrameDev& F, int l, uint32_t px, uint32_t py) {
     const int w = F.w[l], h = F.h[l];
     const float tex_x = 1.0f / (float)w;
     const float tex_y = 1.0f / (float)h;
@@ -415,12 +479,6 @@ __device__ float gauss_tap9_direct(const FrameDev& F, int l, uint32_t px, uint32
         }
     }
     return sum;
-}
-
-__device__ __forceinline__ float gauss_tap9(const FrameDev& F, int l, uint32_t px, uint32_t py) {
-    if (px < (uint32_t)F.w[l] && py < (uint32_t)F.h[l])
-        return __ldg(F.blur[l] + (size_t)py * (size_t)F.w[l] + px);
-    return gauss_tap9_direct(F, l, px, py);
 }
 
 __global__ void __launch_bounds__(KD_THREADS)
@@ -465,20 +523,43 @@ k_describe(const FrameDev* __restrict__ frames, const SegDev* __restrict__ segs,
         float s, c;
         uslam_sincosf(theta, &s, &c);
 
-        // 256 tests, lane j owns tests j, j + 32, ..., j + 224
-        uint32_t words[8];
+        // 256 tests, lane j owns tests j, j + 32, ..., j + 224.  In-range
+        // points read the blur cache (16 independent gathers per lane);
+        // out-of-range points (near borders) are evaluated directly.
+        const float* blur = F.blur[l];
+        uint32_t pa[8], pb[8];  // flat blur index of in-range points (0 otherwise)
+        uint32_t xa[8], ya[8], xb[8], yb[8];
+        float ga[8], gb[8];
+        bool oob = false;
 #pragma unroll
         for (int k = 0; k < 8; ++k) {
             const int4 t = s_pat[lane + 32 * k];
             const float fax = (float)t.x, fay = (float)t.y, fbx = (float)t.z, fby = (float)t.w;
-            const int rax = (int)rintf(fax * c - fay * s);
-            const int ray = (int)rintf(fax * s + fay * c);
-            const int rbx = (int)rintf(fbx * c - fby * s);
-            const int rby = (int)rintf(fbx * s + fby * c);
-            const float ga = gauss_tap9(F, l, (uint32_t)(x + rax), (uint32_t)(y + ray));
-            const float gb = gauss_tap9(F, l, (uint32_t)(x + rbx), (uint32_t)(y + rby));
-            words[k] = __ballot_sync(0xffffffffu, ga > gb);
+            xa[k] = (uint32_t)(x + (int)rintf(fax * c - fay * s));
+            ya[k] = (uint32_t)(y + (int)rintf(fax * s + fay * c));
+            xb[k] = (uint32_t)(x + (int)rintf(fbx * c - fby * s));
+            yb[k] = (uint32_t)(y + (int)rintf(fbx * s + fby * c));
+            const bool ina = xa[k] < (uint32_t)w && ya[k] < (uint32_t)h;
+            const bool inb = xb[k] < (uint32_t)w && yb[k] < (uint32_t)h;
+            pa[k] = ina ? ya[k] * (uint32_t)w + xa[k] : 0u;
+            pb[k] = inb ? yb[k] * (uint32_t)w + xb[k] : 0u;
+            oob = oob || !ina || !inb;
         }
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            ga[k] = __ldg(blur + pa[k]);
+            gb[k] = __ldg(blur + pb[k]);
+        }
+        if (__any_sync(0xffffffffu, oob)) {
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+                if (!(xa[k] < (uint32_t)w && ya[k] < (uint32_t)h)) ga[k] = gauss_tap9_direct(F, l, xa[k], ya[k]);
+                if (!(xb[k] < (uint32_t)w && yb[k] < (uint32_t)h)) gb[k] = gauss_tap9_direct(F, l, xb[k], yb[k]);
+            }
+        }
+        uint32_t words[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) words[k] = __ballot_sync(0xffffffffu, ga[k] > gb[k]);
         uint32_t out = __float_as_uint(theta);
 #pragma unroll
         for (int k = 0; k < 8; ++k)
@@ -518,33 +599,57 @@ __device__ int last_col_le(float hi, float s, int w) {
     return xb;
 }
 
+// One candidate staged in shared memory: LOD-0 coordinates, packed
+// (level, index) and descriptor.
+struct CandSlot {
+    float px, py;
+    int32_t idx;
+    uint32_t pad;
+    uint4 d0, d1;
+};
+
+// A warp takes 32 queries that are consecutive in x (from the query level's
+// x order) and streams the union of their spatial windows, level by level of
+// the pool, through shared memory; every lane tests each broadcast candidate
+// against its own window (match_features_cpu.cpp:108-141) and keeps its
+// running best / second-best distance.  The result does not depend on the
+// candidate order: a tied best always fails the ratio test.
 __global__ void __launch_bounds__(KM_THREADS)
 k_match(const FrameDev* __restrict__ frames, const PairDev* __restrict__ pairs,
         const MatchSegDev* __restrict__ segs, int nseg) {
     __shared__ uint32_t s_pref[MAX_SEGS + 1];
     __shared__ uint32_t s_warp[33];
+    __shared__ CandSlot s_cand[KM_THREADS / 32][32];
     const uint32_t total = segment_prefix(nseg, s_pref, s_warp, [&](int s) {
         const PairDev& P = pairs[segs[s].pair];
         const int qf = segs[s].dir == 0 ? P.curr : P.prev;
-        return frames[qf].kept[segs[s].level];
+        return (frames[qf].kept[segs[s].level] + 31u) / 32u;
     });
     const int lane = threadIdx.x & 31;
-    const int gw = blockIdx.x * (KM_THREADS / 32) + (threadIdx.x >> 5);
+    const int warp = threadIdx.x >> 5;
+    const int gw = blockIdx.x * (KM_THREADS / 32) + warp;
     const int nw = gridDim.x * (KM_THREADS / 32);
+    CandSlot* slots = s_cand[warp];
     for (uint32_t g = gw; g < total; g += nw) {
         const int sidx = find_segment(s_pref, nseg, g);
-        const uint32_t i = g - s_pref[sidx];
+        const uint32_t grp = g - s_pref[sidx];
         const MatchSegDev sg = segs[sidx];
         const PairDev& P = pairs[sg.pair];
         const FrameDev& Q = frames[sg.dir == 0 ? P.curr : P.prev];
         const FrameDev& B = frames[sg.dir == 0 ? P.prev : P.curr];
         const int l = sg.level;
-        const uint32_t* qrec = Q.feats[l] + (size_t)i * 12u;
+        const uint32_t nq = Q.kept[l];
+        const uint32_t qk = grp * 32u + (uint32_t)lane;
+        const bool valid = qk < nq;
+        const uint32_t qi = valid ? __ldg(Q.xorder[l] + qk) : 0u;
+        const uint32_t* qrec = Q.feats[l] + (size_t)qi * 12u;
         const float ql = lod_scale(l);
         const float cx = (float)(uint32_t)__uint_as_float(qrec[0]) * ql;
         const float cy = (float)(uint32_t)__uint_as_float(qrec[1]) * ql;
         const uint4 qd0 = *reinterpret_cast<const uint4*>(qrec + 4);
         const uint4 qd1 = *reinterpret_cast<const uint4*>(qrec + 8);
+        const float lo = cx - P.max_dx, hi = cx + P.max_dx;
+        const float dy = P.max_dy;
 
         uint32_t best = 0xffffffffu, second = 0xffffffffu;
         int32_t bidx = -1;
@@ -553,58 +658,70 @@ k_match(const FrameDev* __restrict__ frames, const PairDev* __restrict__ pairs,
         if (l > 0) pool += B.kept[l - 1];
         if (l + 1 < L) pool += B.kept[l + 1];
         if (pool >= 2u) {
-            const float lo = cx - P.max_dx, hi = cx + P.max_dx;
+            // union of the lanes' windows
+            float lo_min = valid ? lo : __int_as_float(0x7f800000);
+            float hi_max = valid ? hi : -__int_as_float(0x7f800000);
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                lo_min = fminf(lo_min, __shfl_xor_sync(0xffffffffu, lo_min, o));
+                hi_max = fmaxf(hi_max, __shfl_xor_sync(0xffffffffu, hi_max, o));
+            }
             for (int k = 0; k < 3; ++k) {
                 const int pl = k == 0 ? l : (k == 1 ? l - 1 : l + 1);
                 if (pl < 0 || pl >= L) continue;
                 const float ps = lod_scale(pl);
                 const int wpl = B.w[pl];
-                const int xlo = first_col_ge(lo, ps, wpl);
-                const int xhi = last_col_le(hi, ps, wpl);
+                const int xlo = first_col_ge(lo_min, ps, wpl);
+                const int xhi = last_col_le(hi_max, ps, wpl);
                 if (xlo > xhi) continue;
-                const uint32_t c0 = B.colstart[pl][xlo], c1 = B.colstart[pl][xhi + 1];
+                const uint32_t c0 = __ldg(B.colstart[pl] + xlo), c1 = __ldg(B.colstart[pl] + xhi + 1);
                 const uint32_t* xorder = B.xorder[pl];
                 const uint32_t* feats = B.feats[pl];
-                for (uint32_t kk = c0 + lane; kk < c1; kk += 32) {
-                    const uint32_t j = __ldg(xorder + kk);
-                    const uint32_t* rec = feats + (size_t)j * 12u;
-                    const float by = (float)(uint32_t)__uint_as_float(__ldg(rec + 1)) * ps;
-                    if (fabsf(cy - by) > P.max_dy) continue;
-                    const uint4 d0 = __ldg(reinterpret_cast<const uint4*>(rec + 4));
-                    const uint4 d1 = __ldg(reinterpret_cast<const uint4*>(rec + 8));
-                    const uint32_t d = __popc(d0.x ^ qd0.x) + __popc(d0.y ^ qd0.y) + __popc(d0.z ^ qd0.z) +
-                                       __popc(d0.w ^ qd0.w) + __popc(d1.x ^ qd1.x) + __popc(d1.y ^ qd1.y) +
-                                       __popc(d1.z ^ qd1.z) + __popc(d1.w ^ qd1.w);
-                    if (d < best) {
-                        second = best;
-                        best = d;
-                        bidx = USLAM_PACK(pl, j);
-                    } else if (d < second) {
-                        second = d;
+                for (uint32_t base = c0; base < c1; base += 32u) {
+                    const uint32_t kk = base + (uint32_t)lane;
+                    if (kk < c1) {
+                        const uint32_t j = __ldg(xorder + kk);
+                        const uint32_t* rec = feats + (size_t)j * 12u;
+                        CandSlot cs;
+                        cs.px = (float)(uint32_t)__uint_as_float(__ldg(rec)) * ps;
+                        cs.py = (float)(uint32_t)__uint_as_float(__ldg(rec + 1)) * ps;
+                        cs.idx = USLAM_PACK(pl, j);
+                        cs.pad = 0u;
+                        cs.d0 = __ldg(reinterpret_cast<const uint4*>(rec + 4));
+                        cs.d1 = __ldg(reinterpret_cast<const uint4*>(rec + 8));
+                        slots[lane] = cs;
                     }
+                    __syncwarp();
+                    const int n = (int)min(32u, c1 - base);
+                    for (int t = 0; t < n; ++t) {
+                        const float px = slots[t].px, py = slots[t].py;
+                        const bool in = valid && px >= lo && px <= hi && !(fabsf(cy - py) > dy);
+                        if (__any_sync(0xffffffffu, in)) {
+                            const uint4 d0 = slots[t].d0, d1 = slots[t].d1;
+                            const uint32_t d = __popc(d0.x ^ qd0.x) + __popc(d0.y ^ qd0.y) + __popc(d0.z ^ qd0.z) +
+                                               __popc(d0.w ^ qd0.w) + __popc(d1.x ^ qd1.x) + __popc(d1.y ^ qd1.y) +
+                                               __popc(d1.z ^ qd1.z) + __popc(d1.w ^ qd1.w);
+                            if (in) {
+                                if (d < best) {
+                                    second = best;
+                                    best = d;
+                                    bidx = slots[t].idx;
+                                } else if (d < second) {
+                                    second = d;
+                                }
+                            }
+                        }
+                    }
+                    __syncwarp();
                 }
             }
         }
-        // warp merge of (best, second, idx)
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            const uint32_t ob = __shfl_xor_sync(0xffffffffu, best, o);
-            const uint32_t os = __shfl_xor_sync(0xffffffffu, second, o);
-            const int32_t oi = __shfl_xor_sync(0xffffffffu, bidx, o);
-            if (ob < best || (ob == best && oi > bidx)) {
-                second = min(best, os);
-                best = ob;
-                bidx = oi;
-            } else {
-                second = min(second, ob);
-            }
-        }
-        if (lane == 0) {
+        if (valid) {
             int32_t res = -1;
             if (bidx >= 0 && (float)best < 0.85f * (float)second) res = bidx;
             const int capq = Q.cap;
-            if (sg.dir == 0) P.b2a[(size_t)l * capq + i] = res;
-            else P.a2b[(size_t)l * capq + i] = res;
+            if (sg.dir == 0) P.b2a[(size_t)l * capq + qi] = res;
+            else P.a2b[(size_t)l * capq + qi] = res;
         }
     }
 }
