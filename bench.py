@@ -364,7 +364,7 @@ def run_ours(a):
             "plain_fps": plain_fps, "batched_over_plain": value / world / plain_fps,
             "e2e": {"value": n * world / e2e_s, "unit": "frames/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
-            "gpu_launches": 5 * a.steps, "roofline": roofline, "cpu_baseline": cpu, "clocks": clk,
+            "gpu_launches": 6 * a.steps, "roofline": roofline, "cpu_baseline": cpu, "clocks": clk,
             "features_per_frame": sum(kept) / n, "matches_per_pair": sum(nmatch) / max(1, n - 1),
             "wall_s_timed": wall_s,
         }

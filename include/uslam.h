@@ -112,7 +112,7 @@ uslam_status uslam_batch_upload(uslam_batch* b);
 /* Copy caller frames (any host memory, given pitch) into the pinned staging. */
 uslam_status uslam_batch_set_frame(uslam_batch* b, int frame, const uint8_t* img, int pitch);
 /* Launch detect + describe of every frame and match of every pair (one CUDA
- * graph replay: five kernel launches for the whole batch). Asynchronous. */
+ * graph replay: six kernel launches for the whole batch). Asynchronous. */
 uslam_status uslam_batch_run(uslam_batch* b);
 /* Asynchronous device->host copy of every frame's features and every pair's
  * matches into pinned staging (read them with the getters below). */
@@ -127,11 +127,15 @@ uslam_status uslam_batch_matches(uslam_batch* b, int pair, uslam_match* out, int
 /* Parity getters (synchronous, read device memory directly). */
 uslam_status uslam_batch_pyramid_level(uslam_batch* b, int frame, int level, float* out);
 uslam_status uslam_batch_keypoint_map(uslam_batch* b, int frame, int level, uint8_t* out);
+/* The extended blur cache of a level: (h + M + 1) rows of (w + M + 1)
+ * floats, M from uslam_blur_margin; row/column w + M (h + M) hold the value
+ * every negative x (y) takes. */
 uslam_status uslam_batch_blur_level(uslam_batch* b, int frame, int level, float* out);
+uslam_status uslam_blur_margin(const uslam_ctx* ctx, int* margin);
 /* Issue later upload/run/download calls on a caller's cudaStream_t (NULL:
  * the batch's own stream), so callers can record their own events around them. */
 uslam_status uslam_batch_set_stream(uslam_batch* b, void* cuda_stream);
-/* Per-kernel timing: launch the batch's five kernels `iters` times without
+/* Per-kernel timing: launch the batch's six kernels `iters` times without
  * the graph, with CUDA events between them on the batch stream, and return
  * the mean milliseconds per launch of detect, compact, describe, match and
  * mutual in kernel_ms[0..4].  Synchronous. */

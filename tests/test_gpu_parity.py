@@ -66,6 +66,33 @@ def test_blur_cache_bit_exact(ctx):
         b.close()
 
 
+def test_blur_cache_border_bit_exact(ctx):
+    """Cells beyond the level edge and the negative-coordinate sentinels hold
+    G(P) of generate_features.wgsl:149-172 at those points (u32-wrapped)."""
+    f1, _ = synth.config0_pair(2)
+    m = ctx.blur_margin()
+    b = _run(ctx, [f1])
+    try:
+        for l in (2, 5):
+            lvl = oracle.pyramid_level(f1, l)
+            h, w = lvl.shape
+            ext = b.blur_level(0, l, extended=True)
+            assert ext.shape == (h + m + 1, w + m + 1)
+            for ey in range(h + m + 1):
+                py = ey if ey < h + m else 0xFFFFFFFF
+                xs = range(w + m + 1) if ey >= h else range(w, w + m + 1)
+                for ex in xs:
+                    px = ex if ex < w + m else 0xFFFFFFFF
+                    exp = np.float32(oracle.gauss_tap9(lvl, px, py))
+                    assert ext[ey, ex].view(np.uint32) == exp.view(np.uint32), (l, ex, ey)
+            # every negative coordinate the pattern can reach maps to the sentinel
+            for k in (1, 7, m - 1):
+                assert np.float32(oracle.gauss_tap9(lvl, (-k) & 0xFFFFFFFF, 5)).view(np.uint32) == \
+                    ext[5, w + m].view(np.uint32)
+    finally:
+        b.close()
+
+
 def test_keypoint_maps_bit_exact(ctx):
     for seed in (0, 3):
         f1, _ = synth.config0_pair(seed)

@@ -63,6 +63,7 @@ SIGNATURES = {
     "uslam_batch_blur_level": (C.c_int, [_vp, C.c_int, C.c_int, _vp]),
     "uslam_batch_set_stream": (C.c_int, [_vp, _vp]),
     "uslam_batch_profile": (C.c_int, [_vp, C.c_int, _vp]),
+    "uslam_blur_margin": (C.c_int, [_vp, _ip]),
     "uslam_batch_io_bytes": (C.c_int, [_vp, _szp, _szp]),
     "uslam_frontend_create": (C.c_int, [_vp, C.c_int, C.c_int, C.POINTER(_vp)]),
     "uslam_frontend_destroy": (None, [_vp]),

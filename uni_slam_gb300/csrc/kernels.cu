@@ -1,6 +1,7 @@
 // kernels.cu — sm_103a kernels of the GB300 feature front-end.
 //
 //   k_detect   (K1) pyramid level tile + FAST response + cull + blur cache
+//   k_blur_border   blur cache beyond the level edges (BRIEF points outside)
 //   k_compact       per (frame, level): ordered keypoint compaction, cap, x-sort
 //   k_describe (K2) orientation + 256-bit rotated BRIEF, one warp per keypoint
 //   k_match    (K3) windowed top-2 Hamming search, 32 x-adjacent queries per warp
@@ -73,12 +74,6 @@ __device__ float pyramid_pixel(const FrameDev& F, int l, int x, int y) {
     r = r + (na * b) * t01;
     r = r + (a * b) * t11;
     return r;
-}
-
-// Level texel for describe-time reads (level 0 from the u8 frame).
-__device__ __forceinline__ float level_texel(const FrameDev& F, int l, int x, int y) {
-    if (l == 0) return lod0_texel(F, x, y);
-    return __ldg(F.lvl[l] + (size_t)y * (size_t)F.w[l] + x);
 }
 
 // FAST response at smem cell (r, c): 1 + longest non-wrapping run of
@@ -259,7 +254,7 @@ k_detect(const FrameDev* __restrict__ frames, const TileItem* __restrict__ tiles
                 sum = sum + (sv * wt[i]) * wt[j];
             }
         }
-        F.blur[l][p] = sum;
+        F.blur[l][(size_t)y * F.bl_pitch[l] + x] = sum;
     }
 }
 
@@ -450,11 +445,11 @@ __device__ __forceinline__ int find_segment(const uint32_t* s_pref, int nseg, ui
     return lo;
 }
 
-// G(P) evaluated directly (points outside the level; the sampler clamps).
-// Rare (keypoints within ~18 px of a border): kept out of line so the hot
-// loop of k_describe stays small in the instruction cache.
-__device__ __noinline__ float gauss_tap9_direct(const FrameDev& F, int l, uint32_t px, uint32_t py) {
-    const int w = F.w[l], h = F.h[l];
+// G(P) evaluated directly from the level image (the sampler clamps to the
+// edge).  Used for the blur-cache border; texel reads go through the level's
+// own pointer (u8 LOD0 through the LUT, or f32 levels).
+__device__ float gauss_tap9_direct(const uint8_t* img, int pitch, const float* lvl, const float* lut, int w, int h,
+                                   uint32_t px, uint32_t py) {
     const float tex_x = 1.0f / (float)w;
     const float tex_y = 1.0f / (float)h;
     const float uvx = ((float)px + 0.5f) * tex_x;
@@ -462,23 +457,80 @@ __device__ __noinline__ float gauss_tap9_direct(const FrameDev& F, int l, uint32
     const float off[3] = {-1.2f, 0.0f, 1.2f};
     const float wt[3] = {0.3125f, 0.375f, 0.3125f};
     float sum = 0.0f;
+#pragma unroll
     for (int j = 0; j < 3; ++j) {
+        const float v = (uvy + off[j] * tex_y) * (float)h - 0.5f;
+        const float fj = floorf(v);
+        const float b = v - fj;
+        const int j0 = edge_index(fj, h), j1 = edge_index(fj + 1.0f, h);
+#pragma unroll
         for (int i = 0; i < 3; ++i) {
             const float u = (uvx + off[i] * tex_x) * (float)w - 0.5f;
-            const float v = (uvy + off[j] * tex_y) * (float)h - 0.5f;
-            const float fi = floorf(u), fj = floorf(v);
-            const float a = u - fi, b = v - fj;
+            const float fi = floorf(u);
+            const float a = u - fi;
             const int i0 = edge_index(fi, w), i1 = edge_index(fi + 1.0f, w);
-            const int j0 = edge_index(fj, h), j1 = edge_index(fj + 1.0f, h);
+            float t00, t10, t01, t11;
+            if (lvl) {
+                t00 = __ldg(lvl + (size_t)j0 * w + i0);
+                t10 = __ldg(lvl + (size_t)j0 * w + i1);
+                t01 = __ldg(lvl + (size_t)j1 * w + i0);
+                t11 = __ldg(lvl + (size_t)j1 * w + i1);
+            } else {
+                t00 = lut[__ldg(img + (size_t)j0 * pitch + i0)];
+                t10 = lut[__ldg(img + (size_t)j0 * pitch + i1)];
+                t01 = lut[__ldg(img + (size_t)j1 * pitch + i0)];
+                t11 = lut[__ldg(img + (size_t)j1 * pitch + i1)];
+            }
             const float na = 1.0f - a, nb = 1.0f - b;
-            float s = (na * nb) * level_texel(F, l, i0, j0);
-            s = s + (a * nb) * level_texel(F, l, i1, j0);
-            s = s + (na * b) * level_texel(F, l, i0, j1);
-            s = s + (a * b) * level_texel(F, l, i1, j1);
+            float s = (na * nb) * t00;
+            s = s + (a * nb) * t10;
+            s = s + (na * b) * t01;
+            s = s + (a * b) * t11;
             sum = sum + (s * wt[i]) * wt[j];
         }
     }
     return sum;
+}
+
+// Blur-cache border of one level: columns [w, w + M) and the negative-x
+// sentinel column for rows [0, h), then rows [h, h + M) and the negative-y
+// sentinel row for all columns.  A sentinel stands for every negative
+// coordinate: u32(negative) converts to the same f32 2^32 for all offsets a
+// BRIEF test can reach, so G is identical for all of them.
+__device__ __forceinline__ int border_cells(const FrameDev& F, int l) {
+    const int m1 = F.margin + 1;
+    return F.h[l] * m1 + m1 * F.bl_pitch[l];
+}
+
+__global__ void __launch_bounds__(256)
+k_blur_border(const FrameDev* __restrict__ frames, const SegDev* __restrict__ segs, int nseg) {
+    __shared__ uint32_t s_pref[MAX_SEGS + 1];
+    __shared__ uint32_t s_warp[33];
+    __shared__ float s_lut[256];
+    s_lut[threadIdx.x] = (float)threadIdx.x / 255.0f;
+    const uint32_t total = segment_prefix(nseg, s_pref, s_warp, [&](int sg) {
+        return (uint32_t)border_cells(frames[segs[sg].frame], segs[sg].level);
+    });
+    for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < total; g += gridDim.x * blockDim.x) {
+        const int sidx = find_segment(s_pref, nseg, g);
+        const int cell = (int)(g - s_pref[sidx]);
+        const FrameDev& F = frames[segs[sidx].frame];
+        const int l = segs[sidx].level;
+        const int w = F.w[l], h = F.h[l], M = F.margin, m1 = M + 1, bp = F.bl_pitch[l];
+        int ex, ey;
+        if (cell < h * m1) {
+            ey = cell / m1;
+            ex = w + cell % m1;
+        } else {
+            const int c2 = cell - h * m1;
+            ey = h + c2 / bp;
+            ex = c2 % bp;
+        }
+        const uint32_t px = ex < w + M ? (uint32_t)ex : 0xffffffffu;
+        const uint32_t py = ey < h + M ? (uint32_t)ey : 0xffffffffu;
+        F.blur[l][(size_t)ey * bp + ex] =
+            gauss_tap9_direct(F.img, F.img_pitch, l > 0 ? F.lvl[l] : nullptr, s_lut, w, h, px, py);
+    }
 }
 
 __global__ void __launch_bounds__(KD_THREADS)
@@ -487,8 +539,11 @@ k_describe(const FrameDev* __restrict__ frames, const SegDev* __restrict__ segs,
     __shared__ int4 s_pat[256];
     __shared__ uint32_t s_pref[MAX_SEGS + 1];
     __shared__ uint32_t s_warp[33];
-    for (int i = threadIdx.x; i < 256; i += KD_THREADS)
+    __shared__ float s_lut[256];
+    for (int i = threadIdx.x; i < 256; i += KD_THREADS) {
         s_pat[i] = make_int4(pattern[4 * i], pattern[4 * i + 1], pattern[4 * i + 2], pattern[4 * i + 3]);
+        s_lut[i] = (float)i / 255.0f;
+    }
     const uint32_t total = segment_prefix(nseg, s_pref, s_warp, [&](int s) {
         return frames[segs[s].frame].kept[segs[s].level];
     });
@@ -510,7 +565,8 @@ k_describe(const FrameDev* __restrict__ frames, const SegDev* __restrict__ segs,
         if (lane < 29) {
             const int cx = tint_clamp(x + c_disc_x[lane], w);
             const int cy = tint_clamp(y + c_disc_y[lane], h);
-            p = level_texel(F, l, cx, cy);
+            p = l == 0 ? s_lut[__ldg(F.img + (size_t)cy * F.img_pitch + cx)]
+                       : __ldg(F.lvl[l] + (size_t)cy * (size_t)w + cx);
         }
         float m10 = 0.0f, m01 = 0.0f;
 #pragma unroll
@@ -523,39 +579,26 @@ k_describe(const FrameDev* __restrict__ frames, const SegDev* __restrict__ segs,
         float s, c;
         uslam_sincosf(theta, &s, &c);
 
-        // 256 tests, lane j owns tests j, j + 32, ..., j + 224.  In-range
-        // points read the blur cache (16 independent gathers per lane);
-        // out-of-range points (near borders) are evaluated directly.
+        // 256 tests, lane j owns tests j, j + 32, ..., j + 224: 16 independent
+        // gathers from the blur cache (negative coordinates -> sentinel).
         const float* blur = F.blur[l];
-        uint32_t pa[8], pb[8];  // flat blur index of in-range points (0 otherwise)
-        uint32_t xa[8], ya[8], xb[8], yb[8];
+        const int bp = F.bl_pitch[l];
+        const int sx = w + F.margin, sy = h + F.margin;
         float ga[8], gb[8];
-        bool oob = false;
 #pragma unroll
         for (int k = 0; k < 8; ++k) {
             const int4 t = s_pat[lane + 32 * k];
             const float fax = (float)t.x, fay = (float)t.y, fbx = (float)t.z, fby = (float)t.w;
-            xa[k] = (uint32_t)(x + (int)rintf(fax * c - fay * s));
-            ya[k] = (uint32_t)(y + (int)rintf(fax * s + fay * c));
-            xb[k] = (uint32_t)(x + (int)rintf(fbx * c - fby * s));
-            yb[k] = (uint32_t)(y + (int)rintf(fbx * s + fby * c));
-            const bool ina = xa[k] < (uint32_t)w && ya[k] < (uint32_t)h;
-            const bool inb = xb[k] < (uint32_t)w && yb[k] < (uint32_t)h;
-            pa[k] = ina ? ya[k] * (uint32_t)w + xa[k] : 0u;
-            pb[k] = inb ? yb[k] * (uint32_t)w + xb[k] : 0u;
-            oob = oob || !ina || !inb;
-        }
-#pragma unroll
-        for (int k = 0; k < 8; ++k) {
-            ga[k] = __ldg(blur + pa[k]);
-            gb[k] = __ldg(blur + pb[k]);
-        }
-        if (__any_sync(0xffffffffu, oob)) {
-#pragma unroll
-            for (int k = 0; k < 8; ++k) {
-                if (!(xa[k] < (uint32_t)w && ya[k] < (uint32_t)h)) ga[k] = gauss_tap9_direct(F, l, xa[k], ya[k]);
-                if (!(xb[k] < (uint32_t)w && yb[k] < (uint32_t)h)) gb[k] = gauss_tap9_direct(F, l, xb[k], yb[k]);
-            }
+            int xa = x + (int)rintf(fax * c - fay * s);
+            int ya = y + (int)rintf(fax * s + fay * c);
+            int xb = x + (int)rintf(fbx * c - fby * s);
+            int yb = y + (int)rintf(fbx * s + fby * c);
+            xa = xa < 0 ? sx : xa;
+            ya = ya < 0 ? sy : ya;
+            xb = xb < 0 ? sx : xb;
+            yb = yb < 0 ? sy : yb;
+            ga[k] = __ldg(blur + (size_t)ya * bp + xa);
+            gb[k] = __ldg(blur + (size_t)yb * bp + xb);
         }
         uint32_t words[8];
 #pragma unroll
@@ -802,6 +845,12 @@ cudaError_t launch_compact(const FrameDev* frames, const SegDev* segs, int nseg,
     if (nseg <= 0) return cudaSuccess;
     const size_t smem = (size_t)(max_w + 1) * sizeof(uint32_t);
     k_compact<<<nseg, KC_THREADS, smem, st>>>(frames, segs);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_blur_border(const FrameDev* frames, const SegDev* segs, int nseg, int grid, cudaStream_t st) {
+    if (nseg <= 0) return cudaSuccess;
+    k_blur_border<<<grid, 256, 0, st>>>(frames, segs, nseg);
     return cudaGetLastError();
 }
 

@@ -7,7 +7,7 @@
 //   frame, counts + matches of every pair][scratch: pyramid, blur cache,
 //   keypoint maps, x-sort tables, match directions, error word]
 // so one H2D copy feeds the whole batch and one D2H copy returns it.  The
-// batch's launch sequence (5 kernels) is captured once into a CUDA graph.
+// batch's launch sequence (6 kernels) is captured once into a CUDA graph.
 // A frontend (uslam_frontend) is a 2-slot batch driven frame by frame with
 // the reference's FeatureSet(0)/(1) rotation.
 #include <cuda_runtime.h>
@@ -34,6 +34,7 @@ struct MatchSegDev {
 cudaError_t init_constants();
 cudaError_t launch_detect(const FrameDev*, const TileItem*, int, uint32_t*, cudaStream_t);
 cudaError_t launch_compact(const FrameDev*, const SegDev*, int, int, cudaStream_t);
+cudaError_t launch_blur_border(const FrameDev*, const SegDev*, int, int, cudaStream_t);
 cudaError_t launch_describe(const FrameDev*, const SegDev*, int, const int32_t*, int, cudaStream_t);
 cudaError_t launch_match(const FrameDev*, const PairDev*, const void*, int, int, cudaStream_t);
 cudaError_t launch_mutual(const FrameDev*, const PairDev*, const SegDev*, int, uint32_t*, cudaStream_t);
@@ -124,6 +125,7 @@ struct uslam_ctx {
     int max_w = 0, max_h = 0;
     int cap_override = 0;
     int num_sms = 0;
+    int margin = 0;  // blur-cache margin: BRIEF pattern radius + 2
     int32_t* d_pattern = nullptr;
     std::string err;
     std::map<std::pair<int, int>, ResClass> classes;
@@ -257,8 +259,9 @@ cudaError_t enqueue_program(uslam_batch* b, const Program& P) {
     cudaError_t e = cudaSuccess;
     if (P.ntiles > 0) {
         if ((e = launch_detect(b->d_frames, P.tiles, P.ntiles, b->d_err, b->stream)) != cudaSuccess) return e;
-        if ((e = launch_compact(b->d_frames, P.fsegs, P.nfsegs, b->max_w, b->stream)) != cudaSuccess) return e;
         const int grid = c->num_sms * 4;
+        if ((e = launch_blur_border(b->d_frames, P.fsegs, P.nfsegs, grid, b->stream)) != cudaSuccess) return e;
+        if ((e = launch_compact(b->d_frames, P.fsegs, P.nfsegs, b->max_w, b->stream)) != cudaSuccess) return e;
         if ((e = launch_describe(b->d_frames, P.fsegs, P.nfsegs, c->d_pattern, grid, b->stream)) != cudaSuccess)
             return e;
     }
@@ -346,6 +349,7 @@ uslam_status create_batch(uslam_ctx* ctx, int n_frames, const int* widths, const
         F.W0 = W0;
         F.H0 = H0;
         F.levels = L;
+        F.margin = ctx->margin;
         F.img_pitch = static_cast<int>(round_up(static_cast<size_t>(W0), 16));
         level_dims(W0, H0, L, F.w, F.h);
         for (int l = 0; l < L; ++l) {
@@ -369,7 +373,8 @@ uslam_status create_batch(uslam_ctx* ctx, int n_frames, const int* widths, const
             F.kp_pitch[l] = static_cast<int>(round_up(static_cast<size_t>(F.w[l]), 16));
             Ly.feats[l] = take(&out_bytes, capa * 48);
             Ly.lvl[l] = l > 0 ? take(&scratch, n * 4) : 0;
-            Ly.blur[l] = take(&scratch, n * 4);
+            F.bl_pitch[l] = F.w[l] + ctx->margin + 1;
+            Ly.blur[l] = take(&scratch, static_cast<size_t>(F.h[l] + ctx->margin + 1) * F.bl_pitch[l] * 4);
             Ly.kpmap[l] = take(&scratch, static_cast<size_t>(F.h[l]) * F.kp_pitch[l]);
             Ly.xorder[l] = take(&scratch, capa * 4);
             Ly.colstart[l] = take(&scratch, (static_cast<size_t>(F.w[l]) + 1) * 4);
@@ -669,6 +674,18 @@ uslam_status uslam_create(const uslam_params* params, uslam_ctx** out) {
     c->max_w = params->max_width;
     c->max_h = params->max_height;
     c->cap_override = params->cap_per_level;
+    // blur-cache margin: a rotated test point lies within ceil(radius) + 1 of
+    // its keypoint (rounding of the rotation), so radius + 2 covers it.
+    double rmax = 0.0;
+    for (int i = 0; i < 512; ++i) {
+        const double px = params->brief_pattern[2 * i], py = params->brief_pattern[2 * i + 1];
+        rmax = std::max(rmax, std::sqrt(px * px + py * py));
+    }
+    if (rmax > 1024.0) {
+        delete c;
+        return USLAM_INVALID_ARG;
+    }
+    c->margin = static_cast<int>(std::ceil(rmax)) + 2;
     cudaError_t e = cudaSetDevice(c->device);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, c->device);
     if (e == cudaSuccess) e = init_constants();
@@ -779,8 +796,15 @@ uslam_status uslam_batch_blur_level(uslam_batch* b, int frame, int level, float*
     if (!b || !out || frame < 0 || frame >= static_cast<int>(b->frames.size()) || level < 0 || level >= b->levels)
         return USLAM_INVALID_ARG;
     const FrameDev& F = b->frames[frame];
-    cudaError_t e = cudaMemcpy(out, F.blur[level], sizeof(float) * F.w[level] * F.h[level], cudaMemcpyDeviceToHost);
+    const size_t n = static_cast<size_t>(F.h[level] + F.margin + 1) * F.bl_pitch[level];
+    cudaError_t e = cudaMemcpy(out, F.blur[level], sizeof(float) * n, cudaMemcpyDeviceToHost);
     if (e != cudaSuccess) return b->ctx->cuda_fail(e, "blur readback");
+    return USLAM_OK;
+}
+
+uslam_status uslam_blur_margin(const uslam_ctx* ctx, int* margin) {
+    if (!ctx || !margin) return USLAM_INVALID_ARG;
+    *margin = ctx->margin;
     return USLAM_OK;
 }
 
@@ -804,35 +828,42 @@ uslam_status uslam_batch_profile(uslam_batch* b, int iters, float* kernel_ms) {
     if (!b || iters <= 0 || !kernel_ms) return USLAM_INVALID_ARG;
     uslam_ctx* c = b->ctx;
     const Program& P = b->full;
-    cudaEvent_t ev[6];
+    constexpr int K = 6;
+    cudaEvent_t ev[K + 1];
     for (auto& x : ev) x = nullptr;
     cudaError_t e = cudaSuccess;
-    for (int i = 0; i < 6 && e == cudaSuccess; ++i) e = cudaEventCreate(&ev[i]);
-    double acc[5] = {0, 0, 0, 0, 0};
+    for (int i = 0; i <= K && e == cudaSuccess; ++i) e = cudaEventCreate(&ev[i]);
+    double acc[K] = {0, 0, 0, 0, 0, 0};
     const int grid = c->num_sms * 4;
     for (int it = 0; it < iters && e == cudaSuccess; ++it) {
-        e = cudaEventRecord(ev[0], b->stream);
+        int k = 0;
+        auto mark = [&]() {
+            if (e == cudaSuccess) e = cudaEventRecord(ev[k++], b->stream);
+        };
+        mark();
         if (e == cudaSuccess) e = launch_detect(b->d_frames, P.tiles, P.ntiles, b->d_err, b->stream);
-        if (e == cudaSuccess) e = cudaEventRecord(ev[1], b->stream);
+        mark();
+        if (e == cudaSuccess) e = launch_blur_border(b->d_frames, P.fsegs, P.nfsegs, grid, b->stream);
+        mark();
         if (e == cudaSuccess) e = launch_compact(b->d_frames, P.fsegs, P.nfsegs, b->max_w, b->stream);
-        if (e == cudaSuccess) e = cudaEventRecord(ev[2], b->stream);
+        mark();
         if (e == cudaSuccess) e = launch_describe(b->d_frames, P.fsegs, P.nfsegs, c->d_pattern, grid, b->stream);
-        if (e == cudaSuccess) e = cudaEventRecord(ev[3], b->stream);
+        mark();
         if (e == cudaSuccess) e = launch_match(b->d_frames, b->d_pairs, P.msegs, P.nmsegs, grid, b->stream);
-        if (e == cudaSuccess) e = cudaEventRecord(ev[4], b->stream);
+        mark();
         if (e == cudaSuccess) e = launch_mutual(b->d_frames, b->d_pairs, P.usegs, P.nusegs, b->d_err, b->stream);
-        if (e == cudaSuccess) e = cudaEventRecord(ev[5], b->stream);
-        if (e == cudaSuccess) e = cudaEventSynchronize(ev[5]);
-        for (int k = 0; k < 5 && e == cudaSuccess; ++k) {
+        mark();
+        if (e == cudaSuccess) e = cudaEventSynchronize(ev[K]);
+        for (int q = 0; q < K && e == cudaSuccess; ++q) {
             float ms = 0.0f;
-            e = cudaEventElapsedTime(&ms, ev[k], ev[k + 1]);
-            acc[k] += ms;
+            e = cudaEventElapsedTime(&ms, ev[q], ev[q + 1]);
+            acc[q] += ms;
         }
     }
     for (auto& x : ev)
         if (x) cudaEventDestroy(x);
     if (e != cudaSuccess) return c->cuda_fail(e, "profile");
-    for (int k = 0; k < 5; ++k) kernel_ms[k] = static_cast<float>(acc[k] / iters);
+    for (int q = 0; q < K; ++q) kernel_ms[q] = static_cast<float>(acc[q] / iters);
     return check_err_word(b);
 }
 

@@ -5,7 +5,13 @@
 // of one arena allocation per batch):
 //   img      u8   [H0][img_pitch]          LOD0 input (the H2D boundary)
 //   lvl[l]   f32  [h_l][w_l]   (l >= 1)    pyramid level l (parity output)
-//   blur[l]  f32  [h_l][w_l]               9-tap blurred sample G(x, y) of level l
+//   blur[l]  f32  [h_l + M + 1][bl_pitch_l] 9-tap blurred sample G(P) of level l for
+//                                          every integer point a BRIEF test can reach:
+//                                          x in [0, w_l + M) plus one sentinel column
+//                                          (index w_l + M) for every negative x (all
+//                                          negative u32-wrapped x convert to the same
+//                                          f32, 2^32); rows likewise.  M = pattern
+//                                          radius + 2, bl_pitch_l = w_l + M + 1.
 //   kpmap[l] u8   [h_l][kp_pitch_l]        culled FAST strength (0 = no keypoint)
 //   feats[l] Feature[cap]                  gpumodels::Feature records, (y, x) order
 //   xorder[l] u32 [cap]                    feature indices sorted by x (matching)
@@ -24,6 +30,8 @@ struct FrameDev {
     int w[USLAM_MAX_LEVELS];
     int h[USLAM_MAX_LEVELS];
     int kp_pitch[USLAM_MAX_LEVELS];
+    int bl_pitch[USLAM_MAX_LEVELS];  // blur cache row pitch (floats): w + margin + 1
+    int margin;                      // blur cache margin M beyond the level
     float* lvl[USLAM_MAX_LEVELS];
     float* blur[USLAM_MAX_LEVELS];
     uint8_t* kpmap[USLAM_MAX_LEVELS];

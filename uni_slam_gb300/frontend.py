@@ -11,7 +11,7 @@ from . import capi
 from .capi import FEATURE_DTYPE, MATCH_DTYPE, USlamError, iptr, ptr
 
 
-KERNELS = ("k_detect", "k_compact", "k_describe", "k_match", "k_mutual")
+KERNELS = ("k_detect", "k_blur_border", "k_compact", "k_describe", "k_match", "k_mutual")
 
 
 def level_dims(width: int, height: int, levels: int = 6) -> list[tuple[int, int]]:
@@ -41,6 +41,11 @@ class Context:
             raise USlamError(st, "uslam_create failed")
         self.h = h
         self.levels = levels
+
+    def blur_margin(self) -> int:
+        m = C.c_int()
+        self.check(self.lib.uslam_blur_margin(self.h, C.byref(m)), "blur_margin")
+        return m.value
 
     def error(self) -> str:
         return self.lib.uslam_last_error(self.h).decode()
@@ -144,11 +149,14 @@ class Batch:
         self.ctx.check(self.lib.uslam_batch_pyramid_level(self.h, i, level, ptr(out)), "pyramid_level")
         return out
 
-    def blur_level(self, i: int, level: int) -> np.ndarray:
+    def blur_level(self, i: int, level: int, extended: bool = False) -> np.ndarray:
+        """Blur cache of a level: the w x h interior, or the extended cache
+        ((h + M + 1) x (w + M + 1), last row/column = negative-coordinate sentinel)."""
         w, h = self._dims(i, level)
-        out = np.zeros((h, w), np.float32)
+        m = self.ctx.blur_margin()
+        out = np.zeros((h + m + 1, w + m + 1), np.float32)
         self.ctx.check(self.lib.uslam_batch_blur_level(self.h, i, level, ptr(out)), "blur_level")
-        return out
+        return out if extended else np.ascontiguousarray(out[:h, :w])
 
     def keypoint_map(self, i: int, level: int) -> np.ndarray:
         w, h = self._dims(i, level)
@@ -160,7 +168,7 @@ class Batch:
         self.ctx.check(self.lib.uslam_batch_set_stream(self.h, C.c_void_p(cuda_stream or 0)), "set_stream")
 
     def profile(self, iters: int = 5) -> dict[str, float]:
-        ms = np.zeros(5, np.float32)
+        ms = np.zeros(len(KERNELS), np.float32)
         self.ctx.check(self.lib.uslam_batch_profile(self.h, iters, ptr(ms)), "profile")
         return dict(zip(KERNELS, (float(v) for v in ms)))
 
