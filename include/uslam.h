@@ -171,6 +171,38 @@ uslam_status uslam_frontend_enqueue(uslam_frontend* fe, const uint8_t* dev_img, 
                                     int* matched);
 uslam_status uslam_frontend_sync(uslam_frontend* fe);
 
+/* ---- matcher for callers that cannot allocate ---------------------------- */
+
+/* No counterpart in the reference.  For callers that cannot call cudaMalloc
+ * when they need a match (a runtime that owns all device memory through its
+ * own pool, a real-time loop that must not take allocator locks or risk an
+ * allocation failure mid-frame, a context whose memory budget is fixed): the
+ * same mutual windowed match as the batch and frontend paths, of feature set
+ * prev (the reference set) against curr, allocating nothing.
+ *
+ * Inputs and outputs are the caller's device memory: prev_feats/curr_feats
+ * hold the features level after level in (y, x) order (the layout
+ * uslam_batch_features returns), prev_kept/curr_kept (host arrays of
+ * `levels` ints) the per-level counts; out receives levels blocks of
+ * out_cap_per_level uslam_match entries (block l = matches whose previous
+ * feature lies in level l, in that feature's order) and out_counts the
+ * per-level match counts.  out_cap_per_level must be at least the previous
+ * set's largest level count.
+ *
+ * Scratch comes from a file-scope device array of 4 MiB that every GPU which
+ * loads the library holds until the process exits; a call whose scratch need
+ * exceeds it returns USLAM_CAPACITY.  The first call on a device looks up
+ * that array's device address (cudaGetSymbolAddress); make that first call
+ * before any stream capture.  All calls share the array: calls that overlap
+ * on the GPU (different streams or threads at the same time) race and must
+ * not be issued.  The call enqueues on `stream` (a cudaStream_t; NULL = the
+ * default stream) and returns after the work is complete.  err (optional,
+ * err_len bytes) receives a message on failure. */
+uslam_status uslam_match_noalloc(int device, int width, int height, int levels, const uslam_feature* prev_feats,
+                                 const int* prev_kept, const uslam_feature* curr_feats, const int* curr_kept,
+                                 uslam_match* out, uint32_t* out_counts, int out_cap_per_level, void* stream,
+                                 char* err, size_t err_len);
+
 #ifdef __cplusplus
 }
 #endif

@@ -73,6 +73,8 @@ SIGNATURES = {
     "uslam_frontend_matches": (C.c_int, [_vp, _vp, C.c_int, _ip]),
     "uslam_frontend_enqueue": (C.c_int, [_vp, _vp, C.c_int, C.c_int, _ip]),
     "uslam_frontend_sync": (C.c_int, [_vp]),
+    "uslam_match_noalloc": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, _vp, _ip, _vp, _ip, _vp, _vp, C.c_int,
+                                      _vp, C.c_char_p, C.c_size_t]),
 }
 
 _lib = None

@@ -1,0 +1,287 @@
+// noalloc.cu — a matcher entry point that performs no device allocation.
+//
+// Some callers of this library cannot call cudaMalloc at the moment they
+// need a match: a host runtime that hands out device memory only from its own
+// pool, a real-time loop that must not take the allocator's locks or risk an
+// allocation failure mid-frame, or code running where the CUDA context is
+// shared and its memory budget is fixed in advance.  uslam_match_noalloc
+// serves them: the caller passes the two feature sets and the output buffers
+// (all device memory it already owns), and every piece of scratch the match
+// needs lives in one file-scope __device__ array of fixed size, which every
+// GPU that loads the library holds until the process exits.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+
+#include "../../include/uslam.h"
+#include "uslam_internal.h"
+
+namespace uslam {
+struct MatchSegDev {
+    int pair;
+    int dir;
+    int level;
+};
+cudaError_t launch_match(const FrameDev*, const PairDev*, const void*, int, int, cudaStream_t);
+cudaError_t launch_mutual(const FrameDev*, const PairDev*, const SegDev*, int, uint32_t*, cudaStream_t);
+}  // namespace uslam
+
+using namespace uslam;
+
+namespace {
+
+constexpr size_t kNoallocScratchBytes = size_t(4) << 20;  // 4 MiB per device
+constexpr int kMaxDevices = 64;
+constexpr int kXsortThreads = 1024;
+
+// The no-alloc matcher's scratch.  Host code must not use this name as an
+// address: it is a host-side stand-in.  The device address comes from
+// cudaGetSymbolAddress once per device (see scratch_for_device).
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoallocScratchBytes];
+
+// Everything the match kernels read besides the features, written into the
+// scratch by one small kernel that receives it by value (no host copy).
+struct NoallocTables {
+    FrameDev frames[2];
+    PairDev pair;
+    MatchSegDev msegs[2 * USLAM_MAX_LEVELS];
+    SegDev usegs[USLAM_MAX_LEVELS];
+    SegDev xsegs[2 * USLAM_MAX_LEVELS];
+    uint32_t counts[2][2 * USLAM_MAX_LEVELS];  // per frame: kept[levels], raw[levels]
+};
+
+__global__ void k_noalloc_tables(const NoallocTables t, NoallocTables* dst) {
+    const uint32_t* s = reinterpret_cast<const uint32_t*>(&t);
+    uint32_t* d = reinterpret_cast<uint32_t*>(dst);
+    for (size_t i = threadIdx.x; i < sizeof(NoallocTables) / 4; i += blockDim.x) d[i] = s[i];
+}
+
+// x counting sort of one (frame, level): colstart[x] = first slot of column x
+// in xorder, xorder = feature indices by x (the matcher's window lookup).
+__global__ void __launch_bounds__(kXsortThreads)
+k_noalloc_xsort(const FrameDev* __restrict__ frames, const SegDev* __restrict__ segs) {
+    extern __shared__ uint32_t s_hist[];  // [w + 1]
+    __shared__ uint32_t s_part[kXsortThreads / 32 + 1];
+    const FrameDev& F = frames[segs[blockIdx.x].frame];
+    const int l = segs[blockIdx.x].level;
+    const int w = F.w[l];
+    const uint32_t kept = F.kept[l];
+    const uint32_t* feats = F.feats[l];
+    for (int i = threadIdx.x; i <= w; i += kXsortThreads) s_hist[i] = 0u;
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < kept; i += kXsortThreads)
+        atomicAdd(&s_hist[(int)__uint_as_float(feats[(size_t)i * 12u])], 1u);
+    __syncthreads();
+    // exclusive scan of the w + 1 bins: each thread sums a run of bins, the
+    // run totals are scanned by warp 0, then each thread writes its run
+    const int per = (w + kXsortThreads) / kXsortThreads;
+    const int b0 = threadIdx.x * per;
+    uint32_t local = 0;
+    for (int k = 0; k < per; ++k)
+        if (b0 + k < w) local += s_hist[b0 + k];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t incl = local;
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t v = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += v;
+    }
+    if (lane == 31) s_part[warp] = incl;
+    __syncthreads();
+    if (warp == 0) {
+        const uint32_t v = lane < kXsortThreads / 32 ? s_part[lane] : 0u;
+        uint32_t wi = v;
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t u = __shfl_up_sync(0xffffffffu, wi, o);
+            if (lane >= o) wi += u;
+        }
+        if (lane < kXsortThreads / 32) s_part[lane] = wi - v;
+    }
+    __syncthreads();
+    uint32_t run = s_part[warp] + incl - local;
+    uint32_t* colstart = F.colstart[l];
+    for (int k = 0; k < per; ++k) {
+        const int b = b0 + k;
+        if (b <= w) {
+            const uint32_t c = b < w ? s_hist[b] : 0u;
+            colstart[b] = run;
+            run += c;
+        }
+    }
+    __syncthreads();
+    for (int k = 0; k < per; ++k) {
+        const int b = b0 + k;
+        if (b <= w) s_hist[b] = colstart[b];
+    }
+    __syncthreads();
+    uint32_t* xorder = F.xorder[l];
+    for (uint32_t i = threadIdx.x; i < kept; i += kXsortThreads) {
+        const int fx = (int)__uint_as_float(feats[(size_t)i * 12u]);
+        xorder[atomicAdd(&s_hist[fx], 1u)] = i;
+    }
+}
+
+struct DeviceScratch {
+    unsigned char* ptr = nullptr;
+    int num_sms = 0;
+    bool ready = false;
+};
+
+std::mutex g_setup_mutex;
+DeviceScratch g_scratch_by_device[kMaxDevices];
+
+// Set-up, once per device, with that device current: the scratch's device
+// address (cudaGetSymbolAddress) and the SM count.  Happens on the first call
+// on a device; that first call should therefore come before any stream capture.
+cudaError_t scratch_for_device(int device, DeviceScratch* out) {
+    std::lock_guard<std::mutex> lock(g_setup_mutex);
+    DeviceScratch& d = g_scratch_by_device[device];
+    if (!d.ready) {
+        void* p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess) return e;
+        e = cudaDeviceGetAttribute(&d.num_sms, cudaDevAttrMultiProcessorCount, device);
+        if (e != cudaSuccess) return e;
+        d.ptr = static_cast<unsigned char*>(p);
+        d.ready = true;
+    }
+    *out = d;
+    return cudaSuccess;
+}
+
+uslam_status fail(char* err, size_t err_len, uslam_status s, const char* msg) {
+    if (err && err_len > 0) std::snprintf(err, err_len, "%s", msg);
+    return s;
+}
+
+size_t align256(size_t v) { return (v + 255) / 256 * 256; }
+
+}  // namespace
+
+extern "C" uslam_status uslam_match_noalloc(int device, int width, int height, int levels,
+                                            const uslam_feature* prev_feats, const int* prev_kept,
+                                            const uslam_feature* curr_feats, const int* curr_kept, uslam_match* out,
+                                            uint32_t* out_counts, int out_cap_per_level, void* stream, char* err,
+                                            size_t err_len) {
+    if (device < 0 || device >= kMaxDevices || width <= 0 || height <= 0 || width > 12000 || levels < 1 ||
+        levels > USLAM_MAX_LEVELS || !prev_kept || !curr_kept || !out || !out_counts || out_cap_per_level < 1)
+        return fail(err, err_len, USLAM_INVALID_ARG, "match_noalloc: bad arguments");
+    int wl[USLAM_MAX_LEVELS], hl[USLAM_MAX_LEVELS];
+    if (uslam_level_dims(width, height, levels, wl, hl) != USLAM_OK)
+        return fail(err, err_len, USLAM_INVALID_ARG, "match_noalloc: bad frame size");
+    for (int l = 0; l < levels; ++l)
+        if (wl[l] < 1 || hl[l] < 1) return fail(err, err_len, USLAM_INVALID_ARG, "match_noalloc: empty pyramid level");
+    const int* kept[2] = {prev_kept, curr_kept};
+    const uslam_feature* feats[2] = {prev_feats, curr_feats};
+    int cap[2] = {1, 1};
+    long long total[2] = {0, 0};
+    for (int f = 0; f < 2; ++f) {
+        for (int l = 0; l < levels; ++l) {
+            if (kept[f][l] < 0 || kept[f][l] >= (1 << 24))
+                return fail(err, err_len, USLAM_INVALID_ARG, "match_noalloc: feature count out of range");
+            cap[f] = std::max(cap[f], kept[f][l]);
+            total[f] += kept[f][l];
+        }
+        if (total[f] > 0 && !feats[f]) return fail(err, err_len, USLAM_INVALID_ARG, "match_noalloc: null features");
+    }
+    if (out_cap_per_level < cap[0])
+        return fail(err, err_len, USLAM_INVALID_ARG, "match_noalloc: out_cap_per_level below the previous set's largest level");
+
+    // scratch layout: [tables][xorder f0][xorder f1][colstart f0][colstart f1][a2b][b2a][error word]
+    size_t cur = align256(sizeof(NoallocTables));
+    size_t xorder_off[2], colstart_off[2];
+    for (int f = 0; f < 2; ++f) {
+        xorder_off[f] = cur;
+        cur = align256(cur + sizeof(uint32_t) * static_cast<size_t>(levels) * cap[f]);
+    }
+    size_t colsum = 0;
+    for (int l = 0; l < levels; ++l) colsum += static_cast<size_t>(wl[l]) + 1;
+    for (int f = 0; f < 2; ++f) {
+        colstart_off[f] = cur;
+        cur = align256(cur + sizeof(uint32_t) * colsum);
+    }
+    const size_t a2b_off = cur;
+    cur = align256(cur + sizeof(int32_t) * static_cast<size_t>(levels) * cap[0]);
+    const size_t b2a_off = cur;
+    cur = align256(cur + sizeof(int32_t) * static_cast<size_t>(levels) * cap[1]);
+    const size_t err_off = cur;
+    cur += 256;
+    if (cur > kNoallocScratchBytes) {
+        char msg[160];
+        std::snprintf(msg, sizeof msg, "match_noalloc: needs %zu bytes of scratch, the fixed maximum is %zu", cur,
+                      kNoallocScratchBytes);
+        return fail(err, err_len, USLAM_CAPACITY, msg);
+    }
+
+    cudaError_t e = cudaSetDevice(device);
+    DeviceScratch ds;
+    if (e == cudaSuccess) e = scratch_for_device(device, &ds);
+    if (e != cudaSuccess) return fail(err, err_len, USLAM_CUDA_ERROR, cudaGetErrorString(e));
+    unsigned char* base = ds.ptr;
+    auto* dtab = reinterpret_cast<NoallocTables*>(base);
+
+    NoallocTables t;
+    std::memset(&t, 0, sizeof t);
+    for (int f = 0; f < 2; ++f) {
+        FrameDev& F = t.frames[f];
+        F.W0 = width;
+        F.H0 = height;
+        F.levels = levels;
+        F.cap = cap[f];
+        F.kept = reinterpret_cast<uint32_t*>(base + offsetof(NoallocTables, counts)) + f * 2 * USLAM_MAX_LEVELS;
+        F.raw = F.kept + levels;
+        size_t foff = 0, coff = 0;
+        for (int l = 0; l < levels; ++l) {
+            F.w[l] = wl[l];
+            F.h[l] = hl[l];
+            F.feats[l] = reinterpret_cast<uint32_t*>(const_cast<uslam_feature*>(feats[f]) + foff);
+            F.xorder[l] = reinterpret_cast<uint32_t*>(base + xorder_off[f]) + static_cast<size_t>(l) * cap[f];
+            F.colstart[l] = reinterpret_cast<uint32_t*>(base + colstart_off[f]) + coff;
+            t.counts[f][l] = static_cast<uint32_t>(kept[f][l]);
+            t.counts[f][levels + l] = static_cast<uint32_t>(kept[f][l]);
+            foff += static_cast<size_t>(kept[f][l]);
+            coff += static_cast<size_t>(wl[l]) + 1;
+            t.xsegs[f * levels + l] = SegDev{f, l};
+        }
+    }
+    PairDev& P = t.pair;
+    P.prev = 0;
+    P.curr = 1;
+    P.a2b = reinterpret_cast<int32_t*>(base + a2b_off);
+    P.b2a = reinterpret_cast<int32_t*>(base + b2a_off);
+    P.matches = reinterpret_cast<int32_t*>(out);
+    P.match_count = out_counts;
+    P.max_matches_per_level = out_cap_per_level;
+    // match_features_cpu.cpp:76-77: 0.1F * frame size, in f32
+    P.max_dx = 0.1f * static_cast<float>(static_cast<uint32_t>(width));
+    P.max_dy = 0.1f * static_cast<float>(static_cast<uint32_t>(height));
+    for (int l = 0; l < levels; ++l) {
+        t.msegs[2 * l] = MatchSegDev{0, 0, l};
+        t.msegs[2 * l + 1] = MatchSegDev{0, 1, l};
+        t.usegs[l] = SegDev{0, l};
+    }
+
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    uint32_t* derr = reinterpret_cast<uint32_t*>(base + err_off);
+    int max_w = 1;
+    for (int l = 0; l < levels; ++l) max_w = std::max(max_w, wl[l]);
+    k_noalloc_tables<<<1, 256, 0, st>>>(t, dtab);
+    e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemsetAsync(derr, 0, sizeof(uint32_t), st);  // the error word must start at zero
+    if (e == cudaSuccess) {
+        k_noalloc_xsort<<<2 * levels, kXsortThreads, (max_w + 1) * sizeof(uint32_t), st>>>(dtab->frames, dtab->xsegs);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = launch_match(dtab->frames, &dtab->pair, dtab->msegs, 2 * levels, ds.num_sms * 4, st);
+    if (e == cudaSuccess) e = launch_mutual(dtab->frames, &dtab->pair, dtab->usegs, levels, derr, st);
+    uint32_t word = 0;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&word, derr, sizeof word, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return fail(err, err_len, USLAM_CUDA_ERROR, cudaGetErrorString(e));
+    if (word != 0u) return fail(err, err_len, USLAM_KERNEL_CHECK, "match_noalloc: match list overflow");
+    if (err && err_len > 0) err[0] = '\0';
+    return USLAM_OK;
+}
