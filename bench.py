@@ -119,6 +119,20 @@ def summarize_clocks(lines: list[str]) -> dict:
     }
 
 
+# ------------------------------------------------------------------ ranks
+
+def reduce_max(value: float, dist, device: str) -> float:
+    """Max of a per-rank timing over all ranks (the whole job is as slow as
+    its slowest replica); identity without a process group."""
+    if dist is None:
+        return value
+    import torch
+
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 # ------------------------------------------------------------------ bytes
 
 def algorithmic_bytes(kept_per_frame: list[int], matches_per_pair: list[int], frames: int) -> dict:
@@ -273,11 +287,7 @@ def run_ours(a):
     wall_s = time.perf_counter() - t_wall
     clk = clocks.stop()
     step_ms = sum(e0.elapsed_time(e1) for e0, e1 in evs) / a.steps
-    step_ms_max = step_ms
-    if dist is not None:
-        t = torch.tensor([step_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        step_ms_max = float(t.item())
+    step_ms_max = reduce_max(step_ms, dist, "cuda")
     value = n * world / (step_ms_max / 1e3)
 
     # ---- results of one step (counts for the byte model)
@@ -325,11 +335,7 @@ def run_ours(a):
         batch.sync()
         e2e_times.append(time.perf_counter() - t0)
     barrier()
-    e2e_s = statistics.mean(e2e_times)
-    if dist is not None:
-        t = torch.tensor([e2e_s], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    e2e_s = reduce_max(statistics.mean(e2e_times), dist, "cuda")
     h2d, d2h = batch.io_bytes()
 
     # ---- plain per-frame form: one frame per launch sequence, synchronous

@@ -1,0 +1,73 @@
+"""Host-side logic of bench.py: the max-over-ranks reduction across two
+gloo ranks on CPU, the clock-log summary, the byte model, and the reference
+arm (CPU restatement on a process pool) end to end on a small workload."""
+import json
+import os
+import subprocess
+import sys
+
+import pytest
+import torch.distributed as dist
+import torch.multiprocessing as mp
+
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+sys.path.insert(0, REPO)
+import bench  # noqa: E402
+
+
+def _rank(rank, world, port, q):
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port), RANK=str(rank), WORLD_SIZE=str(world))
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    try:
+        q.put((rank, bench.reduce_max(10.0 + 5.0 * rank, dist, "cpu")))
+    finally:
+        dist.destroy_process_group()
+
+
+def test_reduce_max_over_two_gloo_ranks():
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = 29500 + (os.getpid() % 1000)
+    procs = [ctx.Process(target=_rank, args=(r, 2, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    out = dict(q.get(timeout=120) for _ in procs)
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    assert out == {0: 15.0, 1: 15.0}
+    assert bench.reduce_max(3.5, None, "cpu") == 3.5
+
+
+def test_clock_summary_flags_throttle_reasons():
+    lines = ["2070, 2070, 900.1, Not Active, Not Active, Not Active, Not Active",
+             "1980, 2070, 1390.5, Not Active, Not Active, Not Active, Active",
+             "2070, 2070, 1200.0, Not Active, Not Active, Not Active, Not Active", "garbage"]
+    c = bench.summarize_clocks(lines)
+    assert c["sm_mhz"] == 2070 and c["sm_max_mhz"] == 2070 and c["reasons"] == ["sw_power_cap"] and c["samples"] == 3
+
+
+def test_byte_model():
+    b = bench.algorithmic_bytes([100, 200, 300], [10, 20], 3)
+    wh = 752 * 480
+    assert b["pyramid_per_frame"] == wh + 4 * (1047287 - wh)
+    assert b["describe_total"] == 48 * 600
+    assert b["match_total"] == 32 * (600 + 300) + 8 * 30
+    assert b["total_per_step"] == 3 * b["pyramid_per_frame"] + b["describe_total"] + b["match_total"]
+
+
+def test_reference_arm_prints_one_line():
+    env = dict(os.environ)
+    r = subprocess.run([sys.executable, os.path.join(REPO, "bench.py"), "--impl", "reference", "--steps", "1",
+                        "--warmup", "0", "--frames", "3"], capture_output=True, text=True, env=env, timeout=600)
+    assert r.returncode == 0, r.stderr
+    line = json.loads(r.stdout.strip().splitlines()[-1])
+    assert line["impl"] == "reference" and line["unit"] == "frames/s" and line["value"] > 0
+    assert line["cpu_baseline"]["kind"] == "port" and line["e2e"]["h2d_bytes_per_step"] == 0
+
+
+def test_reference_arm_nonzero_rank_exits_quietly():
+    env = dict(os.environ, RANK="1", WORLD_SIZE="2")
+    r = subprocess.run([sys.executable, os.path.join(REPO, "bench.py"), "--impl", "reference", "--steps", "1",
+                        "--warmup", "0", "--frames", "2"], capture_output=True, text=True, env=env, timeout=300)
+    assert r.returncode == 0 and r.stdout.strip() == ""
