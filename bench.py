@@ -135,6 +135,19 @@ def reduce_max(value: float, dist, device: str) -> float:
 
 # ------------------------------------------------------------------ bytes
 
+def measured_traffic() -> dict:
+    """DRAM bytes per unit (frame or frame pair) of each kernel, from the
+    committed summary of one ncu capture."""
+    path = os.path.join(REPO, "profiles", "kernels_752x480_16frames.txt")
+    out = {}
+    if os.path.exists(path):
+        for line in open(path):
+            parts = line.split()
+            if len(parts) == 4 and parts[0] == "traffic":
+                out[parts[1]] = int(parts[3])
+    return out
+
+
 def algorithmic_bytes(kept_per_frame: list[int], matches_per_pair: list[int], frames: int) -> dict:
     """Per-frame algorithmic bytes of the path:
     W*H (u8 LOD0 read) + 4*(P - W*H) (f32 levels written) + 48*N (feature
@@ -202,7 +215,7 @@ def run_reference(a):
     from uni_slam_gb300 import synth
 
     pat = patmod.load()
-    frames = synth.config1_sequence(a.seed, n=a.frames)
+    frames = synth.plane_sequence(a.seed, n=a.frames)
     cores = os.cpu_count() or 1
     ctx = mp.get_context("spawn")
     times = []
@@ -254,7 +267,7 @@ def run_ours(a):
     from uni_slam_gb300 import synth
 
     pat = patmod.load()
-    frames = synth.config1_sequence(a.seed + rank, n=a.frames)
+    frames = synth.plane_sequence(a.seed + rank, n=a.frames)
     n = len(frames)
     ctx = Context(pat, levels=LEVELS, max_width=W, max_height=H, device=local)
     batch = Batch(ctx, [(W, H)] * n, [(i, i + 1) for i in range(n - 1)])
@@ -305,6 +318,9 @@ def run_ours(a):
         "k_describe": nbytes["describe_total"],
         "k_match": nbytes["match_total"],
     }
+    traffic_units = {"k_detect": n, "k_blur_border": n, "k_compact": n, "k_describe": n, "k_match": n - 1}
+    traffic_per_unit = measured_traffic()
+    dom_traffic = traffic_per_unit[dom] * traffic_units[dom] if dom in traffic_per_unit else None
     peaks = json.load(open(os.path.join(REPO, "MEASURED_PEAKS.json"))) if os.path.exists(
         os.path.join(REPO, "MEASURED_PEAKS.json")) else None
     peak = peaks["hbm_gbs"] if peaks else 6800.0
@@ -312,7 +328,8 @@ def run_ours(a):
     achieved = (dom_bytes / (prof[dom] / 1e3) / 1e9) if dom_bytes else None
     roofline = {
         "bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
-        "frac": (achieved / peak) if achieved else None, "traffic": None,
+        "frac": (achieved / peak) if achieved else None, "traffic": dom_traffic,
+        "traffic_source": "profiles/kernels_752x480_16frames.txt (16-frame ncu capture, scaled by frames / pairs)",
         "peak_source": "measured" if peaks else "fallback",
         "kernel_ms": prof, "algorithmic_bytes_per_launch": dom_bytes,
         "path_achieved": nbytes["total_per_step"] / (step_ms / 1e3) / 1e9,

@@ -106,13 +106,13 @@ def main():
 
     digests = {}
     for seed in (0, 1, 2):
-        f1, f2 = synth.config0_pair(seed)
-        digests[f"config0_pair/{seed}/0"] = synth.frame_digest(f1)
-        digests[f"config0_pair/{seed}/1"] = synth.frame_digest(f2)
+        f1, f2 = synth.warped_pair(seed)
+        digests[f"warped_pair/{seed}/0"] = synth.frame_digest(f1)
+        digests[f"warped_pair/{seed}/1"] = synth.frame_digest(f2)
     for seed in (0,):
-        frames = synth.config1_sequence(seed, n=3)
+        frames = synth.plane_sequence(seed, n=3)
         for i, f in enumerate(frames):
-            digests[f"config1_sequence/{seed}/{i}"] = synth.frame_digest(f)
+            digests[f"plane_sequence/{seed}/{i}"] = synth.frame_digest(f)
     with open(os.path.join(HERE, "synth_digests.json"), "w") as f:
         json.dump(digests, f, indent=1, sort_keys=True)
 

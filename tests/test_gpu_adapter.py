@@ -33,7 +33,7 @@ def _build(tmp_path):
 def test_wslam_passes_match_oracle(tmp_path, brief_pattern):
     exe = _build(tmp_path)
     W, H = 752, 480
-    frames = synth.config1_sequence(11, n=5)
+    frames = synth.plane_sequence(11, n=5)
     advance = [0, 0, 1, 0, 1]
     (tmp_path / "pattern.bin").write_bytes(np.ascontiguousarray(brief_pattern, "<i4").tobytes())
     with open(tmp_path / "frames.bin", "wb") as f:

@@ -45,7 +45,7 @@ def _assert_features_equal(got, exp):
 
 
 def test_pyramid_levels_bit_exact(ctx):
-    f1, _ = synth.config0_pair(0)
+    f1, _ = synth.warped_pair(0)
     b = _run(ctx, [f1])
     try:
         for l in range(1, 6):
@@ -56,7 +56,7 @@ def test_pyramid_levels_bit_exact(ctx):
 
 
 def test_blur_cache_bit_exact(ctx):
-    f1, _ = synth.config0_pair(1)
+    f1, _ = synth.warped_pair(1)
     b = _run(ctx, [f1])
     try:
         for l in range(6):
@@ -69,7 +69,7 @@ def test_blur_cache_bit_exact(ctx):
 def test_blur_cache_border_bit_exact(ctx):
     """Cells beyond the level edge and the negative-coordinate sentinels hold
     G(P) of generate_features.wgsl:149-172 at those points (u32-wrapped)."""
-    f1, _ = synth.config0_pair(2)
+    f1, _ = synth.warped_pair(2)
     m = ctx.blur_margin()
     b = _run(ctx, [f1])
     try:
@@ -95,7 +95,7 @@ def test_blur_cache_border_bit_exact(ctx):
 
 def test_keypoint_maps_bit_exact(ctx):
     for seed in (0, 3):
-        f1, _ = synth.config0_pair(seed)
+        f1, _ = synth.warped_pair(seed)
         b = _run(ctx, [f1])
         try:
             for l in range(6):
@@ -108,7 +108,7 @@ def test_keypoint_maps_bit_exact(ctx):
 
 @pytest.mark.parametrize("seed", [0, 1, 2])
 def test_features_and_matches_bit_exact(ctx, brief_pattern, seed):
-    f1, f2 = synth.config0_pair(seed)
+    f1, f2 = synth.warped_pair(seed)
     b = _run(ctx, [f1, f2], [(0, 1)])
     try:
         got = [b.features(i) for i in range(2)]
@@ -130,7 +130,7 @@ def test_uneven_batch_equals_oracle_and_alone(ctx, brief_pattern):
     sizes = [(640, 480), (752, 480), (1280, 720), (97, 61), (333, 211)]
     frames, pairs = [], []
     for k, (w, h) in enumerate(sizes):
-        a, c = synth.config0_pair(100 + k, w, h)
+        a, c = synth.warped_pair(100 + k, w, h)
         frames += [a, c]
         pairs.append((2 * k, 2 * k + 1))
     b = _run(ctx, frames, pairs)
@@ -153,7 +153,7 @@ def test_uneven_batch_equals_oracle_and_alone(ctx, brief_pattern):
 
 
 def test_repeat_runs_are_identical(ctx):
-    frames = synth.config1_sequence(5, n=4)
+    frames = synth.plane_sequence(5, n=4)
     b = Batch(ctx, [(752, 480)] * 4, [(0, 1), (1, 2), (2, 3)])
     try:
         b.process(frames)
@@ -170,8 +170,8 @@ def test_repeat_runs_are_identical(ctx):
 def test_constant_and_tiny_frames(brief_pattern):
     with Context(brief_pattern, levels=6, max_width=64, max_height=64, cap_per_level=50) as c:
         flat = np.full((48, 64), 77, np.uint8)
-        tiny = synth.config_frame(9, 10, 10)
-        odd = synth.config_frame(11, 37, 23)
+        tiny = synth.scene_frame(9, 10, 10)
+        odd = synth.scene_frame(11, 37, 23)
         frames = [flat, flat, tiny, tiny, odd]
         b = _run(c, frames, [(0, 1), (2, 3)])
         try:
@@ -185,7 +185,7 @@ def test_constant_and_tiny_frames(brief_pattern):
 
 
 def test_cap_keeps_first_in_yx_order(brief_pattern):
-    f1, _ = synth.config0_pair(4)
+    f1, _ = synth.warped_pair(4)
     with Context(brief_pattern, levels=6, max_width=752, max_height=480, cap_per_level=100) as c:
         b = _run(c, [f1])
         try:
@@ -200,7 +200,7 @@ def test_cap_keeps_first_in_yx_order(brief_pattern):
 def test_frontend_rotation_matches_reference_rule(ctx, brief_pattern):
     """FeatureSet(1) advances on the marker or when absent
     (load_features_cpu.cpp:111-142); matching is FeatureSet(1) -> FeatureSet(0)."""
-    frames = synth.config1_sequence(7, n=6)
+    frames = synth.plane_sequence(7, n=6)
     advance = [False, False, False, True, False, True]
     fe = Frontend(ctx, 752, 480)
     try:

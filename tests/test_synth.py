@@ -11,13 +11,13 @@ DIG = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "synth_di
 
 @pytest.mark.parametrize("seed", [0, 1, 2])
 def test_config0_digests(seed):
-    f1, f2 = synth.config0_pair(seed)
+    f1, f2 = synth.warped_pair(seed)
     assert f1.shape == (480, 752) and f1.dtype.name == "uint8"
-    assert synth.frame_digest(f1) == DIG[f"config0_pair/{seed}/0"]
-    assert synth.frame_digest(f2) == DIG[f"config0_pair/{seed}/1"]
+    assert synth.frame_digest(f1) == DIG[f"warped_pair/{seed}/0"]
+    assert synth.frame_digest(f2) == DIG[f"warped_pair/{seed}/1"]
 
 
 def test_config1_digests():
-    frames = synth.config1_sequence(0, n=3)
+    frames = synth.plane_sequence(0, n=3)
     for i, f in enumerate(frames):
-        assert synth.frame_digest(f) == DIG[f"config1_sequence/0/{i}"]
+        assert synth.frame_digest(f) == DIG[f"plane_sequence/0/{i}"]

@@ -23,7 +23,7 @@ def test_noalloc_match_equals_batch_path(brief_pattern):
     W, H, L = 752, 480, 6
     frames = []
     for seed in (21, 22):
-        frames += list(synth.config0_pair(seed))
+        frames += list(synth.warped_pair(seed))
     with Context(brief_pattern, levels=L, max_width=W, max_height=H) as ctx:
         b = Batch(ctx, [(W, H)] * 4, [(0, 1), (2, 3)])
         try:

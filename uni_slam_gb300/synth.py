@@ -1,18 +1,18 @@
 """Seeded synthetic camera frames standing in for EuRoC (not available here).
 
-Generators follow the benchmark configurations:
-  * ``config0_pair``  — one 752x480 frame pair: background 128, 200 rectangles
+Generators:
+  * ``warped_pair``  — one 752x480 frame pair: background 128, 200 rectangles
     (sides U[8,80], intensity U[0,255]), 50 checkerboard patches of 8x8 cells
     (cell side U{2..6}, two intensities U[0,255]), additive N(0, 4^2) noise
     blurred with a sigma=1 Gaussian, clamp to u8.  Frame 2 is frame 1's
     noiseless content warped by a homography (rotation U[-5,5] deg, translation
     U[-10,10] px, scale U[0.97,1.03] about the centre) with fresh noise.
-  * ``config1_sequence`` — consecutive 752x480 frames of a camera flying over
-    a textured plane (a 4096x4096 config-0 texture with element counts scaled
-    by area), translation 2-5 cm and rotation 0.5-2 deg per frame, bilinear
-    homography rendering, N(0, 3^2) noise.
-  * ``config_frame`` — one frame of any size from the config-0 recipe with
-    counts scaled by area (the uneven-size batch).
+  * ``plane_sequence`` — consecutive 752x480 frames of a camera flying over
+    a textured plane (a 4096x4096 texture of the same recipe, element counts
+    scaled by area), translation 2-5 cm and rotation 0.5-2 deg per frame,
+    bilinear homography rendering, N(0, 3^2) noise.
+  * ``scene_frame`` — one frame of any size from the same recipe with counts
+    scaled by area (the uneven-size batch).
 
 The legacy ``numpy.random.RandomState`` stream is used: it is frozen across
 numpy versions, so a seed names the same frame everywhere.
@@ -123,7 +123,7 @@ def _counts(w: int, h: int, n_rect: int, n_check: int, scale_by_area: bool) -> t
     return max(1, int(round(n_rect * f))), max(1, int(round(n_check * f)))
 
 
-def config_frame(seed: int, w: int = BASE_W, h: int = BASE_H, n_rect: int = 200, n_check: int = 50,
+def scene_frame(seed: int, w: int = BASE_W, h: int = BASE_H, n_rect: int = 200, n_check: int = 50,
                  scale_by_area: bool = True) -> np.ndarray:
     rs = np.random.RandomState(seed)
     nr, nc = _counts(w, h, n_rect, n_check, scale_by_area)
@@ -131,7 +131,7 @@ def config_frame(seed: int, w: int = BASE_W, h: int = BASE_H, n_rect: int = 200,
     return _to_u8(content + _noise(rs, w, h, 4.0, 1.0))
 
 
-def config0_pair(seed: int, w: int = BASE_W, h: int = BASE_H, n_rect: int = 200, n_check: int = 50,
+def warped_pair(seed: int, w: int = BASE_W, h: int = BASE_H, n_rect: int = 200, n_check: int = 50,
                  scale_by_area: bool = True) -> tuple[np.ndarray, np.ndarray]:
     rs = np.random.RandomState(seed)
     nr, nc = _counts(w, h, n_rect, n_check, scale_by_area)
@@ -195,7 +195,7 @@ class PlaneTrajectory:
         return out
 
 
-def config1_sequence(seed: int, n: int = 64, w: int = BASE_W, h: int = BASE_H) -> list[np.ndarray]:
+def plane_sequence(seed: int, n: int = 64, w: int = BASE_W, h: int = BASE_H) -> list[np.ndarray]:
     return PlaneTrajectory(seed, w, h).frames(n)
 
 
