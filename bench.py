@@ -11,7 +11,8 @@ HBM (graph replay of the 5-kernel batch, L2 flushed between steps);
 ``e2e`` = the same through the C ABI with pinned-host H2D of the frames and
 D2H of every feature record and match list inside the timed region;
 ``plain_fps`` = the plain per-frame form (one frame per launch sequence,
-synchronous per frame).  ``--impl reference`` times the CPU restatement of
+synchronous per frame); ``served`` = 32 camera streams at 20 Hz through the
+serving loop (p50/p99 latency, frames/s).  ``--impl reference`` times the CPU restatement of
 the reference's path (oracle port) on all host cores, on the same workload.
 """
 from __future__ import annotations
@@ -43,6 +44,8 @@ def _args():
     ap.add_argument("--frames", type=int, default=64)
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="bounded CPU-baseline sample")
+    ap.add_argument("--serve-seconds", type=float, default=10.0, help="served-form simulation length (0: skip)")
+    ap.add_argument("--serve-streams", type=int, default=32)
     return ap.parse_args()
 
 
@@ -243,6 +246,83 @@ def run_reference(a):
     print(json.dumps(line), flush=True)
 
 
+# ------------------------------------------------------------------ served form
+
+SERVE_SIZES = [(640, 480), (752, 480), (1280, 720)]
+
+
+def serve_simulation(ctx, seconds: float, n_streams: int = 32, rate_hz: float = 20.0, promote_every: int = 10,
+                     seed: int = 0, frames_per_stream: int = 6) -> dict:
+    """Camera streams of sizes drawn from 640x480 / 752x480 / 1280x720, each
+    sending plane-trajectory frames at rate_hz with exponential inter-arrival
+    times (mean 1/rate_hz), a new keyframe every promote_every frames,
+    through the server (HBM-budget admission, continuous batching).  Latency
+    runs from a frame's scheduled arrival to its completion, so admission
+    waits count."""
+    import heapq
+    import queue
+
+    import numpy as np
+
+    from uni_slam_gb300 import Server, synth
+
+    rs = np.random.RandomState(seed + 7)
+    tex = synth.plane_texture(np.random.RandomState(seed + 11), 4096)
+    sizes = [SERVE_SIZES[rs.randint(len(SERVE_SIZES))] for _ in range(n_streams)]
+    frames = [synth.plane_sequence(1000 + k, frames_per_stream, w, h, texture=tex) for k, (w, h) in enumerate(sizes)]
+    srv = Server(ctx, SERVE_SIZES, hbm_budget_bytes=8 << 30, max_batch=64)
+    ids = [srv.open_stream(w, h) for (w, h) in sizes]
+    count = [0] * n_streams
+    done_q: queue.Queue = queue.Queue()
+    lat: list[float] = []
+
+    def completer():
+        while True:
+            item = done_q.get()
+            if item is None:
+                return
+            tk, admit_delay_ms = item
+            srv.wait(tk, 0)
+            lat.append(admit_delay_ms + srv.latency_ms(tk))
+            srv.release(tk)
+
+    th = threading.Thread(target=completer, daemon=True)
+    th.start()
+    start = time.perf_counter() + 0.05
+    end = start + seconds
+    heap = [(start + rs.exponential(1.0 / rate_hz), k) for k in range(n_streams)]
+    heapq.heapify(heap)
+    refused = 0
+    while heap and heap[0][0] < end:
+        t_sched, k = heapq.heappop(heap)
+        now = time.perf_counter()
+        if t_sched > now:
+            time.sleep(t_sched - now)
+        img = frames[k][count[k] % frames_per_stream]
+        while True:
+            tk = srv.submit(ids[k], img, promote=(count[k] % promote_every == 0))
+            if tk is not None:
+                break
+            refused += 1
+            time.sleep(50e-6)
+        done_q.put((tk, (time.perf_counter() - t_sched) * 1e3))
+        count[k] += 1
+        heapq.heappush(heap, (t_sched + rs.exponential(1.0 / rate_hz), k))
+    done_q.put(None)
+    th.join()
+    elapsed = time.perf_counter() - start
+    st = srv.stats()
+    srv.close()
+    arr = np.array(lat)
+    return {
+        "streams": n_streams, "rate_hz_per_stream": rate_hz, "seconds": seconds, "frames": int(arr.size),
+        "fps": arr.size / elapsed, "p50_ms": float(np.percentile(arr, 50)), "p99_ms": float(np.percentile(arr, 99)),
+        "max_ms": float(arr.max()), "admission_retries": refused, "launches": st["launches"],
+        "max_batch_seen": st["max_batch_seen"], "slots": st["slots"],
+        "sizes": {f"{w}x{h}": sizes.count((w, h)) for (w, h) in SERVE_SIZES},
+    }
+
+
 # ------------------------------------------------------------------ GPU side
 
 def run_ours(a):
@@ -371,6 +451,13 @@ def run_ours(a):
     plain_fps = n / plain_s
     fe.close()
 
+    served = None
+    if a.serve_seconds > 0:
+        # keyframes hold up to 2000 descriptors: 333 per level x 6 levels
+        sctx = Context(pat, levels=LEVELS, max_width=1280, max_height=720, cap_per_level=333, device=local)
+        served = serve_simulation(sctx, a.serve_seconds, n_streams=a.serve_streams, seed=a.seed + rank)
+        sctx.close()
+
     cpu = None
     if rank == 0:
         cpu = cpu_baseline_sample(frames, pat, a.cpu_seconds)
@@ -388,6 +475,7 @@ def run_ours(a):
             "e2e": {"value": n * world / e2e_s, "unit": "frames/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
             "gpu_launches": 6 * a.steps, "roofline": roofline, "cpu_baseline": cpu, "clocks": clk,
+            "served": served,
             "features_per_frame": sum(kept) / n, "matches_per_pair": sum(nmatch) / max(1, n - 1),
             "wall_s_timed": wall_s,
         }

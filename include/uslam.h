@@ -171,6 +171,45 @@ uslam_status uslam_frontend_enqueue(uslam_frontend* fe, const uint8_t* dev_img, 
                                     int* matched);
 uslam_status uslam_frontend_sync(uslam_frontend* fe);
 
+/* ---- served form: many camera streams, continuous batching -------------- */
+
+typedef struct uslam_server uslam_server;
+
+typedef struct uslam_server_params {
+    int n_sizes;              /* frame size classes served */
+    const int* widths;        /* [n_sizes] */
+    const int* heights;       /* [n_sizes] */
+    size_t hbm_budget_bytes;  /* device memory for frame slots, shared equally by the size classes */
+    int max_batch;            /* most frames one launch takes */
+} uslam_server_params;
+
+/* Frame slots (pyramid, features, keyframe pair scratch) are carved from the
+ * budget; admission is by free slot.  A dispatcher thread launches the
+ * queued frames as one batch whenever fewer than two launches are in flight,
+ * on two alternating streams.  Each stream's keyframe features stay in their
+ * slot on the device (the counterpart of FeatureSet(1),
+ * load_features_cpu.cpp:111-142) and every new frame is matched against it. */
+uslam_status uslam_server_create(uslam_ctx* ctx, const uslam_server_params* params, uslam_server** out);
+void uslam_server_destroy(uslam_server* server);
+uslam_status uslam_server_open_stream(uslam_server* server, int width, int height, int* stream_id);
+/* Copy a frame into a free slot and queue it.  promote_keyframe: this frame
+ * becomes the stream's keyframe for the frames submitted after it (a
+ * stream's first frame always does).  USLAM_CAPACITY: no free slot of that
+ * size right now (admission refused; retry later). */
+uslam_status uslam_server_submit(uslam_server* server, int stream, const uint8_t* img, int pitch,
+                                 int promote_keyframe, uint64_t* ticket);
+uslam_status uslam_server_wait(uslam_server* server, uint64_t ticket, int timeout_ms);
+/* Features of the frame (as uslam_batch_features) and its mutual matches
+ * against the keyframe it was submitted against (lod_a/idx_a = keyframe).
+ * latency_ms = submit to completion seen by the dispatcher.  Returns
+ * USLAM_NOT_READY (features filled, no matches) for a stream's first frame. */
+uslam_status uslam_server_result(uslam_server* server, uint64_t ticket, uslam_feature* feats, int max_feats, int* kept,
+                                 int* raw, uslam_match* matches, int max_matches, int* n_matches, double* latency_ms);
+/* Give the request's slot back (it stays held while it is a keyframe). */
+uslam_status uslam_server_release(uslam_server* server, uint64_t ticket);
+uslam_status uslam_server_stats(uslam_server* server, uint64_t* launches, uint64_t* frames, int* max_batch_seen,
+                                int* slots_total);
+
 /* ---- matcher for callers that cannot allocate ---------------------------- */
 
 /* No counterpart in the reference.  For callers that cannot call cudaMalloc

@@ -23,7 +23,7 @@ NVCC_FLAGS = ARCH + [
     "-Xcompiler", "-fPIC,-ffp-contract=off",
     "-I", os.path.join(REPO, "include"),
 ]
-SOURCES = ["kernels.cu", "runtime.cu", "noalloc.cu"]
+SOURCES = ["kernels.cu", "runtime.cu", "server.cu", "noalloc.cu"]
 
 
 def _nvcc() -> str:
@@ -44,7 +44,7 @@ def build_library(force: bool = False, verbose: bool = False) -> str:
     """Compile csrc/*.cu into libuslam.so (translation units in parallel)."""
     os.makedirs(BUILD_DIR, exist_ok=True)
     nvcc = _nvcc()
-    headers = [os.path.join(CSRC, h) for h in os.listdir(CSRC) if h.endswith(".h")]
+    headers = [os.path.join(CSRC, h) for h in os.listdir(CSRC) if h.endswith((".h", ".hpp"))]
     headers += [os.path.join(REPO, "include", h) for h in os.listdir(os.path.join(REPO, "include"))]
     objs = []
     jobs = []

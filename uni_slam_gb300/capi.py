@@ -27,6 +27,13 @@ MATCH_DTYPE = np.dtype([("lod_a", "<i4"), ("idx_a", "<i4"), ("lod_b", "<i4"), ("
 assert FEATURE_DTYPE.itemsize == 48 and MATCH_DTYPE.itemsize == 16
 
 
+class ServerParams(C.Structure):
+    _fields_ = [
+        ("n_sizes", C.c_int), ("widths", C.POINTER(C.c_int)), ("heights", C.POINTER(C.c_int)),
+        ("hbm_budget_bytes", C.c_size_t), ("max_batch", C.c_int),
+    ]
+
+
 class Params(C.Structure):
     _fields_ = [
         ("device", C.c_int), ("levels", C.c_int), ("max_width", C.c_int), ("max_height", C.c_int),
@@ -73,6 +80,15 @@ SIGNATURES = {
     "uslam_frontend_matches": (C.c_int, [_vp, _vp, C.c_int, _ip]),
     "uslam_frontend_enqueue": (C.c_int, [_vp, _vp, C.c_int, C.c_int, _ip]),
     "uslam_frontend_sync": (C.c_int, [_vp]),
+    "uslam_server_create": (C.c_int, [_vp, C.POINTER(ServerParams), C.POINTER(_vp)]),
+    "uslam_server_destroy": (None, [_vp]),
+    "uslam_server_open_stream": (C.c_int, [_vp, C.c_int, C.c_int, _ip]),
+    "uslam_server_submit": (C.c_int, [_vp, C.c_int, _vp, C.c_int, C.c_int, C.POINTER(C.c_uint64)]),
+    "uslam_server_wait": (C.c_int, [_vp, C.c_uint64, C.c_int]),
+    "uslam_server_result": (C.c_int, [_vp, C.c_uint64, _vp, C.c_int, _ip, _ip, _vp, C.c_int, _ip,
+                                      C.POINTER(C.c_double)]),
+    "uslam_server_release": (C.c_int, [_vp, C.c_uint64]),
+    "uslam_server_stats": (C.c_int, [_vp, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64), _ip, _ip]),
     "uslam_match_noalloc": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, _vp, _ip, _vp, _ip, _vp, _vp, C.c_int,
                                       _vp, C.c_char_p, C.c_size_t]),
 }

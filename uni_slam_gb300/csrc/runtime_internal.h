@@ -1,0 +1,160 @@
+// runtime_internal.h — host-runtime internals shared by the batch runtime
+// (runtime.cu) and the serving loop (server.cu): kernel launchers, level
+// dimensions, the cull coverage bitmap and the device context.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "../../include/uslam.h"
+#include "uslam_internal.h"
+
+namespace uslam {
+struct MatchSegDev {
+    int pair;
+    int dir;
+    int level;
+};
+cudaError_t init_constants();
+cudaError_t launch_detect(const FrameDev*, const TileItem*, int, uint32_t*, cudaStream_t);
+cudaError_t launch_compact(const FrameDev*, const SegDev*, int, int, cudaStream_t);
+cudaError_t launch_blur_border(const FrameDev*, const SegDev*, int, int, cudaStream_t);
+cudaError_t launch_describe(const FrameDev*, const SegDev*, int, const int32_t*, int, cudaStream_t);
+cudaError_t launch_match(const FrameDev*, const PairDev*, const void*, int, int, cudaStream_t);
+cudaError_t launch_mutual(const FrameDev*, const PairDev*, const SegDev*, int, uint32_t*, cudaStream_t);
+cudaError_t set_compact_smem(int max_w);
+constexpr int kTileW = 64;
+constexpr int kTileH = 16;
+constexpr int kMaxSegs = 4096;
+constexpr int kMaxWidth = 8192;
+}  // namespace uslam
+
+using namespace uslam;
+
+namespace uslam_rt {
+
+inline size_t round_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+
+inline uslam_status set_err(std::string* dst, uslam_status s, const std::string& msg) {
+    if (dst) *dst = msg;
+    return s;
+}
+
+// Level dims (wslam/src/common.cpp:41-45).
+inline void level_dims(int W0, int H0, int levels, int* w, int* h) {
+    for (int l = 0; l < levels; ++l) {
+        const double factor = l == 0 ? 1.0 : std::pow(1.2, static_cast<double>(l));
+        w[l] = static_cast<int>(static_cast<uint32_t>(static_cast<double>(W0) / factor));
+        h[l] = static_cast<int>(static_cast<uint32_t>(static_cast<double>(H0) / factor));
+    }
+}
+
+inline uint32_t ceil_div_u(uint32_t n, uint32_t d) { return (n + d - 1u) / d; }
+
+// Coverage of the reference's cull passes for one level, as a bitmap.
+// main_horizontal (resources/cull_corners.wgsl:22-57) with dispatch
+// ceil(ceil(W0/3)/64) x H0 x levels workgroups of 64 (cull_corners.cpp:332-341)
+// writes H[9*gx + y*w] = S for every start >= w (the regional loop is empty
+// there because end = min(start+3, w) <= start); in row 0 it keeps the first
+// arg-max of [9k, min(9k+3, w)).  main_vertical (:60-109) with dispatch
+// ceil(W0/64) x ceil(H0/3) copies H at start + k*w, k < min((W0*H0 - start)/w, 3),
+// start = 3*gx + 3*gy*w, and at start itself in every case.  A keypoint is a pixel whose final value is > 0, so:
+//   bit(p) = V(p) && (p < w ? p % 9 < 3 : H(p)),
+// with the row-0 arg-max applied in the kernel.
+inline std::vector<uint32_t> build_cull_mask(int W0, int H0, int w, int h) {
+    const uint64_t n = static_cast<uint64_t>(w) * static_cast<uint64_t>(h);
+    const uint64_t blk = static_cast<uint64_t>(W0) * static_cast<uint64_t>(H0);
+    std::vector<uint8_t> mh(n, 0), mv(n, 0);
+    const uint32_t gx_h = ceil_div_u(ceil_div_u(W0, 3), 64) * 64;
+    const uint32_t gy_h = static_cast<uint32_t>(H0);
+    const uint32_t gx_v = ceil_div_u(W0, 64) * 64;
+    const uint32_t gy_v = ceil_div_u(H0, 3);
+    for (uint32_t y = 0; y < gy_h; ++y)
+        for (uint32_t gx = 0; gx < gx_h; ++gx) {
+            const uint64_t s = 9ull * gx + static_cast<uint64_t>(y) * w;
+            if (s < n && s >= static_cast<uint64_t>(w)) mh[s] = 1;
+        }
+    for (uint32_t gy = 0; gy < gy_v; ++gy)
+        for (uint32_t gx = 0; gx < gx_v; ++gx) {
+            const uint64_t s = 3ull * gx + 3ull * gy * static_cast<uint64_t>(w);
+            if (s >= n) continue;
+            // didFindMax starts as src[start] > 0, so V[start] = H[start] even
+            // when the loop below is empty (cull_corners.wgsl:83-97)
+            mv[s] = 1;
+            uint64_t cnt = (blk - s) / static_cast<uint64_t>(w);
+            if (cnt > 3) cnt = 3;
+            for (uint64_t k = 0; k < cnt; ++k) {
+                const uint64_t i = s + k * static_cast<uint64_t>(w);
+                if (i < n) mv[i] = 1;
+            }
+        }
+    std::vector<uint32_t> bits((n + 31) / 32, 0u);
+    for (uint64_t p = 0; p < n; ++p) {
+        const bool keep = mv[p] && (p < static_cast<uint64_t>(w) ? (p % 9) < 3 : mh[p] != 0);
+        if (keep) bits[p >> 5] |= 1u << (p & 31);
+    }
+    return bits;
+}
+
+struct ResClass {
+    int W0 = 0, H0 = 0;
+    std::vector<uint32_t*> d_mask;
+};
+
+}  // namespace uslam_rt
+
+using namespace uslam_rt;
+
+struct uslam_ctx {
+    int device = 0;
+    int levels = 6;
+    int max_w = 0, max_h = 0;
+    int cap_override = 0;
+    int num_sms = 0;
+    int margin = 0;  // blur-cache margin: BRIEF pattern radius + 2
+    int32_t* d_pattern = nullptr;
+    std::string err;
+    std::map<std::pair<int, int>, ResClass> classes;
+
+    uslam_status cuda_fail(cudaError_t e, const char* what) {
+        err = std::string(what) + ": " + cudaGetErrorString(e);
+        return USLAM_CUDA_ERROR;
+    }
+    // Masks of a resolution class, built and uploaded on first use.
+    uslam_status masks_for(int W0, int H0, const int* w, const int* h, std::vector<uint32_t*>* out) {
+        auto key = std::make_pair(W0, H0);
+        auto it = classes.find(key);
+        if (it == classes.end()) {
+            ResClass rc;
+            rc.W0 = W0;
+            rc.H0 = H0;
+            for (int l = 0; l < levels; ++l) {
+                const std::vector<uint32_t> bits = build_cull_mask(W0, H0, w[l], h[l]);
+                uint32_t* d = nullptr;
+                cudaError_t e = cudaMalloc(&d, bits.size() * sizeof(uint32_t));
+                if (e != cudaSuccess) {
+                    for (auto* p : rc.d_mask) cudaFree(p);
+                    err = std::string("cull mask allocation: ") + cudaGetErrorString(e);
+                    return e == cudaErrorMemoryAllocation ? USLAM_OOM : USLAM_CUDA_ERROR;
+                }
+                e = cudaMemcpy(d, bits.data(), bits.size() * sizeof(uint32_t), cudaMemcpyHostToDevice);
+                if (e != cudaSuccess) {
+                    cudaFree(d);
+                    for (auto* p : rc.d_mask) cudaFree(p);
+                    return cuda_fail(e, "cull mask upload");
+                }
+                rc.d_mask.push_back(d);
+            }
+            it = classes.emplace(key, std::move(rc)).first;
+        }
+        *out = it->second.d_mask;
+        return USLAM_OK;
+    }
+};

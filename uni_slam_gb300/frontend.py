@@ -242,3 +242,74 @@ class Frontend:
         if self.h:
             self.lib.uslam_frontend_destroy(self.h)
             self.h = None
+
+
+class Server:
+    """Served form: camera streams, HBM-budget admission, continuous batching."""
+
+    def __init__(self, ctx: Context, sizes: list[tuple[int, int]], hbm_budget_bytes: int = 4 << 30,
+                 max_batch: int = 64):
+        self.ctx = ctx
+        self.lib = ctx.lib
+        self._w = np.array([s[0] for s in sizes], np.int32)
+        self._h = np.array([s[1] for s in sizes], np.int32)
+        p = capi.ServerParams(len(sizes), iptr(self._w), iptr(self._h), hbm_budget_bytes, max_batch)
+        h = C.c_void_p()
+        ctx.check(self.lib.uslam_server_create(ctx.h, C.byref(p), C.byref(h)), "server_create")
+        self.h = h
+
+    def open_stream(self, width: int, height: int) -> int:
+        sid = C.c_int()
+        self.ctx.check(self.lib.uslam_server_open_stream(self.h, width, height, C.byref(sid)), "open_stream")
+        return sid.value
+
+    def submit(self, stream: int, img: np.ndarray, promote: bool = False) -> int | None:
+        """Ticket of the queued frame, or None when admission is refused (no free slot)."""
+        img = np.ascontiguousarray(img, np.uint8)
+        t = C.c_uint64()
+        st = self.lib.uslam_server_submit(self.h, stream, ptr(img), img.shape[1], int(promote), C.byref(t))
+        if st == capi.CAPACITY:
+            return None
+        self.ctx.check(st, "submit")
+        return t.value
+
+    def wait(self, ticket: int, timeout_ms: int = 0):
+        self.ctx.check(self.lib.uslam_server_wait(self.h, ticket, timeout_ms), "wait")
+
+    def result(self, ticket: int):
+        """(features, kept, raw, matches or None, latency_ms)."""
+        L = self.ctx.levels
+        kept = np.zeros(L, np.int32)
+        raw = np.zeros(L, np.int32)
+        nm = C.c_int()
+        lat = C.c_double()
+        st = self.lib.uslam_server_result(self.h, ticket, None, 0, iptr(kept), iptr(raw), None, 0, C.byref(nm),
+                                          C.byref(lat))
+        self.ctx.check(st, "result", ok=(capi.OK, capi.NOT_READY))
+        feats = np.zeros(int(kept.sum()), FEATURE_DTYPE)
+        m = np.zeros(nm.value, MATCH_DTYPE)
+        st = self.lib.uslam_server_result(self.h, ticket, ptr(feats), feats.size, iptr(kept), iptr(raw), ptr(m),
+                                          m.size, C.byref(nm), C.byref(lat))
+        self.ctx.check(st, "result", ok=(capi.OK, capi.NOT_READY))
+        return feats, kept, raw, (m if st == capi.OK else None), lat.value
+
+    def latency_ms(self, ticket: int) -> float:
+        """Submit-to-completion time of a finished request (no data copied)."""
+        lat = C.c_double()
+        st = self.lib.uslam_server_result(self.h, ticket, None, 0, None, None, None, 0, None, C.byref(lat))
+        self.ctx.check(st, "result", ok=(capi.OK, capi.NOT_READY))
+        return lat.value
+
+    def release(self, ticket: int):
+        self.ctx.check(self.lib.uslam_server_release(self.h, ticket), "release")
+
+    def stats(self) -> dict:
+        a, b = C.c_uint64(), C.c_uint64()
+        c, d = C.c_int(), C.c_int()
+        self.ctx.check(self.lib.uslam_server_stats(self.h, C.byref(a), C.byref(b), C.byref(c), C.byref(d)), "stats")
+        return {"launches": a.value, "frames": b.value, "max_batch_seen": c.value, "slots": d.value}
+
+    def close(self):
+        if self.h:
+            self.lib.uslam_server_destroy(self.h)
+            self.h = None

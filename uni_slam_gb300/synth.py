@@ -146,12 +146,14 @@ class PlaneTrajectory:
     """Camera over a textured plane; frames rendered by bilinear homography."""
 
     def __init__(self, seed: int, w: int = BASE_W, h: int = BASE_H, tex_size: int = 4096,
-                 texel_m: float = 0.004, depth_m: float = 2.0, focal_px: float = 460.0):
+                 texel_m: float = 0.004, depth_m: float = 2.0, focal_px: float = 460.0,
+                 texture: np.ndarray | None = None):
         self.rs = np.random.RandomState(seed)
         self.w, self.h = w, h
-        nr, nc = _counts(tex_size, tex_size, 200, 50, True)
-        self.tex = _content(self.rs, tex_size, tex_size, nr, nc)
-        self.tex += _noise(self.rs, tex_size, tex_size, 4.0, 1.0)
+        if texture is None:
+            texture = plane_texture(self.rs, tex_size)
+        self.tex = texture
+        tex_size = texture.shape[0]
         self.texel_m = texel_m
         self.tex_size = tex_size
         self.K = np.array([[focal_px, 0.0, (w - 1) / 2.0], [0.0, focal_px, (h - 1) / 2.0], [0.0, 0.0, 1.0]])
@@ -195,8 +197,17 @@ class PlaneTrajectory:
         return out
 
 
-def plane_sequence(seed: int, n: int = 64, w: int = BASE_W, h: int = BASE_H) -> list[np.ndarray]:
-    return PlaneTrajectory(seed, w, h).frames(n)
+def plane_texture(rs: np.random.RandomState, tex_size: int = 4096) -> np.ndarray:
+    """The textured plane: the frame recipe at tex_size^2, counts scaled by area."""
+    nr, nc = _counts(tex_size, tex_size, 200, 50, True)
+    tex = _content(rs, tex_size, tex_size, nr, nc)
+    tex += _noise(rs, tex_size, tex_size, 4.0, 1.0)
+    return tex
+
+
+def plane_sequence(seed: int, n: int = 64, w: int = BASE_W, h: int = BASE_H,
+                   texture: np.ndarray | None = None) -> list[np.ndarray]:
+    return PlaneTrajectory(seed, w, h, texture=texture).frames(n)
 
 
 def frame_digest(img: np.ndarray) -> str:
