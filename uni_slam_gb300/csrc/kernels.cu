@@ -20,7 +20,7 @@ namespace uslam {
 
 // K1 tile geometry: TW x TH output pixels, halo HX columns / HY rows.
 constexpr int TW = 64;
-constexpr int TH = 16;
+constexpr int TH = 32;
 constexpr int HX = 5;
 constexpr int HY = 3;
 constexpr int SW = TW + 2 * HX;
@@ -80,6 +80,8 @@ __device__ float pyramid_pixel(const FrameDev& F, int l, int x, int y) {
 // |centre - p_i| > 0.15, kept iff > 9 (detect_corners.wgsl:58-81).
 __device__ __forceinline__ uint32_t fast_response(const float (*sm)[SW], int r, int c) {
     const float center = sm[r][c];
+    // every non-wrapping run of >= 9 of the 16 points contains points 7 and 8
+    if (!(fabsf(center - sm[r + 3][c + 1]) > 0.15f && fabsf(center - sm[r + 3][c]) > 0.15f)) return 0u;
     uint32_t m = 0;
 #pragma unroll
     for (int i = 0; i < 16; ++i) {
@@ -209,6 +211,10 @@ k_detect(const FrameDev* __restrict__ frames, const TileItem* __restrict__ tiles
         }
     }
     const uint32_t* mask = F.mask[l];
+    uint8_t* const kpmap = F.kpmap[l];
+    float* const lvl = F.lvl[l];
+    float* const blur = F.blur[l];
+    const int kp_pitch = F.kp_pitch[l], bl_pitch = F.bl_pitch[l];
     const float wt[3] = {0.3125f, 0.375f, 0.3125f};
     for (int ty = t / TW; ty < TH; ty += K1_THREADS / TW) {
         const int y = Y0 + ty;
@@ -232,8 +238,8 @@ k_detect(const FrameDev* __restrict__ frames, const TileItem* __restrict__ tiles
                 }
             }
         }
-        F.kpmap[l][(size_t)y * F.kp_pitch[l] + x] = (uint8_t)keep;
-        if (l > 0) F.lvl[l][p] = sm[r][c];
+        kpmap[(size_t)y * kp_pitch + x] = (uint8_t)keep;
+        if (l > 0) lvl[p] = sm[r][c];
 
         // 3. blur cache: G(x, y) of generate_features.wgsl:149-172
         float sum = 0.0f;
@@ -254,7 +260,7 @@ k_detect(const FrameDev* __restrict__ frames, const TileItem* __restrict__ tiles
                 sum = sum + (sv * wt[i]) * wt[j];
             }
         }
-        F.blur[l][(size_t)y * F.bl_pitch[l] + x] = sum;
+        blur[(size_t)y * bl_pitch + x] = sum;
     }
 }
 

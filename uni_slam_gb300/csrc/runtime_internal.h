@@ -31,7 +31,7 @@ cudaError_t launch_match(const FrameDev*, const PairDev*, const void*, int, int,
 cudaError_t launch_mutual(const FrameDev*, const PairDev*, const SegDev*, int, uint32_t*, cudaStream_t);
 cudaError_t set_compact_smem(int max_w);
 constexpr int kTileW = 64;
-constexpr int kTileH = 16;
+constexpr int kTileH = 32;  // must equal the tile height TH of k_detect
 constexpr int kMaxSegs = 4096;
 constexpr int kMaxWidth = 8192;
 }  // namespace uslam
