@@ -12,8 +12,11 @@ HBM (graph replay of the 5-kernel batch, L2 flushed between steps);
 D2H of every feature record and match list inside the timed region;
 ``plain_fps`` = the plain per-frame form (one frame per launch sequence,
 synchronous per frame); ``served`` = 32 camera streams at 20 Hz through the
-serving loop (p50/p99 latency, frames/s).  ``--impl reference`` times the CPU restatement of
-the reference's path (oracle port) on all host cores, on the same workload.
+serving loop (p50/p99 latency, frames/s); ``stress`` = 3840x2160 frames,
+8 levels, 2500 features per level (20000 per frame), brute-force top-2
+matching of every frame against a seeded warp of itself, 8 such pairs per
+batch.  ``--impl reference`` times the CPU restatement of the reference's
+path (oracle port) on all host cores, on the same workload.
 """
 from __future__ import annotations
 
@@ -31,6 +34,8 @@ REPO = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, REPO)
 
 W, H, LEVELS = 752, 480, 6
+STRESS_W, STRESS_H, STRESS_LEVELS, STRESS_CAP = 3840, 2160, 8, 2500
+POPC_PER_SM_CLK = 16  # 32-bit population count results per SM per clock (documented issue rate)
 METRIC = "frames/s detect+describe+match @752x480 (batched, 64-frame graph)"
 WORKLOAD = "batched-uniform: 64 consecutive 752x480 u8 frames, plane trajectory, consecutive-pair matching"
 
@@ -46,6 +51,8 @@ def _args():
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="bounded CPU-baseline sample")
     ap.add_argument("--serve-seconds", type=float, default=10.0, help="served-form simulation length (0: skip)")
     ap.add_argument("--serve-streams", type=int, default=32)
+    ap.add_argument("--stress-pairs", type=int, default=8, help="3840x2160 frame/warp pairs (0: skip)")
+    ap.add_argument("--stress-steps", type=int, default=5)
     return ap.parse_args()
 
 
@@ -325,6 +332,78 @@ def serve_simulation(ctx, seconds: float, n_streams: int = 32, rate_hz: float = 
 
 # ------------------------------------------------------------------ GPU side
 
+def _stress_pair(seed: int):
+    from uni_slam_gb300 import synth
+
+    return synth.warped_pair(seed, STRESS_W, STRESS_H, n_rect=5000, n_check=500, scale_by_area=False)
+
+
+def stress_run(pat, local: int, pair_frames, steps: int, warmup: int, seed: int) -> dict:
+    """3840x2160 frames, 8 levels, 2500 kept per level, brute-force top-2
+    matching (ratio 0.8) of each frame against its warp, all pairs in one batch."""
+    import torch
+
+    from uni_slam_gb300 import Batch, Context
+
+    frames = [f for pr in pair_frames for f in pr]
+    npairs = len(pair_frames)
+    ctx = Context(pat, levels=STRESS_LEVELS, max_width=STRESS_W, max_height=STRESS_H, cap_per_level=STRESS_CAP,
+                  device=local, matcher=1, ratio=0.8)
+    batch = Batch(ctx, [(STRESS_W, STRESS_H)] * len(frames), [(2 * k, 2 * k + 1) for k in range(npairs)])
+    try:
+        for i, f in enumerate(frames):
+            batch.set_frame(i, f)
+        batch.upload()
+        batch.sync()
+        stream = torch.cuda.Stream()
+        batch.set_stream(stream.cuda_stream)
+        l2_flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+        for _ in range(warmup):
+            batch.run()
+        stream.synchronize()
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+        with torch.cuda.stream(stream):
+            for e0, e1 in evs:
+                l2_flush.zero_()
+                e0.record(stream)
+                batch.run()
+                e1.record(stream)
+        stream.synchronize()
+        step_ms = sum(e0.elapsed_time(e1) for e0, e1 in evs) / steps
+        e2e = []
+        for _ in range(steps):
+            t0 = time.perf_counter()
+            batch.upload()
+            batch.run()
+            batch.download()
+            batch.sync()
+            e2e.append(time.perf_counter() - t0)
+        kept = [int(batch.features(i)[1].sum()) for i in range(len(frames))]
+        nmatch = [len(batch.matches(k)) for k in range(npairs)]
+        prof = batch.profile(iters=3)
+        # k_match's slot of the profile times the brute-force kernel in this mode
+        prof = {("k_bruteforce" if k == "k_match" else "k_emit" if k == "k_mutual" else k): v for k, v in prof.items()}
+        popc = sum(8 * kept[2 * k] * kept[2 * k + 1] for k in range(npairs))
+        bf_s = prof["k_bruteforce"] / 1e3
+        return {
+            "workload": f"stress: {npairs} pairs of 3840x2160 u8 frames (5000 rectangles, 500 checker patches) and "
+                        f"their seeded warps, {STRESS_LEVELS} levels, {STRESS_CAP} kept per level, brute-force "
+                        "top-2 Hamming matching of every feature against every feature, ratio 0.8",
+            "frames": len(frames), "pairs": npairs, "ms_per_step": step_ms,
+            "frames_per_s": len(frames) / (step_ms / 1e3), "pairs_per_s": npairs / (step_ms / 1e3),
+            "e2e_pairs_per_s": npairs / statistics.mean(e2e),
+            "features_per_frame": sum(kept) / len(kept), "matches_per_pair": sum(nmatch) / npairs,
+            "kernel_ms": prof,
+            "bruteforce": {"popc_per_launch": popc, "ms": prof["k_bruteforce"],
+                           "gpopc_per_s": popc / bf_s / 1e9,
+                           "ms_per_pair": prof["k_bruteforce"] / npairs},
+            "l2": "flushed (256 MiB write) between timed steps", "seed": seed,
+        }
+    finally:
+        batch.close()
+        ctx.close()
+
+
 def run_ours(a):
     rank, world, local = _dist()
     import numpy as np
@@ -347,6 +426,10 @@ def run_ours(a):
     from uni_slam_gb300 import synth
 
     pat = patmod.load()
+    stress_frames = []
+    if a.stress_pairs > 0:
+        with mp.get_context("spawn").Pool(min(a.stress_pairs, os.cpu_count() or 1)) as pool:
+            stress_frames = pool.map(_stress_pair, [a.seed + 100 * (rank + 1) + k for k in range(a.stress_pairs)])
     frames = synth.plane_sequence(a.seed + rank, n=a.frames)
     n = len(frames)
     ctx = Context(pat, levels=LEVELS, max_width=W, max_height=H, device=local)
@@ -458,6 +541,15 @@ def run_ours(a):
         served = serve_simulation(sctx, a.serve_seconds, n_streams=a.serve_streams, seed=a.seed + rank)
         sctx.close()
 
+    stress = None
+    if stress_frames:
+        stress = stress_run(pat, local, stress_frames, a.stress_steps, 2, a.seed)
+        if clk.get("sm_mhz"):
+            peak = POPC_PER_SM_CLK * torch.cuda.get_device_properties(local).multi_processor_count * clk["sm_mhz"] / 1e3
+            stress["bruteforce"]["peak_gpopc_per_s"] = peak
+            stress["bruteforce"]["frac"] = stress["bruteforce"]["gpopc_per_s"] / peak
+            stress["bruteforce"]["peak_source"] = "documented POPC issue rate x SMs x median sampled SM clock"
+
     cpu = None
     if rank == 0:
         cpu = cpu_baseline_sample(frames, pat, a.cpu_seconds)
@@ -475,7 +567,7 @@ def run_ours(a):
             "e2e": {"value": n * world / e2e_s, "unit": "frames/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
             "gpu_launches": 6 * a.steps, "roofline": roofline, "cpu_baseline": cpu, "clocks": clk,
-            "served": served,
+            "served": served, "stress": stress,
             "features_per_frame": sum(kept) / n, "matches_per_pair": sum(nmatch) / max(1, n - 1),
             "wall_s_timed": wall_s,
         }

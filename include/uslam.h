@@ -72,6 +72,11 @@ typedef struct uslam_params {
      * gpumodels::BRIEFTestSet uploaded by GenerateFeaturesPass::writeConstantValues
      * (wslam/src/feature_detect/generate_features.cpp:450-493). */
     const int32_t* brief_pattern;
+    /* 0: the reference's windowed mutual matcher (match_features_cpu.cpp:66-207);
+     * 1: brute-force top-2 over all features of both frames, Lowe test
+     *    best < ratio * second, no window and no cross-check. */
+    int matcher;
+    float ratio;  /* Lowe ratio of matcher 1 (the windowed matcher uses the reference's 0.85) */
 } uslam_params;
 
 /* ---- context ---------------------------------------------------------- */

@@ -43,6 +43,8 @@ def lib():
         L.orc_frame.restype = C.c_int
         L.orc_match.argtypes = [vp, vp, vp, vp, C.c_int, C.c_int, C.c_int, vp, C.c_int]
         L.orc_match.restype = C.c_int
+        L.orc_match_bruteforce.argtypes = [vp, C.c_int, vp, C.c_int, C.c_float, vp]
+        L.orc_match_bruteforce.restype = C.c_int
         L.orc_atan2f.argtypes = [C.c_float, C.c_float]
         L.orc_atan2f.restype = C.c_float
         L.orc_sincosf.argtypes = [C.c_float, vp, vp]
@@ -141,6 +143,23 @@ def match(feats_a, kept_a, feats_b, kept_b, W0: int, H0: int) -> np.ndarray:
     if n < 0:
         raise RuntimeError("orc_match: output buffer too small")
     return out[:n].copy()
+
+
+def match_bruteforce(feats_a, kept_a, feats_b, kept_b, ratio: float = 0.8) -> np.ndarray:
+    """Brute-force top-2 matches (lod_a, idx_a, lod_b, idx_b) of every feature
+    of a against every feature of b, in (lod_a, idx_a) order."""
+    a = np.ascontiguousarray(feats_a, FEATURE_DTYPE)
+    b = np.ascontiguousarray(feats_b, FEATURE_DTYPE)
+    a2b = np.full(max(len(a), 1), -1, np.int32)
+    lib().orc_match_bruteforce(_p(a), len(a), _p(b), len(b), ratio, _p(a2b))
+    a2b = a2b[:len(a)]
+    a_off = np.concatenate([[0], np.cumsum(kept_a)])
+    b_off = np.concatenate([[0], np.cumsum(kept_b)])
+    qa = np.nonzero(a2b >= 0)[0]
+    la = np.searchsorted(a_off, qa, side="right") - 1
+    tb = a2b[qa]
+    lb = np.searchsorted(b_off, tb, side="right") - 1
+    return np.stack([la, qa - a_off[la], lb, tb - b_off[lb]], 1).astype(np.int32).reshape(-1, 4)
 
 
 def atan2f(y: float, x: float) -> float:

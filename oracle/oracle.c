@@ -439,6 +439,32 @@ done:
     return n;
 }
 
+/* ------------------------------------------------------ brute force -- */
+
+int orc_match_bruteforce(const orc_feature* a, int na, const orc_feature* b, int nb, float ratio, int32_t* a2b) {
+    int n = 0;
+    for (int i = 0; i < na; ++i) {
+        uint32_t best = UINT32_MAX, second = UINT32_MAX;
+        int idx = -1;
+        if (nb >= 2) {
+            for (int j = 0; j < nb; ++j) {
+                uint32_t d = 0;
+                for (int w = 0; w < 8; ++w) d += (uint32_t)__builtin_popcount(a[i].descriptor[w] ^ b[j].descriptor[w]);
+                if (d < best) {
+                    second = best;
+                    best = d;
+                    idx = j;
+                } else if (d < second) {
+                    second = d;
+                }
+            }
+        }
+        a2b[i] = (idx >= 0 && (float)best < ratio * (float)second) ? idx : -1;
+        n += a2b[i] >= 0;
+    }
+    return n;
+}
+
 /* ------------------------------------------------------------ exports -- */
 
 float orc_atan2f(float y, float x) { return uslam_atan2f(y, x); }

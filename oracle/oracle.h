@@ -79,6 +79,16 @@ int orc_frame(const uint8_t* img, int W0, int H0, int pitch, int levels, int cap
 int orc_match(const orc_feature* a, const int* a_off, const orc_feature* b, const int* b_off,
               int levels, int W0, int H0, int32_t* out, int max_out);
 
+/* Brute-force top-2 matcher (the benchmark's stress matcher; the reference
+ * has no such mode, so this is pinned by its own definition only): every
+ * feature of a (na, all levels flattened) against every feature of b (nb);
+ * per query the best and second-best Hamming distances (scan rule of
+ * match_features_cpu.cpp:106-119, from UINT32_MAX), accepted iff
+ * f32(best) < ratio * f32(second); no window, no cross-check; nb < 2 gives no
+ * match (match_features_cpu.cpp:80-82).  a2b[i] receives the flat index into
+ * b of query i's match, or -1.  Returns the number of matches. */
+int orc_match_bruteforce(const orc_feature* a, int na, const orc_feature* b, int nb, float ratio, int32_t* a2b);
+
 /* The shared canonical transcendentals (include/uslam_canon.h), exported so
  * the tests can measure their accuracy against a double-precision libm. */
 float orc_atan2f(float y, float x);

@@ -1,0 +1,59 @@
+"""Brute-force top-2 matcher (matcher=1) against the oracle: the full match
+list at 752x480 and on an uneven batch, and at the 3840x2160, 8-level,
+2500-per-level stress size (20000 x 20000 descriptors) as well."""
+import numpy as np
+import pytest
+
+import oracle
+from uni_slam_gb300 import Batch, Context, synth
+
+pytestmark = pytest.mark.gpu
+
+
+def _mm(m):
+    if len(m) == 0:
+        return np.zeros((0, 4), np.int32)
+    return np.stack([m["lod_a"], m["idx_a"], m["lod_b"], m["idx_b"]], 1)
+
+
+def test_bruteforce_equals_oracle_uneven(brief_pattern):
+    frames = list(synth.warped_pair(5)) + list(synth.warped_pair(6, 1280, 720)) + [
+        np.full((480, 640), 77, np.uint8), synth.scene_frame(9, 640, 480)]
+    pairs = [(0, 1), (2, 3), (4, 5), (5, 4), (1, 0)]
+    with Context(brief_pattern, levels=6, max_width=1280, max_height=720, matcher=1, ratio=0.8) as c:
+        b = Batch(c, [(f.shape[1], f.shape[0]) for f in frames], pairs)
+        try:
+            b.process(frames)
+            exp = [oracle.frame(f, brief_pattern) for f in frames]
+            for i in range(len(frames)):
+                gf, gk, _ = b.features(i)
+                assert gf.tobytes() == exp[i][0].tobytes() and np.array_equal(gk, exp[i][1])
+            for k, (p, q) in enumerate(pairs):
+                em = oracle.match_bruteforce(exp[p][0], exp[p][1], exp[q][0], exp[q][1], 0.8)
+                assert np.array_equal(_mm(b.matches(k)), em), f"pair {k}"
+            assert len(_mm(b.matches(0))) > 200
+            assert len(_mm(b.matches(2))) == 0  # constant frame: no features
+        finally:
+            b.close()
+
+
+def test_bruteforce_stress_size(brief_pattern):
+    W, H, L, CAP = 3840, 2160, 8, 2500
+    f0, f1 = synth.warped_pair(2024, W, H, n_rect=5000, n_check=500, scale_by_area=False)
+    with Context(brief_pattern, levels=L, max_width=W, max_height=H, cap_per_level=CAP, matcher=1,
+                 ratio=0.8) as c:
+        b = Batch(c, [(W, H), (W, H)], [(0, 1)])
+        try:
+            b.process([f0, f1])
+            ea = oracle.frame(f0, brief_pattern, levels=L, cap=CAP)
+            eb = oracle.frame(f1, brief_pattern, levels=L, cap=CAP)
+            for i, e in enumerate((ea, eb)):
+                gf, gk, gr = b.features(i)
+                assert np.array_equal(gk, e[1]) and np.array_equal(gr, e[2])
+                assert gf.tobytes() == e[0].tobytes()
+            assert ea[1].sum() > 15000 and eb[1].sum() > 15000
+            em = oracle.match_bruteforce(ea[0], ea[1], eb[0], eb[1], 0.8)
+            assert np.array_equal(_mm(b.matches(0)), em)
+            assert len(em) > 1000
+        finally:
+            b.close()

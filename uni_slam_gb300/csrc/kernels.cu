@@ -6,6 +6,7 @@
 //   k_describe (K2) orientation + 256-bit rotated BRIEF, one warp per keypoint
 //   k_match    (K3) windowed top-2 Hamming search, 32 x-adjacent queries per warp
 //   k_mutual        mutual cross-check and ordered match output
+//   k_bruteforce    brute-force top-2 matching (no window, no cross-check)
 //
 // Arithmetic contract: binary32, round-to-nearest-even, no FMA contraction
 // (the library is compiled with --fmad=false), evaluation order as in the
@@ -775,11 +776,134 @@ k_match(const FrameDev* __restrict__ frames, const PairDev* __restrict__ pairs,
     }
 }
 
+// ----------------------------------------------------- brute force ----
+constexpr int KB_THREADS = 128;  // two queries per thread: 256 queries per CTA
+constexpr int KB_TILE = 256;     // train descriptors per shared-memory tile
+
+// Level of flat index f given the per-level prefix pre[0..L] (pre[L] = total).
+__device__ __forceinline__ int flat_level(const uint32_t* pre, int L, uint32_t f) {
+    int l = 0;
+    while (l + 1 < L && pre[l + 1] <= f) ++l;
+    return l;
+}
+
+__device__ __forceinline__ uint32_t hamming256(const uint4& a0, const uint4& a1, const uint4& b0, const uint4& b1) {
+    return __popc(a0.x ^ b0.x) + __popc(a0.y ^ b0.y) + __popc(a0.z ^ b0.z) + __popc(a0.w ^ b0.w) +
+           __popc(a1.x ^ b1.x) + __popc(a1.y ^ b1.y) + __popc(a1.z ^ b1.z) + __popc(a1.w ^ b1.w);
+}
+
+// Brute-force top-2 matching (the benchmark's `cfg` matcher): every feature
+// of frame prev (all levels) against every feature of frame curr, Lowe test
+// best < ratio * second in f32, no window and no cross-check.  One CTA holds
+// 256 queries in registers and streams the train set through shared memory
+// in tiles of 256 descriptors.  A tied best fails the ratio test, so the
+// result does not depend on the scan order; a train set of fewer than two
+// features gives no match (the pool rule of match_features_cpu.cpp:80-82).
+// Result per query a in a2b: packed (level, index) of its match in curr, or -1.
+__global__ void __launch_bounds__(KB_THREADS)
+k_bruteforce(const FrameDev* __restrict__ frames, const PairDev* __restrict__ pairs, const SegDev* __restrict__ psegs,
+             int npairs, float ratio) {
+    __shared__ uint32_t s_pref[MAX_SEGS + 1];
+    __shared__ uint32_t s_warp[33];
+    __shared__ uint4 s_d[2 * KB_TILE];
+    __shared__ int32_t s_id[KB_TILE];
+    __shared__ uint32_t s_qpre[USLAM_MAX_LEVELS + 1], s_tpre[USLAM_MAX_LEVELS + 1];
+    const uint32_t total = segment_prefix(npairs, s_pref, s_warp, [&](int s) {
+        const FrameDev& A = frames[pairs[psegs[s].frame].prev];
+        uint32_t n = 0;
+        for (int l = 0; l < A.levels; ++l) n += A.kept[l];
+        return (n + 2u * KB_THREADS - 1u) / (2u * KB_THREADS);
+    });
+    const int tid = threadIdx.x;
+    for (uint32_t g = blockIdx.x; g < total; g += gridDim.x) {
+        const int sidx = find_segment(s_pref, npairs, g);
+        const uint32_t blk = g - s_pref[sidx];
+        const PairDev& P = pairs[psegs[sidx].frame];
+        const FrameDev& A = frames[P.prev];
+        const FrameDev& B = frames[P.curr];
+        const int LA = A.levels, LB = B.levels;
+        if (tid == 0) {
+            uint32_t ra = 0, rb = 0;
+            for (int l = 0; l <= USLAM_MAX_LEVELS; ++l) {
+                s_qpre[l] = ra;
+                s_tpre[l] = rb;
+                if (l < LA) ra += A.kept[l];
+                if (l < LB) rb += B.kept[l];
+            }
+        }
+        __syncthreads();
+        const uint32_t nq = s_qpre[LA], nt = s_tpre[LB];
+        uint4 q0[2], q1[2];
+        uint32_t best[2], second[2];
+        int32_t bidx[2];
+        int ql[2];
+        uint32_t qi[2];
+        bool qv[2];
+#pragma unroll
+        for (int k = 0; k < 2; ++k) {
+            const uint32_t f = blk * 2u * KB_THREADS + 2u * tid + k;
+            qv[k] = f < nq;
+            ql[k] = qv[k] ? flat_level(s_qpre, LA, f) : 0;
+            qi[k] = qv[k] ? f - s_qpre[ql[k]] : 0u;
+            const uint32_t* rec = A.feats[ql[k]] + (size_t)qi[k] * 12u;
+            q0[k] = qv[k] ? *reinterpret_cast<const uint4*>(rec + 4) : make_uint4(0, 0, 0, 0);
+            q1[k] = qv[k] ? *reinterpret_cast<const uint4*>(rec + 8) : make_uint4(0, 0, 0, 0);
+            best[k] = second[k] = 0xffffffffu;
+            bidx[k] = -1;
+        }
+        for (uint32_t t0 = 0; t0 < nt; t0 += KB_TILE) {
+            __syncthreads();
+            for (int j = tid; j < KB_TILE; j += KB_THREADS) {
+                const uint32_t f = t0 + (uint32_t)j;
+                if (f < nt) {
+                    const int l = flat_level(s_tpre, LB, f);
+                    const uint32_t i = f - s_tpre[l];
+                    const uint32_t* rec = B.feats[l] + (size_t)i * 12u;
+                    s_d[2 * j] = __ldg(reinterpret_cast<const uint4*>(rec + 4));
+                    s_d[2 * j + 1] = __ldg(reinterpret_cast<const uint4*>(rec + 8));
+                    s_id[j] = USLAM_PACK(l, i);
+                }
+            }
+            __syncthreads();
+            const int n = (int)min((uint32_t)KB_TILE, nt - t0);
+            for (int j = 0; j < n; ++j) {
+                const uint4 d0 = s_d[2 * j], d1 = s_d[2 * j + 1];
+#pragma unroll
+                for (int k = 0; k < 2; ++k) {
+                    const uint32_t d = hamming256(q0[k], q1[k], d0, d1);
+                    if (d < best[k]) {
+                        second[k] = best[k];
+                        best[k] = d;
+                        bidx[k] = j;  // tile-local; resolved below
+                    } else if (d < second[k]) {
+                        second[k] = d;
+                    }
+                }
+            }
+            // resolve tile-local winners to packed ids before the tile is overwritten
+#pragma unroll
+            for (int k = 0; k < 2; ++k)
+                if (bidx[k] >= 0 && bidx[k] < KB_TILE) bidx[k] = KB_TILE + s_id[bidx[k]];
+        }
+#pragma unroll
+        for (int k = 0; k < 2; ++k) {
+            if (!qv[k]) continue;
+            const int32_t id = bidx[k] >= 0 ? bidx[k] - KB_TILE : -1;
+            const int32_t res = (nt >= 2u && id >= 0 && (float)best[k] < ratio * (float)second[k]) ? id : -1;
+            P.a2b[(size_t)ql[k] * A.cap + qi[k]] = res;
+        }
+        __syncthreads();  // s_qpre / s_tpre are rewritten by the next work unit
+    }
+}
+
 // ---------------------------------------------------------- mutual ----
 constexpr int KU_THREADS = 256;
 
 // One CTA per (pair, level of a): keep (a, b) iff b2a[b] == a, in a order
 // (match_features_cpu.cpp:196-205).
+// MUTUAL = false: every a with a2b[a] >= 0 is emitted (brute-force mode,
+// which has no cross-check).
+template <bool MUTUAL>
 __global__ void __launch_bounds__(KU_THREADS)
 k_mutual(const FrameDev* __restrict__ frames, const PairDev* __restrict__ pairs, const SegDev* __restrict__ segs,
          uint32_t* err) {
@@ -799,7 +923,7 @@ k_mutual(const FrameDev* __restrict__ frames, const PairDev* __restrict__ pairs,
             m = P.a2b[(size_t)l * A.cap + i];
             if (m >= 0) {
                 const int bl = USLAM_PACK_LEVEL(m), bi = USLAM_PACK_INDEX(m);
-                ok = P.b2a[(size_t)bl * B.cap + bi] == USLAM_PACK(l, i);
+                ok = !MUTUAL || P.b2a[(size_t)bl * B.cap + bi] == USLAM_PACK(l, i);
             }
         }
         uint32_t tot;
@@ -877,7 +1001,21 @@ cudaError_t launch_match(const FrameDev* frames, const PairDev* pairs, const voi
 cudaError_t launch_mutual(const FrameDev* frames, const PairDev* pairs, const SegDev* segs, int nseg,
                           uint32_t* err, cudaStream_t st) {
     if (nseg <= 0) return cudaSuccess;
-    k_mutual<<<nseg, KU_THREADS, 0, st>>>(frames, pairs, segs, err);
+    k_mutual<true><<<nseg, KU_THREADS, 0, st>>>(frames, pairs, segs, err);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_emit(const FrameDev* frames, const PairDev* pairs, const SegDev* segs, int nseg, uint32_t* err,
+                        cudaStream_t st) {
+    if (nseg <= 0) return cudaSuccess;
+    k_mutual<false><<<nseg, KU_THREADS, 0, st>>>(frames, pairs, segs, err);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_bruteforce(const FrameDev* frames, const PairDev* pairs, const SegDev* psegs, int npairs,
+                              float ratio, int grid, cudaStream_t st) {
+    if (npairs <= 0) return cudaSuccess;
+    k_bruteforce<<<grid, KB_THREADS, 0, st>>>(frames, pairs, psegs, npairs, ratio);
     return cudaGetLastError();
 }
 

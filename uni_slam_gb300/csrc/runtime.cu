@@ -31,11 +31,12 @@ namespace {
 
 // Launch tables of one program (a subset of the batch's frames and pairs).
 struct Program {
-    int ntiles = 0, nfsegs = 0, nmsegs = 0, nusegs = 0;
+    int ntiles = 0, nfsegs = 0, nmsegs = 0, nusegs = 0, npsegs = 0;
     TileItem* tiles = nullptr;
     SegDev* fsegs = nullptr;
     MatchSegDev* msegs = nullptr;
     SegDev* usegs = nullptr;
+    SegDev* psegs = nullptr;  // one (pair, 0) entry per pair (brute-force matcher)
     std::vector<char> host;  // host image of the tables
     cudaGraphExec_t graph = nullptr;
 };
@@ -71,7 +72,7 @@ namespace {
 
 uslam_status build_program(uslam_batch* b, const std::vector<int>& fr, const std::vector<int>& pr, Program* P) {
     std::vector<TileItem> tiles;
-    std::vector<SegDev> fsegs, usegs;
+    std::vector<SegDev> fsegs, usegs, psegs;
     std::vector<MatchSegDev> msegs;
     for (int f : fr) {
         const FrameDev& F = b->frames[f];
@@ -90,6 +91,7 @@ uslam_status build_program(uslam_batch* b, const std::vector<int>& fr, const std
         }
     }
     for (int p : pr) {
+        psegs.push_back(SegDev{p, 0});
         for (int l = 0; l < b->levels; ++l) {
             msegs.push_back(MatchSegDev{p, 0, l});
             msegs.push_back(MatchSegDev{p, 1, l});
@@ -102,15 +104,18 @@ uslam_status build_program(uslam_batch* b, const std::vector<int>& fr, const std
     P->nfsegs = static_cast<int>(fsegs.size());
     P->nmsegs = static_cast<int>(msegs.size());
     P->nusegs = static_cast<int>(usegs.size());
+    P->npsegs = static_cast<int>(psegs.size());
     const size_t t_bytes = round_up(tiles.size() * sizeof(TileItem), 256);
     const size_t f_bytes = round_up(fsegs.size() * sizeof(SegDev), 256);
     const size_t m_bytes = round_up(msegs.size() * sizeof(MatchSegDev), 256);
     const size_t u_bytes = round_up(usegs.size() * sizeof(SegDev), 256);
-    P->host.assign(t_bytes + f_bytes + m_bytes + u_bytes, 0);
+    const size_t p_bytes = round_up(psegs.size() * sizeof(SegDev), 256);
+    P->host.assign(t_bytes + f_bytes + m_bytes + u_bytes + p_bytes, 0);
     std::memcpy(P->host.data(), tiles.data(), tiles.size() * sizeof(TileItem));
     std::memcpy(P->host.data() + t_bytes, fsegs.data(), fsegs.size() * sizeof(SegDev));
     std::memcpy(P->host.data() + t_bytes + f_bytes, msegs.data(), msegs.size() * sizeof(MatchSegDev));
     std::memcpy(P->host.data() + t_bytes + f_bytes + m_bytes, usegs.data(), usegs.size() * sizeof(SegDev));
+    std::memcpy(P->host.data() + t_bytes + f_bytes + m_bytes + u_bytes, psegs.data(), psegs.size() * sizeof(SegDev));
     return USLAM_OK;
 }
 
@@ -128,9 +133,18 @@ cudaError_t enqueue_program(uslam_batch* b, const Program& P) {
     }
     if (P.nmsegs > 0) {
         const int grid = c->num_sms * 4;
-        if ((e = launch_match(b->d_frames, b->d_pairs, P.msegs, P.nmsegs, grid, b->stream)) != cudaSuccess) return e;
-        if ((e = launch_mutual(b->d_frames, b->d_pairs, P.usegs, P.nusegs, b->d_err, b->stream)) != cudaSuccess)
-            return e;
+        if (c->matcher == 1) {
+            if ((e = launch_bruteforce(b->d_frames, b->d_pairs, P.psegs, P.npsegs, c->ratio, grid, b->stream)) !=
+                cudaSuccess)
+                return e;
+            if ((e = launch_emit(b->d_frames, b->d_pairs, P.usegs, P.nusegs, b->d_err, b->stream)) != cudaSuccess)
+                return e;
+        } else {
+            if ((e = launch_match(b->d_frames, b->d_pairs, P.msegs, P.nmsegs, grid, b->stream)) != cudaSuccess)
+                return e;
+            if ((e = launch_mutual(b->d_frames, b->d_pairs, P.usegs, P.nusegs, b->d_err, b->stream)) != cudaSuccess)
+                return e;
+        }
     }
     return cudaSuccess;
 }
@@ -394,6 +408,8 @@ uslam_status create_batch(uslam_ctx* ctx, int n_frames, const int* widths, const
         const size_t t_bytes = round_up(P->ntiles * sizeof(TileItem), 256);
         const size_t f_bytes = round_up(P->nfsegs * sizeof(SegDev), 256);
         const size_t m_bytes = round_up(P->nmsegs * sizeof(MatchSegDev), 256);
+        const size_t u_bytes = round_up(P->nusegs * sizeof(SegDev), 256);
+        P->psegs = reinterpret_cast<SegDev*>(base + t_bytes + f_bytes + m_bytes + u_bytes);
         P->tiles = reinterpret_cast<TileItem*>(base);
         P->fsegs = reinterpret_cast<SegDev*>(base + t_bytes);
         P->msegs = reinterpret_cast<MatchSegDev*>(base + t_bytes + f_bytes);
@@ -527,7 +543,8 @@ uslam_status uslam_create(const uslam_params* params, uslam_ctx** out) {
     *out = nullptr;
     if (params->levels < 1 || params->levels > USLAM_MAX_LEVELS || params->max_width < 1 ||
         params->max_width > kMaxWidth || params->max_height < 1 || params->max_height > 65535 ||
-        params->cap_per_level < 0 || params->cap_per_level >= (1 << 24) || !params->brief_pattern)
+        params->cap_per_level < 0 || params->cap_per_level >= (1 << 24) || !params->brief_pattern ||
+        (params->matcher != 0 && params->matcher != 1) || (params->matcher == 1 && !(params->ratio > 0.0f)))
         return USLAM_INVALID_ARG;
     auto* c = new uslam_ctx();
     c->device = params->device;
@@ -535,6 +552,8 @@ uslam_status uslam_create(const uslam_params* params, uslam_ctx** out) {
     c->max_w = params->max_width;
     c->max_h = params->max_height;
     c->cap_override = params->cap_per_level;
+    c->matcher = params->matcher;
+    c->ratio = params->ratio;
     // blur-cache margin: a rotated test point lies within ceil(radius) + 1 of
     // its keypoint (rounding of the rotation), so radius + 2 covers it.
     double rmax = 0.0;
@@ -710,9 +729,13 @@ uslam_status uslam_batch_profile(uslam_batch* b, int iters, float* kernel_ms) {
         mark();
         if (e == cudaSuccess) e = launch_describe(b->d_frames, P.fsegs, P.nfsegs, c->d_pattern, grid, b->stream);
         mark();
-        if (e == cudaSuccess) e = launch_match(b->d_frames, b->d_pairs, P.msegs, P.nmsegs, grid, b->stream);
+        if (e == cudaSuccess)
+            e = c->matcher == 1 ? launch_bruteforce(b->d_frames, b->d_pairs, P.psegs, P.npsegs, c->ratio, grid, b->stream)
+                                : launch_match(b->d_frames, b->d_pairs, P.msegs, P.nmsegs, grid, b->stream);
         mark();
-        if (e == cudaSuccess) e = launch_mutual(b->d_frames, b->d_pairs, P.usegs, P.nusegs, b->d_err, b->stream);
+        if (e == cudaSuccess)
+            e = c->matcher == 1 ? launch_emit(b->d_frames, b->d_pairs, P.usegs, P.nusegs, b->d_err, b->stream)
+                                : launch_mutual(b->d_frames, b->d_pairs, P.usegs, P.nusegs, b->d_err, b->stream);
         mark();
         if (e == cudaSuccess) e = cudaEventSynchronize(ev[K]);
         for (int q = 0; q < K && e == cudaSuccess; ++q) {

@@ -29,6 +29,8 @@ cudaError_t launch_blur_border(const FrameDev*, const SegDev*, int, int, cudaStr
 cudaError_t launch_describe(const FrameDev*, const SegDev*, int, const int32_t*, int, cudaStream_t);
 cudaError_t launch_match(const FrameDev*, const PairDev*, const void*, int, int, cudaStream_t);
 cudaError_t launch_mutual(const FrameDev*, const PairDev*, const SegDev*, int, uint32_t*, cudaStream_t);
+cudaError_t launch_emit(const FrameDev*, const PairDev*, const SegDev*, int, uint32_t*, cudaStream_t);
+cudaError_t launch_bruteforce(const FrameDev*, const PairDev*, const SegDev*, int, float, int, cudaStream_t);
 cudaError_t set_compact_smem(int max_w);
 constexpr int kTileW = 64;
 constexpr int kTileH = 32;  // must equal the tile height TH of k_detect
@@ -119,6 +121,8 @@ struct uslam_ctx {
     int cap_override = 0;
     int num_sms = 0;
     int margin = 0;  // blur-cache margin: BRIEF pattern radius + 2
+    int matcher = 0;      // 0 windowed mutual (reference), 1 brute-force top-2
+    float ratio = 0.8f;   // Lowe ratio of the brute-force matcher
     int32_t* d_pattern = nullptr;
     std::string err;
     std::map<std::pair<int, int>, ResClass> classes;

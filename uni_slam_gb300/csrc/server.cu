@@ -308,6 +308,8 @@ extern "C" {
 uslam_status uslam_server_create(uslam_ctx* ctx, const uslam_server_params* p, uslam_server** out) {
     if (!ctx || !p || !out || p->n_sizes < 1 || !p->widths || !p->heights || p->max_batch < 1 || p->max_batch > 4096)
         return set_err(ctx ? &ctx->err : nullptr, USLAM_INVALID_ARG, "server_create: bad arguments");
+    if (ctx->matcher != 0)
+        return set_err(&ctx->err, USLAM_INVALID_ARG, "server_create: the served form runs the windowed matcher only");
     cudaError_t e = cudaSetDevice(ctx->device);
     if (e != cudaSuccess) return ctx->cuda_fail(e, "cudaSetDevice");
     auto* s = new uslam_server();

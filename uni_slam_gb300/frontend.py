@@ -28,13 +28,13 @@ class Context:
     """Device context: BRIEF table, level count, cap, size limits."""
 
     def __init__(self, pattern: np.ndarray, levels: int = 6, max_width: int = 4096, max_height: int = 4096,
-                 cap_per_level: int = 0, device: int = 0):
+                 cap_per_level: int = 0, device: int = 0, matcher: int = 0, ratio: float = 0.8):
         self.lib = capi.load()
         self._pattern = np.ascontiguousarray(pattern, dtype=np.int32).reshape(-1)
         if self._pattern.size != 1024:
             raise ValueError("pattern must hold 256 x (ax, ay, bx, by)")
         p = capi.Params(device, levels, max_width, max_height, cap_per_level,
-                        self._pattern.ctypes.data_as(C.POINTER(C.c_int32)))
+                        self._pattern.ctypes.data_as(C.POINTER(C.c_int32)), matcher, ratio)
         h = C.c_void_p()
         st = self.lib.uslam_create(C.byref(p), C.byref(h))
         if st != capi.OK:
