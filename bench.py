@@ -12,7 +12,9 @@ HBM (graph replay of the 5-kernel batch, L2 flushed between steps);
 D2H of every feature record and match list inside the timed region;
 ``plain_fps`` = the plain per-frame form (one frame per launch sequence,
 synchronous per frame); ``served`` = 32 camera streams at 20 Hz through the
-serving loop (p50/p99 latency, frames/s); ``stress`` = 3840x2160 frames,
+serving loop (p50/p99 latency, frames/s); ``uneven`` = 46 frames of five
+sizes (640x480 .. 3840x2160) each matched against its warp in one graph,
+per-32x32-cell caps, detect tiles autotuned per size; ``stress`` = 3840x2160 frames,
 8 levels, 2500 features per level (20000 per frame), brute-force top-2
 matching of every frame against a seeded warp of itself, 8 such pairs per
 batch.  ``--impl reference`` times the CPU restatement of the reference's
@@ -53,6 +55,7 @@ def _args():
     ap.add_argument("--serve-streams", type=int, default=32)
     ap.add_argument("--stress-pairs", type=int, default=8, help="3840x2160 frame/warp pairs (0: skip)")
     ap.add_argument("--stress-steps", type=int, default=5)
+    ap.add_argument("--uneven", type=int, default=1, help="batched-uneven workload (0: skip)")
     return ap.parse_args()
 
 
@@ -332,6 +335,84 @@ def serve_simulation(ctx, seconds: float, n_streams: int = 32, rate_hz: float = 
 
 # ------------------------------------------------------------------ GPU side
 
+UNEVEN_MIX = [(640, 480, 16), (752, 480, 16), (1280, 720, 8), (1920, 1080, 4), (3840, 2160, 2)]
+UNEVEN_CELL_CAP = 4  # per 32x32 cell and level: about the W0*H0/250 level-cap density (1024/250)
+
+
+def _uneven_pair(args):
+    seed, w, h = args
+    from uni_slam_gb300 import synth
+
+    return synth.warped_pair(seed, w, h)
+
+
+def uneven_run(pat, local: int, pair_frames, steps: int, warmup: int, seed: int) -> dict:
+    """Batched-uneven workload: 16x640x480, 16x752x480, 8x1280x720,
+    4x1920x1080 and 2x3840x2160 frames, each matched against a seeded warp of
+    itself (92 frames, 46 pairs) in one graph; per-32x32-cell caps; detect
+    tile shape autotuned per resolution class."""
+    import torch
+
+    from uni_slam_gb300 import Batch, Context
+
+    frames = [f for pr in pair_frames for f in pr]
+    npairs = len(pair_frames)
+    ctx = Context(pat, levels=LEVELS, max_width=3840, max_height=2160, device=local, cell_cap=UNEVEN_CELL_CAP)
+    tuned = {}
+    for a, _ in pair_frames:
+        h, w = a.shape
+        if f"{w}x{h}" not in tuned:
+            shape, ms = ctx.autotune(a, n_frames=4, reps=5)
+            tuned[f"{w}x{h}"] = {"shape": ctx.tile_shapes()[shape], "ms_per_shape": ms}
+    batch = Batch(ctx, [(f.shape[1], f.shape[0]) for f in frames], [(2 * k, 2 * k + 1) for k in range(npairs)])
+    try:
+        for i, f in enumerate(frames):
+            batch.set_frame(i, f)
+        batch.upload()
+        batch.sync()
+        stream = torch.cuda.Stream()
+        batch.set_stream(stream.cuda_stream)
+        l2_flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+        for _ in range(warmup):
+            batch.run()
+        stream.synchronize()
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+        with torch.cuda.stream(stream):
+            for e0, e1 in evs:
+                l2_flush.zero_()
+                e0.record(stream)
+                batch.run()
+                e1.record(stream)
+        stream.synchronize()
+        step_ms = sum(e0.elapsed_time(e1) for e0, e1 in evs) / steps
+        e2e = []
+        for _ in range(steps):
+            t0 = time.perf_counter()
+            batch.upload()
+            batch.run()
+            batch.download()
+            batch.sync()
+            e2e.append(time.perf_counter() - t0)
+        kept = [int(batch.features(i)[1].sum()) for i in range(len(frames))]
+        nmatch = [len(batch.matches(k)) for k in range(npairs)]
+        prof = batch.profile(iters=3)
+        px = sum(f.size for f in frames)
+        return {
+            "workload": "batched-uneven: 16x640x480, 16x752x480, 8x1280x720, 4x1920x1080, 2x3840x2160 frames, each "
+                        "matched against a seeded warp of itself, one graph; per-32x32-cell caps "
+                        f"({UNEVEN_CELL_CAP} per cell and level) then the W0*H0/250 level cap",
+            "frames": len(frames), "pairs": npairs, "ms_per_step": step_ms,
+            "frames_per_s": len(frames) / (step_ms / 1e3), "mpix_per_s": px / (step_ms / 1e3) / 1e6,
+            "e2e_frames_per_s": len(frames) / statistics.mean(e2e),
+            "features_per_frame": sum(kept) / len(kept), "matches_per_pair": sum(nmatch) / npairs,
+            "kernel_ms": prof, "autotuned_tile_shapes": tuned,
+            "l2": "flushed (256 MiB write) between timed steps", "seed": seed,
+        }
+    finally:
+        batch.close()
+        ctx.close()
+
+
 def _stress_pair(seed: int):
     from uni_slam_gb300 import synth
 
@@ -426,10 +507,22 @@ def run_ours(a):
     from uni_slam_gb300 import synth
 
     pat = patmod.load()
-    stress_frames = []
-    if a.stress_pairs > 0:
-        with mp.get_context("spawn").Pool(min(a.stress_pairs, os.cpu_count() or 1)) as pool:
-            stress_frames = pool.map(_stress_pair, [a.seed + 100 * (rank + 1) + k for k in range(a.stress_pairs)])
+    stress_frames, uneven_frames = [], []
+    if a.stress_pairs > 0 or a.uneven:
+        with mp.get_context("spawn").Pool(os.cpu_count() or 1) as pool:
+            jobs = []
+            if a.uneven:
+                mix = [(a.seed + 300 + 1000 * rank + k, w, h) for k, (w, h) in
+                       enumerate((w, h) for (w, h, n) in UNEVEN_MIX for _ in range(n))]
+                jobs.append(pool.map_async(_uneven_pair, mix))
+            if a.stress_pairs > 0:
+                jobs.append(pool.map_async(_stress_pair,
+                                           [a.seed + 100 * (rank + 1) + k for k in range(a.stress_pairs)]))
+            res = [j.get() for j in jobs]
+            if a.uneven:
+                uneven_frames = res.pop(0)
+            if a.stress_pairs > 0:
+                stress_frames = res.pop(0)
     frames = synth.plane_sequence(a.seed + rank, n=a.frames)
     n = len(frames)
     ctx = Context(pat, levels=LEVELS, max_width=W, max_height=H, device=local)
@@ -541,6 +634,10 @@ def run_ours(a):
         served = serve_simulation(sctx, a.serve_seconds, n_streams=a.serve_streams, seed=a.seed + rank)
         sctx.close()
 
+    uneven = None
+    if uneven_frames:
+        uneven = uneven_run(pat, local, uneven_frames, a.stress_steps, 2, a.seed)
+
     stress = None
     if stress_frames:
         stress = stress_run(pat, local, stress_frames, a.stress_steps, 2, a.seed)
@@ -567,7 +664,7 @@ def run_ours(a):
             "e2e": {"value": n * world / e2e_s, "unit": "frames/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
             "gpu_launches": 6 * a.steps, "roofline": roofline, "cpu_baseline": cpu, "clocks": clk,
-            "served": served, "stress": stress,
+            "served": served, "uneven": uneven, "stress": stress,
             "features_per_frame": sum(kept) / n, "matches_per_pair": sum(nmatch) / max(1, n - 1),
             "wall_s_timed": wall_s,
         }

@@ -77,6 +77,14 @@ typedef struct uslam_params {
      *    best < ratio * second, no window and no cross-check. */
     int matcher;
     float ratio;  /* Lowe ratio of matcher 1 (the windowed matcher uses the reference's 0.85) */
+    /* 0: a level's keypoints in (y, x) order, the first cap_per_level kept.
+     * 1..1024: per-cell caps -- each level is cut into 32x32 cells from its
+     * origin; the first cell_cap keypoints of each cell in (y, x) order are
+     * kept, listed cell by cell (cells in row-major order), and the level cap
+     * then keeps the first cap_per_level of that list.  No reference
+     * counterpart: the reference keeps whichever keypoints win its atomic
+     * append (generate_features.wgsl:67-70). */
+    int cell_cap;
 } uslam_params;
 
 /* ---- context ---------------------------------------------------------- */
@@ -98,6 +106,23 @@ uslam_status uslam_level_dims(int width, int height, int levels, int* w_out, int
  * response is > 0 (row 0 additionally needs the 1x3 first arg-max, applied
  * on the device).  Needs no GPU. */
 uslam_status uslam_cull_coverage(int W0, int H0, int w, int h, uint32_t* bits_out);
+
+/* ---- detect tile shapes and the autotuner ------------------------------
+ * k_detect is built for several tile shapes; every shape computes the same
+ * values, so the choice per resolution class changes speed only.  A batch or
+ * server created afterwards uses the shape stored for each frame size
+ * (default: shape 0).  No reference counterpart (the WGSL passes use fixed
+ * 16x16 / 64-wide workgroups). */
+uslam_status uslam_tile_shapes(int* n_out, int* tile_w, int* tile_h);
+uslam_status uslam_set_tile_shape(uslam_ctx* ctx, int width, int height, int shape);
+uslam_status uslam_get_tile_shape(const uslam_ctx* ctx, int width, int height, int* shape);
+/* Time the detect kernel in every shape on n_frames copies of a
+ * representative frame (median of `reps` launches), store the fastest for
+ * width x height and return it in *shape_out; ms_out (n entries from
+ * uslam_tile_shapes, or NULL) receives each shape's median time.  Allocates
+ * a temporary batch; synchronous. */
+uslam_status uslam_autotune(uslam_ctx* ctx, int width, int height, const uint8_t* img, int pitch, int n_frames,
+                            int reps, int* shape_out, float* ms_out);
 
 /* ---- batched form: a work table over many frames and frame pairs -------- */
 

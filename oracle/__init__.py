@@ -41,6 +41,8 @@ def lib():
         L.orc_gauss_tap9.restype = C.c_float
         L.orc_frame.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, vp, vp, C.c_int, vp, vp]
         L.orc_frame.restype = C.c_int
+        L.orc_frame_ex.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, vp, vp, C.c_int, vp, vp]
+        L.orc_frame_ex.restype = C.c_int
         L.orc_match.argtypes = [vp, vp, vp, vp, C.c_int, C.c_int, C.c_int, vp, C.c_int]
         L.orc_match.restype = C.c_int
         L.orc_match_bruteforce.argtypes = [vp, C.c_int, vp, C.c_int, C.c_float, vp]
@@ -112,8 +114,9 @@ def describe(lvl: np.ndarray, x: int, y: int, pattern: np.ndarray):
     return float(th[0]), d
 
 
-def frame(img: np.ndarray, pattern: np.ndarray, levels: int = 6, cap: int | None = None):
-    """Features of one frame: (features[FEATURE_DTYPE], kept[levels], raw[levels])."""
+def frame(img: np.ndarray, pattern: np.ndarray, levels: int = 6, cap: int | None = None, cell_cap: int = 0):
+    """Features of one frame: (features[FEATURE_DTYPE], kept[levels], raw[levels]).
+    cell_cap > 0 keeps at most cell_cap keypoints per 32x32 cell, listed cell by cell."""
     img = np.ascontiguousarray(img, np.uint8)
     H0, W0 = img.shape
     if cap is None:
@@ -124,7 +127,8 @@ def frame(img: np.ndarray, pattern: np.ndarray, levels: int = 6, cap: int | None
     feats = np.zeros(max_feats, FEATURE_DTYPE)
     kept = np.zeros(levels, np.int32)
     raw = np.zeros(levels, np.int32)
-    n = lib().orc_frame(_p(img), W0, H0, W0, levels, cap, _p(pat), _p(feats), max_feats, _p(kept), _p(raw))
+    n = lib().orc_frame_ex(_p(img), W0, H0, W0, levels, cap, cell_cap, _p(pat), _p(feats), max_feats, _p(kept),
+                           _p(raw))
     if n < 0:
         raise RuntimeError("orc_frame: feature buffer too small")
     return feats[:n].copy(), kept, raw

@@ -255,12 +255,25 @@ void orc_describe(const float* lvl, uint32_t w, uint32_t h, int x, int y, const 
 
 /* --------------------------------------------------------------- frame -- */
 
-int orc_frame(const uint8_t* img, int W0, int H0, int pitch, int levels, int cap,
-              const int32_t* pattern, orc_feature* feats, int max_feats, int* kept, int* raw) {
+/* Keep one keypoint: header plus descriptor; returns 0 if feats is full. */
+static int emit(const float* lvl, uint32_t w, uint32_t h, int x, int y, uint32_t strength, const int32_t* pattern,
+                orc_feature* feats, int max_feats, int* total) {
+    if (*total >= max_feats) return 0;
+    orc_feature* f = &feats[*total];
+    f->x = (float)x;
+    f->y = (float)y;
+    f->strength = strength;
+    orc_describe(lvl, w, h, x, y, pattern, &f->orientation, f->descriptor);
+    ++*total;
+    return 1;
+}
+
+int orc_frame_ex(const uint8_t* img, int W0, int H0, int pitch, int levels, int cap, int cell_cap,
+                 const int32_t* pattern, orc_feature* feats, int max_feats, int* kept, int* raw) {
     uint32_t ws[32], hs[32];
     orc_level_dims(W0, H0, levels, ws, hs);
-    int total = 0;
-    for (int l = 0; l < levels; ++l) {
+    int total = 0, ok = 1;
+    for (int l = 0; l < levels && ok; ++l) {
         const uint32_t w = ws[l], h = hs[l];
         const size_t n = (size_t)w * h;
         float* lvl = (float*)malloc(n * sizeof(float));
@@ -270,26 +283,32 @@ int orc_frame(const uint8_t* img, int W0, int H0, int pitch, int levels, int cap
         orc_detect(lvl, w, h, resp);
         orc_cull(resp, w, h, W0, H0, culled);
         int nraw = 0, nkept = 0;
-        /* canonical order (y, x); keep the first `cap` (the reference's
-         * atomic append order is nondeterministic, generate_features.wgsl:67-70) */
-        for (size_t p = 0; p < n; ++p) {
-            if (culled[p] == 0u) continue;
-            ++nraw;
-            if (nkept >= cap) continue;
-            if (total >= max_feats) {
-                free(lvl);
-                free(resp);
-                free(culled);
-                return -1;
+        for (size_t p = 0; p < n; ++p) nraw += culled[p] != 0u;
+        if (cell_cap <= 0) {
+            /* canonical order (y, x); keep the first `cap` (the reference's
+             * atomic append order is nondeterministic, generate_features.wgsl:67-70) */
+            for (size_t p = 0; p < n && ok && nkept < cap; ++p) {
+                if (culled[p] == 0u) continue;
+                ok = emit(lvl, w, h, (int)(p % w), (int)(p / w), culled[p], pattern, feats, max_feats, &total);
+                nkept += ok;
             }
-            orc_feature* f = &feats[total];
-            const int x = (int)(p % w), y = (int)(p / w);
-            f->x = (float)x;
-            f->y = (float)y;
-            f->strength = culled[p];
-            orc_describe(lvl, w, h, x, y, pattern, &f->orientation, f->descriptor);
-            ++nkept;
-            ++total;
+        } else {
+            /* per-cell caps: 32x32 cells in row-major order, (y, x) within a
+             * cell, the first cell_cap of each cell, then the level cap */
+            for (uint32_t cy = 0; cy * 32u < h && ok; ++cy)
+                for (uint32_t cx = 0; cx * 32u < w && ok; ++cx) {
+                    int in_cell = 0;
+                    for (uint32_t y = cy * 32u; y < cy * 32u + 32u && y < h && ok; ++y)
+                        for (uint32_t x = cx * 32u; x < cx * 32u + 32u && x < w && ok; ++x) {
+                            const uint32_t s = culled[(size_t)y * w + x];
+                            if (s == 0u) continue;
+                            if (in_cell < cell_cap && nkept < cap) {
+                                ok = emit(lvl, w, h, (int)x, (int)y, s, pattern, feats, max_feats, &total);
+                                nkept += ok;
+                            }
+                            ++in_cell;
+                        }
+                }
         }
         kept[l] = nkept;
         raw[l] = nraw;
@@ -297,7 +316,12 @@ int orc_frame(const uint8_t* img, int W0, int H0, int pitch, int levels, int cap
         free(resp);
         free(culled);
     }
-    return total;
+    return ok ? total : -1;
+}
+
+int orc_frame(const uint8_t* img, int W0, int H0, int pitch, int levels, int cap,
+              const int32_t* pattern, orc_feature* feats, int max_feats, int* kept, int* raw) {
+    return orc_frame_ex(img, W0, H0, pitch, levels, cap, 0, pattern, feats, max_feats, kept, raw);
 }
 
 /* --------------------------------------------------------------- match -- */

@@ -69,6 +69,12 @@ float orc_gauss_tap9(const float* lvl, uint32_t w, uint32_t h, uint32_t px, uint
  * total number of kept features, or -1 if max_feats is too small. */
 int orc_frame(const uint8_t* img, int W0, int H0, int pitch, int levels, int cap,
               const int32_t* pattern, orc_feature* feats, int max_feats, int* kept, int* raw);
+/* As orc_frame; cell_cap > 0 selects per-cell caps: each level is cut into
+ * 32x32 cells from its origin, cells visited in row-major order and pixels
+ * within a cell in (y, x) order; the first cell_cap keypoints of each cell
+ * are kept, and the level cap keeps the first `cap` of that sequence. */
+int orc_frame_ex(const uint8_t* img, int W0, int H0, int pitch, int levels, int cap, int cell_cap,
+                 const int32_t* pattern, orc_feature* feats, int max_feats, int* kept, int* raw);
 
 /* Matcher restated from wslam/src/pose_estimate_cpu/match_features_cpu.cpp:27-207.
  * a = previous (reference) set, b = current set; a_off/b_off hold levels+1

@@ -38,7 +38,7 @@ class Params(C.Structure):
     _fields_ = [
         ("device", C.c_int), ("levels", C.c_int), ("max_width", C.c_int), ("max_height", C.c_int),
         ("cap_per_level", C.c_int), ("brief_pattern", C.POINTER(C.c_int32)), ("matcher", C.c_int),
-        ("ratio", C.c_float),
+        ("ratio", C.c_float), ("cell_cap", C.c_int),
     ]
 
 
@@ -73,6 +73,10 @@ SIGNATURES = {
     "uslam_batch_profile": (C.c_int, [_vp, C.c_int, _vp]),
     "uslam_blur_margin": (C.c_int, [_vp, _ip]),
     "uslam_batch_io_bytes": (C.c_int, [_vp, _szp, _szp]),
+    "uslam_tile_shapes": (C.c_int, [_ip, _ip, _ip]),
+    "uslam_set_tile_shape": (C.c_int, [_vp, C.c_int, C.c_int, C.c_int]),
+    "uslam_get_tile_shape": (C.c_int, [_vp, C.c_int, C.c_int, _ip]),
+    "uslam_autotune": (C.c_int, [_vp, C.c_int, C.c_int, _vp, C.c_int, C.c_int, C.c_int, _ip, _vp]),
     "uslam_frontend_create": (C.c_int, [_vp, C.c_int, C.c_int, C.POINTER(_vp)]),
     "uslam_frontend_destroy": (None, [_vp]),
     "uslam_frontend_process": (C.c_int, [_vp, _vp, C.c_int, C.c_int]),

@@ -19,13 +19,10 @@
 
 namespace uslam {
 
-// K1 tile geometry: TW x TH output pixels, halo HX columns / HY rows.
-constexpr int TW = 64;
-constexpr int TH = 32;
+// K1 tile geometry: TW x TH output pixels (a template parameter pair, one of
+// kTileShapes), halo HX columns / HY rows.
 constexpr int HX = 5;
 constexpr int HY = 3;
-constexpr int SW = TW + 2 * HX;
-constexpr int SH = TH + 2 * HY;
 constexpr int K1_THREADS = 256;
 
 // Bresenham circle of radius 3 (resources/detect_corners.wgsl:31-32).
@@ -79,6 +76,7 @@ __device__ float pyramid_pixel(const FrameDev& F, int l, int x, int y) {
 
 // FAST response at smem cell (r, c): 1 + longest non-wrapping run of
 // |centre - p_i| > 0.15, kept iff > 9 (detect_corners.wgsl:58-81).
+template <int SW>
 __device__ __forceinline__ uint32_t fast_response(const float (*sm)[SW], int r, int c) {
     const float center = sm[r][c];
     // every non-wrapping run of >= 9 of the 16 points contains points 7 and 8
@@ -113,8 +111,12 @@ __device__ __forceinline__ bool mask_bit(const uint32_t* mask, int p) {
 // value and the blur-cache value G(x, y).  Sampling coordinates depend only
 // on the row or only on the column, so they are computed once per tile row /
 // column (same operations as the per-pixel formula, hence the same bits).
+template <int TW, int TH>
 __global__ void __launch_bounds__(K1_THREADS)
 k_detect(const FrameDev* __restrict__ frames, const TileItem* __restrict__ tiles, uint32_t* err) {
+    constexpr int SW = TW + 2 * HX;
+    constexpr int SH = TH + 2 * HY;
+    static_assert(K1_THREADS % TW == 0 && SW + SH + 3 * TH <= 2 * K1_THREADS, "tile shape");
     __shared__ float sm[SH][SW];
     __shared__ float s_lut[256];                 // f32(u8) / 255
     __shared__ int s_fx0[SW], s_fx1[SW];         // LOD0 source columns per staged column
@@ -137,34 +139,38 @@ k_detect(const FrameDev* __restrict__ frames, const TileItem* __restrict__ tiles
 
     // 0. per-tile tables
     s_lut[t] = (float)t / 255.0f;
-    if (l > 0 && t < SW) {
-        // create_pyramid.wgsl:11-12 + canonical bilinear, x part
-        const int gx = tint_clamp(X0 - HX + t, w);
-        const float u = (((float)gx + 0.5f) / (float)w) * (float)F.W0 - 0.5f;
-        const float fi = floorf(u);
-        s_fa[t] = u - fi;
-        s_fx0[t] = edge_index(fi, F.W0);
-        s_fx1[t] = edge_index(fi + 1.0f, F.W0);
-    } else if (l > 0 && t >= 96 && t < 96 + SH) {
-        const int r = t - 96;
-        const int gy = tint_clamp(Y0 - HY + r, h);
-        const float v = (((float)gy + 0.5f) / (float)h) * (float)F.H0 - 0.5f;
-        const float fj = floorf(v);
-        s_fb[r] = v - fj;
-        s_fy0[r] = edge_index(fj, F.H0);
-        s_fy1[r] = edge_index(fj + 1.0f, F.H0);
-    } else if (t >= 160 && t < 160 + 3 * TH) {
-        // generate_features.wgsl:153-169, y part of the 9 taps
-        const int ty = (t - 160) / 3, k = (t - 160) % 3;
-        const float uvy = ((float)(Y0 + ty) + 0.5f) * tex_y;
-        const float offk = k == 0 ? -1.2f : (k == 1 ? 0.0f : 1.2f);
-        const float v = (uvy + offk * tex_y) * (float)h - 0.5f;
-        const float fj = floorf(v);
-        int r0 = edge_index(fj, h) - (Y0 - HY), r1 = edge_index(fj + 1.0f, h) - (Y0 - HY);
-        if (Y0 + ty < h && (r0 < 0 || r1 >= SH)) atomicOr(err, USLAM_ERR_SMEM_RANGE);
-        s_bb[k][ty] = v - fj;
-        s_by0[k][ty] = min(max(r0, 0), SH - 1);
-        s_by1[k][ty] = min(max(r1, 0), SH - 1);
+    for (int i = t; i < SW + SH + 3 * TH; i += K1_THREADS) {
+        if (i < SW) {
+            if (l == 0) continue;
+            // create_pyramid.wgsl:11-12 + canonical bilinear, x part
+            const int gx = tint_clamp(X0 - HX + i, w);
+            const float u = (((float)gx + 0.5f) / (float)w) * (float)F.W0 - 0.5f;
+            const float fi = floorf(u);
+            s_fa[i] = u - fi;
+            s_fx0[i] = edge_index(fi, F.W0);
+            s_fx1[i] = edge_index(fi + 1.0f, F.W0);
+        } else if (i < SW + SH) {
+            if (l == 0) continue;
+            const int r = i - SW;
+            const int gy = tint_clamp(Y0 - HY + r, h);
+            const float v = (((float)gy + 0.5f) / (float)h) * (float)F.H0 - 0.5f;
+            const float fj = floorf(v);
+            s_fb[r] = v - fj;
+            s_fy0[r] = edge_index(fj, F.H0);
+            s_fy1[r] = edge_index(fj + 1.0f, F.H0);
+        } else {
+            // generate_features.wgsl:153-169, y part of the 9 taps
+            const int ty = (i - SW - SH) / 3, k = (i - SW - SH) % 3;
+            const float uvy = ((float)(Y0 + ty) + 0.5f) * tex_y;
+            const float offk = k == 0 ? -1.2f : (k == 1 ? 0.0f : 1.2f);
+            const float v = (uvy + offk * tex_y) * (float)h - 0.5f;
+            const float fj = floorf(v);
+            int r0 = edge_index(fj, h) - (Y0 - HY), r1 = edge_index(fj + 1.0f, h) - (Y0 - HY);
+            if (Y0 + ty < h && (r0 < 0 || r1 >= SH)) atomicOr(err, USLAM_ERR_SMEM_RANGE);
+            s_bb[k][ty] = v - fj;
+            s_by0[k][ty] = min(max(r0, 0), SH - 1);
+            s_by1[k][ty] = min(max(r1, 0), SH - 1);
+        }
     }
     __syncthreads();
 
@@ -303,33 +309,10 @@ __device__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* s_warp, uint32_t*
     return res;
 }
 
-// One CTA per (frame, level): keypoints in (y, x) order from the culled
-// strength map, cap applied to the first `cap`, then a counting sort of the
-// kept features by x for the matcher's window lookup.
-__global__ void __launch_bounds__(KC_THREADS)
-k_compact(const FrameDev* __restrict__ frames, const SegDev* __restrict__ segs) {
-    extern __shared__ uint32_t s_hist[];  // [w + 1]
-    __shared__ uint32_t s_warp[33];
-    __shared__ uint32_t s_base[32];
-    const SegDev sg = segs[blockIdx.x];
-    const FrameDev& F = frames[sg.frame];
-    const int l = sg.level;
-    const int w = F.w[l], h = F.h[l], kpitch = F.kp_pitch[l];
-    const uint8_t* kp = F.kpmap[l];
+// Exclusive scan of the 32 per-warp values s_base[0..31] in place (warp 0);
+// the sum goes to *sum_out (shared).
+__device__ __forceinline__ void scan_warp_bases(uint32_t* s_base, uint32_t* sum_out) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int rows_per = (h + 31) / 32;
-    const int r0 = warp * rows_per, r1 = min(h, r0 + rows_per);
-    const uint32_t cap = (uint32_t)F.cap;
-
-    // pass 1: count per warp
-    uint32_t cnt = 0;
-    for (int y = r0; y < r1; ++y) {
-        const uint32_t* row = reinterpret_cast<const uint32_t*>(kp + (size_t)y * kpitch);
-        for (int x4 = lane; x4 * 4 < w; x4 += 32) cnt += nonzero_bytes(row[x4]);
-    }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
-    if (lane == 0) s_base[warp] = cnt;
     __syncthreads();
     if (warp == 0) {
         const uint32_t v = s_base[lane];
@@ -340,14 +323,35 @@ k_compact(const FrameDev* __restrict__ frames, const SegDev* __restrict__ segs) 
             if (lane >= o) incl += t;
         }
         s_base[lane] = incl - v;
-        if (lane == 31) s_warp[32] = incl;
+        if (lane == 31) *sum_out = incl;
     }
     __syncthreads();
-    const uint32_t total = s_warp[32];
+}
 
-    // pass 2: ordered write of (x, y, strength) headers
+__device__ __forceinline__ void write_header(uint32_t* feats, uint32_t pos, int x, int y, uint32_t s) {
+    uint32_t* rec = feats + (size_t)pos * 12u;
+    rec[0] = __float_as_uint((float)x);
+    rec[1] = __float_as_uint((float)y);
+    rec[2] = s;
+}
+
+// (y, x) order: warp k owns a band of rows; count, scan, ordered write.
+__device__ void compact_rows(const uint8_t* kp, int kpitch, int w, int h, uint32_t cap, uint32_t* feats,
+                             uint32_t* s_base, uint32_t* s_warp, uint32_t* total_out) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int rows_per = (h + 31) / 32;
+    const int r0 = warp * rows_per, r1 = min(h, r0 + rows_per);
+    uint32_t cnt = 0;
+    for (int y = r0; y < r1; ++y) {
+        const uint32_t* row = reinterpret_cast<const uint32_t*>(kp + (size_t)y * kpitch);
+        for (int x4 = lane; x4 * 4 < w; x4 += 32) cnt += nonzero_bytes(row[x4]);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+    if (lane == 0) s_base[warp] = cnt;
+    scan_warp_bases(s_base, &s_warp[32]);
+    *total_out = s_warp[32];
     uint32_t running = s_base[warp];
-    uint32_t* feats = F.feats[l];
     for (int y = r0; y < r1; ++y) {
         const uint32_t* row = reinterpret_cast<const uint32_t*>(kp + (size_t)y * kpitch);
         for (int base = 0; base < w; base += 128) {
@@ -362,20 +366,126 @@ k_compact(const FrameDev* __restrict__ frames, const SegDev* __restrict__ segs) 
             }
             uint32_t pos = running + incl - n;
             for (int b = 0; b < 4; ++b) {
-                const uint32_t s = (v >> (8 * b)) & 0xffu;
-                if (s == 0u) continue;
-                if (pos < cap) {
-                    uint32_t* rec = feats + (size_t)pos * 12u;
-                    rec[0] = __float_as_uint((float)(x4 * 4 + b));
-                    rec[1] = __float_as_uint((float)y);
-                    rec[2] = s;
-                }
+                const uint32_t sv = (v >> (8 * b)) & 0xffu;
+                if (sv == 0u) continue;
+                if (pos < cap) write_header(feats, pos, x4 * 4 + b, y, sv);
                 ++pos;
             }
             running += __shfl_sync(0xffffffffu, incl, 31);
         }
     }
-    const uint32_t kept = total < cap ? total : cap;
+}
+
+// One lane's 32-pixel row segment of a 32x32 cell (bytes at x >= w zeroed).
+__device__ __forceinline__ void load_cell_row(const uint8_t* kp, int kpitch, int w, int h, int x0, int y,
+                                              uint32_t v[8]) {
+#pragma unroll
+    for (int k = 0; k < 8; ++k) v[k] = 0u;
+    if (y >= h) return;
+    const uint8_t* row = kp + (size_t)y * kpitch + x0;
+#pragma unroll
+    for (int j = 0; j < 2; ++j) {
+        if (x0 + 16 * j < w) {  // then x0 + 16 j + 16 <= kpitch (a multiple of 16)
+            const uint4 q = *reinterpret_cast<const uint4*>(row + 16 * j);
+            v[4 * j] = q.x;
+            v[4 * j + 1] = q.y;
+            v[4 * j + 2] = q.z;
+            v[4 * j + 3] = q.w;
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        const int rem = w - (x0 + 4 * k);
+        if (rem <= 0) v[k] = 0u;
+        else if (rem < 4) v[k] &= (1u << (8 * rem)) - 1u;
+    }
+}
+
+// Cell order: warp k owns a run of 32x32 cells (row-major); lane r holds
+// row r of the current cell.  The first ccap keypoints of each cell in
+// (y, x) order are kept; the level cap applies to the cell-ordered list.
+__device__ void compact_cells(const uint8_t* kp, int kpitch, int w, int h, uint32_t cap, uint32_t ccap,
+                              uint32_t* feats, uint32_t* s_base, uint32_t* s_warp, uint32_t* total_out,
+                              uint32_t* kept_out) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int ncx = (w + 31) / 32, ncy = (h + 31) / 32, ncell = ncx * ncy;
+    const int cells_per = (ncell + 31) / 32;
+    const int c0 = warp * cells_per, c1 = min(ncell, c0 + cells_per);
+    uint32_t raw = 0, cnt = 0;
+    for (int ci = c0; ci < c1; ++ci) {
+        const int cy = ci / ncx, cx = ci - cy * ncx;
+        uint32_t v[8];
+        load_cell_row(kp, kpitch, w, h, cx * 32, cy * 32 + lane, v);
+        uint32_t n = 0;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) n += (uint32_t)nonzero_bytes(v[k]);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) n += __shfl_xor_sync(0xffffffffu, n, o);
+        raw += n;
+        cnt += n < ccap ? n : ccap;
+    }
+    if (lane == 0) s_base[warp] = raw;
+    scan_warp_bases(s_base, &s_warp[32]);
+    *total_out = s_warp[32];
+    __syncthreads();
+    if (lane == 0) s_base[warp] = cnt;
+    scan_warp_bases(s_base, &s_warp[32]);
+    const uint32_t kept_cells = s_warp[32];
+    *kept_out = kept_cells < cap ? kept_cells : cap;
+    uint32_t running = s_base[warp];
+    for (int ci = c0; ci < c1; ++ci) {
+        const int cy = ci / ncx, cx = ci - cy * ncx;
+        const int y = cy * 32 + lane;
+        uint32_t v[8];
+        load_cell_row(kp, kpitch, w, h, cx * 32, y, v);
+        uint32_t n = 0;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) n += (uint32_t)nonzero_bytes(v[k]);
+        uint32_t incl = n;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += t;
+        }
+        const uint32_t tot = __shfl_sync(0xffffffffu, incl, 31);
+        uint32_t rank = incl - n;
+        for (int k = 0; k < 8 && rank < ccap; ++k) {
+            if (v[k] == 0u) continue;
+            for (int b = 0; b < 4; ++b) {
+                const uint32_t sv = (v[k] >> (8 * b)) & 0xffu;
+                if (sv == 0u) continue;
+                if (rank < ccap && running + rank < cap) write_header(feats, running + rank, cx * 32 + 4 * k + b, y, sv);
+                ++rank;
+            }
+        }
+        running += tot < ccap ? tot : ccap;
+    }
+}
+
+// One CTA per (frame, level): keypoints in (y, x) order (or cell order with
+// per-cell caps) from the culled strength map, the level cap applied to the
+// first `cap`, then a counting sort of the kept features by x for the
+// matcher's window lookup.
+__global__ void __launch_bounds__(KC_THREADS)
+k_compact(const FrameDev* __restrict__ frames, const SegDev* __restrict__ segs) {
+    extern __shared__ uint32_t s_hist[];  // [w + 1]
+    __shared__ uint32_t s_warp[33];
+    __shared__ uint32_t s_base[32];
+    const SegDev sg = segs[blockIdx.x];
+    const FrameDev& F = frames[sg.frame];
+    const int l = sg.level;
+    const int w = F.w[l], h = F.h[l], kpitch = F.kp_pitch[l];
+    const uint8_t* kp = F.kpmap[l];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t cap = (uint32_t)F.cap;
+    uint32_t* feats = F.feats[l];
+    uint32_t total, kept;
+    if (F.cell_cap <= 0) {
+        compact_rows(kp, kpitch, w, h, cap, feats, s_base, s_warp, &total);
+        kept = total < cap ? total : cap;
+    } else {
+        compact_cells(kp, kpitch, w, h, cap, (uint32_t)F.cell_cap, feats, s_base, s_warp, &total, &kept);
+    }
     if (threadIdx.x == 0) {
         F.raw[l] = total;
         F.kept[l] = kept;
@@ -964,10 +1074,17 @@ cudaError_t init_constants() {
     return cudaMemcpyToSymbol(c_disc_y, dy, sizeof(dy));
 }
 
-cudaError_t launch_detect(const FrameDev* frames, const TileItem* tiles, int ntiles, uint32_t* err,
+cudaError_t launch_detect(const FrameDev* frames, const TileItem* tiles, int ntiles, int shape, uint32_t* err,
                           cudaStream_t st) {
     if (ntiles <= 0) return cudaSuccess;
-    k_detect<<<ntiles, K1_THREADS, 0, st>>>(frames, tiles, err);
+    switch (shape) {
+        case 0: k_detect<64, 32><<<ntiles, K1_THREADS, 0, st>>>(frames, tiles, err); break;
+        case 1: k_detect<128, 32><<<ntiles, K1_THREADS, 0, st>>>(frames, tiles, err); break;
+        case 2: k_detect<64, 16><<<ntiles, K1_THREADS, 0, st>>>(frames, tiles, err); break;
+        case 3: k_detect<32, 32><<<ntiles, K1_THREADS, 0, st>>>(frames, tiles, err); break;
+        case 4: k_detect<128, 16><<<ntiles, K1_THREADS, 0, st>>>(frames, tiles, err); break;
+        default: return cudaErrorInvalidValue;
+    }
     return cudaGetLastError();
 }
 

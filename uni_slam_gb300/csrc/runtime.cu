@@ -32,6 +32,7 @@ namespace {
 // Launch tables of one program (a subset of the batch's frames and pairs).
 struct Program {
     int ntiles = 0, nfsegs = 0, nmsegs = 0, nusegs = 0, npsegs = 0;
+    int tile_begin[kNumTileShapes + 1] = {0};  // tiles grouped by shape
     TileItem* tiles = nullptr;
     SegDev* fsegs = nullptr;
     MatchSegDev* msegs = nullptr;
@@ -71,25 +72,17 @@ struct uslam_batch {
 namespace {
 
 uslam_status build_program(uslam_batch* b, const std::vector<int>& fr, const std::vector<int>& pr, Program* P) {
-    std::vector<TileItem> tiles;
+    ShapedTiles st;
     std::vector<SegDev> fsegs, usegs, psegs;
     std::vector<MatchSegDev> msegs;
     for (int f : fr) {
         const FrameDev& F = b->frames[f];
-        for (int l = 0; l < F.levels; ++l) {
-            const int nx = (F.w[l] + kTileW - 1) / kTileW, ny = (F.h[l] + kTileH - 1) / kTileH;
-            for (int ty = 0; ty < ny; ++ty)
-                for (int tx = 0; tx < nx; ++tx) {
-                    TileItem t{};
-                    t.frame = static_cast<uint16_t>(f);
-                    t.level = static_cast<uint8_t>(l);
-                    t.tx = static_cast<uint16_t>(tx);
-                    t.ty = static_cast<uint16_t>(ty);
-                    tiles.push_back(t);
-                }
-            fsegs.push_back(SegDev{f, l});
-        }
+        append_tiles(&st.by_shape[b->ctx->shape_for(F.W0, F.H0)], f, F, b->ctx->shape_for(F.W0, F.H0));
+        for (int l = 0; l < F.levels; ++l) fsegs.push_back(SegDev{f, l});
     }
+    st.finish();
+    const std::vector<TileItem>& tiles = st.flat;
+    std::memcpy(P->tile_begin, st.begin, sizeof(P->tile_begin));
     for (int p : pr) {
         psegs.push_back(SegDev{p, 0});
         for (int l = 0; l < b->levels; ++l) {
@@ -124,7 +117,8 @@ cudaError_t enqueue_program(uslam_batch* b, const Program& P) {
     uslam_ctx* c = b->ctx;
     cudaError_t e = cudaSuccess;
     if (P.ntiles > 0) {
-        if ((e = launch_detect(b->d_frames, P.tiles, P.ntiles, b->d_err, b->stream)) != cudaSuccess) return e;
+        if ((e = launch_detect_shaped(b->d_frames, P.tiles, P.tile_begin, b->d_err, b->stream)) != cudaSuccess)
+            return e;
         const int grid = c->num_sms * 4;
         if ((e = launch_blur_border(b->d_frames, P.fsegs, P.nfsegs, grid, b->stream)) != cudaSuccess) return e;
         if ((e = launch_compact(b->d_frames, P.fsegs, P.nfsegs, b->max_w, b->stream)) != cudaSuccess) return e;
@@ -225,6 +219,7 @@ uslam_status create_batch(uslam_ctx* ctx, int n_frames, const int* widths, const
         F.H0 = H0;
         F.levels = L;
         F.margin = ctx->margin;
+        F.cell_cap = ctx->cell_cap;
         F.img_pitch = static_cast<int>(round_up(static_cast<size_t>(W0), 16));
         level_dims(W0, H0, L, F.w, F.h);
         for (int l = 0; l < L; ++l) {
@@ -544,7 +539,8 @@ uslam_status uslam_create(const uslam_params* params, uslam_ctx** out) {
     if (params->levels < 1 || params->levels > USLAM_MAX_LEVELS || params->max_width < 1 ||
         params->max_width > kMaxWidth || params->max_height < 1 || params->max_height > 65535 ||
         params->cap_per_level < 0 || params->cap_per_level >= (1 << 24) || !params->brief_pattern ||
-        (params->matcher != 0 && params->matcher != 1) || (params->matcher == 1 && !(params->ratio > 0.0f)))
+        (params->matcher != 0 && params->matcher != 1) || (params->matcher == 1 && !(params->ratio > 0.0f)) ||
+        params->cell_cap < 0 || params->cell_cap > 1024)
         return USLAM_INVALID_ARG;
     auto* c = new uslam_ctx();
     c->device = params->device;
@@ -554,6 +550,7 @@ uslam_status uslam_create(const uslam_params* params, uslam_ctx** out) {
     c->cap_override = params->cap_per_level;
     c->matcher = params->matcher;
     c->ratio = params->ratio;
+    c->cell_cap = params->cell_cap;
     // blur-cache margin: a rotated test point lies within ceil(radius) + 1 of
     // its keypoint (rounding of the rotation), so radius + 2 covers it.
     double rmax = 0.0;
@@ -721,7 +718,7 @@ uslam_status uslam_batch_profile(uslam_batch* b, int iters, float* kernel_ms) {
             if (e == cudaSuccess) e = cudaEventRecord(ev[k++], b->stream);
         };
         mark();
-        if (e == cudaSuccess) e = launch_detect(b->d_frames, P.tiles, P.ntiles, b->d_err, b->stream);
+        if (e == cudaSuccess) e = launch_detect_shaped(b->d_frames, P.tiles, P.tile_begin, b->d_err, b->stream);
         mark();
         if (e == cudaSuccess) e = launch_blur_border(b->d_frames, P.fsegs, P.nfsegs, grid, b->stream);
         mark();
@@ -749,6 +746,94 @@ uslam_status uslam_batch_profile(uslam_batch* b, int iters, float* kernel_ms) {
     if (e != cudaSuccess) return c->cuda_fail(e, "profile");
     for (int q = 0; q < K; ++q) kernel_ms[q] = static_cast<float>(acc[q] / iters);
     return check_err_word(b);
+}
+
+uslam_status uslam_tile_shapes(int* n_out, int* tw, int* th) {
+    if (!n_out) return USLAM_INVALID_ARG;
+    *n_out = kNumTileShapes;
+    for (int s = 0; s < kNumTileShapes; ++s) {
+        if (tw) tw[s] = kTileShapes[s][0];
+        if (th) th[s] = kTileShapes[s][1];
+    }
+    return USLAM_OK;
+}
+
+uslam_status uslam_set_tile_shape(uslam_ctx* ctx, int width, int height, int shape) {
+    if (!ctx || width < 1 || height < 1 || shape < 0 || shape >= kNumTileShapes)
+        return set_err(ctx ? &ctx->err : nullptr, USLAM_INVALID_ARG, "set_tile_shape: bad arguments");
+    ctx->tile_shape[std::make_pair(width, height)] = shape;
+    return USLAM_OK;
+}
+
+uslam_status uslam_get_tile_shape(const uslam_ctx* ctx, int width, int height, int* shape) {
+    if (!ctx || !shape) return USLAM_INVALID_ARG;
+    *shape = ctx->shape_for(width, height);
+    return USLAM_OK;
+}
+
+// Autotuner: a throwaway batch of n_frames copies of the caller's frame runs
+// once (pyramid masks, cull coverage), then k_detect is timed over every
+// frame's tiles in each shape (CUDA events on the batch stream, median of
+// `reps` launches); the fastest shape is stored for the resolution class.
+uslam_status uslam_autotune(uslam_ctx* ctx, int width, int height, const uint8_t* img, int pitch, int n_frames,
+                            int reps, int* shape_out, float* ms_out) {
+    if (!ctx || !img || n_frames < 1 || n_frames > 1024 || reps < 1 || reps > 1000 || pitch < width)
+        return set_err(ctx ? &ctx->err : nullptr, USLAM_INVALID_ARG, "autotune: bad arguments");
+    std::vector<int> ws(n_frames, width), hs(n_frames, height);
+    uslam_batch* b = nullptr;
+    uslam_status st = create_batch(ctx, n_frames, ws.data(), hs.data(), 0, nullptr, nullptr, false, &b);
+    if (st != USLAM_OK) return st;
+    for (int f = 0; f < n_frames && st == USLAM_OK; ++f) st = uslam_batch_set_frame(b, f, img, pitch);
+    if (st == USLAM_OK) st = uslam_batch_upload(b);
+    if (st == USLAM_OK) st = uslam_batch_run(b);
+    if (st == USLAM_OK) st = uslam_batch_sync(b, 0);
+    TileItem* d_tiles = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    float best_ms = 0.0f;
+    int best = -1;
+    cudaError_t e = cudaSuccess;
+    if (st == USLAM_OK) {
+        e = cudaEventCreate(&e0);
+        if (e == cudaSuccess) e = cudaEventCreate(&e1);
+    }
+    for (int s = 0; s < kNumTileShapes && st == USLAM_OK && e == cudaSuccess; ++s) {
+        std::vector<TileItem> tiles;
+        for (int f = 0; f < n_frames; ++f) append_tiles(&tiles, f, b->frames[f], s);
+        if (d_tiles) cudaFree(d_tiles);
+        d_tiles = nullptr;
+        e = cudaMalloc(&d_tiles, tiles.size() * sizeof(TileItem));
+        if (e == cudaSuccess)
+            e = cudaMemcpy(d_tiles, tiles.data(), tiles.size() * sizeof(TileItem), cudaMemcpyHostToDevice);
+        const int n = static_cast<int>(tiles.size());
+        std::vector<float> t;
+        for (int r = -2; r < reps && e == cudaSuccess; ++r) {
+            e = cudaEventRecord(e0, b->stream);
+            if (e == cudaSuccess) e = launch_detect(b->d_frames, d_tiles, n, s, b->d_err, b->stream);
+            if (e == cudaSuccess) e = cudaEventRecord(e1, b->stream);
+            if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+            float ms = 0.0f;
+            if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+            if (r >= 0) t.push_back(ms);  // two untimed warm-up launches
+        }
+        if (e != cudaSuccess) break;
+        std::sort(t.begin(), t.end());
+        const float med = t[t.size() / 2];
+        if (ms_out) ms_out[s] = med;
+        if (best < 0 || med < best_ms) {
+            best = s;
+            best_ms = med;
+        }
+    }
+    if (d_tiles) cudaFree(d_tiles);
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    if (st == USLAM_OK && e != cudaSuccess) st = ctx->cuda_fail(e, "autotune");
+    if (st == USLAM_OK) st = check_err_word(b);
+    free_batch(b);
+    if (st != USLAM_OK) return st;
+    ctx->tile_shape[std::make_pair(width, height)] = best;
+    if (shape_out) *shape_out = best;
+    return USLAM_OK;
 }
 
 uslam_status uslam_batch_io_bytes(uslam_batch* b, size_t* h2d, size_t* d2h) {

@@ -23,7 +23,7 @@ struct MatchSegDev {
     int level;
 };
 cudaError_t init_constants();
-cudaError_t launch_detect(const FrameDev*, const TileItem*, int, uint32_t*, cudaStream_t);
+cudaError_t launch_detect(const FrameDev*, const TileItem*, int, int, uint32_t*, cudaStream_t);
 cudaError_t launch_compact(const FrameDev*, const SegDev*, int, int, cudaStream_t);
 cudaError_t launch_blur_border(const FrameDev*, const SegDev*, int, int, cudaStream_t);
 cudaError_t launch_describe(const FrameDev*, const SegDev*, int, const int32_t*, int, cudaStream_t);
@@ -32,8 +32,11 @@ cudaError_t launch_mutual(const FrameDev*, const PairDev*, const SegDev*, int, u
 cudaError_t launch_emit(const FrameDev*, const PairDev*, const SegDev*, int, uint32_t*, cudaStream_t);
 cudaError_t launch_bruteforce(const FrameDev*, const PairDev*, const SegDev*, int, float, int, cudaStream_t);
 cudaError_t set_compact_smem(int max_w);
-constexpr int kTileW = 64;
-constexpr int kTileH = 32;  // must equal the tile height TH of k_detect
+// Tile shapes (width, height) that k_detect is instantiated for; the index
+// is the `shape` argument of launch_detect.  Every shape computes the same
+// values (the arithmetic is per pixel), so the choice affects speed only.
+constexpr int kNumTileShapes = 5;
+constexpr int kTileShapes[kNumTileShapes][2] = {{64, 32}, {128, 32}, {64, 16}, {32, 32}, {128, 16}};
 constexpr int kMaxSegs = 4096;
 constexpr int kMaxWidth = 8192;
 }  // namespace uslam
@@ -105,6 +108,50 @@ inline std::vector<uint32_t> build_cull_mask(int W0, int H0, int w, int h) {
     return bits;
 }
 
+// Append the detect tiles of one frame for tile shape `shape`.
+inline void append_tiles(std::vector<TileItem>* out, int frame, const FrameDev& F, int shape) {
+    const int tw = kTileShapes[shape][0], th = kTileShapes[shape][1];
+    for (int l = 0; l < F.levels; ++l) {
+        const int nx = (F.w[l] + tw - 1) / tw, ny = (F.h[l] + th - 1) / th;
+        for (int ty = 0; ty < ny; ++ty)
+            for (int tx = 0; tx < nx; ++tx) {
+                TileItem t{};
+                t.frame = static_cast<uint16_t>(frame);
+                t.level = static_cast<uint8_t>(l);
+                t.tx = static_cast<uint16_t>(tx);
+                t.ty = static_cast<uint16_t>(ty);
+                out->push_back(t);
+            }
+    }
+}
+
+// Tiles grouped by shape: tiles[begin[s] .. begin[s+1]) use shape s.
+struct ShapedTiles {
+    std::vector<TileItem> by_shape[kNumTileShapes];
+    std::vector<TileItem> flat;
+    int begin[kNumTileShapes + 1] = {0};
+    void finish() {
+        flat.clear();
+        for (int s = 0; s < kNumTileShapes; ++s) {
+            begin[s] = static_cast<int>(flat.size());
+            flat.insert(flat.end(), by_shape[s].begin(), by_shape[s].end());
+        }
+        begin[kNumTileShapes] = static_cast<int>(flat.size());
+    }
+};
+
+// One k_detect launch per tile shape present.
+inline cudaError_t launch_detect_shaped(const FrameDev* frames, const TileItem* d_tiles, const int* begin,
+                                        uint32_t* err, cudaStream_t st) {
+    for (int s = 0; s < kNumTileShapes; ++s) {
+        const int n = begin[s + 1] - begin[s];
+        if (n <= 0) continue;
+        const cudaError_t e = launch_detect(frames, d_tiles + begin[s], n, s, err, st);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
 struct ResClass {
     int W0 = 0, H0 = 0;
     std::vector<uint32_t*> d_mask;
@@ -123,6 +170,12 @@ struct uslam_ctx {
     int margin = 0;  // blur-cache margin: BRIEF pattern radius + 2
     int matcher = 0;      // 0 windowed mutual (reference), 1 brute-force top-2
     float ratio = 0.8f;   // Lowe ratio of the brute-force matcher
+    int cell_cap = 0;     // > 0: keypoints kept per 32x32 cell of a level, cell order
+    std::map<std::pair<int, int>, int> tile_shape;  // per resolution class (autotuned or set)
+    int shape_for(int W0, int H0) const {
+        auto it = tile_shape.find(std::make_pair(W0, H0));
+        return it == tile_shape.end() ? 0 : it->second;
+    }
     int32_t* d_pattern = nullptr;
     std::string err;
     std::map<std::pair<int, int>, ResClass> classes;

@@ -37,6 +37,7 @@ struct SrvClass {
     int W0 = 0, H0 = 0;
     int first_slot = 0, n_slots = 0;
     int tiles_per_frame = 0;
+    int shape = 0;                // detect tile shape (index into kTileShapes)
     std::vector<TileItem> tiles;  // one frame's tile list (frame field patched per launch)
 };
 
@@ -145,7 +146,7 @@ cudaError_t launch_batch(uslam_server* s, const std::vector<uint64_t>& tickets, 
     LaunchBuf& B = s->bufs[bufi];
     cudaStream_t st = s->cs[bufi];
     const int lv = s->levels;
-    std::vector<TileItem> tiles;
+    ShapedTiles shaped;
     std::vector<SegDev> fsegs, usegs;
     std::vector<MatchSegDev> msegs;
     std::vector<PairDev> pairs;
@@ -156,7 +157,7 @@ cudaError_t launch_batch(uslam_server* s, const std::vector<uint64_t>& tickets, 
         const SrvClass& C = s->classes[sl.cls];
         for (TileItem t : C.tiles) {
             t.frame = static_cast<uint16_t>(r.slot);
-            tiles.push_back(t);
+            shaped.by_shape[C.shape].push_back(t);
         }
         for (int l = 0; l < lv; ++l) fsegs.push_back(SegDev{r.slot, l});
         const FrameDev& F = s->frames[r.slot];
@@ -192,6 +193,8 @@ cudaError_t launch_batch(uslam_server* s, const std::vector<uint64_t>& tickets, 
             }
         }
     }
+    shaped.finish();
+    const std::vector<TileItem>& tiles = shaped.flat;
     // table image: tiles | fsegs | msegs | usegs | pairs
     const size_t t_b = round_up(tiles.size() * sizeof(TileItem), 256);
     const size_t f_b = round_up(fsegs.size() * sizeof(SegDev), 256);
@@ -215,7 +218,7 @@ cudaError_t launch_batch(uslam_server* s, const std::vector<uint64_t>& tickets, 
     const auto* d_pairs = reinterpret_cast<const PairDev*>(B.d + t_b + f_b + m_b + u_b);
     const int grid = c->num_sms * 4;
     const int nf = static_cast<int>(fsegs.size());
-    if ((e = launch_detect(s->d_frames, d_tiles, static_cast<int>(tiles.size()), s->d_err, st)) != cudaSuccess) return e;
+    if ((e = launch_detect_shaped(s->d_frames, d_tiles, shaped.begin, s->d_err, st)) != cudaSuccess) return e;
     if ((e = launch_blur_border(s->d_frames, d_fsegs, nf, grid, st)) != cudaSuccess) return e;
     if ((e = launch_compact(s->d_frames, d_fsegs, nf, s->max_w, st)) != cudaSuccess) return e;
     if ((e = launch_describe(s->d_frames, d_fsegs, nf, c->d_pattern, grid, st)) != cudaSuccess) return e;
@@ -337,6 +340,7 @@ uslam_status uslam_server_create(uslam_ctx* ctx, const uslam_server_params* p, u
         F.H0 = H0;
         F.levels = L;
         F.margin = ctx->margin;
+        F.cell_cap = ctx->cell_cap;
         F.img_pitch = static_cast<int>(round_up(static_cast<size_t>(W0), 16));
         level_dims(W0, H0, L, F.w, F.h);
         for (int l = 0; l < L; ++l)
@@ -368,16 +372,9 @@ uslam_status uslam_server_create(uslam_ctx* ctx, const uslam_server_params* p, u
             Y.kpmap[l] = take(static_cast<size_t>(F.h[l]) * F.kp_pitch[l]);
             Y.xorder[l] = take(capa * 4);
             Y.colstart[l] = take((static_cast<size_t>(F.w[l]) + 1) * 4);
-            const int nx = (F.w[l] + kTileW - 1) / kTileW, ny = (F.h[l] + kTileH - 1) / kTileH;
-            for (int ty = 0; ty < ny; ++ty)
-                for (int tx = 0; tx < nx; ++tx) {
-                    TileItem t{};
-                    t.level = static_cast<uint8_t>(l);
-                    t.tx = static_cast<uint16_t>(tx);
-                    t.ty = static_cast<uint16_t>(ty);
-                    C.tiles.push_back(t);
-                }
         }
+        C.shape = ctx->shape_for(W0, H0);
+        append_tiles(&C.tiles, 0, F, C.shape);
         Y.a2b = take(static_cast<size_t>(L) * capa * 4);
         Y.b2a = take(static_cast<size_t>(L) * capa * 4);
         Y.matches = take(static_cast<size_t>(L) * capa * 16);

@@ -32,6 +32,7 @@ struct FrameDev {
     int kp_pitch[USLAM_MAX_LEVELS];
     int bl_pitch[USLAM_MAX_LEVELS];  // blur cache row pitch (floats): w + margin + 1
     int margin;                      // blur cache margin M beyond the level
+    int cell_cap;                    // > 0: keypoints kept per 32x32 cell (cell order); 0: (y, x) order
     float* lvl[USLAM_MAX_LEVELS];
     float* blur[USLAM_MAX_LEVELS];
     uint8_t* kpmap[USLAM_MAX_LEVELS];

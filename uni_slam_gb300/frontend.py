@@ -25,16 +25,19 @@ def level_dims(width: int, height: int, levels: int = 6) -> list[tuple[int, int]
 
 
 class Context:
-    """Device context: BRIEF table, level count, cap, size limits."""
+    """Device context: BRIEF table, level count, caps (per level and, with
+    cell_cap > 0, per 32x32 cell), size limits, matcher (0: the reference's
+    windowed mutual matcher, 1: brute-force top-2 with Lowe ``ratio``)."""
 
     def __init__(self, pattern: np.ndarray, levels: int = 6, max_width: int = 4096, max_height: int = 4096,
-                 cap_per_level: int = 0, device: int = 0, matcher: int = 0, ratio: float = 0.8):
+                 cap_per_level: int = 0, device: int = 0, matcher: int = 0, ratio: float = 0.8,
+                 cell_cap: int = 0):
         self.lib = capi.load()
         self._pattern = np.ascontiguousarray(pattern, dtype=np.int32).reshape(-1)
         if self._pattern.size != 1024:
             raise ValueError("pattern must hold 256 x (ax, ay, bx, by)")
         p = capi.Params(device, levels, max_width, max_height, cap_per_level,
-                        self._pattern.ctypes.data_as(C.POINTER(C.c_int32)), matcher, ratio)
+                        self._pattern.ctypes.data_as(C.POINTER(C.c_int32)), matcher, ratio, cell_cap)
         h = C.c_void_p()
         st = self.lib.uslam_create(C.byref(p), C.byref(h))
         if st != capi.OK:
@@ -46,6 +49,33 @@ class Context:
         m = C.c_int()
         self.check(self.lib.uslam_blur_margin(self.h, C.byref(m)), "blur_margin")
         return m.value
+
+    def tile_shapes(self) -> list[tuple[int, int]]:
+        n = C.c_int()
+        self.check(self.lib.uslam_tile_shapes(C.byref(n), None, None), "tile_shapes")
+        tw = np.zeros(n.value, np.int32)
+        th = np.zeros(n.value, np.int32)
+        self.check(self.lib.uslam_tile_shapes(C.byref(n), iptr(tw), iptr(th)), "tile_shapes")
+        return [(int(a), int(b)) for a, b in zip(tw, th)]
+
+    def set_tile_shape(self, width: int, height: int, shape: int):
+        self.check(self.lib.uslam_set_tile_shape(self.h, width, height, shape), "set_tile_shape")
+
+    def tile_shape(self, width: int, height: int) -> int:
+        s = C.c_int()
+        self.check(self.lib.uslam_get_tile_shape(self.h, width, height, C.byref(s)), "get_tile_shape")
+        return s.value
+
+    def autotune(self, frame: np.ndarray, n_frames: int = 8, reps: int = 10) -> tuple[int, list[float]]:
+        """Time k_detect in every tile shape on n_frames copies of `frame`;
+        store the fastest for the frame's size.  Returns (shape, per-shape ms)."""
+        img = np.ascontiguousarray(frame, np.uint8)
+        h, w = img.shape
+        ms = np.zeros(len(self.tile_shapes()), np.float32)
+        s = C.c_int()
+        self.check(self.lib.uslam_autotune(self.h, w, h, ptr(img), w, n_frames, reps, C.byref(s), ptr(ms)),
+                   "autotune")
+        return s.value, [float(v) for v in ms]
 
     def error(self) -> str:
         return self.lib.uslam_last_error(self.h).decode()
