@@ -728,6 +728,30 @@ k_describe(const FrameDev* __restrict__ frames, const SegDev* __restrict__ segs,
     }
 }
 
+// ------------------------------------------------- Hamming distance ----
+// popcount(a ^ b) over 256 bits with 4 POPC instead of 8: three carry-save
+// adders fold x0..x6 into ones (o3) and twos (t1, t2, t3), a fourth folds
+// the twos into twos (tw) and fours (f); x7 is added as ones.  Per bit
+// position x0 + .. + x7 = o3 + x7 + 2 tw + 4 f, so the sum of the weighted
+// popcounts is the exact distance (integer arithmetic, no rounding).
+// POPC issues at a quarter of the ALU rate, so this trades 4 POPC for
+// 8 LOP3.
+__device__ __forceinline__ uint32_t hamming256(const uint4& a0, const uint4& a1, const uint4& b0, const uint4& b1) {
+    const uint32_t x0 = a0.x ^ b0.x, x1 = a0.y ^ b0.y, x2 = a0.z ^ b0.z, x3 = a0.w ^ b0.w;
+    const uint32_t x4 = a1.x ^ b1.x, x5 = a1.y ^ b1.y, x6 = a1.z ^ b1.z, x7 = a1.w ^ b1.w;
+    const uint32_t o1 = x0 ^ x1 ^ x2, t1 = (x0 & x1) | (x2 & (x0 ^ x1));
+    const uint32_t o2 = o1 ^ x3 ^ x4, t2 = (o1 & x3) | (x4 & (o1 ^ x3));
+    const uint32_t o3 = o2 ^ x5 ^ x6, t3 = (o2 & x5) | (x6 & (o2 ^ x5));
+    const uint32_t tw = t1 ^ t2 ^ t3, f = (t1 & t2) | (t3 & (t1 ^ t2));
+    return (uint32_t)__popc(o3) + (uint32_t)__popc(x7) + 2u * (uint32_t)__popc(tw) + 4u * (uint32_t)__popc(f);
+}
+
+// Index of the lowest set bit of a non-zero word without the XU pipe: the
+// isolated bit times a de Bruijn constant puts a distinct 5-bit pattern in
+// the top bits (the classic multiply-and-lookup method).
+__constant__ uint8_t c_debruijn[32] = {0,  1,  28, 2,  29, 14, 24, 3,  30, 22, 20, 15, 25, 17, 4,  8,
+                                      31, 27, 13, 23, 21, 19, 16, 7,  26, 12, 18, 6,  11, 5,  10, 9};
+
 // ------------------------------------------------------------- K3 ----
 constexpr int KM_THREADS = 256;
 
@@ -759,27 +783,30 @@ __device__ int last_col_le(float hi, float s, int w) {
     return xb;
 }
 
-// One candidate staged in shared memory: LOD-0 coordinates, packed
-// (level, index) and descriptor.
-struct CandSlot {
-    float px, py;
-    int32_t idx;
-    uint32_t pad;
-    uint4 d0, d1;
+// Candidates staged in shared memory per warp (32 at a time): LOD-0 y,
+// packed (level, index) and descriptor halves.
+struct CandStage {
+    float py[32];
+    int32_t idx[32];
+    uint4 d0[32], d1[32];
+    uint8_t debruijn[32];  // shared-memory copy of c_debruijn (lanes index it divergently)
 };
 
 // A warp takes 32 queries that are consecutive in x (from the query level's
 // x order) and streams the union of their spatial windows, level by level of
-// the pool, through shared memory; every lane tests each broadcast candidate
-// against its own window (match_features_cpu.cpp:108-141) and keeps its
-// running best / second-best distance.  The result does not depend on the
+// the pool, through shared memory.  Each lane's own x-window is an exact
+// index range of the x-ordered pool ([colstart[first col >= lo],
+// colstart[last col <= hi + 1])), so per staged batch a lane tests the y
+// condition only inside its range, collects the hits in a bit mask and
+// computes Hamming distances for those hits alone
+// (match_features_cpu.cpp:108-141).  The result does not depend on the
 // candidate order: a tied best always fails the ratio test.
 __global__ void __launch_bounds__(KM_THREADS)
 k_match(const FrameDev* __restrict__ frames, const PairDev* __restrict__ pairs,
         const MatchSegDev* __restrict__ segs, int nseg) {
     __shared__ uint32_t s_pref[MAX_SEGS + 1];
     __shared__ uint32_t s_warp[33];
-    __shared__ CandSlot s_cand[KM_THREADS / 32][32];
+    __shared__ CandStage s_stage[KM_THREADS / 32];
     const uint32_t total = segment_prefix(nseg, s_pref, s_warp, [&](int s) {
         const PairDev& P = pairs[segs[s].pair];
         const int qf = segs[s].dir == 0 ? P.curr : P.prev;
@@ -789,7 +816,9 @@ k_match(const FrameDev* __restrict__ frames, const PairDev* __restrict__ pairs,
     const int warp = threadIdx.x >> 5;
     const int gw = blockIdx.x * (KM_THREADS / 32) + warp;
     const int nw = gridDim.x * (KM_THREADS / 32);
-    CandSlot* slots = s_cand[warp];
+    CandStage& S = s_stage[warp];
+    S.debruijn[lane] = c_debruijn[lane];
+    __syncwarp();
     for (uint32_t g = gw; g < total; g += nw) {
         const int sidx = find_segment(s_pref, nseg, g);
         const uint32_t grp = g - s_pref[sidx];
@@ -818,23 +847,30 @@ k_match(const FrameDev* __restrict__ frames, const PairDev* __restrict__ pairs,
         if (l > 0) pool += B.kept[l - 1];
         if (l + 1 < L) pool += B.kept[l + 1];
         if (pool >= 2u) {
-            // union of the lanes' windows
-            float lo_min = valid ? lo : __int_as_float(0x7f800000);
-            float hi_max = valid ? hi : -__int_as_float(0x7f800000);
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) {
-                lo_min = fminf(lo_min, __shfl_xor_sync(0xffffffffu, lo_min, o));
-                hi_max = fmaxf(hi_max, __shfl_xor_sync(0xffffffffu, hi_max, o));
-            }
             for (int k = 0; k < 3; ++k) {
                 const int pl = k == 0 ? l : (k == 1 ? l - 1 : l + 1);
                 if (pl < 0 || pl >= L) continue;
                 const float ps = lod_scale(pl);
                 const int wpl = B.w[pl];
-                const int xlo = first_col_ge(lo_min, ps, wpl);
-                const int xhi = last_col_le(hi_max, ps, wpl);
-                if (xlo > xhi) continue;
-                const uint32_t c0 = __ldg(B.colstart[pl] + xlo), c1 = __ldg(B.colstart[pl] + xhi + 1);
+                const uint32_t* colstart = B.colstart[pl];
+                // this lane's exact candidate range
+                uint32_t m0 = 0u, m1 = 0u;
+                if (valid) {
+                    const int xlo = first_col_ge(lo, ps, wpl);
+                    const int xhi = last_col_le(hi, ps, wpl);
+                    if (xlo <= xhi) {
+                        m0 = __ldg(colstart + xlo);
+                        m1 = __ldg(colstart + xhi + 1);
+                    }
+                }
+                // union over the warp (lanes are x-sorted, so this is contiguous)
+                uint32_t c0 = m0 < m1 ? m0 : 0xffffffffu, c1 = m1;
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) {
+                    c0 = min(c0, __shfl_xor_sync(0xffffffffu, c0, o));
+                    c1 = max(c1, __shfl_xor_sync(0xffffffffu, c1, o));
+                }
+                if (c0 >= c1) continue;
                 const uint32_t* xorder = B.xorder[pl];
                 const uint32_t* feats = B.feats[pl];
                 for (uint32_t base = c0; base < c1; base += 32u) {
@@ -842,34 +878,27 @@ k_match(const FrameDev* __restrict__ frames, const PairDev* __restrict__ pairs,
                     if (kk < c1) {
                         const uint32_t j = __ldg(xorder + kk);
                         const uint32_t* rec = feats + (size_t)j * 12u;
-                        CandSlot cs;
-                        cs.px = (float)(uint32_t)__uint_as_float(__ldg(rec)) * ps;
-                        cs.py = (float)(uint32_t)__uint_as_float(__ldg(rec + 1)) * ps;
-                        cs.idx = USLAM_PACK(pl, j);
-                        cs.pad = 0u;
-                        cs.d0 = __ldg(reinterpret_cast<const uint4*>(rec + 4));
-                        cs.d1 = __ldg(reinterpret_cast<const uint4*>(rec + 8));
-                        slots[lane] = cs;
+                        S.py[lane] = (float)(uint32_t)__uint_as_float(__ldg(rec + 1)) * ps;
+                        S.idx[lane] = USLAM_PACK(pl, j);
+                        S.d0[lane] = __ldg(reinterpret_cast<const uint4*>(rec + 4));
+                        S.d1[lane] = __ldg(reinterpret_cast<const uint4*>(rec + 8));
                     }
                     __syncwarp();
-                    const int n = (int)min(32u, c1 - base);
-                    for (int t = 0; t < n; ++t) {
-                        const float px = slots[t].px, py = slots[t].py;
-                        const bool in = valid && px >= lo && px <= hi && !(fabsf(cy - py) > dy);
-                        if (__any_sync(0xffffffffu, in)) {
-                            const uint4 d0 = slots[t].d0, d1 = slots[t].d1;
-                            const uint32_t d = __popc(d0.x ^ qd0.x) + __popc(d0.y ^ qd0.y) + __popc(d0.z ^ qd0.z) +
-                                               __popc(d0.w ^ qd0.w) + __popc(d1.x ^ qd1.x) + __popc(d1.y ^ qd1.y) +
-                                               __popc(d1.z ^ qd1.z) + __popc(d1.w ^ qd1.w);
-                            if (in) {
-                                if (d < best) {
-                                    second = best;
-                                    best = d;
-                                    bidx = slots[t].idx;
-                                } else if (d < second) {
-                                    second = d;
-                                }
-                            }
+                    const int a = (int)(max(m0, base) - base);
+                    const int b = (int)(min(m1, base + 32u) > base ? min(m1, base + 32u) - base : 0u);
+                    uint32_t hits = 0u;
+                    for (int t = a; t < b; ++t)
+                        if (!(fabsf(cy - S.py[t]) > dy)) hits |= 1u << t;
+                    while (hits) {
+                        const int t = S.debruijn[((hits & (0u - hits)) * 0x077CB531u) >> 27];
+                        hits &= hits - 1u;
+                        const uint32_t d = hamming256(S.d0[t], S.d1[t], qd0, qd1);
+                        if (d < best) {
+                            second = best;
+                            best = d;
+                            bidx = S.idx[t];
+                        } else if (d < second) {
+                            second = d;
                         }
                     }
                     __syncwarp();
@@ -895,11 +924,6 @@ __device__ __forceinline__ int flat_level(const uint32_t* pre, int L, uint32_t f
     int l = 0;
     while (l + 1 < L && pre[l + 1] <= f) ++l;
     return l;
-}
-
-__device__ __forceinline__ uint32_t hamming256(const uint4& a0, const uint4& a1, const uint4& b0, const uint4& b1) {
-    return __popc(a0.x ^ b0.x) + __popc(a0.y ^ b0.y) + __popc(a0.z ^ b0.z) + __popc(a0.w ^ b0.w) +
-           __popc(a1.x ^ b1.x) + __popc(a1.y ^ b1.y) + __popc(a1.z ^ b1.z) + __popc(a1.w ^ b1.w);
 }
 
 // Brute-force top-2 matching (the benchmark's `cfg` matcher): every feature
