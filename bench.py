@@ -14,7 +14,9 @@ D2H of every feature record and match list inside the timed region;
 synchronous per frame); ``served`` = 32 camera streams at 20 Hz through the
 serving loop (p50/p99 latency, frames/s); ``uneven`` = 46 frames of five
 sizes (640x480 .. 3840x2160) each matched against its warp in one graph,
-per-32x32-cell caps, detect tiles autotuned per size; ``stress`` = 3840x2160 frames,
+per-32x32-cell caps, detect tiles autotuned per size; ``cfg`` = the main
+workload in the cfg profile (FAST 9-of-16 at 20/255, 3x3 NMS, brute-force
+ratio 0.8); ``stress`` = 3840x2160 frames,
 8 levels, 2500 features per level (20000 per frame), brute-force top-2
 matching of every frame against a seeded warp of itself, 8 such pairs per
 batch.  ``--impl reference`` times the CPU restatement of the reference's
@@ -57,6 +59,7 @@ def _args():
     ap.add_argument("--stress-pairs", type=int, default=8, help="3840x2160 frame/warp pairs (0: skip)")
     ap.add_argument("--stress-steps", type=int, default=5)
     ap.add_argument("--uneven", type=int, default=1, help="batched-uneven workload (0: skip)")
+    ap.add_argument("--cfg", type=int, default=1, help="cfg detection/matching profile on the main workload (0: skip)")
     return ap.parse_args()
 
 
@@ -414,6 +417,55 @@ def uneven_run(pat, local: int, pair_frames, steps: int, warmup: int, seed: int)
         ctx.close()
 
 
+def cfg_run(pat, local: int, frames, steps: int, warmup: int) -> dict:
+    """The batched-uniform workload in the cfg profile: FAST 9-of-16 at 20/255
+    with 3x3 NMS, brute-force top-2 matching at ratio 0.8 (all features of
+    each frame against all features of the previous one)."""
+    import torch
+
+    from uni_slam_gb300 import Batch, Context
+
+    n = len(frames)
+    ctx = Context(pat, levels=LEVELS, max_width=W, max_height=H, device=local, detector=1, matcher=1, ratio=0.8)
+    batch = Batch(ctx, [(W, H)] * n, [(i, i + 1) for i in range(n - 1)])
+    try:
+        for i, f in enumerate(frames):
+            batch.set_frame(i, f)
+        batch.upload()
+        batch.sync()
+        stream = torch.cuda.Stream()
+        batch.set_stream(stream.cuda_stream)
+        l2_flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+        for _ in range(warmup):
+            batch.run()
+        stream.synchronize()
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+        with torch.cuda.stream(stream):
+            for e0, e1 in evs:
+                l2_flush.zero_()
+                e0.record(stream)
+                batch.run()
+                e1.record(stream)
+        stream.synchronize()
+        step_ms = sum(e0.elapsed_time(e1) for e0, e1 in evs) / steps
+        batch.download()
+        batch.sync()
+        kept = [int(batch.features(i)[1].sum()) for i in range(n)]
+        nmatch = [len(batch.matches(k)) for k in range(n - 1)]
+        prof = batch.profile(iters=3)
+        prof = {("k_bruteforce" if k == "k_match" else "k_emit" if k == "k_mutual" else k): v for k, v in prof.items()}
+        return {
+            "workload": f"cfg profile on the batched-uniform workload: {n} frames of 752x480, FAST 9-of-16 at 20/255 "
+                        "with 3x3 NMS, brute-force top-2 Hamming matching at ratio 0.8 against the previous frame",
+            "frames": n, "ms_per_step": step_ms, "frames_per_s": n / (step_ms / 1e3),
+            "features_per_frame": sum(kept) / n, "matches_per_pair": sum(nmatch) / max(1, n - 1),
+            "kernel_ms": prof, "l2": "flushed (256 MiB write) between timed steps",
+        }
+    finally:
+        batch.close()
+        ctx.close()
+
+
 def _stress_pair(seed: int):
     from uni_slam_gb300 import synth
 
@@ -635,6 +687,8 @@ def run_ours(a):
         served = serve_simulation(sctx, a.serve_seconds, n_streams=a.serve_streams, seed=a.seed + rank)
         sctx.close()
 
+    cfg = cfg_run(pat, local, frames, a.stress_steps, 2) if a.cfg else None
+
     uneven = None
     if uneven_frames:
         uneven = uneven_run(pat, local, uneven_frames, a.stress_steps, 2, a.seed)
@@ -667,7 +721,7 @@ def run_ours(a):
             "e2e": {"value": n * world / e2e_s, "unit": "frames/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
             "gpu_launches": 6 * a.steps, "roofline": roofline, "cpu_baseline": cpu, "clocks": clk,
-            "served": served, "uneven": uneven, "stress": stress,
+            "served": served, "uneven": uneven, "stress": stress, "cfg": cfg,
             "features_per_frame": sum(kept) / n, "matches_per_pair": sum(nmatch) / max(1, n - 1),
             "wall_s_timed": wall_s,
         }

@@ -85,6 +85,15 @@ typedef struct uslam_params {
      * counterpart: the reference keeps whichever keypoints win its atomic
      * append (generate_features.wgsl:67-70). */
     int cell_cap;
+    /* 0: the reference's detector (FAST response, resources/detect_corners.wgsl,
+     *    and its cull, resources/cull_corners.wgsl).
+     * 1: the `cfg` profile, no reference counterpart: FAST 9-of-16 with
+     *    wrap-around, a circle point brighter iff p - c > 20/255 or darker iff
+     *    c - p > 20/255; pixels within 3 of a level edge are never corners;
+     *    score = sum of (|p - c| - 20/255) over the qualifying points in
+     *    circle order; 3x3 non-maximum suppression on the score, a tie going
+     *    to the first pixel in raster order; strength = the arc length. */
+    int detector;
 } uslam_params;
 
 /* ---- context ---------------------------------------------------------- */

@@ -41,7 +41,10 @@ def lib():
         L.orc_gauss_tap9.restype = C.c_float
         L.orc_frame.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, vp, vp, C.c_int, vp, vp]
         L.orc_frame.restype = C.c_int
-        L.orc_frame_ex.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, vp, vp, C.c_int, vp, vp]
+        L.orc_frame_ex.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, vp, vp, C.c_int,
+                                   vp, vp]
+        L.orc_detect_cfg.argtypes = [vp, C.c_uint32, C.c_uint32, vp]
+        L.orc_detect_cfg.restype = None
         L.orc_frame_ex.restype = C.c_int
         L.orc_match.argtypes = [vp, vp, vp, vp, C.c_int, C.c_int, C.c_int, vp, C.c_int]
         L.orc_match.restype = C.c_int
@@ -90,6 +93,15 @@ def cull(resp: np.ndarray, W0: int, H0: int) -> np.ndarray:
     return out
 
 
+def detect_cfg(lvl: np.ndarray) -> np.ndarray:
+    """cfg detection profile on one level: arc length of NMS survivors, else 0."""
+    lvl = np.ascontiguousarray(lvl, np.float32)
+    h, w = lvl.shape
+    out = np.zeros((h, w), np.uint32)
+    lib().orc_detect_cfg(_p(lvl), w, h, _p(out))
+    return out
+
+
 def gauss_tap9(lvl: np.ndarray, px: int, py: int) -> float:
     lvl = np.ascontiguousarray(lvl, np.float32)
     h, w = lvl.shape
@@ -114,9 +126,11 @@ def describe(lvl: np.ndarray, x: int, y: int, pattern: np.ndarray):
     return float(th[0]), d
 
 
-def frame(img: np.ndarray, pattern: np.ndarray, levels: int = 6, cap: int | None = None, cell_cap: int = 0):
+def frame(img: np.ndarray, pattern: np.ndarray, levels: int = 6, cap: int | None = None, cell_cap: int = 0,
+          detector: int = 0):
     """Features of one frame: (features[FEATURE_DTYPE], kept[levels], raw[levels]).
-    cell_cap > 0 keeps at most cell_cap keypoints per 32x32 cell, listed cell by cell."""
+    cell_cap > 0 keeps at most cell_cap keypoints per 32x32 cell, listed cell by cell;
+    detector = 1 selects the cfg detection profile (FAST 9-of-16 at 20/255, 3x3 NMS)."""
     img = np.ascontiguousarray(img, np.uint8)
     H0, W0 = img.shape
     if cap is None:
@@ -127,8 +141,8 @@ def frame(img: np.ndarray, pattern: np.ndarray, levels: int = 6, cap: int | None
     feats = np.zeros(max_feats, FEATURE_DTYPE)
     kept = np.zeros(levels, np.int32)
     raw = np.zeros(levels, np.int32)
-    n = lib().orc_frame_ex(_p(img), W0, H0, W0, levels, cap, cell_cap, _p(pat), _p(feats), max_feats, _p(kept),
-                           _p(raw))
+    n = lib().orc_frame_ex(_p(img), W0, H0, W0, levels, cap, cell_cap, detector, _p(pat), _p(feats), max_feats,
+                           _p(kept), _p(raw))
     if n < 0:
         raise RuntimeError("orc_frame: feature buffer too small")
     return feats[:n].copy(), kept, raw

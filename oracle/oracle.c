@@ -255,6 +255,74 @@ void orc_describe(const float* lvl, uint32_t w, uint32_t h, int x, int y, const 
 
 /* --------------------------------------------------------------- frame -- */
 
+/* ---------------------------------------------------- cfg detector -- */
+/* The benchmark's `cfg` detection profile (no counterpart in the reference,
+ * pinned by this definition): FAST 9-of-16 with wrap-around on the level's
+ * f32 pixels, threshold T = 20/255 (brighter iff p - c > T, darker iff
+ * c - p > T), circle of resources/detect_corners.wgsl:31-32; pixels within 3
+ * of a level edge are never corners; score = sum over the qualifying
+ * polarity's points, in circle order, of (|p - c| - T); 3x3 non-maximum
+ * suppression on the score, a tie going to the first pixel in raster order;
+ * strength = the longest circular arc (9..16). */
+static const int circ_x[16] = {0, 1, 2, 3, 3, 3, 2, 1, 0, -1, -2, -3, -3, -3, -2, -1};
+static const int circ_y[16] = {-3, -3, -2, -1, 0, 1, 2, 3, 3, 3, 2, 1, 0, -1, -2, -3};
+
+static uint32_t circ_run(uint32_t m) {
+    if (m == 0xffffu) return 16u;
+    uint32_t x = m | (m << 16), run = 0;
+    while (x) {
+        x &= x << 1;
+        ++run;
+    }
+    return run;
+}
+
+void orc_detect_cfg(const float* lvl, uint32_t w, uint32_t h, uint32_t* out) {
+    const float T = 20.0f / 255.0f;
+    const size_t n = (size_t)w * h;
+    float* score = (float*)calloc(n, sizeof(float));
+    uint32_t* arc = (uint32_t*)calloc(n, sizeof(uint32_t));
+    for (uint32_t y = 3; y + 3 < h; ++y)
+        for (uint32_t x = 3; x + 3 < w; ++x) {
+            const float c = lvl[(size_t)y * w + x];
+            uint32_t mb = 0, md = 0;
+            for (int i = 0; i < 16; ++i) {
+                const float p = lvl[(size_t)(y + circ_y[i]) * w + (x + circ_x[i])];
+                if (p - c > T) mb |= 1u << i;
+                if (c - p > T) md |= 1u << i;
+            }
+            const uint32_t rb = circ_run(mb), rd = circ_run(md);
+            if (rb < 9u && rd < 9u) continue;
+            const int bright = rb >= 9u;
+            const uint32_t m = bright ? mb : md;
+            float sc = 0.0f;
+            for (int i = 0; i < 16; ++i) {
+                if (!((m >> i) & 1u)) continue;
+                const float p = lvl[(size_t)(y + circ_y[i]) * w + (x + circ_x[i])];
+                sc = sc + ((bright ? p - c : c - p) - T);
+            }
+            score[(size_t)y * w + x] = sc;
+            arc[(size_t)y * w + x] = bright ? rb : rd;
+        }
+    for (uint32_t y = 0; y < h; ++y)
+        for (uint32_t x = 0; x < w; ++x) {
+            const size_t p = (size_t)y * w + x;
+            uint32_t keep = arc[p];
+            for (int dy = -1; dy <= 1 && keep; ++dy)
+                for (int dx = -1; dx <= 1 && keep; ++dx) {
+                    if (dy == 0 && dx == 0) continue;
+                    const long qy = (long)y + dy, qx = (long)x + dx;
+                    if (qy < 0 || qx < 0 || qy >= (long)h || qx >= (long)w) continue;
+                    const float q = score[(size_t)qy * w + (size_t)qx];
+                    const int earlier = dy < 0 || (dy == 0 && dx < 0);
+                    if (earlier ? !(score[p] > q) : !(score[p] >= q)) keep = 0;
+                }
+            out[p] = keep;
+        }
+    free(score);
+    free(arc);
+}
+
 /* Keep one keypoint: header plus descriptor; returns 0 if feats is full. */
 static int emit(const float* lvl, uint32_t w, uint32_t h, int x, int y, uint32_t strength, const int32_t* pattern,
                 orc_feature* feats, int max_feats, int* total) {
@@ -268,7 +336,7 @@ static int emit(const float* lvl, uint32_t w, uint32_t h, int x, int y, uint32_t
     return 1;
 }
 
-int orc_frame_ex(const uint8_t* img, int W0, int H0, int pitch, int levels, int cap, int cell_cap,
+int orc_frame_ex(const uint8_t* img, int W0, int H0, int pitch, int levels, int cap, int cell_cap, int detector,
                  const int32_t* pattern, orc_feature* feats, int max_feats, int* kept, int* raw) {
     uint32_t ws[32], hs[32];
     orc_level_dims(W0, H0, levels, ws, hs);
@@ -280,8 +348,12 @@ int orc_frame_ex(const uint8_t* img, int W0, int H0, int pitch, int levels, int 
         uint32_t* resp = (uint32_t*)malloc(n * sizeof(uint32_t));
         uint32_t* culled = (uint32_t*)malloc(n * sizeof(uint32_t));
         orc_pyramid_level(img, W0, H0, pitch, w, h, l == 0, lvl);
-        orc_detect(lvl, w, h, resp);
-        orc_cull(resp, w, h, W0, H0, culled);
+        if (detector == 1) {
+            orc_detect_cfg(lvl, w, h, culled);
+        } else {
+            orc_detect(lvl, w, h, resp);
+            orc_cull(resp, w, h, W0, H0, culled);
+        }
         int nraw = 0, nkept = 0;
         for (size_t p = 0; p < n; ++p) nraw += culled[p] != 0u;
         if (cell_cap <= 0) {
@@ -321,7 +393,7 @@ int orc_frame_ex(const uint8_t* img, int W0, int H0, int pitch, int levels, int 
 
 int orc_frame(const uint8_t* img, int W0, int H0, int pitch, int levels, int cap,
               const int32_t* pattern, orc_feature* feats, int max_feats, int* kept, int* raw) {
-    return orc_frame_ex(img, W0, H0, pitch, levels, cap, 0, pattern, feats, max_feats, kept, raw);
+    return orc_frame_ex(img, W0, H0, pitch, levels, cap, 0, 0, pattern, feats, max_feats, kept, raw);
 }
 
 /* --------------------------------------------------------------- match -- */

@@ -11,6 +11,9 @@
  *    wslam/src/pose_estimate_cpu/match_features_cpu.cpp, compiled unmodified
  *    with shim headers (oracle/Makefile, oracle/ref_harness.cpp), on random
  *    feature sets, and against golden vectors made from that build.
+ *  - cfg detection profile (orc_detect_cfg) and the brute-force matcher
+ *    (orc_match_bruteforce): defined here, no reference counterpart; pinned
+ *    by numpy statements of the same definitions in the tests.
  *  - Pyramid / detect / cull / describe: PARITY UNPINNED.  They restate the
  *    WGSL shaders (resources/*.wgsl) line by line, but the reference cannot
  *    execute them anywhere (Dawn is not built, and there is no graphics stack)
@@ -73,8 +76,14 @@ int orc_frame(const uint8_t* img, int W0, int H0, int pitch, int levels, int cap
  * 32x32 cells from its origin, cells visited in row-major order and pixels
  * within a cell in (y, x) order; the first cell_cap keypoints of each cell
  * are kept, and the level cap keeps the first `cap` of that sequence. */
-int orc_frame_ex(const uint8_t* img, int W0, int H0, int pitch, int levels, int cap, int cell_cap,
+int orc_frame_ex(const uint8_t* img, int W0, int H0, int pitch, int levels, int cap, int cell_cap, int detector,
                  const int32_t* pattern, orc_feature* feats, int max_feats, int* kept, int* raw);
+/* The `cfg` detection profile on one level (detector = 1 of orc_frame_ex):
+ * FAST 9-of-16 with wrap-around at 20/255, score = sum of (|p - c| - 20/255)
+ * over the qualifying points, 3x3 NMS (ties to the first pixel in raster
+ * order), pixels within 3 of the edge excluded.  out[p] = arc length (9..16)
+ * of a surviving corner, else 0.  No reference counterpart. */
+void orc_detect_cfg(const float* lvl, uint32_t w, uint32_t h, uint32_t* out);
 
 /* Matcher restated from wslam/src/pose_estimate_cpu/match_features_cpu.cpp:27-207.
  * a = previous (reference) set, b = current set; a_off/b_off hold levels+1

@@ -1,6 +1,7 @@
 // kernels.cu — sm_103a kernels of the GB300 feature front-end.
 //
 //   k_detect   (K1) pyramid level tile + FAST response + cull + blur cache
+//                   (or, in the cfg profile, FAST 9-of-16 at 20/255 + 3x3 NMS)
 //   k_blur_border   blur cache beyond the level edges (BRIEF points outside)
 //   k_compact       per (frame, level): ordered keypoint compaction, cap, x-sort
 //   k_describe (K2) orientation + 256-bit rotated BRIEF, one warp per keypoint
@@ -20,10 +21,14 @@
 namespace uslam {
 
 // K1 tile geometry: TW x TH output pixels (a template parameter pair, one of
-// kTileShapes), halo HX columns / HY rows.
+// kTileShapes), halo HX columns / HY rows (HY_CFG with the cfg profile, whose
+// 3x3 NMS needs the FAST score one pixel beyond the tile).
 constexpr int HX = 5;
 constexpr int HY = 3;
+constexpr int HY_CFG = 4;
 constexpr int K1_THREADS = 256;
+// cfg detection profile threshold: 20 grey levels on the u8/255 scale.
+constexpr float kCfgThreshold = 20.0f / 255.0f;
 
 // Bresenham circle of radius 3 (resources/detect_corners.wgsl:31-32).
 __constant__ int8_t c_circle_x[16] = {0, 1, 2, 3, 3, 3, 2, 1, 0, -1, -2, -3, -3, -3, -2, -1};
@@ -101,6 +106,51 @@ __device__ __forceinline__ uint32_t fast_response(const float (*sm)[SW], int r, 
     return run + 1u;
 }
 
+// Longest run of ones of a 16-bit circle mask, wrapping around (16 if all set).
+__device__ __forceinline__ uint32_t circular_run(uint32_t m) {
+    if (m == 0xffffu) return 16u;
+    uint32_t x = m | (m << 16), run = 0;
+    while (x) {
+        x &= x << 1;
+        ++run;
+    }
+    return run;
+}
+
+// cfg profile corner test at smem cell (r, c): FAST 9-of-16 with wrap-around,
+// brighter iff p - c > T, darker iff c - p > T (T = 20/255).  Returns the
+// score (sum over i = 0..15 of (|p_i - c| - T) for the points of the
+// qualifying polarity, added in index order) and the arc length (longest
+// circular run, 9..16) in *arc; 0 and 0 if not a corner.
+template <int SW>
+__device__ __forceinline__ float cfg_corner(const float (*sm)[SW], int r, int c, uint32_t* arc) {
+    const float center = sm[r][c];
+    float d[16];
+    uint32_t mb = 0, md = 0;
+#pragma unroll
+    for (int i = 0; i < 16; ++i) {
+        const float p = sm[r + c_circle_y[i]][c + c_circle_x[i]];
+        d[i] = p - center;
+        mb |= (d[i] > kCfgThreshold ? 1u : 0u) << i;
+        md |= ((center - p) > kCfgThreshold ? 1u : 0u) << i;
+    }
+    *arc = 0u;
+    if (__popc(mb) < 9 && __popc(md) < 9) return 0.0f;
+    const uint32_t rb = circular_run(mb), rd = circular_run(md);
+    if (rb < 9u && rd < 9u) return 0.0f;
+    const bool bright = rb >= 9u;
+    const uint32_t m = bright ? mb : md;
+    float score = 0.0f;
+#pragma unroll
+    for (int i = 0; i < 16; ++i) {
+        if (!((m >> i) & 1u)) continue;
+        const float dv = bright ? d[i] : (sm[r][c] - sm[r + c_circle_y[i]][c + c_circle_x[i]]);
+        score = score + (dv - kCfgThreshold);
+    }
+    *arc = bright ? rb : rd;
+    return score;
+}
+
 __device__ __forceinline__ bool mask_bit(const uint32_t* mask, int p) {
     return (__ldg(mask + (p >> 5)) >> (p & 31)) & 1u;
 }
@@ -111,9 +161,10 @@ __device__ __forceinline__ bool mask_bit(const uint32_t* mask, int p) {
 // value and the blur-cache value G(x, y).  Sampling coordinates depend only
 // on the row or only on the column, so they are computed once per tile row /
 // column (same operations as the per-pixel formula, hence the same bits).
-template <int TW, int TH>
+template <int TW, int TH, bool CFG>
 __global__ void __launch_bounds__(K1_THREADS)
 k_detect(const FrameDev* __restrict__ frames, const TileItem* __restrict__ tiles, uint32_t* err) {
+    constexpr int HY = CFG ? HY_CFG : uslam::HY;
     constexpr int SW = TW + 2 * HX;
     constexpr int SH = TH + 2 * HY;
     static_assert(K1_THREADS % TW == 0 && SW + SH + 3 * TH <= 2 * K1_THREADS, "tile shape");
@@ -125,6 +176,8 @@ k_detect(const FrameDev* __restrict__ frames, const TileItem* __restrict__ tiles
     __shared__ float s_fb[SH];
     __shared__ int s_by0[3][TH], s_by1[3][TH];   // blur taps: staged rows per output row
     __shared__ float s_bb[3][TH];
+    __shared__ float s_score[CFG ? TH + 2 : 1][CFG ? TW + 2 : 1];  // cfg: FAST score, tile + 1 ring
+    __shared__ uint8_t s_arc[CFG ? TH + 2 : 1][CFG ? TW + 2 : 1];
     const TileItem it = tiles[blockIdx.x];
     const FrameDev& F = frames[it.frame];
     const int l = it.level;
@@ -198,6 +251,21 @@ k_detect(const FrameDev* __restrict__ frames, const TileItem* __restrict__ tiles
     }
     __syncthreads();
 
+    if constexpr (CFG) {
+        // score of every pixel of the tile and its 1-pixel ring; pixels within
+        // 3 of the level edge (and outside the level) are never corners
+        for (int i = t; i < (TH + 2) * (TW + 2); i += K1_THREADS) {
+            const int sr = i / (TW + 2), sc = i - sr * (TW + 2);
+            const int y = Y0 - 1 + sr, x = X0 - 1 + sc;
+            uint32_t arc = 0u;
+            float score = 0.0f;
+            if (y >= 3 && y < h - 3 && x >= 3 && x < w - 3) score = cfg_corner(sm, sr - 1 + HY, sc - 1 + HX, &arc);
+            s_score[sr][sc] = score;
+            s_arc[sr][sc] = (uint8_t)arc;
+        }
+        __syncthreads();
+    }
+
     const int tx = t % TW;
     const int x = X0 + tx;
     if (x >= w) return;
@@ -229,19 +297,38 @@ k_detect(const FrameDev* __restrict__ frames, const TileItem* __restrict__ tiles
         const int r = ty + HY, c = tx + HX;
         const size_t p = (size_t)y * (size_t)w + (size_t)x;
 
-        // 2. FAST response + cull (resources/cull_corners.wgsl; see mask_bit)
-        const uint32_t S = fast_response(sm, r, c);
         uint32_t keep = 0;
-        if (S > 0u && mask_bit(mask, (int)p)) {
-            keep = S;
-            if (y == 0) {
-                // row 0: first arg-max of the 1x3 region [9k, min(9k+3, w))
-                const int start = x - x % 9;
-                const int end = min(start + 3, w);
-                for (int q = start; q < end; ++q) {
-                    if (q == x) continue;
-                    const uint32_t Sq = fast_response(sm, r, c + (q - x));
-                    if ((q < x && Sq >= S) || (q > x && Sq > S)) keep = 0;
+        if constexpr (CFG) {
+            // 3x3 NMS on the score; a tie goes to the first pixel in raster order
+            const uint32_t A = s_arc[ty + 1][tx + 1];
+            if (A) {
+                const float Sc = s_score[ty + 1][tx + 1];
+                bool ok = true;
+#pragma unroll
+                for (int dy = -1; dy <= 1; ++dy)
+#pragma unroll
+                    for (int dx = -1; dx <= 1; ++dx) {
+                        if (dy == 0 && dx == 0) continue;
+                        const float q = s_score[ty + 1 + dy][tx + 1 + dx];
+                        const bool earlier = dy < 0 || (dy == 0 && dx < 0);
+                        ok = ok && (earlier ? (Sc > q) : (Sc >= q));
+                    }
+                keep = ok ? A : 0u;
+            }
+        } else {
+            // 2. FAST response + cull (resources/cull_corners.wgsl; see mask_bit)
+            const uint32_t S = fast_response(sm, r, c);
+            if (S > 0u && mask_bit(mask, (int)p)) {
+                keep = S;
+                if (y == 0) {
+                    // row 0: first arg-max of the 1x3 region [9k, min(9k+3, w))
+                    const int start = x - x % 9;
+                    const int end = min(start + 3, w);
+                    for (int q = start; q < end; ++q) {
+                        if (q == x) continue;
+                        const uint32_t Sq = fast_response(sm, r, c + (q - x));
+                        if ((q < x && Sq >= S) || (q > x && Sq > S)) keep = 0;
+                    }
                 }
             }
         }
@@ -1098,18 +1185,25 @@ cudaError_t init_constants() {
     return cudaMemcpyToSymbol(c_disc_y, dy, sizeof(dy));
 }
 
-cudaError_t launch_detect(const FrameDev* frames, const TileItem* tiles, int ntiles, int shape, uint32_t* err,
-                          cudaStream_t st) {
-    if (ntiles <= 0) return cudaSuccess;
+template <bool CFG>
+cudaError_t launch_detect_profile(const FrameDev* frames, const TileItem* tiles, int ntiles, int shape, uint32_t* err,
+                                  cudaStream_t st) {
     switch (shape) {
-        case 0: k_detect<64, 32><<<ntiles, K1_THREADS, 0, st>>>(frames, tiles, err); break;
-        case 1: k_detect<128, 32><<<ntiles, K1_THREADS, 0, st>>>(frames, tiles, err); break;
-        case 2: k_detect<64, 16><<<ntiles, K1_THREADS, 0, st>>>(frames, tiles, err); break;
-        case 3: k_detect<32, 32><<<ntiles, K1_THREADS, 0, st>>>(frames, tiles, err); break;
-        case 4: k_detect<128, 16><<<ntiles, K1_THREADS, 0, st>>>(frames, tiles, err); break;
+        case 0: k_detect<64, 32, CFG><<<ntiles, K1_THREADS, 0, st>>>(frames, tiles, err); break;
+        case 1: k_detect<128, 32, CFG><<<ntiles, K1_THREADS, 0, st>>>(frames, tiles, err); break;
+        case 2: k_detect<64, 16, CFG><<<ntiles, K1_THREADS, 0, st>>>(frames, tiles, err); break;
+        case 3: k_detect<32, 32, CFG><<<ntiles, K1_THREADS, 0, st>>>(frames, tiles, err); break;
+        case 4: k_detect<128, 16, CFG><<<ntiles, K1_THREADS, 0, st>>>(frames, tiles, err); break;
         default: return cudaErrorInvalidValue;
     }
     return cudaGetLastError();
+}
+
+cudaError_t launch_detect(const FrameDev* frames, const TileItem* tiles, int ntiles, int shape, int detector,
+                          uint32_t* err, cudaStream_t st) {
+    if (ntiles <= 0) return cudaSuccess;
+    return detector == 1 ? launch_detect_profile<true>(frames, tiles, ntiles, shape, err, st)
+                         : launch_detect_profile<false>(frames, tiles, ntiles, shape, err, st);
 }
 
 cudaError_t launch_compact(const FrameDev* frames, const SegDev* segs, int nseg, int max_w, cudaStream_t st) {

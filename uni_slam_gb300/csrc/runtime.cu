@@ -117,7 +117,7 @@ cudaError_t enqueue_program(uslam_batch* b, const Program& P) {
     uslam_ctx* c = b->ctx;
     cudaError_t e = cudaSuccess;
     if (P.ntiles > 0) {
-        if ((e = launch_detect_shaped(b->d_frames, P.tiles, P.tile_begin, b->d_err, b->stream)) != cudaSuccess)
+        if ((e = launch_detect_shaped(b->d_frames, P.tiles, P.tile_begin, c->detector, b->d_err, b->stream)) != cudaSuccess)
             return e;
         const int grid = c->num_sms * 4;
         if ((e = launch_blur_border(b->d_frames, P.fsegs, P.nfsegs, grid, b->stream)) != cudaSuccess) return e;
@@ -540,7 +540,7 @@ uslam_status uslam_create(const uslam_params* params, uslam_ctx** out) {
         params->max_width > kMaxWidth || params->max_height < 1 || params->max_height > 65535 ||
         params->cap_per_level < 0 || params->cap_per_level >= (1 << 24) || !params->brief_pattern ||
         (params->matcher != 0 && params->matcher != 1) || (params->matcher == 1 && !(params->ratio > 0.0f)) ||
-        params->cell_cap < 0 || params->cell_cap > 1024)
+        params->cell_cap < 0 || params->cell_cap > 1024 || (params->detector != 0 && params->detector != 1))
         return USLAM_INVALID_ARG;
     auto* c = new uslam_ctx();
     c->device = params->device;
@@ -551,6 +551,7 @@ uslam_status uslam_create(const uslam_params* params, uslam_ctx** out) {
     c->matcher = params->matcher;
     c->ratio = params->ratio;
     c->cell_cap = params->cell_cap;
+    c->detector = params->detector;
     // blur-cache margin: a rotated test point lies within ceil(radius) + 1 of
     // its keypoint (rounding of the rotation), so radius + 2 covers it.
     double rmax = 0.0;
@@ -718,7 +719,7 @@ uslam_status uslam_batch_profile(uslam_batch* b, int iters, float* kernel_ms) {
             if (e == cudaSuccess) e = cudaEventRecord(ev[k++], b->stream);
         };
         mark();
-        if (e == cudaSuccess) e = launch_detect_shaped(b->d_frames, P.tiles, P.tile_begin, b->d_err, b->stream);
+        if (e == cudaSuccess) e = launch_detect_shaped(b->d_frames, P.tiles, P.tile_begin, c->detector, b->d_err, b->stream);
         mark();
         if (e == cudaSuccess) e = launch_blur_border(b->d_frames, P.fsegs, P.nfsegs, grid, b->stream);
         mark();
@@ -808,7 +809,7 @@ uslam_status uslam_autotune(uslam_ctx* ctx, int width, int height, const uint8_t
         std::vector<float> t;
         for (int r = -2; r < reps && e == cudaSuccess; ++r) {
             e = cudaEventRecord(e0, b->stream);
-            if (e == cudaSuccess) e = launch_detect(b->d_frames, d_tiles, n, s, b->d_err, b->stream);
+            if (e == cudaSuccess) e = launch_detect(b->d_frames, d_tiles, n, s, ctx->detector, b->d_err, b->stream);
             if (e == cudaSuccess) e = cudaEventRecord(e1, b->stream);
             if (e == cudaSuccess) e = cudaEventSynchronize(e1);
             float ms = 0.0f;

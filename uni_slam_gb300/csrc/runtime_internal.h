@@ -23,7 +23,7 @@ struct MatchSegDev {
     int level;
 };
 cudaError_t init_constants();
-cudaError_t launch_detect(const FrameDev*, const TileItem*, int, int, uint32_t*, cudaStream_t);
+cudaError_t launch_detect(const FrameDev*, const TileItem*, int, int, int, uint32_t*, cudaStream_t);
 cudaError_t launch_compact(const FrameDev*, const SegDev*, int, int, cudaStream_t);
 cudaError_t launch_blur_border(const FrameDev*, const SegDev*, int, int, cudaStream_t);
 cudaError_t launch_describe(const FrameDev*, const SegDev*, int, const int32_t*, int, cudaStream_t);
@@ -142,11 +142,11 @@ struct ShapedTiles {
 
 // One k_detect launch per tile shape present.
 inline cudaError_t launch_detect_shaped(const FrameDev* frames, const TileItem* d_tiles, const int* begin,
-                                        uint32_t* err, cudaStream_t st) {
+                                        int detector, uint32_t* err, cudaStream_t st) {
     for (int s = 0; s < kNumTileShapes; ++s) {
         const int n = begin[s + 1] - begin[s];
         if (n <= 0) continue;
-        const cudaError_t e = launch_detect(frames, d_tiles + begin[s], n, s, err, st);
+        const cudaError_t e = launch_detect(frames, d_tiles + begin[s], n, s, detector, err, st);
         if (e != cudaSuccess) return e;
     }
     return cudaSuccess;
@@ -171,6 +171,7 @@ struct uslam_ctx {
     int matcher = 0;      // 0 windowed mutual (reference), 1 brute-force top-2
     float ratio = 0.8f;   // Lowe ratio of the brute-force matcher
     int cell_cap = 0;     // > 0: keypoints kept per 32x32 cell of a level, cell order
+    int detector = 0;     // 0 reference FAST + cull, 1 cfg profile (FAST 9-of-16 at 20/255 + 3x3 NMS)
     std::map<std::pair<int, int>, int> tile_shape;  // per resolution class (autotuned or set)
     int shape_for(int W0, int H0) const {
         auto it = tile_shape.find(std::make_pair(W0, H0));

@@ -218,7 +218,7 @@ cudaError_t launch_batch(uslam_server* s, const std::vector<uint64_t>& tickets, 
     const auto* d_pairs = reinterpret_cast<const PairDev*>(B.d + t_b + f_b + m_b + u_b);
     const int grid = c->num_sms * 4;
     const int nf = static_cast<int>(fsegs.size());
-    if ((e = launch_detect_shaped(s->d_frames, d_tiles, shaped.begin, s->d_err, st)) != cudaSuccess) return e;
+    if ((e = launch_detect_shaped(s->d_frames, d_tiles, shaped.begin, c->detector, s->d_err, st)) != cudaSuccess) return e;
     if ((e = launch_blur_border(s->d_frames, d_fsegs, nf, grid, st)) != cudaSuccess) return e;
     if ((e = launch_compact(s->d_frames, d_fsegs, nf, s->max_w, st)) != cudaSuccess) return e;
     if ((e = launch_describe(s->d_frames, d_fsegs, nf, c->d_pattern, grid, st)) != cudaSuccess) return e;
