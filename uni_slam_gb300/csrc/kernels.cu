@@ -833,12 +833,6 @@ __device__ __forceinline__ uint32_t hamming256(const uint4& a0, const uint4& a1,
     return (uint32_t)__popc(o3) + (uint32_t)__popc(x7) + 2u * (uint32_t)__popc(tw) + 4u * (uint32_t)__popc(f);
 }
 
-// Index of the lowest set bit of a non-zero word without the XU pipe: the
-// isolated bit times a de Bruijn constant puts a distinct 5-bit pattern in
-// the top bits (the classic multiply-and-lookup method).
-__constant__ uint8_t c_debruijn[32] = {0,  1,  28, 2,  29, 14, 24, 3,  30, 22, 20, 15, 25, 17, 4,  8,
-                                      31, 27, 13, 23, 21, 19, 16, 7,  26, 12, 18, 6,  11, 5,  10, 9};
-
 // ------------------------------------------------------------- K3 ----
 constexpr int KM_THREADS = 256;
 
@@ -876,7 +870,6 @@ struct CandStage {
     float py[32];
     int32_t idx[32];
     uint4 d0[32], d1[32];
-    uint8_t debruijn[32];  // shared-memory copy of c_debruijn (lanes index it divergently)
 };
 
 // A warp takes 32 queries that are consecutive in x (from the query level's
@@ -904,8 +897,6 @@ k_match(const FrameDev* __restrict__ frames, const PairDev* __restrict__ pairs,
     const int gw = blockIdx.x * (KM_THREADS / 32) + warp;
     const int nw = gridDim.x * (KM_THREADS / 32);
     CandStage& S = s_stage[warp];
-    S.debruijn[lane] = c_debruijn[lane];
-    __syncwarp();
     for (uint32_t g = gw; g < total; g += nw) {
         const int sidx = find_segment(s_pref, nseg, g);
         const uint32_t grp = g - s_pref[sidx];
@@ -927,7 +918,9 @@ k_match(const FrameDev* __restrict__ frames, const PairDev* __restrict__ pairs,
         const float lo = cx - P.max_dx, hi = cx + P.max_dx;
         const float dy = P.max_dy;
 
-        uint32_t best = 0xffffffffu, second = 0xffffffffu;
+        // best / second-best as keys (distance << 5 | slot); a tie on the best
+        // distance leaves second >> 5 == best >> 5, which fails the ratio test
+        uint32_t bestk = 0xffffffffu, secondk = 0xffffffffu;
         int32_t bidx = -1;
         const int L = B.levels;
         uint32_t pool = B.kept[l];
@@ -976,25 +969,25 @@ k_match(const FrameDev* __restrict__ frames, const PairDev* __restrict__ pairs,
                     uint32_t hits = 0u;
                     for (int t = a; t < b; ++t)
                         if (!(fabsf(cy - S.py[t]) > dy)) hits |= 1u << t;
+                    // keys (distance << 5 | batch slot): min/max keep the two
+                    // smallest distances without branches; the slot of the best
+                    // is resolved to its candidate once per batch
+                    const uint32_t prev = bestk;
                     while (hits) {
-                        const int t = S.debruijn[((hits & (0u - hits)) * 0x077CB531u) >> 27];
-                        hits &= hits - 1u;
-                        const uint32_t d = hamming256(S.d0[t], S.d1[t], qd0, qd1);
-                        if (d < best) {
-                            second = best;
-                            best = d;
-                            bidx = S.idx[t];
-                        } else if (d < second) {
-                            second = d;
-                        }
+                        const int t = 31 - __clz(hits);
+                        hits ^= 1u << t;
+                        const uint32_t key = (hamming256(S.d0[t], S.d1[t], qd0, qd1) << 5) | (uint32_t)t;
+                        secondk = min(secondk, max(bestk, key));
+                        bestk = min(bestk, key);
                     }
+                    if (bestk != prev) bidx = S.idx[bestk & 31u];
                     __syncwarp();
                 }
             }
         }
         if (valid) {
             int32_t res = -1;
-            if (bidx >= 0 && (float)best < 0.85f * (float)second) res = bidx;
+            if (bidx >= 0 && (float)(bestk >> 5) < 0.85f * (float)(secondk >> 5)) res = bidx;
             const int capq = Q.cap;
             if (sg.dir == 0) P.b2a[(size_t)l * capq + qi] = res;
             else P.a2b[(size_t)l * capq + qi] = res;
@@ -1005,6 +998,7 @@ k_match(const FrameDev* __restrict__ frames, const PairDev* __restrict__ pairs,
 // ----------------------------------------------------- brute force ----
 constexpr int KB_THREADS = 128;  // two queries per thread: 256 queries per CTA
 constexpr int KB_TILE = 256;     // train descriptors per shared-memory tile
+static_assert(KB_TILE <= 256, "tile slots are packed into 8 bits of the top-2 keys");
 
 // Level of flat index f given the per-level prefix pre[0..L] (pre[L] = total).
 __device__ __forceinline__ int flat_level(const uint32_t* pre, int L, uint32_t f) {
@@ -1069,7 +1063,7 @@ k_bruteforce(const FrameDev* __restrict__ frames, const PairDev* __restrict__ pa
             const uint32_t* rec = A.feats[ql[k]] + (size_t)qi[k] * 12u;
             q0[k] = qv[k] ? *reinterpret_cast<const uint4*>(rec + 4) : make_uint4(0, 0, 0, 0);
             q1[k] = qv[k] ? *reinterpret_cast<const uint4*>(rec + 8) : make_uint4(0, 0, 0, 0);
-            best[k] = second[k] = 0xffffffffu;
+            best[k] = second[k] = 0xffffffffu;  // keys: distance << 8 | tile slot
             bidx[k] = -1;
         }
         for (uint32_t t0 = 0; t0 < nt; t0 += KB_TILE) {
@@ -1087,30 +1081,27 @@ k_bruteforce(const FrameDev* __restrict__ frames, const PairDev* __restrict__ pa
             }
             __syncthreads();
             const int n = (int)min((uint32_t)KB_TILE, nt - t0);
+            const uint32_t prev0 = best[0], prev1 = best[1];
             for (int j = 0; j < n; ++j) {
                 const uint4 d0 = s_d[2 * j], d1 = s_d[2 * j + 1];
 #pragma unroll
                 for (int k = 0; k < 2; ++k) {
-                    const uint32_t d = hamming256(q0[k], q1[k], d0, d1);
-                    if (d < best[k]) {
-                        second[k] = best[k];
-                        best[k] = d;
-                        bidx[k] = j;  // tile-local; resolved below
-                    } else if (d < second[k]) {
-                        second[k] = d;
-                    }
+                    // min/max on (distance << 8 | slot) keep the two smallest
+                    // distances; a tie leaves second >> 8 == best >> 8
+                    const uint32_t key = (hamming256(q0[k], q1[k], d0, d1) << 8) | (uint32_t)j;
+                    second[k] = min(second[k], max(best[k], key));
+                    best[k] = min(best[k], key);
                 }
             }
-            // resolve tile-local winners to packed ids before the tile is overwritten
-#pragma unroll
-            for (int k = 0; k < 2; ++k)
-                if (bidx[k] >= 0 && bidx[k] < KB_TILE) bidx[k] = KB_TILE + s_id[bidx[k]];
+            // resolve this tile's winners to packed ids before the tile is overwritten
+            if (best[0] != prev0) bidx[0] = s_id[best[0] & 255u];
+            if (best[1] != prev1) bidx[1] = s_id[best[1] & 255u];
         }
 #pragma unroll
         for (int k = 0; k < 2; ++k) {
             if (!qv[k]) continue;
-            const int32_t id = bidx[k] >= 0 ? bidx[k] - KB_TILE : -1;
-            const int32_t res = (nt >= 2u && id >= 0 && (float)best[k] < ratio * (float)second[k]) ? id : -1;
+            const int32_t res =
+                (nt >= 2u && bidx[k] >= 0 && (float)(best[k] >> 8) < ratio * (float)(second[k] >> 8)) ? bidx[k] : -1;
             P.a2b[(size_t)ql[k] * A.cap + qi[k]] = res;
         }
         __syncthreads();  // s_qpre / s_tpre are rewritten by the next work unit
