@@ -63,6 +63,8 @@ struct uslam_batch {
     char* d_tables = nullptr;
     cudaStream_t stream = nullptr;      // stream in use (own or caller's)
     cudaStream_t own_stream = nullptr;  // created with the batch
+    cudaStream_t aux_stream = nullptr;  // k_blur_border's branch beside k_compact
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     Program full;
     std::vector<Program> frame_prog;  // per frame: detect+describe only
     std::vector<Program> pair_prog;   // per pair: match only
@@ -120,8 +122,16 @@ cudaError_t enqueue_program(uslam_batch* b, const Program& P) {
         if ((e = launch_detect_shaped(b->d_frames, P.tiles, P.tile_begin, c->detector, b->d_err, b->stream)) != cudaSuccess)
             return e;
         const int grid = c->num_sms * 4;
-        if ((e = launch_blur_border(b->d_frames, P.fsegs, P.nfsegs, grid, b->stream)) != cudaSuccess) return e;
+        // k_blur_border (the blur cache's border) and k_compact (the keypoint
+        // lists) both read only what k_detect wrote: the border runs on a
+        // forked stream beside the compaction and joins before k_describe,
+        // which needs both (in a captured graph this is a fork/join).
+        if ((e = cudaEventRecord(b->ev_fork, b->stream)) != cudaSuccess) return e;
+        if ((e = cudaStreamWaitEvent(b->aux_stream, b->ev_fork, 0)) != cudaSuccess) return e;
+        if ((e = launch_blur_border(b->d_frames, P.fsegs, P.nfsegs, grid, b->aux_stream)) != cudaSuccess) return e;
+        if ((e = cudaEventRecord(b->ev_join, b->aux_stream)) != cudaSuccess) return e;
         if ((e = launch_compact(b->d_frames, P.fsegs, P.nfsegs, b->max_w, b->stream)) != cudaSuccess) return e;
+        if ((e = cudaStreamWaitEvent(b->stream, b->ev_join, 0)) != cudaSuccess) return e;
         if ((e = launch_describe(b->d_frames, P.fsegs, P.nfsegs, c->d_pattern, grid, b->stream)) != cudaSuccess)
             return e;
     }
@@ -171,6 +181,9 @@ void free_batch(uslam_batch* b) {
     for (auto& P : b->frame_prog) drop(P);
     for (auto& P : b->pair_prog) drop(P);
     if (b->own_stream) cudaStreamDestroy(b->own_stream);
+    if (b->aux_stream) cudaStreamDestroy(b->aux_stream);
+    if (b->ev_fork) cudaEventDestroy(b->ev_fork);
+    if (b->ev_join) cudaEventDestroy(b->ev_join);
     if (b->arena) cudaFree(b->arena);
     if (b->d_tables) cudaFree(b->d_tables);
     if (b->h_in) cudaFreeHost(b->h_in);
@@ -308,6 +321,9 @@ uslam_status create_batch(uslam_ctx* ctx, int n_frames, const int* widths, const
         return ctx->cuda_fail(e, "arena clear");
     }
     e = cudaStreamCreateWithFlags(&b->own_stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->aux_stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->ev_fork, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->ev_join, cudaEventDisableTiming);
     if (e != cudaSuccess) {
         free_batch(b);
         return ctx->cuda_fail(e, "stream create");
