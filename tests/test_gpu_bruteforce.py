@@ -57,3 +57,27 @@ def test_bruteforce_stress_size(brief_pattern):
             assert len(em) > 1000
         finally:
             b.close()
+
+
+def test_bruteforce_split_and_unsplit_agree(brief_pattern):
+    """A launch with few pairs splits each train set over several CTAs and
+    merges the partial top-2 records; a launch with many query blocks (large
+    per-level caps) does not split.  Both equal the oracle."""
+    pairs_frames = [synth.warped_pair(130 + k, 640, 480) for k in range(3)]
+    frames = [f for pr in pairs_frames for f in pr]
+    pairs = [(2 * k, 2 * k + 1) for k in range(3)]
+    exp = [oracle.frame(f, brief_pattern, cap=20000) for f in frames]
+    for cap in (20000, 1000):  # 3 x 469 query blocks: no split; 3 x 24: split
+        with Context(brief_pattern, levels=6, max_width=640, max_height=480, cap_per_level=cap, matcher=1,
+                     ratio=0.8) as c:
+            b = Batch(c, [(640, 480)] * len(frames), pairs)
+            try:
+                b.process(frames)
+                for k, (p, q) in enumerate(pairs):
+                    ep = exp[p] if cap == 20000 else oracle.frame(frames[p], brief_pattern, cap=cap)
+                    eq = exp[q] if cap == 20000 else oracle.frame(frames[q], brief_pattern, cap=cap)
+                    em = oracle.match_bruteforce(ep[0], ep[1], eq[0], eq[1], 0.8)
+                    assert np.array_equal(_mm(b.matches(k)), em), (cap, k)
+                    assert len(em) > 50
+            finally:
+                b.close()

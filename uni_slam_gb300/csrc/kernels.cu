@@ -1015,7 +1015,7 @@ __device__ __forceinline__ int flat_level(const uint32_t* pre, int L, uint32_t f
 // result does not depend on the scan order; a train set of fewer than two
 // features gives no match (the pool rule of match_features_cpu.cpp:80-82).
 // Result per query a in a2b: packed (level, index) of its match in curr, or -1.
-__global__ void __launch_bounds__(KB_THREADS)
+__global__ void __launch_bounds__(KB_THREADS, 8)
 k_bruteforce(const FrameDev* __restrict__ frames, const PairDev* __restrict__ pairs, const SegDev* __restrict__ psegs,
              int npairs, float ratio) {
     __shared__ uint32_t s_pref[MAX_SEGS + 1];
@@ -1024,16 +1024,19 @@ k_bruteforce(const FrameDev* __restrict__ frames, const PairDev* __restrict__ pa
     __shared__ int32_t s_id[KB_TILE];
     __shared__ uint32_t s_qpre[USLAM_MAX_LEVELS + 1], s_tpre[USLAM_MAX_LEVELS + 1];
     const uint32_t total = segment_prefix(npairs, s_pref, s_warp, [&](int s) {
-        const FrameDev& A = frames[pairs[psegs[s].frame].prev];
+        const PairDev& P = pairs[psegs[s].frame];
+        const FrameDev& A = frames[P.prev];
         uint32_t n = 0;
         for (int l = 0; l < A.levels; ++l) n += A.kept[l];
-        return (n + 2u * KB_THREADS - 1u) / (2u * KB_THREADS);
+        return (n + 2u * KB_THREADS - 1u) / (2u * KB_THREADS) * (uint32_t)max(P.bf_splits, 1);
     });
     const int tid = threadIdx.x;
     for (uint32_t g = blockIdx.x; g < total; g += gridDim.x) {
         const int sidx = find_segment(s_pref, npairs, g);
-        const uint32_t blk = g - s_pref[sidx];
         const PairDev& P = pairs[psegs[sidx].frame];
+        const uint32_t nsplit = (uint32_t)max(P.bf_splits, 1);
+        const uint32_t unit = g - s_pref[sidx];
+        const uint32_t blk = unit / nsplit, split = unit - blk * nsplit;
         const FrameDev& A = frames[P.prev];
         const FrameDev& B = frames[P.curr];
         const int LA = A.levels, LB = B.levels;
@@ -1066,11 +1069,15 @@ k_bruteforce(const FrameDev* __restrict__ frames, const PairDev* __restrict__ pa
             best[k] = second[k] = 0xffffffffu;  // keys: distance << 8 | tile slot
             bidx[k] = -1;
         }
-        for (uint32_t t0 = 0; t0 < nt; t0 += KB_TILE) {
+        // this unit's share of the train set: tiles [split T / S, (split + 1) T / S)
+        const uint32_t ntiles = (nt + KB_TILE - 1) / KB_TILE;
+        const uint32_t tb = split * ntiles / nsplit, te = (split + 1u) * ntiles / nsplit;
+        const uint32_t t_end = min(nt, te * (uint32_t)KB_TILE);
+        for (uint32_t t0 = tb * (uint32_t)KB_TILE; t0 < t_end; t0 += KB_TILE) {
             __syncthreads();
             for (int j = tid; j < KB_TILE; j += KB_THREADS) {
                 const uint32_t f = t0 + (uint32_t)j;
-                if (f < nt) {
+                if (f < t_end) {
                     const int l = flat_level(s_tpre, LB, f);
                     const uint32_t i = f - s_tpre[l];
                     const uint32_t* rec = B.feats[l] + (size_t)i * 12u;
@@ -1080,7 +1087,7 @@ k_bruteforce(const FrameDev* __restrict__ frames, const PairDev* __restrict__ pa
                 }
             }
             __syncthreads();
-            const int n = (int)min((uint32_t)KB_TILE, nt - t0);
+            const int n = (int)min((uint32_t)KB_TILE, t_end - t0);
             const uint32_t prev0 = best[0], prev1 = best[1];
             for (int j = 0; j < n; ++j) {
                 const uint4 d0 = s_d[2 * j], d1 = s_d[2 * j + 1];
@@ -1100,9 +1107,18 @@ k_bruteforce(const FrameDev* __restrict__ frames, const PairDev* __restrict__ pa
 #pragma unroll
         for (int k = 0; k < 2; ++k) {
             if (!qv[k]) continue;
-            const int32_t res =
-                (nt >= 2u && bidx[k] >= 0 && (float)(best[k] >> 8) < ratio * (float)(second[k] >> 8)) ? bidx[k] : -1;
-            P.a2b[(size_t)ql[k] * A.cap + qi[k]] = res;
+            const size_t q = (size_t)ql[k] * A.cap + qi[k];
+            if (nsplit == 1u) {
+                const int32_t res =
+                    (nt >= 2u && bidx[k] >= 0 && (float)(best[k] >> 8) < ratio * (float)(second[k] >> 8)) ? bidx[k]
+                                                                                                          : -1;
+                P.a2b[q] = res;
+            } else {
+                // partial record of this split; the emit kernel merges the splits
+                const size_t stride = (size_t)A.levels * A.cap;
+                *reinterpret_cast<uint4*>(P.bf_part + (split * stride + q) * 4u) =
+                    make_uint4(best[k], second[k], (uint32_t)bidx[k], 0u);
+            }
         }
         __syncthreads();  // s_qpre / s_tpre are rewritten by the next work unit
     }
@@ -1132,7 +1148,32 @@ k_mutual(const FrameDev* __restrict__ frames, const PairDev* __restrict__ pairs,
         int32_t m = -1;
         bool ok = false;
         if (i < n) {
-            m = P.a2b[(size_t)l * A.cap + i];
+            if (!MUTUAL && P.bf_splits > 1) {
+                // merge the brute-force splits: the two smallest distances of the
+                // union of the splits' (best, second) pairs; a tie on the best
+                // leaves second == best, which fails the ratio test
+                uint32_t bd = 0xffffffffu, sd = 0xffffffffu;
+                int32_t bi = -1;
+                const size_t stride = (size_t)A.levels * A.cap;
+                for (int sp = 0; sp < P.bf_splits; ++sp) {
+                    const uint4 e = *reinterpret_cast<const uint4*>(P.bf_part +
+                                                                    (sp * stride + (size_t)l * A.cap + i) * 4u);
+                    const uint32_t b = e.x >> 8, c = e.y >> 8;
+                    if (b < bd) {
+                        sd = min(bd, c);
+                        bd = b;
+                        bi = (int32_t)e.z;
+                    } else {
+                        sd = min(sd, b);
+                    }
+                }
+                uint32_t nt = 0;
+                for (int q = 0; q < B.levels; ++q) nt += B.kept[q];
+                m = (nt >= 2u && bi >= 0 && (float)bd < P.bf_ratio * (float)sd) ? bi : -1;
+                P.a2b[(size_t)l * A.cap + i] = m;
+            } else {
+                m = P.a2b[(size_t)l * A.cap + i];
+            }
             if (m >= 0) {
                 const int bl = USLAM_PACK_LEVEL(m), bi = USLAM_PACK_INDEX(m);
                 ok = !MUTUAL || P.b2a[(size_t)bl * B.cap + bi] == USLAM_PACK(l, i);

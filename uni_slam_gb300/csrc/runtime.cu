@@ -289,6 +289,24 @@ uslam_status create_batch(uslam_ctx* ctx, int n_frames, const int* widths, const
         b->pair_off[p] = take(&out_bytes, round_up(sizeof(uint32_t) * L, 16) + static_cast<size_t>(L) * capa * 16);
         dirs[p].first = take(&scratch, static_cast<size_t>(L) * capa * 4);
         dirs[p].second = take(&scratch, static_cast<size_t>(L) * capc * 4);
+        P.bf_splits = 1;
+        P.bf_ratio = ctx->ratio;
+    }
+    // Brute-force matcher: split each pair's train set so that the launch has
+    // about 8 CTAs (of 128 threads, 256 queries each) per SM.
+    std::vector<size_t> bf_off(n_pairs, 0);
+    if (ctx->matcher == 1 && n_pairs > 0) {
+        size_t units = 0;
+        for (int p = 0; p < n_pairs; ++p)
+            units += (static_cast<size_t>(L) * std::max(b->frames[pair_prev[p]].cap, 1) + 255) / 256;
+        const size_t target = static_cast<size_t>(std::max(ctx->num_sms, 1)) * 8;
+        const int splits = static_cast<int>(std::min<size_t>(16, std::max<size_t>(1, (target + units - 1) / units)));
+        if (splits > 1)
+            for (int p = 0; p < n_pairs; ++p) {
+                b->pairs[p].bf_splits = splits;
+                bf_off[p] = take(&scratch, static_cast<size_t>(splits) * L *
+                                               std::max(b->frames[pair_prev[p]].cap, 1) * 16);
+            }
     }
     const size_t err_off = take(&scratch, 256);
     const size_t frames_off = take(&scratch, sizeof(FrameDev) * n_frames);
@@ -360,6 +378,7 @@ uslam_status create_batch(uslam_ctx* ctx, int n_frames, const int* widths, const
         P.matches = reinterpret_cast<int32_t*>(out_base + b->pair_off[p] + round_up(sizeof(uint32_t) * L, 16));
         P.a2b = reinterpret_cast<int32_t*>(sc_base + dirs[p].first);
         P.b2a = reinterpret_cast<int32_t*>(sc_base + dirs[p].second);
+        P.bf_part = P.bf_splits > 1 ? reinterpret_cast<uint32_t*>(sc_base + bf_off[p]) : nullptr;
     }
     b->d_err = reinterpret_cast<uint32_t*>(sc_base + err_off);
     b->d_frames = reinterpret_cast<FrameDev*>(sc_base + frames_off);

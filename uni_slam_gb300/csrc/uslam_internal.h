@@ -53,6 +53,13 @@ struct PairDev {
     uint32_t* match_count;  // [levels] matches whose a lies in that level
     int max_matches_per_level;
     float max_dx, max_dy;   // 0.1f * W0, 0.1f * H0 of the frame size
+    // brute-force matcher split over the train set: bf_splits partial top-2
+    // records (best key, second key, best id, unused) per query, at
+    // bf_part[(split * levels * cap_prev + level * cap_prev + index) * 4];
+    // unused (nullptr, 1) when the train set is not split
+    uint32_t* bf_part;
+    int bf_splits;
+    float bf_ratio;
 };
 
 // K1 work item: one TW x TH tile of one level of one frame.
