@@ -181,11 +181,17 @@ def algorithmic_bytes(kept_per_frame: list[int], matches_per_pair: list[int], fr
     M = sum(kept_per_frame[:-1])  # each pair's reference set is the previous frame
     K = sum(matches_per_pair)
     total = frames * (wh + 4 * (P - wh)) + 48 * N + 32 * (N + M) + 8 * K
+    margin = 21  # blur-cache margin beyond each level edge (pattern radius + 2)
+    border = sum((w + margin + 1) * (h + margin + 1) - w * h for w, h in dims)
     return {
         "pyramid_per_frame": wh + 4 * (P - wh),
         "describe_total": 48 * N,
         "match_total": 32 * (N + M) + 8 * K,
         "total_per_step": total,
+        # per-kernel shares outside the path model, for the roofline of whichever kernel dominates:
+        "border_total": frames * 4 * border,   # blur-cache border cells written (f32)
+        "compact_total": frames * P + 12 * N,  # keypoint maps read (u8) + feature headers written
+        "mutual_total": 16 * K + 8 * M,        # match records written + direction tables read
     }
 
 
@@ -626,8 +632,11 @@ def run_ours(a):
     dom = max(prof, key=prof.get)
     kernel_bytes = {
         "k_detect": nbytes["pyramid_per_frame"] * n,
+        "k_blur_border": nbytes["border_total"],
+        "k_compact": nbytes["compact_total"],
         "k_describe": nbytes["describe_total"],
         "k_match": nbytes["match_total"],
+        "k_mutual": nbytes["mutual_total"],
     }
     traffic_units = {"k_detect": n, "k_blur_border": n, "k_compact": n, "k_describe": n, "k_match": n - 1}
     traffic_per_unit = measured_traffic()
