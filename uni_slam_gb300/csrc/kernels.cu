@@ -549,6 +549,8 @@ __device__ void compact_cells(const uint8_t* kp, int kpitch, int w, int h, uint3
     }
 }
 
+__device__ void xsort_level(const FrameDev& F, int l, uint32_t kept, uint32_t* s_hist, uint32_t* s_warp);
+
 // One CTA per (frame, level): keypoints in (y, x) order (or cell order with
 // per-cell caps) from the culled strength map, the level cap applied to the
 // first `cap`, then a counting sort of the kept features by x for the
@@ -578,15 +580,23 @@ k_compact(const FrameDev* __restrict__ frames, const SegDev* __restrict__ segs) 
         F.kept[l] = kept;
     }
 
-    // counting sort of kept features by x
-    for (int i = threadIdx.x; i <= w; i += KC_THREADS) s_hist[i] = 0u;
     __syncthreads();
-    for (uint32_t i = threadIdx.x; i < kept; i += KC_THREADS) {
+    xsort_level(F, l, kept, s_hist, s_warp);
+}
+
+// Counting sort of one level's kept features by x (dynamic shared memory
+// s_hist of w + 1 counters): colstart[x] = first slot of column x in xorder.
+__device__ void xsort_level(const FrameDev& F, int l, uint32_t kept, uint32_t* s_hist, uint32_t* s_warp) {
+    const int w = F.w[l];
+    const uint32_t* feats = F.feats[l];
+    for (int i = threadIdx.x; i <= w; i += blockDim.x) s_hist[i] = 0u;
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < kept; i += blockDim.x) {
         const int fx = (int)__uint_as_float(feats[(size_t)i * 12u]);
         atomicAdd(&s_hist[fx], 1u);
     }
     __syncthreads();
-    const int per = (w + KC_THREADS) / KC_THREADS;  // bins per thread over w + 1 bins
+    const int per = (w + (int)blockDim.x) / (int)blockDim.x;  // bins per thread over w + 1 bins
     const int b0 = threadIdx.x * per;
     uint32_t local = 0;
     for (int k = 0; k < per; ++k) {
@@ -607,10 +617,199 @@ k_compact(const FrameDev* __restrict__ frames, const SegDev* __restrict__ segs) 
     }
     __syncthreads();
     uint32_t* xorder = F.xorder[l];
-    for (uint32_t i = threadIdx.x; i < kept; i += KC_THREADS) {
+    for (uint32_t i = threadIdx.x; i < kept; i += blockDim.x) {
         const int fx = (int)__uint_as_float(feats[(size_t)i * 12u]);
         const uint32_t slot = atomicAdd(&s_hist[fx], 1u);
         xorder[slot] = i;
+    }
+}
+
+// Per (frame, level): the x counting sort after the banded compaction.
+__global__ void __launch_bounds__(KC_THREADS)
+k_xsort(const FrameDev* __restrict__ frames, const SegDev* __restrict__ segs) {
+    extern __shared__ uint32_t s_hist[];  // [w + 1]
+    __shared__ uint32_t s_warp[33];
+    const SegDev sg = segs[blockIdx.x];
+    const FrameDev& F = frames[sg.frame];
+    xsort_level(F, sg.level, F.kept[sg.level], s_hist, s_warp);
+}
+
+// --------------------------------------------------- banded compaction ----
+// The same compaction as k_compact, spread over one CTA per 32-row band of
+// every level (a band is also one row of 32x32 cells):
+//   k_band_count  per band: raw keypoints and keypoints kept by the cell caps
+//   k_band_write  per band: prefix of the earlier bands' kept counts, then the
+//                 ordered write of the band's headers below the level cap;
+//                 band 0 also writes the level's raw / kept totals
+//   k_xsort       per level: counting sort of the kept features by x
+// Positions equal k_compact's: the list order ((y, x), or cell order) is the
+// band order followed by the order inside each band.
+constexpr int KBAND_THREADS = 256;
+constexpr int KBAND_WARPS = KBAND_THREADS / 32;
+
+// This warp's share of a band and its counts.  Rows mode: 4 rows per warp.
+// Cells mode: a contiguous run of the band's cells per warp.
+__device__ __forceinline__ void band_warp_counts(const FrameDev& F, int l, int band, uint32_t* raw, uint32_t* kept) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int w = F.w[l], h = F.h[l], kpitch = F.kp_pitch[l];
+    const uint8_t* kp = F.kpmap[l];
+    uint32_t r = 0, k = 0;
+    if (F.cell_cap <= 0) {
+        const int y0 = band * 32 + warp * (32 / KBAND_WARPS);
+        for (int y = y0; y < min(h, y0 + 32 / KBAND_WARPS); ++y) {
+            const uint32_t* row = reinterpret_cast<const uint32_t*>(kp + (size_t)y * kpitch);
+            for (int x4 = lane; x4 * 4 < w; x4 += 32) r += nonzero_bytes(row[x4]);
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) r += __shfl_xor_sync(0xffffffffu, r, o);
+        k = r;
+    } else {
+        const uint32_t ccap = (uint32_t)F.cell_cap;
+        const int ncx = (w + 31) / 32, per = (ncx + KBAND_WARPS - 1) / KBAND_WARPS;
+        for (int cx = warp * per; cx < min(ncx, (warp + 1) * per); ++cx) {
+            uint32_t v[8];
+            load_cell_row(kp, kpitch, w, h, cx * 32, band * 32 + lane, v);
+            uint32_t n = 0;
+#pragma unroll
+            for (int q = 0; q < 8; ++q) n += (uint32_t)nonzero_bytes(v[q]);
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) n += __shfl_xor_sync(0xffffffffu, n, o);
+            r += n;
+            k += n < ccap ? n : ccap;
+        }
+    }
+    *raw = r;
+    *kept = k;
+}
+
+__global__ void __launch_bounds__(KBAND_THREADS)
+k_band_count(const FrameDev* __restrict__ frames, const BandItem* __restrict__ items) {
+    __shared__ uint32_t s_raw[KBAND_WARPS], s_kept[KBAND_WARPS];
+    const BandItem it = items[blockIdx.x];
+    const FrameDev& F = frames[it.frame];
+    uint32_t r, k;
+    band_warp_counts(F, it.level, it.band, &r, &k);
+    if ((threadIdx.x & 31) == 0) {
+        s_raw[threadIdx.x >> 5] = r;
+        s_kept[threadIdx.x >> 5] = k;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t R = 0, K = 0;
+        for (int q = 0; q < KBAND_WARPS; ++q) {
+            R += s_raw[q];
+            K += s_kept[q];
+        }
+        F.bands[it.level][2 * it.band] = R;
+        F.bands[it.level][2 * it.band + 1] = K;
+    }
+}
+
+__global__ void __launch_bounds__(KBAND_THREADS)
+k_band_write(const FrameDev* __restrict__ frames, const BandItem* __restrict__ items) {
+    __shared__ uint32_t s_red[2][KBAND_WARPS];
+    __shared__ uint32_t s_wbase[KBAND_WARPS];
+    const BandItem it = items[blockIdx.x];
+    const FrameDev& F = frames[it.frame];
+    const int l = it.level, band = it.band;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int w = F.w[l], h = F.h[l], kpitch = F.kp_pitch[l];
+    const uint8_t* kp = F.kpmap[l];
+    const uint32_t cap = (uint32_t)F.cap;
+    const int nb = (h + 31) / 32;
+    const uint32_t* bc = F.bands[l];
+    // prefix of the earlier bands' kept counts (band 0: also the level totals)
+    uint32_t pk = 0, tr = 0, tk = 0;
+    for (int q = threadIdx.x; q < nb; q += KBAND_THREADS) {
+        const uint32_t kq = bc[2 * q + 1];
+        if (q < band) pk += kq;
+        tr += bc[2 * q];
+        tk += kq;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        pk += __shfl_xor_sync(0xffffffffu, pk, o);
+        tr += __shfl_xor_sync(0xffffffffu, tr, o);
+        tk += __shfl_xor_sync(0xffffffffu, tk, o);
+    }
+    if (lane == 0) {
+        s_red[0][warp] = pk;
+        s_red[1][warp] = tr;
+    }
+    __shared__ uint32_t s_tk[KBAND_WARPS];
+    if (lane == 0) s_tk[warp] = tk;
+    uint32_t r, k;
+    band_warp_counts(F, l, band, &r, &k);
+    if (lane == 0) s_wbase[warp] = k;
+    __syncthreads();
+    uint32_t prefix = 0;
+    for (int q = 0; q < KBAND_WARPS; ++q) prefix += s_red[0][q];
+    if (band == 0 && threadIdx.x == 0) {
+        uint32_t R = 0, K = 0;
+        for (int q = 0; q < KBAND_WARPS; ++q) {
+            R += s_red[1][q];
+            K += s_tk[q];
+        }
+        F.raw[l] = R;
+        F.kept[l] = K < cap ? K : cap;
+    }
+    uint32_t running = prefix;
+    for (int q = 0; q < warp; ++q) running += s_wbase[q];
+    if (prefix >= cap) return;
+    uint32_t* feats = F.feats[l];
+    if (F.cell_cap <= 0) {
+        const int y0 = band * 32 + warp * (32 / KBAND_WARPS);
+        for (int y = y0; y < min(h, y0 + 32 / KBAND_WARPS); ++y) {
+            const uint32_t* row = reinterpret_cast<const uint32_t*>(kp + (size_t)y * kpitch);
+            for (int base = 0; base < w; base += 128) {
+                const int x4 = base / 4 + lane;
+                const uint32_t v = (x4 * 4 < w) ? row[x4] : 0u;
+                const uint32_t n = (uint32_t)nonzero_bytes(v);
+                uint32_t incl = n;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+                    if (lane >= o) incl += t;
+                }
+                uint32_t pos = running + incl - n;
+                for (int b = 0; b < 4; ++b) {
+                    const uint32_t sv = (v >> (8 * b)) & 0xffu;
+                    if (sv == 0u) continue;
+                    if (pos < cap) write_header(feats, pos, x4 * 4 + b, y, sv);
+                    ++pos;
+                }
+                running += __shfl_sync(0xffffffffu, incl, 31);
+            }
+        }
+    } else {
+        const uint32_t ccap = (uint32_t)F.cell_cap;
+        const int ncx = (w + 31) / 32, per = (ncx + KBAND_WARPS - 1) / KBAND_WARPS;
+        const int y = band * 32 + lane;
+        for (int cx = warp * per; cx < min(ncx, (warp + 1) * per); ++cx) {
+            uint32_t v[8];
+            load_cell_row(kp, kpitch, w, h, cx * 32, y, v);
+            uint32_t n = 0;
+#pragma unroll
+            for (int q = 0; q < 8; ++q) n += (uint32_t)nonzero_bytes(v[q]);
+            uint32_t incl = n;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o) incl += t;
+            }
+            const uint32_t tot = __shfl_sync(0xffffffffu, incl, 31);
+            uint32_t rank = incl - n;
+            for (int q = 0; q < 8 && rank < ccap; ++q) {
+                if (v[q] == 0u) continue;
+                for (int b = 0; b < 4; ++b) {
+                    const uint32_t sv = (v[q] >> (8 * b)) & 0xffu;
+                    if (sv == 0u) continue;
+                    if (rank < ccap && running + rank < cap) write_header(feats, running + rank, cx * 32 + 4 * q + b, y, sv);
+                    ++rank;
+                }
+            }
+            running += tot < ccap ? tot : ccap;
+        }
     }
 }
 
@@ -1245,6 +1444,18 @@ cudaError_t launch_compact(const FrameDev* frames, const SegDev* segs, int nseg,
     return cudaGetLastError();
 }
 
+cudaError_t launch_compact_banded(const FrameDev* frames, const BandItem* bands, int nbands, const SegDev* segs,
+                                  int nseg, int max_w, cudaStream_t st) {
+    if (nseg <= 0) return cudaSuccess;
+    k_band_count<<<nbands, KBAND_THREADS, 0, st>>>(frames, bands);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    k_band_write<<<nbands, KBAND_THREADS, 0, st>>>(frames, bands);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    k_xsort<<<nseg, KC_THREADS, (size_t)(max_w + 1) * sizeof(uint32_t), st>>>(frames, segs);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_blur_border(const FrameDev* frames, const SegDev* segs, int nseg, int grid, cudaStream_t st) {
     if (nseg <= 0) return cudaSuccess;
     k_blur_border<<<grid, 256, 0, st>>>(frames, segs, nseg);
@@ -1289,7 +1500,9 @@ cudaError_t launch_bruteforce(const FrameDev* frames, const PairDev* pairs, cons
 cudaError_t set_compact_smem(int max_w) {
     const size_t smem = (size_t)(max_w + 1) * sizeof(uint32_t);
     if (smem <= 48 * 1024) return cudaSuccess;
-    return cudaFuncSetAttribute(k_compact, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = cudaFuncSetAttribute(k_compact, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    return cudaFuncSetAttribute(k_xsort, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
 }
 
 }  // namespace uslam

@@ -31,7 +31,8 @@ namespace {
 
 // Launch tables of one program (a subset of the batch's frames and pairs).
 struct Program {
-    int ntiles = 0, nfsegs = 0, nmsegs = 0, nusegs = 0, npsegs = 0;
+    int ntiles = 0, nfsegs = 0, nmsegs = 0, nusegs = 0, npsegs = 0, nbands = 0;
+    BandItem* bands = nullptr;  // compaction work items: one per 32-row band of every (frame, level)
     int tile_begin[kNumTileShapes + 1] = {0};  // tiles grouped by shape
     TileItem* tiles = nullptr;
     SegDev* fsegs = nullptr;
@@ -77,10 +78,20 @@ uslam_status build_program(uslam_batch* b, const std::vector<int>& fr, const std
     ShapedTiles st;
     std::vector<SegDev> fsegs, usegs, psegs;
     std::vector<MatchSegDev> msegs;
+    std::vector<BandItem> bands;
     for (int f : fr) {
         const FrameDev& F = b->frames[f];
         append_tiles(&st.by_shape[b->ctx->shape_for(F.W0, F.H0)], f, F, b->ctx->shape_for(F.W0, F.H0));
-        for (int l = 0; l < F.levels; ++l) fsegs.push_back(SegDev{f, l});
+        for (int l = 0; l < F.levels; ++l) {
+            fsegs.push_back(SegDev{f, l});
+            for (int q = 0; q < (F.h[l] + 31) / 32; ++q) {
+                BandItem bi{};
+                bi.frame = static_cast<uint16_t>(f);
+                bi.level = static_cast<uint8_t>(l);
+                bi.band = static_cast<uint16_t>(q);
+                bands.push_back(bi);
+            }
+        }
     }
     st.finish();
     const std::vector<TileItem>& tiles = st.flat;
@@ -100,17 +111,21 @@ uslam_status build_program(uslam_batch* b, const std::vector<int>& fr, const std
     P->nmsegs = static_cast<int>(msegs.size());
     P->nusegs = static_cast<int>(usegs.size());
     P->npsegs = static_cast<int>(psegs.size());
+    P->nbands = static_cast<int>(bands.size());
     const size_t t_bytes = round_up(tiles.size() * sizeof(TileItem), 256);
     const size_t f_bytes = round_up(fsegs.size() * sizeof(SegDev), 256);
     const size_t m_bytes = round_up(msegs.size() * sizeof(MatchSegDev), 256);
     const size_t u_bytes = round_up(usegs.size() * sizeof(SegDev), 256);
     const size_t p_bytes = round_up(psegs.size() * sizeof(SegDev), 256);
-    P->host.assign(t_bytes + f_bytes + m_bytes + u_bytes + p_bytes, 0);
+    const size_t b_bytes = round_up(bands.size() * sizeof(BandItem), 256);
+    P->host.assign(t_bytes + f_bytes + m_bytes + u_bytes + p_bytes + b_bytes, 0);
     std::memcpy(P->host.data(), tiles.data(), tiles.size() * sizeof(TileItem));
     std::memcpy(P->host.data() + t_bytes, fsegs.data(), fsegs.size() * sizeof(SegDev));
     std::memcpy(P->host.data() + t_bytes + f_bytes, msegs.data(), msegs.size() * sizeof(MatchSegDev));
     std::memcpy(P->host.data() + t_bytes + f_bytes + m_bytes, usegs.data(), usegs.size() * sizeof(SegDev));
     std::memcpy(P->host.data() + t_bytes + f_bytes + m_bytes + u_bytes, psegs.data(), psegs.size() * sizeof(SegDev));
+    std::memcpy(P->host.data() + t_bytes + f_bytes + m_bytes + u_bytes + p_bytes, bands.data(),
+                bands.size() * sizeof(BandItem));
     return USLAM_OK;
 }
 
@@ -130,7 +145,9 @@ cudaError_t enqueue_program(uslam_batch* b, const Program& P) {
         if ((e = cudaStreamWaitEvent(b->aux_stream, b->ev_fork, 0)) != cudaSuccess) return e;
         if ((e = launch_blur_border(b->d_frames, P.fsegs, P.nfsegs, grid, b->aux_stream)) != cudaSuccess) return e;
         if ((e = cudaEventRecord(b->ev_join, b->aux_stream)) != cudaSuccess) return e;
-        if ((e = launch_compact(b->d_frames, P.fsegs, P.nfsegs, b->max_w, b->stream)) != cudaSuccess) return e;
+        if ((e = launch_compact_banded(b->d_frames, P.bands, P.nbands, P.fsegs, P.nfsegs, b->max_w, b->stream)) !=
+            cudaSuccess)
+            return e;
         if ((e = cudaStreamWaitEvent(b->stream, b->ev_join, 0)) != cudaSuccess) return e;
         if ((e = launch_describe(b->d_frames, P.fsegs, P.nfsegs, c->d_pattern, grid, b->stream)) != cudaSuccess)
             return e;
@@ -214,7 +231,7 @@ uslam_status create_batch(uslam_ctx* ctx, int n_frames, const int* widths, const
     };
     struct FrameLayout {
         size_t lvl[USLAM_MAX_LEVELS], blur[USLAM_MAX_LEVELS], kpmap[USLAM_MAX_LEVELS], feats[USLAM_MAX_LEVELS],
-            xorder[USLAM_MAX_LEVELS], colstart[USLAM_MAX_LEVELS], counts;
+            xorder[USLAM_MAX_LEVELS], colstart[USLAM_MAX_LEVELS], bands[USLAM_MAX_LEVELS], counts;
     };
     std::vector<FrameLayout> fl(n_frames);
     for (int f = 0; f < n_frames; ++f) {
@@ -261,6 +278,7 @@ uslam_status create_batch(uslam_ctx* ctx, int n_frames, const int* widths, const
             Ly.kpmap[l] = take(&scratch, static_cast<size_t>(F.h[l]) * F.kp_pitch[l]);
             Ly.xorder[l] = take(&scratch, capa * 4);
             Ly.colstart[l] = take(&scratch, (static_cast<size_t>(F.w[l]) + 1) * 4);
+            Ly.bands[l] = take(&scratch, static_cast<size_t>((F.h[l] + 31) / 32) * 8);
         }
         b->max_w = std::max(b->max_w, F.w[0]);
     }
@@ -369,6 +387,7 @@ uslam_status create_batch(uslam_ctx* ctx, int n_frames, const int* widths, const
             F.feats[l] = reinterpret_cast<uint32_t*>(out_base + Ly.feats[l]);
             F.xorder[l] = reinterpret_cast<uint32_t*>(sc_base + Ly.xorder[l]);
             F.colstart[l] = reinterpret_cast<uint32_t*>(sc_base + Ly.colstart[l]);
+            F.bands[l] = reinterpret_cast<uint32_t*>(sc_base + Ly.bands[l]);
             F.mask[l] = masks[l];
         }
     }
@@ -440,6 +459,8 @@ uslam_status create_batch(uslam_ctx* ctx, int n_frames, const int* widths, const
         const size_t m_bytes = round_up(P->nmsegs * sizeof(MatchSegDev), 256);
         const size_t u_bytes = round_up(P->nusegs * sizeof(SegDev), 256);
         P->psegs = reinterpret_cast<SegDev*>(base + t_bytes + f_bytes + m_bytes + u_bytes);
+        const size_t p_bytes = round_up(P->npsegs * sizeof(SegDev), 256);
+        P->bands = reinterpret_cast<BandItem*>(base + t_bytes + f_bytes + m_bytes + u_bytes + p_bytes);
         P->tiles = reinterpret_cast<TileItem*>(base);
         P->fsegs = reinterpret_cast<SegDev*>(base + t_bytes);
         P->msegs = reinterpret_cast<MatchSegDev*>(base + t_bytes + f_bytes);
@@ -758,7 +779,8 @@ uslam_status uslam_batch_profile(uslam_batch* b, int iters, float* kernel_ms) {
         mark();
         if (e == cudaSuccess) e = launch_blur_border(b->d_frames, P.fsegs, P.nfsegs, grid, b->stream);
         mark();
-        if (e == cudaSuccess) e = launch_compact(b->d_frames, P.fsegs, P.nfsegs, b->max_w, b->stream);
+        if (e == cudaSuccess)
+            e = launch_compact_banded(b->d_frames, P.bands, P.nbands, P.fsegs, P.nfsegs, b->max_w, b->stream);
         mark();
         if (e == cudaSuccess) e = launch_describe(b->d_frames, P.fsegs, P.nfsegs, c->d_pattern, grid, b->stream);
         mark();

@@ -13,6 +13,7 @@
 //                                          f32, 2^32); rows likewise.  M = pattern
 //                                          radius + 2, bl_pitch_l = w_l + M + 1.
 //   kpmap[l] u8   [h_l][kp_pitch_l]        culled FAST strength (0 = no keypoint)
+//   bands[l] u32  [ceil(h_l / 32)][2]      raw and kept keypoint counts per 32-row band
 //   feats[l] Feature[cap]                  gpumodels::Feature records, (y, x) order
 //   xorder[l] u32 [cap]                    feature indices sorted by x (matching)
 //   colstart[l] u32 [w_l + 1]              first xorder slot of each column
@@ -36,6 +37,7 @@ struct FrameDev {
     float* lvl[USLAM_MAX_LEVELS];
     float* blur[USLAM_MAX_LEVELS];
     uint8_t* kpmap[USLAM_MAX_LEVELS];
+    uint32_t* bands[USLAM_MAX_LEVELS];       // per 32-row band: raw and kept keypoint counts
     const uint32_t* mask[USLAM_MAX_LEVELS];  // combined cull coverage bitmap
     uint32_t* feats[USLAM_MAX_LEVELS];       // 12 u32 (48 B) per feature
     uint32_t* xorder[USLAM_MAX_LEVELS];
@@ -74,6 +76,15 @@ struct TileItem {
 struct SegDev {
     int frame;
     int level;
+};
+
+// Compaction work item: one 32-row band (a row of 32x32 cells) of one level.
+struct BandItem {
+    uint16_t frame;
+    uint8_t level;
+    uint8_t pad;
+    uint16_t band;
+    uint16_t pad2;
 };
 
 #define USLAM_ERR_SMEM_RANGE 1u
