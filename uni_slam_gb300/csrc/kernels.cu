@@ -939,12 +939,18 @@ k_blur_border(const FrameDev* __restrict__ frames, const SegDev* __restrict__ se
 __global__ void __launch_bounds__(KD_THREADS)
 k_describe(const FrameDev* __restrict__ frames, const SegDev* __restrict__ segs, int nseg,
            const int32_t* __restrict__ pattern) {
-    __shared__ int4 s_pat[256];
+    // the test pattern as f32 (each coordinate converted once per CTA, exactly)
+    __shared__ float4 s_pat[256];
     __shared__ uint32_t s_pref[MAX_SEGS + 1];
     __shared__ uint32_t s_warp[33];
     __shared__ float s_lut[256];
+    // the r = 3 disc in (dy outer, dx inner) order as compile-time constants, so
+    // the unrolled moment sum multiplies by immediates (same f32 operations)
+    constexpr int8_t kdx[29] = {0, -2, -1, 0, 1, 2, -2, -1, 0, 1, 2, -3, -2, -1, 0, 1, 2, 3, -2, -1, 0, 1, 2, -2, -1, 0, 1, 2, 0};
+    constexpr int8_t kdy[29] = {-3, -2, -2, -2, -2, -2, -1, -1, -1, -1, -1, 0, 0, 0, 0, 0, 0, 0, 1, 1, 1, 1, 1, 2, 2, 2, 2, 2, 3};
     for (int i = threadIdx.x; i < 256; i += KD_THREADS) {
-        s_pat[i] = make_int4(pattern[4 * i], pattern[4 * i + 1], pattern[4 * i + 2], pattern[4 * i + 3]);
+        s_pat[i] = make_float4((float)pattern[4 * i], (float)pattern[4 * i + 1], (float)pattern[4 * i + 2],
+                               (float)pattern[4 * i + 3]);
         s_lut[i] = (float)i / 255.0f;
     }
     const uint32_t total = segment_prefix(nseg, s_pref, s_warp, [&](int s) {
@@ -975,8 +981,8 @@ k_describe(const FrameDev* __restrict__ frames, const SegDev* __restrict__ segs,
 #pragma unroll
         for (int k = 0; k < 29; ++k) {
             const float v = __shfl_sync(0xffffffffu, p, k);
-            m10 = m10 + (float)c_disc_x[k] * v;
-            m01 = m01 + (float)c_disc_y[k] * v;
+            m10 = m10 + (float)kdx[k] * v;
+            m01 = m01 + (float)kdy[k] * v;
         }
         const float theta = uslam_atan2f(m01, m10);
         float s, c;
@@ -990,8 +996,8 @@ k_describe(const FrameDev* __restrict__ frames, const SegDev* __restrict__ segs,
         float ga[8], gb[8];
 #pragma unroll
         for (int k = 0; k < 8; ++k) {
-            const int4 t = s_pat[lane + 32 * k];
-            const float fax = (float)t.x, fay = (float)t.y, fbx = (float)t.z, fby = (float)t.w;
+            const float4 t = s_pat[lane + 32 * k];
+            const float fax = t.x, fay = t.y, fbx = t.z, fby = t.w;
             int xa = x + (int)rintf(fax * c - fay * s);
             int ya = y + (int)rintf(fax * s + fay * c);
             int xb = x + (int)rintf(fbx * c - fby * s);
