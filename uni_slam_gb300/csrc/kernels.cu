@@ -30,9 +30,15 @@ constexpr int K1_THREADS = 256;
 // cfg detection profile threshold: 20 grey levels on the u8/255 scale.
 constexpr float kCfgThreshold = 20.0f / 255.0f;
 
-// Bresenham circle of radius 3 (resources/detect_corners.wgsl:31-32).
-__constant__ int8_t c_circle_x[16] = {0, 1, 2, 3, 3, 3, 2, 1, 0, -1, -2, -3, -3, -3, -2, -1};
-__constant__ int8_t c_circle_y[16] = {-3, -3, -2, -1, 0, 1, 2, 3, 3, 3, 2, 1, 0, -1, -2, -3};
+// Bresenham circle of radius 3 (resources/detect_corners.wgsl:31-32) as
+// compile-time constants: in the unrolled loops the shared-memory offsets fold
+// into immediates.
+__device__ __forceinline__ constexpr int circle_x(int i) {
+    return i == 0 ? 0 : i == 1 ? 1 : i == 2 ? 2 : i <= 5 ? 3 : i == 6 ? 2 : i == 7 ? 1 : i == 8 ? 0
+         : i == 9 ? -1 : i == 10 ? -2 : i <= 13 ? -3 : i == 14 ? -2 : -1;
+}
+// A quarter turn maps point i to point i + 4 ((x, y) -> (-y, x)), so y_i = -x_(i+4).
+__device__ __forceinline__ constexpr int circle_y(int i) { return -circle_x((i + 4) & 15); }
 
 // Orientation disc r = 3 in (dy outer, dx inner) order (generate_features.wgsl:87-97).
 __constant__ int8_t c_disc_x[32];
@@ -89,7 +95,7 @@ __device__ __forceinline__ uint32_t fast_response(const float (*sm)[SW], int r, 
     uint32_t m = 0;
 #pragma unroll
     for (int i = 0; i < 16; ++i) {
-        const float p = sm[r + c_circle_y[i]][c + c_circle_x[i]];
+        const float p = sm[r + circle_y(i)][c + circle_x(i)];
         m |= (fabsf(center - p) > 0.15f ? 1u : 0u) << i;
     }
     // run >= 9 test: AND of the mask shifted by 0..8
@@ -129,7 +135,7 @@ __device__ __forceinline__ float cfg_corner(const float (*sm)[SW], int r, int c,
     uint32_t mb = 0, md = 0;
 #pragma unroll
     for (int i = 0; i < 16; ++i) {
-        const float p = sm[r + c_circle_y[i]][c + c_circle_x[i]];
+        const float p = sm[r + circle_y(i)][c + circle_x(i)];
         d[i] = p - center;
         mb |= (d[i] > kCfgThreshold ? 1u : 0u) << i;
         md |= ((center - p) > kCfgThreshold ? 1u : 0u) << i;
@@ -144,7 +150,7 @@ __device__ __forceinline__ float cfg_corner(const float (*sm)[SW], int r, int c,
 #pragma unroll
     for (int i = 0; i < 16; ++i) {
         if (!((m >> i) & 1u)) continue;
-        const float dv = bright ? d[i] : (sm[r][c] - sm[r + c_circle_y[i]][c + c_circle_x[i]]);
+        const float dv = bright ? d[i] : (sm[r][c] - sm[r + circle_y(i)][c + circle_x(i)]);
         score = score + (dv - kCfgThreshold);
     }
     *arc = bright ? rb : rd;
