@@ -633,12 +633,12 @@ def run_ours(a):
     kernel_bytes = {
         "k_detect": nbytes["pyramid_per_frame"] * n,
         "k_blur_border": nbytes["border_total"],
-        "k_compact": nbytes["compact_total"],
+        "compaction": nbytes["compact_total"],
         "k_describe": nbytes["describe_total"],
         "k_match": nbytes["match_total"],
         "k_mutual": nbytes["mutual_total"],
     }
-    traffic_units = {"k_detect": n, "k_blur_border": n, "k_compact": n, "k_describe": n, "k_match": n - 1}
+    traffic_units = {"k_detect": n, "k_blur_border": n, "compaction": n, "k_describe": n, "k_match": n - 1}
     traffic_per_unit = measured_traffic()
     dom_traffic = traffic_per_unit[dom] * traffic_units[dom] if dom in traffic_per_unit else None
     peaks = json.load(open(os.path.join(REPO, "MEASURED_PEAKS.json"))) if os.path.exists(

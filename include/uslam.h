@@ -174,10 +174,13 @@ uslam_status uslam_blur_margin(const uslam_ctx* ctx, int* margin);
 /* Issue later upload/run/download calls on a caller's cudaStream_t (NULL:
  * the batch's own stream), so callers can record their own events around them. */
 uslam_status uslam_batch_set_stream(uslam_batch* b, void* cuda_stream);
-/* Per-kernel timing: launch the batch's six kernels `iters` times without
- * the graph, with CUDA events between them on the batch stream, and return
- * the mean milliseconds per launch of detect, compact, describe, match and
- * mutual in kernel_ms[0..4].  Synchronous. */
+/* Per-stage timing: launch the batch's stages `iters` times without the
+ * graph and without the fork, with CUDA events between them on the batch
+ * stream, and return the mean milliseconds per launch in kernel_ms[0..5]:
+ * detect (k_detect, one launch per tile shape), blur-cache border
+ * (k_blur_border), compaction (k_band_count + k_band_write + k_xsort),
+ * describe (k_describe), match (k_match, or k_bruteforce with matcher 1) and
+ * mutual check / emit (k_mutual).  Synchronous. */
 uslam_status uslam_batch_profile(uslam_batch* b, int iters, float* kernel_ms);
 /* Bytes moved by upload and download per call (for end-to-end accounting). */
 uslam_status uslam_batch_io_bytes(uslam_batch* b, size_t* h2d, size_t* d2h);

@@ -3,7 +3,8 @@
 //   k_detect   (K1) pyramid level tile + FAST response + cull + blur cache
 //                   (or, in the cfg profile, FAST 9-of-16 at 20/255 + 3x3 NMS)
 //   k_blur_border   blur cache beyond the level edges (BRIEF points outside)
-//   k_compact       per (frame, level): ordered keypoint compaction, cap, x-sort
+//   k_band_count, k_band_write, k_xsort
+//                   ordered keypoint compaction over 32-row bands, cap, x-sort
 //   k_describe (K2) orientation + 256-bit rotated BRIEF, one warp per keypoint
 //   k_match    (K3) windowed top-2 Hamming search, 32 x-adjacent queries per warp
 //   k_mutual        mutual cross-check and ordered match output
@@ -402,71 +403,11 @@ __device__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* s_warp, uint32_t*
     return res;
 }
 
-// Exclusive scan of the 32 per-warp values s_base[0..31] in place (warp 0);
-// the sum goes to *sum_out (shared).
-__device__ __forceinline__ void scan_warp_bases(uint32_t* s_base, uint32_t* sum_out) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    __syncthreads();
-    if (warp == 0) {
-        const uint32_t v = s_base[lane];
-        uint32_t incl = v;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
-            if (lane >= o) incl += t;
-        }
-        s_base[lane] = incl - v;
-        if (lane == 31) *sum_out = incl;
-    }
-    __syncthreads();
-}
-
 __device__ __forceinline__ void write_header(uint32_t* feats, uint32_t pos, int x, int y, uint32_t s) {
     uint32_t* rec = feats + (size_t)pos * 12u;
     rec[0] = __float_as_uint((float)x);
     rec[1] = __float_as_uint((float)y);
     rec[2] = s;
-}
-
-// (y, x) order: warp k owns a band of rows; count, scan, ordered write.
-__device__ void compact_rows(const uint8_t* kp, int kpitch, int w, int h, uint32_t cap, uint32_t* feats,
-                             uint32_t* s_base, uint32_t* s_warp, uint32_t* total_out) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int rows_per = (h + 31) / 32;
-    const int r0 = warp * rows_per, r1 = min(h, r0 + rows_per);
-    uint32_t cnt = 0;
-    for (int y = r0; y < r1; ++y) {
-        const uint32_t* row = reinterpret_cast<const uint32_t*>(kp + (size_t)y * kpitch);
-        for (int x4 = lane; x4 * 4 < w; x4 += 32) cnt += nonzero_bytes(row[x4]);
-    }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
-    if (lane == 0) s_base[warp] = cnt;
-    scan_warp_bases(s_base, &s_warp[32]);
-    *total_out = s_warp[32];
-    uint32_t running = s_base[warp];
-    for (int y = r0; y < r1; ++y) {
-        const uint32_t* row = reinterpret_cast<const uint32_t*>(kp + (size_t)y * kpitch);
-        for (int base = 0; base < w; base += 128) {
-            const int x4 = base / 4 + lane;
-            const uint32_t v = (x4 * 4 < w) ? row[x4] : 0u;
-            const uint32_t n = (uint32_t)nonzero_bytes(v);
-            uint32_t incl = n;
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
-                if (lane >= o) incl += t;
-            }
-            uint32_t pos = running + incl - n;
-            for (int b = 0; b < 4; ++b) {
-                const uint32_t sv = (v >> (8 * b)) & 0xffu;
-                if (sv == 0u) continue;
-                if (pos < cap) write_header(feats, pos, x4 * 4 + b, y, sv);
-                ++pos;
-            }
-            running += __shfl_sync(0xffffffffu, incl, 31);
-        }
-    }
 }
 
 // One lane's 32-pixel row segment of a 32x32 cell (bytes at x >= w zeroed).
@@ -494,101 +435,7 @@ __device__ __forceinline__ void load_cell_row(const uint8_t* kp, int kpitch, int
     }
 }
 
-// Cell order: warp k owns a run of 32x32 cells (row-major); lane r holds
-// row r of the current cell.  The first ccap keypoints of each cell in
-// (y, x) order are kept; the level cap applies to the cell-ordered list.
-__device__ void compact_cells(const uint8_t* kp, int kpitch, int w, int h, uint32_t cap, uint32_t ccap,
-                              uint32_t* feats, uint32_t* s_base, uint32_t* s_warp, uint32_t* total_out,
-                              uint32_t* kept_out) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int ncx = (w + 31) / 32, ncy = (h + 31) / 32, ncell = ncx * ncy;
-    const int cells_per = (ncell + 31) / 32;
-    const int c0 = warp * cells_per, c1 = min(ncell, c0 + cells_per);
-    uint32_t raw = 0, cnt = 0;
-    for (int ci = c0; ci < c1; ++ci) {
-        const int cy = ci / ncx, cx = ci - cy * ncx;
-        uint32_t v[8];
-        load_cell_row(kp, kpitch, w, h, cx * 32, cy * 32 + lane, v);
-        uint32_t n = 0;
-#pragma unroll
-        for (int k = 0; k < 8; ++k) n += (uint32_t)nonzero_bytes(v[k]);
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) n += __shfl_xor_sync(0xffffffffu, n, o);
-        raw += n;
-        cnt += n < ccap ? n : ccap;
-    }
-    if (lane == 0) s_base[warp] = raw;
-    scan_warp_bases(s_base, &s_warp[32]);
-    *total_out = s_warp[32];
-    __syncthreads();
-    if (lane == 0) s_base[warp] = cnt;
-    scan_warp_bases(s_base, &s_warp[32]);
-    const uint32_t kept_cells = s_warp[32];
-    *kept_out = kept_cells < cap ? kept_cells : cap;
-    uint32_t running = s_base[warp];
-    for (int ci = c0; ci < c1; ++ci) {
-        const int cy = ci / ncx, cx = ci - cy * ncx;
-        const int y = cy * 32 + lane;
-        uint32_t v[8];
-        load_cell_row(kp, kpitch, w, h, cx * 32, y, v);
-        uint32_t n = 0;
-#pragma unroll
-        for (int k = 0; k < 8; ++k) n += (uint32_t)nonzero_bytes(v[k]);
-        uint32_t incl = n;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
-            if (lane >= o) incl += t;
-        }
-        const uint32_t tot = __shfl_sync(0xffffffffu, incl, 31);
-        uint32_t rank = incl - n;
-        for (int k = 0; k < 8 && rank < ccap; ++k) {
-            if (v[k] == 0u) continue;
-            for (int b = 0; b < 4; ++b) {
-                const uint32_t sv = (v[k] >> (8 * b)) & 0xffu;
-                if (sv == 0u) continue;
-                if (rank < ccap && running + rank < cap) write_header(feats, running + rank, cx * 32 + 4 * k + b, y, sv);
-                ++rank;
-            }
-        }
-        running += tot < ccap ? tot : ccap;
-    }
-}
-
 __device__ void xsort_level(const FrameDev& F, int l, uint32_t kept, uint32_t* s_hist, uint32_t* s_warp);
-
-// One CTA per (frame, level): keypoints in (y, x) order (or cell order with
-// per-cell caps) from the culled strength map, the level cap applied to the
-// first `cap`, then a counting sort of the kept features by x for the
-// matcher's window lookup.
-__global__ void __launch_bounds__(KC_THREADS)
-k_compact(const FrameDev* __restrict__ frames, const SegDev* __restrict__ segs) {
-    extern __shared__ uint32_t s_hist[];  // [w + 1]
-    __shared__ uint32_t s_warp[33];
-    __shared__ uint32_t s_base[32];
-    const SegDev sg = segs[blockIdx.x];
-    const FrameDev& F = frames[sg.frame];
-    const int l = sg.level;
-    const int w = F.w[l], h = F.h[l], kpitch = F.kp_pitch[l];
-    const uint8_t* kp = F.kpmap[l];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const uint32_t cap = (uint32_t)F.cap;
-    uint32_t* feats = F.feats[l];
-    uint32_t total, kept;
-    if (F.cell_cap <= 0) {
-        compact_rows(kp, kpitch, w, h, cap, feats, s_base, s_warp, &total);
-        kept = total < cap ? total : cap;
-    } else {
-        compact_cells(kp, kpitch, w, h, cap, (uint32_t)F.cell_cap, feats, s_base, s_warp, &total, &kept);
-    }
-    if (threadIdx.x == 0) {
-        F.raw[l] = total;
-        F.kept[l] = kept;
-    }
-
-    __syncthreads();
-    xsort_level(F, l, kept, s_hist, s_warp);
-}
 
 // Counting sort of one level's kept features by x (dynamic shared memory
 // s_hist of w + 1 counters): colstart[x] = first slot of column x in xorder.
@@ -641,15 +488,17 @@ k_xsort(const FrameDev* __restrict__ frames, const SegDev* __restrict__ segs) {
 }
 
 // --------------------------------------------------- banded compaction ----
-// The same compaction as k_compact, spread over one CTA per 32-row band of
-// every level (a band is also one row of 32x32 cells):
+// Keypoint compaction, spread over one CTA per 32-row band of every level (a
+// band is also one row of 32x32 cells):
 //   k_band_count  per band: raw keypoints and keypoints kept by the cell caps
 //   k_band_write  per band: prefix of the earlier bands' kept counts, then the
 //                 ordered write of the band's headers below the level cap;
 //                 band 0 also writes the level's raw / kept totals
 //   k_xsort       per level: counting sort of the kept features by x
-// Positions equal k_compact's: the list order ((y, x), or cell order) is the
-// band order followed by the order inside each band.
+// The list order ((y, x), or cell order with per-cell caps) is the band
+// order followed by the order inside each band; the level cap keeps the
+// first `cap` of it (generate_features.wgsl:67-70 appends in a racy order,
+// so this canonical order is the deterministic policy).
 constexpr int KBAND_THREADS = 256;
 constexpr int KBAND_WARPS = KBAND_THREADS / 32;
 
@@ -1449,13 +1298,6 @@ cudaError_t launch_detect(const FrameDev* frames, const TileItem* tiles, int nti
                          : launch_detect_profile<false>(frames, tiles, ntiles, shape, err, st);
 }
 
-cudaError_t launch_compact(const FrameDev* frames, const SegDev* segs, int nseg, int max_w, cudaStream_t st) {
-    if (nseg <= 0) return cudaSuccess;
-    const size_t smem = (size_t)(max_w + 1) * sizeof(uint32_t);
-    k_compact<<<nseg, KC_THREADS, smem, st>>>(frames, segs);
-    return cudaGetLastError();
-}
-
 cudaError_t launch_compact_banded(const FrameDev* frames, const BandItem* bands, int nbands, const SegDev* segs,
                                   int nseg, int max_w, cudaStream_t st) {
     if (nseg <= 0) return cudaSuccess;
@@ -1512,8 +1354,6 @@ cudaError_t launch_bruteforce(const FrameDev* frames, const PairDev* pairs, cons
 cudaError_t set_compact_smem(int max_w) {
     const size_t smem = (size_t)(max_w + 1) * sizeof(uint32_t);
     if (smem <= 48 * 1024) return cudaSuccess;
-    cudaError_t e = cudaFuncSetAttribute(k_compact, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
     return cudaFuncSetAttribute(k_xsort, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
 }
 

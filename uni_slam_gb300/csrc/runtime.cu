@@ -64,7 +64,7 @@ struct uslam_batch {
     char* d_tables = nullptr;
     cudaStream_t stream = nullptr;      // stream in use (own or caller's)
     cudaStream_t own_stream = nullptr;  // created with the batch
-    cudaStream_t aux_stream = nullptr;  // k_blur_border's branch beside k_compact
+    cudaStream_t aux_stream = nullptr;  // k_blur_border's branch beside the compaction
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     Program full;
     std::vector<Program> frame_prog;  // per frame: detect+describe only
@@ -137,8 +137,8 @@ cudaError_t enqueue_program(uslam_batch* b, const Program& P) {
         if ((e = launch_detect_shaped(b->d_frames, P.tiles, P.tile_begin, c->detector, b->d_err, b->stream)) != cudaSuccess)
             return e;
         const int grid = c->num_sms * 4;
-        // k_blur_border (the blur cache's border) and k_compact (the keypoint
-        // lists) both read only what k_detect wrote: the border runs on a
+        // k_blur_border (the blur cache's border) and the compaction (the
+        // keypoint lists) both read only what k_detect wrote: the border runs on a
         // forked stream beside the compaction and joins before k_describe,
         // which needs both (in a captured graph this is a fork/join).
         if ((e = cudaEventRecord(b->ev_fork, b->stream)) != cudaSuccess) return e;

@@ -24,7 +24,6 @@ struct MatchSegDev {
 };
 cudaError_t init_constants();
 cudaError_t launch_detect(const FrameDev*, const TileItem*, int, int, int, uint32_t*, cudaStream_t);
-cudaError_t launch_compact(const FrameDev*, const SegDev*, int, int, cudaStream_t);
 cudaError_t launch_compact_banded(const FrameDev*, const BandItem*, int, const SegDev*, int, int, cudaStream_t);
 cudaError_t launch_blur_border(const FrameDev*, const SegDev*, int, int, cudaStream_t);
 cudaError_t launch_describe(const FrameDev*, const SegDev*, int, const int32_t*, int, cudaStream_t);

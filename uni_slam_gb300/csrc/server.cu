@@ -39,6 +39,7 @@ struct SrvClass {
     int tiles_per_frame = 0;
     int shape = 0;                // detect tile shape (index into kTileShapes)
     std::vector<TileItem> tiles;  // one frame's tile list (frame field patched per launch)
+    std::vector<BandItem> bands;  // one frame's compaction bands (frame field patched per launch)
 };
 
 struct SrvSlot {
@@ -111,13 +112,14 @@ struct uslam_server {
 
 namespace {
 
-size_t tables_bytes(int max_batch, int max_tiles_per_frame, int levels) {
+size_t tables_bytes(int max_batch, int max_tiles_per_frame, int max_bands_per_frame, int levels) {
     const size_t t = round_up(sizeof(TileItem) * static_cast<size_t>(max_batch) * max_tiles_per_frame, 256);
     const size_t f = round_up(sizeof(SegDev) * static_cast<size_t>(max_batch) * levels, 256);
     const size_t m = round_up(sizeof(MatchSegDev) * static_cast<size_t>(max_batch) * 2 * levels, 256);
     const size_t u = round_up(sizeof(SegDev) * static_cast<size_t>(max_batch) * levels, 256);
     const size_t p = round_up(sizeof(PairDev) * static_cast<size_t>(max_batch), 256);
-    return t + f + m + u + p;
+    const size_t b = round_up(sizeof(BandItem) * static_cast<size_t>(max_batch) * max_bands_per_frame, 256);
+    return t + f + m + u + p + b;
 }
 
 void free_server(uslam_server* s) {
@@ -150,6 +152,7 @@ cudaError_t launch_batch(uslam_server* s, const std::vector<uint64_t>& tickets, 
     std::vector<SegDev> fsegs, usegs;
     std::vector<MatchSegDev> msegs;
     std::vector<PairDev> pairs;
+    std::vector<BandItem> bands;
     cudaError_t e = cudaSuccess;
     for (uint64_t tk : tickets) {
         SrvReq& r = s->reqs[tk];
@@ -160,6 +163,10 @@ cudaError_t launch_batch(uslam_server* s, const std::vector<uint64_t>& tickets, 
             shaped.by_shape[C.shape].push_back(t);
         }
         for (int l = 0; l < lv; ++l) fsegs.push_back(SegDev{r.slot, l});
+        for (BandItem bi : C.bands) {
+            bi.frame = static_cast<uint16_t>(r.slot);
+            bands.push_back(bi);
+        }
         const FrameDev& F = s->frames[r.slot];
         e = cudaMemcpyAsync(const_cast<uint8_t*>(F.img), sl.h_in, static_cast<size_t>(F.H0) * F.img_pitch,
                             cudaMemcpyHostToDevice, st);
@@ -195,20 +202,22 @@ cudaError_t launch_batch(uslam_server* s, const std::vector<uint64_t>& tickets, 
     }
     shaped.finish();
     const std::vector<TileItem>& tiles = shaped.flat;
-    // table image: tiles | fsegs | msegs | usegs | pairs
+    // table image: tiles | fsegs | msegs | usegs | pairs | bands
     const size_t t_b = round_up(tiles.size() * sizeof(TileItem), 256);
     const size_t f_b = round_up(fsegs.size() * sizeof(SegDev), 256);
     const size_t m_b = round_up(msegs.size() * sizeof(MatchSegDev), 256);
     const size_t u_b = round_up(usegs.size() * sizeof(SegDev), 256);
     const size_t p_b = round_up(pairs.size() * sizeof(PairDev), 256);
-    if (t_b + f_b + m_b + u_b + p_b > B.bytes) return cudaErrorInvalidValue;
+    const size_t b_b = round_up(bands.size() * sizeof(BandItem), 256);
+    if (t_b + f_b + m_b + u_b + p_b + b_b > B.bytes) return cudaErrorInvalidValue;
     char* h = B.h;
     std::memcpy(h, tiles.data(), tiles.size() * sizeof(TileItem));
     std::memcpy(h + t_b, fsegs.data(), fsegs.size() * sizeof(SegDev));
     std::memcpy(h + t_b + f_b, msegs.data(), msegs.size() * sizeof(MatchSegDev));
     std::memcpy(h + t_b + f_b + m_b, usegs.data(), usegs.size() * sizeof(SegDev));
     std::memcpy(h + t_b + f_b + m_b + u_b, pairs.data(), pairs.size() * sizeof(PairDev));
-    const size_t total = t_b + f_b + m_b + u_b + p_b;
+    std::memcpy(h + t_b + f_b + m_b + u_b + p_b, bands.data(), bands.size() * sizeof(BandItem));
+    const size_t total = t_b + f_b + m_b + u_b + p_b + b_b;
     e = cudaMemcpyAsync(B.d, h, total, cudaMemcpyHostToDevice, st);
     if (e != cudaSuccess) return e;
     const auto* d_tiles = reinterpret_cast<const TileItem*>(B.d);
@@ -216,11 +225,14 @@ cudaError_t launch_batch(uslam_server* s, const std::vector<uint64_t>& tickets, 
     const auto* d_msegs = B.d + t_b + f_b;
     const auto* d_usegs = reinterpret_cast<const SegDev*>(B.d + t_b + f_b + m_b);
     const auto* d_pairs = reinterpret_cast<const PairDev*>(B.d + t_b + f_b + m_b + u_b);
+    const auto* d_bands = reinterpret_cast<const BandItem*>(B.d + t_b + f_b + m_b + u_b + p_b);
     const int grid = c->num_sms * 4;
     const int nf = static_cast<int>(fsegs.size());
     if ((e = launch_detect_shaped(s->d_frames, d_tiles, shaped.begin, c->detector, s->d_err, st)) != cudaSuccess) return e;
     if ((e = launch_blur_border(s->d_frames, d_fsegs, nf, grid, st)) != cudaSuccess) return e;
-    if ((e = launch_compact(s->d_frames, d_fsegs, nf, s->max_w, st)) != cudaSuccess) return e;
+    if ((e = launch_compact_banded(s->d_frames, d_bands, static_cast<int>(bands.size()), d_fsegs, nf, s->max_w,
+                                   st)) != cudaSuccess)
+        return e;
     if ((e = launch_describe(s->d_frames, d_fsegs, nf, c->d_pattern, grid, st)) != cudaSuccess) return e;
     if (!pairs.empty()) {
         if ((e = launch_match(s->d_frames, d_pairs, d_msegs, static_cast<int>(msegs.size()), grid, st)) != cudaSuccess)
@@ -323,11 +335,11 @@ uslam_status uslam_server_create(uslam_ctx* ctx, const uslam_server_params* p, u
     // slot bytes per class, then slots per class from an equal share of the budget
     struct SlotLayout {
         size_t bytes, in, counts, lvl[USLAM_MAX_LEVELS], blur[USLAM_MAX_LEVELS], kpmap[USLAM_MAX_LEVELS],
-            feats[USLAM_MAX_LEVELS], xorder[USLAM_MAX_LEVELS], colstart[USLAM_MAX_LEVELS], a2b, b2a, matches, mcount;
+            feats[USLAM_MAX_LEVELS], xorder[USLAM_MAX_LEVELS], colstart[USLAM_MAX_LEVELS], bands[USLAM_MAX_LEVELS], a2b, b2a, matches, mcount;
     };
     std::vector<SlotLayout> lay(p->n_sizes);
     std::vector<FrameDev> proto(p->n_sizes);
-    int max_tiles = 1;
+    int max_tiles = 1, max_bands = 1;
     for (int k = 0; k < p->n_sizes; ++k) {
         const int W0 = p->widths[k], H0 = p->heights[k];
         if (W0 < 1 || H0 < 1 || W0 > ctx->max_w || H0 > ctx->max_h) {
@@ -372,9 +384,17 @@ uslam_status uslam_server_create(uslam_ctx* ctx, const uslam_server_params* p, u
             Y.kpmap[l] = take(static_cast<size_t>(F.h[l]) * F.kp_pitch[l]);
             Y.xorder[l] = take(capa * 4);
             Y.colstart[l] = take((static_cast<size_t>(F.w[l]) + 1) * 4);
+            Y.bands[l] = take(static_cast<size_t>((F.h[l] + 31) / 32) * 8);
         }
         C.shape = ctx->shape_for(W0, H0);
         append_tiles(&C.tiles, 0, F, C.shape);
+        for (int l = 0; l < L; ++l)
+            for (int q = 0; q < (F.h[l] + 31) / 32; ++q) {
+                BandItem bi{};
+                bi.level = static_cast<uint8_t>(l);
+                bi.band = static_cast<uint16_t>(q);
+                C.bands.push_back(bi);
+            }
         Y.a2b = take(static_cast<size_t>(L) * capa * 4);
         Y.b2a = take(static_cast<size_t>(L) * capa * 4);
         Y.matches = take(static_cast<size_t>(L) * capa * 16);
@@ -382,6 +402,7 @@ uslam_status uslam_server_create(uslam_ctx* ctx, const uslam_server_params* p, u
         Y.bytes = round_up(cur, 256);
         C.tiles_per_frame = static_cast<int>(C.tiles.size());
         max_tiles = std::max(max_tiles, C.tiles_per_frame);
+        max_bands = std::max(max_bands, static_cast<int>(C.bands.size()));
         s->max_w = std::max(s->max_w, F.w[0]);
         s->classes.push_back(std::move(C));
     }
@@ -432,6 +453,7 @@ uslam_status uslam_server_create(uslam_ctx* ctx, const uslam_server_params* p, u
                 F.feats[l] = reinterpret_cast<uint32_t*>(base + Y.feats[l]);
                 F.xorder[l] = reinterpret_cast<uint32_t*>(base + Y.xorder[l]);
                 F.colstart[l] = reinterpret_cast<uint32_t*>(base + Y.colstart[l]);
+                F.bands[l] = reinterpret_cast<uint32_t*>(base + Y.bands[l]);
                 F.mask[l] = masks[l];
             }
             s->frames[g] = F;
@@ -448,7 +470,7 @@ uslam_status uslam_server_create(uslam_ctx* ctx, const uslam_server_params* p, u
     if (e == cudaSuccess)
         e = cudaMemcpy(s->d_frames, s->frames.data(), sizeof(FrameDev) * nslots, cudaMemcpyHostToDevice);
     for (int b = 0; b < 2 && e == cudaSuccess; ++b) {
-        s->bufs[b].bytes = tables_bytes(s->max_batch, max_tiles, L);
+        s->bufs[b].bytes = tables_bytes(s->max_batch, max_tiles, max_bands, L);
         e = cudaHostAlloc(&s->bufs[b].h, s->bufs[b].bytes, cudaHostAllocDefault);
         if (e == cudaSuccess) e = cudaMalloc(&s->bufs[b].d, s->bufs[b].bytes);
         if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->cs[b], cudaStreamNonBlocking);
