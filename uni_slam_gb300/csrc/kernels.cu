@@ -1026,9 +1026,21 @@ k_match(const FrameDev* __restrict__ frames, const PairDev* __restrict__ pairs,
                     __syncwarp();
                     const int a = (int)(max(m0, base) - base);
                     const int b = (int)(min(m1, base + 32u) > base ? min(m1, base + 32u) - base : 0u);
-                    uint32_t hits = 0u;
-                    for (int t = a; t < b; ++t)
-                        if (!(fabsf(cy - S.py[t]) > dy)) hits |= 1u << t;
+                    // y test of all 32 staged candidates (unrolled, float4 loads),
+                    // masked by this lane's slots [a, b)
+                    uint32_t ymask = 0u;
+                    const float4* py4 = reinterpret_cast<const float4*>(S.py);
+#pragma unroll
+                    for (int q = 0; q < 8; ++q) {
+                        const float4 v = py4[q];
+                        ymask |= (!(fabsf(cy - v.x) > dy) ? 1u : 0u) << (4 * q);
+                        ymask |= (!(fabsf(cy - v.y) > dy) ? 1u : 0u) << (4 * q + 1);
+                        ymask |= (!(fabsf(cy - v.z) > dy) ? 1u : 0u) << (4 * q + 2);
+                        ymask |= (!(fabsf(cy - v.w) > dy) ? 1u : 0u) << (4 * q + 3);
+                    }
+                    const uint32_t lo_mask = a >= 32 ? 0u : (0xffffffffu << a);
+                    const uint32_t hi_mask = b >= 32 ? 0xffffffffu : ((1u << b) - 1u);
+                    uint32_t hits = ymask & lo_mask & hi_mask;
                     // keys (distance << 5 | batch slot): min/max keep the two
                     // smallest distances without branches; the slot of the best
                     // is resolved to its candidate once per batch
