@@ -14,7 +14,8 @@ batches in flight, so one step's copies overlap the next step's kernels;
 ``e2e.unpipelined_value`` is one batch with a sync after every step);
 ``plain_fps`` = the plain per-frame form (one frame per launch sequence,
 synchronous per frame); ``served`` = 32 camera streams at 20 Hz through the
-serving loop (p50/p99 latency, frames/s); ``uneven`` = 46 frames of five
+serving loop (p50/p99 latency, frames/s), and ``served.saturation`` = the
+same streams closed-loop with 4 frames in flight each (capacity); ``uneven`` = 46 frames of five
 sizes (640x480 .. 3840x2160) each matched against its warp in one graph,
 per-32x32-cell caps, detect tiles autotuned per size; ``cfg`` = the main
 workload in the cfg profile (FAST 9-of-16 at 20/255, 3x3 NMS, brute-force
@@ -342,6 +343,93 @@ def serve_simulation(ctx, seconds: float, n_streams: int = 32, rate_hz: float = 
         "max_ms": float(arr.max()), "admission_retries": refused, "launches": st["launches"],
         "max_batch_seen": st["max_batch_seen"], "slots": st["slots"],
         "sizes": {f"{w}x{h}": sizes.count((w, h)) for (w, h) in SERVE_SIZES},
+    }
+
+
+def serve_saturation(ctx, seconds: float, n_streams: int = 32, inflight: int = 4, promote_every: int = 10,
+                     seed: int = 0, frames_per_stream: int = 6, submitters: int = 4) -> dict:
+    """Closed-loop capacity of the serving loop: the same streams as
+    serve_simulation, each keeping `inflight` frames outstanding (a new frame
+    is submitted as soon as one completes), so the dispatcher always finds
+    queued requests and batches them.  `submitters` host threads each feed a
+    share of the streams (frame copies into pinned staging run in parallel).
+    Latency runs from submit to completion."""
+    import queue
+
+    import numpy as np
+
+    from uni_slam_gb300 import Server, synth
+
+    rs = np.random.RandomState(seed + 7)
+    tex = synth.plane_texture(np.random.RandomState(seed + 11), 4096)
+    sizes = [SERVE_SIZES[rs.randint(len(SERVE_SIZES))] for _ in range(n_streams)]
+    frames = [synth.plane_sequence(1000 + k, frames_per_stream, w, h, texture=tex) for k, (w, h) in enumerate(sizes)]
+    srv = Server(ctx, SERVE_SIZES, hbm_budget_bytes=8 << 30, max_batch=64)
+    ids = [srv.open_stream(w, h) for (w, h) in sizes]
+    count = [0] * n_streams
+    outstanding = [0] * n_streams
+    lock = threading.Lock()
+    done_q: queue.Queue = queue.Queue()
+    lat: list[float] = []
+
+    def completer():
+        while True:
+            item = done_q.get()
+            if item is None:
+                return
+            tk, k = item
+            srv.wait(tk, 0)
+            lat.append(srv.latency_ms(tk))
+            srv.release(tk)
+            with lock:
+                outstanding[k] -= 1
+
+    th = threading.Thread(target=completer, daemon=True)
+    th.start()
+    start = time.perf_counter()
+    end = start + seconds
+    refused = [0] * submitters
+
+    def submitter(me: int):
+        mine = range(me, n_streams, submitters)
+        while time.perf_counter() < end:
+            progressed = False
+            for k in mine:
+                with lock:
+                    free = outstanding[k] < inflight
+                if not free:
+                    continue
+                tk = srv.submit(ids[k], frames[k][count[k] % frames_per_stream],
+                                promote=(count[k] % promote_every == 0))
+                if tk is None:
+                    refused[me] += 1
+                    continue
+                with lock:
+                    outstanding[k] += 1
+                done_q.put((tk, k))
+                count[k] += 1
+                progressed = True
+            if not progressed:
+                time.sleep(20e-6)
+
+    subs = [threading.Thread(target=submitter, args=(m,), daemon=True) for m in range(submitters)]
+    for t in subs:
+        t.start()
+    for t in subs:
+        t.join()
+    refused = sum(refused)
+    done_q.put(None)
+    th.join()
+    elapsed = time.perf_counter() - start
+    st = srv.stats()
+    srv.close()
+    arr = np.array(lat)
+    return {
+        "streams": n_streams, "inflight_per_stream": inflight, "submit_threads": submitters, "seconds": seconds,
+        "frames": int(arr.size),
+        "fps": arr.size / elapsed, "p50_ms": float(np.percentile(arr, 50)), "p99_ms": float(np.percentile(arr, 99)),
+        "admission_retries": refused, "launches": st["launches"], "max_batch_seen": st["max_batch_seen"],
+        "frames_per_launch": arr.size / max(1, st["launches"]),
     }
 
 
@@ -725,6 +813,8 @@ def run_ours(a):
         # keyframes hold up to 2000 descriptors: 333 per level x 6 levels
         sctx = Context(pat, levels=LEVELS, max_width=1280, max_height=720, cap_per_level=333, device=local)
         served = serve_simulation(sctx, a.serve_seconds, n_streams=a.serve_streams, seed=a.seed + rank)
+        served["saturation"] = serve_saturation(sctx, min(a.serve_seconds, 5.0), n_streams=a.serve_streams,
+                                                seed=a.seed + rank)
         sctx.close()
 
     cfg = cfg_run(pat, local, frames, a.stress_steps, 2) if a.cfg else None

@@ -237,7 +237,10 @@ uslam_status uslam_server_open_stream(uslam_server* server, int width, int heigh
 /* Copy a frame into a free slot and queue it.  promote_keyframe: this frame
  * becomes the stream's keyframe for the frames submitted after it (a
  * stream's first frame always does).  USLAM_CAPACITY: no free slot of that
- * size right now (admission refused; retry later). */
+ * size right now (admission refused; retry later).  Different streams may
+ * submit from different threads at the same time (the frame copy runs
+ * outside the server's lock); the frames of one stream come from one thread
+ * at a time, in order. */
 uslam_status uslam_server_submit(uslam_server* server, int stream, const uint8_t* img, int pitch,
                                  int promote_keyframe, uint64_t* ticket);
 uslam_status uslam_server_wait(uslam_server* server, uint64_t ticket, int timeout_ms);

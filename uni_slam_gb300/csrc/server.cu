@@ -537,15 +537,19 @@ uslam_status uslam_server_submit(uslam_server* s, int stream, const uint8_t* img
     if (slot < 0) return set_err(&s->ctx->err, USLAM_CAPACITY, "submit: no free slot of this size (HBM budget)");
     SrvSlot& sl = s->slots[slot];
     const FrameDev& F = s->frames[slot];
+    // reserve the slot, copy the frame into its pinned staging without the
+    // lock (several submitting threads copy in parallel), then queue it
+    sl.in_use = true;
+    lk.unlock();
     for (int y = 0; y < F.H0; ++y)
         std::memcpy(sl.h_in + static_cast<size_t>(y) * F.img_pitch, img + static_cast<size_t>(y) * pitch, F.W0);
+    lk.lock();
     SrvReq r;
     r.stream = stream;
     r.slot = slot;
     r.ref = S.keyframe;
     r.promote = promote_keyframe != 0 || S.keyframe < 0;
     r.t_submit = Clock::now();
-    sl.in_use = true;
     if (r.ref >= 0) ++s->slots[r.ref].refs;
     if (r.promote) {
         if (S.keyframe >= 0) s->slots[S.keyframe].keyframe = false;
