@@ -31,6 +31,12 @@ constexpr int K1_THREADS = 256;
 // cfg detection profile threshold: 20 grey levels on the u8/255 scale.
 constexpr float kCfgThreshold = 20.0f / 255.0f;
 
+// Matcher band of a LOD-0 y in a frame of height H (rows [b H / B, (b + 1) H / B)).
+__device__ __forceinline__ int match_band(float y, float H) {
+    const int b = (int)floorf(y * (float)USLAM_MATCH_BANDS / H);
+    return b < 0 ? 0 : (b >= USLAM_MATCH_BANDS ? USLAM_MATCH_BANDS - 1 : b);
+}
+
 // Bresenham circle of radius 3 (resources/detect_corners.wgsl:31-32) as
 // compile-time constants: in the unrolled loops the shared-memory offsets fold
 // into immediates.
@@ -437,17 +443,17 @@ __device__ __forceinline__ void load_cell_row(const uint8_t* kp, int kpitch, int
 
 __device__ void xsort_level(const FrameDev& F, int l, uint32_t kept, uint32_t* s_hist, uint32_t* s_warp);
 
-// Counting sort of one level's kept features by x (dynamic shared memory
-// s_hist of w + 1 counters): colstart[x] = first slot of column x in xorder.
-__device__ void xsort_level(const FrameDev& F, int l, uint32_t kept, uint32_t* s_hist, uint32_t* s_warp) {
-    const int w = F.w[l];
-    const uint32_t* feats = F.feats[l];
+// One counting-sort pass over a level's kept features (dynamic shared memory
+// s_hist of w + 1 counters): the indices of the features with pick(i) true,
+// sorted by x, go to order_out; colstart_out (if given) receives the first
+// slot of each column.  Returns the number of features picked.
+template <typename Pick>
+__device__ uint32_t xsort_pass(const uint32_t* feats, uint32_t kept, int w, Pick pick, uint32_t* order_out,
+                               uint32_t* colstart_out, uint32_t* s_hist, uint32_t* s_warp) {
     for (int i = threadIdx.x; i <= w; i += blockDim.x) s_hist[i] = 0u;
     __syncthreads();
-    for (uint32_t i = threadIdx.x; i < kept; i += blockDim.x) {
-        const int fx = (int)__uint_as_float(feats[(size_t)i * 12u]);
-        atomicAdd(&s_hist[fx], 1u);
-    }
+    for (uint32_t i = threadIdx.x; i < kept; i += blockDim.x)
+        if (pick(i)) atomicAdd(&s_hist[(int)__uint_as_float(feats[(size_t)i * 12u])], 1u);
     __syncthreads();
     const int per = (w + (int)blockDim.x) / (int)blockDim.x;  // bins per thread over w + 1 bins
     const int b0 = threadIdx.x * per;
@@ -458,23 +464,64 @@ __device__ void xsort_level(const FrameDev& F, int l, uint32_t kept, uint32_t* s
     }
     uint32_t tot;
     uint32_t run = block_exclusive_scan(local, s_warp, &tot);
-    uint32_t* colstart = F.colstart[l];
     for (int k = 0; k < per; ++k) {
         const int b = b0 + k;
         if (b <= w) {
             const uint32_t c = b < w ? s_hist[b] : 0u;
-            colstart[b] = run;
+            if (colstart_out) colstart_out[b] = run;
             s_hist[b] = run;  // becomes the fill cursor
             run += c;
         }
     }
     __syncthreads();
-    uint32_t* xorder = F.xorder[l];
-    for (uint32_t i = threadIdx.x; i < kept; i += blockDim.x) {
-        const int fx = (int)__uint_as_float(feats[(size_t)i * 12u]);
-        const uint32_t slot = atomicAdd(&s_hist[fx], 1u);
-        xorder[slot] = i;
+    for (uint32_t i = threadIdx.x; i < kept; i += blockDim.x)
+        if (pick(i)) order_out[atomicAdd(&s_hist[(int)__uint_as_float(feats[(size_t)i * 12u])], 1u)] = i;
+    __syncthreads();
+    return tot;
+}
+
+// LOD-0 y of a feature (match_features_cpu.cpp:58-64: f32 scale iterated).
+__device__ __forceinline__ float lod0_y(const uint32_t* feats, uint32_t i, float scale) {
+    return (float)(uint32_t)__uint_as_float(feats[(size_t)i * 12u + 1u]) * scale;
+}
+
+// The matcher's index of one level.  The frame height is cut into
+// USLAM_MATCH_BANDS bands (LOD-0 rows [b H0 / B, (b + 1) H0 / B)):
+//  * candidate list b = the features whose LOD-0 y lies in band b widened by
+//    0.1 H0 + 2 (the window half-height plus slack), sorted by x, with the
+//    first slot of each column; every feature inside the window of a query
+//    of band b is in list b;
+//  * query order = the features grouped by the band of their own LOD-0 y,
+//    sorted by x within a band, with the band offsets after the column tables.
+__device__ void xsort_level(const FrameDev& F, int l, uint32_t kept, uint32_t* s_hist, uint32_t* s_warp) {
+    constexpr int NB = USLAM_MATCH_BANDS;
+    const int w = F.w[l];
+    const uint32_t* feats = F.feats[l];
+    float scale = 1.0f;
+    for (int i = 0; i < l; ++i) scale = scale * 1.2f;
+    const float H = (float)(uint32_t)F.H0;
+    const float margin = 0.1f * H + 2.0f;
+    const size_t cap = (size_t)(F.cap > 0 ? F.cap : 1);
+    uint32_t* qband = F.colstart[l] + (size_t)NB * (size_t)(w + 1);
+    for (int b = 0; b < NB; ++b) {
+        const float lo = (float)b * H / (float)NB - margin, hi = (float)(b + 1) * H / (float)NB + margin;
+        xsort_pass(
+            feats, kept, w,
+            [&](uint32_t i) {
+                const float y = lod0_y(feats, i, scale);
+                return y >= lo && y <= hi;
+            },
+            F.xorder[l] + (size_t)b * cap, F.colstart[l] + (size_t)b * (size_t)(w + 1), s_hist, s_warp);
     }
+    uint32_t base = 0;
+    for (int b = 0; b < NB; ++b) {
+        const uint32_t n = xsort_pass(
+            feats, kept, w, [&](uint32_t i) { return match_band(lod0_y(feats, i, scale), H) == b; },
+            F.qorder[l] + base, nullptr, s_hist, s_warp);
+        if (threadIdx.x == 0) qband[b] = base;
+        base += n;
+    }
+    if (threadIdx.x == 0) qband[NB] = base;
 }
 
 // Per (frame, level): the x counting sort after the banded compaction.
@@ -947,10 +994,16 @@ k_match(const FrameDev* __restrict__ frames, const PairDev* __restrict__ pairs,
     __shared__ uint32_t s_pref[MAX_SEGS + 1];
     __shared__ uint32_t s_warp[33];
     __shared__ CandStage s_stage[KM_THREADS / 32];
+    // work units: groups of 32 queries of one band (band offsets follow the
+    // query level's column tables)
     const uint32_t total = segment_prefix(nseg, s_pref, s_warp, [&](int s) {
         const PairDev& P = pairs[segs[s].pair];
-        const int qf = segs[s].dir == 0 ? P.curr : P.prev;
-        return (frames[qf].kept[segs[s].level] + 31u) / 32u;
+        const FrameDev& Qf = frames[segs[s].dir == 0 ? P.curr : P.prev];
+        const int ql = segs[s].level;
+        const uint32_t* qb = Qf.colstart[ql] + (size_t)USLAM_MATCH_BANDS * (size_t)(Qf.w[ql] + 1);
+        uint32_t n = 0;
+        for (int b = 0; b < USLAM_MATCH_BANDS; ++b) n += (qb[b + 1] - qb[b] + 31u) / 32u;
+        return n;
     });
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
@@ -959,16 +1012,21 @@ k_match(const FrameDev* __restrict__ frames, const PairDev* __restrict__ pairs,
     CandStage& S = s_stage[warp];
     for (uint32_t g = gw; g < total; g += nw) {
         const int sidx = find_segment(s_pref, nseg, g);
-        const uint32_t grp = g - s_pref[sidx];
+        uint32_t grp = g - s_pref[sidx];
         const MatchSegDev sg = segs[sidx];
         const PairDev& P = pairs[sg.pair];
         const FrameDev& Q = frames[sg.dir == 0 ? P.curr : P.prev];
         const FrameDev& B = frames[sg.dir == 0 ? P.prev : P.curr];
         const int l = sg.level;
-        const uint32_t nq = Q.kept[l];
-        const uint32_t qk = grp * 32u + (uint32_t)lane;
-        const bool valid = qk < nq;
-        const uint32_t qi = valid ? __ldg(Q.xorder[l] + qk) : 0u;
+        const uint32_t* qband = Q.colstart[l] + (size_t)USLAM_MATCH_BANDS * (size_t)(Q.w[l] + 1);
+        int band = 0;
+        while (band + 1 < USLAM_MATCH_BANDS && grp >= (qband[band + 1] - qband[band] + 31u) / 32u) {
+            grp -= (qband[band + 1] - qband[band] + 31u) / 32u;
+            ++band;
+        }
+        const uint32_t qk = qband[band] + grp * 32u + (uint32_t)lane;
+        const bool valid = qk < qband[band + 1];
+        const uint32_t qi = valid ? __ldg(Q.qorder[l] + qk) : 0u;
         const uint32_t* qrec = Q.feats[l] + (size_t)qi * 12u;
         const float ql = lod_scale(l);
         const float cx = (float)(uint32_t)__uint_as_float(qrec[0]) * ql;
@@ -992,7 +1050,8 @@ k_match(const FrameDev* __restrict__ frames, const PairDev* __restrict__ pairs,
                 if (pl < 0 || pl >= L) continue;
                 const float ps = lod_scale(pl);
                 const int wpl = B.w[pl];
-                const uint32_t* colstart = B.colstart[pl];
+                // the pool's candidate list of this band
+                const uint32_t* colstart = B.colstart[pl] + (size_t)band * (size_t)(wpl + 1);
                 // this lane's exact candidate range
                 uint32_t m0 = 0u, m1 = 0u;
                 if (valid) {
@@ -1011,7 +1070,7 @@ k_match(const FrameDev* __restrict__ frames, const PairDev* __restrict__ pairs,
                     c1 = max(c1, __shfl_xor_sync(0xffffffffu, c1, o));
                 }
                 if (c0 >= c1) continue;
-                const uint32_t* xorder = B.xorder[pl];
+                const uint32_t* xorder = B.xorder[pl] + (size_t)band * (size_t)(B.cap > 0 ? B.cap : 1);
                 const uint32_t* feats = B.feats[pl];
                 for (uint32_t base = c0; base < c1; base += 32u) {
                     const uint32_t kk = base + (uint32_t)lane;
@@ -1318,6 +1377,12 @@ cudaError_t launch_compact_banded(const FrameDev* frames, const BandItem* bands,
     if (e != cudaSuccess) return e;
     k_band_write<<<nbands, KBAND_THREADS, 0, st>>>(frames, bands);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    k_xsort<<<nseg, KC_THREADS, (size_t)(max_w + 1) * sizeof(uint32_t), st>>>(frames, segs);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_xsort(const FrameDev* frames, const SegDev* segs, int nseg, int max_w, cudaStream_t st) {
+    if (nseg <= 0) return cudaSuccess;
     k_xsort<<<nseg, KC_THREADS, (size_t)(max_w + 1) * sizeof(uint32_t), st>>>(frames, segs);
     return cudaGetLastError();
 }

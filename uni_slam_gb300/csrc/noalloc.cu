@@ -28,6 +28,8 @@ struct MatchSegDev {
 };
 cudaError_t launch_match(const FrameDev*, const PairDev*, const void*, int, int, cudaStream_t);
 cudaError_t launch_mutual(const FrameDev*, const PairDev*, const SegDev*, int, uint32_t*, cudaStream_t);
+cudaError_t launch_xsort(const FrameDev*, const SegDev*, int, int, cudaStream_t);
+cudaError_t set_compact_smem(int max_w);
 }  // namespace uslam
 
 using namespace uslam;
@@ -36,7 +38,6 @@ namespace {
 
 constexpr size_t kNoallocScratchBytes = size_t(4) << 20;  // 4 MiB per device
 constexpr int kMaxDevices = 64;
-constexpr int kXsortThreads = 1024;
 
 // The no-alloc matcher's scratch.  Host code must not use this name as an
 // address: it is a host-side stand-in.  The device address comes from
@@ -58,70 +59,6 @@ __global__ void k_noalloc_tables(const NoallocTables t, NoallocTables* dst) {
     const uint32_t* s = reinterpret_cast<const uint32_t*>(&t);
     uint32_t* d = reinterpret_cast<uint32_t*>(dst);
     for (size_t i = threadIdx.x; i < sizeof(NoallocTables) / 4; i += blockDim.x) d[i] = s[i];
-}
-
-// x counting sort of one (frame, level): colstart[x] = first slot of column x
-// in xorder, xorder = feature indices by x (the matcher's window lookup).
-__global__ void __launch_bounds__(kXsortThreads)
-k_noalloc_xsort(const FrameDev* __restrict__ frames, const SegDev* __restrict__ segs) {
-    extern __shared__ uint32_t s_hist[];  // [w + 1]
-    __shared__ uint32_t s_part[kXsortThreads / 32 + 1];
-    const FrameDev& F = frames[segs[blockIdx.x].frame];
-    const int l = segs[blockIdx.x].level;
-    const int w = F.w[l];
-    const uint32_t kept = F.kept[l];
-    const uint32_t* feats = F.feats[l];
-    for (int i = threadIdx.x; i <= w; i += kXsortThreads) s_hist[i] = 0u;
-    __syncthreads();
-    for (uint32_t i = threadIdx.x; i < kept; i += kXsortThreads)
-        atomicAdd(&s_hist[(int)__uint_as_float(feats[(size_t)i * 12u])], 1u);
-    __syncthreads();
-    // exclusive scan of the w + 1 bins: each thread sums a run of bins, the
-    // run totals are scanned by warp 0, then each thread writes its run
-    const int per = (w + kXsortThreads) / kXsortThreads;
-    const int b0 = threadIdx.x * per;
-    uint32_t local = 0;
-    for (int k = 0; k < per; ++k)
-        if (b0 + k < w) local += s_hist[b0 + k];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    uint32_t incl = local;
-    for (int o = 1; o < 32; o <<= 1) {
-        const uint32_t v = __shfl_up_sync(0xffffffffu, incl, o);
-        if (lane >= o) incl += v;
-    }
-    if (lane == 31) s_part[warp] = incl;
-    __syncthreads();
-    if (warp == 0) {
-        const uint32_t v = lane < kXsortThreads / 32 ? s_part[lane] : 0u;
-        uint32_t wi = v;
-        for (int o = 1; o < 32; o <<= 1) {
-            const uint32_t u = __shfl_up_sync(0xffffffffu, wi, o);
-            if (lane >= o) wi += u;
-        }
-        if (lane < kXsortThreads / 32) s_part[lane] = wi - v;
-    }
-    __syncthreads();
-    uint32_t run = s_part[warp] + incl - local;
-    uint32_t* colstart = F.colstart[l];
-    for (int k = 0; k < per; ++k) {
-        const int b = b0 + k;
-        if (b <= w) {
-            const uint32_t c = b < w ? s_hist[b] : 0u;
-            colstart[b] = run;
-            run += c;
-        }
-    }
-    __syncthreads();
-    for (int k = 0; k < per; ++k) {
-        const int b = b0 + k;
-        if (b <= w) s_hist[b] = colstart[b];
-    }
-    __syncthreads();
-    uint32_t* xorder = F.xorder[l];
-    for (uint32_t i = threadIdx.x; i < kept; i += kXsortThreads) {
-        const int fx = (int)__uint_as_float(feats[(size_t)i * 12u]);
-        xorder[atomicAdd(&s_hist[fx], 1u)] = i;
-    }
 }
 
 struct DeviceScratch {
@@ -190,15 +127,19 @@ extern "C" uslam_status uslam_match_noalloc(int device, int width, int height, i
     if (out_cap_per_level < cap[0])
         return fail(err, err_len, USLAM_INVALID_ARG, "match_noalloc: out_cap_per_level below the previous set's largest level");
 
-    // scratch layout: [tables][xorder f0][xorder f1][colstart f0][colstart f1][a2b][b2a][error word]
+    // scratch layout: [tables][xorder, qorder f0][xorder, qorder f1][colstart f0][colstart f1][a2b][b2a][error]
+    // (per level: USLAM_MATCH_BANDS candidate lists of cap entries, the query order, and per band
+    // the column table, then the band offsets)
     size_t cur = align256(sizeof(NoallocTables));
-    size_t xorder_off[2], colstart_off[2];
+    size_t xorder_off[2], qorder_off[2], colstart_off[2];
     for (int f = 0; f < 2; ++f) {
         xorder_off[f] = cur;
+        cur = align256(cur + sizeof(uint32_t) * USLAM_MATCH_BANDS * static_cast<size_t>(levels) * cap[f]);
+        qorder_off[f] = cur;
         cur = align256(cur + sizeof(uint32_t) * static_cast<size_t>(levels) * cap[f]);
     }
     size_t colsum = 0;
-    for (int l = 0; l < levels; ++l) colsum += static_cast<size_t>(wl[l]) + 1;
+    for (int l = 0; l < levels; ++l) colsum += USLAM_MATCH_BANDS * (static_cast<size_t>(wl[l]) + 1) + USLAM_MATCH_BANDS + 1;
     for (int f = 0; f < 2; ++f) {
         colstart_off[f] = cur;
         cur = align256(cur + sizeof(uint32_t) * colsum);
@@ -238,12 +179,14 @@ extern "C" uslam_status uslam_match_noalloc(int device, int width, int height, i
             F.w[l] = wl[l];
             F.h[l] = hl[l];
             F.feats[l] = reinterpret_cast<uint32_t*>(const_cast<uslam_feature*>(feats[f]) + foff);
-            F.xorder[l] = reinterpret_cast<uint32_t*>(base + xorder_off[f]) + static_cast<size_t>(l) * cap[f];
+            F.xorder[l] = reinterpret_cast<uint32_t*>(base + xorder_off[f]) +
+                          static_cast<size_t>(l) * USLAM_MATCH_BANDS * cap[f];
+            F.qorder[l] = reinterpret_cast<uint32_t*>(base + qorder_off[f]) + static_cast<size_t>(l) * cap[f];
             F.colstart[l] = reinterpret_cast<uint32_t*>(base + colstart_off[f]) + coff;
             t.counts[f][l] = static_cast<uint32_t>(kept[f][l]);
             t.counts[f][levels + l] = static_cast<uint32_t>(kept[f][l]);
             foff += static_cast<size_t>(kept[f][l]);
-            coff += static_cast<size_t>(wl[l]) + 1;
+            coff += USLAM_MATCH_BANDS * (static_cast<size_t>(wl[l]) + 1) + USLAM_MATCH_BANDS + 1;
             t.xsegs[f * levels + l] = SegDev{f, l};
         }
     }
@@ -272,8 +215,8 @@ extern "C" uslam_status uslam_match_noalloc(int device, int width, int height, i
     e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaMemsetAsync(derr, 0, sizeof(uint32_t), st);  // the error word must start at zero
     if (e == cudaSuccess) {
-        k_noalloc_xsort<<<2 * levels, kXsortThreads, (max_w + 1) * sizeof(uint32_t), st>>>(dtab->frames, dtab->xsegs);
-        e = cudaGetLastError();
+        e = set_compact_smem(max_w);  // a function attribute, not an allocation
+        if (e == cudaSuccess) e = launch_xsort(dtab->frames, dtab->xsegs, 2 * levels, max_w, st);
     }
     if (e == cudaSuccess) e = launch_match(dtab->frames, &dtab->pair, dtab->msegs, 2 * levels, ds.num_sms * 4, st);
     if (e == cudaSuccess) e = launch_mutual(dtab->frames, &dtab->pair, dtab->usegs, levels, derr, st);

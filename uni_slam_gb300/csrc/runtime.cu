@@ -231,7 +231,7 @@ uslam_status create_batch(uslam_ctx* ctx, int n_frames, const int* widths, const
     };
     struct FrameLayout {
         size_t lvl[USLAM_MAX_LEVELS], blur[USLAM_MAX_LEVELS], kpmap[USLAM_MAX_LEVELS], feats[USLAM_MAX_LEVELS],
-            xorder[USLAM_MAX_LEVELS], colstart[USLAM_MAX_LEVELS], bands[USLAM_MAX_LEVELS], counts;
+            xorder[USLAM_MAX_LEVELS], colstart[USLAM_MAX_LEVELS], qorder[USLAM_MAX_LEVELS], bands[USLAM_MAX_LEVELS], counts;
     };
     std::vector<FrameLayout> fl(n_frames);
     for (int f = 0; f < n_frames; ++f) {
@@ -276,8 +276,9 @@ uslam_status create_batch(uslam_ctx* ctx, int n_frames, const int* widths, const
             F.bl_pitch[l] = F.w[l] + ctx->margin + 1;
             Ly.blur[l] = take(&scratch, static_cast<size_t>(F.h[l] + ctx->margin + 1) * F.bl_pitch[l] * 4);
             Ly.kpmap[l] = take(&scratch, static_cast<size_t>(F.h[l]) * F.kp_pitch[l]);
-            Ly.xorder[l] = take(&scratch, capa * 4);
-            Ly.colstart[l] = take(&scratch, (static_cast<size_t>(F.w[l]) + 1) * 4);
+            Ly.xorder[l] = take(&scratch, USLAM_MATCH_BANDS * capa * 4);
+            Ly.colstart[l] = take(&scratch, (USLAM_MATCH_BANDS * (static_cast<size_t>(F.w[l]) + 1) + USLAM_MATCH_BANDS + 1) * 4);
+            Ly.qorder[l] = take(&scratch, capa * 4);
             Ly.bands[l] = take(&scratch, static_cast<size_t>((F.h[l] + 31) / 32) * 8);
         }
         b->max_w = std::max(b->max_w, F.w[0]);
@@ -387,6 +388,7 @@ uslam_status create_batch(uslam_ctx* ctx, int n_frames, const int* widths, const
             F.feats[l] = reinterpret_cast<uint32_t*>(out_base + Ly.feats[l]);
             F.xorder[l] = reinterpret_cast<uint32_t*>(sc_base + Ly.xorder[l]);
             F.colstart[l] = reinterpret_cast<uint32_t*>(sc_base + Ly.colstart[l]);
+            F.qorder[l] = reinterpret_cast<uint32_t*>(sc_base + Ly.qorder[l]);
             F.bands[l] = reinterpret_cast<uint32_t*>(sc_base + Ly.bands[l]);
             F.mask[l] = masks[l];
         }

@@ -335,7 +335,7 @@ uslam_status uslam_server_create(uslam_ctx* ctx, const uslam_server_params* p, u
     // slot bytes per class, then slots per class from an equal share of the budget
     struct SlotLayout {
         size_t bytes, in, counts, lvl[USLAM_MAX_LEVELS], blur[USLAM_MAX_LEVELS], kpmap[USLAM_MAX_LEVELS],
-            feats[USLAM_MAX_LEVELS], xorder[USLAM_MAX_LEVELS], colstart[USLAM_MAX_LEVELS], bands[USLAM_MAX_LEVELS], a2b, b2a, matches, mcount;
+            feats[USLAM_MAX_LEVELS], xorder[USLAM_MAX_LEVELS], colstart[USLAM_MAX_LEVELS], qorder[USLAM_MAX_LEVELS], bands[USLAM_MAX_LEVELS], a2b, b2a, matches, mcount;
     };
     std::vector<SlotLayout> lay(p->n_sizes);
     std::vector<FrameDev> proto(p->n_sizes);
@@ -382,8 +382,9 @@ uslam_status uslam_server_create(uslam_ctx* ctx, const uslam_server_params* p, u
             Y.lvl[l] = l > 0 ? take(n * 4) : 0;
             Y.blur[l] = take(static_cast<size_t>(F.h[l] + ctx->margin + 1) * F.bl_pitch[l] * 4);
             Y.kpmap[l] = take(static_cast<size_t>(F.h[l]) * F.kp_pitch[l]);
-            Y.xorder[l] = take(capa * 4);
-            Y.colstart[l] = take((static_cast<size_t>(F.w[l]) + 1) * 4);
+            Y.xorder[l] = take(USLAM_MATCH_BANDS * capa * 4);
+            Y.colstart[l] = take((USLAM_MATCH_BANDS * (static_cast<size_t>(F.w[l]) + 1) + USLAM_MATCH_BANDS + 1) * 4);
+            Y.qorder[l] = take(capa * 4);
             Y.bands[l] = take(static_cast<size_t>((F.h[l] + 31) / 32) * 8);
         }
         C.shape = ctx->shape_for(W0, H0);
@@ -453,6 +454,7 @@ uslam_status uslam_server_create(uslam_ctx* ctx, const uslam_server_params* p, u
                 F.feats[l] = reinterpret_cast<uint32_t*>(base + Y.feats[l]);
                 F.xorder[l] = reinterpret_cast<uint32_t*>(base + Y.xorder[l]);
                 F.colstart[l] = reinterpret_cast<uint32_t*>(base + Y.colstart[l]);
+                F.qorder[l] = reinterpret_cast<uint32_t*>(base + Y.qorder[l]);
                 F.bands[l] = reinterpret_cast<uint32_t*>(base + Y.bands[l]);
                 F.mask[l] = masks[l];
             }

@@ -15,14 +15,22 @@
 //   kpmap[l] u8   [h_l][kp_pitch_l]        culled FAST strength (0 = no keypoint)
 //   bands[l] u32  [ceil(h_l / 32)][2]      raw and kept keypoint counts per 32-row band
 //   feats[l] Feature[cap]                  gpumodels::Feature records, (y, x) order
-//   xorder[l] u32 [cap]                    feature indices sorted by x (matching)
-//   colstart[l] u32 [w_l + 1]              first xorder slot of each column
+//   xorder[l] u32 [B][cap]                 per band b of the frame height (B =
+//                                          USLAM_MATCH_BANDS): indices of the features
+//                                          whose LOD-0 y lies in the band widened by the
+//                                          window half-height + 2, sorted by x (the
+//                                          matcher's candidate lists)
+//   colstart[l] u32 [B][w_l + 1] + [B + 1] first xorder slot of each column per band,
+//                                          then the band offsets into qorder
+//   qorder[l] u32 [cap]                    feature indices grouped by band (of their own
+//                                          LOD-0 y), sorted by x within a band (queries)
 //   counts   u32  [2][levels]              kept (<= cap) and raw keypoint counts
 #pragma once
 
 #include <stdint.h>
 
 #define USLAM_MAX_LEVELS 12
+#define USLAM_MATCH_BANDS 3  // horizontal bands of the frame for the matcher's lists
 
 // Device copy of one frame's geometry and buffer addresses.
 struct FrameDev {
@@ -42,6 +50,7 @@ struct FrameDev {
     uint32_t* feats[USLAM_MAX_LEVELS];       // 12 u32 (48 B) per feature
     uint32_t* xorder[USLAM_MAX_LEVELS];
     uint32_t* colstart[USLAM_MAX_LEVELS];
+    uint32_t* qorder[USLAM_MAX_LEVELS];
     uint32_t* kept;  // [levels]
     uint32_t* raw;   // [levels]
 };
