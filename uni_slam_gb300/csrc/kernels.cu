@@ -750,63 +750,25 @@ __device__ __forceinline__ int find_segment(const uint32_t* s_pref, int nseg, ui
     return lo;
 }
 
-// G(P) evaluated directly from the level image (the sampler clamps to the
-// edge).  Used for the blur-cache border; texel reads go through the level's
-// own pointer (u8 LOD0 through the LUT, or f32 levels).
-__device__ float gauss_tap9_direct(const uint8_t* img, int pitch, const float* lvl, const float* lut, int w, int h,
-                                   uint32_t px, uint32_t py) {
-    const float tex_x = 1.0f / (float)w;
-    const float tex_y = 1.0f / (float)h;
-    const float uvx = ((float)px + 0.5f) * tex_x;
-    const float uvy = ((float)py + 0.5f) * tex_y;
-    const float off[3] = {-1.2f, 0.0f, 1.2f};
-    const float wt[3] = {0.3125f, 0.375f, 0.3125f};
-    float sum = 0.0f;
-#pragma unroll
-    for (int j = 0; j < 3; ++j) {
-        const float v = (uvy + off[j] * tex_y) * (float)h - 0.5f;
-        const float fj = floorf(v);
-        const float b = v - fj;
-        const int j0 = edge_index(fj, h), j1 = edge_index(fj + 1.0f, h);
-#pragma unroll
-        for (int i = 0; i < 3; ++i) {
-            const float u = (uvx + off[i] * tex_x) * (float)w - 0.5f;
-            const float fi = floorf(u);
-            const float a = u - fi;
-            const int i0 = edge_index(fi, w), i1 = edge_index(fi + 1.0f, w);
-            float t00, t10, t01, t11;
-            if (lvl) {
-                t00 = __ldg(lvl + (size_t)j0 * w + i0);
-                t10 = __ldg(lvl + (size_t)j0 * w + i1);
-                t01 = __ldg(lvl + (size_t)j1 * w + i0);
-                t11 = __ldg(lvl + (size_t)j1 * w + i1);
-            } else {
-                t00 = lut[__ldg(img + (size_t)j0 * pitch + i0)];
-                t10 = lut[__ldg(img + (size_t)j0 * pitch + i1)];
-                t01 = lut[__ldg(img + (size_t)j1 * pitch + i0)];
-                t11 = lut[__ldg(img + (size_t)j1 * pitch + i1)];
-            }
-            const float na = 1.0f - a, nb = 1.0f - b;
-            float s = (na * nb) * t00;
-            s = s + (a * nb) * t10;
-            s = s + (na * b) * t01;
-            s = s + (a * b) * t11;
-            sum = sum + (s * wt[i]) * wt[j];
-        }
-    }
-    return sum;
-}
 
 // Blur-cache border of one level: columns [w, w + M) and the negative-x
 // sentinel column for rows [0, h), then rows [h, h + M) and the negative-y
 // sentinel row for all columns.  A sentinel stands for every negative
 // coordinate: u32(negative) converts to the same f32 2^32 for all offsets a
 // BRIEF test can reach, so G is identical for all of them.
-__device__ __forceinline__ int border_cells(const FrameDev& F, int l) {
-    const int m1 = F.margin + 1;
-    return F.h[l] * m1 + m1 * F.bl_pitch[l];
+// Work units of one level's border: runs of 32 rows of the right margin
+// (columns w .. w + M) and runs of 32 columns of the bottom margin (rows
+// h .. h + M, all columns including the corner and the sentinel column).
+__device__ __forceinline__ uint32_t border_units(const FrameDev& F, int l) {
+    return (uint32_t)((F.h[l] + 31) / 32 + (F.bl_pitch[l] + 31) / 32);
 }
 
+// The blur cache beyond the level edges: G(P) of generate_features.wgsl:149-172
+// for every border cell, with the operation sequence of k_detect's blur
+// (canonical bilinear taps read from the level in global memory, coordinates
+// clamped to the edge) and the x part of the 9 taps computed once per lane (a
+// lane keeps one column and walks the rows of its unit).  Cells of the sentinel row / column use the
+// u32-wrapped coordinate 0xffffffff that every negative coordinate becomes.
 __global__ void __launch_bounds__(256)
 k_blur_border(const FrameDev* __restrict__ frames, const SegDev* __restrict__ segs, int nseg) {
     __shared__ uint32_t s_pref[MAX_SEGS + 1];
@@ -814,27 +776,87 @@ k_blur_border(const FrameDev* __restrict__ frames, const SegDev* __restrict__ se
     __shared__ float s_lut[256];
     s_lut[threadIdx.x] = (float)threadIdx.x / 255.0f;
     const uint32_t total = segment_prefix(nseg, s_pref, s_warp, [&](int sg) {
-        return (uint32_t)border_cells(frames[segs[sg].frame], segs[sg].level);
+        return border_units(frames[segs[sg].frame], segs[sg].level);
     });
-    for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < total; g += gridDim.x * blockDim.x) {
+    const int lane = threadIdx.x & 31;
+    const int gw = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    const int nw = gridDim.x * (blockDim.x >> 5);
+    const float off[3] = {-1.2f, 0.0f, 1.2f};
+    const float wt[3] = {0.3125f, 0.375f, 0.3125f};
+    for (uint32_t g = gw; g < total; g += nw) {
         const int sidx = find_segment(s_pref, nseg, g);
-        const int cell = (int)(g - s_pref[sidx]);
+        const int unit = (int)(g - s_pref[sidx]);
         const FrameDev& F = frames[segs[sidx].frame];
         const int l = segs[sidx].level;
-        const int w = F.w[l], h = F.h[l], M = F.margin, m1 = M + 1, bp = F.bl_pitch[l];
-        int ex, ey;
-        if (cell < h * m1) {
-            ey = cell / m1;
-            ex = w + cell % m1;
+        const int w = F.w[l], h = F.h[l], M = F.margin, bp = F.bl_pitch[l];
+        const int nr = (h + 31) / 32;
+        int ex, ey0, ey1;
+        bool active;
+        if (unit < nr) {
+            ex = w + lane;
+            active = lane <= M;
+            ey0 = unit * 32;
+            ey1 = min(h, ey0 + 32);
         } else {
-            const int c2 = cell - h * m1;
-            ey = h + c2 / bp;
-            ex = c2 % bp;
+            ex = (unit - nr) * 32 + lane;
+            active = ex < bp;
+            ey0 = h;
+            ey1 = h + M + 1;
         }
+        if (!active) continue;
+        const uint8_t* img = F.img;
+        const int pitch = F.img_pitch;
+        const float* lvl = l > 0 ? F.lvl[l] : nullptr;
+        const float tex_x = 1.0f / (float)w;
+        const float tex_y = 1.0f / (float)h;
         const uint32_t px = ex < w + M ? (uint32_t)ex : 0xffffffffu;
-        const uint32_t py = ey < h + M ? (uint32_t)ey : 0xffffffffu;
-        F.blur[l][(size_t)ey * bp + ex] =
-            gauss_tap9_direct(F.img, F.img_pitch, l > 0 ? F.lvl[l] : nullptr, s_lut, w, h, px, py);
+        const float uvx = ((float)px + 0.5f) * tex_x;
+        float ax[3];
+        int ix0[3], ix1[3];
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+            const float u = (uvx + off[i] * tex_x) * (float)w - 0.5f;
+            const float fi = floorf(u);
+            ax[i] = u - fi;
+            ix0[i] = edge_index(fi, w);
+            ix1[i] = edge_index(fi + 1.0f, w);
+        }
+        float* out = F.blur[l];
+        for (int ey = ey0; ey < ey1; ++ey) {
+            const uint32_t py = ey < h + M ? (uint32_t)ey : 0xffffffffu;
+            const float uvy = ((float)py + 0.5f) * tex_y;
+            float sum = 0.0f;
+#pragma unroll
+            for (int j = 0; j < 3; ++j) {
+                const float v = (uvy + off[j] * tex_y) * (float)h - 0.5f;
+                const float fj = floorf(v);
+                const float b = v - fj;
+                const int j0 = edge_index(fj, h), j1 = edge_index(fj + 1.0f, h);
+#pragma unroll
+                for (int i = 0; i < 3; ++i) {
+                    float t00, t10, t01, t11;
+                    if (lvl) {
+                        t00 = __ldg(lvl + (size_t)j0 * w + ix0[i]);
+                        t10 = __ldg(lvl + (size_t)j0 * w + ix1[i]);
+                        t01 = __ldg(lvl + (size_t)j1 * w + ix0[i]);
+                        t11 = __ldg(lvl + (size_t)j1 * w + ix1[i]);
+                    } else {
+                        t00 = s_lut[__ldg(img + (size_t)j0 * pitch + ix0[i])];
+                        t10 = s_lut[__ldg(img + (size_t)j0 * pitch + ix1[i])];
+                        t01 = s_lut[__ldg(img + (size_t)j1 * pitch + ix0[i])];
+                        t11 = s_lut[__ldg(img + (size_t)j1 * pitch + ix1[i])];
+                    }
+                    const float a = ax[i];
+                    const float na = 1.0f - a, nb = 1.0f - b;
+                    float sv = (na * nb) * t00;
+                    sv = sv + (a * nb) * t10;
+                    sv = sv + (na * b) * t01;
+                    sv = sv + (a * b) * t11;
+                    sum = sum + (sv * wt[i]) * wt[j];
+                }
+            }
+            out[(size_t)ey * bp + ex] = sum;
+        }
     }
 }
 
