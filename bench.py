@@ -812,9 +812,21 @@ def run_ours(a):
     if a.serve_seconds > 0:
         # keyframes hold up to 2000 descriptors: 333 per level x 6 levels
         sctx = Context(pat, levels=LEVELS, max_width=1280, max_height=720, cap_per_level=333, device=local)
-        served = serve_simulation(sctx, a.serve_seconds, n_streams=a.serve_streams, seed=a.seed + rank)
-        served["saturation"] = serve_saturation(sctx, min(a.serve_seconds, 5.0), n_streams=a.serve_streams,
-                                                seed=a.seed + rank)
+        # The simulated camera client is Python: a full garbage collection with
+        # torch loaded pauses it for ~0.1 s, which would show up as client-side
+        # latency.  The collector is paused for the two runs (the server itself
+        # is native code and unaffected either way).
+        import gc
+
+        gc.collect()
+        gc.disable()
+        try:
+            served = serve_simulation(sctx, a.serve_seconds, n_streams=a.serve_streams, seed=a.seed + rank)
+            served["saturation"] = serve_saturation(sctx, min(a.serve_seconds, 5.0), n_streams=a.serve_streams,
+                                                    seed=a.seed + rank)
+        finally:
+            gc.enable()
+        served["client_gc"] = "paused during the runs"
         sctx.close()
 
     cfg = cfg_run(pat, local, frames, a.stress_steps, 2) if a.cfg else None
