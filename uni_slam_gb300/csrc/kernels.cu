@@ -47,9 +47,6 @@ __device__ __forceinline__ constexpr int circle_x(int i) {
 // A quarter turn maps point i to point i + 4 ((x, y) -> (-y, x)), so y_i = -x_(i+4).
 __device__ __forceinline__ constexpr int circle_y(int i) { return -circle_x((i + 4) & 15); }
 
-// Orientation disc r = 3 in (dy outer, dx inner) order (generate_features.wgsl:87-97).
-__constant__ int8_t c_disc_x[32];
-__constant__ int8_t c_disc_y[32];
 
 // Tint robustness clamp of textureLoad coordinates: min(u32(c), n - 1).
 __device__ __forceinline__ int tint_clamp(int c, int n) {
@@ -883,64 +880,86 @@ k_describe(const FrameDev* __restrict__ frames, const SegDev* __restrict__ segs,
     const int lane = threadIdx.x & 31;
     const int gw = blockIdx.x * (KD_THREADS / 32) + (threadIdx.x >> 5);
     const int nw = gridDim.x * (KD_THREADS / 32);
-    for (uint32_t g = gw; g < total; g += nw) {
-        const int sidx = find_segment(s_pref, nseg, g);
-        const uint32_t i = g - s_pref[sidx];
-        const FrameDev& F = frames[segs[sidx].frame];
-        const int l = segs[sidx].level;
-        const int w = F.w[l], h = F.h[l];
-        uint32_t* rec = F.feats[l] + (size_t)i * 12u;
-        const int x = (int)__uint_as_float(rec[0]);
-        const int y = (int)__uint_as_float(rec[1]);
+    // A warp takes G consecutive keypoints: lane j < G first computes the
+    // orientation of keypoint j, then the warp runs the 256 tests of each in
+    // turn with its position and angle broadcast from that lane.  G = 32 when
+    // the launch has enough keypoints to give every warp 32 of them, else the
+    // largest power of two that still occupies every warp (small launches).
+    uint32_t G = 32u;
+    while (G > 1u && total < G * (uint32_t)nw) G >>= 1;
+    for (uint32_t g0 = (uint32_t)gw * G; g0 < total; g0 += (uint32_t)nw * G) {
+        // orientation (generate_features.wgsl:80-99): intensity moments over
+        // the r = 3 disc, summed in the reference's order, then atan2
+        int my_seg = 0;
+        uint32_t my_idx = 0;
+        float my_theta = 0.0f, my_s = 0.0f, my_c = 0.0f;
+        if ((uint32_t)lane < G && g0 + lane < total) {
+            my_seg = find_segment(s_pref, nseg, g0 + lane);
+            my_idx = g0 + lane - s_pref[my_seg];
+            const FrameDev& F = frames[segs[my_seg].frame];
+            const int l = segs[my_seg].level;
+            const int w = F.w[l], h = F.h[l];
+            const uint32_t* rec = F.feats[l] + (size_t)my_idx * 12u;
+            const int x = (int)__uint_as_float(rec[0]);
+            const int y = (int)__uint_as_float(rec[1]);
+            const float* lvl = F.lvl[l];
+            float m10 = 0.0f, m01 = 0.0f;
+#pragma unroll
+            for (int k = 0; k < 29; ++k) {
+                const int cx = tint_clamp(x + kdx[k], w);
+                const int cy = tint_clamp(y + kdy[k], h);
+                const float v = l == 0 ? s_lut[__ldg(F.img + (size_t)cy * F.img_pitch + cx)]
+                                       : __ldg(lvl + (size_t)cy * (size_t)w + cx);
+                m10 = m10 + (float)kdx[k] * v;
+                m01 = m01 + (float)kdy[k] * v;
+            }
+            my_theta = uslam_atan2f(m01, m10);
+            uslam_sincosf(my_theta, &my_s, &my_c);
+        }
+        const int nk = (int)min(G, total - g0);
+        for (int kp = 0; kp < nk; ++kp) {
+            const int sidx = __shfl_sync(0xffffffffu, my_seg, kp);
+            const uint32_t i = __shfl_sync(0xffffffffu, my_idx, kp);
+            const float theta = __shfl_sync(0xffffffffu, my_theta, kp);
+            const float s = __shfl_sync(0xffffffffu, my_s, kp);
+            const float c = __shfl_sync(0xffffffffu, my_c, kp);
+            const FrameDev& F = frames[segs[sidx].frame];
+            const int l = segs[sidx].level;
+            const int w = F.w[l], h = F.h[l];
+            uint32_t* rec = F.feats[l] + (size_t)i * 12u;
+            const int x = (int)__uint_as_float(rec[0]);
+            const int y = (int)__uint_as_float(rec[1]);
 
-        // orientation: intensity moments over the r = 3 disc, summed in order
-        float p = 0.0f;
-        if (lane < 29) {
-            const int cx = tint_clamp(x + c_disc_x[lane], w);
-            const int cy = tint_clamp(y + c_disc_y[lane], h);
-            p = l == 0 ? s_lut[__ldg(F.img + (size_t)cy * F.img_pitch + cx)]
-                       : __ldg(F.lvl[l] + (size_t)cy * (size_t)w + cx);
+            // 256 tests, lane j owns tests j, j + 32, ..., j + 224: 16 independent
+            // gathers from the blur cache (negative coordinates -> sentinel).
+            const float* blur = F.blur[l];
+            const int bp = F.bl_pitch[l];
+            const int sx = w + F.margin, sy = h + F.margin;
+            float ga[8], gb[8];
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+                const float4 t = s_pat[lane + 32 * k];
+                const float fax = t.x, fay = t.y, fbx = t.z, fby = t.w;
+                int xa = x + (int)rintf(fax * c - fay * s);
+                int ya = y + (int)rintf(fax * s + fay * c);
+                int xb = x + (int)rintf(fbx * c - fby * s);
+                int yb = y + (int)rintf(fbx * s + fby * c);
+                xa = xa < 0 ? sx : xa;
+                ya = ya < 0 ? sy : ya;
+                xb = xb < 0 ? sx : xb;
+                yb = yb < 0 ? sy : yb;
+                ga[k] = __ldg(blur + (size_t)ya * bp + xa);
+                gb[k] = __ldg(blur + (size_t)yb * bp + xb);
+            }
+            uint32_t words[8];
+#pragma unroll
+            for (int k = 0; k < 8; ++k) words[k] = __ballot_sync(0xffffffffu, ga[k] > gb[k]);
+            uint32_t out = __float_as_uint(theta);
+#pragma unroll
+            for (int k = 0; k < 8; ++k)
+                if (lane == 4 + k) out = words[k];
+            if (lane >= 3 && lane < 12) rec[lane] = out;
         }
-        float m10 = 0.0f, m01 = 0.0f;
-#pragma unroll
-        for (int k = 0; k < 29; ++k) {
-            const float v = __shfl_sync(0xffffffffu, p, k);
-            m10 = m10 + (float)kdx[k] * v;
-            m01 = m01 + (float)kdy[k] * v;
-        }
-        const float theta = uslam_atan2f(m01, m10);
-        float s, c;
-        uslam_sincosf(theta, &s, &c);
-
-        // 256 tests, lane j owns tests j, j + 32, ..., j + 224: 16 independent
-        // gathers from the blur cache (negative coordinates -> sentinel).
-        const float* blur = F.blur[l];
-        const int bp = F.bl_pitch[l];
-        const int sx = w + F.margin, sy = h + F.margin;
-        float ga[8], gb[8];
-#pragma unroll
-        for (int k = 0; k < 8; ++k) {
-            const float4 t = s_pat[lane + 32 * k];
-            const float fax = t.x, fay = t.y, fbx = t.z, fby = t.w;
-            int xa = x + (int)rintf(fax * c - fay * s);
-            int ya = y + (int)rintf(fax * s + fay * c);
-            int xb = x + (int)rintf(fbx * c - fby * s);
-            int yb = y + (int)rintf(fbx * s + fby * c);
-            xa = xa < 0 ? sx : xa;
-            ya = ya < 0 ? sy : ya;
-            xb = xb < 0 ? sx : xb;
-            yb = yb < 0 ? sy : yb;
-            ga[k] = __ldg(blur + (size_t)ya * bp + xa);
-            gb[k] = __ldg(blur + (size_t)yb * bp + xb);
-        }
-        uint32_t words[8];
-#pragma unroll
-        for (int k = 0; k < 8; ++k) words[k] = __ballot_sync(0xffffffffu, ga[k] > gb[k]);
-        uint32_t out = __float_as_uint(theta);
-#pragma unroll
-        for (int k = 0; k < 8; ++k)
-            if (lane == 4 + k) out = words[k];
-        if (lane >= 3 && lane < 12) rec[lane] = out;
     }
 }
 
@@ -1355,20 +1374,7 @@ k_mutual(const FrameDev* __restrict__ frames, const PairDev* __restrict__ pairs,
 // ------------------------------------------------------------ launch ----
 namespace uslam {
 
-cudaError_t init_constants() {
-    int8_t dx[32] = {0}, dy[32] = {0};
-    int n = 0;
-    for (int y = -3; y <= 3; ++y)
-        for (int x = -3; x <= 3; ++x)
-            if (x * x + y * y <= 9) {
-                dx[n] = (int8_t)x;
-                dy[n] = (int8_t)y;
-                ++n;
-            }
-    cudaError_t e = cudaMemcpyToSymbol(c_disc_x, dx, sizeof(dx));
-    if (e != cudaSuccess) return e;
-    return cudaMemcpyToSymbol(c_disc_y, dy, sizeof(dy));
-}
+cudaError_t init_constants() { return cudaSuccess; }
 
 template <bool CFG>
 cudaError_t launch_detect_profile(const FrameDev* frames, const TileItem* tiles, int ntiles, int shape, uint32_t* err,
