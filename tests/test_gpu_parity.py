@@ -220,3 +220,22 @@ def test_frontend_rotation_matches_reference_rule(ctx, brief_pattern):
                 assert np.array_equal(_mm(fe.matches()), em), f"frame {i}"
     finally:
         fe.close()
+
+
+def test_large_batch_bit_exact(ctx, brief_pattern):
+    """22 frames (~170k keypoints): enough keypoints per launch that k_describe
+    gives every warp 32 keypoints (smaller tests use smaller groups)."""
+    frames = synth.plane_sequence(77, n=22)
+    b = _run(ctx, frames, [(i, i + 1) for i in range(len(frames) - 1)])
+    try:
+        total = 0
+        for i, f in enumerate(frames):
+            exp = oracle.frame(f, brief_pattern)
+            _assert_features_equal(b.features(i), exp)
+            total += int(exp[1].sum())
+        assert total > 160_000
+        a, c = oracle.frame(frames[20], brief_pattern), oracle.frame(frames[21], brief_pattern)
+        em = oracle.match(a[0], a[1], c[0], c[1], 752, 480)
+        assert np.array_equal(_mm(b.matches(20)), em)
+    finally:
+        b.close()
