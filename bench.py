@@ -298,15 +298,18 @@ def serve_simulation(ctx, seconds: float, n_streams: int = 32, rate_hz: float = 
     count = [0] * n_streams
     done_q: queue.Queue = queue.Queue()
     lat: list[float] = []
+    parts: list[tuple[float, float, float]] = []  # (time since start, admission delay, server latency) in ms
 
     def completer():
         while True:
             item = done_q.get()
             if item is None:
                 return
-            tk, admit_delay_ms = item
+            tk, admit_delay_ms, t_rel = item
             srv.wait(tk, 0)
-            lat.append(admit_delay_ms + srv.latency_ms(tk))
+            server_ms = srv.latency_ms(tk)
+            lat.append(admit_delay_ms + server_ms)
+            parts.append((t_rel, admit_delay_ms, server_ms))
             srv.release(tk)
 
     th = threading.Thread(target=completer, daemon=True)
@@ -328,7 +331,7 @@ def serve_simulation(ctx, seconds: float, n_streams: int = 32, rate_hz: float = 
                 break
             refused += 1
             time.sleep(50e-6)
-        done_q.put((tk, (time.perf_counter() - t_sched) * 1e3))
+        done_q.put((tk, (time.perf_counter() - t_sched) * 1e3, (t_sched - start) * 1e3))
         count[k] += 1
         heapq.heappush(heap, (t_sched + rs.exponential(1.0 / rate_hz), k))
     done_q.put(None)
@@ -340,7 +343,12 @@ def serve_simulation(ctx, seconds: float, n_streams: int = 32, rate_hz: float = 
     return {
         "streams": n_streams, "rate_hz_per_stream": rate_hz, "seconds": seconds, "frames": int(arr.size),
         "fps": arr.size / elapsed, "p50_ms": float(np.percentile(arr, 50)), "p99_ms": float(np.percentile(arr, 99)),
-        "max_ms": float(arr.max()), "admission_retries": refused, "launches": st["launches"],
+        "max_ms": float(arr.max()),
+        # the five slowest frames: when, and how the latency splits between the
+        # client's admission (the frame waited to be submitted) and the server
+        "slowest": [{"t_ms": round(t, 1), "admission_ms": round(a, 3), "server_ms": round(b, 3)}
+                    for t, a, b in sorted(parts, key=lambda x: -(x[1] + x[2]))[:5]],
+        "admission_retries": refused, "launches": st["launches"],
         "max_batch_seen": st["max_batch_seen"], "slots": st["slots"],
         "sizes": {f"{w}x{h}": sizes.count((w, h)) for (w, h) in SERVE_SIZES},
     }
@@ -634,6 +642,28 @@ def stress_run(pat, local: int, pair_frames, steps: int, warmup: int, seed: int)
         ctx.close()
 
 
+def side_workload_frames(a, rank: int):
+    """Frames of the uneven and stress workloads, generated on a spawn pool
+    of all host cores (numpy only; safe after CUDA is initialised)."""
+    stress_frames, uneven_frames = [], []
+    if a.stress_pairs > 0 or a.uneven:
+        with mp.get_context("spawn").Pool(os.cpu_count() or 1) as pool:
+            jobs = []
+            if a.uneven:
+                mix = [(a.seed + 300 + 1000 * rank + k, w, h) for k, (w, h) in
+                       enumerate((w, h) for (w, h, n) in UNEVEN_MIX for _ in range(n))]
+                jobs.append(pool.map_async(_uneven_pair, mix))
+            if a.stress_pairs > 0:
+                jobs.append(pool.map_async(_stress_pair,
+                                           [a.seed + 100 * (rank + 1) + k for k in range(a.stress_pairs)]))
+            res = [j.get() for j in jobs]
+            if a.uneven:
+                uneven_frames = res.pop(0)
+            if a.stress_pairs > 0:
+                stress_frames = res.pop(0)
+    return stress_frames, uneven_frames
+
+
 def run_ours(a):
     rank, world, local = _dist()
     import numpy as np
@@ -656,22 +686,6 @@ def run_ours(a):
     from uni_slam_gb300 import synth
 
     pat = patmod.load()
-    stress_frames, uneven_frames = [], []
-    if a.stress_pairs > 0 or a.uneven:
-        with mp.get_context("spawn").Pool(os.cpu_count() or 1) as pool:
-            jobs = []
-            if a.uneven:
-                mix = [(a.seed + 300 + 1000 * rank + k, w, h) for k, (w, h) in
-                       enumerate((w, h) for (w, h, n) in UNEVEN_MIX for _ in range(n))]
-                jobs.append(pool.map_async(_uneven_pair, mix))
-            if a.stress_pairs > 0:
-                jobs.append(pool.map_async(_stress_pair,
-                                           [a.seed + 100 * (rank + 1) + k for k in range(a.stress_pairs)]))
-            res = [j.get() for j in jobs]
-            if a.uneven:
-                uneven_frames = res.pop(0)
-            if a.stress_pairs > 0:
-                stress_frames = res.pop(0)
     frames = synth.plane_sequence(a.seed + rank, n=a.frames)
     n = len(frames)
     ctx = Context(pat, levels=LEVELS, max_width=W, max_height=H, device=local)
@@ -828,6 +842,10 @@ def run_ours(a):
             gc.enable()
         served["client_gc"] = "paused during the runs"
         sctx.close()
+
+    # the side workloads' frames are generated after the served runs, so the
+    # serving loop runs in the same host state as in a stand-alone service
+    stress_frames, uneven_frames = side_workload_frames(a, rank)
 
     cfg = cfg_run(pat, local, frames, a.stress_steps, 2) if a.cfg else None
 
