@@ -44,6 +44,9 @@ W, H, LEVELS = 752, 480, 6
 STRESS_W, STRESS_H, STRESS_LEVELS, STRESS_CAP = 3840, 2160, 8, 2500
 POPC_PER_SM_CLK = 16  # 32-bit population count results per SM per clock (documented issue rate)
 POPC_PER_DISTANCE = 4  # carry-save-adder Hamming distance of 256 bits
+# kernels of one graph replay of the uniform batch (one tile shape): k_detect,
+# k_blur_border, k_band_count, k_band_write, k_xsort, k_describe, k_match, k_mutual
+KERNELS_PER_STEP = 8
 METRIC = "frames/s detect+describe+match @752x480 (batched, 64-frame graph)"
 WORKLOAD = "batched-uniform: 64 consecutive 752x480 u8 frames, plane trajectory, consecutive-pair matching"
 
@@ -883,7 +886,7 @@ def run_ours(a):
                     "method": "two batches in flight (double buffering): per step pinned H2D of the frames, "
                               "graph, D2H of every feature record and match block, on the batch's own stream",
                     "unpipelined_value": n * world / e2e_serial_s},
-            "gpu_launches": 6 * a.steps, "roofline": roofline, "cpu_baseline": cpu, "clocks": clk,
+            "gpu_launches": KERNELS_PER_STEP * a.steps, "roofline": roofline, "cpu_baseline": cpu, "clocks": clk,
             "served": served, "uneven": uneven, "stress": stress, "cfg": cfg,
             "features_per_frame": sum(kept) / n, "matches_per_pair": sum(nmatch) / max(1, n - 1),
             "wall_s_timed": wall_s,

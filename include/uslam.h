@@ -151,7 +151,8 @@ uslam_status uslam_batch_upload(uslam_batch* b);
 /* Copy caller frames (any host memory, given pitch) into the pinned staging. */
 uslam_status uslam_batch_set_frame(uslam_batch* b, int frame, const uint8_t* img, int pitch);
 /* Launch detect + describe of every frame and match of every pair (one CUDA
- * graph replay: six kernel launches for the whole batch). Asynchronous. */
+ * graph replay: about nine kernel launches for the whole batch, whatever its
+ * size). Asynchronous. */
 uslam_status uslam_batch_run(uslam_batch* b);
 /* Asynchronous device->host copy of every frame's features and every pair's
  * matches into pinned staging (read them with the getters below). */

@@ -3,10 +3,14 @@
 //   k_detect   (K1) pyramid level tile + FAST response + cull + blur cache
 //                   (or, in the cfg profile, FAST 9-of-16 at 20/255 + 3x3 NMS)
 //   k_blur_border   blur cache beyond the level edges (BRIEF points outside)
-//   k_band_count, k_band_write, k_xsort
-//                   ordered keypoint compaction over 32-row bands, cap, x-sort
-//   k_describe (K2) orientation + 256-bit rotated BRIEF, one warp per keypoint
-//   k_match    (K3) windowed top-2 Hamming search, 32 x-adjacent queries per warp
+//   k_band_count, k_band_write
+//                   ordered keypoint compaction over 32-row bands, cap
+//   k_xsort         the matcher's lists: per horizontal band an x-sorted
+//                   candidate list, and the band-grouped query order
+//   k_describe (K2) orientation (one lane per keypoint) + 256-bit rotated
+//                   BRIEF (a warp per keypoint)
+//   k_match    (K3) windowed top-2 Hamming search, 32 x-adjacent queries of
+//                   one band per warp
 //   k_mutual        mutual cross-check and ordered match output
 //   k_bruteforce    brute-force top-2 matching (no window, no cross-check)
 //

@@ -5,9 +5,12 @@
 // frames and frame pairs with every buffer carved out of one arena:
 //   [inputs: LOD0 u8 of every frame][outputs: counts + features of every
 //   frame, counts + matches of every pair][scratch: pyramid, blur cache,
-//   keypoint maps, x-sort tables, match directions, error word]
+//   keypoint maps, band counts, the matcher's band lists, match directions,
+//   error word]
 // so one H2D copy feeds the whole batch and one D2H copy returns it.  The
-// batch's launch sequence (6 kernels) is captured once into a CUDA graph.
+// batch's launch sequence (k_detect per tile shape; k_blur_border on a forked
+// branch beside k_band_count, k_band_write, k_xsort; k_describe; k_match or
+// k_bruteforce; k_mutual or the emit) is captured once into a CUDA graph.
 // A frontend (uslam_frontend) is a 2-slot batch driven frame by frame with
 // the reference's FeatureSet(0)/(1) rotation.
 #include <cuda_runtime.h>

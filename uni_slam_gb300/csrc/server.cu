@@ -11,7 +11,7 @@
 // A dispatcher thread launches, whenever requests are waiting and fewer than
 // two launches are in flight, one batch of everything queued (up to
 // max_batch frames): H2D of the frames from pinned staging, its work tables,
-// and the six kernels of the batch path over those frames and their
+// and the kernels of the batch path over those frames and their
 // (keyframe, frame) pairs.  Launches alternate between two CUDA streams, so
 // a batch admitted while another is on the GPU runs alongside it; a pair
 // whose keyframe is produced by a launch still in flight on the other stream
