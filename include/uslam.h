@@ -133,6 +133,32 @@ uslam_status uslam_get_tile_shape(const uslam_ctx* ctx, int width, int height, i
 uslam_status uslam_autotune(uslam_ctx* ctx, int width, int height, const uint8_t* img, int pitch, int n_frames,
                             int reps, int* shape_out, float* ms_out);
 
+/* ---- single-frame export set ---------------------------------------------
+ * A device-resident feature set (replaces one FeatureSet of the reference,
+ * wslam/src/models.hpp, produced by the four feature-detect passes), a
+ * one-shot detect + describe into it, a host copy of it, and a match between
+ * two sets (the reference's MatchFeaturesCPU, match_features_cpu.cpp:217-268,
+ * with the context's matcher).  Synchronous.  Sets of one context share its
+ * device; a set belongs to one host thread at a time. */
+typedef struct uslam_featset uslam_featset;
+uslam_status uslam_featset_create(uslam_ctx* ctx, int width, int height, uslam_featset** out);
+void uslam_featset_destroy(uslam_featset* set);
+/* u8 frame (pitch in bytes) of the set's size. */
+uslam_status uslam_detect_describe(uslam_ctx* ctx, const uint8_t* img, int width, int height, int pitch,
+                                   uslam_featset* out);
+/* f32 frame in [0, 1] (pitch in floats), the reference's FrameBW: exact for
+ * values u8 / 255 (data/src/provider_base.cpp:121-124); other values round to
+ * the nearest 1/255. */
+uslam_status uslam_detect_describe_f32(uslam_ctx* ctx, const float* img, int width, int height, int pitch,
+                                       uslam_featset* out);
+/* Host copy: features level by level in the set's order; kept/raw receive
+ * `levels` counts each. */
+uslam_status uslam_featset_features(uslam_featset* set, uslam_feature* out, int max_out, int* kept, int* raw);
+/* Matches of prev (the reference set) against curr, both from frames of the
+ * same size; out may be NULL to ask for the count. */
+uslam_status uslam_match_sets(uslam_ctx* ctx, const uslam_featset* prev, const uslam_featset* curr, uslam_match* out,
+                              int max_out, int* n_out);
+
 /* ---- batched form: a work table over many frames and frame pairs -------- */
 
 /* Plan a batch of n_frames frames (any mix of sizes) and n_pairs matches

@@ -4,5 +4,5 @@ cull, rotated BRIEF, windowed mutual Hamming matching) behind a C ABI.
 The compute path is ``libuslam.so`` (hand-written sm_103a kernels); these
 Python modules are thin ctypes handles used by tests and the benchmark.
 """
-from .frontend import Batch, Context, Frontend, Server, level_dims  # noqa: F401
+from .frontend import Batch, Context, FeatureSet, Frontend, Server, level_dims  # noqa: F401
 from .capi import FEATURE_DTYPE, MATCH_DTYPE, USlamError  # noqa: F401

@@ -94,6 +94,12 @@ SIGNATURES = {
                                       C.POINTER(C.c_double)]),
     "uslam_server_release": (C.c_int, [_vp, C.c_uint64]),
     "uslam_server_stats": (C.c_int, [_vp, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64), _ip, _ip]),
+    "uslam_featset_create": (C.c_int, [_vp, C.c_int, C.c_int, C.POINTER(_vp)]),
+    "uslam_featset_destroy": (None, [_vp]),
+    "uslam_detect_describe": (C.c_int, [_vp, _vp, C.c_int, C.c_int, C.c_int, _vp]),
+    "uslam_detect_describe_f32": (C.c_int, [_vp, _vp, C.c_int, C.c_int, C.c_int, _vp]),
+    "uslam_featset_features": (C.c_int, [_vp, _vp, C.c_int, _ip, _ip]),
+    "uslam_match_sets": (C.c_int, [_vp, _vp, _vp, _vp, C.c_int, _ip]),
     "uslam_match_noalloc": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, _vp, _ip, _vp, _ip, _vp, _vp, C.c_int,
                                       _vp, C.c_char_p, C.c_size_t]),
 }

@@ -646,6 +646,7 @@ void uslam_destroy(uslam_ctx* c) {
     cudaSetDevice(c->device);
     for (auto& kv : c->classes)
         for (auto* p : kv.second.d_mask) cudaFree(p);
+    for (auto& kv : c->match_batches) free_batch(kv.second);
     if (c->d_pattern) cudaFree(c->d_pattern);
     delete c;
 }
@@ -1042,6 +1043,139 @@ uslam_status uslam_frontend_matches(uslam_frontend* fe, uslam_match* out, int ma
     if (e != cudaSuccess) return b->ctx->cuda_fail(e, "matches readback");
     const int pair = fe->cur == 0 ? 0 : 1;
     return copy_matches(b, b->h_out, pair, out, max_out, n_out);
+}
+
+}  // extern "C"
+
+// ============================================================ feature sets
+// The single-frame export set: a device-resident feature set, one-shot detect
+// + describe into it, and a match between two sets.
+
+struct uslam_featset {
+    uslam_ctx* ctx = nullptr;
+    uslam_batch* b = nullptr;  // one frame, no pairs
+    int W = 0, H = 0;
+    bool valid = false;
+};
+
+namespace {
+
+// Copy frame 0 of a one-frame batch (feature blocks, counts and the matcher's
+// lists) into frame `slot` of a batch of the same frame size.
+cudaError_t copy_frame_state(const uslam_batch* src, uslam_batch* dst, int slot, cudaStream_t st) {
+    const FrameDev& A = src->frames[0];
+    const FrameDev& B = dst->frames[slot];
+    const size_t capa = static_cast<size_t>(std::max(A.cap, 1));
+    cudaError_t e = cudaMemcpyAsync(B.kept, A.kept, 2 * sizeof(uint32_t) * A.levels, cudaMemcpyDeviceToDevice, st);
+    for (int l = 0; l < A.levels && e == cudaSuccess; ++l) {
+        const size_t cols = USLAM_MATCH_BANDS * (static_cast<size_t>(A.w[l]) + 1) + USLAM_MATCH_BANDS + 1;
+        e = cudaMemcpyAsync(B.feats[l], A.feats[l], capa * 48, cudaMemcpyDeviceToDevice, st);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(B.xorder[l], A.xorder[l], USLAM_MATCH_BANDS * capa * 4, cudaMemcpyDeviceToDevice, st);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(B.colstart[l], A.colstart[l], cols * 4, cudaMemcpyDeviceToDevice, st);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(B.qorder[l], A.qorder[l], capa * 4, cudaMemcpyDeviceToDevice, st);
+    }
+    return e;
+}
+
+}  // namespace
+
+extern "C" {
+
+uslam_status uslam_featset_create(uslam_ctx* ctx, int width, int height, uslam_featset** out) {
+    if (!ctx || !out) return USLAM_INVALID_ARG;
+    uslam_batch* b = nullptr;
+    uslam_status s = create_batch(ctx, 1, &width, &height, 0, nullptr, nullptr, false, &b);
+    if (s != USLAM_OK) return s;
+    auto* fs = new uslam_featset();
+    fs->ctx = ctx;
+    fs->b = b;
+    fs->W = width;
+    fs->H = height;
+    *out = fs;
+    return USLAM_OK;
+}
+
+void uslam_featset_destroy(uslam_featset* fs) {
+    if (!fs) return;
+    free_batch(fs->b);
+    delete fs;
+}
+
+uslam_status uslam_detect_describe(uslam_ctx* ctx, const uint8_t* img, int width, int height, int pitch,
+                                   uslam_featset* out) {
+    if (!ctx || !img || !out || out->ctx != ctx) return USLAM_INVALID_ARG;
+    if (width != out->W || height != out->H)
+        return set_err(&ctx->err, USLAM_INVALID_ARG, "detect_describe: frame size differs from the feature set's");
+    uslam_status s = uslam_batch_set_frame(out->b, 0, img, pitch);
+    if (s == USLAM_OK) s = uslam_batch_upload(out->b);
+    if (s == USLAM_OK) s = uslam_batch_run(out->b);
+    if (s == USLAM_OK) s = uslam_batch_sync(out->b, 0);
+    out->valid = s == USLAM_OK;
+    return s;
+}
+
+uslam_status uslam_detect_describe_f32(uslam_ctx* ctx, const float* img, int width, int height, int pitch,
+                                       uslam_featset* out) {
+    if (!ctx || !img || !out || out->ctx != ctx || pitch < width || width < 1 || height < 1)
+        return USLAM_INVALID_ARG;
+    if (width != out->W || height != out->H)
+        return set_err(&ctx->err, USLAM_INVALID_ARG, "detect_describe_f32: frame size differs from the feature set's");
+    // f32 pixels in [0, 1] (the reference's FrameBW, u8 / 255) back to u8:
+    // exact for u8 / 255 values, others round to the nearest step
+    uint8_t* host = nullptr;
+    int hp = 0;
+    uslam_status s = uslam_batch_input_host(out->b, 0, &host, &hp);
+    if (s != USLAM_OK) return s;
+    for (int y = 0; y < height; ++y)
+        for (int x = 0; x < width; ++x) {
+            const float v = img[static_cast<size_t>(y) * pitch + x] * 255.0f;
+            host[static_cast<size_t>(y) * hp + x] = static_cast<uint8_t>(std::lrint(std::min(std::max(v, 0.0f), 255.0f)));
+        }
+    s = uslam_batch_upload(out->b);
+    if (s == USLAM_OK) s = uslam_batch_run(out->b);
+    if (s == USLAM_OK) s = uslam_batch_sync(out->b, 0);
+    out->valid = s == USLAM_OK;
+    return s;
+}
+
+uslam_status uslam_featset_features(uslam_featset* fs, uslam_feature* out, int max_out, int* kept, int* raw) {
+    if (!fs) return USLAM_INVALID_ARG;
+    if (!fs->valid) return set_err(&fs->ctx->err, USLAM_NOT_READY, "featset_features: nothing detected yet");
+    uslam_status s = uslam_batch_download(fs->b);
+    if (s == USLAM_OK) s = uslam_batch_sync(fs->b, 0);
+    if (s == USLAM_OK) s = uslam_batch_features(fs->b, 0, out, max_out, kept, raw);
+    return s;
+}
+
+uslam_status uslam_match_sets(uslam_ctx* ctx, const uslam_featset* prev, const uslam_featset* curr, uslam_match* out,
+                              int max_out, int* n_out) {
+    if (!ctx || !prev || !curr || !n_out || prev->ctx != ctx || curr->ctx != ctx) return USLAM_INVALID_ARG;
+    if (!prev->valid || !curr->valid) return set_err(&ctx->err, USLAM_NOT_READY, "match: a feature set is empty");
+    if (prev->W != curr->W || prev->H != curr->H)
+        return set_err(&ctx->err, USLAM_INVALID_ARG, "match: the feature sets come from frames of different sizes");
+    const auto key = std::make_pair(prev->W, prev->H);
+    auto it = ctx->match_batches.find(key);
+    if (it == ctx->match_batches.end()) {
+        const int ws[2] = {prev->W, prev->W}, hs[2] = {prev->H, prev->H};
+        const int pp = 0, pc = 1;
+        uslam_batch* mb = nullptr;
+        uslam_status s = create_batch(ctx, 2, ws, hs, 1, &pp, &pc, true, &mb);
+        if (s != USLAM_OK) return s;
+        it = ctx->match_batches.emplace(key, mb).first;
+    }
+    uslam_batch* mb = it->second;
+    // the sets' last work is complete (detect_describe synchronises); the
+    // copies and the match run on the match batch's stream
+    cudaError_t e = copy_frame_state(prev->b, mb, 0, mb->stream);
+    if (e == cudaSuccess) e = copy_frame_state(curr->b, mb, 1, mb->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(mb->d_err, 0, sizeof(uint32_t), mb->stream);
+    if (e == cudaSuccess) e = enqueue_program(mb, mb->pair_prog[0]);
+    if (e != cudaSuccess) return ctx->cuda_fail(e, "match");
+    uslam_status s = uslam_batch_download(mb);
+    if (s == USLAM_OK) s = uslam_batch_sync(mb, 0);
+    if (s == USLAM_OK) s = uslam_batch_matches(mb, 0, out, max_out, n_out);
+    return s;
 }
 
 }  // extern "C"

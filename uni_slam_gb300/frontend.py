@@ -82,6 +82,14 @@ class Context:
                    "autotune")
         return s.value, [float(v) for v in ms]
 
+    def match(self, prev: "FeatureSet", curr: "FeatureSet") -> np.ndarray:
+        """Matches of prev (reference set) against curr (uslam_match_sets)."""
+        n = C.c_int()
+        self.check(self.lib.uslam_match_sets(self.h, prev.h, curr.h, None, 0, C.byref(n)), "match_sets")
+        out = np.zeros(n.value, MATCH_DTYPE)
+        self.check(self.lib.uslam_match_sets(self.h, prev.h, curr.h, ptr(out), out.size, C.byref(n)), "match_sets")
+        return out
+
     def error(self) -> str:
         return self.lib.uslam_last_error(self.h).decode()
 
@@ -348,3 +356,46 @@ class Server:
         if self.h:
             self.lib.uslam_server_destroy(self.h)
             self.h = None
+
+
+class FeatureSet:
+    """A device-resident feature set of one frame size (uslam_featset):
+    detect(frame) fills it from a u8 frame or an f32 frame in [0, 1]."""
+
+    def __init__(self, ctx: Context, width: int, height: int):
+        self.ctx, self.lib = ctx, ctx.lib
+        self.width, self.height = width, height
+        h = C.c_void_p()
+        ctx.check(self.lib.uslam_featset_create(ctx.h, width, height, C.byref(h)), "featset_create")
+        self.h = h
+
+    def detect(self, frame: np.ndarray):
+        if frame.dtype == np.float32:
+            img = np.ascontiguousarray(frame, np.float32)
+            fn = self.lib.uslam_detect_describe_f32
+        else:
+            img = np.ascontiguousarray(frame, np.uint8)
+            fn = self.lib.uslam_detect_describe
+        h, w = img.shape
+        self.ctx.check(fn(self.ctx.h, ptr(img), w, h, w, self.h), "detect_describe")
+
+    def features(self):
+        levels = self.ctx.levels
+        kept = np.zeros(levels, np.int32)
+        raw = np.zeros(levels, np.int32)
+        self.ctx.check(self.lib.uslam_featset_features(self.h, None, 0, iptr(kept), iptr(raw)), "featset_features")
+        out = np.zeros(int(kept.sum()), FEATURE_DTYPE)
+        self.ctx.check(self.lib.uslam_featset_features(self.h, ptr(out), out.size, iptr(kept), iptr(raw)),
+                       "featset_features")
+        return out, kept, raw
+
+    def close(self):
+        if self.h:
+            self.lib.uslam_featset_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
