@@ -66,6 +66,7 @@ def _args():
     ap.add_argument("--stress-steps", type=int, default=5)
     ap.add_argument("--uneven", type=int, default=1, help="batched-uneven workload (0: skip)")
     ap.add_argument("--cfg", type=int, default=1, help="cfg detection/matching profile on the main workload (0: skip)")
+    ap.add_argument("--ransac", type=int, default=1, help="RANSAC hypothesis scoring on the workload's matches (0: skip)")
     return ap.parse_args()
 
 
@@ -573,6 +574,60 @@ def cfg_run(pat, local: int, frames, steps: int, warmup: int) -> dict:
         ctx.close()
 
 
+def ransac_run(ctx, batch, pairs: int, n_hyp: int = 500, reps: int = 20) -> dict:
+    """Batched RANSAC hypothesis scoring (the stage after matching) on the
+    matches of the workload's first pairs: n_hyp fundamental matrices fitted on
+    the host to random 8-samples, scored on the GPU over all matches of the
+    pair (uslam_ransac_score, host buffers, copies included), beside the
+    oracle's single-threaded scoring of the same matrices."""
+    import numpy as np
+
+    import oracle
+
+    rs = np.random.RandomState(5)
+    scale = [1.2 ** l for l in range(LEVELS)]
+    feats = {}
+
+    def lod0(frame, lod, idx):
+        if frame not in feats:
+            f, kept, _ = batch.features(frame)
+            feats[frame] = (f, np.concatenate([[0], np.cumsum(kept)]))
+        f, off = feats[frame]
+        r = f[off[lod] + idx]
+        return float(r["x"]) * scale[lod], float(r["y"]) * scale[lod]
+
+    gpu_s, cpu_s, n_total, h_total = 0.0, 0.0, 0, 0
+    for k in range(pairs):
+        m = batch.matches(k)
+        p = np.array([lod0(k, la, ia) for la, ia in zip(m["lod_a"], m["idx_a"])])
+        q = np.array([lod0(k + 1, lb, ib) for lb, ib in zip(m["lod_b"], m["idx_b"])])
+        Fs = []
+        for _ in range(n_hyp):
+            smp = rs.choice(len(p), 8, replace=False)
+            A = np.c_[q[smp, 0:1] * p[smp], q[smp, 0:1], q[smp, 1:2] * p[smp], q[smp, 1:2], p[smp], np.ones((8, 1))]
+            Fs.append(np.linalg.svd(A)[2][-1].reshape(3, 3))
+        Fs = np.array(Fs)
+        ctx.ransac_score(Fs, p, q)  # warm-up
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            counts = ctx.ransac_score(Fs, p, q)
+        gpu_s += (time.perf_counter() - t0) / reps
+        t0 = time.perf_counter()
+        ec, _ = oracle.sampson_counts(Fs, p, q, 3.84)
+        cpu_s += time.perf_counter() - t0
+        assert np.array_equal(counts, ec)
+        n_total += len(p)
+        h_total += n_hyp
+    return {
+        "workload": f"{n_hyp} fundamental matrices per pair (8-point fits to random samples) scored against all "
+                    f"matches of the first {pairs} pairs of the main workload; Sampson distance < 3.84 px^2",
+        "pairs": pairs, "matches_per_pair": n_total / pairs, "hypotheses_per_s": h_total / gpu_s,
+        "scores_per_s": n_hyp * n_total / gpu_s, "ms_per_pair": gpu_s / pairs * 1e3,
+        "cpu_oracle_ms_per_pair": cpu_s / pairs * 1e3, "equal_to_oracle": True,
+        "note": "host buffers in, counts out (copies and launch inside the time)",
+    }
+
+
 def _stress_pair(seed: int):
     from uni_slam_gb300 import synth
 
@@ -846,6 +901,8 @@ def run_ours(a):
         served["client_gc"] = "paused during the runs"
         sctx.close()
 
+    ransac = ransac_run(ctx, batch, pairs=min(4, n - 1)) if a.ransac and rank == 0 else None
+
     # the side workloads' frames are generated after the served runs, so the
     # serving loop runs in the same host state as in a stand-alone service
     stress_frames, uneven_frames = side_workload_frames(a, rank)
@@ -887,7 +944,7 @@ def run_ours(a):
                               "graph, D2H of every feature record and match block, on the batch's own stream",
                     "unpipelined_value": n * world / e2e_serial_s},
             "gpu_launches": KERNELS_PER_STEP * a.steps, "roofline": roofline, "cpu_baseline": cpu, "clocks": clk,
-            "served": served, "uneven": uneven, "stress": stress, "cfg": cfg,
+            "served": served, "uneven": uneven, "stress": stress, "cfg": cfg, "ransac": ransac,
             "features_per_frame": sum(kept) / n, "matches_per_pair": sum(nmatch) / max(1, n - 1),
             "wall_s_timed": wall_s,
         }

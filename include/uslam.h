@@ -159,6 +159,22 @@ uslam_status uslam_featset_features(uslam_featset* set, uslam_feature* out, int 
 uslam_status uslam_match_sets(uslam_ctx* ctx, const uslam_featset* prev, const uslam_featset* curr, uslam_match* out,
                               int max_out, int* n_out);
 
+/* ---- RANSAC hypothesis scoring (the stage after matching) ----------------
+ * No counterpart as a GPU pass in the reference: RansacCPU
+ * (wslam/src/pose_estimate_cpu/ransac_cpu.cpp) scores one fundamental matrix
+ * per iteration on the host (SampsonDistance :173-188, ClassifyInliers
+ * :190-203).  This scores n_hyp matrices (row-major 3x3 doubles, the
+ * reference's convention: prev = point of the first image, curr = second)
+ * against n_matches correspondences in LOD-0 pixels (x, y doubles):
+ * counts[h] = number of matches with Sampson distance < threshold (px^2;
+ * the reference's default 3.84).  masks (NULL or n_hyp * ceil(n / 32) words)
+ * receives the inlier bitmask of every hypothesis (bit i of word i / 32).
+ * Double precision, no contraction, a fixed evaluation order written in
+ * ransac.cu.  Host buffers; synchronous. */
+uslam_status uslam_ransac_score(uslam_ctx* ctx, const double* fmats, int n_hyp, const double* prev_xy,
+                                const double* curr_xy, int n_matches, double threshold, int* counts,
+                                uint32_t* masks);
+
 /* ---- batched form: a work table over many frames and frame pairs -------- */
 
 /* Plan a batch of n_frames frames (any mix of sizes) and n_pairs matches

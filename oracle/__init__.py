@@ -50,6 +50,8 @@ def lib():
         L.orc_match.restype = C.c_int
         L.orc_match_bruteforce.argtypes = [vp, C.c_int, vp, C.c_int, C.c_float, vp]
         L.orc_match_bruteforce.restype = C.c_int
+        L.orc_sampson_counts.argtypes = [vp, C.c_int, vp, vp, C.c_int, C.c_double, vp, vp]
+        L.orc_sampson_counts.restype = None
         L.orc_atan2f.argtypes = [C.c_float, C.c_float]
         L.orc_atan2f.restype = C.c_float
         L.orc_sincosf.argtypes = [C.c_float, vp, vp]
@@ -178,6 +180,18 @@ def match_bruteforce(feats_a, kept_a, feats_b, kept_b, ratio: float = 0.8) -> np
     tb = a2b[qa]
     lb = np.searchsorted(b_off, tb, side="right") - 1
     return np.stack([la, qa - a_off[la], lb, tb - b_off[lb]], 1).astype(np.int32).reshape(-1, 4)
+
+
+def sampson_counts(fmats: np.ndarray, prev_xy: np.ndarray, curr_xy: np.ndarray, thr: float = 3.84):
+    """(counts[H], masks[H, ceil(N/32)]) of the Sampson inlier test."""
+    F = np.ascontiguousarray(fmats, np.float64).reshape(-1, 9)
+    p = np.ascontiguousarray(prev_xy, np.float64).reshape(-1, 2)
+    q = np.ascontiguousarray(curr_xy, np.float64).reshape(-1, 2)
+    n = len(p)
+    counts = np.zeros(len(F), np.int32)
+    masks = np.zeros((len(F), max(1, (n + 31) // 32)), np.uint32)
+    lib().orc_sampson_counts(_p(F), len(F), _p(p), _p(q), n, thr, _p(counts), _p(masks))
+    return counts, masks[:, :(n + 31) // 32]
 
 
 def atan2f(y: float, x: float) -> float:

@@ -561,6 +561,38 @@ int orc_match_bruteforce(const orc_feature* a, int na, const orc_feature* b, int
     return n;
 }
 
+/* ----------------------------------------------------- RANSAC scoring -- */
+/* Sampson distance of wslam/src/pose_estimate_cpu/ransac_cpu.cpp:173-188 in
+ * double, in the evaluation order written in the CUDA file (left to right,
+ * no contraction); inlier iff d < threshold (ClassifyInliers, :190-203). */
+static int sampson_inlier(const double* F, double xp, double yp, double xc, double yc, double thr) {
+    const double fx0 = (F[0] * xp + F[1] * yp) + F[2];
+    const double fx1 = (F[3] * xp + F[4] * yp) + F[5];
+    const double fx2 = (F[6] * xp + F[7] * yp) + F[8];
+    const double ft0 = (F[0] * xc + F[3] * yc) + F[6];
+    const double ft1 = (F[1] * xc + F[4] * yc) + F[7];
+    const double num = (xc * fx0 + yc * fx1) + fx2;
+    const double den = ((fx0 * fx0 + fx1 * fx1) + ft0 * ft0) + ft1 * ft1;
+    if (den < 1e-12) return 0;
+    return (num * num) / den < thr;
+}
+
+void orc_sampson_counts(const double* fmats, int n_hyp, const double* prev_xy, const double* curr_xy, int n,
+                        double thr, int* counts, uint32_t* masks) {
+    const int words = (n + 31) / 32;
+    for (int h = 0; h < n_hyp; ++h) {
+        int c = 0;
+        for (int w = 0; masks && w < words; ++w) masks[(size_t)h * words + w] = 0u;
+        for (int i = 0; i < n; ++i) {
+            const int in = sampson_inlier(fmats + (size_t)h * 9, prev_xy[2 * i], prev_xy[2 * i + 1], curr_xy[2 * i],
+                                          curr_xy[2 * i + 1], thr);
+            c += in;
+            if (in && masks) masks[(size_t)h * words + i / 32] |= 1u << (i % 32);
+        }
+        counts[h] = c;
+    }
+}
+
 /* ------------------------------------------------------------ exports -- */
 
 float orc_atan2f(float y, float x) { return uslam_atan2f(y, x); }

@@ -104,6 +104,13 @@ int orc_match(const orc_feature* a, const int* a_off, const orc_feature* b, cons
  * b of query i's match, or -1.  Returns the number of matches. */
 int orc_match_bruteforce(const orc_feature* a, int na, const orc_feature* b, int nb, float ratio, int32_t* a2b);
 
+/* RANSAC scoring (no GPU counterpart in the reference): counts[h] = number of
+ * correspondences whose Sampson distance to fundamental matrix h (row-major
+ * 3x3 double) is below thr (ransac_cpu.cpp:173-203), in the evaluation order
+ * documented with the CUDA kernel; masks (or NULL) receive the inlier bits. */
+void orc_sampson_counts(const double* fmats, int n_hyp, const double* prev_xy, const double* curr_xy, int n,
+                        double thr, int* counts, uint32_t* masks);
+
 /* The shared canonical transcendentals (include/uslam_canon.h), exported so
  * the tests can measure their accuracy against a double-precision libm. */
 float orc_atan2f(float y, float x);

@@ -100,6 +100,7 @@ SIGNATURES = {
     "uslam_detect_describe_f32": (C.c_int, [_vp, _vp, C.c_int, C.c_int, C.c_int, _vp]),
     "uslam_featset_features": (C.c_int, [_vp, _vp, C.c_int, _ip, _ip]),
     "uslam_match_sets": (C.c_int, [_vp, _vp, _vp, _vp, C.c_int, _ip]),
+    "uslam_ransac_score": (C.c_int, [_vp, _vp, C.c_int, _vp, _vp, C.c_int, C.c_double, _ip, _vp]),
     "uslam_match_noalloc": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, _vp, _ip, _vp, _ip, _vp, _vp, C.c_int,
                                       _vp, C.c_char_p, C.c_size_t]),
 }

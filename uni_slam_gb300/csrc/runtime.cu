@@ -647,6 +647,7 @@ void uslam_destroy(uslam_ctx* c) {
     for (auto& kv : c->classes)
         for (auto* p : kv.second.d_mask) cudaFree(p);
     for (auto& kv : c->match_batches) free_batch(kv.second);
+    if (c->ransac_buf) cudaFree(c->ransac_buf);
     if (c->d_pattern) cudaFree(c->d_pattern);
     delete c;
 }

@@ -9,6 +9,7 @@
 #include <cmath>
 #include <cstring>
 #include <map>
+#include <mutex>
 #include <string>
 #include <utility>
 #include <vector>
@@ -174,6 +175,9 @@ struct uslam_ctx {
     int detector = 0;     // 0 reference FAST + cull, 1 cfg profile (FAST 9-of-16 at 20/255 + 3x3 NMS)
     std::map<std::pair<int, int>, int> tile_shape;  // per resolution class (autotuned or set)
     std::map<std::pair<int, int>, uslam_batch*> match_batches;  // uslam_match: a 2-frame batch per frame size
+    void* ransac_buf = nullptr;  // uslam_ransac_score scratch, grown on demand
+    size_t ransac_bytes = 0;
+    std::mutex ransac_mu;
     int shape_for(int W0, int H0) const {
         auto it = tile_shape.find(std::make_pair(W0, H0));
         return it == tile_shape.end() ? 0 : it->second;

@@ -90,6 +90,20 @@ class Context:
         self.check(self.lib.uslam_match_sets(self.h, prev.h, curr.h, ptr(out), out.size, C.byref(n)), "match_sets")
         return out
 
+    def ransac_score(self, fmats: np.ndarray, prev_xy: np.ndarray, curr_xy: np.ndarray, threshold: float = 3.84,
+                     masks: bool = False):
+        """Inlier counts of H fundamental matrices over N correspondences
+        (uslam_ransac_score); with masks=True also the inlier bitmasks."""
+        F = np.ascontiguousarray(fmats, np.float64).reshape(-1, 9)
+        p = np.ascontiguousarray(prev_xy, np.float64).reshape(-1, 2)
+        q = np.ascontiguousarray(curr_xy, np.float64).reshape(-1, 2)
+        n = len(p)
+        counts = np.zeros(len(F), np.int32)
+        m = np.zeros((len(F), max(1, (n + 31) // 32)), np.uint32) if masks else None
+        self.check(self.lib.uslam_ransac_score(self.h, ptr(F), len(F), ptr(p), ptr(q), n, threshold, iptr(counts),
+                                               ptr(m) if masks else None), "ransac_score")
+        return (counts, m[:, :(n + 31) // 32]) if masks else counts
+
     def error(self) -> str:
         return self.lib.uslam_last_error(self.h).decode()
 
