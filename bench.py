@@ -159,6 +159,19 @@ def reduce_max(value: float, dist, device: str) -> float:
 
 # ------------------------------------------------------------------ bytes
 
+def measured_pipes() -> dict:
+    """Issue and pipe utilisation (% of peak while active) per kernel, from the
+    committed summary of the same ncu capture as measured_traffic()."""
+    path = os.path.join(REPO, "profiles", "kernels_752x480_16frames.txt")
+    out = {}
+    if os.path.exists(path):
+        for line in open(path):
+            parts = line.split()
+            if len(parts) >= 4 and parts[0] == "pipe":
+                out[parts[1]] = {parts[i]: float(parts[i + 1]) for i in range(2, len(parts) - 1, 2)}
+    return out
+
+
 def measured_traffic() -> dict:
     """DRAM bytes per unit (frame or frame pair) of each kernel, from the
     committed summary of one ncu capture."""
@@ -812,6 +825,9 @@ def run_ours(a):
         "traffic_source": "profiles/kernels_752x480_16frames.txt (16-frame ncu capture, scaled by frames / pairs)",
         "peak_source": "measured" if peaks else "fallback",
         "kernel_ms": prof, "algorithmic_bytes_per_launch": dom_bytes,
+        # the path is SM-bound, not HBM-bound: the binding SM resource of the
+        # dominant kernel from the ncu capture (issue slots or a pipe, % of peak)
+        "sm_bound": dict(measured_pipes().get(dom, {}), source="profiles/kernels_752x480_16frames.txt (ncu)"),
         "path_achieved": nbytes["total_per_step"] / (step_ms / 1e3) / 1e9,
         "path_frac": nbytes["total_per_step"] / (step_ms / 1e3) / 1e9 / peak,
     }
