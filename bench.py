@@ -67,6 +67,7 @@ def _args():
     ap.add_argument("--uneven", type=int, default=1, help="batched-uneven workload (0: skip)")
     ap.add_argument("--cfg", type=int, default=1, help="cfg detection/matching profile on the main workload (0: skip)")
     ap.add_argument("--ransac", type=int, default=1, help="RANSAC hypothesis scoring on the workload's matches (0: skip)")
+    ap.add_argument("--triangulate", type=int, default=1, help="batched two-view triangulation section (0: skip)")
     return ap.parse_args()
 
 
@@ -641,6 +642,71 @@ def ransac_run(ctx, batch, pairs: int, n_hyp: int = 500, reps: int = 20) -> dict
     }
 
 
+def triangulate_run(ctx, pairs: int = 8, rows: int = 1500, reps: int = 10) -> dict:
+    """Batched two-view triangulation (the pass after RANSAC, uslam_triangulate):
+    `pairs` seeded scenes of `rows` RANSAC inliers each (1% residual outliers)
+    in one call with host buffers (copies and the five launches inside the
+    time), beside the reference's own TriangulateCPU compiled from its source
+    (oracle/_ref, when built on this machine) or else the oracle restatement,
+    both on one core, on the first two pairs."""
+    import os
+
+    import numpy as np
+
+    from oracle import triangulate as T
+    from uni_slam_gb300 import synth
+
+    cam = synth.SCENE_CAMERA
+    scenes = [synth.two_view_scene(seed=700 + k, n=rows, outlier_frac=0.01)[0] for k in range(pairs)]
+    parts = [r[:, 1:5].astype(np.float64) for r in scenes]
+    res = ctx.triangulate(parts, cam)  # warm-up (also grows the scratch)
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        res = ctx.triangulate(parts, cam)
+    gpu_s = (time.perf_counter() - t0) / reps
+
+    # parity of the timed results against the oracle (tolerances of the tests)
+    for px, r in zip(parts, res):
+        w = T.triangulate(px, cam)
+        assert r["landmark_count"] == w["landmark_count"] and r["cheirality_passes"] == w["cheirality_passes"]
+        assert np.array_equal(r["keep"], w["keep"])
+        k = w["keep"]
+        assert np.all(np.abs(r["landmarks"][k, :3] - w["landmarks"][k, :3])
+                      <= 1e-8 * np.maximum(1.0, np.abs(w["landmarks"][k, 2:3])))
+
+    sample = min(2, pairs)
+    ref_lib = os.path.join(REPO, "oracle", "_ref", "libref_triangulate.so")
+    if os.path.exists(ref_lib):
+        import ctypes as C
+
+        lib = C.CDLL(ref_lib)
+        opts = np.array([4.0, 1e-3, 1e3, 8, 20, 1e-9])
+        p = lambda a: a.ctypes.data_as(C.c_void_p)  # noqa: E731
+        t0 = time.perf_counter()
+        for r in scenes[:sample]:
+            n = len(r)
+            pose, st, keep, lm = np.zeros(12), np.zeros(6), np.zeros(n, np.int32), np.zeros((n, 4))
+            lib.ref_triangulate(p(r), C.c_int(n), p(cam), p(opts), p(pose), p(st), p(keep), p(lm))
+        cpu_s = (time.perf_counter() - t0) / sample
+        kind = "reference (wslam/src/pose_estimate_cpu/triangulate_cpu.cpp with Eigen 3.4, one core)"
+    else:
+        t0 = time.perf_counter()
+        for px in parts[:sample]:
+            T.triangulate(px, cam)
+        cpu_s = (time.perf_counter() - t0) / sample
+        kind = "port (oracle/triangulate.py: numpy, LAPACK SVDs)"
+    landmarks = sum(r["landmark_count"] for r in res)
+    return {
+        "workload": f"{pairs} frame pairs x {rows} RANSAC inliers (seeded two-view scenes, 752x480 camera with "
+                    f"radial-tangential distortion, 1% residual outliers)",
+        "pairs": pairs, "rows_per_pair": rows, "ms_per_call": gpu_s * 1e3, "pairs_per_s": pairs / gpu_s,
+        "rows_per_s": pairs * rows / gpu_s, "landmarks_per_call": landmarks,
+        "cpu_ms_per_pair": cpu_s * 1e3, "cpu_kind": kind, "cpu_sample_pairs": sample,
+        "gpu_over_cpu_per_pair": (cpu_s * pairs) / gpu_s, "equal_to_oracle_within_tolerance": True,
+        "note": "host buffers in, results out (copies and launches inside the time); synchronous call",
+    }
+
+
 def _stress_pair(seed: int):
     from uni_slam_gb300 import synth
 
@@ -918,6 +984,7 @@ def run_ours(a):
         sctx.close()
 
     ransac = ransac_run(ctx, batch, pairs=min(4, n - 1)) if a.ransac and rank == 0 else None
+    tri = triangulate_run(ctx) if a.triangulate and rank == 0 else None
 
     # the side workloads' frames are generated after the served runs, so the
     # serving loop runs in the same host state as in a stand-alone service
@@ -961,6 +1028,7 @@ def run_ours(a):
                     "unpipelined_value": n * world / e2e_serial_s},
             "gpu_launches": KERNELS_PER_STEP * a.steps, "roofline": roofline, "cpu_baseline": cpu, "clocks": clk,
             "served": served, "uneven": uneven, "stress": stress, "cfg": cfg, "ransac": ransac,
+            "triangulate": tri,
             "features_per_frame": sum(kept) / n, "matches_per_pair": sum(nmatch) / max(1, n - 1),
             "wall_s_timed": wall_s,
         }

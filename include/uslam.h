@@ -175,6 +175,59 @@ uslam_status uslam_ransac_score(uslam_ctx* ctx, const double* fmats, int n_hyp, 
                                 const double* curr_xy, int n_matches, double threshold, int* counts,
                                 uint32_t* masks);
 
+/* ---- two-view triangulation (the pass after RANSAC) ---------------------
+ * TriangulateCPU::execute (wslam/src/pose_estimate_cpu/triangulate_cpu.cpp:342-513)
+ * for n_pairs independent frame pairs in one call.  Pair p's rows are
+ * offsets[p] .. offsets[p + 1] - 1 of px: (prev_x, prev_y, curr_x, curr_y),
+ * the LOD-0 pixels of its RANSAC inliers (util::ToLod0Pixel of the two
+ * features).  The reference visits the rows per level in the order of its
+ * flat_map keys, so rows in that order give the same results.  Per pair:
+ * the rays are undistorted (bit-exact), the essential matrix is re-fitted on
+ * all rays, the four (R, t) of its decomposition are scored by cheirality,
+ * and the best pose's points pass the depth range and the reprojection
+ * filter.  results[p] receives the TriangulationResult fields
+ * (wslam/src/models.hpp:163-184); landmarks (NULL or 4 doubles per row:
+ * x, y, z in the current camera, mean reprojection error) and keep (NULL or
+ * one byte per row) mark the rows that became landmarks; other rows are 0.
+ * opts NULL means the reference's defaults (uslam_tri_default_opts).  Pose
+ * and points agree with the reference to rounding (its SVDs are computed
+ * by other algorithms), see triangulate.cu.  Host buffers; synchronous. */
+typedef struct uslam_camera {
+    double fu, fv, cu, cv; /* intrinsics, LOD-0 pixels (CamSensorParams::intrinsics) */
+    double k1, k2, p1, p2; /* radial-tangential distortion (distortion_coefficients) */
+} uslam_camera;
+
+typedef struct uslam_tri_opts {
+    double max_reprojection_px; /* 4.0 */
+    double min_depth;           /* 1e-3 */
+    double max_depth;           /* 1e3 */
+    double undistort_tolerance; /* 1e-9 */
+    int min_inliers;            /* 8 (values below 8 are refused) */
+    int undistort_iterations;   /* 20 */
+} uslam_tri_opts;
+
+typedef struct uslam_tri_result {
+    double rotation[9];    /* row-major, p_curr = R p_prev + t; identity when no pose */
+    double translation[3]; /* unit norm */
+    double mean_reprojection_error_px;
+    double rotation_angle_rad;
+    int input_matches;
+    int landmark_count;
+    int cheirality_passes;
+    int pose_recovered;
+} uslam_tri_result;
+
+void uslam_tri_default_opts(uslam_tri_opts* opts);
+/* util::PixelToNormalised (wslam/src/map/map_helpers_lods.hpp:110-120), the
+ * undistortion CollectInliers applies to every inlier pixel
+ * (triangulate_cpu.cpp:220-246): n pixels (x, y doubles) -> n calibrated
+ * rays, equal to the reference's bit for bit.  Host buffers; synchronous. */
+uslam_status uslam_pixel_to_normalised(uslam_ctx* ctx, const uslam_camera* cam, int iterations, double tolerance,
+                                       const double* px, int n, double* out);
+uslam_status uslam_triangulate(uslam_ctx* ctx, const uslam_camera* cam, const uslam_tri_opts* opts, int n_pairs,
+                               const int* offsets, const double* px, uslam_tri_result* results, double* landmarks,
+                               uint8_t* keep);
+
 /* ---- batched form: a work table over many frames and frame pairs -------- */
 
 /* Plan a batch of n_frames frames (any mix of sizes) and n_pairs matches

@@ -1,6 +1,7 @@
 // Minimal restatement of wslam/include/wslam/common.hpp for compiling the
-// reference matcher: the constants it reads (GPUConst), the AnyBag keys it
-// uses, and an AnyBag with the two members it calls.  Test infrastructure.
+// reference matcher and triangulation pass: the constants they read
+// (GPUConst), the AnyBag keys they use (common.hpp:124-153), and an AnyBag
+// with the two members they call.  Test infrastructure.
 #pragma once
 #include <any>
 #include <cstdint>
@@ -49,5 +50,11 @@ inline std::string GetFeatureSetName(size_t keyframes_ago) {
     return std::format("gen:feat:-{}", keyframes_ago);
 }
 inline const std::string MatchedFeaturesName = "gen:feat:match";
+inline const std::string RansacResultName = "gen:feat:ransac";
+inline const std::string TriangulationResultName = "gen:tri";
+inline std::string GetImuVecName() { return "res:imu:vec"; }
+inline std::string GetCameraIntrinsicsName(uint32_t cam_idx) {
+    return std::format("res:cam:intrinsics:{}", cam_idx);
+}
 }  // namespace ResourceIdentifier
 }  // namespace wslam

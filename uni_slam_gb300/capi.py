@@ -42,6 +42,26 @@ class Params(C.Structure):
     ]
 
 
+class Camera(C.Structure):
+    _fields_ = [(n, C.c_double) for n in ("fu", "fv", "cu", "cv", "k1", "k2", "p1", "p2")]
+
+
+class TriOpts(C.Structure):
+    _fields_ = [
+        ("max_reprojection_px", C.c_double), ("min_depth", C.c_double), ("max_depth", C.c_double),
+        ("undistort_tolerance", C.c_double), ("min_inliers", C.c_int), ("undistort_iterations", C.c_int),
+    ]
+
+
+# uslam_tri_result (128 bytes)
+TRI_RESULT_DTYPE = np.dtype([
+    ("rotation", "<f8", (9,)), ("translation", "<f8", (3,)), ("mean_reprojection_error_px", "<f8"),
+    ("rotation_angle_rad", "<f8"), ("input_matches", "<i4"), ("landmark_count", "<i4"),
+    ("cheirality_passes", "<i4"), ("pose_recovered", "<i4"),
+])
+assert TRI_RESULT_DTYPE.itemsize == 128
+
+
 _vp = C.c_void_p
 _ip = C.POINTER(C.c_int)
 _u8pp = C.POINTER(C.POINTER(C.c_uint8))
@@ -101,6 +121,9 @@ SIGNATURES = {
     "uslam_featset_features": (C.c_int, [_vp, _vp, C.c_int, _ip, _ip]),
     "uslam_match_sets": (C.c_int, [_vp, _vp, _vp, _vp, C.c_int, _ip]),
     "uslam_ransac_score": (C.c_int, [_vp, _vp, C.c_int, _vp, _vp, C.c_int, C.c_double, _ip, _vp]),
+    "uslam_tri_default_opts": (None, [C.POINTER(TriOpts)]),
+    "uslam_pixel_to_normalised": (C.c_int, [_vp, C.POINTER(Camera), C.c_int, C.c_double, _vp, C.c_int, _vp]),
+    "uslam_triangulate": (C.c_int, [_vp, C.POINTER(Camera), C.POINTER(TriOpts), C.c_int, _ip, _vp, _vp, _vp, _vp]),
     "uslam_match_noalloc": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, _vp, _ip, _vp, _ip, _vp, _vp, C.c_int,
                                       _vp, C.c_char_p, C.c_size_t]),
 }

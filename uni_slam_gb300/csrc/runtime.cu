@@ -648,6 +648,7 @@ void uslam_destroy(uslam_ctx* c) {
         for (auto* p : kv.second.d_mask) cudaFree(p);
     for (auto& kv : c->match_batches) free_batch(kv.second);
     if (c->ransac_buf) cudaFree(c->ransac_buf);
+    if (c->tri_buf) cudaFree(c->tri_buf);
     if (c->d_pattern) cudaFree(c->d_pattern);
     delete c;
 }

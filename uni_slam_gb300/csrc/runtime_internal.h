@@ -178,6 +178,9 @@ struct uslam_ctx {
     void* ransac_buf = nullptr;  // uslam_ransac_score scratch, grown on demand
     size_t ransac_bytes = 0;
     std::mutex ransac_mu;
+    void* tri_buf = nullptr;  // uslam_triangulate scratch, grown on demand
+    size_t tri_bytes = 0;
+    std::mutex tri_mu;
     int shape_for(int W0, int H0) const {
         auto it = tile_shape.find(std::make_pair(W0, H0));
         return it == tile_shape.end() ? 0 : it->second;

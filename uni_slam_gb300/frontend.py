@@ -104,6 +104,54 @@ class Context:
                                                ptr(m) if masks else None), "ransac_score")
         return (counts, m[:, :(n + 31) // 32]) if masks else counts
 
+    def pixel_to_normalised(self, px, cam, iterations: int = 20, tolerance: float = 1e-9) -> np.ndarray:
+        """Calibrated rays of LOD-0 pixels (uslam_pixel_to_normalised)."""
+        p = np.ascontiguousarray(px, np.float64).reshape(-1, 2)
+        out = np.zeros_like(p)
+        c = capi.Camera(*[float(v) for v in np.asarray(cam, np.float64).reshape(8)])
+        self.check(self.lib.uslam_pixel_to_normalised(self.h, C.byref(c), iterations, tolerance, ptr(p), len(p),
+                                                      ptr(out)), "pixel_to_normalised")
+        return out
+
+    def triangulate(self, px, cam, opts: dict | None = None):
+        """Two-view triangulation of one or many frame pairs (uslam_triangulate).
+
+        px: one (n, 4) array of LOD-0 pixels (prev_x, prev_y, curr_x, curr_y)
+        or a list of them, one per pair; cam: fu, fv, cu, cv, k1, k2, p1, p2;
+        opts: TriangulateCPU::Opts fields to override.  Returns, per pair, a dict
+        of the TriangulationResult fields plus ``keep`` (bool per row) and
+        ``landmarks`` ((n, 4): x, y, z in the current camera, reprojection
+        error; zero where not kept)."""
+        single = isinstance(px, np.ndarray) and px.ndim == 2
+        parts = [np.asarray(px, np.float64).reshape(-1, 4)] if single else \
+            [np.asarray(a, np.float64).reshape(-1, 4) for a in px]
+        offsets = np.zeros(len(parts) + 1, np.int32)
+        offsets[1:] = np.cumsum([len(a) for a in parts])
+        rows = np.ascontiguousarray(np.concatenate(parts) if parts else np.zeros((0, 4)), np.float64)
+        c = capi.Camera(*[float(v) for v in np.asarray(cam, np.float64).reshape(8)])
+        o = capi.TriOpts()
+        self.lib.uslam_tri_default_opts(C.byref(o))
+        for k, v in (opts or {}).items():
+            setattr(o, k, v)
+        res = np.zeros(len(parts), capi.TRI_RESULT_DTYPE)
+        lm = np.zeros((len(rows), 4))
+        keep = np.zeros(len(rows), np.uint8)
+        self.check(self.lib.uslam_triangulate(self.h, C.byref(c), C.byref(o), len(parts), iptr(offsets),
+                                              ptr(rows), ptr(res), ptr(lm), ptr(keep)), "triangulate")
+        out = []
+        for k in range(len(parts)):
+            a, b = offsets[k], offsets[k + 1]
+            r = res[k]
+            out.append({
+                "rotation": r["rotation"].reshape(3, 3).copy(), "translation": r["translation"].copy(),
+                "input_matches": int(r["input_matches"]), "landmark_count": int(r["landmark_count"]),
+                "cheirality_passes": int(r["cheirality_passes"]), "pose_recovered": bool(r["pose_recovered"]),
+                "mean_reprojection_error_px": float(r["mean_reprojection_error_px"]),
+                "rotation_angle_rad": float(r["rotation_angle_rad"]),
+                "keep": keep[a:b].astype(bool), "landmarks": lm[a:b].copy(),
+            })
+        return out[0] if single else out
+
     def error(self) -> str:
         return self.lib.uslam_last_error(self.h).decode()
 

@@ -212,3 +212,66 @@ def plane_sequence(seed: int, n: int = 64, w: int = BASE_W, h: int = BASE_H,
 
 def frame_digest(img: np.ndarray) -> str:
     return hashlib.sha256(np.ascontiguousarray(img).tobytes()).hexdigest()
+
+
+# Camera of the two-view scenes: a 752x480 pinhole with radial-tangential
+# distortion of the size typical for wide-angle grey-scale SLAM cameras
+# (fu, fv, cu, cv, k1, k2, p1, p2).
+SCENE_CAMERA = np.array([460.0, 458.0, 376.0, 240.0, -0.28, 0.07, 2e-4, 2e-5])
+
+
+def two_view_scene(seed: int, n: int, w: int = BASE_W, h: int = BASE_H, noise_px: float = 0.3,
+                   outlier_frac: float = 0.0, depth=(4.0, 30.0), rot_sigma: float = 0.02,
+                   baseline: float = 1.0, cam: np.ndarray | None = None):
+    """Seeded RANSAC-inlier correspondences of a rigid two-view scene.
+
+    Random points in front of the first camera are seen from a second pose
+    (p_curr = R p_prev + t, a small random rotation, |t| = baseline), projected
+    with the distortion model, perturbed by Gaussian pixel noise and truncated
+    to integer pixels (the features' u32 coordinates); outlier_frac of the
+    current pixels are replaced by uniform ones.  Rows are (lod, prev_x,
+    prev_y, curr_x, curr_y) with a random level, unique current pixel per
+    level, sorted by (level, curr_x, curr_y): the order in which the
+    reference's triangulation pass visits its inliers.  Returns
+    (rows u32 (n, 5), cam, R, t).
+    """
+    rng = np.random.default_rng(seed)
+    cam = SCENE_CAMERA if cam is None else np.asarray(cam, np.float64)
+    ang = rng.normal(0.0, rot_sigma, 3)
+    th = float(np.linalg.norm(ang))
+    if th > 0.0:
+        k = ang / th
+        kx = np.array([[0.0, -k[2], k[1]], [k[2], 0.0, -k[0]], [-k[1], k[0], 0.0]])
+        R = np.eye(3) + np.sin(th) * kx + (1.0 - np.cos(th)) * kx @ kx
+    else:
+        R = np.eye(3)
+    t = rng.normal(0.0, 1.0, 3)
+    t[2] *= 0.3
+    t *= baseline / np.linalg.norm(t) if baseline > 0 else 0.0
+
+    def proj(P):
+        x, y = P[:, 0] / P[:, 2], P[:, 1] / P[:, 2]
+        r2 = x * x + y * y
+        k1, k2, p1, p2 = cam[4:8]
+        rad = 1.0 + k1 * r2 + k2 * r2 * r2
+        xd = x * rad + 2.0 * p1 * x * y + p2 * (r2 + 2.0 * x * x)
+        yd = y * rad + p1 * (r2 + 2.0 * y * y) + 2.0 * p2 * x * y
+        return np.stack([cam[0] * xd + cam[2], cam[1] * yd + cam[3]], 1)
+
+    m = max(8 * n, 64)
+    P = np.stack([rng.uniform(-8.0, 8.0, m), rng.uniform(-5.0, 5.0, m), rng.uniform(depth[0], depth[1], m)], 1)
+    Q = P @ R.T + t
+    a, b = proj(P), proj(Q)
+    inside = (Q[:, 2] > 0.5) & np.all((a >= 0) & (a < [w, h]) & (b >= 0) & (b < [w, h]), 1)
+    a, b = a[inside], b[inside]
+    a = np.floor(a + rng.normal(0.0, noise_px, a.shape)).clip(0, [w - 1, h - 1])
+    b = np.floor(b + rng.normal(0.0, noise_px, b.shape)).clip(0, [w - 1, h - 1])
+    n_out = int(round(outlier_frac * len(b)))
+    if n_out:
+        idx = rng.choice(len(b), n_out, replace=False)
+        b[idx] = rng.integers(0, [w, h], (n_out, 2))
+    rows = np.stack([rng.integers(0, 6, len(a)), a[:, 0], a[:, 1], b[:, 0], b[:, 1]], 1).astype(np.uint32)
+    _, first = np.unique(rows[:, [0, 3, 4]], axis=0, return_index=True)
+    rows = rows[np.sort(first)][:n]
+    rows = rows[np.lexsort((rows[:, 4], rows[:, 3], rows[:, 0]))]
+    return np.ascontiguousarray(rows), cam.copy(), R, t
