@@ -165,6 +165,35 @@ __device__ __forceinline__ float cfg_corner(const float (*sm)[SW], int r, int c,
     return score;
 }
 
+// Packed binary32 products (sm_100 family mul.f32x2): one instruction rounds
+// each lane to nearest even exactly as the scalar mul.rn would, so two
+// independent products cost one issue slot with unchanged bits.  Sums stay
+// scalar: ptxas (CUDA 13.0) contracts mul.rn.f32x2 feeding add.rn.f32x2 into
+// one fused multiply-add (a single rounding) in spite of .rn and
+// --fmad=false, while a packed product feeding a scalar add.rn is kept as two
+// roundings.
+__device__ __forceinline__ float2 mul2_rn(float2 a, float2 b) {
+    float2 d;
+    asm("{\n\t.reg .b64 pa, pb, pd;\n\t"
+        "mov.b64 pa, {%2, %3};\n\tmov.b64 pb, {%4, %5};\n\t"
+        "mul.rn.f32x2 pd, pa, pb;\n\tmov.b64 {%0, %1}, pd;\n\t}"
+        : "=f"(d.x), "=f"(d.y)
+        : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+    return d;
+}
+
+// Left-to-right sum of four packed products, lane by lane, in scalar adds.
+__device__ __forceinline__ float2 sum4(float2 p, float2 q, float2 r, float2 t) {
+    float x = p.x, y = p.y;
+    x = x + q.x;
+    y = y + q.y;
+    x = x + r.x;
+    y = y + r.y;
+    x = x + t.x;
+    y = y + t.y;
+    return make_float2(x, y);
+}
+
 __device__ __forceinline__ bool mask_bit(const uint32_t* mask, int p) {
     return (__ldg(mask + (p >> 5)) >> (p & 31)) & 1u;
 }
@@ -176,7 +205,7 @@ __device__ __forceinline__ bool mask_bit(const uint32_t* mask, int p) {
 // on the row or only on the column, so they are computed once per tile row /
 // column (same operations as the per-pixel formula, hence the same bits).
 template <int TW, int TH, bool CFG>
-__global__ void __launch_bounds__(K1_THREADS)
+__global__ void __launch_bounds__(K1_THREADS, 5)
 k_detect(const FrameDev* __restrict__ frames, const TileItem* __restrict__ tiles, uint32_t* err) {
     constexpr int HY = CFG ? HY_CFG : uslam::HY;
     constexpr int SW = TW + 2 * HX;
@@ -184,12 +213,14 @@ k_detect(const FrameDev* __restrict__ frames, const TileItem* __restrict__ tiles
     static_assert(K1_THREADS % TW == 0 && SW + SH + 3 * TH <= 2 * K1_THREADS, "tile shape");
     __shared__ float sm[SH][SW];
     __shared__ float s_lut[256];                 // f32(u8) / 255
-    __shared__ int s_fx0[SW], s_fx1[SW];         // LOD0 source columns per staged column
-    __shared__ float s_fa[SW];
-    __shared__ int s_fy0[SH], s_fy1[SH];         // LOD0 source rows per staged row
-    __shared__ float s_fb[SH];
+    __shared__ int2 s_fx[SW];                    // LOD0 source columns (x0, x1) per staged column
+    __shared__ float2 s_fa[SW];                  // (1 - a, a)
+    __shared__ int2 s_fy[SH];                    // LOD0 source rows (y0, y1) per staged row
+    __shared__ float2 s_fnb[SH], s_fb[SH];       // (1 - b, 1 - b), (b, b)
     __shared__ int s_by0[3][TH], s_by1[3][TH];   // blur taps: staged rows per output row
-    __shared__ float s_bb[3][TH];
+    // blur taps, y weights per output row as pairs: rows j = 0, 1 side by
+    // side, and row j = 2 twice
+    __shared__ float2 s_b01[TH], s_nb01[TH], s_b22[TH], s_nb22[TH];
     __shared__ float s_score[CFG ? TH + 2 : 1][CFG ? TW + 2 : 1];  // cfg: FAST score, tile + 1 ring
     __shared__ uint8_t s_arc[CFG ? TH + 2 : 1][CFG ? TW + 2 : 1];
     const TileItem it = tiles[blockIdx.x];
@@ -213,18 +244,19 @@ k_detect(const FrameDev* __restrict__ frames, const TileItem* __restrict__ tiles
             const int gx = tint_clamp(X0 - HX + i, w);
             const float u = (((float)gx + 0.5f) / (float)w) * (float)F.W0 - 0.5f;
             const float fi = floorf(u);
-            s_fa[i] = u - fi;
-            s_fx0[i] = edge_index(fi, F.W0);
-            s_fx1[i] = edge_index(fi + 1.0f, F.W0);
+            const float a = u - fi;
+            s_fa[i] = make_float2(1.0f - a, a);
+            s_fx[i] = make_int2(edge_index(fi, F.W0), edge_index(fi + 1.0f, F.W0));
         } else if (i < SW + SH) {
             if (l == 0) continue;
             const int r = i - SW;
             const int gy = tint_clamp(Y0 - HY + r, h);
             const float v = (((float)gy + 0.5f) / (float)h) * (float)F.H0 - 0.5f;
             const float fj = floorf(v);
-            s_fb[r] = v - fj;
-            s_fy0[r] = edge_index(fj, F.H0);
-            s_fy1[r] = edge_index(fj + 1.0f, F.H0);
+            const float b = v - fj, nb = 1.0f - b;
+            s_fb[r] = make_float2(b, b);
+            s_fnb[r] = make_float2(nb, nb);
+            s_fy[r] = make_int2(edge_index(fj, F.H0), edge_index(fj + 1.0f, F.H0));
         } else {
             // generate_features.wgsl:153-169, y part of the 9 taps
             const int ty = (i - SW - SH) / 3, k = (i - SW - SH) % 3;
@@ -234,7 +266,14 @@ k_detect(const FrameDev* __restrict__ frames, const TileItem* __restrict__ tiles
             const float fj = floorf(v);
             int r0 = edge_index(fj, h) - (Y0 - HY), r1 = edge_index(fj + 1.0f, h) - (Y0 - HY);
             if (Y0 + ty < h && (r0 < 0 || r1 >= SH)) atomicOr(err, USLAM_ERR_SMEM_RANGE);
-            s_bb[k][ty] = v - fj;
+            const float b = v - fj, nb = 1.0f - b;
+            if (k == 2) {
+                s_b22[ty] = make_float2(b, b);
+                s_nb22[ty] = make_float2(nb, nb);
+            } else {
+                reinterpret_cast<float*>(&s_b01[ty])[k] = b;
+                reinterpret_cast<float*>(&s_nb01[ty])[k] = nb;
+            }
             s_by0[k][ty] = min(max(r0, 0), SH - 1);
             s_by1[k][ty] = min(max(r1, 0), SH - 1);
         }
@@ -250,16 +289,20 @@ k_detect(const FrameDev* __restrict__ frames, const TileItem* __restrict__ tiles
             const int gx = tint_clamp(X0 - HX + c, w);
             val = s_lut[__ldg(img + (size_t)gy * pitch + gx)];
         } else {
-            const float a = s_fa[c], b = s_fb[r];
-            const uint8_t* r0 = img + (size_t)s_fy0[r] * pitch;
-            const uint8_t* r1 = img + (size_t)s_fy1[r] * pitch;
-            const float t00 = s_lut[__ldg(r0 + s_fx0[c])], t10 = s_lut[__ldg(r0 + s_fx1[c])];
-            const float t01 = s_lut[__ldg(r1 + s_fx0[c])], t11 = s_lut[__ldg(r1 + s_fx1[c])];
-            const float na = 1.0f - a, nb = 1.0f - b;
-            val = (na * nb) * t00;
-            val = val + (a * nb) * t10;
-            val = val + (na * b) * t01;
-            val = val + (a * b) * t11;
+            // weights (na nb, a nb) and (na b, a b) as two packed products,
+            // then the texel products in pairs; the sum in the scalar order
+            const float2 nab = s_fa[c];
+            const int2 fx = s_fx[c], fy = s_fy[r];
+            const uint8_t* r0 = img + (size_t)fy.x * pitch;
+            const uint8_t* r1 = img + (size_t)fy.y * pitch;
+            const float2 t0 = make_float2(s_lut[__ldg(r0 + fx.x)], s_lut[__ldg(r0 + fx.y)]);
+            const float2 t1 = make_float2(s_lut[__ldg(r1 + fx.x)], s_lut[__ldg(r1 + fx.y)]);
+            const float2 p0 = mul2_rn(mul2_rn(nab, s_fnb[r]), t0);
+            const float2 p1 = mul2_rn(mul2_rn(nab, s_fb[r]), t1);
+            val = p0.x;
+            val = val + p0.y;
+            val = val + p1.x;
+            val = val + p1.y;
         }
         sm[r][c] = val;
     }
@@ -304,7 +347,20 @@ k_detect(const FrameDev* __restrict__ frames, const TileItem* __restrict__ tiles
     float* const lvl = F.lvl[l];
     float* const blur = F.blur[l];
     const int kp_pitch = F.kp_pitch[l], bl_pitch = F.bl_pitch[l];
-    const float wt[3] = {0.3125f, 0.375f, 0.3125f};
+    // x weights of the taps as pairs: (a_i, a_i) and (1 - a_i, 1 - a_i) for
+    // the pairs (i, j = 0 | 1), and (a_0, a_1), (1 - a_0, 1 - a_1) for the pair
+    // (i = 0 | 1, j = 2); tap weights 0.3125, 0.375, 0.3125
+    float2 pa[3], pna[3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        pa[i] = make_float2(ax[i], ax[i]);
+        pna[i] = make_float2(1.0f - ax[i], 1.0f - ax[i]);
+    }
+    const float2 pa01 = make_float2(ax[0], ax[1]);
+    const float2 pna01 = make_float2(1.0f - ax[0], 1.0f - ax[1]);
+    const float2 wt_same[3] = {make_float2(0.3125f, 0.3125f), make_float2(0.375f, 0.375f),
+                               make_float2(0.3125f, 0.3125f)};
+    const float2 wt01 = make_float2(0.3125f, 0.375f);
     for (int ty = t / TW; ty < TH; ty += K1_THREADS / TW) {
         const int y = Y0 + ty;
         if (y >= h) break;
@@ -349,25 +405,58 @@ k_detect(const FrameDev* __restrict__ frames, const TileItem* __restrict__ tiles
         kpmap[(size_t)y * kp_pitch + x] = (uint8_t)keep;
         if (l > 0) lvl[p] = sm[r][c];
 
-        // 3. blur cache: G(x, y) of generate_features.wgsl:149-172
-        float sum = 0.0f;
+        // 3. blur cache: G(x, y) of generate_features.wgsl:149-172.  Tap (i, j)
+        // is sv = (na nb) T00 + (a nb) T10 + (na b) T01 + (a b) T11 summed
+        // left to right, then q = (sv wt_i) wt_j, and G = the q summed j-major,
+        // i-minor from 0.  The products of two taps run as packed pairs
+        // ((i, 0) with (i, 1), and (0, 2) with (1, 2)); every lane is the scalar
+        // product, and the sums are scalar in the written order.
+        const float* row0[3];
+        const float* row1[3];
 #pragma unroll
         for (int j = 0; j < 3; ++j) {
-            const float b = s_bb[j][ty];
-            const float* row0 = sm[s_by0[j][ty]];
-            const float* row1 = sm[s_by1[j][ty]];
-            const float nb = 1.0f - b;
+            row0[j] = sm[s_by0[j][ty]];
+            row1[j] = sm[s_by1[j][ty]];
+        }
+        float q[3][3];
+        {
+            const float2 b01 = s_b01[ty], nb01 = s_nb01[ty];
 #pragma unroll
             for (int i = 0; i < 3; ++i) {
-                const float a = ax[i];
-                const float na = 1.0f - a;
-                float sv = (na * nb) * row0[ix0[i]];
-                sv = sv + (a * nb) * row0[ix1[i]];
-                sv = sv + (na * b) * row1[ix0[i]];
-                sv = sv + (a * b) * row1[ix1[i]];
-                sum = sum + (sv * wt[i]) * wt[j];
+                const float2 t00 = make_float2(row0[0][ix0[i]], row0[1][ix0[i]]);
+                const float2 t10 = make_float2(row0[0][ix1[i]], row0[1][ix1[i]]);
+                const float2 t01 = make_float2(row1[0][ix0[i]], row1[1][ix0[i]]);
+                const float2 t11 = make_float2(row1[0][ix1[i]], row1[1][ix1[i]]);
+                const float2 sv = sum4(mul2_rn(mul2_rn(pna[i], nb01), t00), mul2_rn(mul2_rn(pa[i], nb01), t10),
+                                       mul2_rn(mul2_rn(pna[i], b01), t01), mul2_rn(mul2_rn(pa[i], b01), t11));
+                const float2 qq = mul2_rn(mul2_rn(sv, wt_same[i]), wt01);
+                q[0][i] = qq.x;
+                q[1][i] = qq.y;
             }
         }
+        {
+            const float2 b22 = s_b22[ty], nb22 = s_nb22[ty];
+            const float2 t00 = make_float2(row0[2][ix0[0]], row0[2][ix0[1]]);
+            const float2 t10 = make_float2(row0[2][ix1[0]], row0[2][ix1[1]]);
+            const float2 t01 = make_float2(row1[2][ix0[0]], row1[2][ix0[1]]);
+            const float2 t11 = make_float2(row1[2][ix1[0]], row1[2][ix1[1]]);
+            const float2 sv = sum4(mul2_rn(mul2_rn(pna01, nb22), t00), mul2_rn(mul2_rn(pa01, nb22), t10),
+                                   mul2_rn(mul2_rn(pna01, b22), t01), mul2_rn(mul2_rn(pa01, b22), t11));
+            const float2 qq = mul2_rn(mul2_rn(sv, wt01), wt_same[2]);
+            q[2][0] = qq.x;
+            q[2][1] = qq.y;
+            const float a = ax[2], na = pna[2].x, b = b22.x, nb = nb22.x;
+            float s2 = (na * nb) * row0[2][ix0[2]];
+            s2 = s2 + (a * nb) * row0[2][ix1[2]];
+            s2 = s2 + (na * b) * row1[2][ix0[2]];
+            s2 = s2 + (a * b) * row1[2][ix1[2]];
+            q[2][2] = (s2 * 0.3125f) * 0.3125f;
+        }
+        float sum = 0.0f;
+#pragma unroll
+        for (int j = 0; j < 3; ++j)
+#pragma unroll
+            for (int i = 0; i < 3; ++i) sum = sum + q[j][i];
         blur[(size_t)y * bl_pitch + x] = sum;
     }
 }
