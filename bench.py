@@ -44,9 +44,10 @@ W, H, LEVELS = 752, 480, 6
 STRESS_W, STRESS_H, STRESS_LEVELS, STRESS_CAP = 3840, 2160, 8, 2500
 POPC_PER_SM_CLK = 16  # 32-bit population count results per SM per clock (documented issue rate)
 POPC_PER_DISTANCE = 4  # carry-save-adder Hamming distance of 256 bits
-# kernels of one graph replay of the uniform batch (one tile shape): k_detect,
-# k_blur_border, k_band_count, k_band_write, k_xsort, k_describe, k_match, k_mutual
-KERNELS_PER_STEP = 8
+# kernels of one graph replay of the uniform batch (one tile shape): k_pyramid,
+# k_detect, k_blur_border, k_band_count, k_band_write, k_xsort, k_describe,
+# k_match, k_mutual
+KERNELS_PER_STEP = 9
 METRIC = "frames/s detect+describe+match @752x480 (batched, 64-frame graph)"
 WORKLOAD = "batched-uniform: 64 consecutive 752x480 u8 frames, plane trajectory, consecutive-pair matching"
 
@@ -208,6 +209,7 @@ def algorithmic_bytes(kept_per_frame: list[int], matches_per_pair: list[int], fr
         "match_total": 32 * (N + M) + 8 * K,
         "total_per_step": total,
         # per-kernel shares outside the path model, for the roofline of whichever kernel dominates:
+        "detect_total": frames * 5 * P,        # f32 level tiles read + u8 keypoint maps written
         "border_total": frames * 4 * border,   # blur-cache border cells written (f32)
         "compact_total": frames * P + 12 * N,  # keypoint maps read (u8) + feature headers written
         "mutual_total": 16 * K + 8 * M,        # match records written + direction tables read
@@ -870,14 +872,16 @@ def run_ours(a):
     prof = batch.profile(iters=5)
     dom = max(prof, key=prof.get)
     kernel_bytes = {
-        "k_detect": nbytes["pyramid_per_frame"] * n,
+        "k_pyramid": nbytes["pyramid_per_frame"] * n,
+        "k_detect": nbytes["detect_total"],
         "k_blur_border": nbytes["border_total"],
         "compaction": nbytes["compact_total"],
         "k_describe": nbytes["describe_total"],
         "k_match": nbytes["match_total"],
         "k_mutual": nbytes["mutual_total"],
     }
-    traffic_units = {"k_detect": n, "k_blur_border": n, "compaction": n, "k_describe": n, "k_match": n - 1}
+    traffic_units = {"k_pyramid": n, "k_detect": n, "k_blur_border": n, "compaction": n, "k_describe": n,
+                     "k_match": n - 1}
     traffic_per_unit = measured_traffic()
     dom_traffic = traffic_per_unit[dom] * traffic_units[dom] if dom in traffic_per_unit else None
     peaks = json.load(open(os.path.join(REPO, "MEASURED_PEAKS.json"))) if os.path.exists(

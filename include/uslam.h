@@ -272,8 +272,9 @@ uslam_status uslam_blur_margin(const uslam_ctx* ctx, int* margin);
 uslam_status uslam_batch_set_stream(uslam_batch* b, void* cuda_stream);
 /* Per-stage timing: launch the batch's stages `iters` times without the
  * graph and without the fork, with CUDA events between them on the batch
- * stream, and return the mean milliseconds per launch in kernel_ms[0..5]:
- * detect (k_detect, one launch per tile shape), blur-cache border
+ * stream, and return the mean milliseconds per launch in kernel_ms[0..6]:
+ * pyramid (k_pyramid, one launch per tile shape), detect (k_detect, one
+ * launch per tile shape), blur-cache border
  * (k_blur_border), compaction (k_band_count + k_band_write + k_xsort),
  * describe (k_describe), match (k_match, or k_bruteforce with matcher 1) and
  * mutual check / emit (k_mutual).  Synchronous. */

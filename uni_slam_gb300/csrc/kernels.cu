@@ -28,10 +28,13 @@ namespace uslam {
 // K1 tile geometry: TW x TH output pixels (a template parameter pair, one of
 // kTileShapes), halo HX columns / HY rows (HY_CFG with the cfg profile, whose
 // 3x3 NMS needs the FAST score one pixel beyond the tile).
-constexpr int HX = 5;
-constexpr int HY = 3;
-constexpr int HY_CFG = 4;
+constexpr int HX = USLAM_TILE_HX;
+constexpr int HY = USLAM_TILE_HY;
+constexpr int HY_CFG = USLAM_TILE_HY_CFG;
 constexpr int K1_THREADS = 256;
+// Spin limit of a tile load's mbarrier wait (try_wait polls); past it the
+// kernel records USLAM_ERR_TMA_TIMEOUT and leaves the tile.
+constexpr uint32_t kTmaWaitLimit = 1u << 20;
 // cfg detection profile threshold: 20 grey levels on the u8/255 scale.
 constexpr float kCfgThreshold = 20.0f / 255.0f;
 
@@ -198,25 +201,163 @@ __device__ __forceinline__ bool mask_bit(const uint32_t* mask, int p) {
     return (__ldg(mask + (p >> 5)) >> (p & 31)) & 1u;
 }
 
+// ------------------------------------------------------ TMA + mbarrier ----
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+    // make the initialised barrier visible to the async (TMA) proxy
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+                 : "memory");
+}
+// Bounded wait for phase `parity` of the barrier: true when it completed.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint32_t limit) {
+    const uint32_t a = smem_addr(bar);
+    for (uint32_t i = 0; i < limit; ++i) {
+        uint32_t done;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(done)
+            : "r"(a), "r"(parity)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+// 2D tiled TMA load of the map's box at element coordinates (x, y) into
+// shared memory, completing on the barrier (x * 4 bytes is 32-byte aligned
+// for every caller: x = tile origin - 8, tile widths multiples of 32).
+__device__ __forceinline__ void tma_load_2d(void* dst, const void* tmap, int x, int y, uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::
+            "r"(smem_addr(dst)),
+        "l"(tmap), "r"(x), "r"(y), "r"(smem_addr(bar))
+        : "memory");
+}
+
+// ----------------------------------------------------------- pyramid ----
+// Level l of one TW x TH tile into lvl[l] (row pitch lvl_pitch): l = 0 is
+// f32(u8) / 255 (provider_base.cpp:121-124), read 8 pixels per 8-byte load
+// and stored as two 16-byte vectors; l >= 1 is one canonical bilinear tap of
+// LOD0 at the texel centre (create_pyramid.wgsl:11-12).  Sampling
+// coordinates depend only on the row or only on the column, so they are
+// computed once per tile row / column (the per-pixel operations, so the same
+// bits).  The weights (na nb, a nb) and (na b, a b) are packed products and
+// the sum is scalar in the written order.
+template <int TW, int TH>
+__global__ void __launch_bounds__(K1_THREADS)
+k_pyramid(const FrameDev* __restrict__ frames, const TileItem* __restrict__ tiles) {
+    static_assert(K1_THREADS % TW == 0 && TW % 8 == 0, "tile shape");
+    __shared__ float s_lut[256];  // f32(u8) / 255
+    __shared__ int2 s_fx[TW];     // LOD0 source columns (x0, x1) per tile column
+    __shared__ float2 s_fa[TW];   // (1 - a, a)
+    __shared__ int2 s_fy[TH];     // LOD0 source rows (y0, y1) per tile row
+    __shared__ float2 s_fnb[TH], s_fb[TH];  // (1 - b, 1 - b), (b, b)
+    const TileItem it = tiles[blockIdx.x];
+    const FrameDev& F = frames[it.frame];
+    const int l = it.level;
+    const int w = F.w[l], h = F.h[l];
+    const int X0 = it.tx * TW, Y0 = it.ty * TH;
+    const int t = threadIdx.x;
+    float* const out = F.lvl[l];
+    const int lp = F.lvl_pitch[l];
+    const uint8_t* img = F.img;
+    const int pitch = F.img_pitch;
+    s_lut[t] = (float)t / 255.0f;
+    if (l == 0) {
+        __syncthreads();
+        constexpr int SEGS = TW / 8;
+        for (int u = t; u < SEGS * TH; u += K1_THREADS) {
+            const int r = u / SEGS;
+            const int x = X0 + (u - r * SEGS) * 8, y = Y0 + r;
+            if (y >= h || x >= w) continue;
+            // x is a multiple of 8 below w, so x + 8 <= the 16-byte image pitch
+            const uint2 q = *reinterpret_cast<const uint2*>(img + (size_t)y * pitch + x);
+            float v[8];
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                v[k] = s_lut[(q.x >> (8 * k)) & 255u];
+                v[4 + k] = s_lut[(q.y >> (8 * k)) & 255u];
+            }
+            float* o = out + (size_t)y * lp + x;
+            if (x + 8 <= lp) {
+                reinterpret_cast<float4*>(o)[0] = make_float4(v[0], v[1], v[2], v[3]);
+                reinterpret_cast<float4*>(o)[1] = make_float4(v[4], v[5], v[6], v[7]);
+            } else {
+#pragma unroll
+                for (int k = 0; k < 8; ++k)
+                    if (x + k < w) o[k] = v[k];
+            }
+        }
+        return;
+    }
+    for (int i = t; i < TW + TH; i += K1_THREADS) {
+        if (i < TW) {
+            const int gx = min(X0 + i, w - 1);
+            const float u = (((float)gx + 0.5f) / (float)w) * (float)F.W0 - 0.5f;
+            const float fi = floorf(u);
+            const float a = u - fi;
+            s_fa[i] = make_float2(1.0f - a, a);
+            s_fx[i] = make_int2(edge_index(fi, F.W0), edge_index(fi + 1.0f, F.W0));
+        } else {
+            const int r = i - TW;
+            const int gy = min(Y0 + r, h - 1);
+            const float v = (((float)gy + 0.5f) / (float)h) * (float)F.H0 - 0.5f;
+            const float fj = floorf(v);
+            const float b = v - fj, nb = 1.0f - b;
+            s_fb[r] = make_float2(b, b);
+            s_fnb[r] = make_float2(nb, nb);
+            s_fy[r] = make_int2(edge_index(fj, F.H0), edge_index(fj + 1.0f, F.H0));
+        }
+    }
+    __syncthreads();
+    const int tx = t % TW;
+    const int x = X0 + tx;
+    if (x >= w) return;
+    const float2 nab = s_fa[tx];
+    const int2 fx = s_fx[tx];
+    for (int ty = t / TW; ty < TH; ty += K1_THREADS / TW) {
+        const int y = Y0 + ty;
+        if (y >= h) break;
+        const int2 fy = s_fy[ty];
+        const uint8_t* r0 = img + (size_t)fy.x * pitch;
+        const uint8_t* r1 = img + (size_t)fy.y * pitch;
+        const float2 t0 = make_float2(s_lut[__ldg(r0 + fx.x)], s_lut[__ldg(r0 + fx.y)]);
+        const float2 t1 = make_float2(s_lut[__ldg(r1 + fx.x)], s_lut[__ldg(r1 + fx.y)]);
+        const float2 p0 = mul2_rn(mul2_rn(nab, s_fnb[ty]), t0);
+        const float2 p1 = mul2_rn(mul2_rn(nab, s_fb[ty]), t1);
+        float val = p0.x;
+        val = val + p0.y;
+        val = val + p1.x;
+        val = val + p1.y;
+        out[(size_t)y * lp + x] = val;
+    }
+}
+
 // ---------------------------------------------------------------- K1 ----
-// One TW x TH tile of one level: stage the level pixels (+ halo) in shared
-// memory, then per pixel the FAST response, the cull decision, the level
-// value and the blur-cache value G(x, y).  Sampling coordinates depend only
-// on the row or only on the column, so they are computed once per tile row /
-// column (same operations as the per-pixel formula, hence the same bits).
+// One TW x TH tile of one level: one TMA load stages the level pixels plus
+// halo (written by k_pyramid) in shared memory, then per pixel the FAST
+// response, the cull decision and the blur-cache value G(x, y).  The blur
+// taps' sampling coordinates depend only on the row or only on the column,
+// so they are computed once per tile row / column (same operations as the
+// per-pixel formula, hence the same bits).
 template <int TW, int TH, bool CFG>
 __global__ void __launch_bounds__(K1_THREADS, 5)
-k_detect(const FrameDev* __restrict__ frames, const TileItem* __restrict__ tiles, uint32_t* err) {
+k_detect(const FrameDev* __restrict__ frames, const TileItem* __restrict__ tiles, int shape, uint32_t* err) {
     constexpr int HY = CFG ? HY_CFG : uslam::HY;
-    constexpr int SW = TW + 2 * HX;
-    constexpr int SH = TH + 2 * HY;
-    static_assert(K1_THREADS % TW == 0 && SW + SH + 3 * TH <= 2 * K1_THREADS, "tile shape");
-    __shared__ float sm[SH][SW];
-    __shared__ float s_lut[256];                 // f32(u8) / 255
-    __shared__ int2 s_fx[SW];                    // LOD0 source columns (x0, x1) per staged column
-    __shared__ float2 s_fa[SW];                  // (1 - a, a)
-    __shared__ int2 s_fy[SH];                    // LOD0 source rows (y0, y1) per staged row
-    __shared__ float2 s_fnb[SH], s_fb[SH];       // (1 - b, 1 - b), (b, b)
+    constexpr int SW = TW + 2 * HX;                   // staged columns [X0 - HX, X0 + TW + HX)
+    constexpr int SH = TH + 2 * HY;                   // staged rows [Y0 - HY, Y0 + TH + HY)
+    constexpr int BW = TW + 2 * USLAM_TILE_XPAD;      // TMA box columns [X0 - XPAD, X0 + TW + XPAD)
+    constexpr int CX = USLAM_TILE_XPAD - HX;          // box column of staged column 0
+    static_assert(K1_THREADS % TW == 0 && CX >= 0 && (BW * 4) % 16 == 0 && BW <= 256 && SH <= 256, "tile shape");
+    __shared__ __align__(128) float sbox[SH][BW];
+    __shared__ __align__(8) uint64_t s_bar;
     __shared__ int s_by0[3][TH], s_by1[3][TH];   // blur taps: staged rows per output row
     // blur taps, y weights per output row as pairs: rows j = 0, 1 side by
     // side, and row j = 2 twice
@@ -232,81 +373,60 @@ k_detect(const FrameDev* __restrict__ frames, const TileItem* __restrict__ tiles
     const float tex_x = 1.0f / (float)w;
     const float tex_y = 1.0f / (float)h;
     const float off[3] = {-1.2f, 0.0f, 1.2f};
-    const uint8_t* img = F.img;
-    const int pitch = F.img_pitch;
 
-    // 0. per-tile tables
-    s_lut[t] = (float)t / 255.0f;
-    for (int i = t; i < SW + SH + 3 * TH; i += K1_THREADS) {
-        if (i < SW) {
-            if (l == 0) continue;
-            // create_pyramid.wgsl:11-12 + canonical bilinear, x part
-            const int gx = tint_clamp(X0 - HX + i, w);
-            const float u = (((float)gx + 0.5f) / (float)w) * (float)F.W0 - 0.5f;
-            const float fi = floorf(u);
-            const float a = u - fi;
-            s_fa[i] = make_float2(1.0f - a, a);
-            s_fx[i] = make_int2(edge_index(fi, F.W0), edge_index(fi + 1.0f, F.W0));
-        } else if (i < SW + SH) {
-            if (l == 0) continue;
-            const int r = i - SW;
-            const int gy = tint_clamp(Y0 - HY + r, h);
-            const float v = (((float)gy + 0.5f) / (float)h) * (float)F.H0 - 0.5f;
-            const float fj = floorf(v);
-            const float b = v - fj, nb = 1.0f - b;
-            s_fb[r] = make_float2(b, b);
-            s_fnb[r] = make_float2(nb, nb);
-            s_fy[r] = make_int2(edge_index(fj, F.H0), edge_index(fj + 1.0f, F.H0));
-        } else {
-            // generate_features.wgsl:153-169, y part of the 9 taps
-            const int ty = (i - SW - SH) / 3, k = (i - SW - SH) % 3;
-            const float uvy = ((float)(Y0 + ty) + 0.5f) * tex_y;
-            const float offk = k == 0 ? -1.2f : (k == 1 ? 0.0f : 1.2f);
-            const float v = (uvy + offk * tex_y) * (float)h - 0.5f;
-            const float fj = floorf(v);
-            int r0 = edge_index(fj, h) - (Y0 - HY), r1 = edge_index(fj + 1.0f, h) - (Y0 - HY);
-            if (Y0 + ty < h && (r0 < 0 || r1 >= SH)) atomicOr(err, USLAM_ERR_SMEM_RANGE);
-            const float b = v - fj, nb = 1.0f - b;
-            if (k == 2) {
-                s_b22[ty] = make_float2(b, b);
-                s_nb22[ty] = make_float2(nb, nb);
-            } else {
-                reinterpret_cast<float*>(&s_b01[ty])[k] = b;
-                reinterpret_cast<float*>(&s_nb01[ty])[k] = nb;
-            }
-            s_by0[k][ty] = min(max(r0, 0), SH - 1);
-            s_by1[k][ty] = min(max(r1, 0), SH - 1);
-        }
+    // 0. one thread starts the tile load; the others build the tap tables
+    //    meanwhile.  Box cells outside the level arrive as 0 and are
+    //    replaced below.
+    if (t == 0) {
+        const void* tmap = static_cast<const char*>(F.tmaps) +
+                           (size_t)(l * USLAM_NUM_TILE_SHAPES + shape) * USLAM_TMAP_BYTES;
+        mbar_init(&s_bar, 1u);
+        mbar_expect_tx(&s_bar, (uint32_t)(SH * BW * 4));
+        tma_load_2d(&sbox[0][0], tmap, X0 - USLAM_TILE_XPAD, Y0 - HY, &s_bar);
     }
-    __syncthreads();
+    for (int i = t; i < 3 * TH; i += K1_THREADS) {
+        // generate_features.wgsl:153-169, y part of the 9 taps
+        const int ty = i / 3, k = i % 3;
+        const float uvy = ((float)(Y0 + ty) + 0.5f) * tex_y;
+        const float offk = k == 0 ? -1.2f : (k == 1 ? 0.0f : 1.2f);
+        const float v = (uvy + offk * tex_y) * (float)h - 0.5f;
+        const float fj = floorf(v);
+        int r0 = edge_index(fj, h) - (Y0 - HY), r1 = edge_index(fj + 1.0f, h) - (Y0 - HY);
+        if (Y0 + ty < h && (r0 < 0 || r1 >= SH)) atomicOr(err, USLAM_ERR_SMEM_RANGE);
+        const float b = v - fj, nb = 1.0f - b;
+        if (k == 2) {
+            s_b22[ty] = make_float2(b, b);
+            s_nb22[ty] = make_float2(nb, nb);
+        } else {
+            reinterpret_cast<float*>(&s_b01[ty])[k] = b;
+            reinterpret_cast<float*>(&s_nb01[ty])[k] = nb;
+        }
+        s_by0[k][ty] = min(max(r0, 0), SH - 1);
+        s_by1[k][ty] = min(max(r1, 0), SH - 1);
+    }
+    __syncthreads();  // the barrier is initialised before anyone polls it
+    const bool landed = mbar_wait(&s_bar, 0u, kTmaWaitLimit);
+    if (__syncthreads_or(!landed)) {
+        if (t == 0) atomicOr(err, USLAM_ERR_TMA_TIMEOUT);
+        mbar_wait(&s_bar, 0u, kTmaWaitLimit);  // the copy in flight, again bounded
+        return;
+    }
 
-    // 1. level tile + halo; halo cells follow the Tint clamp (far edge for < 0)
-    for (int idx = t; idx < SH * SW; idx += K1_THREADS) {
-        const int r = idx / SW, c = idx - r * SW;
-        float val;
-        if (l == 0) {
-            const int gy = tint_clamp(Y0 - HY + r, h);
-            const int gx = tint_clamp(X0 - HX + c, w);
-            val = s_lut[__ldg(img + (size_t)gy * pitch + gx)];
-        } else {
-            // weights (na nb, a nb) and (na b, a b) as two packed products,
-            // then the texel products in pairs; the sum in the scalar order
-            const float2 nab = s_fa[c];
-            const int2 fx = s_fx[c], fy = s_fy[r];
-            const uint8_t* r0 = img + (size_t)fy.x * pitch;
-            const uint8_t* r1 = img + (size_t)fy.y * pitch;
-            const float2 t0 = make_float2(s_lut[__ldg(r0 + fx.x)], s_lut[__ldg(r0 + fx.y)]);
-            const float2 t1 = make_float2(s_lut[__ldg(r1 + fx.x)], s_lut[__ldg(r1 + fx.y)]);
-            const float2 p0 = mul2_rn(mul2_rn(nab, s_fnb[r]), t0);
-            const float2 p1 = mul2_rn(mul2_rn(nab, s_fb[r]), t1);
-            val = p0.x;
-            val = val + p0.y;
-            val = val + p1.x;
-            val = val + p1.y;
+    // 1. halo cells outside the level follow the Tint clamp min(u32(c), n - 1)
+    //    (a negative coordinate reads the far edge)
+    if (X0 < HX || X0 + TW + HX > w || Y0 < HY || Y0 + TH + HY > h) {
+        const float* lv = F.lvl[l];
+        const int lp = F.lvl_pitch[l];
+        for (int idx = t; idx < SH * SW; idx += K1_THREADS) {
+            const int r = idx / SW, c = idx - r * SW;
+            const int gy = Y0 - HY + r, gx = X0 - HX + c;
+            if ((unsigned)gy < (unsigned)h && (unsigned)gx < (unsigned)w) continue;
+            sbox[r][c + CX] = __ldg(lv + (size_t)tint_clamp(gy, h) * lp + tint_clamp(gx, w));
         }
-        sm[r][c] = val;
+        __syncthreads();
     }
-    __syncthreads();
+    // staged cell (r, c) = sm[r][c], c counted from X0 - HX
+    const float(*sm)[BW] = reinterpret_cast<const float(*)[BW]>(&sbox[0][CX]);
 
     if constexpr (CFG) {
         // score of every pixel of the tile and its 1-pixel ring; pixels within
@@ -344,7 +464,6 @@ k_detect(const FrameDev* __restrict__ frames, const TileItem* __restrict__ tiles
     }
     const uint32_t* mask = F.mask[l];
     uint8_t* const kpmap = F.kpmap[l];
-    float* const lvl = F.lvl[l];
     float* const blur = F.blur[l];
     const int kp_pitch = F.kp_pitch[l], bl_pitch = F.bl_pitch[l];
     // x weights of the taps as pairs: (a_i, a_i) and (1 - a_i, 1 - a_i) for
@@ -403,7 +522,6 @@ k_detect(const FrameDev* __restrict__ frames, const TileItem* __restrict__ tiles
             }
         }
         kpmap[(size_t)y * kp_pitch + x] = (uint8_t)keep;
-        if (l > 0) lvl[p] = sm[r][c];
 
         // 3. blur cache: G(x, y) of generate_features.wgsl:149-172.  Tap (i, j)
         // is sv = (na nb) T00 + (a nb) T10 + (na b) T01 + (a b) T11 summed
@@ -897,6 +1015,7 @@ k_blur_border(const FrameDev* __restrict__ frames, const SegDev* __restrict__ se
         const uint8_t* img = F.img;
         const int pitch = F.img_pitch;
         const float* lvl = l > 0 ? F.lvl[l] : nullptr;
+        const int lp = F.lvl_pitch[l];
         const float tex_x = 1.0f / (float)w;
         const float tex_y = 1.0f / (float)h;
         const uint32_t px = ex < w + M ? (uint32_t)ex : 0xffffffffu;
@@ -926,10 +1045,10 @@ k_blur_border(const FrameDev* __restrict__ frames, const SegDev* __restrict__ se
                 for (int i = 0; i < 3; ++i) {
                     float t00, t10, t01, t11;
                     if (lvl) {
-                        t00 = __ldg(lvl + (size_t)j0 * w + ix0[i]);
-                        t10 = __ldg(lvl + (size_t)j0 * w + ix1[i]);
-                        t01 = __ldg(lvl + (size_t)j1 * w + ix0[i]);
-                        t11 = __ldg(lvl + (size_t)j1 * w + ix1[i]);
+                        t00 = __ldg(lvl + (size_t)j0 * lp + ix0[i]);
+                        t10 = __ldg(lvl + (size_t)j0 * lp + ix1[i]);
+                        t01 = __ldg(lvl + (size_t)j1 * lp + ix0[i]);
+                        t11 = __ldg(lvl + (size_t)j1 * lp + ix1[i]);
                     } else {
                         t00 = s_lut[__ldg(img + (size_t)j0 * pitch + ix0[i])];
                         t10 = s_lut[__ldg(img + (size_t)j0 * pitch + ix1[i])];
@@ -996,13 +1115,14 @@ k_describe(const FrameDev* __restrict__ frames, const SegDev* __restrict__ segs,
             const int x = (int)__uint_as_float(rec[0]);
             const int y = (int)__uint_as_float(rec[1]);
             const float* lvl = F.lvl[l];
+            const int lp = F.lvl_pitch[l];
             float m10 = 0.0f, m01 = 0.0f;
 #pragma unroll
             for (int k = 0; k < 29; ++k) {
                 const int cx = tint_clamp(x + kdx[k], w);
                 const int cy = tint_clamp(y + kdy[k], h);
                 const float v = l == 0 ? s_lut[__ldg(F.img + (size_t)cy * F.img_pitch + cx)]
-                                       : __ldg(lvl + (size_t)cy * (size_t)w + cx);
+                                       : __ldg(lvl + (size_t)cy * (size_t)lp + cx);
                 m10 = m10 + (float)kdx[k] * v;
                 m01 = m01 + (float)kdy[k] * v;
             }
@@ -1473,11 +1593,23 @@ template <bool CFG>
 cudaError_t launch_detect_profile(const FrameDev* frames, const TileItem* tiles, int ntiles, int shape, uint32_t* err,
                                   cudaStream_t st) {
     switch (shape) {
-        case 0: k_detect<64, 32, CFG><<<ntiles, K1_THREADS, 0, st>>>(frames, tiles, err); break;
-        case 1: k_detect<128, 32, CFG><<<ntiles, K1_THREADS, 0, st>>>(frames, tiles, err); break;
-        case 2: k_detect<64, 16, CFG><<<ntiles, K1_THREADS, 0, st>>>(frames, tiles, err); break;
-        case 3: k_detect<32, 32, CFG><<<ntiles, K1_THREADS, 0, st>>>(frames, tiles, err); break;
-        case 4: k_detect<128, 16, CFG><<<ntiles, K1_THREADS, 0, st>>>(frames, tiles, err); break;
+        case 0: k_detect<64, 32, CFG><<<ntiles, K1_THREADS, 0, st>>>(frames, tiles, shape, err); break;
+        case 1: k_detect<128, 32, CFG><<<ntiles, K1_THREADS, 0, st>>>(frames, tiles, shape, err); break;
+        case 2: k_detect<64, 16, CFG><<<ntiles, K1_THREADS, 0, st>>>(frames, tiles, shape, err); break;
+        case 3: k_detect<32, 32, CFG><<<ntiles, K1_THREADS, 0, st>>>(frames, tiles, shape, err); break;
+        case 4: k_detect<128, 16, CFG><<<ntiles, K1_THREADS, 0, st>>>(frames, tiles, shape, err); break;
+        default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+cudaError_t launch_pyramid(const FrameDev* frames, const TileItem* tiles, int ntiles, int shape, cudaStream_t st) {
+    if (ntiles <= 0) return cudaSuccess;
+    switch (shape) {
+        case 0: k_pyramid<64, 32><<<ntiles, K1_THREADS, 0, st>>>(frames, tiles); break;
+        case 1: k_pyramid<128, 32><<<ntiles, K1_THREADS, 0, st>>>(frames, tiles); break;
+        case 2: k_pyramid<64, 16><<<ntiles, K1_THREADS, 0, st>>>(frames, tiles); break;
+        case 3: k_pyramid<32, 32><<<ntiles, K1_THREADS, 0, st>>>(frames, tiles); break;
+        case 4: k_pyramid<128, 16><<<ntiles, K1_THREADS, 0, st>>>(frames, tiles); break;
         default: return cudaErrorInvalidValue;
     }
     return cudaGetLastError();

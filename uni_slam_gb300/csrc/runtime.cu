@@ -13,6 +13,7 @@
 // k_bruteforce; k_mutual or the emit) is captured once into a CUDA graph.
 // A frontend (uslam_frontend) is a 2-slot batch driven frame by frame with
 // the reference's FeatureSet(0)/(1) rotation.
+#include <cuda.h>  // CUtensorMap and its encode enums (types only: the entry point comes through the runtime)
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -20,6 +21,7 @@
 #include <cmath>
 #include <cstring>
 #include <map>
+#include <mutex>
 #include <string>
 #include <thread>
 #include <utility>
@@ -234,7 +236,8 @@ uslam_status create_batch(uslam_ctx* ctx, int n_frames, const int* widths, const
     };
     struct FrameLayout {
         size_t lvl[USLAM_MAX_LEVELS], blur[USLAM_MAX_LEVELS], kpmap[USLAM_MAX_LEVELS], feats[USLAM_MAX_LEVELS],
-            xorder[USLAM_MAX_LEVELS], colstart[USLAM_MAX_LEVELS], qorder[USLAM_MAX_LEVELS], bands[USLAM_MAX_LEVELS], counts;
+            xorder[USLAM_MAX_LEVELS], colstart[USLAM_MAX_LEVELS], qorder[USLAM_MAX_LEVELS], bands[USLAM_MAX_LEVELS], counts,
+            tmaps;
     };
     std::vector<FrameLayout> fl(n_frames);
     for (int f = 0; f < n_frames; ++f) {
@@ -272,10 +275,10 @@ uslam_status create_batch(uslam_ctx* ctx, int n_frames, const int* widths, const
         FrameLayout& Ly = fl[f];
         Ly.counts = b->feat_off[f];
         for (int l = 0; l < L; ++l) {
-            const size_t n = static_cast<size_t>(F.w[l]) * F.h[l];
             F.kp_pitch[l] = static_cast<int>(round_up(static_cast<size_t>(F.w[l]), 16));
             Ly.feats[l] = take(&out_bytes, capa * 48);
-            Ly.lvl[l] = l > 0 ? take(&scratch, n * 4) : 0;
+            F.lvl_pitch[l] = lvl_pitch_of(F.w[l]);
+            Ly.lvl[l] = take(&scratch, static_cast<size_t>(F.h[l]) * F.lvl_pitch[l] * 4);
             F.bl_pitch[l] = F.w[l] + ctx->margin + 1;
             Ly.blur[l] = take(&scratch, static_cast<size_t>(F.h[l] + ctx->margin + 1) * F.bl_pitch[l] * 4);
             Ly.kpmap[l] = take(&scratch, static_cast<size_t>(F.h[l]) * F.kp_pitch[l]);
@@ -284,6 +287,7 @@ uslam_status create_batch(uslam_ctx* ctx, int n_frames, const int* widths, const
             Ly.qorder[l] = take(&scratch, capa * 4);
             Ly.bands[l] = take(&scratch, static_cast<size_t>((F.h[l] + 31) / 32) * 8);
         }
+        Ly.tmaps = take(&scratch, static_cast<size_t>(L) * kNumTileShapes * USLAM_TMAP_BYTES);
         b->max_w = std::max(b->max_w, F.w[0]);
     }
     b->pairs.resize(n_pairs);
@@ -385,7 +389,7 @@ uslam_status create_batch(uslam_ctx* ctx, int n_frames, const int* widths, const
             return s;
         }
         for (int l = 0; l < L; ++l) {
-            F.lvl[l] = l > 0 ? reinterpret_cast<float*>(sc_base + Ly.lvl[l]) : nullptr;
+            F.lvl[l] = reinterpret_cast<float*>(sc_base + Ly.lvl[l]);
             F.blur[l] = reinterpret_cast<float*>(sc_base + Ly.blur[l]);
             F.kpmap[l] = reinterpret_cast<uint8_t*>(sc_base + Ly.kpmap[l]);
             F.feats[l] = reinterpret_cast<uint32_t*>(out_base + Ly.feats[l]);
@@ -394,6 +398,17 @@ uslam_status create_batch(uslam_ctx* ctx, int n_frames, const int* widths, const
             F.qorder[l] = reinterpret_cast<uint32_t*>(sc_base + Ly.qorder[l]);
             F.bands[l] = reinterpret_cast<uint32_t*>(sc_base + Ly.bands[l]);
             F.mask[l] = masks[l];
+        }
+        F.tmaps = sc_base + Ly.tmaps;
+        std::vector<char> maps(static_cast<size_t>(L) * kNumTileShapes * USLAM_TMAP_BYTES);
+        s = encode_tile_maps(F, ctx->detector, maps.data(), &ctx->err);
+        if (s == USLAM_OK) {
+            e = cudaMemcpy(sc_base + Ly.tmaps, maps.data(), maps.size(), cudaMemcpyHostToDevice);
+            if (e != cudaSuccess) s = ctx->cuda_fail(e, "tensor map upload");
+        }
+        if (s != USLAM_OK) {
+            free_batch(b);
+            return s;
         }
     }
     for (int p = 0; p < n_pairs; ++p) {
@@ -495,6 +510,7 @@ uslam_status check_err_word(uslam_batch* b) {
         std::string m = "kernel bounds check tripped:";
         if (word & USLAM_ERR_SMEM_RANGE) m += " blur tap outside the staged tile;";
         if (word & USLAM_ERR_MATCH_OVERFLOW) m += " match list overflow;";
+        if (word & USLAM_ERR_TMA_TIMEOUT) m += " tile load wait limit reached;";
         return set_err(b->err(), USLAM_KERNEL_CHECK, m);
     }
     return USLAM_OK;
@@ -729,7 +745,8 @@ uslam_status uslam_batch_pyramid_level(uslam_batch* b, int frame, int level, flo
     if (!b || !out || frame < 0 || frame >= static_cast<int>(b->frames.size()) || level < 1 || level >= b->levels)
         return USLAM_INVALID_ARG;
     const FrameDev& F = b->frames[frame];
-    cudaError_t e = cudaMemcpy(out, F.lvl[level], sizeof(float) * F.w[level] * F.h[level], cudaMemcpyDeviceToHost);
+    cudaError_t e = cudaMemcpy2D(out, sizeof(float) * F.w[level], F.lvl[level], sizeof(float) * F.lvl_pitch[level],
+                                 sizeof(float) * F.w[level], F.h[level], cudaMemcpyDeviceToHost);
     if (e != cudaSuccess) return b->ctx->cuda_fail(e, "pyramid readback");
     return USLAM_OK;
 }
@@ -770,12 +787,12 @@ uslam_status uslam_batch_profile(uslam_batch* b, int iters, float* kernel_ms) {
     if (!b || iters <= 0 || !kernel_ms) return USLAM_INVALID_ARG;
     uslam_ctx* c = b->ctx;
     const Program& P = b->full;
-    constexpr int K = 6;
+    constexpr int K = 7;
     cudaEvent_t ev[K + 1];
     for (auto& x : ev) x = nullptr;
     cudaError_t e = cudaSuccess;
     for (int i = 0; i <= K && e == cudaSuccess; ++i) e = cudaEventCreate(&ev[i]);
-    double acc[K] = {0, 0, 0, 0, 0, 0};
+    double acc[K] = {0, 0, 0, 0, 0, 0, 0};
     const int grid = c->num_sms * 4;
     for (int it = 0; it < iters && e == cudaSuccess; ++it) {
         int k = 0;
@@ -783,7 +800,13 @@ uslam_status uslam_batch_profile(uslam_batch* b, int iters, float* kernel_ms) {
             if (e == cudaSuccess) e = cudaEventRecord(ev[k++], b->stream);
         };
         mark();
-        if (e == cudaSuccess) e = launch_detect_shaped(b->d_frames, P.tiles, P.tile_begin, c->detector, b->d_err, b->stream);
+        for (int sh = 0; sh < kNumTileShapes && e == cudaSuccess; ++sh)
+            e = launch_pyramid(b->d_frames, P.tiles + P.tile_begin[sh], P.tile_begin[sh + 1] - P.tile_begin[sh], sh,
+                               b->stream);
+        mark();
+        for (int sh = 0; sh < kNumTileShapes && e == cudaSuccess; ++sh)
+            e = launch_detect(b->d_frames, P.tiles + P.tile_begin[sh], P.tile_begin[sh + 1] - P.tile_begin[sh], sh,
+                              c->detector, b->d_err, b->stream);
         mark();
         if (e == cudaSuccess) e = launch_blur_border(b->d_frames, P.fsegs, P.nfsegs, grid, b->stream);
         mark();
@@ -838,8 +861,8 @@ uslam_status uslam_get_tile_shape(const uslam_ctx* ctx, int width, int height, i
 }
 
 // Autotuner: a throwaway batch of n_frames copies of the caller's frame runs
-// once (pyramid masks, cull coverage), then k_detect is timed over every
-// frame's tiles in each shape (CUDA events on the batch stream, median of
+// once (pyramid masks, cull coverage), then k_pyramid + k_detect are timed
+// over every frame's tiles in each shape (CUDA events on the batch stream, median of
 // `reps` launches); the fastest shape is stored for the resolution class.
 uslam_status uslam_autotune(uslam_ctx* ctx, int width, int height, const uint8_t* img, int pitch, int n_frames,
                             int reps, int* shape_out, float* ms_out) {
@@ -874,6 +897,7 @@ uslam_status uslam_autotune(uslam_ctx* ctx, int width, int height, const uint8_t
         std::vector<float> t;
         for (int r = -2; r < reps && e == cudaSuccess; ++r) {
             e = cudaEventRecord(e0, b->stream);
+            if (e == cudaSuccess) e = launch_pyramid(b->d_frames, d_tiles, n, s, b->stream);
             if (e == cudaSuccess) e = launch_detect(b->d_frames, d_tiles, n, s, ctx->detector, b->d_err, b->stream);
             if (e == cudaSuccess) e = cudaEventRecord(e1, b->stream);
             if (e == cudaSuccess) e = cudaEventSynchronize(e1);
@@ -1181,3 +1205,54 @@ uslam_status uslam_match_sets(uslam_ctx* ctx, const uslam_featset* prev, const u
 }
 
 }  // extern "C"
+
+namespace uslam_rt {
+
+namespace {
+using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                   const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_tiled() {
+    static EncodeTiledFn fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<EncodeTiledFn>(p);
+        cudaGetLastError();
+    });
+    return fn;
+}
+}  // namespace
+
+uslam_status encode_tile_maps(const FrameDev& F, int detector, void* out, std::string* err) {
+    static_assert(sizeof(CUtensorMap) == USLAM_TMAP_BYTES, "tensor map size");
+    const EncodeTiledFn fn = encode_tiled();
+    if (!fn) return set_err(err, USLAM_CUDA_ERROR, "cuTensorMapEncodeTiled is not available from the driver");
+    const int hy = detector == 1 ? USLAM_TILE_HY_CFG : USLAM_TILE_HY;
+    for (int l = 0; l < F.levels; ++l)
+        for (int sh = 0; sh < kNumTileShapes; ++sh) {
+            CUtensorMap* m =
+                reinterpret_cast<CUtensorMap*>(static_cast<char*>(out) + (static_cast<size_t>(l) * kNumTileShapes + sh) *
+                                                                             USLAM_TMAP_BYTES);
+            const cuuint64_t dims[2] = {static_cast<cuuint64_t>(F.w[l]), static_cast<cuuint64_t>(F.h[l])};
+            const cuuint64_t strides[1] = {static_cast<cuuint64_t>(F.lvl_pitch[l]) * 4u};
+            const cuuint32_t box[2] = {static_cast<cuuint32_t>(kTileShapes[sh][0] + 2 * USLAM_TILE_XPAD),
+                                       static_cast<cuuint32_t>(kTileShapes[sh][1] + 2 * hy)};
+            const cuuint32_t estr[2] = {1u, 1u};
+            const CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, F.lvl[l], dims, strides, box, estr,
+                                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                                  CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+            if (r != CUDA_SUCCESS)
+                return set_err(err, USLAM_CUDA_ERROR,
+                               "tensor map encode failed (level " + std::to_string(l) + ", shape " + std::to_string(sh) +
+                                   ", code " + std::to_string(static_cast<int>(r)) + ")");
+        }
+    return USLAM_OK;
+}
+
+}  // namespace uslam_rt

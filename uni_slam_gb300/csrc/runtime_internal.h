@@ -25,6 +25,7 @@ struct MatchSegDev {
 };
 cudaError_t init_constants();
 cudaError_t launch_detect(const FrameDev*, const TileItem*, int, int, int, uint32_t*, cudaStream_t);
+cudaError_t launch_pyramid(const FrameDev*, const TileItem*, int, int, cudaStream_t);
 cudaError_t launch_compact_banded(const FrameDev*, const BandItem*, int, const SegDev*, int, int, cudaStream_t);
 cudaError_t launch_blur_border(const FrameDev*, const SegDev*, int, int, cudaStream_t);
 cudaError_t launch_describe(const FrameDev*, const SegDev*, int, const int32_t*, int, cudaStream_t);
@@ -36,7 +37,7 @@ cudaError_t set_compact_smem(int max_w);
 // Tile shapes (width, height) that k_detect is instantiated for; the index
 // is the `shape` argument of launch_detect.  Every shape computes the same
 // values (the arithmetic is per pixel), so the choice affects speed only.
-constexpr int kNumTileShapes = 5;
+constexpr int kNumTileShapes = USLAM_NUM_TILE_SHAPES;
 constexpr int kTileShapes[kNumTileShapes][2] = {{64, 32}, {128, 32}, {64, 16}, {32, 32}, {128, 16}};
 constexpr int kMaxSegs = 4096;
 constexpr int kMaxWidth = 8192;
@@ -141,9 +142,16 @@ struct ShapedTiles {
     }
 };
 
-// One k_detect launch per tile shape present.
+// One k_pyramid launch, then one k_detect launch, per tile shape present
+// (every pyramid level is written before any tile of that shape reads it).
 inline cudaError_t launch_detect_shaped(const FrameDev* frames, const TileItem* d_tiles, const int* begin,
                                         int detector, uint32_t* err, cudaStream_t st) {
+    for (int s = 0; s < kNumTileShapes; ++s) {
+        const int n = begin[s + 1] - begin[s];
+        if (n <= 0) continue;
+        const cudaError_t e = launch_pyramid(frames, d_tiles + begin[s], n, s, st);
+        if (e != cudaSuccess) return e;
+    }
     for (int s = 0; s < kNumTileShapes; ++s) {
         const int n = begin[s + 1] - begin[s];
         if (n <= 0) continue;
@@ -152,6 +160,15 @@ inline cudaError_t launch_detect_shaped(const FrameDev* frames, const TileItem* 
     }
     return cudaSuccess;
 }
+
+// Row pitch (floats) of a pyramid level buffer: 16-byte rows for TMA.
+inline int lvl_pitch_of(int w) { return static_cast<int>(round_up(static_cast<size_t>(w), 4)); }
+
+// Encode the tensor maps of k_detect's tile loads for one frame whose level
+// buffers F.lvl[] are set: per level and tile shape a 2D f32 map over
+// [h][w] (row pitch lvl_pitch) with box (TW + 2 XPAD) x (TH + 2 HY), HY of
+// the detector.  out holds levels * kNumTileShapes maps of USLAM_TMAP_BYTES.
+uslam_status encode_tile_maps(const FrameDev& F, int detector, void* out, std::string* err);
 
 struct ResClass {
     int W0 = 0, H0 = 0;

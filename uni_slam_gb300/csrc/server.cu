@@ -335,7 +335,8 @@ uslam_status uslam_server_create(uslam_ctx* ctx, const uslam_server_params* p, u
     // slot bytes per class, then slots per class from an equal share of the budget
     struct SlotLayout {
         size_t bytes, in, counts, lvl[USLAM_MAX_LEVELS], blur[USLAM_MAX_LEVELS], kpmap[USLAM_MAX_LEVELS],
-            feats[USLAM_MAX_LEVELS], xorder[USLAM_MAX_LEVELS], colstart[USLAM_MAX_LEVELS], qorder[USLAM_MAX_LEVELS], bands[USLAM_MAX_LEVELS], a2b, b2a, matches, mcount;
+            feats[USLAM_MAX_LEVELS], xorder[USLAM_MAX_LEVELS], colstart[USLAM_MAX_LEVELS], qorder[USLAM_MAX_LEVELS], bands[USLAM_MAX_LEVELS], a2b, b2a, matches, mcount,
+            tmaps;
     };
     std::vector<SlotLayout> lay(p->n_sizes);
     std::vector<FrameDev> proto(p->n_sizes);
@@ -375,11 +376,11 @@ uslam_status uslam_server_create(uslam_ctx* ctx, const uslam_server_params* p, u
         C.W0 = W0;
         C.H0 = H0;
         for (int l = 0; l < L; ++l) {
-            const size_t n = static_cast<size_t>(F.w[l]) * F.h[l];
             F.kp_pitch[l] = static_cast<int>(round_up(static_cast<size_t>(F.w[l]), 16));
             F.bl_pitch[l] = F.w[l] + ctx->margin + 1;
+            F.lvl_pitch[l] = lvl_pitch_of(F.w[l]);
             Y.feats[l] = take(capa * 48);
-            Y.lvl[l] = l > 0 ? take(n * 4) : 0;
+            Y.lvl[l] = take(static_cast<size_t>(F.h[l]) * F.lvl_pitch[l] * 4);
             Y.blur[l] = take(static_cast<size_t>(F.h[l] + ctx->margin + 1) * F.bl_pitch[l] * 4);
             Y.kpmap[l] = take(static_cast<size_t>(F.h[l]) * F.kp_pitch[l]);
             Y.xorder[l] = take(USLAM_MATCH_BANDS * capa * 4);
@@ -400,6 +401,7 @@ uslam_status uslam_server_create(uslam_ctx* ctx, const uslam_server_params* p, u
         Y.b2a = take(static_cast<size_t>(L) * capa * 4);
         Y.matches = take(static_cast<size_t>(L) * capa * 16);
         Y.mcount = take(sizeof(uint32_t) * L);
+        Y.tmaps = take(static_cast<size_t>(L) * kNumTileShapes * USLAM_TMAP_BYTES);
         Y.bytes = round_up(cur, 256);
         C.tiles_per_frame = static_cast<int>(C.tiles.size());
         max_tiles = std::max(max_tiles, C.tiles_per_frame);
@@ -448,7 +450,7 @@ uslam_status uslam_server_create(uslam_ctx* ctx, const uslam_server_params* p, u
             F.kept = reinterpret_cast<uint32_t*>(base + Y.counts);
             F.raw = F.kept + L;
             for (int l = 0; l < L; ++l) {
-                F.lvl[l] = l > 0 ? reinterpret_cast<float*>(base + Y.lvl[l]) : nullptr;
+                F.lvl[l] = reinterpret_cast<float*>(base + Y.lvl[l]);
                 F.blur[l] = reinterpret_cast<float*>(base + Y.blur[l]);
                 F.kpmap[l] = reinterpret_cast<uint8_t*>(base + Y.kpmap[l]);
                 F.feats[l] = reinterpret_cast<uint32_t*>(base + Y.feats[l]);
@@ -458,6 +460,14 @@ uslam_status uslam_server_create(uslam_ctx* ctx, const uslam_server_params* p, u
                 F.bands[l] = reinterpret_cast<uint32_t*>(base + Y.bands[l]);
                 F.mask[l] = masks[l];
             }
+            F.tmaps = base + Y.tmaps;
+            std::vector<char> maps(static_cast<size_t>(L) * kNumTileShapes * USLAM_TMAP_BYTES);
+            const uslam_status ts = encode_tile_maps(F, ctx->detector, maps.data(), &ctx->err);
+            if (ts != USLAM_OK) {
+                free_server(s);
+                return ts;
+            }
+            e = cudaMemcpy(base + Y.tmaps, maps.data(), maps.size(), cudaMemcpyHostToDevice);
             s->frames[g] = F;
             SrvSlot& sl = s->slots[g];
             sl.cls = k;
@@ -465,7 +475,7 @@ uslam_status uslam_server_create(uslam_ctx* ctx, const uslam_server_params* p, u
             sl.b2a = reinterpret_cast<int32_t*>(base + Y.b2a);
             sl.matches = reinterpret_cast<int32_t*>(base + Y.matches);
             sl.match_count = reinterpret_cast<uint32_t*>(base + Y.mcount);
-            e = cudaHostAlloc(&sl.h_in, static_cast<size_t>(F.H0) * F.img_pitch, cudaHostAllocDefault);
+            if (e == cudaSuccess) e = cudaHostAlloc(&sl.h_in, static_cast<size_t>(F.H0) * F.img_pitch, cudaHostAllocDefault);
         }
     }
     if (e == cudaSuccess) e = cudaMalloc(&s->d_frames, sizeof(FrameDev) * nslots);

@@ -4,7 +4,14 @@
 // HBM layout of one frame slot (all sub-buffers 256-byte aligned, carved out
 // of one arena allocation per batch):
 //   img      u8   [H0][img_pitch]          LOD0 input (the H2D boundary)
-//   lvl[l]   f32  [h_l][w_l]   (l >= 1)    pyramid level l (parity output)
+//   lvl[l]   f32  [h_l][lvl_pitch_l]       pyramid level l (l = 0: u8/255), written by
+//                                          k_pyramid; the source of k_detect's TMA tile
+//                                          loads, so lvl_pitch_l = w_l rounded up to 4
+//                                          floats (16-byte rows) and the base is 256-byte
+//                                          aligned
+//   tmaps    CUtensorMap [levels][USLAM_NUM_TILE_SHAPES]  2D tiled maps over lvl[l], one per tile
+//                                          shape (box = tile + halo, widened to TW + 16
+//                                          columns), 128 bytes each
 //   blur[l]  f32  [h_l + M + 1][bl_pitch_l] 9-tap blurred sample G(P) of level l for
 //                                          every integer point a BRIEF test can reach:
 //                                          x in [0, w_l + M) plus one sentinel column
@@ -40,9 +47,11 @@ struct FrameDev {
     int h[USLAM_MAX_LEVELS];
     int kp_pitch[USLAM_MAX_LEVELS];
     int bl_pitch[USLAM_MAX_LEVELS];  // blur cache row pitch (floats): w + margin + 1
+    int lvl_pitch[USLAM_MAX_LEVELS]; // pyramid level row pitch (floats): w rounded up to 4
     int margin;                      // blur cache margin M beyond the level
     int cell_cap;                    // > 0: keypoints kept per 32x32 cell (cell order); 0: (y, x) order
     float* lvl[USLAM_MAX_LEVELS];
+    const void* tmaps;  // CUtensorMap [levels][USLAM_NUM_TILE_SHAPES] over lvl (device, 64-byte aligned)
     float* blur[USLAM_MAX_LEVELS];
     uint8_t* kpmap[USLAM_MAX_LEVELS];
     uint32_t* bands[USLAM_MAX_LEVELS];       // per 32-row band: raw and kept keypoint counts
@@ -98,6 +107,18 @@ struct BandItem {
 
 #define USLAM_ERR_SMEM_RANGE 1u
 #define USLAM_ERR_MATCH_OVERFLOW 2u
+#define USLAM_ERR_TMA_TIMEOUT 4u  // a tile load did not complete within the wait limit
+
+// k_detect tile staging: halo of HX columns and HY rows (HY_CFG with the cfg
+// profile, whose 3x3 NMS needs the FAST score one pixel beyond the tile); the
+// TMA box starts XPAD columns left of the tile (a 32-byte aligned x for every
+// tile width) and is TW + 2 XPAD columns wide.
+#define USLAM_TILE_HX 5
+#define USLAM_TILE_HY 3
+#define USLAM_TILE_HY_CFG 4
+#define USLAM_TILE_XPAD 8
+#define USLAM_TMAP_BYTES 128
+#define USLAM_NUM_TILE_SHAPES 5  // k_detect tile shapes (kTileShapes of the runtime)
 
 // Packed match-partner encoding: level in the top 8 bits, index in the low 24.
 #define USLAM_PACK(l, i) (((int32_t)(l) << 24) | (int32_t)(i))

@@ -13,7 +13,7 @@ from .capi import FEATURE_DTYPE, MATCH_DTYPE, USlamError, iptr, ptr
 
 # stages timed by uslam_batch_profile (the compaction stage is three kernels:
 # k_band_count, k_band_write, k_xsort)
-KERNELS = ("k_detect", "k_blur_border", "compaction", "k_describe", "k_match", "k_mutual")
+KERNELS = ("k_pyramid", "k_detect", "k_blur_border", "compaction", "k_describe", "k_match", "k_mutual")
 
 
 def level_dims(width: int, height: int, levels: int = 6) -> list[tuple[int, int]]:
