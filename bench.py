@@ -187,6 +187,37 @@ def measured_traffic() -> dict:
     return out
 
 
+def _mm_digest(m) -> str:
+    """SHA-256 of a match list (lod_a, idx_a, lod_b, idx_b), to show that two
+    matchers returned identical lists."""
+    import hashlib
+
+    import numpy as np
+
+    if len(m) == 0:
+        return hashlib.sha256(b"").hexdigest()[:16]
+    a = np.stack([m["lod_a"], m["idx_a"], m["lod_b"], m["idx_b"]], 1).astype(np.int32)
+    return hashlib.sha256(a.tobytes()).hexdigest()[:16]
+
+
+def _tensor_core_leg(tc: dict, base: dict, npairs_key: str) -> dict:
+    """Summary of a matcher-2 run beside the matcher-1 run of the same workload."""
+    bf = tc["kernel_ms"]["k_bruteforce"]
+    out = {"matcher": "2: brute-force top-2 with distances from FP8 dot products on the tensor cores (tcgen05)",
+           "ms_per_step": tc["ms_per_step"], "frames_per_s": tc["frames_per_s"], "kernel_ms": tc["kernel_ms"],
+           "k_bf_mma_ms": bf, "match_lists_equal": tc["match_lists"] == base["match_lists"]}
+    if "bruteforce" in tc:
+        d = tc["bruteforce"]["distances_per_launch"]
+        out["gdist_per_s"] = d / (bf / 1e3) / 1e9
+        out["ms_per_pair"] = bf / tc[npairs_key]
+        # FP8 multiply-adds of the distances proper (256 per distance), as a
+        # fraction of the nominal dense FP8 rate (4.5 PFLOP/s, twice the
+        # nominal bf16 rate; the measured file holds bf16 only)
+        out["fp8_tflops"] = 2 * 256 * d / (bf / 1e3) / 1e12
+        out["fp8_frac_of_nominal"] = out["fp8_tflops"] / 4500.0
+    return out
+
+
 def algorithmic_bytes(kept_per_frame: list[int], matches_per_pair: list[int], frames: int) -> dict:
     """Per-frame algorithmic bytes of the path:
     W*H (u8 LOD0 read) + 4*(P - W*H) (f32 levels written) + 48*N (feature
@@ -541,16 +572,17 @@ def uneven_run(pat, local: int, pair_frames, steps: int, warmup: int, seed: int)
         ctx.close()
 
 
-def cfg_run(pat, local: int, frames, steps: int, warmup: int) -> dict:
+def cfg_run(pat, local: int, frames, steps: int, warmup: int, matcher: int = 1) -> dict:
     """The batched-uniform workload in the cfg profile: FAST 9-of-16 at 20/255
     with 3x3 NMS, brute-force top-2 matching at ratio 0.8 (all features of
-    each frame against all features of the previous one)."""
+    each frame against all features of the previous one); matcher 1 computes
+    the distances on the integer pipes, matcher 2 on the tensor cores."""
     import torch
 
     from uni_slam_gb300 import Batch, Context
 
     n = len(frames)
-    ctx = Context(pat, levels=LEVELS, max_width=W, max_height=H, device=local, detector=1, matcher=1, ratio=0.8)
+    ctx = Context(pat, levels=LEVELS, max_width=W, max_height=H, device=local, detector=1, matcher=matcher, ratio=0.8)
     batch = Batch(ctx, [(W, H)] * n, [(i, i + 1) for i in range(n - 1)])
     try:
         for i, f in enumerate(frames):
@@ -584,6 +616,7 @@ def cfg_run(pat, local: int, frames, steps: int, warmup: int) -> dict:
             "frames": n, "ms_per_step": step_ms, "frames_per_s": n / (step_ms / 1e3),
             "features_per_frame": sum(kept) / n, "matches_per_pair": sum(nmatch) / max(1, n - 1),
             "kernel_ms": prof, "l2": "flushed (256 MiB write) between timed steps",
+            "match_lists": [_mm_digest(batch.matches(k)) for k in range(n - 1)],
         }
     finally:
         batch.close()
@@ -715,9 +748,11 @@ def _stress_pair(seed: int):
     return synth.warped_pair(seed, STRESS_W, STRESS_H, n_rect=5000, n_check=500, scale_by_area=False)
 
 
-def stress_run(pat, local: int, pair_frames, steps: int, warmup: int, seed: int) -> dict:
+def stress_run(pat, local: int, pair_frames, steps: int, warmup: int, seed: int, matcher: int = 1) -> dict:
     """3840x2160 frames, 8 levels, 2500 kept per level, brute-force top-2
-    matching (ratio 0.8) of each frame against its warp, all pairs in one batch."""
+    matching (ratio 0.8) of each frame against its warp, all pairs in one
+    batch; matcher 1 computes the distances on the integer pipes (XOR +
+    popcount), matcher 2 on the tensor cores (FP8 dot products, tcgen05)."""
     import torch
 
     from uni_slam_gb300 import Batch, Context
@@ -725,7 +760,7 @@ def stress_run(pat, local: int, pair_frames, steps: int, warmup: int, seed: int)
     frames = [f for pr in pair_frames for f in pr]
     npairs = len(pair_frames)
     ctx = Context(pat, levels=STRESS_LEVELS, max_width=STRESS_W, max_height=STRESS_H, cap_per_level=STRESS_CAP,
-                  device=local, matcher=1, ratio=0.8)
+                  device=local, matcher=matcher, ratio=0.8)
     batch = Batch(ctx, [(STRESS_W, STRESS_H)] * len(frames), [(2 * k, 2 * k + 1) for k in range(npairs)])
     try:
         for i, f in enumerate(frames):
@@ -772,9 +807,10 @@ def stress_run(pat, local: int, pair_frames, steps: int, warmup: int, seed: int)
             "features_per_frame": sum(kept) / len(kept), "matches_per_pair": sum(nmatch) / npairs,
             "kernel_ms": prof,
             "bruteforce": {"distances_per_launch": dists, "ms": prof["k_bruteforce"],
-                           "gdist_per_s": dists / bf_s / 1e9, "popc_per_distance": POPC_PER_DISTANCE,
+                           "gdist_per_s": dists / bf_s / 1e9,
                            "ms_per_pair": prof["k_bruteforce"] / npairs},
             "l2": "flushed (256 MiB write) between timed steps", "seed": seed,
+            "match_lists": [_mm_digest(batch.matches(k)) for k in range(npairs)],
         }
     finally:
         batch.close()
@@ -995,6 +1031,8 @@ def run_ours(a):
     stress_frames, uneven_frames = side_workload_frames(a, rank)
 
     cfg = cfg_run(pat, local, frames, a.stress_steps, 2) if a.cfg else None
+    if cfg:
+        cfg["tensor_core"] = _tensor_core_leg(cfg_run(pat, local, frames, a.stress_steps, 2, matcher=2), cfg, "frames")
 
     uneven = None
     if uneven_frames:
@@ -1003,6 +1041,8 @@ def run_ours(a):
     stress = None
     if stress_frames:
         stress = stress_run(pat, local, stress_frames, a.stress_steps, 2, a.seed)
+        stress["tensor_core"] = _tensor_core_leg(
+            stress_run(pat, local, stress_frames, a.stress_steps, 2, a.seed, matcher=2), stress, "pairs")
         if clk.get("sm_mhz"):
             sms = torch.cuda.get_device_properties(local).multi_processor_count
             peak = POPC_PER_SM_CLK * sms * clk["sm_mhz"] / 1e3 / POPC_PER_DISTANCE

@@ -74,9 +74,12 @@ typedef struct uslam_params {
     const int32_t* brief_pattern;
     /* 0: the reference's windowed mutual matcher (match_features_cpu.cpp:66-207);
      * 1: brute-force top-2 over all features of both frames, Lowe test
-     *    best < ratio * second, no window and no cross-check. */
+     *    best < ratio * second, no window and no cross-check (XOR + popcount
+     *    on the integer pipes);
+     * 2: the same brute-force top-2 with the distances from the tensor cores
+     *    (popc(a & b) as an FP8 0/1 dot product, exact): identical results. */
     int matcher;
-    float ratio;  /* Lowe ratio of matcher 1 (the windowed matcher uses the reference's 0.85) */
+    float ratio;  /* Lowe ratio of matchers 1 and 2 (the windowed matcher uses the reference's 0.85) */
     /* 0: a level's keypoints in (y, x) order, the first cap_per_level kept.
      * 1..1024: per-cell caps -- each level is cut into 32x32 cells from its
      * origin; the first cell_cap keypoints of each cell in (y, x) order are
@@ -276,7 +279,7 @@ uslam_status uslam_batch_set_stream(uslam_batch* b, void* cuda_stream);
  * pyramid (k_pyramid, one launch per tile shape), detect (k_detect, one
  * launch per tile shape), blur-cache border
  * (k_blur_border), compaction (k_band_count + k_band_write + k_xsort),
- * describe (k_describe), match (k_match, or k_bruteforce with matcher 1) and
+ * describe (k_describe), match (k_match, k_bruteforce with matcher 1, k_bf_mma with matcher 2) and
  * mutual check / emit (k_mutual).  Synchronous. */
 uslam_status uslam_batch_profile(uslam_batch* b, int iters, float* kernel_ms);
 /* Bytes moved by upload and download per call (for end-to-end accounting). */

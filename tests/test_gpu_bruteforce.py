@@ -1,5 +1,7 @@
-"""Brute-force top-2 matcher (matcher=1) against the oracle: the full match
-list at 752x480 and on an uneven batch, and at the 3840x2160, 8-level,
+"""Brute-force top-2 matchers against the oracle: matcher 1 (XOR + popcount
+on the integer pipes) and matcher 2 (distances from FP8 dot products on the
+tensor cores, tcgen05), which must give identical match lists.  The full
+match list at 752x480 and on an uneven batch, and at the 3840x2160, 8-level,
 2500-per-level stress size (20000 x 20000 descriptors) as well."""
 import numpy as np
 import pytest
@@ -16,11 +18,12 @@ def _mm(m):
     return np.stack([m["lod_a"], m["idx_a"], m["lod_b"], m["idx_b"]], 1)
 
 
-def test_bruteforce_equals_oracle_uneven(brief_pattern):
+@pytest.mark.parametrize("matcher", [1, 2])
+def test_bruteforce_equals_oracle_uneven(brief_pattern, matcher):
     frames = list(synth.warped_pair(5)) + list(synth.warped_pair(6, 1280, 720)) + [
         np.full((480, 640), 77, np.uint8), synth.scene_frame(9, 640, 480)]
     pairs = [(0, 1), (2, 3), (4, 5), (5, 4), (1, 0)]
-    with Context(brief_pattern, levels=6, max_width=1280, max_height=720, matcher=1, ratio=0.8) as c:
+    with Context(brief_pattern, levels=6, max_width=1280, max_height=720, matcher=matcher, ratio=0.8) as c:
         b = Batch(c, [(f.shape[1], f.shape[0]) for f in frames], pairs)
         try:
             b.process(frames)
@@ -37,10 +40,11 @@ def test_bruteforce_equals_oracle_uneven(brief_pattern):
             b.close()
 
 
-def test_bruteforce_stress_size(brief_pattern):
+@pytest.mark.parametrize("matcher", [1, 2])
+def test_bruteforce_stress_size(brief_pattern, matcher):
     W, H, L, CAP = 3840, 2160, 8, 2500
     f0, f1 = synth.warped_pair(2024, W, H, n_rect=5000, n_check=500, scale_by_area=False)
-    with Context(brief_pattern, levels=L, max_width=W, max_height=H, cap_per_level=CAP, matcher=1,
+    with Context(brief_pattern, levels=L, max_width=W, max_height=H, cap_per_level=CAP, matcher=matcher,
                  ratio=0.8) as c:
         b = Batch(c, [(W, H), (W, H)], [(0, 1)])
         try:
@@ -59,7 +63,8 @@ def test_bruteforce_stress_size(brief_pattern):
             b.close()
 
 
-def test_bruteforce_split_and_unsplit_agree(brief_pattern):
+@pytest.mark.parametrize("matcher", [1, 2])
+def test_bruteforce_split_and_unsplit_agree(brief_pattern, matcher):
     """A launch with few pairs splits each train set over several CTAs and
     merges the partial top-2 records; a launch with many query blocks (large
     per-level caps) does not split.  Both equal the oracle."""
@@ -68,7 +73,7 @@ def test_bruteforce_split_and_unsplit_agree(brief_pattern):
     pairs = [(2 * k, 2 * k + 1) for k in range(3)]
     exp = [oracle.frame(f, brief_pattern, cap=20000) for f in frames]
     for cap in (20000, 1000):  # 3 x 469 query blocks: no split; 3 x 24: split
-        with Context(brief_pattern, levels=6, max_width=640, max_height=480, cap_per_level=cap, matcher=1,
+        with Context(brief_pattern, levels=6, max_width=640, max_height=480, cap_per_level=cap, matcher=matcher,
                      ratio=0.8) as c:
             b = Batch(c, [(640, 480)] * len(frames), pairs)
             try:

@@ -1069,6 +1069,17 @@ k_blur_border(const FrameDev* __restrict__ frames, const SegDev* __restrict__ se
     }
 }
 
+// FP8 E4M3 code of an integer 0..16 (all exact: 2^k (1 + m / 8) with
+// k = floor(log2 v) <= 4 and m = (v - 2^k) 8 / 2^k an integer).
+__device__ __forceinline__ uint32_t e4m3_small_int(int v) {
+    if (v <= 0) return 0u;
+    const int k = 31 - __clz(v);
+    return (uint32_t)(((k + 7) << 3) | (((v - (1 << k)) << 3) >> k));
+}
+
+// PACK: also write the tensor-core matcher's operand rows of every feature
+// (FrameDev::bf8 / bfext / bfpop / bfid).
+template <bool PACK>
 __global__ void __launch_bounds__(KD_THREADS)
 k_describe(const FrameDev* __restrict__ frames, const SegDev* __restrict__ segs, int nseg,
            const int32_t* __restrict__ pattern) {
@@ -1172,6 +1183,50 @@ k_describe(const FrameDev* __restrict__ frames, const SegDev* __restrict__ segs,
             for (int k = 0; k < 8; ++k)
                 if (lane == 4 + k) out = words[k];
             if (lane >= 3 && lane < 12) rec[lane] = out;
+            if constexpr (PACK) {
+                // tensor-core operand rows of this feature (flat index f over
+                // the levels): lane j writes the FP8 values of descriptor bits
+                // 8j .. 8j + 7 (K chunk j / 2, half j % 2); lanes 0-3 write
+                // the 32-value extension row (popcount split into 16 integers
+                // <= 16, then 16 x 16.0)
+                uint32_t f = i;
+                for (int q = 0; q < l; ++q) f += F.kept[q];
+                uint32_t wj = words[0];
+                uint32_t pc = 0;
+#pragma unroll
+                for (int k = 0; k < 8; ++k) {
+                    if ((lane >> 2) == k) wj = words[k];
+                    pc += (uint32_t)__popc(words[k]);
+                }
+                const uint32_t bits = (wj >> (8 * (lane & 3))) & 0xffu;
+                uint32_t lo = 0u, hi = 0u;
+#pragma unroll
+                for (int b = 0; b < 4; ++b) {
+                    lo |= ((bits >> b) & 1u) * (0x38u << (8 * b));
+                    hi |= ((bits >> (b + 4)) & 1u) * (0x38u << (8 * b));
+                }
+                *reinterpret_cast<uint2*>(F.bf8 + (size_t)(f >> 3) * 2048u + (lane >> 1) * 128u + (f & 7u) * 16u +
+                                          (lane & 1) * 8u) = make_uint2(lo, hi);
+                if (lane < 4) {
+                    uint32_t ext[2] = {0u, 0u};
+#pragma unroll
+                    for (int k = 0; k < 8; ++k) {
+                        const int e = 8 * lane + k;  // extension value index 0..31
+                        uint32_t code = 0x58u;       // 16.0
+                        if (e < 16) {
+                            const int v = min(16, max(0, (int)pc - 16 * e));
+                            code = e4m3_small_int(v);
+                        }
+                        ext[k >> 2] |= code << (8 * (k & 3));
+                    }
+                    *reinterpret_cast<uint2*>(F.bfext + (size_t)(f >> 3) * 256u + (lane >> 1) * 128u + (f & 7u) * 16u +
+                                              (lane & 1) * 8u) = make_uint2(ext[0], ext[1]);
+                }
+                if (lane == 0) {
+                    F.bfpop[f] = pc;
+                    F.bfid[f] = USLAM_PACK(l, i);
+                }
+            }
         }
     }
 }
@@ -1647,9 +1702,10 @@ cudaError_t launch_blur_border(const FrameDev* frames, const SegDev* segs, int n
 }
 
 cudaError_t launch_describe(const FrameDev* frames, const SegDev* segs, int nseg, const int32_t* pattern,
-                            int grid, cudaStream_t st) {
+                            int grid, bool pack, cudaStream_t st) {
     if (nseg <= 0) return cudaSuccess;
-    k_describe<<<grid, KD_THREADS, 0, st>>>(frames, segs, nseg, pattern);
+    if (pack) k_describe<true><<<grid, KD_THREADS, 0, st>>>(frames, segs, nseg, pattern);
+    else k_describe<false><<<grid, KD_THREADS, 0, st>>>(frames, segs, nseg, pattern);
     return cudaGetLastError();
 }
 

@@ -154,15 +154,17 @@ cudaError_t enqueue_program(uslam_batch* b, const Program& P) {
             cudaSuccess)
             return e;
         if ((e = cudaStreamWaitEvent(b->stream, b->ev_join, 0)) != cudaSuccess) return e;
-        if ((e = launch_describe(b->d_frames, P.fsegs, P.nfsegs, c->d_pattern, grid, b->stream)) != cudaSuccess)
+        if ((e = launch_describe(b->d_frames, P.fsegs, P.nfsegs, c->d_pattern, grid, c->matcher == 2, b->stream)) != cudaSuccess)
             return e;
     }
     if (P.nmsegs > 0) {
         const int grid = c->num_sms * 4;
-        if (c->matcher == 1) {
-            if ((e = launch_bruteforce(b->d_frames, b->d_pairs, P.psegs, P.npsegs, c->ratio, grid, b->stream)) !=
-                cudaSuccess)
-                return e;
+        if (c->matcher != 0) {
+            if (c->matcher == 1)
+                e = launch_bruteforce(b->d_frames, b->d_pairs, P.psegs, P.npsegs, c->ratio, grid, b->stream);
+            else
+                e = launch_bf_mma(b->d_frames, b->d_pairs, P.psegs, P.npsegs, c->ratio, c->num_sms, b->d_err, b->stream);
+            if (e != cudaSuccess) return e;
             if ((e = launch_emit(b->d_frames, b->d_pairs, P.usegs, P.nusegs, b->d_err, b->stream)) != cudaSuccess)
                 return e;
         } else {
@@ -237,7 +239,7 @@ uslam_status create_batch(uslam_ctx* ctx, int n_frames, const int* widths, const
     struct FrameLayout {
         size_t lvl[USLAM_MAX_LEVELS], blur[USLAM_MAX_LEVELS], kpmap[USLAM_MAX_LEVELS], feats[USLAM_MAX_LEVELS],
             xorder[USLAM_MAX_LEVELS], colstart[USLAM_MAX_LEVELS], qorder[USLAM_MAX_LEVELS], bands[USLAM_MAX_LEVELS], counts,
-            tmaps;
+            tmaps, bf8, bfext, bfpop, bfid;
     };
     std::vector<FrameLayout> fl(n_frames);
     for (int f = 0; f < n_frames; ++f) {
@@ -288,6 +290,13 @@ uslam_status create_batch(uslam_ctx* ctx, int n_frames, const int* widths, const
             Ly.bands[l] = take(&scratch, static_cast<size_t>((F.h[l] + 31) / 32) * 8);
         }
         Ly.tmaps = take(&scratch, static_cast<size_t>(L) * kNumTileShapes * USLAM_TMAP_BYTES);
+        if (ctx->matcher == 2) {
+            const size_t rows = round_up(static_cast<size_t>(L) * capa, 256);
+            Ly.bf8 = take(&scratch, rows * 256);
+            Ly.bfext = take(&scratch, rows * 32);
+            Ly.bfpop = take(&scratch, rows * 4);
+            Ly.bfid = take(&scratch, rows * 4);
+        }
         b->max_w = std::max(b->max_w, F.w[0]);
     }
     b->pairs.resize(n_pairs);
@@ -320,12 +329,15 @@ uslam_status create_batch(uslam_ctx* ctx, int n_frames, const int* widths, const
     }
     // Brute-force matcher: split each pair's train set so that the launch has
     // about 8 CTAs (of 128 threads, 256 queries each) per SM.
+    // Tensor-core matcher: 128 queries per unit, one CTA per SM, about two
+    // units per SM.
     std::vector<size_t> bf_off(n_pairs, 0);
-    if (ctx->matcher == 1 && n_pairs > 0) {
+    if (ctx->matcher != 0 && n_pairs > 0) {
+        const size_t per_unit = ctx->matcher == 1 ? 256 : 128;
         size_t units = 0;
         for (int p = 0; p < n_pairs; ++p)
-            units += (static_cast<size_t>(L) * std::max(b->frames[pair_prev[p]].cap, 1) + 255) / 256;
-        const size_t target = static_cast<size_t>(std::max(ctx->num_sms, 1)) * 8;
+            units += (static_cast<size_t>(L) * std::max(b->frames[pair_prev[p]].cap, 1) + per_unit - 1) / per_unit;
+        const size_t target = static_cast<size_t>(std::max(ctx->num_sms, 1)) * (ctx->matcher == 1 ? 8 : 2);
         const int splits = static_cast<int>(std::min<size_t>(16, std::max<size_t>(1, (target + units - 1) / units)));
         if (splits > 1)
             for (int p = 0; p < n_pairs; ++p) {
@@ -400,6 +412,12 @@ uslam_status create_batch(uslam_ctx* ctx, int n_frames, const int* widths, const
             F.mask[l] = masks[l];
         }
         F.tmaps = sc_base + Ly.tmaps;
+        if (ctx->matcher == 2) {
+            F.bf8 = reinterpret_cast<uint8_t*>(sc_base + Ly.bf8);
+            F.bfext = reinterpret_cast<uint8_t*>(sc_base + Ly.bfext);
+            F.bfpop = reinterpret_cast<uint32_t*>(sc_base + Ly.bfpop);
+            F.bfid = reinterpret_cast<int32_t*>(sc_base + Ly.bfid);
+        }
         std::vector<char> maps(static_cast<size_t>(L) * kNumTileShapes * USLAM_TMAP_BYTES);
         s = encode_tile_maps(F, ctx->detector, maps.data(), &ctx->err);
         if (s == USLAM_OK) {
@@ -616,7 +634,7 @@ uslam_status uslam_create(const uslam_params* params, uslam_ctx** out) {
     if (params->levels < 1 || params->levels > USLAM_MAX_LEVELS || params->max_width < 1 ||
         params->max_width > kMaxWidth || params->max_height < 1 || params->max_height > 65535 ||
         params->cap_per_level < 0 || params->cap_per_level >= (1 << 24) || !params->brief_pattern ||
-        (params->matcher != 0 && params->matcher != 1) || (params->matcher == 1 && !(params->ratio > 0.0f)) ||
+        (params->matcher < 0 || params->matcher > 2) || (params->matcher != 0 && !(params->ratio > 0.0f)) ||
         params->cell_cap < 0 || params->cell_cap > 1024 || (params->detector != 0 && params->detector != 1))
         return USLAM_INVALID_ARG;
     auto* c = new uslam_ctx();
@@ -813,14 +831,16 @@ uslam_status uslam_batch_profile(uslam_batch* b, int iters, float* kernel_ms) {
         if (e == cudaSuccess)
             e = launch_compact_banded(b->d_frames, P.bands, P.nbands, P.fsegs, P.nfsegs, b->max_w, b->stream);
         mark();
-        if (e == cudaSuccess) e = launch_describe(b->d_frames, P.fsegs, P.nfsegs, c->d_pattern, grid, b->stream);
+        if (e == cudaSuccess) e = launch_describe(b->d_frames, P.fsegs, P.nfsegs, c->d_pattern, grid, c->matcher == 2, b->stream);
         mark();
         if (e == cudaSuccess)
             e = c->matcher == 1 ? launch_bruteforce(b->d_frames, b->d_pairs, P.psegs, P.npsegs, c->ratio, grid, b->stream)
-                                : launch_match(b->d_frames, b->d_pairs, P.msegs, P.nmsegs, grid, b->stream);
+                : c->matcher == 2
+                    ? launch_bf_mma(b->d_frames, b->d_pairs, P.psegs, P.npsegs, c->ratio, c->num_sms, b->d_err, b->stream)
+                    : launch_match(b->d_frames, b->d_pairs, P.msegs, P.nmsegs, grid, b->stream);
         mark();
         if (e == cudaSuccess)
-            e = c->matcher == 1 ? launch_emit(b->d_frames, b->d_pairs, P.usegs, P.nusegs, b->d_err, b->stream)
+            e = c->matcher != 0 ? launch_emit(b->d_frames, b->d_pairs, P.usegs, P.nusegs, b->d_err, b->stream)
                                 : launch_mutual(b->d_frames, b->d_pairs, P.usegs, P.nusegs, b->d_err, b->stream);
         mark();
         if (e == cudaSuccess) e = cudaEventSynchronize(ev[K]);
@@ -1100,6 +1120,13 @@ cudaError_t copy_frame_state(const uslam_batch* src, uslam_batch* dst, int slot,
             e = cudaMemcpyAsync(B.xorder[l], A.xorder[l], USLAM_MATCH_BANDS * capa * 4, cudaMemcpyDeviceToDevice, st);
         if (e == cudaSuccess) e = cudaMemcpyAsync(B.colstart[l], A.colstart[l], cols * 4, cudaMemcpyDeviceToDevice, st);
         if (e == cudaSuccess) e = cudaMemcpyAsync(B.qorder[l], A.qorder[l], capa * 4, cudaMemcpyDeviceToDevice, st);
+    }
+    if (A.bf8 && B.bf8 && e == cudaSuccess) {
+        const size_t rows = round_up(static_cast<size_t>(A.levels) * capa, 256);
+        e = cudaMemcpyAsync(B.bf8, A.bf8, rows * 256, cudaMemcpyDeviceToDevice, st);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(B.bfext, A.bfext, rows * 32, cudaMemcpyDeviceToDevice, st);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(B.bfpop, A.bfpop, rows * 4, cudaMemcpyDeviceToDevice, st);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(B.bfid, A.bfid, rows * 4, cudaMemcpyDeviceToDevice, st);
     }
     return e;
 }

@@ -28,11 +28,12 @@ cudaError_t launch_detect(const FrameDev*, const TileItem*, int, int, int, uint3
 cudaError_t launch_pyramid(const FrameDev*, const TileItem*, int, int, cudaStream_t);
 cudaError_t launch_compact_banded(const FrameDev*, const BandItem*, int, const SegDev*, int, int, cudaStream_t);
 cudaError_t launch_blur_border(const FrameDev*, const SegDev*, int, int, cudaStream_t);
-cudaError_t launch_describe(const FrameDev*, const SegDev*, int, const int32_t*, int, cudaStream_t);
+cudaError_t launch_describe(const FrameDev*, const SegDev*, int, const int32_t*, int, bool, cudaStream_t);
 cudaError_t launch_match(const FrameDev*, const PairDev*, const void*, int, int, cudaStream_t);
 cudaError_t launch_mutual(const FrameDev*, const PairDev*, const SegDev*, int, uint32_t*, cudaStream_t);
 cudaError_t launch_emit(const FrameDev*, const PairDev*, const SegDev*, int, uint32_t*, cudaStream_t);
 cudaError_t launch_bruteforce(const FrameDev*, const PairDev*, const SegDev*, int, float, int, cudaStream_t);
+cudaError_t launch_bf_mma(const FrameDev*, const PairDev*, const SegDev*, int, float, int, uint32_t*, cudaStream_t);
 cudaError_t set_compact_smem(int max_w);
 // Tile shapes (width, height) that k_detect is instantiated for; the index
 // is the `shape` argument of launch_detect.  Every shape computes the same
