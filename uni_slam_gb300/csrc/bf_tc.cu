@@ -8,14 +8,17 @@
 // Every partial sum of such a dot product is an integer <= 256, exact in the
 // f32 accumulator whatever the summation order, so the distances are exact.
 //
-// k_describe writes each frame's descriptors in that form (uslam_internal.h:
-// bf8 rows of 256 bytes in the K-major no-swizzle core-matrix layout, and a
-// 32-value extension row per feature: its popcount split into 16 integers
-// <= 16, then 16 x 16.0).  Against a constant query-side extension (16 x -0.5,
-// 16 x 1.0) a ninth K step adds -popc(b) / 2 + 256, so the accumulator holds
-//   v = dot - popc(b) / 2 + 256 = 512 - (distance - popc(a)) / 2,
-// a half-integer in [128, 384]: every product and partial sum is exact.
-// For a query, a larger v is a smaller distance.
+// k_describe writes each frame's descriptors in that form, with each bit as
+// 8.0 (uslam_internal.h: bf8 rows of 256 bytes in the K-major no-swizzle
+// core-matrix layout), and a 32-value extension row per feature: its
+// popcount split into 16 integers <= 16, 256, its row index within its
+// 32-row group (s) split into two integers <= 16, 1.  Against the constant
+// query-side extension (16 x -32, 32, 1, 1, 32) a ninth K step adds
+// -32 popc(b) + 32 * 257 + s, so the accumulator holds the integer
+//   key = 32 (2 dot - popc(b) + 257) + s,   32 <= key <= 16447,
+// every product and partial sum exact in f32.  For a query a larger key is a
+// smaller distance (distance = popc(a) + 257 - (key >> 5)), and s tells the
+// columns of a 32-column group apart.
 //
 // One persistent CTA per SM holds 512 TMEM columns: two 128 x 256 f32
 // accumulators.  A work unit is 128 queries of one pair against its train set
@@ -23,14 +26,14 @@
 // (32 KB) and the train tiles (64 KB + 8 KB extension, double-buffered) are
 // staged by bulk copies; one thread issues nine tcgen05.mma (K = 32 each) per
 // train tile into one accumulator while eight warps reduce the other (two
-// warps per TMEM lane quarter, 128 columns each; tcgen05.ld, one query row per
-// thread) to keys and a branch-free top-2 over four independent chains.
-//
-// Key of a candidate: bits(v) | slot.  v is positive with its low 8 mantissa
-// bits zero, so keys order like v; max/min on keys keep the two largest v
-// (the two smallest distances); a tie on the best leaves equal distances,
-// which fail the ratio test (the rule of k_bruteforce), so the result does
-// not depend on the scan order.
+// warps per TMEM lane quarter, 128 columns each; tcgen05.ld, one query row
+// per thread).  The keys fit 16 bits: adding 2^23 in f32 leaves a key in the
+// low bits of the sum, a byte permute packs columns j and j + 32 of a
+// 64-column group into one register, and the top-2 runs on both halves at
+// once with max/min.u16x2 over four independent chains.  At the end of a
+// group the 16-bit keys widen to (key >> 5) << 8 | column-in-tile.  A tie on
+// the best leaves equal distances, which fail the ratio test (the rule of
+// k_bruteforce), so the result does not depend on the scan order.
 //
 // Every mbarrier wait is bounded; past the limit the kernel records
 // USLAM_ERR_TMA_TIMEOUT, drains what it issued (again bounded), frees its TMEM
@@ -44,16 +47,19 @@ namespace uslam {
 
 namespace {
 
-constexpr int TC_THREADS = 256;                 // 8 warps: two per TMEM lane quarter
-constexpr int TC_M = 128;                       // queries per work unit
-constexpr int TC_N = 256;                       // train rows per tile
+constexpr int TC_CONSUMERS = 8;                 // epilogue warps: two per TMEM lane quarter
+constexpr int TC_THREADS = 32 * (TC_CONSUMERS + 1);    // plus one producer warp
+constexpr int TC_M = 128;                       // queries per accumulator (TMEM lanes)
+constexpr int TC_Q = 2 * TC_M;                  // queries per work unit: two accumulators share each train tile
+constexpr int TC_N = 128;                       // train rows per tile
+constexpr int TC_STAGES = 3;                    // train tiles in flight
 constexpr uint32_t TC_ROW_BYTES = 256;          // 256 FP8 values per descriptor
-constexpr uint32_t TC_A_BYTES = TC_M * TC_ROW_BYTES;   // 32 KB
-constexpr uint32_t TC_B_BYTES = TC_N * TC_ROW_BYTES;   // 64 KB
+constexpr uint32_t TC_A_BYTES = TC_Q * TC_ROW_BYTES;   // 64 KB
 constexpr uint32_t TC_AX_BYTES = TC_M * 32;            // query-side extension (constant)
+constexpr uint32_t TC_B_BYTES = TC_N * TC_ROW_BYTES;   // 32 KB
 constexpr uint32_t TC_BX_BYTES = TC_N * 32;            // train-side extension rows
-constexpr uint32_t TC_SMEM = TC_A_BYTES + TC_AX_BYTES + 2 * (TC_B_BYTES + TC_BX_BYTES);
-constexpr uint32_t TC_TMEM_COLS = 512;          // two accumulators of TC_N columns
+constexpr uint32_t TC_SMEM = TC_A_BYTES + TC_AX_BYTES + TC_STAGES * (TC_B_BYTES + TC_BX_BYTES);
+constexpr uint32_t TC_TMEM_COLS = 512;          // 2 buffers x 2 accumulators x 128 columns
 constexpr uint32_t kWaitLimit = 1u << 24;       // try_wait polls per wait
 constexpr int kMaxPairs = 4096;
 
@@ -61,6 +67,9 @@ __device__ __forceinline__ uint32_t saddr(const void* p) { return (uint32_t)__cv
 
 __device__ __forceinline__ void bar_init(uint64_t* b, uint32_t n) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(saddr(b)), "r"(n) : "memory");
+}
+__device__ __forceinline__ void bar_arrive(uint64_t* b) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(saddr(b)) : "memory");
 }
 __device__ __forceinline__ void bar_expect(uint64_t* b, uint32_t bytes) {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(saddr(b)), "r"(bytes) : "memory");
@@ -96,7 +105,7 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint3
            ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
 }
 // Instruction descriptor of kind::f8f6f4: D f32 (bits 4-5 = 1), A and B E4M3
-// (0), both K-major, N >> 3 at bit 17, M >> 4 at bit 24.
+// (0), both K-major, N >> 3 at bit 17, M >> 4 at bit 24 (M = N = 128).
 constexpr uint32_t kIdesc = (1u << 4) | ((uint32_t)(TC_N >> 3) << 17) | ((uint32_t)(TC_M >> 4) << 24);
 
 __device__ __forceinline__ void mma_f8(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t accumulate) {
@@ -127,11 +136,35 @@ __device__ __forceinline__ void tmem_ld32_issue(uint32_t addr, uint32_t (&r)[32]
 }
 __device__ __forceinline__ void tmem_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
-// Top-2 of keys (largest first): (b, s) <- the two largest of {b, s, key}.
-__device__ __forceinline__ void top2(uint32_t& b, uint32_t& s, uint32_t key) {
-    s = max(s, min(b, key));
-    b = max(b, key);
+// Two 16-bit lanes at once: unsigned max / min per halfword.
+__device__ __forceinline__ uint32_t vmax2(uint32_t a, uint32_t b) {
+    uint32_t d;
+    asm("max.u16x2 %0, %1, %2;" : "=r"(d) : "r"(a), "r"(b));
+    return d;
 }
+__device__ __forceinline__ uint32_t vmin2(uint32_t a, uint32_t b) {
+    uint32_t d;
+    asm("min.u16x2 %0, %1, %2;" : "=r"(d) : "r"(a), "r"(b));
+    return d;
+}
+__device__ __forceinline__ void top2x2(uint32_t& b, uint32_t& s, uint32_t key) {
+    s = vmax2(s, vmin2(b, key));
+    b = vmax2(b, key);
+}
+__device__ __forceinline__ void top2x2_merge(uint32_t& b, uint32_t& s, uint32_t b2, uint32_t s2) {
+    s = vmax2(vmin2(b, b2), vmax2(s, s2));
+    b = vmax2(b, b2);
+}
+// 16-bit key of group column base + j (0 = none) -> (key >> 5) << 8 | column
+__device__ __forceinline__ uint32_t widen(uint32_t k16, uint32_t base) {
+    return k16 ? (((k16 >> 5) << 8) | (base + (k16 & 31u))) : 0u;
+}
+// Key of an accumulator value: the integer in the low bits of value + 2^23.
+__device__ __forceinline__ uint32_t acc_key(uint32_t bits) {
+    return __float_as_uint(__uint_as_float(bits) + 8388608.0f);
+}
+
+// Top-2 of keys (largest first): (b, s) <- the two largest of {b, s, b2, s2}.
 __device__ __forceinline__ void top2_merge(uint32_t& b, uint32_t& s, uint32_t b2, uint32_t s2) {
     s = max(min(b, b2), max(s, s2));
     b = max(b, b2);
@@ -145,6 +178,44 @@ __device__ __forceinline__ uint32_t total_kept(const FrameDev& F) {
 
 }  // namespace
 
+// Work units: 256 queries of one pair (two 128-row accumulators) against
+// the pair's train set, or a share of it when the train set is split.  Both
+// roles walk the same unit sequence and count the train tiles they pass
+// (kk, across units): tile kk uses stage kk % 3 and accumulator buffer
+// kk % 2, and the parity of the barrier phase it waits for follows from kk.
+struct TcUnit {
+    const PairDev* P;
+    const FrameDev* A;
+    const FrameDev* B;
+    uint32_t nq, nt, qbase, tb, split, nsplit;
+    int NT;
+};
+
+__device__ __forceinline__ TcUnit tc_unit(const FrameDev* frames, const PairDev* pairs, const SegDev* psegs,
+                                          const uint32_t* pref, int npairs, uint32_t g) {
+    int lo = 0, hi = npairs - 1;  // pair with pref[p] <= g < pref[p + 1]
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (pref[mid] <= g) lo = mid;
+        else hi = mid - 1;
+    }
+    TcUnit u;
+    u.P = &pairs[psegs[lo].frame];
+    u.A = &frames[u.P->prev];
+    u.B = &frames[u.P->curr];
+    u.nsplit = (uint32_t)max(u.P->bf_splits, 1);
+    const uint32_t unit = g - pref[lo];
+    const uint32_t qt = unit / u.nsplit;
+    u.split = unit - qt * u.nsplit;
+    u.qbase = qt * (uint32_t)TC_Q;
+    u.nq = total_kept(*u.A);
+    u.nt = total_kept(*u.B);
+    const uint32_t ntiles = (u.nt + TC_N - 1) / TC_N;
+    u.tb = u.split * ntiles / u.nsplit;
+    u.NT = (int)((u.split + 1u) * ntiles / u.nsplit - u.tb);
+    return u;
+}
+
 // Result per query a in a2b (packed (level, index) of its match in curr, or
 // -1), or, when the pair's train set is split, one partial record per split
 // ((distance << 8) of best and second, best id) merged by the emit kernel.
@@ -152,40 +223,45 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 k_bf_mma(const FrameDev* __restrict__ frames, const PairDev* __restrict__ pairs, const SegDev* __restrict__ psegs,
          int npairs, float ratio, uint32_t* err) {
     extern __shared__ __align__(1024) uint8_t tc_smem[];
-    __shared__ __align__(8) uint64_t bar_a, bar_b[2], bar_m[2];
+    __shared__ __align__(8) uint64_t bar_a, b_full[TC_STAGES], b_empty[TC_STAGES], acc_full[2], acc_empty[2];
     __shared__ uint32_t s_tmem;
+    __shared__ int s_fail;
     __shared__ uint32_t s_pref[kMaxPairs + 1];
-    __shared__ uint32_t s_hb[TC_M], s_hs[TC_M];  // the second column half's top-2 per query row
-    __shared__ int32_t s_hi[TC_M];
     uint8_t* sA = tc_smem;
     uint8_t* sAx = sA + TC_A_BYTES;
-    uint8_t* sB[2] = {sAx + TC_AX_BYTES, sAx + TC_AX_BYTES + TC_B_BYTES};
-    uint8_t* sBx[2] = {sAx + TC_AX_BYTES + 2 * TC_B_BYTES, sAx + TC_AX_BYTES + 2 * TC_B_BYTES + TC_BX_BYTES};
+    uint8_t* sB = sAx + TC_AX_BYTES;                   // stage s: sB + s * TC_B_BYTES
+    uint8_t* sBx = sB + TC_STAGES * TC_B_BYTES;        // stage s: sBx + s * TC_BX_BYTES
     const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
-    const int quarter = warp & 3, half = warp >> 2;
-    const int row = 32 * quarter + lane;  // this thread's query row (TMEM lane)
+    volatile int* fail = &s_fail;
 
-    // work units per pair: query tiles x train splits
+    // work units per pair: query blocks x train splits
     for (int p = t; p < npairs; p += TC_THREADS) {
         const PairDev& P = pairs[psegs[p].frame];
         const uint32_t nq = total_kept(frames[P.prev]);
-        s_pref[p + 1] = (nq + TC_M - 1) / TC_M * (uint32_t)max(P.bf_splits, 1);
+        s_pref[p + 1] = (nq + TC_Q - 1) / TC_Q * (uint32_t)max(P.bf_splits, 1);
     }
-    // query-side extension, the same for every row: 16 x -0.5 (0xB0), 16 x 1.0 (0x38)
+    // query-side extension, the same for every row: 16 x -32 (0xE0), 32 (0x60),
+    // 1, 1 (0x38), 32, zeros
     for (int i = t; i < (int)TC_AX_BYTES; i += TC_THREADS) {
         const int r = i >> 5, k = i & 31;
-        sAx[(r >> 3) * 256 + (k >> 4) * 128 + (r & 7) * 16 + (k & 15)] = k < 16 ? 0xB0 : 0x38;
+        const uint8_t v = k < 16 ? 0xE0 : (k == 16 || k == 19) ? 0x60 : (k == 17 || k == 18) ? 0x38 : 0x00;
+        sAx[(r >> 3) * 256 + (k >> 4) * 128 + (r & 7) * 16 + (k & 15)] = v;
     }
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     if (t == 0) {
+        s_fail = 0;
         bar_init(&bar_a, 1);
-        bar_init(&bar_b[0], 1);
-        bar_init(&bar_b[1], 1);
-        bar_init(&bar_m[0], 1);
-        bar_init(&bar_m[1], 1);
+        for (int i = 0; i < TC_STAGES; ++i) {
+            bar_init(&b_full[i], 1);
+            bar_init(&b_empty[i], 1);
+        }
+        for (int i = 0; i < 2; ++i) {
+            bar_init(&acc_full[i], 1);
+            bar_init(&acc_empty[i], TC_CONSUMERS);
+        }
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
-    if (warp == 0) {
+    if (warp == TC_CONSUMERS) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(saddr(&s_tmem)),
                      "r"(TC_TMEM_COLS)
                      : "memory");
@@ -202,168 +278,154 @@ k_bf_mma(const FrameDev* __restrict__ frames, const PairDev* __restrict__ pairs,
     const uint32_t tmem = s_tmem;
     const uint32_t total = s_pref[npairs];
 
-    // parities of the next completion to wait for (bar_a / bar_b: thread 0
-    // only; bar_m: every thread, uniformly)
-    uint32_t ph_a = 0, ph_b0 = 0, ph_b1 = 0, ph_m0 = 0, ph_m1 = 0;
-    uint32_t pend_b = 0, pend_m = 0;  // thread 0: copies / MMA groups issued and not yet waited for
-    bool fail = false;
-
-    // thread 0: stage train tile `tile` of B into buffer s
-    auto load_b = [&](const FrameDev& B, uint32_t tile, int s) {
-        bar_expect(&bar_b[s], TC_B_BYTES + TC_BX_BYTES);
-        bulk_load(sB[s], B.bf8 + (size_t)tile * TC_B_BYTES, TC_B_BYTES, &bar_b[s]);
-        bulk_load(sBx[s], B.bfext + (size_t)tile * TC_BX_BYTES, TC_BX_BYTES, &bar_b[s]);
-        pend_b |= 1u << s;
-    };
-    // thread 0: the nine MMAs of the train tile in buffer s into accumulator s
-    auto issue_mma = [&](int s) {
-        fence_after();
-        const uint32_t a0 = saddr(sA), b0 = saddr(sB[s]), d = tmem + (uint32_t)(s * TC_N);
-#pragma unroll
-        for (int k = 0; k < 8; ++k)
-            mma_f8(d, smem_desc(a0 + 256u * k, 128u, 2048u), smem_desc(b0 + 256u * k, 128u, 2048u), k > 0);
-        mma_f8(d, smem_desc(saddr(sAx), 128u, 256u), smem_desc(saddr(sBx[s]), 128u, 256u), 1u);
-        mma_commit(&bar_m[s]);
-        pend_m |= 1u << s;
-    };
-
-    for (uint32_t g = blockIdx.x; g < total && !fail; g += gridDim.x) {
-        int lo = 0, hi = npairs - 1;  // pair with s_pref[p] <= g < s_pref[p + 1]
-        while (lo < hi) {
-            const int mid = (lo + hi + 1) >> 1;
-            if (s_pref[mid] <= g) lo = mid;
-            else hi = mid - 1;
-        }
-        const PairDev& P = pairs[psegs[lo].frame];
-        const FrameDev& A = frames[P.prev];
-        const FrameDev& B = frames[P.curr];
-        const uint32_t nsplit = (uint32_t)max(P.bf_splits, 1);
-        const uint32_t unit = g - s_pref[lo];
-        const uint32_t qt = unit / nsplit, split = unit - qt * nsplit;
-        const uint32_t nq = total_kept(A), nt = total_kept(B);
-        const uint32_t ntiles = (nt + TC_N - 1) / TC_N;
-        const uint32_t tb = split * ntiles / nsplit, te = (split + 1u) * ntiles / nsplit;
-        const int NT = (int)(te - tb);
-        uint32_t best = 0u, second = 0u;  // keys; 0 = no candidate
-        int32_t bidx = -1;
-
-        if (NT > 0) {
-            if (t == 0) {
-                bar_expect(&bar_a, TC_A_BYTES);
-                bulk_load(sA, A.bf8 + (size_t)qt * TC_A_BYTES, TC_A_BYTES, &bar_a);
-                load_b(B, tb, 0);
-                if (NT > 1) load_b(B, tb + 1u, 1);
-                bool ok = bar_wait(&bar_a, ph_a);
-                ph_a ^= 1u;
-                ok = ok && bar_wait(&bar_b[0], ph_b0);
-                ph_b0 ^= 1u;
-                pend_b &= ~1u;
-                if (ok) issue_mma(0);
-                else fail = true;
-            }
-            fail = __syncthreads_or(fail);
-            for (int n = 0; n < NT && !fail; ++n) {
-                const int b = n & 1;
-                if (t == 0 && n + 1 < NT) {
-                    // the next tile's MMAs into the other accumulator (read out
-                    // before the last barrier)
-                    const int nb = b ^ 1;
-                    const bool ok = bar_wait(&bar_b[nb], nb ? ph_b1 : ph_b0);
-                    if (nb) ph_b1 ^= 1u;
-                    else ph_b0 ^= 1u;
-                    pend_b &= ~(1u << nb);
-                    if (ok) issue_mma(nb);
-                    else fail = true;
+    if (warp == TC_CONSUMERS) {
+        // ------------------------------------------------ producer (one lane)
+        if (lane == 0) {
+            uint32_t kk = 0, units_loaded = 0;
+            int64_t last_mma = -1;  // tile index of the last MMA group committed
+            int64_t loaded_to = 0;  // tiles [.., loaded_to) have had their loads issued
+            auto load_b = [&](const TcUnit& u, uint32_t tile_kk, uint32_t n) -> bool {
+                const uint32_t st = tile_kk % TC_STAGES;
+                // the stage's previous tile (tile_kk - 3) must have been read by its MMAs
+                if (!bar_wait(&b_empty[st], ((tile_kk / TC_STAGES) + 1u) & 1u)) return false;
+                bar_expect(&b_full[st], TC_B_BYTES + TC_BX_BYTES);
+                const uint32_t tile = u.tb + n;
+                bulk_load(sB + st * TC_B_BYTES, u.B->bf8 + (size_t)tile * TC_B_BYTES, TC_B_BYTES, &b_full[st]);
+                bulk_load(sBx + st * TC_BX_BYTES, u.B->bfext + (size_t)tile * TC_BX_BYTES, TC_BX_BYTES, &b_full[st]);
+                loaded_to = (int64_t)tile_kk + 1;
+                return true;
+            };
+            for (uint32_t g = blockIdx.x; g < total && !*fail; g += gridDim.x) {
+                const TcUnit u = tc_unit(frames, pairs, psegs, s_pref, npairs, g);
+                if (u.NT <= 0) continue;
+                bool ok = true;
+                // the query tiles are rewritten: the previous unit's MMAs must be done
+                if (last_mma >= 0) ok = bar_wait(&acc_full[last_mma & 1], (uint32_t)(last_mma >> 1) & 1u);
+                if (ok) {
+                    bar_expect(&bar_a, TC_A_BYTES);
+                    bulk_load(sA, u.A->bf8 + (size_t)u.qbase * TC_ROW_BYTES, TC_A_BYTES, &bar_a);
+                    ok = bar_wait(&bar_a, units_loaded & 1u);
+                    ++units_loaded;
                 }
-                // this tile's accumulator
-                const bool landed = bar_wait(&bar_m[b], b ? ph_m1 : ph_m0);
-                if (b) ph_m1 ^= 1u;
-                else ph_m0 ^= 1u;
-                if (t == 0) pend_m &= ~(1u << b);
-                if (!landed) fail = true;
+                for (int n = 0; n < 2 && n < u.NT && ok; ++n) ok = load_b(u, kk + (uint32_t)n, (uint32_t)n);
+                for (int n = 0; n < u.NT && ok; ++n) {
+                    const uint32_t tk = kk + (uint32_t)n, st = tk % TC_STAGES, buf = tk & 1u;
+                    ok = bar_wait(&b_full[st], (tk / TC_STAGES) & 1u) &&
+                         bar_wait(&acc_empty[buf], ((tk >> 1) + 1u) & 1u);
+                    if (!ok) break;
+                    fence_after();
+                    const uint32_t b0 = saddr(sB + st * TC_B_BYTES), bx = saddr(sBx + st * TC_BX_BYTES);
+#pragma unroll
+                    for (int h = 0; h < 2; ++h) {
+                        const uint32_t a0 = saddr(sA + h * (TC_A_BYTES / 2));
+                        const uint32_t d = tmem + buf * (uint32_t)(2 * TC_N) + (uint32_t)(h * TC_N);
+#pragma unroll
+                        for (int k = 0; k < 8; ++k)
+                            mma_f8(d, smem_desc(a0 + 256u * k, 128u, 2048u), smem_desc(b0 + 256u * k, 128u, 2048u),
+                                   k > 0);
+                        mma_f8(d, smem_desc(saddr(sAx), 128u, 256u), smem_desc(bx, 128u, 256u), 1u);
+                    }
+                    mma_commit(&acc_full[buf]);
+                    mma_commit(&b_empty[st]);
+                    last_mma = (int64_t)tk;
+                    if (n + 2 < u.NT) ok = load_b(u, tk + 2u, (uint32_t)n + 2u);
+                }
+                kk += (uint32_t)u.NT;
+                if (!ok) *fail = 1;
+            }
+            if (*fail) {
+                atomicOr(err, USLAM_ERR_TMA_TIMEOUT);
+                // drain what was issued, each wait bounded
+                if (last_mma >= 0) bar_wait(&acc_full[last_mma & 1], (uint32_t)(last_mma >> 1) & 1u);
+                for (int64_t i = max(last_mma + 1, loaded_to - TC_STAGES); i < loaded_to; ++i)
+                    bar_wait(&b_full[i % TC_STAGES], (uint32_t)(i / TC_STAGES) & 1u);
+            }
+        }
+        __syncwarp();
+    } else {
+        // ----------------------------------------------------------- consumers
+        const int quarter = warp & 3, half = warp >> 2;  // TMEM lanes, accumulator (query tile)
+        const int row = 32 * quarter + lane;
+        uint32_t kk = 0;
+        for (uint32_t g = blockIdx.x; g < total; g += gridDim.x) {
+            const TcUnit u = tc_unit(frames, pairs, psegs, s_pref, npairs, g);
+            uint32_t best = 0u, second = 0u;  // widened keys; 0 = no candidate
+            int32_t bidx = -1;
+            bool bad = false;
+            for (int n = 0; n < u.NT; ++n) {
+                const uint32_t tk = kk + (uint32_t)n, buf = tk & 1u;
+                bad = bad || *fail != 0 || !bar_wait(&acc_full[buf], (tk >> 1) & 1u);
                 fence_after();
-                if (t == 0 && !fail && n + 2 < NT) load_b(B, tb + (uint32_t)n + 2u, b);  // its buffer is free
                 // tcgen05.ld is warp-wide: a warp reads the accumulator only if
                 // every lane saw it complete
-                if (__all_sync(0xffffffffu, !fail)) {
-                    const uint32_t base = (tb + (uint32_t)n) * (uint32_t)TC_N;
-                    const uint32_t valid = nt - base < (uint32_t)TC_N ? nt - base : (uint32_t)TC_N;
-                    uint32_t cb[4] = {0u, 0u, 0u, 0u}, cs[4] = {0u, 0u, 0u, 0u};
+                if (__all_sync(0xffffffffu, !bad)) {
+                    const uint32_t base = (u.tb + (uint32_t)n) * (uint32_t)TC_N;
+                    const uint32_t valid = u.nt - base < (uint32_t)TC_N ? u.nt - base : (uint32_t)TC_N;
+                    uint32_t tb = 0u, ts = 0u;  // this tile's top-2 (widened keys)
 #pragma unroll
                     for (int c = 0; c < 2; ++c) {
                         uint32_t r0[32], r1[32];
-                        const uint32_t col = (uint32_t)(b * TC_N + half * 128 + 64 * c);
+                        const uint32_t col = buf * (uint32_t)(2 * TC_N) + (uint32_t)(half * TC_N + 64 * c);
                         const uint32_t addr = tmem + ((uint32_t)(32 * quarter) << 16) + col;
                         tmem_ld32_issue(addr, r0);
                         tmem_ld32_issue(addr + 32u, r1);
                         tmem_wait();
-                        const uint32_t s0 = (uint32_t)(half * 128 + 64 * c);
+                        const uint32_t s0 = (uint32_t)(64 * c);  // group's first column in the tile
+                        uint32_t cb[4] = {0u, 0u, 0u, 0u}, cs[4] = {0u, 0u, 0u, 0u};
                         if (valid == (uint32_t)TC_N) {
 #pragma unroll
-                            for (int j = 0; j < 32; ++j) {
-                                top2(cb[j & 3], cs[j & 3], r0[j] | (s0 + (uint32_t)j));
-                                top2(cb[j & 3], cs[j & 3], r1[j] | (s0 + 32u + (uint32_t)j));
-                            }
+                            for (int j = 0; j < 32; ++j)
+                                top2x2(cb[j & 3], cs[j & 3], __byte_perm(acc_key(r0[j]), acc_key(r1[j]), 0x5410));
                         } else {  // the last tile of the train set: columns past its end are no candidates
 #pragma unroll
                             for (int j = 0; j < 32; ++j) {
                                 const uint32_t k0 = s0 + (uint32_t)j, k1 = k0 + 32u;
-                                top2(cb[j & 3], cs[j & 3], k0 < valid ? (r0[j] | k0) : 0u);
-                                top2(cb[j & 3], cs[j & 3], k1 < valid ? (r1[j] | k1) : 0u);
+                                const uint32_t lo = k0 < valid ? (acc_key(r0[j]) & 0xffffu) : 0u;
+                                const uint32_t hi = k1 < valid ? (acc_key(r1[j]) << 16) : 0u;
+                                top2x2(cb[j & 3], cs[j & 3], lo | hi);
                             }
                         }
+                        top2x2_merge(cb[0], cs[0], cb[1], cs[1]);
+                        top2x2_merge(cb[2], cs[2], cb[3], cs[3]);
+                        top2x2_merge(cb[0], cs[0], cb[2], cs[2]);
+                        top2_merge(tb, ts, widen(cb[0] & 0xffffu, s0), widen(cs[0] & 0xffffu, s0));
+                        top2_merge(tb, ts, widen(cb[0] >> 16, s0 + 32u), widen(cs[0] >> 16, s0 + 32u));
                     }
-                    top2_merge(cb[0], cs[0], cb[1], cs[1]);
-                    top2_merge(cb[2], cs[2], cb[3], cs[3]);
-                    top2_merge(cb[0], cs[0], cb[2], cs[2]);
-                    if (cb[0] > best) bidx = __ldg(B.bfid + base + (cb[0] & 255u));
-                    top2_merge(best, second, cb[0], cs[0]);
+                    if (tb > best) bidx = __ldg(u.B->bfid + base + (tb & 255u));
+                    top2_merge(best, second, tb, ts);
+                } else {
+                    bad = true;
                 }
                 fence_before();
-                fail = __syncthreads_or(fail);
+                __syncwarp();
+                if (lane == 0) bar_arrive(&acc_empty[buf]);
             }
-        }
-        // merge the two column halves of each query row
-        if (half == 1) {
-            s_hb[row] = best;
-            s_hs[row] = second;
-            s_hi[row] = bidx;
-        }
-        __syncthreads();
-        const uint32_t q = qt * TC_M + (uint32_t)row;
-        if (half == 0 && !fail && q < nq) {
-            const uint32_t ob = s_hb[row];
-            if (ob > best) bidx = s_hi[row];
-            top2_merge(best, second, ob, s_hs[row]);
-            const int32_t qid = __ldg(A.bfid + q);
-            const size_t slot = (size_t)USLAM_PACK_LEVEL(qid) * A.cap + (size_t)USLAM_PACK_INDEX(qid);
-            // distance = popc(a) + 512 - 2 v
-            const uint32_t pq = __ldg(A.bfpop + q);
-            const uint32_t db = best == 0u ? 0xffffffu : pq + 512u - (uint32_t)(2.0f * __uint_as_float(best & ~255u));
-            const uint32_t ds =
-                second == 0u ? 0xffffffu : pq + 512u - (uint32_t)(2.0f * __uint_as_float(second & ~255u));
-            if (nsplit == 1u) {
-                P.a2b[slot] = (nt >= 2u && bidx >= 0 && (float)db < ratio * (float)ds) ? bidx : -1;
-            } else {
-                const size_t stride = (size_t)A.levels * A.cap;
-                *reinterpret_cast<uint4*>(P.bf_part + (split * stride + slot) * 4u) =
-                    make_uint4(db << 8, ds << 8, (uint32_t)bidx, 0u);
+            kk += (uint32_t)max(u.NT, 0);
+            if (bad) *fail = 1;
+            const uint32_t q = u.qbase + (uint32_t)(half * TC_M + row);
+            if (!bad && q < u.nq) {
+                const FrameDev& A = *u.A;
+                const int32_t qid = __ldg(A.bfid + q);
+                const size_t slot = (size_t)USLAM_PACK_LEVEL(qid) * A.cap + (size_t)USLAM_PACK_INDEX(qid);
+                // distance = popc(a) + 257 - (key >> 5), key >> 5 = widened key >> 8
+                const uint32_t pq = __ldg(A.bfpop + q);
+                const uint32_t db = best == 0u ? 0xffffffu : pq + 257u - (best >> 8);
+                const uint32_t ds = second == 0u ? 0xffffffu : pq + 257u - (second >> 8);
+                if (u.nsplit == 1u) {
+                    u.P->a2b[slot] = (u.nt >= 2u && bidx >= 0 && (float)db < ratio * (float)ds) ? bidx : -1;
+                } else {
+                    const size_t stride = (size_t)A.levels * A.cap;
+                    *reinterpret_cast<uint4*>(u.P->bf_part + (u.split * stride + slot) * 4u) =
+                        make_uint4(db << 8, ds << 8, (uint32_t)bidx, 0u);
+                }
             }
+            if (*fail) break;
         }
-        __syncthreads();  // s_hb / s_hs / s_hi are rewritten by the next unit
-    }
-    if (fail && t == 0) {
-        atomicOr(err, USLAM_ERR_TMA_TIMEOUT);
-        // drain what this thread issued, each wait bounded
-        if (pend_b & 1u) bar_wait(&bar_b[0], ph_b0);
-        if (pend_b & 2u) bar_wait(&bar_b[1], ph_b1);
-        if (pend_m & 1u) bar_wait(&bar_m[0], ph_m0);
-        if (pend_m & 2u) bar_wait(&bar_m[1], ph_m1);
     }
     fence_before();
     __syncthreads();
     fence_after();
-    if (warp == 0)
+    if (warp == TC_CONSUMERS)
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TC_TMEM_COLS) : "memory");
 }
 

@@ -1186,9 +1186,10 @@ k_describe(const FrameDev* __restrict__ frames, const SegDev* __restrict__ segs,
             if constexpr (PACK) {
                 // tensor-core operand rows of this feature (flat index f over
                 // the levels): lane j writes the FP8 values of descriptor bits
-                // 8j .. 8j + 7 (K chunk j / 2, half j % 2); lanes 0-3 write
-                // the 32-value extension row (popcount split into 16 integers
-                // <= 16, then 16 x 16.0)
+                // 8j .. 8j + 7 (8.0 or 0; K chunk j / 2, half j % 2); lanes 0-3
+                // write the 32-value extension row: the popcount split into 16
+                // integers <= 16, then 256, the row's index within its 32-row
+                // group split into two integers <= 16, then 1, then zeros
                 uint32_t f = i;
                 for (int q = 0; q < l; ++q) f += F.kept[q];
                 uint32_t wj = words[0];
@@ -1202,8 +1203,8 @@ k_describe(const FrameDev* __restrict__ frames, const SegDev* __restrict__ segs,
                 uint32_t lo = 0u, hi = 0u;
 #pragma unroll
                 for (int b = 0; b < 4; ++b) {
-                    lo |= ((bits >> b) & 1u) * (0x38u << (8 * b));
-                    hi |= ((bits >> (b + 4)) & 1u) * (0x38u << (8 * b));
+                    lo |= ((bits >> b) & 1u) * (0x50u << (8 * b));
+                    hi |= ((bits >> (b + 4)) & 1u) * (0x50u << (8 * b));
                 }
                 *reinterpret_cast<uint2*>(F.bf8 + (size_t)(f >> 3) * 2048u + (lane >> 1) * 128u + (f & 7u) * 16u +
                                           (lane & 1) * 8u) = make_uint2(lo, hi);
@@ -1212,11 +1213,13 @@ k_describe(const FrameDev* __restrict__ frames, const SegDev* __restrict__ segs,
 #pragma unroll
                     for (int k = 0; k < 8; ++k) {
                         const int e = 8 * lane + k;  // extension value index 0..31
-                        uint32_t code = 0x58u;       // 16.0
-                        if (e < 16) {
-                            const int v = min(16, max(0, (int)pc - 16 * e));
-                            code = e4m3_small_int(v);
-                        }
+                        const int grp = (int)(f & 31u);
+                        uint32_t code = 0u;
+                        if (e < 16) code = e4m3_small_int(min(16, max(0, (int)pc - 16 * e)));
+                        else if (e == 16) code = 0x78u;  // 256
+                        else if (e == 17) code = e4m3_small_int(min(grp, 16));
+                        else if (e == 18) code = e4m3_small_int(max(grp - 16, 0));
+                        else if (e == 19) code = 0x38u;  // 1
                         ext[k >> 2] |= code << (8 * (k & 3));
                     }
                     *reinterpret_cast<uint2*>(F.bfext + (size_t)(f >> 3) * 256u + (lane >> 1) * 128u + (f & 7u) * 16u +

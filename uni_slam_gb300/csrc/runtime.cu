@@ -327,18 +327,32 @@ uslam_status create_batch(uslam_ctx* ctx, int n_frames, const int* widths, const
         P.bf_splits = 1;
         P.bf_ratio = ctx->ratio;
     }
-    // Brute-force matcher: split each pair's train set so that the launch has
-    // about 8 CTAs (of 128 threads, 256 queries each) per SM.
-    // Tensor-core matcher: 128 queries per unit, one CTA per SM, about two
-    // units per SM.
+    // Both brute-force matchers take 256 queries per work unit.  Matcher 1
+    // runs about 8 CTAs per SM: split each train set until the launch has
+    // that many units.  Matcher 2 runs one CTA per SM: pick the smallest
+    // split (<= 8) whose units fill at least 95 % of whole waves over the SMs.
     std::vector<size_t> bf_off(n_pairs, 0);
     if (ctx->matcher != 0 && n_pairs > 0) {
-        const size_t per_unit = ctx->matcher == 1 ? 256 : 128;
         size_t units = 0;
         for (int p = 0; p < n_pairs; ++p)
-            units += (static_cast<size_t>(L) * std::max(b->frames[pair_prev[p]].cap, 1) + per_unit - 1) / per_unit;
-        const size_t target = static_cast<size_t>(std::max(ctx->num_sms, 1)) * (ctx->matcher == 1 ? 8 : 2);
-        const int splits = static_cast<int>(std::min<size_t>(16, std::max<size_t>(1, (target + units - 1) / units)));
+            units += (static_cast<size_t>(L) * std::max(b->frames[pair_prev[p]].cap, 1) + 255) / 256;
+        const size_t sms = static_cast<size_t>(std::max(ctx->num_sms, 1));
+        int splits = 1;
+        if (ctx->matcher == 1) {
+            const size_t target = sms * 8;
+            splits = static_cast<int>(std::min<size_t>(16, std::max<size_t>(1, (target + units - 1) / units)));
+        } else {
+            double best_eff = 0.0;
+            for (int sp = 1; sp <= 8; ++sp) {
+                const size_t u = units * static_cast<size_t>(sp);
+                const double eff = static_cast<double>(u) / static_cast<double>((u + sms - 1) / sms * sms);
+                if (eff > best_eff + 1e-9) {
+                    best_eff = eff;
+                    splits = sp;
+                }
+                if (eff >= 0.95) break;
+            }
+        }
         if (splits > 1)
             for (int p = 0; p < n_pairs; ++p) {
                 b->pairs[p].bf_splits = splits;

@@ -65,13 +65,13 @@ struct FrameDev {
     // tensor-core brute-force matcher (matcher 2; null otherwise): the frame's
     // descriptors over all levels (level-major flat order), written by
     // k_describe.  bf8 row f = 256 FP8 E4M3 values (bit k of the descriptor
-    // -> 0x38 = 1.0 or 0x00), in 8-row groups of 2048 bytes: byte k of row f
+    // -> 0x50 = 8.0 or 0x00), in 8-row groups of 2048 bytes: byte k of row f
     // at (f / 8) * 2048 + (k / 16) * 128 + (f % 8) * 16 + k % 16 (the K-major
     // no-swizzle core-matrix layout of tcgen05 operands); bfext row f = 32
-    // E4M3 values, the popcount split into 16 integers <= 16 then 16 x 16.0,
-    // in 8-row groups of 256 bytes (same layout, K = 32); bfpop[f] =
-    // popcount; bfid[f] = packed (level, index).  Rows are allocated up to a
-    // multiple of 256.
+    // E4M3 values (the popcount split into 16 integers <= 16, 256, f % 32
+    // split into two integers <= 16, 1, zeros) in 8-row groups of 256 bytes
+    // (same layout, K = 32); bfpop[f] = popcount; bfid[f] = packed (level,
+    // index).  Rows are allocated up to a multiple of 256.
     uint8_t* bf8;
     uint8_t* bfext;
     uint32_t* bfpop;
