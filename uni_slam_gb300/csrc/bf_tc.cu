@@ -20,20 +20,22 @@
 // smaller distance (distance = popc(a) + 257 - (key >> 5)), and s tells the
 // columns of a 32-column group apart.
 //
-// One persistent CTA per SM holds 512 TMEM columns: two 128 x 256 f32
-// accumulators.  A work unit is 128 queries of one pair against its train set
-// (or a share of it when the pair's train set is split): the query tile
-// (32 KB) and the train tiles (64 KB + 8 KB extension, double-buffered) are
-// staged by bulk copies; one thread issues nine tcgen05.mma (K = 32 each) per
-// train tile into one accumulator while eight warps reduce the other (two
-// warps per TMEM lane quarter, 128 columns each; tcgen05.ld, one query row
-// per thread).  The keys fit 16 bits: adding 2^23 in f32 leaves a key in the
-// low bits of the sum, a byte permute packs columns j and j + 32 of a
-// 64-column group into one register, and the top-2 runs on both halves at
-// once with max/min.u16x2 over four independent chains.  At the end of a
-// group the 16-bit keys widen to (key >> 5) << 8 | column-in-tile.  A tie on
-// the best leaves equal distances, which fail the ratio test (the rule of
-// k_bruteforce), so the result does not depend on the scan order.
+// One persistent CTA per SM holds 512 TMEM columns: two buffers of two
+// 128 x 128 f32 accumulators.  A work unit is 256 queries of one pair (one
+// accumulator per 128) against the pair's train set, or a share of it when
+// the train set is split.  A producer warp stages the query tile (64 KB) and
+// the train tiles (128 rows: 32 KB + 4 KB extension, four stages) by bulk
+// copies and issues, per train tile, nine tcgen05.mma (K = 32) into each
+// accumulator of one buffer; sixteen consumer warps (four per TMEM lane
+// quarter: accumulator x 64-column group) read the other buffer with
+// tcgen05.ld, release it, and reduce it, one query row per thread.  The keys
+// fit 16 bits: adding 2^23 in f32 leaves a key in the low bits of the sum, a
+// byte permute packs columns j and j + 32 of a 64-column group into one
+// register, and the top-2 runs on both halves at once with max/min.u16x2 over
+// four independent chains.  At the end of a group the 16-bit keys widen to
+// (key >> 5) << 8 | column-in-tile.  A tie on the best leaves equal
+// distances, which fail the ratio test (the rule of k_bruteforce), so the
+// result does not depend on the scan order.  At most 1024 pairs per launch.
 //
 // Every mbarrier wait is bounded; past the limit the kernel records
 // USLAM_ERR_TMA_TIMEOUT, drains what it issued (again bounded), frees its TMEM
@@ -47,12 +49,12 @@ namespace uslam {
 
 namespace {
 
-constexpr int TC_CONSUMERS = 8;                 // epilogue warps: two per TMEM lane quarter
+constexpr int TC_CONSUMERS = 16;                // epilogue warps: 4 per TMEM lane quarter (2 accumulators x 2 column halves)
 constexpr int TC_THREADS = 32 * (TC_CONSUMERS + 1);    // plus one producer warp
 constexpr int TC_M = 128;                       // queries per accumulator (TMEM lanes)
 constexpr int TC_Q = 2 * TC_M;                  // queries per work unit: two accumulators share each train tile
 constexpr int TC_N = 128;                       // train rows per tile
-constexpr int TC_STAGES = 3;                    // train tiles in flight
+constexpr int TC_STAGES = 4;                    // train tiles in flight
 constexpr uint32_t TC_ROW_BYTES = 256;          // 256 FP8 values per descriptor
 constexpr uint32_t TC_A_BYTES = TC_Q * TC_ROW_BYTES;   // 64 KB
 constexpr uint32_t TC_AX_BYTES = TC_M * 32;            // query-side extension (constant)
@@ -61,7 +63,7 @@ constexpr uint32_t TC_BX_BYTES = TC_N * 32;            // train-side extension r
 constexpr uint32_t TC_SMEM = TC_A_BYTES + TC_AX_BYTES + TC_STAGES * (TC_B_BYTES + TC_BX_BYTES);
 constexpr uint32_t TC_TMEM_COLS = 512;          // 2 buffers x 2 accumulators x 128 columns
 constexpr uint32_t kWaitLimit = 1u << 24;       // try_wait polls per wait
-constexpr int kMaxPairs = 4096;
+constexpr int kMaxPairs = 1024;                 // pairs per launch (the unit table lives in shared memory)
 
 __device__ __forceinline__ uint32_t saddr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -134,7 +136,18 @@ __device__ __forceinline__ void tmem_ld32_issue(uint32_t addr, uint32_t (&r)[32]
         : "r"(addr)
         : "memory");
 }
-__device__ __forceinline__ void tmem_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+// Wait for this thread's tcgen05.ld results; the registers pass through the
+// statement, so no use of them can be scheduled before the wait.
+__device__ __forceinline__ void tmem_wait(uint32_t (&r)[32]) {
+    asm volatile("tcgen05.wait::ld.sync.aligned;"
+                 : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4]), "+r"(r[5]), "+r"(r[6]), "+r"(r[7]),
+                   "+r"(r[8]), "+r"(r[9]), "+r"(r[10]), "+r"(r[11]), "+r"(r[12]), "+r"(r[13]), "+r"(r[14]),
+                   "+r"(r[15]), "+r"(r[16]), "+r"(r[17]), "+r"(r[18]), "+r"(r[19]), "+r"(r[20]), "+r"(r[21]),
+                   "+r"(r[22]), "+r"(r[23]), "+r"(r[24]), "+r"(r[25]), "+r"(r[26]), "+r"(r[27]), "+r"(r[28]),
+                   "+r"(r[29]), "+r"(r[30]), "+r"(r[31])
+                 :
+                 : "memory");
+}
 
 // Two 16-bit lanes at once: unsigned max / min per halfword.
 __device__ __forceinline__ uint32_t vmax2(uint32_t a, uint32_t b) {
@@ -163,7 +176,6 @@ __device__ __forceinline__ uint32_t widen(uint32_t k16, uint32_t base) {
 __device__ __forceinline__ uint32_t acc_key(uint32_t bits) {
     return __float_as_uint(__uint_as_float(bits) + 8388608.0f);
 }
-
 // Top-2 of keys (largest first): (b, s) <- the two largest of {b, s, b2, s2}.
 __device__ __forceinline__ void top2_merge(uint32_t& b, uint32_t& s, uint32_t b2, uint32_t s2) {
     s = max(min(b, b2), max(s, s2));
@@ -227,6 +239,8 @@ k_bf_mma(const FrameDev* __restrict__ frames, const PairDev* __restrict__ pairs,
     __shared__ uint32_t s_tmem;
     __shared__ int s_fail;
     __shared__ uint32_t s_pref[kMaxPairs + 1];
+    __shared__ uint32_t s_hb[TC_Q], s_hs[TC_Q];  // second column group's top-2 per query row
+    __shared__ int32_t s_hi[TC_Q];
     uint8_t* sA = tc_smem;
     uint8_t* sAx = sA + TC_A_BYTES;
     uint8_t* sB = sAx + TC_AX_BYTES;                   // stage s: sB + s * TC_B_BYTES
@@ -281,6 +295,11 @@ k_bf_mma(const FrameDev* __restrict__ frames, const PairDev* __restrict__ pairs,
     if (warp == TC_CONSUMERS) {
         // ------------------------------------------------ producer (one lane)
         if (lane == 0) {
+            // operand descriptors of stage 0 / query tile 0 (K-major, no swizzle)
+            const uint64_t desc_a = smem_desc(saddr(sA), 128u, 2048u);
+            const uint64_t desc_ax = smem_desc(saddr(sAx), 128u, 256u);
+            const uint64_t desc_b = smem_desc(saddr(sB), 128u, 2048u);
+            const uint64_t desc_bx = smem_desc(saddr(sBx), 128u, 256u);
             uint32_t kk = 0, units_loaded = 0;
             int64_t last_mma = -1;  // tile index of the last MMA group committed
             int64_t loaded_to = 0;  // tiles [.., loaded_to) have had their loads issued
@@ -307,28 +326,30 @@ k_bf_mma(const FrameDev* __restrict__ frames, const PairDev* __restrict__ pairs,
                     ok = bar_wait(&bar_a, units_loaded & 1u);
                     ++units_loaded;
                 }
-                for (int n = 0; n < 2 && n < u.NT && ok; ++n) ok = load_b(u, kk + (uint32_t)n, (uint32_t)n);
+                for (int n = 0; n < TC_STAGES - 1 && n < u.NT && ok; ++n) ok = load_b(u, kk + (uint32_t)n, (uint32_t)n);
                 for (int n = 0; n < u.NT && ok; ++n) {
                     const uint32_t tk = kk + (uint32_t)n, st = tk % TC_STAGES, buf = tk & 1u;
                     ok = bar_wait(&b_full[st], (tk / TC_STAGES) & 1u) &&
                          bar_wait(&acc_empty[buf], ((tk >> 1) + 1u) & 1u);
                     if (!ok) break;
                     fence_after();
-                    const uint32_t b0 = saddr(sB + st * TC_B_BYTES), bx = saddr(sBx + st * TC_BX_BYTES);
+                    // descriptor start addresses advance in 16-byte units
+                    const uint64_t db = desc_b + (uint64_t)((st * TC_B_BYTES) >> 4);
+                    const uint64_t dbx = desc_bx + (uint64_t)((st * TC_BX_BYTES) >> 4);
 #pragma unroll
                     for (int h = 0; h < 2; ++h) {
-                        const uint32_t a0 = saddr(sA + h * (TC_A_BYTES / 2));
+                        const uint64_t da = desc_a + (uint64_t)((h * (TC_A_BYTES / 2)) >> 4);
                         const uint32_t d = tmem + buf * (uint32_t)(2 * TC_N) + (uint32_t)(h * TC_N);
 #pragma unroll
-                        for (int k = 0; k < 8; ++k)
-                            mma_f8(d, smem_desc(a0 + 256u * k, 128u, 2048u), smem_desc(b0 + 256u * k, 128u, 2048u),
-                                   k > 0);
-                        mma_f8(d, smem_desc(saddr(sAx), 128u, 256u), smem_desc(bx, 128u, 256u), 1u);
+                        for (int k = 0; k < 8; ++k) mma_f8(d, da + (uint64_t)(16 * k), db + (uint64_t)(16 * k), k > 0);
+                        mma_f8(d, desc_ax, dbx, 1u);
                     }
                     mma_commit(&acc_full[buf]);
                     mma_commit(&b_empty[st]);
                     last_mma = (int64_t)tk;
-                    if (n + 2 < u.NT) ok = load_b(u, tk + 2u, (uint32_t)n + 2u);
+                    // the stage of tile tk - 1 takes tile tk + TC_STAGES - 1
+                    if (n + TC_STAGES - 1 < u.NT)
+                        ok = load_b(u, tk + (uint32_t)(TC_STAGES - 1), (uint32_t)(n + TC_STAGES - 1));
                 }
                 kk += (uint32_t)u.NT;
                 if (!ok) *fail = 1;
@@ -344,8 +365,11 @@ k_bf_mma(const FrameDev* __restrict__ frames, const PairDev* __restrict__ pairs,
         __syncwarp();
     } else {
         // ----------------------------------------------------------- consumers
-        const int quarter = warp & 3, half = warp >> 2;  // TMEM lanes, accumulator (query tile)
+        // warp w: TMEM lane quarter w % 4, accumulator (query tile) (w / 4) % 2,
+        // columns 64 (w / 8) .. + 63 of each train tile
+        const int quarter = warp & 3, half = (warp >> 2) & 1, cgrp = warp >> 3;
         const int row = 32 * quarter + lane;
+        const uint32_t s0 = (uint32_t)(64 * cgrp);  // this warp's first column in a tile
         uint32_t kk = 0;
         for (uint32_t g = blockIdx.x; g < total; g += gridDim.x) {
             const TcUnit u = tc_unit(frames, pairs, psegs, s_pref, npairs, g);
@@ -358,52 +382,64 @@ k_bf_mma(const FrameDev* __restrict__ frames, const PairDev* __restrict__ pairs,
                 fence_after();
                 // tcgen05.ld is warp-wide: a warp reads the accumulator only if
                 // every lane saw it complete
-                if (__all_sync(0xffffffffu, !bad)) {
+                const bool go = __all_sync(0xffffffffu, !bad);
+                uint32_t r0[32], r1[32];
+                if (go) {
+                    const uint32_t col = buf * (uint32_t)(2 * TC_N) + (uint32_t)(half * TC_N) + s0;
+                    const uint32_t addr = tmem + ((uint32_t)(32 * quarter) << 16) + col;
+                    tmem_ld32_issue(addr, r0);
+                    tmem_ld32_issue(addr + 32u, r1);
+                    tmem_wait(r0);
+                    tmem_wait(r1);
+                }
+                // the accumulator is read: release it to the producer
+                fence_before();
+                __syncwarp();
+                if (lane == 0) bar_arrive(&acc_empty[buf]);
+                if (go) {
                     const uint32_t base = (u.tb + (uint32_t)n) * (uint32_t)TC_N;
                     const uint32_t valid = u.nt - base < (uint32_t)TC_N ? u.nt - base : (uint32_t)TC_N;
-                    uint32_t tb = 0u, ts = 0u;  // this tile's top-2 (widened keys)
+                    uint32_t cb[4] = {0u, 0u, 0u, 0u}, cs[4] = {0u, 0u, 0u, 0u};
+                    if (valid == (uint32_t)TC_N) {
 #pragma unroll
-                    for (int c = 0; c < 2; ++c) {
-                        uint32_t r0[32], r1[32];
-                        const uint32_t col = buf * (uint32_t)(2 * TC_N) + (uint32_t)(half * TC_N + 64 * c);
-                        const uint32_t addr = tmem + ((uint32_t)(32 * quarter) << 16) + col;
-                        tmem_ld32_issue(addr, r0);
-                        tmem_ld32_issue(addr + 32u, r1);
-                        tmem_wait();
-                        const uint32_t s0 = (uint32_t)(64 * c);  // group's first column in the tile
-                        uint32_t cb[4] = {0u, 0u, 0u, 0u}, cs[4] = {0u, 0u, 0u, 0u};
-                        if (valid == (uint32_t)TC_N) {
+                        for (int j = 0; j < 32; ++j)
+                            top2x2(cb[j & 3], cs[j & 3], __byte_perm(acc_key(r0[j]), acc_key(r1[j]), 0x5410));
+                    } else {  // the last tile of the train set: columns past its end are no candidates
 #pragma unroll
-                            for (int j = 0; j < 32; ++j)
-                                top2x2(cb[j & 3], cs[j & 3], __byte_perm(acc_key(r0[j]), acc_key(r1[j]), 0x5410));
-                        } else {  // the last tile of the train set: columns past its end are no candidates
-#pragma unroll
-                            for (int j = 0; j < 32; ++j) {
-                                const uint32_t k0 = s0 + (uint32_t)j, k1 = k0 + 32u;
-                                const uint32_t lo = k0 < valid ? (acc_key(r0[j]) & 0xffffu) : 0u;
-                                const uint32_t hi = k1 < valid ? (acc_key(r1[j]) << 16) : 0u;
-                                top2x2(cb[j & 3], cs[j & 3], lo | hi);
-                            }
+                        for (int j = 0; j < 32; ++j) {
+                            const uint32_t k0 = s0 + (uint32_t)j, k1 = k0 + 32u;
+                            const uint32_t lo = k0 < valid ? (acc_key(r0[j]) & 0xffffu) : 0u;
+                            const uint32_t hi = k1 < valid ? (acc_key(r1[j]) << 16) : 0u;
+                            top2x2(cb[j & 3], cs[j & 3], lo | hi);
                         }
-                        top2x2_merge(cb[0], cs[0], cb[1], cs[1]);
-                        top2x2_merge(cb[2], cs[2], cb[3], cs[3]);
-                        top2x2_merge(cb[0], cs[0], cb[2], cs[2]);
-                        top2_merge(tb, ts, widen(cb[0] & 0xffffu, s0), widen(cs[0] & 0xffffu, s0));
-                        top2_merge(tb, ts, widen(cb[0] >> 16, s0 + 32u), widen(cs[0] >> 16, s0 + 32u));
                     }
+                    top2x2_merge(cb[0], cs[0], cb[1], cs[1]);
+                    top2x2_merge(cb[2], cs[2], cb[3], cs[3]);
+                    top2x2_merge(cb[0], cs[0], cb[2], cs[2]);
+                    uint32_t tb = widen(cb[0] & 0xffffu, s0), ts = widen(cs[0] & 0xffffu, s0);
+                    top2_merge(tb, ts, widen(cb[0] >> 16, s0 + 32u), widen(cs[0] >> 16, s0 + 32u));
                     if (tb > best) bidx = __ldg(u.B->bfid + base + (tb & 255u));
                     top2_merge(best, second, tb, ts);
                 } else {
                     bad = true;
                 }
-                fence_before();
-                __syncwarp();
-                if (lane == 0) bar_arrive(&acc_empty[buf]);
             }
             kk += (uint32_t)max(u.NT, 0);
             if (bad) *fail = 1;
-            const uint32_t q = u.qbase + (uint32_t)(half * TC_M + row);
-            if (!bad && q < u.nq) {
+            // merge the two column groups of each query row (named barrier 1:
+            // the consumer warps only)
+            const int slot_row = half * TC_M + row;
+            if (cgrp == 1) {
+                s_hb[slot_row] = best;
+                s_hs[slot_row] = second;
+                s_hi[slot_row] = bidx;
+            }
+            asm volatile("bar.sync 1, %0;" ::"r"(32 * TC_CONSUMERS) : "memory");
+            const uint32_t q = u.qbase + (uint32_t)slot_row;
+            if (cgrp == 0 && !bad && q < u.nq) {
+                const uint32_t ob = s_hb[slot_row];
+                if (ob > best) bidx = s_hi[slot_row];
+                top2_merge(best, second, ob, s_hs[slot_row]);
                 const FrameDev& A = *u.A;
                 const int32_t qid = __ldg(A.bfid + q);
                 const size_t slot = (size_t)USLAM_PACK_LEVEL(qid) * A.cap + (size_t)USLAM_PACK_INDEX(qid);
@@ -419,6 +455,7 @@ k_bf_mma(const FrameDev* __restrict__ frames, const PairDev* __restrict__ pairs,
                         make_uint4(db << 8, ds << 8, (uint32_t)bidx, 0u);
                 }
             }
+            asm volatile("bar.sync 1, %0;" ::"r"(32 * TC_CONSUMERS) : "memory");  // s_h* reused by the next unit
             if (*fail) break;
         }
     }

@@ -332,6 +332,10 @@ uslam_status create_batch(uslam_ctx* ctx, int n_frames, const int* widths, const
     // that many units.  Matcher 2 runs one CTA per SM: pick the smallest
     // split (<= 8) whose units fill at least 95 % of whole waves over the SMs.
     std::vector<size_t> bf_off(n_pairs, 0);
+    if (ctx->matcher == 2 && n_pairs > 1024) {
+        free_batch(b);
+        return set_err(&ctx->err, USLAM_CAPACITY, "batch_create: the tensor-core matcher takes at most 1024 pairs per batch");
+    }
     if (ctx->matcher != 0 && n_pairs > 0) {
         size_t units = 0;
         for (int p = 0; p < n_pairs; ++p)

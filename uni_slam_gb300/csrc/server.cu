@@ -92,6 +92,7 @@ struct uslam_server {
     FrameDev* d_frames = nullptr;
     char* arena = nullptr;
     uint32_t* d_err = nullptr;
+    uint32_t* h_err = nullptr;  // pinned: the error word as of the end of each table buffer's last launch
     int max_w = 0;
     cudaStream_t cs[2] = {nullptr, nullptr};
     LaunchBuf bufs[2];
@@ -104,6 +105,7 @@ struct uslam_server {
     uint64_t n_launches = 0, n_frames = 0;
     int max_batch_seen = 0;
     std::string fatal;  // first dispatcher failure
+    uslam_status fatal_status = USLAM_OK;
     std::mutex mu;
     std::condition_variable cv_work, cv_done;
     bool stop = false;
@@ -135,6 +137,7 @@ void free_server(uslam_server* s) {
     for (auto& c : s->cs)
         if (c) cudaStreamDestroy(c);
     if (s->arena) cudaFree(s->arena);
+    if (s->h_err) cudaFreeHost(s->h_err);
     delete s;
 }
 
@@ -241,6 +244,10 @@ cudaError_t launch_batch(uslam_server* s, const std::vector<uint64_t>& tickets, 
             cudaSuccess)
             return e;
     }
+    // the error word (kernel bounds checks, tile-load wait limits) travels
+    // with the launch and is read when the launch completes
+    if ((e = cudaMemcpyAsync(&s->h_err[bufi], s->d_err, sizeof(uint32_t), cudaMemcpyDeviceToHost, st)) != cudaSuccess)
+        return e;
     return cudaEventRecord(L->done, st);
 }
 
@@ -254,7 +261,14 @@ void dispatcher(uslam_server* s) {
             SrvLaunch& L = s->inflight.front();
             const cudaError_t q = cudaEventQuery(L.done);
             if (q == cudaErrorNotReady) break;
-            if (q != cudaSuccess && s->fatal.empty()) s->fatal = std::string("launch failed: ") + cudaGetErrorString(q);
+            if (q != cudaSuccess && s->fatal.empty()) {
+                s->fatal = std::string("launch failed: ") + cudaGetErrorString(q);
+                s->fatal_status = USLAM_CUDA_ERROR;
+            }
+            if (q == cudaSuccess && s->h_err[L.buf] != 0u && s->fatal.empty()) {
+                s->fatal = "kernel check tripped (error word " + std::to_string(s->h_err[L.buf]) + ")";
+                s->fatal_status = USLAM_KERNEL_CHECK;
+            }
             const auto now = Clock::now();
             for (uint64_t tk : L.tickets) {
                 SrvReq& r = s->reqs[tk];
@@ -285,7 +299,10 @@ void dispatcher(uslam_server* s) {
             for (uint64_t tk : batch) s->slots[s->reqs[tk].slot].producer_launch = L.id;
             if (e == cudaSuccess) e = launch_batch(s, batch, bufi, &L);
             if (e != cudaSuccess) {
-                if (s->fatal.empty()) s->fatal = std::string("launch: ") + cudaGetErrorString(e);
+                if (s->fatal.empty()) {
+                    s->fatal = std::string("launch: ") + cudaGetErrorString(e);
+                    s->fatal_status = USLAM_CUDA_ERROR;
+                }
                 if (L.done) cudaEventDestroy(L.done);
                 const auto now = Clock::now();
                 for (uint64_t tk : batch) {
@@ -481,6 +498,8 @@ uslam_status uslam_server_create(uslam_ctx* ctx, const uslam_server_params* p, u
     if (e == cudaSuccess) e = cudaMalloc(&s->d_frames, sizeof(FrameDev) * nslots);
     if (e == cudaSuccess)
         e = cudaMemcpy(s->d_frames, s->frames.data(), sizeof(FrameDev) * nslots, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaHostAlloc(&s->h_err, 2 * sizeof(uint32_t), cudaHostAllocDefault);
+    if (e == cudaSuccess) s->h_err[0] = s->h_err[1] = 0u;
     for (int b = 0; b < 2 && e == cudaSuccess; ++b) {
         s->bufs[b].bytes = tables_bytes(s->max_batch, max_tiles, max_bands, L);
         e = cudaHostAlloc(&s->bufs[b].h, s->bufs[b].bytes, cudaHostAllocDefault);
@@ -536,7 +555,7 @@ uslam_status uslam_server_submit(uslam_server* s, int stream, const uint8_t* img
     std::unique_lock<std::mutex> lk(s->mu);
     if (stream < 0 || stream >= static_cast<int>(s->streams.size()))
         return set_err(&s->ctx->err, USLAM_INVALID_ARG, "submit: unknown stream");
-    if (!s->fatal.empty()) return set_err(&s->ctx->err, USLAM_CUDA_ERROR, s->fatal);
+    if (!s->fatal.empty()) return set_err(&s->ctx->err, s->fatal_status, s->fatal);
     SrvStream& S = s->streams[stream];
     const SrvClass& C = s->classes[S.cls];
     if (pitch < C.W0) return set_err(&s->ctx->err, USLAM_INVALID_ARG, "submit: pitch smaller than the frame width");
@@ -588,7 +607,7 @@ uslam_status uslam_server_wait(uslam_server* s, uint64_t ticket, int timeout_ms)
     } else if (!s->cv_done.wait_for(lk, std::chrono::milliseconds(timeout_ms), ready)) {
         return set_err(&s->ctx->err, USLAM_TIMEOUT, "wait: request not finished in time");
     }
-    if (!s->fatal.empty()) return set_err(&s->ctx->err, USLAM_CUDA_ERROR, s->fatal);
+    if (!s->fatal.empty()) return set_err(&s->ctx->err, s->fatal_status, s->fatal);
     return USLAM_OK;
 }
 
