@@ -466,16 +466,16 @@ k_bf_mma(const FrameDev* __restrict__ frames, const PairDev* __restrict__ pairs,
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TC_TMEM_COLS) : "memory");
 }
 
+// The kernel's dynamic shared memory limit, per device: called when a batch
+// for the tensor-core matcher is created, with its device current.
+cudaError_t set_bf_mma_smem() {
+    return cudaFuncSetAttribute(k_bf_mma, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TC_SMEM);
+}
+
 cudaError_t launch_bf_mma(const FrameDev* frames, const PairDev* pairs, const SegDev* psegs, int npairs, float ratio,
                           int grid, uint32_t* err, cudaStream_t st) {
     if (npairs <= 0) return cudaSuccess;
     if (npairs > kMaxPairs) return cudaErrorInvalidValue;
-    static bool attr = false;
-    if (!attr) {
-        const cudaError_t e = cudaFuncSetAttribute(k_bf_mma, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TC_SMEM);
-        if (e != cudaSuccess) return e;
-        attr = true;
-    }
     k_bf_mma<<<grid, TC_THREADS, TC_SMEM, st>>>(frames, pairs, psegs, npairs, ratio, err);
     return cudaGetLastError();
 }

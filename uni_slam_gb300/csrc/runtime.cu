@@ -466,9 +466,10 @@ uslam_status create_batch(uslam_ctx* ctx, int n_frames, const int* widths, const
         return ctx->cuda_fail(e, "frame table upload");
     }
     e = set_compact_smem(b->max_w);
+    if (e == cudaSuccess && ctx->matcher == 2) e = set_bf_mma_smem();
     if (e != cudaSuccess) {
         free_batch(b);
-        return ctx->cuda_fail(e, "compact smem attribute");
+        return ctx->cuda_fail(e, "shared memory attribute");
     }
     // ---- programs
     std::vector<int> all_f(n_frames), all_p(n_pairs);

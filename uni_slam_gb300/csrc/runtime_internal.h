@@ -35,6 +35,7 @@ cudaError_t launch_emit(const FrameDev*, const PairDev*, const SegDev*, int, uin
 cudaError_t launch_bruteforce(const FrameDev*, const PairDev*, const SegDev*, int, float, int, cudaStream_t);
 cudaError_t launch_bf_mma(const FrameDev*, const PairDev*, const SegDev*, int, float, int, uint32_t*, cudaStream_t);
 cudaError_t set_compact_smem(int max_w);
+cudaError_t set_bf_mma_smem();
 // Tile shapes (width, height) that k_detect is instantiated for; the index
 // is the `shape` argument of launch_detect.  Every shape computes the same
 // values (the arithmetic is per pixel), so the choice affects speed only.
