@@ -1302,7 +1302,7 @@ struct CandStage {
 // candidate order: a tied best always fails the ratio test.
 __global__ void __launch_bounds__(KM_THREADS)
 k_match(const FrameDev* __restrict__ frames, const PairDev* __restrict__ pairs,
-        const MatchSegDev* __restrict__ segs, int nseg) {
+        const MatchSegDev* __restrict__ segs, int nseg, uint32_t* next_group) {
     __shared__ uint32_t s_pref[MAX_SEGS + 1];
     __shared__ uint32_t s_warp[33];
     __shared__ CandStage s_stage[KM_THREADS / 32];
@@ -1322,7 +1322,18 @@ k_match(const FrameDev* __restrict__ frames, const PairDev* __restrict__ pairs,
     const int gw = blockIdx.x * (KM_THREADS / 32) + warp;
     const int nw = gridDim.x * (KM_THREADS / 32);
     CandStage& S = s_stage[warp];
-    for (uint32_t g = gw; g < total; g += nw) {
+    // Query groups cost very different amounts (the hits in their windows).
+    // With next_group (a counter zeroed before the launch) a warp claims the
+    // next group when it finishes one; without it warps take every nw-th
+    // group.  Each group writes only its own queries' results, so the order
+    // does not change them.
+    auto claim = [&](uint32_t g) -> uint32_t {
+        if (!next_group) return g + (uint32_t)nw;
+        uint32_t n = 0;
+        if (lane == 0) n = atomicAdd(next_group, 1u);
+        return __shfl_sync(0xffffffffu, n, 0);
+    };
+    for (uint32_t g = next_group ? claim(0u) : (uint32_t)gw; g < total; g = claim(g)) {
         const int sidx = find_segment(s_pref, nseg, g);
         uint32_t grp = g - s_pref[sidx];
         const MatchSegDev sg = segs[sidx];
@@ -1577,7 +1588,10 @@ constexpr int KU_THREADS = 256;
 template <bool MUTUAL>
 __global__ void __launch_bounds__(KU_THREADS)
 k_mutual(const FrameDev* __restrict__ frames, const PairDev* __restrict__ pairs, const SegDev* __restrict__ segs,
-         uint32_t* err) {
+         uint32_t* err, uint32_t* reset_word) {
+    // k_match's group counter for its next launch on this stream (k_mutual
+    // always follows k_match, which has finished with it)
+    if (reset_word && blockIdx.x == 0 && threadIdx.x == 0) *reset_word = 0u;
     __shared__ uint32_t s_warp[33];
     const int pi = segs[blockIdx.x].frame;  // pair index
     const int l = segs[blockIdx.x].level;
@@ -1715,21 +1729,36 @@ cudaError_t launch_describe(const FrameDev* frames, const SegDev* segs, int nseg
 cudaError_t launch_match(const FrameDev* frames, const PairDev* pairs, const void* segs, int nseg, int grid,
                          cudaStream_t st) {
     if (nseg <= 0) return cudaSuccess;
-    k_match<<<grid, KM_THREADS, 0, st>>>(frames, pairs, static_cast<const MatchSegDev*>(segs), nseg);
+    k_match<<<grid, KM_THREADS, 0, st>>>(frames, pairs, static_cast<const MatchSegDev*>(segs), nseg, nullptr);
+    return cudaGetLastError();
+}
+// Dynamic distribution of the query groups: next_group (device, 4 bytes)
+// holds 0 at the launch: zero when allocated, and zeroed again by the
+// k_mutual launch that follows every k_match launch (launch_mutual_reset).
+cudaError_t launch_match_dyn(const FrameDev* frames, const PairDev* pairs, const void* segs, int nseg, int grid,
+                             uint32_t* next_group, cudaStream_t st) {
+    if (nseg <= 0) return cudaSuccess;
+    k_match<<<grid, KM_THREADS, 0, st>>>(frames, pairs, static_cast<const MatchSegDev*>(segs), nseg, next_group);
     return cudaGetLastError();
 }
 
 cudaError_t launch_mutual(const FrameDev* frames, const PairDev* pairs, const SegDev* segs, int nseg,
                           uint32_t* err, cudaStream_t st) {
     if (nseg <= 0) return cudaSuccess;
-    k_mutual<true><<<nseg, KU_THREADS, 0, st>>>(frames, pairs, segs, err);
+    k_mutual<true><<<nseg, KU_THREADS, 0, st>>>(frames, pairs, segs, err, nullptr);
+    return cudaGetLastError();
+}
+cudaError_t launch_mutual_reset(const FrameDev* frames, const PairDev* pairs, const SegDev* segs, int nseg,
+                                uint32_t* err, uint32_t* next_group, cudaStream_t st) {
+    if (nseg <= 0) return cudaSuccess;
+    k_mutual<true><<<nseg, KU_THREADS, 0, st>>>(frames, pairs, segs, err, next_group);
     return cudaGetLastError();
 }
 
 cudaError_t launch_emit(const FrameDev* frames, const PairDev* pairs, const SegDev* segs, int nseg, uint32_t* err,
                         cudaStream_t st) {
     if (nseg <= 0) return cudaSuccess;
-    k_mutual<false><<<nseg, KU_THREADS, 0, st>>>(frames, pairs, segs, err);
+    k_mutual<false><<<nseg, KU_THREADS, 0, st>>>(frames, pairs, segs, err, nullptr);
     return cudaGetLastError();
 }
 

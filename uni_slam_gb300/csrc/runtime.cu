@@ -34,6 +34,11 @@
 
 namespace {
 
+// k_match CTAs per SM in the batch path: its warps claim query groups until
+// none is left, so fewer CTAs than fit (4) leave room on every SM for the
+// kernels of another batch in flight on another stream.
+constexpr int kMatchCtasPerSm = 3;
+
 // Launch tables of one program (a subset of the batch's frames and pairs).
 struct Program {
     int ntiles = 0, nfsegs = 0, nmsegs = 0, nusegs = 0, npsegs = 0, nbands = 0;
@@ -168,9 +173,11 @@ cudaError_t enqueue_program(uslam_batch* b, const Program& P) {
             if ((e = launch_emit(b->d_frames, b->d_pairs, P.usegs, P.nusegs, b->d_err, b->stream)) != cudaSuccess)
                 return e;
         } else {
-            if ((e = launch_match(b->d_frames, b->d_pairs, P.msegs, P.nmsegs, grid, b->stream)) != cudaSuccess)
+            if ((e = launch_match_dyn(b->d_frames, b->d_pairs, P.msegs, P.nmsegs, c->num_sms * kMatchCtasPerSm,
+                                      b->d_err + 1, b->stream)) != cudaSuccess)
                 return e;
-            if ((e = launch_mutual(b->d_frames, b->d_pairs, P.usegs, P.nusegs, b->d_err, b->stream)) != cudaSuccess)
+            if ((e = launch_mutual_reset(b->d_frames, b->d_pairs, P.usegs, P.nusegs, b->d_err, b->d_err + 1,
+                                         b->stream)) != cudaSuccess)
                 return e;
         }
     }
@@ -364,7 +371,7 @@ uslam_status create_batch(uslam_ctx* ctx, int n_frames, const int* widths, const
                                                std::max(b->frames[pair_prev[p]].cap, 1) * 16);
             }
     }
-    const size_t err_off = take(&scratch, 256);
+    const size_t err_off = take(&scratch, 256);  // error word, then k_match's group counter
     const size_t frames_off = take(&scratch, sizeof(FrameDev) * n_frames);
     const size_t pairs_off = take(&scratch, sizeof(PairDev) * std::max(n_pairs, 1));
     in_bytes = round_up(in_bytes, 256);
@@ -856,11 +863,13 @@ uslam_status uslam_batch_profile(uslam_batch* b, int iters, float* kernel_ms) {
             e = c->matcher == 1 ? launch_bruteforce(b->d_frames, b->d_pairs, P.psegs, P.npsegs, c->ratio, grid, b->stream)
                 : c->matcher == 2
                     ? launch_bf_mma(b->d_frames, b->d_pairs, P.psegs, P.npsegs, c->ratio, c->num_sms, b->d_err, b->stream)
-                    : launch_match(b->d_frames, b->d_pairs, P.msegs, P.nmsegs, grid, b->stream);
+                    : launch_match_dyn(b->d_frames, b->d_pairs, P.msegs, P.nmsegs, c->num_sms * kMatchCtasPerSm,
+                                       b->d_err + 1, b->stream);
         mark();
         if (e == cudaSuccess)
             e = c->matcher != 0 ? launch_emit(b->d_frames, b->d_pairs, P.usegs, P.nusegs, b->d_err, b->stream)
-                                : launch_mutual(b->d_frames, b->d_pairs, P.usegs, P.nusegs, b->d_err, b->stream);
+                                : launch_mutual_reset(b->d_frames, b->d_pairs, P.usegs, P.nusegs, b->d_err,
+                                                      b->d_err + 1, b->stream);
         mark();
         if (e == cudaSuccess) e = cudaEventSynchronize(ev[K]);
         for (int q = 0; q < K && e == cudaSuccess; ++q) {

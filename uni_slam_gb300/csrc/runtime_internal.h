@@ -30,7 +30,10 @@ cudaError_t launch_compact_banded(const FrameDev*, const BandItem*, int, const S
 cudaError_t launch_blur_border(const FrameDev*, const SegDev*, int, int, cudaStream_t);
 cudaError_t launch_describe(const FrameDev*, const SegDev*, int, const int32_t*, int, bool, cudaStream_t);
 cudaError_t launch_match(const FrameDev*, const PairDev*, const void*, int, int, cudaStream_t);
+cudaError_t launch_match_dyn(const FrameDev*, const PairDev*, const void*, int, int, uint32_t*, cudaStream_t);
 cudaError_t launch_mutual(const FrameDev*, const PairDev*, const SegDev*, int, uint32_t*, cudaStream_t);
+cudaError_t launch_mutual_reset(const FrameDev*, const PairDev*, const SegDev*, int, uint32_t*, uint32_t*,
+                                cudaStream_t);
 cudaError_t launch_emit(const FrameDev*, const PairDev*, const SegDev*, int, uint32_t*, cudaStream_t);
 cudaError_t launch_bruteforce(const FrameDev*, const PairDev*, const SegDev*, int, float, int, cudaStream_t);
 cudaError_t launch_bf_mma(const FrameDev*, const PairDev*, const SegDev*, int, float, int, uint32_t*, cudaStream_t);
