@@ -86,3 +86,21 @@ def test_bruteforce_split_and_unsplit_agree(brief_pattern, matcher):
                     assert len(em) > 50
             finally:
                 b.close()
+
+
+def test_tensor_core_matcher_pair_limit(brief_pattern):
+    """Matcher 2 keeps its per-launch unit table in shared memory: a batch
+    with more than 1024 pairs is refused with CAPACITY at creation, and 1024
+    pairs are accepted."""
+    from uni_slam_gb300 import USlamError, capi
+
+    with Context(brief_pattern, levels=2, max_width=64, max_height=64, matcher=2, ratio=0.8) as c:
+        for n, ok in ((1024, True), (1025, False)):
+            sizes = [(64, 64)] * (n + 1)
+            pairs = [(i, i + 1) for i in range(n)]
+            if ok:
+                Batch(c, sizes, pairs).close()
+            else:
+                with pytest.raises(USlamError) as ei:
+                    Batch(c, sizes, pairs)
+                assert ei.value.status == capi.CAPACITY
