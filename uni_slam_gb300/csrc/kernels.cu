@@ -1105,11 +1105,13 @@ k_describe(const FrameDev* __restrict__ frames, const SegDev* __restrict__ segs,
     const int nw = gridDim.x * (KD_THREADS / 32);
     // A warp takes G consecutive keypoints: lane j < G first computes the
     // orientation of keypoint j, then the warp runs the 256 tests of each in
-    // turn with its position and angle broadcast from that lane.  G = 32 when
-    // the launch has enough keypoints to give every warp 32 of them, else the
-    // largest power of two that still occupies every warp (small launches).
-    uint32_t G = 32u;
-    while (G > 1u && total < G * (uint32_t)nw) G >>= 1;
+    // turn with its position and angle broadcast from that lane.  Warps take
+    // every nw-th group; k = the groups per warp at 32 keypoints each, and G
+    // (<= 32) the group size that spreads the keypoints evenly over k groups
+    // per warp, so that no warp runs a group more than the others.
+    const uint32_t per_round = 32u * (uint32_t)nw;
+    const uint32_t kq = (total + per_round - 1u) / per_round;
+    const uint32_t G = kq ? (total + kq * (uint32_t)nw - 1u) / (kq * (uint32_t)nw) : 1u;
     for (uint32_t g0 = (uint32_t)gw * G; g0 < total; g0 += (uint32_t)nw * G) {
         // orientation (generate_features.wgsl:80-99): intensity moments over
         // the r = 3 disc, summed in the reference's order, then atan2
