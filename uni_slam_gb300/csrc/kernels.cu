@@ -1,18 +1,24 @@
 // kernels.cu — sm_103a kernels of the GB300 feature front-end.
 //
-//   k_detect   (K1) pyramid level tile + FAST response + cull + blur cache
-//                   (or, in the cfg profile, FAST 9-of-16 at 20/255 + 3x3 NMS)
+//   k_pyramid       every pyramid level as f32 rows of 16-byte pitch (level 0 =
+//                   u8 / 255, levels >= 1 one bilinear tap of LOD0): the
+//                   source of k_detect's tile loads
+//   k_detect   (K1) TMA-staged level tile + halo, FAST response + cull, blur
+//                   cache (or, in the cfg profile, FAST 9-of-16 at 20/255 +
+//                   3x3 NMS)
 //   k_blur_border   blur cache beyond the level edges (BRIEF points outside)
 //   k_band_count, k_band_write
 //                   ordered keypoint compaction over 32-row bands, cap
 //   k_xsort         the matcher's lists: per horizontal band an x-sorted
 //                   candidate list, and the band-grouped query order
-//   k_describe (K2) orientation (one lane per keypoint) + 256-bit rotated
-//                   BRIEF (a warp per keypoint)
-//   k_match    (K3) windowed top-2 Hamming search, 32 x-adjacent queries of
-//                   one band per warp
+//   k_describe (K2) orientation (one lane per keypoint of a warp's group) +
+//                   256-bit rotated BRIEF (the warp's lanes take 8 tests each)
+//   k_match    (K3) windowed top-2 Hamming search; a warp claims groups of 32
+//                   x-adjacent queries of one band
 //   k_mutual        mutual cross-check and ordered match output
-//   k_bruteforce    brute-force top-2 matching (no window, no cross-check)
+//   k_bruteforce    brute-force top-2 matching (no window, no cross-check) on
+//                   the integer pipes; the tensor-core form is k_bf_mma
+//                   (bf_tc.cu)
 //
 // Arithmetic contract: binary32, round-to-nearest-even, no FMA contraction
 // (the library is compiled with --fmad=false), evaluation order as in the
