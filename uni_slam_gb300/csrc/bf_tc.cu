@@ -37,7 +37,9 @@
 // distances, which fail the ratio test (the rule of k_bruteforce), so the
 // result does not depend on the scan order.  At most 1024 pairs per launch.
 //
-// Every mbarrier wait is bounded; past the limit the kernel records
+// Every mbarrier wait is bounded (attempts that suspend the warp until the
+// phase completes or a hint expires, so waiting warps leave the issue slots
+// to the others); past the limit the kernel records
 // USLAM_ERR_TMA_TIMEOUT, drains what it issued (again bounded), frees its TMEM
 // and leaves.
 #include <cuda_runtime.h>
@@ -62,7 +64,8 @@ constexpr uint32_t TC_B_BYTES = TC_N * TC_ROW_BYTES;   // 32 KB
 constexpr uint32_t TC_BX_BYTES = TC_N * 32;            // train-side extension rows
 constexpr uint32_t TC_SMEM = TC_A_BYTES + TC_AX_BYTES + TC_STAGES * (TC_B_BYTES + TC_BX_BYTES);
 constexpr uint32_t TC_TMEM_COLS = 512;          // 2 buffers x 2 accumulators x 128 columns
-constexpr uint32_t kWaitLimit = 1u << 24;       // try_wait polls per wait
+constexpr uint32_t kWaitLimit = 1u << 16;       // try_wait attempts per wait (each suspends up to kWaitHintNs)
+constexpr uint32_t kWaitHintNs = 10000u;        // suspend-time hint of one attempt (the attempt returns at completion)
 constexpr int kMaxPairs = 1024;                 // pairs per launch (the unit table lives in shared memory)
 
 __device__ __forceinline__ uint32_t saddr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -82,10 +85,10 @@ __device__ __forceinline__ bool bar_wait(uint64_t* b, uint32_t parity) {
         uint32_t done;
         asm volatile(
             "{\n\t.reg .pred p;\n\t"
-            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
             "selp.u32 %0, 1, 0, p;\n\t}"
             : "=r"(done)
-            : "r"(a), "r"(parity)
+            : "r"(a), "r"(parity), "r"(kWaitHintNs)
             : "memory");
         if (done) return true;
     }
