@@ -39,6 +39,10 @@ namespace {
 // kernels of another batch in flight on another stream.
 constexpr int kMatchCtasPerSm = 3;
 
+// Batches of at least this many frames are captured as two halves on two
+// streams (see enqueue_split).
+constexpr int kSplitFrames = 16;
+
 // Launch tables of one program (a subset of the batch's frames and pairs).
 struct Program {
     int ntiles = 0, nfsegs = 0, nmsegs = 0, nusegs = 0, npsegs = 0, nbands = 0;
@@ -76,6 +80,12 @@ struct uslam_batch {
     cudaStream_t own_stream = nullptr;  // created with the batch
     cudaStream_t aux_stream = nullptr;  // k_blur_border's branch beside the compaction
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    // graph of a batch of >= kSplitFrames frames: two halves of the frames on
+    // two lanes (streams), so that each half's kernels fill the other's tails
+    bool split = false;
+    cudaStream_t stream2 = nullptr, aux_stream2 = nullptr;
+    cudaEvent_t ev_fork2 = nullptr, ev_join2 = nullptr, ev_start = nullptr, ev_desc = nullptr, ev_end2 = nullptr;
+    Program half[2];
     Program full;
     std::vector<Program> frame_prog;  // per frame: detect+describe only
     std::vector<Program> pair_prog;   // per pair: match only
@@ -139,49 +149,83 @@ uslam_status build_program(uslam_batch* b, const std::vector<int>& fr, const std
     return USLAM_OK;
 }
 
-// Enqueue a program's launch sequence on the batch stream.
-cudaError_t enqueue_program(uslam_batch* b, const Program& P) {
+// A lane of launches: a stream, the stream k_blur_border forks to, their
+// fork/join events, and the word k_match claims its query groups from.
+struct Lane {
+    cudaStream_t st, aux;
+    cudaEvent_t fork, join;
+    uint32_t* next_group;
+};
+
+Lane lane0(uslam_batch* b) { return Lane{b->stream, b->aux_stream, b->ev_fork, b->ev_join, b->d_err + 1}; }
+
+// The frame stages of a program: pyramid, detect, blur border, compaction, describe.
+cudaError_t enqueue_frames(uslam_batch* b, const Program& P, const Lane& ln) {
     uslam_ctx* c = b->ctx;
     cudaError_t e = cudaSuccess;
-    if (P.ntiles > 0) {
-        if ((e = launch_detect_shaped(b->d_frames, P.tiles, P.tile_begin, c->detector, b->d_err, b->stream)) != cudaSuccess)
-            return e;
-        const int grid = c->num_sms * 4;
-        // k_blur_border (the blur cache's border) and the compaction (the
-        // keypoint lists) both read only what k_detect wrote: the border runs on a
-        // forked stream beside the compaction and joins before k_describe,
-        // which needs both (in a captured graph this is a fork/join).
-        if ((e = cudaEventRecord(b->ev_fork, b->stream)) != cudaSuccess) return e;
-        if ((e = cudaStreamWaitEvent(b->aux_stream, b->ev_fork, 0)) != cudaSuccess) return e;
-        if ((e = launch_blur_border(b->d_frames, P.fsegs, P.nfsegs, grid, b->aux_stream)) != cudaSuccess) return e;
-        if ((e = cudaEventRecord(b->ev_join, b->aux_stream)) != cudaSuccess) return e;
-        if ((e = launch_compact_banded(b->d_frames, P.bands, P.nbands, P.fsegs, P.nfsegs, b->max_w, b->stream)) !=
-            cudaSuccess)
-            return e;
-        if ((e = cudaStreamWaitEvent(b->stream, b->ev_join, 0)) != cudaSuccess) return e;
-        if ((e = launch_describe(b->d_frames, P.fsegs, P.nfsegs, c->d_pattern, grid, c->matcher == 2, b->stream)) != cudaSuccess)
-            return e;
+    if (P.ntiles <= 0) return e;
+    if ((e = launch_detect_shaped(b->d_frames, P.tiles, P.tile_begin, c->detector, b->d_err, ln.st)) != cudaSuccess)
+        return e;
+    const int grid = c->num_sms * 4;
+    // k_blur_border (the blur cache's border) and the compaction (the
+    // keypoint lists) both read only what k_detect wrote: the border runs on a
+    // forked stream beside the compaction and joins before k_describe,
+    // which needs both (in a captured graph this is a fork/join).
+    if ((e = cudaEventRecord(ln.fork, ln.st)) != cudaSuccess) return e;
+    if ((e = cudaStreamWaitEvent(ln.aux, ln.fork, 0)) != cudaSuccess) return e;
+    if ((e = launch_blur_border(b->d_frames, P.fsegs, P.nfsegs, grid, ln.aux)) != cudaSuccess) return e;
+    if ((e = cudaEventRecord(ln.join, ln.aux)) != cudaSuccess) return e;
+    if ((e = launch_compact_banded(b->d_frames, P.bands, P.nbands, P.fsegs, P.nfsegs, b->max_w, ln.st)) !=
+        cudaSuccess)
+        return e;
+    if ((e = cudaStreamWaitEvent(ln.st, ln.join, 0)) != cudaSuccess) return e;
+    return launch_describe(b->d_frames, P.fsegs, P.nfsegs, c->d_pattern, grid, c->matcher == 2, ln.st);
+}
+
+// The pair stages of a program: match and the mutual check / emit.
+cudaError_t enqueue_pairs(uslam_batch* b, const Program& P, const Lane& ln) {
+    uslam_ctx* c = b->ctx;
+    cudaError_t e = cudaSuccess;
+    if (P.nmsegs <= 0) return e;
+    const int grid = c->num_sms * 4;
+    if (c->matcher != 0) {
+        if (c->matcher == 1)
+            e = launch_bruteforce(b->d_frames, b->d_pairs, P.psegs, P.npsegs, c->ratio, grid, ln.st);
+        else
+            e = launch_bf_mma(b->d_frames, b->d_pairs, P.psegs, P.npsegs, c->ratio, c->num_sms, b->d_err, ln.st);
+        if (e != cudaSuccess) return e;
+        return launch_emit(b->d_frames, b->d_pairs, P.usegs, P.nusegs, b->d_err, ln.st);
     }
-    if (P.nmsegs > 0) {
-        const int grid = c->num_sms * 4;
-        if (c->matcher != 0) {
-            if (c->matcher == 1)
-                e = launch_bruteforce(b->d_frames, b->d_pairs, P.psegs, P.npsegs, c->ratio, grid, b->stream);
-            else
-                e = launch_bf_mma(b->d_frames, b->d_pairs, P.psegs, P.npsegs, c->ratio, c->num_sms, b->d_err, b->stream);
-            if (e != cudaSuccess) return e;
-            if ((e = launch_emit(b->d_frames, b->d_pairs, P.usegs, P.nusegs, b->d_err, b->stream)) != cudaSuccess)
-                return e;
-        } else {
-            if ((e = launch_match_dyn(b->d_frames, b->d_pairs, P.msegs, P.nmsegs, c->num_sms * kMatchCtasPerSm,
-                                      b->d_err + 1, b->stream)) != cudaSuccess)
-                return e;
-            if ((e = launch_mutual_reset(b->d_frames, b->d_pairs, P.usegs, P.nusegs, b->d_err, b->d_err + 1,
-                                         b->stream)) != cudaSuccess)
-                return e;
-        }
-    }
-    return cudaSuccess;
+    if ((e = launch_match_dyn(b->d_frames, b->d_pairs, P.msegs, P.nmsegs, c->num_sms * kMatchCtasPerSm,
+                              ln.next_group, ln.st)) != cudaSuccess)
+        return e;
+    return launch_mutual_reset(b->d_frames, b->d_pairs, P.usegs, P.nusegs, b->d_err, ln.next_group, ln.st);
+}
+
+// Enqueue a program's launch sequence on the batch stream.
+cudaError_t enqueue_program(uslam_batch* b, const Program& P) {
+    const Lane ln = lane0(b);
+    cudaError_t e = enqueue_frames(b, P, ln);
+    return e == cudaSuccess ? enqueue_pairs(b, P, ln) : e;
+}
+
+// The split sequence: lane 0 runs the first half's frames then its pairs;
+// lane 1 runs the second half's frames, then waits for the first half's
+// describe (its first pair reaches into the first half) and runs its pairs.
+cudaError_t enqueue_split(uslam_batch* b) {
+    const Lane l0 = lane0(b);
+    const Lane l1{b->stream2, b->aux_stream2, b->ev_fork2, b->ev_join2, b->d_err + 2};
+    cudaError_t e = cudaEventRecord(b->ev_start, b->stream);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(b->stream2, b->ev_start, 0);
+    if (e == cudaSuccess) e = enqueue_frames(b, b->half[0], l0);
+    if (e == cudaSuccess) e = cudaEventRecord(b->ev_desc, b->stream);
+    if (e == cudaSuccess) e = enqueue_frames(b, b->half[1], l1);
+    if (e == cudaSuccess) e = enqueue_pairs(b, b->half[0], l0);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(b->stream2, b->ev_desc, 0);
+    if (e == cudaSuccess) e = enqueue_pairs(b, b->half[1], l1);
+    if (e == cudaSuccess) e = cudaEventRecord(b->ev_end2, b->stream2);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(b->stream, b->ev_end2, 0);
+    return e;
 }
 
 uslam_status capture_graph(uslam_batch* b, Program* P) {
@@ -189,7 +233,7 @@ uslam_status capture_graph(uslam_batch* b, Program* P) {
     cudaError_t e = cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal);
     if (e != cudaSuccess) return b->ctx->cuda_fail(e, "begin capture");
     e = cudaMemsetAsync(b->d_err, 0, sizeof(uint32_t), b->stream);
-    cudaError_t e2 = e == cudaSuccess ? enqueue_program(b, *P) : e;
+    cudaError_t e2 = e == cudaSuccess ? (b->split && P == &b->full ? enqueue_split(b) : enqueue_program(b, *P)) : e;
     e = cudaStreamEndCapture(b->stream, &g);
     if (e2 != cudaSuccess) {
         if (g) cudaGraphDestroy(g);
@@ -215,6 +259,10 @@ void free_batch(uslam_batch* b) {
     if (b->aux_stream) cudaStreamDestroy(b->aux_stream);
     if (b->ev_fork) cudaEventDestroy(b->ev_fork);
     if (b->ev_join) cudaEventDestroy(b->ev_join);
+    for (cudaStream_t st : {b->stream2, b->aux_stream2})
+        if (st) cudaStreamDestroy(st);
+    for (cudaEvent_t ev : {b->ev_fork2, b->ev_join2, b->ev_start, b->ev_desc, b->ev_end2})
+        if (ev) cudaEventDestroy(ev);
     if (b->arena) cudaFree(b->arena);
     if (b->d_tables) cudaFree(b->d_tables);
     if (b->h_in) cudaFreeHost(b->h_in);
@@ -489,6 +537,30 @@ uslam_status create_batch(uslam_ctx* ctx, int n_frames, const int* widths, const
         return s;
     }
     progs.push_back(&b->full);
+    // (not with matcher 1: its launches are each sized to fill the GPU, and two
+    // of them side by side ran the stress step 15 % slower)
+    if (n_frames >= kSplitFrames && !per_item_programs && ctx->matcher != 1) {
+        // first half: frames [0, m) and the pairs within them; second half: the rest
+        const int m = n_frames / 2;
+        std::vector<int> fa, fb, pa, pb;
+        for (int f = 0; f < n_frames; ++f) (f < m ? fa : fb).push_back(f);
+        for (int p = 0; p < n_pairs; ++p) (pair_prev[p] < m && pair_curr[p] < m ? pa : pb).push_back(p);
+        if ((s = build_program(b, fa, pa, &b->half[0])) != USLAM_OK || (s = build_program(b, fb, pb, &b->half[1])) != USLAM_OK) {
+            free_batch(b);
+            return s;
+        }
+        progs.push_back(&b->half[0]);
+        progs.push_back(&b->half[1]);
+        e = cudaStreamCreateWithFlags(&b->stream2, cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->aux_stream2, cudaStreamNonBlocking);
+        for (cudaEvent_t* ev : {&b->ev_fork2, &b->ev_join2, &b->ev_start, &b->ev_desc, &b->ev_end2})
+            if (e == cudaSuccess) e = cudaEventCreateWithFlags(ev, cudaEventDisableTiming);
+        if (e != cudaSuccess) {
+            free_batch(b);
+            return ctx->cuda_fail(e, "stream create");
+        }
+        b->split = true;
+    }
     if (per_item_programs) {
         b->frame_prog.resize(n_frames);
         b->pair_prog.resize(n_pairs);
