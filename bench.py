@@ -44,10 +44,11 @@ W, H, LEVELS = 752, 480, 6
 STRESS_W, STRESS_H, STRESS_LEVELS, STRESS_CAP = 3840, 2160, 8, 2500
 POPC_PER_SM_CLK = 16  # 32-bit population count results per SM per clock (documented issue rate)
 POPC_PER_DISTANCE = 4  # carry-save-adder Hamming distance of 256 bits
-# kernels of one graph replay of the uniform batch (one tile shape): k_pyramid,
-# k_detect, k_blur_border, k_band_count, k_band_write, k_xsort, k_describe,
-# k_match, k_mutual
-KERNELS_PER_STEP = 9
+# kernels of one graph replay of the uniform batch (one tile shape), which the
+# runtime captures as two halves of the frames on two streams: per half
+# k_pyramid, k_detect, k_blur_border, k_band_count, k_band_write, k_xsort,
+# k_describe, k_match, k_mutual
+KERNELS_PER_STEP = 18
 # batches in flight in the pipelined end-to-end measurement
 E2E_DEPTH = 3
 METRIC = "frames/s detect+describe+match @752x480 (batched, 64-frame graph)"
