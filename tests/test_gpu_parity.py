@@ -223,8 +223,9 @@ def test_frontend_rotation_matches_reference_rule(ctx, brief_pattern):
 
 
 def test_large_batch_bit_exact(ctx, brief_pattern):
-    """22 frames (~170k keypoints): enough keypoints per launch that k_describe
-    gives every warp 32 keypoints (smaller tests use smaller groups)."""
+    """22 frames (~170k keypoints, larger describe groups than the small
+    tests), captured as two halves on two streams: every frame's features and
+    a pair within the second half equal the oracle."""
     frames = synth.plane_sequence(77, n=22)
     b = _run(ctx, frames, [(i, i + 1) for i in range(len(frames) - 1)])
     try:
@@ -239,3 +240,30 @@ def test_large_batch_bit_exact(ctx, brief_pattern):
         assert np.array_equal(_mm(b.matches(20)), em)
     finally:
         b.close()
+
+
+@pytest.mark.parametrize("matcher", [0, 2])
+def test_split_batch_pairs_across_halves(brief_pattern, matcher):
+    """A batch of 20 frames is captured as two halves (frames 0-9 and 10-19)
+    on two streams.  Pairs within either half, from the first half into the
+    second and from the second back into the first all equal the oracle, with
+    the windowed matcher and with the tensor-core brute-force matcher."""
+    W, H = 320, 240
+    frames = [synth.scene_frame(300 + k, W, H) for k in range(20)]
+    pairs = [(0, 1), (3, 12), (15, 2), (10, 11), (19, 0), (9, 10), (8, 9), (12, 19)]
+    with Context(brief_pattern, levels=6, max_width=W, max_height=H, matcher=matcher, ratio=0.8) as c:
+        b = Batch(c, [(W, H)] * len(frames), pairs)
+        try:
+            b.process(frames)
+            exp = [oracle.frame(f, brief_pattern) for f in frames]
+            for i in range(len(frames)):
+                _assert_features_equal(b.features(i), exp[i])
+            for k, (p, q) in enumerate(pairs):
+                if matcher == 0:
+                    em = oracle.match(exp[p][0], exp[p][1], exp[q][0], exp[q][1], W, H)
+                else:
+                    em = oracle.match_bruteforce(exp[p][0], exp[p][1], exp[q][0], exp[q][1], 0.8)
+                assert np.array_equal(_mm(b.matches(k)), em), (matcher, k, p, q)
+            assert sum(len(b.matches(k)) for k in range(len(pairs))) > 50
+        finally:
+            b.close()
