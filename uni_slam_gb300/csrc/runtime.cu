@@ -34,10 +34,12 @@
 
 namespace {
 
-// k_match CTAs per SM in the batch path: its warps claim query groups until
-// none is left, so fewer CTAs than fit (4) leave room on every SM for the
-// kernels of another batch in flight on another stream.
-constexpr int kMatchCtasPerSm = 3;
+// k_match CTAs per SM in the batch path (all that fit).  Its warps claim
+// query groups until none is left.  With one stream, 3 CTAs per SM left room
+// for a second batch in flight and measured better end to end; with the
+// two-half graph (kSplitFrames) the halves fill each other's gaps and 4 is
+// better on every measure.
+constexpr int kMatchCtasPerSm = 4;
 
 // Batches of at least this many frames are captured as two halves on two
 // streams (see enqueue_split).
