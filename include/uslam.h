@@ -250,7 +250,8 @@ uslam_status uslam_batch_upload(uslam_batch* b);
 uslam_status uslam_batch_set_frame(uslam_batch* b, int frame, const uint8_t* img, int pitch);
 /* Launch detect + describe of every frame and match of every pair (one CUDA
  * graph replay: about nine kernel launches for the whole batch, whatever its
- * size). Asynchronous. */
+ * size; a batch of 16 or more frames runs them once for each half of its
+ * frames, the halves side by side on two streams). Asynchronous. */
 uslam_status uslam_batch_run(uslam_batch* b);
 /* Asynchronous device->host copy of every frame's features and every pair's
  * matches into pinned staging (read them with the getters below). */
