@@ -34,6 +34,8 @@
 
 namespace {
 
+constexpr int kLanes = 2;  // parts of a split batch graph (3 measured no better)
+
 // k_match CTAs per SM in the batch path (all that fit).  Its warps claim
 // query groups until none is left.  With one stream, 3 CTAs per SM left room
 // for a second batch in flight and measured better end to end; with the
@@ -41,8 +43,8 @@ namespace {
 // better on every measure.
 constexpr int kMatchCtasPerSm = 4;
 
-// Batches of at least this many frames are captured as two halves on two
-// streams (see enqueue_split).
+// Batches of at least this many frames are captured as kLanes parts of their
+// frames on as many streams (see enqueue_split).
 constexpr int kSplitFrames = 16;
 
 // Launch tables of one program (a subset of the batch's frames and pairs).
@@ -82,12 +84,13 @@ struct uslam_batch {
     cudaStream_t own_stream = nullptr;  // created with the batch
     cudaStream_t aux_stream = nullptr;  // k_blur_border's branch beside the compaction
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
-    // graph of a batch of >= kSplitFrames frames: two halves of the frames on
-    // two lanes (streams), so that each half's kernels fill the other's tails
-    bool split = false;
-    cudaStream_t stream2 = nullptr, aux_stream2 = nullptr;
-    cudaEvent_t ev_fork2 = nullptr, ev_join2 = nullptr, ev_start = nullptr, ev_desc = nullptr, ev_end2 = nullptr;
-    Program half[2];
+    // graph of a batch of >= kSplitFrames frames: kLanes parts of the frames on
+    // as many lanes (streams), so that each part's kernels fill the others' tails
+    int nparts = 0;
+    Program part[kLanes];
+    cudaStream_t lane_st[kLanes] = {}, lane_aux[kLanes] = {};  // lane 0 uses the batch's own streams
+    cudaEvent_t lane_fork[kLanes] = {}, lane_join[kLanes] = {}, lane_desc[kLanes] = {}, lane_end[kLanes] = {};
+    cudaEvent_t ev_start = nullptr;
     Program full;
     std::vector<Program> frame_prog;  // per frame: detect+describe only
     std::vector<Program> pair_prog;   // per pair: match only
@@ -211,22 +214,27 @@ cudaError_t enqueue_program(uslam_batch* b, const Program& P) {
     return e == cudaSuccess ? enqueue_pairs(b, P, ln) : e;
 }
 
-// The split sequence: lane 0 runs the first half's frames then its pairs;
-// lane 1 runs the second half's frames, then waits for the first half's
-// describe (its first pair reaches into the first half) and runs its pairs.
+// The split sequence: lane j runs part j's frames, records that its describe
+// is done, then waits for the earlier lanes' describe (its pairs may reach
+// into their frames) and runs its pairs; lane 0 joins the others at the end.
 cudaError_t enqueue_split(uslam_batch* b) {
-    const Lane l0 = lane0(b);
-    const Lane l1{b->stream2, b->aux_stream2, b->ev_fork2, b->ev_join2, b->d_err + 2};
+    const int K = b->nparts;
+    Lane ln[kLanes];
+    for (int j = 0; j < K; ++j)
+        ln[j] = j == 0 ? lane0(b)
+                       : Lane{b->lane_st[j], b->lane_aux[j], b->lane_fork[j], b->lane_join[j], b->d_err + 1 + j};
     cudaError_t e = cudaEventRecord(b->ev_start, b->stream);
-    if (e == cudaSuccess) e = cudaStreamWaitEvent(b->stream2, b->ev_start, 0);
-    if (e == cudaSuccess) e = enqueue_frames(b, b->half[0], l0);
-    if (e == cudaSuccess) e = cudaEventRecord(b->ev_desc, b->stream);
-    if (e == cudaSuccess) e = enqueue_frames(b, b->half[1], l1);
-    if (e == cudaSuccess) e = enqueue_pairs(b, b->half[0], l0);
-    if (e == cudaSuccess) e = cudaStreamWaitEvent(b->stream2, b->ev_desc, 0);
-    if (e == cudaSuccess) e = enqueue_pairs(b, b->half[1], l1);
-    if (e == cudaSuccess) e = cudaEventRecord(b->ev_end2, b->stream2);
-    if (e == cudaSuccess) e = cudaStreamWaitEvent(b->stream, b->ev_end2, 0);
+    for (int j = 1; j < K && e == cudaSuccess; ++j) e = cudaStreamWaitEvent(ln[j].st, b->ev_start, 0);
+    for (int j = 0; j < K && e == cudaSuccess; ++j) {
+        e = enqueue_frames(b, b->part[j], ln[j]);
+        if (e == cudaSuccess) e = cudaEventRecord(b->lane_desc[j], ln[j].st);
+    }
+    for (int j = 0; j < K && e == cudaSuccess; ++j) {
+        for (int i = 0; i < j && e == cudaSuccess; ++i) e = cudaStreamWaitEvent(ln[j].st, b->lane_desc[i], 0);
+        if (e == cudaSuccess) e = enqueue_pairs(b, b->part[j], ln[j]);
+        if (e == cudaSuccess && j > 0) e = cudaEventRecord(b->lane_end[j], ln[j].st);
+    }
+    for (int j = 1; j < K && e == cudaSuccess; ++j) e = cudaStreamWaitEvent(b->stream, b->lane_end[j], 0);
     return e;
 }
 
@@ -235,7 +243,7 @@ uslam_status capture_graph(uslam_batch* b, Program* P) {
     cudaError_t e = cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal);
     if (e != cudaSuccess) return b->ctx->cuda_fail(e, "begin capture");
     e = cudaMemsetAsync(b->d_err, 0, sizeof(uint32_t), b->stream);
-    cudaError_t e2 = e == cudaSuccess ? (b->split && P == &b->full ? enqueue_split(b) : enqueue_program(b, *P)) : e;
+    cudaError_t e2 = e == cudaSuccess ? (b->nparts > 1 && P == &b->full ? enqueue_split(b) : enqueue_program(b, *P)) : e;
     e = cudaStreamEndCapture(b->stream, &g);
     if (e2 != cudaSuccess) {
         if (g) cudaGraphDestroy(g);
@@ -261,10 +269,13 @@ void free_batch(uslam_batch* b) {
     if (b->aux_stream) cudaStreamDestroy(b->aux_stream);
     if (b->ev_fork) cudaEventDestroy(b->ev_fork);
     if (b->ev_join) cudaEventDestroy(b->ev_join);
-    for (cudaStream_t st : {b->stream2, b->aux_stream2})
-        if (st) cudaStreamDestroy(st);
-    for (cudaEvent_t ev : {b->ev_fork2, b->ev_join2, b->ev_start, b->ev_desc, b->ev_end2})
-        if (ev) cudaEventDestroy(ev);
+    for (int j = 0; j < kLanes; ++j) {
+        for (cudaStream_t st : {b->lane_st[j], b->lane_aux[j]})
+            if (st) cudaStreamDestroy(st);
+        for (cudaEvent_t ev : {b->lane_fork[j], b->lane_join[j], b->lane_desc[j], b->lane_end[j]})
+            if (ev) cudaEventDestroy(ev);
+    }
+    if (b->ev_start) cudaEventDestroy(b->ev_start);
     if (b->arena) cudaFree(b->arena);
     if (b->d_tables) cudaFree(b->d_tables);
     if (b->h_in) cudaFreeHost(b->h_in);
@@ -542,26 +553,33 @@ uslam_status create_batch(uslam_ctx* ctx, int n_frames, const int* widths, const
     // (not with matcher 1: its launches are each sized to fill the GPU, and two
     // of them side by side ran the stress step 15 % slower)
     if (n_frames >= kSplitFrames && !per_item_programs && ctx->matcher != 1) {
-        // first half: frames [0, m) and the pairs within them; second half: the rest
-        const int m = n_frames / 2;
-        std::vector<int> fa, fb, pa, pb;
-        for (int f = 0; f < n_frames; ++f) (f < m ? fa : fb).push_back(f);
-        for (int p = 0; p < n_pairs; ++p) (pair_prev[p] < m && pair_curr[p] < m ? pa : pb).push_back(p);
-        if ((s = build_program(b, fa, pa, &b->half[0])) != USLAM_OK || (s = build_program(b, fb, pb, &b->half[1])) != USLAM_OK) {
-            free_batch(b);
-            return s;
+        // part j: frames [j n / K, (j + 1) n / K) and the pairs whose later frame lies there
+        const int K = kLanes;
+        auto part_of = [&](int f) { return static_cast<int>(static_cast<long long>(f) * K / n_frames); };
+        std::vector<int> fr[kLanes], pr[kLanes];
+        for (int f = 0; f < n_frames; ++f) fr[part_of(f)].push_back(f);
+        for (int p = 0; p < n_pairs; ++p) pr[std::max(part_of(pair_prev[p]), part_of(pair_curr[p]))].push_back(p);
+        for (int j = 0; j < K; ++j) {
+            if ((s = build_program(b, fr[j], pr[j], &b->part[j])) != USLAM_OK) {
+                free_batch(b);
+                return s;
+            }
+            progs.push_back(&b->part[j]);
         }
-        progs.push_back(&b->half[0]);
-        progs.push_back(&b->half[1]);
-        e = cudaStreamCreateWithFlags(&b->stream2, cudaStreamNonBlocking);
-        if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->aux_stream2, cudaStreamNonBlocking);
-        for (cudaEvent_t* ev : {&b->ev_fork2, &b->ev_join2, &b->ev_start, &b->ev_desc, &b->ev_end2})
-            if (e == cudaSuccess) e = cudaEventCreateWithFlags(ev, cudaEventDisableTiming);
+        e = cudaEventCreateWithFlags(&b->ev_start, cudaEventDisableTiming);
+        for (int j = 0; j < K && e == cudaSuccess; ++j) {
+            if (j > 0) {
+                e = cudaStreamCreateWithFlags(&b->lane_st[j], cudaStreamNonBlocking);
+                if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->lane_aux[j], cudaStreamNonBlocking);
+            }
+            for (cudaEvent_t* ev : {&b->lane_fork[j], &b->lane_join[j], &b->lane_desc[j], &b->lane_end[j]})
+                if (e == cudaSuccess) e = cudaEventCreateWithFlags(ev, cudaEventDisableTiming);
+        }
         if (e != cudaSuccess) {
             free_batch(b);
             return ctx->cuda_fail(e, "stream create");
         }
-        b->split = true;
+        b->nparts = K;
     }
     if (per_item_programs) {
         b->frame_prog.resize(n_frames);
