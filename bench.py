@@ -85,23 +85,27 @@ def _dist():
 # ------------------------------------------------------------------ clocks
 
 class ClockSampler:
-    """nvidia-smi samples of SM clock and throttle reasons during a region."""
+    """nvidia-smi samples of SM clock and throttle reasons during a region.
+    A timed region shorter than the sampling interval is padded by the
+    caller with the same work before and after it (wait_samples), so that
+    every sample is taken under that load."""
 
     FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
               "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
               "clocks_event_reasons.sw_power_cap")
+    INTERVAL_MS = 100
 
-    def __init__(self, index: int):
+    def __init__(self, index: int, cmd: list[str] | None = None):
         self.index = index
+        self.cmd = cmd or ["nvidia-smi", "-i", str(index), f"--query-gpu={self.FIELDS}",
+                           "--format=csv,noheader,nounits", "-lms", str(self.INTERVAL_MS)]
         self.proc = None
         self.lines = []
         self.thread = None
 
     def start(self):
         try:
-            self.proc = subprocess.Popen(
-                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
-                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.proc = subprocess.Popen(self.cmd, stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         except (OSError, ValueError):
             self.proc = None
             return
@@ -112,9 +116,20 @@ class ClockSampler:
         for line in self.proc.stdout:
             self.lines.append(line.strip())
 
+    @property
+    def running(self) -> bool:
+        return self.proc is not None and self.proc.poll() is None
+
+    def wait_samples(self, n: int, busy, limit_s: float = 3.0):
+        """Call busy() (a short burst of the measured work) until n more
+        samples have arrived or limit_s has passed."""
+        target = len(self.lines) + n
+        t0 = time.perf_counter()
+        while self.running and len(self.lines) < target and time.perf_counter() - t0 < limit_s:
+            busy()
+
     def stop(self) -> dict:
         if self.proc is not None:
-            time.sleep(0.25)
             self.proc.terminate()
             try:
                 self.proc.wait(timeout=5)
@@ -882,9 +897,17 @@ def run_ours(a):
         batch.run()
     stream.synchronize()
     evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(a.steps)]
+    def busy():  # untimed steps of the same work, to hold the load while clocks are sampled
+        with torch.cuda.stream(stream):
+            for _ in range(4):
+                l2_flush.zero_()
+                batch.run()
+        stream.synchronize()
+
     clocks = ClockSampler(local)
-    barrier()
     clocks.start()
+    clocks.wait_samples(2, busy)  # the sampler is up and reporting under this load
+    barrier()
     t_wall = time.perf_counter()
     with torch.cuda.stream(stream):
         for e0, e1 in evs:
@@ -895,7 +918,10 @@ def run_ours(a):
     stream.synchronize()
     barrier()
     wall_s = time.perf_counter() - t_wall
+    clocks.wait_samples(1, busy)  # one more sample under the same load after the region
     clk = clocks.stop()
+    clk["window"] = (f"nvidia-smi every {ClockSampler.INTERVAL_MS} ms; the timed region is padded before and after "
+                     "with untimed steps of the same work, so every sample is under this load")
     step_ms = sum(e0.elapsed_time(e1) for e0, e1 in evs) / a.steps
     step_ms_max = reduce_max(step_ms, dist, "cuda")
     value = n * world / (step_ms_max / 1e3)

@@ -1,10 +1,12 @@
 """Host-side logic of bench.py: the max-over-ranks reduction across two
-gloo ranks on CPU, the clock-log summary, the byte model, and the reference
-arm (CPU restatement on a process pool) end to end on a small workload."""
+gloo ranks on CPU, the clock-log summary and the sampler's bounded padding,
+the byte model, and the reference arm (CPU restatement on a process pool)
+end to end on a small workload."""
 import json
 import os
 import subprocess
 import sys
+import time
 
 import pytest
 import torch.distributed as dist
@@ -45,6 +47,37 @@ def test_clock_summary_flags_throttle_reasons():
              "2070, 2070, 1200.0, Not Active, Not Active, Not Active, Not Active", "garbage"]
     c = bench.summarize_clocks(lines)
     assert c["sm_mhz"] == 2070 and c["sm_max_mhz"] == 2070 and c["reasons"] == ["sw_power_cap"] and c["samples"] == 3
+
+
+def test_clock_sampler_padding_is_bounded(tmp_path):
+    fake = tmp_path / "fake_smi.py"
+    fake.write_text("import sys, time\n"
+                    "for _ in range(200):\n"
+                    "    print('2070, 2070, 1000.0, Not Active, Not Active, Not Active, Not Active', flush=True)\n"
+                    "    time.sleep(0.05)\n")
+    calls = []
+
+    def busy():
+        calls.append(1)
+        time.sleep(0.01)
+
+    c = bench.ClockSampler(0, cmd=[sys.executable, str(fake)])
+    c.start()
+    c.wait_samples(2, busy)
+    n0 = len(c.lines)
+    c.wait_samples(1, busy)
+    out = c.stop()
+    assert n0 >= 2 and len(c.lines) >= n0 + 1 and calls
+    assert out["samples"] >= 3 and out["sm_mhz"] == 2070 and out["reasons"] == []
+    # no sampler (missing tool or one that exits at once): the padding returns without waiting
+    for cmd in (["/nonexistent/nvidia-smi"], [sys.executable, "-c", "pass"]):
+        c = bench.ClockSampler(0, cmd=cmd)
+        c.start()
+        time.sleep(0.2)
+        t0 = time.perf_counter()
+        c.wait_samples(2, busy)
+        assert time.perf_counter() - t0 < 0.5
+        assert c.stop()["samples"] == 0
 
 
 def test_byte_model():
