@@ -184,6 +184,26 @@ def test_constant_and_tiny_frames(brief_pattern):
             b.close()
 
 
+def test_widest_tallest_frames_and_most_levels(brief_pattern):
+    """The largest frame width the context accepts (8192) and a frame of that
+    height, each as a warped pair, with the most pyramid levels (12; level 11
+    is 1102 x 12 or 12 x 1102): bit-exact against the oracle."""
+    with Context(brief_pattern, levels=12, max_width=8192, max_height=8192) as c:
+        frames = list(synth.warped_pair(21, 8192, 96)) + list(synth.warped_pair(22, 96, 8192))
+        b = _run(c, frames, [(0, 1), (2, 3)])
+        try:
+            for k, (w, h) in enumerate([(8192, 96), (96, 8192)]):
+                exp = [oracle.frame(frames[2 * k + j], brief_pattern, levels=12) for j in range(2)]
+                for j in range(2):
+                    _assert_features_equal(b.features(2 * k + j), exp[j])
+                    assert exp[j][1][11] > 0, "no feature on the smallest level"
+                em = oracle.match(exp[0][0], exp[0][1], exp[1][0], exp[1][1], w, h)
+                assert len(em) > 0
+                assert np.array_equal(_mm(b.matches(k)), em), f"pair {k} {w}x{h}"
+        finally:
+            b.close()
+
+
 def test_cap_keeps_first_in_yx_order(brief_pattern):
     f1, _ = synth.warped_pair(4)
     with Context(brief_pattern, levels=6, max_width=752, max_height=480, cap_per_level=100) as c:
