@@ -88,6 +88,48 @@ def test_bruteforce_split_and_unsplit_agree(brief_pattern, matcher):
                 b.close()
 
 
+@pytest.mark.parametrize("matcher", [0, 1, 2])
+def test_single_feature_sets(brief_pattern, matcher):
+    """Frames with exactly one feature (one bright pixel on a flat frame: at
+    (297, 262) it survives on level 0 only, at (579, 137) on level 1 only):
+    a train set or pool of one feature gives no match (fewer than two,
+    match_features_cpu.cpp:80-82), and a single query finds its own feature
+    in a train set of two.  For matcher 2 the train rows sit in a 128-row tile
+    whose other rows are not features."""
+    W, H = 640, 480
+    one_a = np.full((H, W), 128, np.uint8)
+    one_a[262, 297] = 255
+    one_b = np.full((H, W), 128, np.uint8)
+    one_b[137, 579] = 255
+    full = synth.scene_frame(9, W, H)
+    two = one_a.copy()  # both pixels: both features
+    two[137, 579] = 255
+    frames = [one_a, one_b, full, two]
+    pairs = [(0, 2), (2, 0), (0, 1), (1, 0), (2, 1), (0, 3), (3, 0)]
+    with Context(brief_pattern, levels=6, max_width=W, max_height=H, matcher=matcher, ratio=0.8) as c:
+        b = Batch(c, [(W, H)] * len(frames), pairs)
+        try:
+            b.process(frames)
+            exp = [oracle.frame(f, brief_pattern) for f in frames]
+            assert exp[0][1].tolist() == [1, 0, 0, 0, 0, 0] and exp[1][1].tolist() == [0, 1, 0, 0, 0, 0]
+            assert exp[3][1].tolist() == [1, 1, 0, 0, 0, 0]
+            for i in range(len(frames)):
+                gf, gk, _ = b.features(i)
+                assert gf.tobytes() == exp[i][0].tobytes() and np.array_equal(gk, exp[i][1])
+            for k, (p, q) in enumerate(pairs):
+                if matcher == 0:
+                    em = oracle.match(exp[p][0], exp[p][1], exp[q][0], exp[q][1], W, H)
+                else:
+                    em = oracle.match_bruteforce(exp[p][0], exp[p][1], exp[q][0], exp[q][1], 0.8)
+                    if len(exp[q][0]) < 2:
+                        assert len(em) == 0
+                assert np.array_equal(_mm(b.matches(k)), em), f"pair {k}"
+            if matcher != 0:  # the single query finds itself among two train features
+                assert len(_mm(b.matches(5))) == 1
+        finally:
+            b.close()
+
+
 def test_tensor_core_matcher_pair_limit(brief_pattern):
     """Matcher 2 keeps its per-launch unit table in shared memory: a batch
     with more than 1024 pairs is refused with CAPACITY at creation, and 1024
