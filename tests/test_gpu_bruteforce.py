@@ -130,6 +130,48 @@ def test_single_feature_sets(brief_pattern, matcher):
             b.close()
 
 
+@pytest.mark.parametrize("matcher", [0, 1, 2])
+def test_tied_best_is_rejected(brief_pattern, matcher):
+    """Exact ties: frame B1 holds two features whose descriptors both equal
+    the single feature of frame A (bright pixels at (297, 262) and (315, 262)
+    on a flat frame), so a query for that descriptor meets two candidates at
+    distance 0 and the ratio test rejects it (best == second;
+    match_features_cpu.cpp:128-141).  B2 (second pixel at (324, 262)) has a
+    different second descriptor and matches.  All 12 ordered pairs of
+    A, B1, B2 and C (A plus a far feature) equal the oracle."""
+    W, H = 640, 480
+    base = np.full((H, W), 128, np.uint8)
+    base[262, 297] = 255
+    b1, b2, cc = base.copy(), base.copy(), base.copy()
+    b1[262, 315] = 255
+    b2[262, 324] = 255
+    cc[137, 579] = 255
+    frames = [base, b1, b2, cc]
+    pairs = [(p, q) for p in range(4) for q in range(4) if p != q]
+    with Context(brief_pattern, levels=6, max_width=W, max_height=H, matcher=matcher, ratio=0.8) as c:
+        b = Batch(c, [(W, H)] * len(frames), pairs)
+        try:
+            b.process(frames)
+            exp = [oracle.frame(f, brief_pattern) for f in frames]
+            d = exp[1][0]["descriptor"]
+            assert exp[1][1].tolist() == [2, 0, 0, 0, 0, 0] and (d == exp[0][0]["descriptor"][0]).all()
+            got = {}
+            for k, (p, q) in enumerate(pairs):
+                if matcher == 0:
+                    em = oracle.match(exp[p][0], exp[p][1], exp[q][0], exp[q][1], W, H)
+                else:
+                    em = oracle.match_bruteforce(exp[p][0], exp[p][1], exp[q][0], exp[q][1], 0.8)
+                g = _mm(b.matches(k))
+                assert np.array_equal(g, em), f"pair {p}->{q}"
+                got[(p, q)] = len(g)
+            if matcher == 0:  # C -> B1 tied (no mutual pair), C -> B2 not
+                assert got[(3, 1)] == 0 and got[(3, 2)] == 1
+            else:  # A -> B1 tied, A -> B2 not
+                assert got[(0, 1)] == 0 and got[(0, 2)] == 1
+        finally:
+            b.close()
+
+
 def test_tensor_core_matcher_pair_limit(brief_pattern):
     """Matcher 2 keeps its per-launch unit table in shared memory: a batch
     with more than 1024 pairs is refused with CAPACITY at creation, and 1024
