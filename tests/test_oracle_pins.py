@@ -67,3 +67,30 @@ def test_matcher_against_compiled_reference_live(size):
         exp = ref(fa, ka, fb, kb)
         got = oracle.match(fa, ka, fb, kb, *size)
         assert np.array_equal(got, exp), f"trial {trial}"
+
+
+@pytest.mark.parametrize("d1,d2,expected", [(17, 20, 0), (16, 19, 1), (0, 0, 0)])
+def test_matcher_ratio_boundary(d1, d2, expected):
+    """Planted distances at the f32 Lowe-ratio boundary: 0.85f * 20 is
+    exactly 17.0f, so 17 vs 20 is rejected and 16 vs 19 accepted; a tie at 0
+    is rejected.  The oracle, and the compiled reference where present."""
+    rs = np.random.RandomState(d1 + 100)
+    D = rs.randint(0, 2**32, size=8, dtype=np.uint64).astype(np.uint32)
+
+    def flip(n):
+        bits = np.unpackbits(D.view(np.uint8), bitorder="little")
+        bits[rs.choice(256, n, replace=False)] ^= 1
+        return np.packbits(bits, bitorder="little").view("<u4")
+
+    fa = np.zeros(2, oracle.FEATURE_DTYPE)
+    fa["x"], fa["y"], fa["strength"] = [100, 600], [100, 400], 12
+    fa["descriptor"][0], fa["descriptor"][1] = D, ~D
+    fb = np.zeros(2, oracle.FEATURE_DTYPE)
+    fb["x"], fb["y"], fb["strength"] = [102, 110], [101, 104], 12
+    fb["descriptor"][0], fb["descriptor"][1] = flip(d1), flip(d2)
+    k = np.array([2, 0, 0, 0, 0, 0], np.int32)
+    got = oracle.match(fa, k, fb, k, 752, 480)
+    assert len(got) == expected
+    ref = oracle.ref_matcher(752, 480)
+    if ref is not None:
+        assert np.array_equal(got, ref(fa, k, fb, k))

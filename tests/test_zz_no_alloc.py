@@ -67,3 +67,52 @@ def test_noalloc_rejects_oversize_and_bad_args():
     st = lib.uslam_match_noalloc(0, 0, 480, 6, None, capi.iptr(small), None, capi.iptr(small), C.c_void_p(1),
                                  C.c_void_p(1), 1, None, err, len(err))
     assert st == capi.INVALID_ARG
+
+
+def _flip(d: np.ndarray, n: int, rs) -> np.ndarray:
+    bits = np.unpackbits(d.view(np.uint8), bitorder="little")
+    bits[rs.choice(256, n, replace=False)] ^= 1
+    return np.packbits(bits, bitorder="little").view("<u4")
+
+
+@pytest.mark.parametrize("d1,d2,expected", [(17, 20, 0), (16, 19, 1)])
+def test_noalloc_ratio_boundary(d1, d2, expected):
+    """Planted descriptors at the Lowe-ratio boundary (accept iff
+    (float)best < 0.85f * (float)second, match_features_cpu.cpp:141):
+    0.85f * 20 rounds to exactly 17.0f in f32, so best 17 against second 20
+    is rejected, and 16 against 19 (16.15) accepted.  One previous feature
+    a0 meets the current features b0 (distance d1) and b1 (d2) in its
+    window; a far feature a1 keeps both pools at two."""
+    import torch
+
+    import oracle
+
+    assert not np.float32(17) < np.float32(0.85) * np.float32(20)
+    lib = capi.load()
+    W, H, L = 752, 480, 6
+    rs = np.random.RandomState(d1)
+    D = rs.randint(0, 2**32, size=8, dtype=np.uint64).astype(np.uint32)
+    fa = np.zeros(2, oracle.FEATURE_DTYPE)
+    fa["x"], fa["y"], fa["strength"] = [100, 600], [100, 400], 12
+    fa["descriptor"][0], fa["descriptor"][1] = D, ~D
+    fb = np.zeros(2, oracle.FEATURE_DTYPE)
+    fb["x"], fb["y"], fb["strength"] = [102, 110], [101, 104], 12
+    fb["descriptor"][0], fb["descriptor"][1] = _flip(D, d1, rs), _flip(D, d2, rs)
+    ka = np.array([2, 0, 0, 0, 0, 0], np.int32)
+    kb = ka.copy()
+    em = oracle.match(fa, ka, fb, kb, W, H)
+    assert len(em) == expected
+    da = torch.from_numpy(fa.view(np.uint8).copy()).cuda()
+    db = torch.from_numpy(fb.view(np.uint8).copy()).cuda()
+    out = torch.full((L * 2 * 4,), -7, dtype=torch.int32, device="cuda")
+    counts = torch.zeros(L, dtype=torch.int32, device="cuda")
+    torch.cuda.synchronize()
+    err = C.create_string_buffer(256)
+    st = lib.uslam_match_noalloc(0, W, H, L, C.c_void_p(da.data_ptr()), capi.iptr(ka), C.c_void_p(db.data_ptr()),
+                                 capi.iptr(kb), C.c_void_p(out.data_ptr()), C.c_void_p(counts.data_ptr()), 2,
+                                 C.c_void_p(torch.cuda.current_stream().cuda_stream), err, len(err))
+    assert st == capi.OK, err.value.decode()
+    o = out.cpu().numpy().reshape(L, 2, 4)
+    n = counts.cpu().numpy()
+    got = np.concatenate([o[l, :n[l]] for l in range(L)]) if n.sum() else np.zeros((0, 4), np.int32)
+    assert np.array_equal(got, em)
