@@ -13,7 +13,9 @@
  *
  * Plain pointers and sizes only.  Every call returns a uslam_status; on
  * failure uslam_last_error(ctx) holds a message.  No call throws.  A context
- * and everything created from it belong to one host thread at a time.
+ * and everything created from it belong to one host thread at a time, except
+ * a server, whose submit / wait / result / release may come from several
+ * threads (see uslam_server_submit).
  */
 #ifndef USLAM_H
 #define USLAM_H
@@ -105,6 +107,8 @@ typedef struct uslam_params {
  * every Pass::initialize of the feature-detect stage). */
 uslam_status uslam_create(const uslam_params* params, uslam_ctx** out);
 void uslam_destroy(uslam_ctx* ctx);
+/* The message of the context's last failed call.  The pointer is a copy for
+ * the calling thread, valid until that thread calls uslam_last_error again. */
 const char* uslam_last_error(const uslam_ctx* ctx);
 const char* uslam_status_string(uslam_status s);
 /* Level dimensions w_l = (uint32)(W0 / pow(1.2, l)) (wslam/src/common.cpp:41-45). */

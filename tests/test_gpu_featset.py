@@ -51,3 +51,35 @@ def test_match_sets_bruteforce(brief_pattern):
             b.detect(f1)
             em = oracle.match_bruteforce(e0[0], e0[1], e1[0], e1[1], 0.8)
             assert np.array_equal(_mm(c.match(a, b)), em) and len(em) > 200
+
+
+def test_last_error_from_many_threads(brief_pattern):
+    """Calls failing on one context from several host threads at once (the
+    served form's submitting threads can do this): every thread's
+    uslam_last_error reads a whole message.  The failing call, features of a
+    set with nothing detected, does no GPU work."""
+    import threading
+
+    from uni_slam_gb300 import capi
+
+    with Context(brief_pattern, levels=6, max_width=64, max_height=64) as c:
+        lib = c.lib
+        sets = [FeatureSet(c, 64, 64) for _ in range(4)]
+        statuses, msgs = [], []
+
+        def worker(fs):
+            kept = np.zeros(6, np.int32)
+            raw = np.zeros(6, np.int32)
+            for _ in range(2000):
+                statuses.append(lib.uslam_featset_features(fs.h, None, 0, capi.iptr(kept), capi.iptr(raw)))
+                msgs.append(lib.uslam_last_error(c.h))
+
+        threads = [threading.Thread(target=worker, args=(fs,)) for fs in sets]
+        for t in threads:
+            t.start()
+        for t in threads:
+            t.join()
+        for fs in sets:
+            fs.close()
+        assert set(statuses) == {capi.NOT_READY}
+        assert set(msgs) == {b"featset_features: nothing detected yet"}

@@ -94,7 +94,7 @@ struct uslam_batch {
     Program full;
     std::vector<Program> frame_prog;  // per frame: detect+describe only
     std::vector<Program> pair_prog;   // per pair: match only
-    std::string* err() { return &ctx->err; }
+    ErrText* err() { return &ctx->err; }
 };
 
 namespace {
@@ -805,7 +805,12 @@ void uslam_destroy(uslam_ctx* c) {
     delete c;
 }
 
-const char* uslam_last_error(const uslam_ctx* c) { return c ? c->err.c_str() : "null context"; }
+const char* uslam_last_error(const uslam_ctx* c) {
+    // a copy per calling thread: valid until this thread's next call here
+    thread_local std::string copy;
+    copy = c ? c->err.get() : std::string("null context");
+    return copy.c_str();
+}
 
 uslam_status uslam_batch_create(uslam_ctx* ctx, int n_frames, const int* widths, const int* heights, int n_pairs,
                                 const int* pair_prev, const int* pair_curr, uslam_batch** out) {
@@ -1376,7 +1381,7 @@ EncodeTiledFn encode_tiled() {
 }
 }  // namespace
 
-uslam_status encode_tile_maps(const FrameDev& F, int detector, void* out, std::string* err) {
+uslam_status encode_tile_maps(const FrameDev& F, int detector, void* out, ErrText* err) {
     static_assert(sizeof(CUtensorMap) == USLAM_TMAP_BYTES, "tensor map size");
     const EncodeTiledFn fn = encode_tiled();
     if (!fn) return set_err(err, USLAM_CUDA_ERROR, "cuTensorMapEncodeTiled is not available from the driver");

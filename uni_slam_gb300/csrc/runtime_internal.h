@@ -54,7 +54,27 @@ namespace uslam_rt {
 
 inline size_t round_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
 
-inline uslam_status set_err(std::string* dst, uslam_status s, const std::string& msg) {
+// A context's last error message.  Calls on one server may fail on several
+// host threads at once (submitting threads, result readers), so a write and
+// a reader's copy each take the lock.
+class ErrText {
+   public:
+    ErrText& operator=(const std::string& msg) {
+        std::lock_guard<std::mutex> g(mu_);
+        text_ = msg;
+        return *this;
+    }
+    std::string get() const {
+        std::lock_guard<std::mutex> g(mu_);
+        return text_;
+    }
+
+   private:
+    mutable std::mutex mu_;
+    std::string text_;
+};
+
+inline uslam_status set_err(ErrText* dst, uslam_status s, const std::string& msg) {
     if (dst) *dst = msg;
     return s;
 }
@@ -173,7 +193,7 @@ inline int lvl_pitch_of(int w) { return static_cast<int>(round_up(static_cast<si
 // buffers F.lvl[] are set: per level and tile shape a 2D f32 map over
 // [h][w] (row pitch lvl_pitch) with box (TW + 2 XPAD) x (TH + 2 HY), HY of
 // the detector.  out holds levels * kNumTileShapes maps of USLAM_TMAP_BYTES.
-uslam_status encode_tile_maps(const FrameDev& F, int detector, void* out, std::string* err);
+uslam_status encode_tile_maps(const FrameDev& F, int detector, void* out, ErrText* err);
 
 struct ResClass {
     int W0 = 0, H0 = 0;
@@ -208,7 +228,7 @@ struct uslam_ctx {
         return it == tile_shape.end() ? 0 : it->second;
     }
     int32_t* d_pattern = nullptr;
-    std::string err;
+    ErrText err;
     std::map<std::pair<int, int>, ResClass> classes;
 
     uslam_status cuda_fail(cudaError_t e, const char* what) {

@@ -739,7 +739,7 @@ uslam_status uslam_pixel_to_normalised(uslam_ctx* ctx, const uslam_camera* cam, 
 uslam_status uslam_triangulate(uslam_ctx* ctx, const uslam_camera* cam, const uslam_tri_opts* opts, int n_pairs,
                                const int* offsets, const double* px, uslam_tri_result* results, double* landmarks,
                                uint8_t* keep) {
-    std::string* err = ctx ? &ctx->err : nullptr;
+    ErrText* err = ctx ? &ctx->err : nullptr;
     if (!ctx || !cam || n_pairs < 0 || (n_pairs > 0 && (!offsets || !results)))
         return set_err(err, USLAM_INVALID_ARG, "triangulate: bad arguments");
     uslam_tri_opts o;
