@@ -378,11 +378,11 @@ uslam_status uslam_server_stats(uslam_server* server, uint64_t* launches, uint64
  * per-level match counts.  out_cap_per_level must be at least the previous
  * set's largest level count.
  *
- * Precondition on the records: each feature's x and y are integers (as f32)
- * inside its level (0 <= x < w_l, 0 <= y < h_l), as every detector of this
- * library and of the reference produces them.  The counts and sizes are
- * checked on the host; the records, being device memory, are not checked, and
- * a coordinate outside its level is undefined behaviour.
+ * Each feature's x and y must be integers (as f32) inside its level
+ * (0 <= x < w_l, 0 <= y < h_l), as every detector of this library and of the
+ * reference produces them.  The counts and sizes are checked on the host and
+ * the records by a kernel before anything indexes by them: a record outside
+ * its level returns USLAM_INVALID_ARG.
  *
  * Scratch comes from a file-scope device array of 4 MiB that every GPU which
  * loads the library holds until the process exits; a call whose scratch need

@@ -116,3 +116,39 @@ def test_noalloc_ratio_boundary(d1, d2, expected):
     n = counts.cpu().numpy()
     got = np.concatenate([o[l, :n[l]] for l in range(L)]) if n.sum() else np.zeros((0, 4), np.int32)
     assert np.array_equal(got, em)
+
+
+def test_noalloc_rejects_records_outside_level():
+    """Records whose x is not an integer inside its level are refused with
+    USLAM_INVALID_ARG before any kernel indexes by them (the planted values,
+    x = w and x = 10.5, stay inside the sort's histogram even unchecked),
+    and the next valid call succeeds."""
+    import torch
+
+    import oracle
+
+    lib = capi.load()
+    W, H, L = 752, 480, 6
+    f = np.zeros(2, oracle.FEATURE_DTYPE)
+    f["x"], f["y"], f["strength"] = [100, 110], [100, 104], 12
+    f["descriptor"] = np.random.RandomState(3).randint(0, 2**32, size=(2, 8), dtype=np.uint64).astype(np.uint32)
+    k = np.array([2, 0, 0, 0, 0, 0], np.int32)
+    out = torch.zeros((L * 2 * 4,), dtype=torch.int32, device="cuda")
+    counts = torch.zeros(L, dtype=torch.int32, device="cuda")
+    stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    err = C.create_string_buffer(256)
+
+    def call(fa, fb):
+        da = torch.from_numpy(fa.view(np.uint8).copy()).cuda()
+        db = torch.from_numpy(fb.view(np.uint8).copy()).cuda()
+        torch.cuda.synchronize()
+        return lib.uslam_match_noalloc(0, W, H, L, C.c_void_p(da.data_ptr()), capi.iptr(k), C.c_void_p(db.data_ptr()),
+                                       capi.iptr(k), C.c_void_p(out.data_ptr()), C.c_void_p(counts.data_ptr()), 2,
+                                       stream, err, len(err))
+
+    for bad_x, which in ((float(W), 0), (10.5, 1)):
+        g = f.copy()
+        g["x"][1] = bad_x
+        st = call(g, f) if which == 0 else call(f, g)
+        assert st == capi.INVALID_ARG and b"inside its level" in err.value, (bad_x, st, err.value)
+    assert call(f, f) == capi.OK, err.value.decode()

@@ -61,6 +61,27 @@ __global__ void k_noalloc_tables(const NoallocTables t, NoallocTables* dst) {
     for (size_t i = threadIdx.x; i < sizeof(NoallocTables) / 4; i += blockDim.x) d[i] = s[i];
 }
 
+// The caller's feature records are device memory the host cannot check, and
+// the x-sort indexes its shared histogram by x: every record's x and y must be
+// integers (as f32) inside its level.  A record that is not (NaN included)
+// sets *bad, and the host returns USLAM_INVALID_ARG before the sort runs.
+__global__ void k_noalloc_validate(const NoallocTables* t, uint32_t* bad) {
+    for (int f = 0; f < 2; ++f) {
+        const FrameDev& F = t->frames[f];
+        for (int l = 0; l < F.levels; ++l) {
+            const uint32_t n = F.kept[l];
+            const uint32_t* rec = F.feats[l];
+            const float w = (float)F.w[l], h = (float)F.h[l];
+            for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+                const float x = __uint_as_float(rec[(size_t)i * 12u]);
+                const float y = __uint_as_float(rec[(size_t)i * 12u + 1u]);
+                const bool ok = x >= 0.0f && x < w && y >= 0.0f && y < h && x == truncf(x) && y == truncf(y);
+                if (!ok) atomicOr(bad, 1u);
+            }
+        }
+    }
+}
+
 struct DeviceScratch {
     unsigned char* ptr = nullptr;
     int num_sms = 0;
@@ -214,6 +235,16 @@ extern "C" uslam_status uslam_match_noalloc(int device, int width, int height, i
     k_noalloc_tables<<<1, 256, 0, st>>>(t, dtab);
     e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaMemsetAsync(derr, 0, sizeof(uint32_t), st);  // the error word must start at zero
+    uint32_t bad = 0;
+    if (e == cudaSuccess && (total[0] > 0 || total[1] > 0)) {
+        k_noalloc_validate<<<ds.num_sms, 256, 0, st>>>(dtab, derr);
+        e = cudaGetLastError();
+        if (e == cudaSuccess) e = cudaMemcpyAsync(&bad, derr, sizeof bad, cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        if (e == cudaSuccess && bad != 0u)
+            return fail(err, err_len, USLAM_INVALID_ARG,
+                        "match_noalloc: a feature record's x or y is not an integer inside its level");
+    }
     if (e == cudaSuccess) {
         e = set_compact_smem(max_w);  // a function attribute, not an allocation
         if (e == cudaSuccess) e = launch_xsort(dtab->frames, dtab->xsegs, 2 * levels, max_w, st);
