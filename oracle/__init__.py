@@ -232,5 +232,32 @@ def ref_matcher(W0: int = 752, H0: int = 480):
     return run
 
 
+def ref_sampson():
+    """The reference's own RANSAC inlier test (ransac_cpu.cpp SampsonDistance
+    and ClassifyInliers, compiled by oracle/Makefile), or None.  The callable
+    returns (counts[H], masks[H, ceil(N/32)], distances[H, N])."""
+    path = os.path.join(REF_DIR, "libref_ransac.so")
+    if not os.path.exists(path):
+        return None
+    L = C.CDLL(path)
+    vp = C.c_void_p
+    L.ref_sampson_classify.argtypes = [vp, C.c_int, vp, vp, C.c_int, C.c_double, vp, vp, vp]
+    L.ref_sampson_classify.restype = None
+
+    def run(fmats, prev_xy, curr_xy, thr: float = 3.84):
+        F = np.ascontiguousarray(fmats, np.float64).reshape(-1, 9)
+        pp = np.ascontiguousarray(prev_xy, np.float64).reshape(-1, 2)
+        q = np.ascontiguousarray(curr_xy, np.float64).reshape(-1, 2)
+        n = len(pp)
+        counts = np.zeros(len(F), np.int32)
+        masks = np.zeros((len(F), max(1, (n + 31) // 32)), np.uint32)
+        dist = np.zeros((len(F), max(1, n)), np.float64)
+        L.ref_sampson_classify(_p(F), len(F), _p(pp), _p(q), n, thr, _p(counts), _p(masks), _p(dist))
+        return counts, masks[:, :(n + 31) // 32], dist[:, :n]
+
+    return run
+
+
 def ref_matcher_sizes():
-    return sorted(os.path.basename(p)[len("libref_matcher_"):-3] for p in glob.glob(os.path.join(REF_DIR, "*.so")))
+    return sorted(os.path.basename(p)[len("libref_matcher_"):-3]
+                  for p in glob.glob(os.path.join(REF_DIR, "libref_matcher_*.so")))

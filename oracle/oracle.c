@@ -562,9 +562,9 @@ int orc_match_bruteforce(const orc_feature* a, int na, const orc_feature* b, int
 }
 
 /* ----------------------------------------------------- RANSAC scoring -- */
-/* Sampson distance of wslam/src/pose_estimate_cpu/ransac_cpu.cpp:173-188 in
+/* Sampson distance of wslam/src/pose_estimate_cpu/ransac_cpu.cpp:183-196 in
  * double, in the evaluation order written in the CUDA file (left to right,
- * no contraction); inlier iff d < threshold (ClassifyInliers, :190-203). */
+ * no contraction); inlier iff d < threshold (ClassifyInliers, :198-210). */
 static int sampson_inlier(const double* F, double xp, double yp, double xc, double yc, double thr) {
     const double fx0 = (F[0] * xp + F[1] * yp) + F[2];
     const double fx1 = (F[3] * xp + F[4] * yp) + F[5];

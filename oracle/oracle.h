@@ -106,7 +106,7 @@ int orc_match_bruteforce(const orc_feature* a, int na, const orc_feature* b, int
 
 /* RANSAC scoring (no GPU counterpart in the reference): counts[h] = number of
  * correspondences whose Sampson distance to fundamental matrix h (row-major
- * 3x3 double) is below thr (ransac_cpu.cpp:173-203), in the evaluation order
+ * 3x3 double) is below thr (ransac_cpu.cpp:183-210), in the evaluation order
  * documented with the CUDA kernel; masks (or NULL) receive the inlier bits. */
 void orc_sampson_counts(const double* fmats, int n_hyp, const double* prev_xy, const double* curr_xy, int n,
                         double thr, int* counts, uint32_t* masks);

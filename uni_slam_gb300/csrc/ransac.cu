@@ -2,8 +2,8 @@
 //
 // The reference's RansacCPU (wslam/src/pose_estimate_cpu/ransac_cpu.cpp)
 // fits a fundamental matrix to 8 random matches per iteration and classifies
-// every match by its Sampson distance (SampsonDistance, :173-188;
-// ClassifyInliers, :190-203).  The fit (an SVD) stays on the host; this file
+// every match by its Sampson distance (SampsonDistance, :183-196;
+// ClassifyInliers, :198-210).  The fit (an SVD) stays on the host; this file
 // scores many hypotheses against all matches at once on the GPU.
 //
 // Arithmetic: binary64, no contraction (--fmad=false), in this order:
