@@ -227,7 +227,7 @@ typedef struct uslam_tri_result {
 void uslam_tri_default_opts(uslam_tri_opts* opts);
 /* util::PixelToNormalised (wslam/src/map/map_helpers_lods.hpp:110-120), the
  * undistortion CollectInliers applies to every inlier pixel
- * (triangulate_cpu.cpp:220-246): n pixels (x, y doubles) -> n calibrated
+ * (triangulate_cpu.cpp:218-247): n pixels (x, y doubles) -> n calibrated
  * rays, equal to the reference's bit for bit.  Host buffers; synchronous. */
 uslam_status uslam_pixel_to_normalised(uslam_ctx* ctx, const uslam_camera* cam, int iterations, double tolerance,
                                        const double* px, int n, double* out);

@@ -98,7 +98,7 @@ int orc_match(const orc_feature* a, const int* a_off, const orc_feature* b, cons
  * has no such mode, so this is pinned by its own definition only): every
  * feature of a (na, all levels flattened) against every feature of b (nb);
  * per query the best and second-best Hamming distances (scan rule of
- * match_features_cpu.cpp:106-119, from UINT32_MAX), accepted iff
+ * match_features_cpu.cpp:108-140, from UINT32_MAX), accepted iff
  * f32(best) < ratio * f32(second); no window, no cross-check; nb < 2 gives no
  * match (match_features_cpu.cpp:80-82).  a2b[i] receives the flat index into
  * b of query i's match, or -1.  Returns the number of matches. */

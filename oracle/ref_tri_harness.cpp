@@ -39,7 +39,7 @@ extern "C" void ref_pixel_to_normalised(double px, double py, const double* cam,
     out[1] = r.y();
 }
 
-// impl::FitEssentialMatrix (triangulate_cpu.cpp:79-141); E row-major.
+// impl::FitEssentialMatrix (triangulate_cpu.cpp:77-140); E row-major.
 extern "C" int ref_fit_essential(const double* xy_prev, const double* xy_curr, int n, double* e_out) {
     std::vector<Eigen::Vector2d> p, q;
     for (int i = 0; i < n; ++i) {
@@ -53,7 +53,7 @@ extern "C" int ref_fit_essential(const double* xy_prev, const double* xy_curr, i
     return 1;
 }
 
-// impl::DecomposeEssential (triangulate_cpu.cpp:150-176): 4 x (R row-major, t).
+// impl::DecomposeEssential (triangulate_cpu.cpp:149-172): 4 x (R row-major, t).
 extern "C" void ref_decompose_essential(const double* e_in, double* out) {
     Eigen::Matrix3d e;
     for (int r = 0; r < 3; ++r)
@@ -66,7 +66,7 @@ extern "C" void ref_decompose_essential(const double* e_in, double* out) {
     }
 }
 
-// impl::TriangulatePoint (triangulate_cpu.cpp:184-209); pose = R row-major, t.
+// impl::TriangulatePoint (triangulate_cpu.cpp:180-207); pose = R row-major, t.
 extern "C" int ref_triangulate_point(const double* pose, const double* xy_prev, const double* xy_curr,
                                      double* out) {
     Eigen::Matrix3d r;

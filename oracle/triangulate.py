@@ -4,14 +4,14 @@ INFRASTRUCTURE ONLY (tests/ and the CPU-baseline leg of bench.py).
 Follows TriangulateCPU::execute (wslam/src/pose_estimate_cpu/triangulate_cpu.cpp:342-513)
 step by step:
 
-  CollectInliers       triangulate_cpu.cpp:220-246  LOD-0 pixels -> calibrated rays
-  PixelToNormalised    wslam/src/map/map_helpers_lods.hpp:110-120 (+ UndistortNormalised :41-77)
-  FitEssentialMatrix   triangulate_cpu.cpp:79-141   normalised 8-point on all rays
-  NormalisingTransform triangulate_cpu.cpp:48-75
-  DecomposeEssential   triangulate_cpu.cpp:150-176  four (R, t) candidates
-  TriangulatePoint     triangulate_cpu.cpp:184-209  linear DLT, right null vector of a 4x4
+  CollectInliers       triangulate_cpu.cpp:218-247  LOD-0 pixels -> calibrated rays
+  PixelToNormalised    wslam/src/map/map_helpers_lods.hpp:110-120 (+ UndistortNormalised :41-76)
+  FitEssentialMatrix   triangulate_cpu.cpp:77-140   normalised 8-point on all rays
+  NormalisingTransform triangulate_cpu.cpp:48-73
+  DecomposeEssential   triangulate_cpu.cpp:149-172  four (R, t) candidates
+  TriangulatePoint     triangulate_cpu.cpp:180-207  linear DLT, right null vector of a 4x4
   ScoreCandidate       triangulate_cpu.cpp:257-278  points in front of both cameras
-  landmark filter      triangulate_cpu.cpp:446-486  depth range + mean reprojection error
+  landmark filter      triangulate_cpu.cpp:444-488  depth range + mean reprojection error
   ProjectToPixel       triangulate_cpu.cpp:34-45 with DistortNormalised (map_helpers_lods.hpp:16-29)
   ComputeRotationAngle map_helpers_lods.hpp:33-36
 
@@ -46,7 +46,7 @@ SQRT2 = 1.4142135623730951  # std::numbers::sqrt2
 
 
 def undistort_normalised(dist: np.ndarray, d, max_iters: int, tol: float) -> np.ndarray:
-    """UndistortNormalised (map_helpers_lods.hpp:45-77) for every row of dist (n, 2)."""
+    """UndistortNormalised (map_helpers_lods.hpp:45-76) for every row of dist (n, 2)."""
     dist = np.asarray(dist, np.float64)
     k1, k2, p1, p2 = (float(v) for v in d)
     xy = dist.copy()
@@ -101,7 +101,7 @@ def project_to_pixel(p: np.ndarray, cam) -> np.ndarray:
 
 
 def normalising_transform(points: np.ndarray) -> np.ndarray:
-    """NormalisingTransform (triangulate_cpu.cpp:48-75), sums taken in row order."""
+    """NormalisingTransform (triangulate_cpu.cpp:48-73), sums taken in row order."""
     n = float(len(points))
     c = np.array([np.cumsum(points[:, 0])[-1], np.cumsum(points[:, 1])[-1]]) / n
     d = points - c
@@ -116,7 +116,7 @@ def normalising_transform(points: np.ndarray) -> np.ndarray:
 
 
 def fit_essential(prev: np.ndarray, curr: np.ndarray):
-    """FitEssentialMatrix (triangulate_cpu.cpp:79-141); None where it fails."""
+    """FitEssentialMatrix (triangulate_cpu.cpp:77-140); None where it fails."""
     tp, tc = normalising_transform(prev), normalising_transform(curr)
     p = prev @ tp[:2, :2].T + tp[:2, 2]
     q = curr @ tc[:2, :2].T + tc[:2, 2]
@@ -134,7 +134,7 @@ def fit_essential(prev: np.ndarray, curr: np.ndarray):
 
 
 def decompose_essential(e: np.ndarray):
-    """DecomposeEssential (triangulate_cpu.cpp:150-176): [(R1, t), (R1, -t), (R2, t), (R2, -t)]."""
+    """DecomposeEssential (triangulate_cpu.cpp:149-172): [(R1, t), (R1, -t), (R2, t), (R2, -t)]."""
     u, _, vt = np.linalg.svd(e)
     v = vt.T.copy()
     u = u.copy()
@@ -150,7 +150,7 @@ def decompose_essential(e: np.ndarray):
 
 
 def triangulate_points(r: np.ndarray, t: np.ndarray, xy_prev: np.ndarray, xy_curr: np.ndarray) -> np.ndarray:
-    """TriangulatePoint (triangulate_cpu.cpp:184-209) for every row: (n, 3), NaN where it fails."""
+    """TriangulatePoint (triangulate_cpu.cpp:180-207) for every row: (n, 3), NaN where it fails."""
     n = len(xy_prev)
     p2 = np.concatenate([r, t[:, None]], 1)
     a = np.zeros((n, 4, 4))

@@ -136,7 +136,7 @@ def test_tied_best_is_rejected(brief_pattern, matcher):
     the single feature of frame A (bright pixels at (297, 262) and (315, 262)
     on a flat frame), so a query for that descriptor meets two candidates at
     distance 0 and the ratio test rejects it (best == second;
-    match_features_cpu.cpp:128-141).  B2 (second pixel at (324, 262)) has a
+    match_features_cpu.cpp:133-146).  B2 (second pixel at (324, 262)) has a
     different second descriptor and matches.  All 12 ordered pairs of
     A, B1, B2 and C (A plus a far feature) equal the oracle."""
     W, H = 640, 480

@@ -78,7 +78,7 @@ def _flip(d: np.ndarray, n: int, rs) -> np.ndarray:
 @pytest.mark.parametrize("d1,d2,expected", [(17, 20, 0), (16, 19, 1)])
 def test_noalloc_ratio_boundary(d1, d2, expected):
     """Planted descriptors at the Lowe-ratio boundary (accept iff
-    (float)best < 0.85f * (float)second, match_features_cpu.cpp:141):
+    (float)best < 0.85f * (float)second, match_features_cpu.cpp:142-146):
     0.85f * 20 rounds to exactly 17.0f in f32, so best 17 against second 20
     is rejected, and 16 against 19 (16.15) accepted.  One previous feature
     a0 meets the current features b0 (distance d1) and b1 (d2) in its

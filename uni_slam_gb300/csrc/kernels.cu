@@ -1306,7 +1306,7 @@ struct CandStage {
 // colstart[last col <= hi + 1])), so per staged batch a lane tests the y
 // condition only inside its range, collects the hits in a bit mask and
 // computes Hamming distances for those hits alone
-// (match_features_cpu.cpp:108-141).  The result does not depend on the
+// (match_features_cpu.cpp:108-148).  The result does not depend on the
 // candidate order: a tied best always fails the ratio test.
 __global__ void __launch_bounds__(KM_THREADS)
 k_match(const FrameDev* __restrict__ frames, const PairDev* __restrict__ pairs,

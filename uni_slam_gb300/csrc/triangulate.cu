@@ -8,7 +8,7 @@
 // partials in chunk order, so results do not depend on scheduling and nothing
 // waits on another CTA.
 //
-//   k_tri_rays        PixelToNormalised of both pixels (map_helpers_lods.hpp:41-77, 110-120):
+//   k_tri_rays        PixelToNormalised of both pixels (map_helpers_lods.hpp:41-76, 110-120):
 //                     the reference's double operations in its order, so the rays equal its
 //                     bits; last chunk: the centroids of NormalisingTransform (:48-75)
 //   k_tri_spread      distances to the centroids; last chunk: the Hartley scales
