@@ -274,32 +274,76 @@ def _cpu_frame(args):
     return oracle.frame(img, pattern)
 
 
-def _cpu_match(args):
-    fa, fb = args
+def _matcher():
+    """The reference's own matcher (match_features_cpu.cpp compiled unmodified
+    into oracle/_ref), or the oracle's restatement where it was not built;
+    returns (callable, kind)."""
     import oracle
 
-    return len(oracle.match(fa[0], fa[1], fb[0], fb[1], W, H))
+    ref = oracle.ref_matcher(W, H)
+    if ref is not None:
+        return ref, "reference"
+    return (lambda fa, ka, fb, kb: oracle.match(fa, ka, fb, kb, W, H)), "port"
+
+
+def _cpu_match(args):
+    fa, fb = args
+    match, _ = _matcher()
+    return len(match(fa[0], fa[1], fb[0], fb[1]))
+
+
+CPU_SAMPLE_TEXT = ("detect+describe: the CPU restatement of the reference's WGSL passes (Dawn cannot run on this "
+                   "box); match: {match}")
+
+
+def _matcher_text(kind: str) -> str:
+    return ("the reference's own match_features_cpu.cpp, compiled unmodified (oracle/_ref)" if kind == "reference"
+            else "the oracle's restatement of match_features_cpu.cpp (the compiled reference was not built)")
 
 
 def cpu_baseline_sample(frames, pattern, seconds: float) -> dict:
-    """Single-threaded oracle port on a time-bounded prefix of the workload."""
+    """Single-threaded CPU path on a time-bounded prefix of the workload."""
     import oracle
 
+    match, kind = _matcher()
     t0 = time.perf_counter()
     prev = None
     n = 0
     for img in frames:
         cur = oracle.frame(img, pattern)
         if prev is not None:
-            oracle.match(prev[0], prev[1], cur[0], cur[1], W, H)
+            match(prev[0], prev[1], cur[0], cur[1])
         prev = cur
         n += 1
         if time.perf_counter() - t0 >= seconds and n >= 2:
             break
     dt = time.perf_counter() - t0
-    return {"value": n / dt, "unit": "frames/s", "cores": 1, "kind": "port",
+    return {"value": n / dt, "unit": "frames/s", "cores": 1, "kind": kind,
             "sample": f"first {n} frames of the workload (detect+describe each, match each against the previous), "
-                      f"CPU restatement of the reference path, 1 thread, {dt:.1f} s"}
+                      f"1 thread, {dt:.1f} s; " + CPU_SAMPLE_TEXT.format(match=_matcher_text(kind))}
+
+
+def reference_match_check(batch, n: int) -> dict:
+    """The reference's compiled matcher on the GPU's feature sets of every pair
+    of the timed workload, against the GPU's match lists."""
+    import numpy as np
+
+    import oracle
+
+    ref = oracle.ref_matcher(W, H)
+    if ref is None:
+        return {"compared": False, "why": "the reference matcher was not built (no checkout and no staged copy)"}
+    feats = [batch.features(i) for i in range(n)]
+    equal = 0
+    total = 0
+    for p in range(n - 1):
+        m = batch.matches(p)
+        g = np.stack([m["lod_a"], m["idx_a"], m["lod_b"], m["idx_b"]], 1) if len(m) else np.zeros((0, 4), np.int32)
+        r = ref(feats[p][0], feats[p][1], feats[p + 1][0], feats[p + 1][1])
+        equal += int(np.array_equal(g, r))
+        total += len(r)
+    return {"compared": True, "pairs": n - 1, "pairs_equal": equal, "reference_matches": total,
+            "matcher": "match_features_cpu.cpp compiled unmodified (oracle/_ref), on the GPU's feature sets"}
 
 
 def run_reference(a):
@@ -311,6 +355,7 @@ def run_reference(a):
 
     pat = patmod.load()
     frames = synth.plane_sequence(a.seed, n=a.frames)
+    _, kind = _matcher()
     cores = os.cpu_count() or 1
     ctx = mp.get_context("spawn")
     times = []
@@ -327,15 +372,19 @@ def run_reference(a):
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "frames/s", "n_gpus": a.gpus,
         "steps": a.steps, "warmup": a.warmup, "ms_per_step": step_s * 1e3, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32+u32", "data": "synthetic (seeded; EuRoC absent)",
-        "config": {"workload": WORKLOAD, "frames": a.frames, "levels": LEVELS, "seed": a.seed},
-        "cpu_baseline": {"value": value, "unit": "frames/s", "cores": cores, "kind": "port",
-                         "sample": f"the full {a.frames}-frame step on a {cores}-process pool (CPU restatement of "
-                                   "the reference's WGSL passes + matcher; the WGSL passes cannot run through Dawn "
-                                   "on this box)"},
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32+u32", "data": "synthetic (seeded plane trajectory; EuRoC absent)",
+        "config": _config(a.frames, a.seed, world),
+        "cpu_baseline": {"value": value, "unit": "frames/s", "cores": cores, "kind": kind,
+                         "sample": f"the full {a.frames}-frame step on a {cores}-process pool; "
+                                   + CPU_SAMPLE_TEXT.format(match=_matcher_text(kind))},
         "e2e": {"value": value, "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
+
+
+def _config(frames: int, seed: int, world: int) -> dict:
+    return {"workload": WORKLOAD, "frames": frames, "pairs": frames - 1, "levels": LEVELS, "seed": seed,
+            "l2": "flushed (256 MiB write) between timed steps", "parallelism": f"replicas x{world}"}
 
 
 # ------------------------------------------------------------------ served form
@@ -633,6 +682,7 @@ def cfg_run(pat, local: int, frames, steps: int, warmup: int, matcher: int = 1) 
                         "with 3x3 NMS, brute-force top-2 Hamming matching at ratio 0.8 against the previous frame",
             "frames": n, "ms_per_step": step_ms, "frames_per_s": n / (step_ms / 1e3),
             "features_per_frame": sum(kept) / n, "matches_per_pair": sum(nmatch) / max(1, n - 1),
+            "reference_match_check": ref_check,
             "kernel_ms": prof, "l2": "flushed (256 MiB write) between timed steps",
             "match_lists": [_mm_digest(batch.matches(k)) for k in range(n - 1)],
         }
@@ -932,6 +982,7 @@ def run_ours(a):
     kept = [int(batch.features(i)[1].sum()) for i in range(n)]
     nmatch = [len(batch.matches(p)) for p in range(n - 1)]
     nbytes = algorithmic_bytes(kept, nmatch, n)
+    ref_check = reference_match_check(batch, n) if rank == 0 else None
 
     # ---- per-kernel timing for the roofline (events on the launching stream)
     prof = batch.profile(iters=5)
@@ -1096,8 +1147,7 @@ def run_ours(a):
             "metric": METRIC, "value": value, "unit": "frames/s", "n_gpus": world, "steps": a.steps,
             "warmup": a.warmup, "ms_per_step": step_ms_max, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32+u32", "data": "synthetic (seeded plane trajectory; EuRoC absent)",
-            "config": {"workload": WORKLOAD, "frames": n, "pairs": n - 1, "levels": LEVELS, "seed": a.seed,
-                       "l2": "flushed (256 MiB write) between timed steps", "parallelism": f"replicas x{world}"},
+            "config": _config(n, a.seed, world),
             "plain_fps": plain_fps, "batched_over_plain": value / world / plain_fps,
             "e2e": {"value": n * world / e2e_s, "unit": "frames/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h,
@@ -1108,6 +1158,7 @@ def run_ours(a):
             "served": served, "uneven": uneven, "stress": stress, "cfg": cfg, "ransac": ransac,
             "triangulate": tri,
             "features_per_frame": sum(kept) / n, "matches_per_pair": sum(nmatch) / max(1, n - 1),
+            "reference_match_check": ref_check,
             "wall_s_timed": wall_s,
         }
         print(json.dumps(line), flush=True)

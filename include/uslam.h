@@ -376,7 +376,10 @@ uslam_status uslam_server_stats(uslam_server* server, uint64_t* launches, uint64
  * out_cap_per_level uslam_match entries (block l = matches whose previous
  * feature lies in level l, in that feature's order) and out_counts the
  * per-level match counts.  out_cap_per_level must be at least the previous
- * set's largest level count.
+ * set's largest level count.  The feature arrays must be 16-byte aligned
+ * (the matcher reads each descriptor as two 16-byte vectors; a sub-pointer
+ * into a caller's pool must keep that alignment), out and out_counts 4-byte
+ * aligned; other pointers return USLAM_INVALID_ARG before any device work.
  *
  * Each feature's x and y must be integers (as f32) inside its level
  * (0 <= x < w_l, 0 <= y < h_l), as every detector of this library and of the
@@ -387,12 +390,15 @@ uslam_status uslam_server_stats(uslam_server* server, uint64_t* launches, uint64
  * Scratch comes from a file-scope device array of 4 MiB that every GPU which
  * loads the library holds until the process exits; a call whose scratch need
  * exceeds it returns USLAM_CAPACITY.  The first call on a device looks up
- * that array's device address (cudaGetSymbolAddress); make that first call
- * before any stream capture.  All calls share the array: calls that overlap
- * on the GPU (different streams or threads at the same time) race and must
- * not be issued.  The call enqueues on `stream` (a cudaStream_t; NULL = the
- * default stream) and returns after the work is complete.  err (optional,
- * err_len bytes) receives a message on failure. */
+ * that array's device address (cudaGetSymbolAddress), and so does the first
+ * call after the device's context was reset; make that first call before any
+ * stream capture.  All calls share the array: calls that overlap on the GPU
+ * (different streams or threads at the same time) race and must not be
+ * issued.  The call makes `device` current while it runs and restores the
+ * caller's current device before it returns.  It enqueues on `stream` (a
+ * cudaStream_t; NULL = the default stream), waits once after the record
+ * check and once at the end, and returns after the work is complete.  err
+ * (optional, err_len bytes) receives a message on failure. */
 uslam_status uslam_match_noalloc(int device, int width, int height, int levels, const uslam_feature* prev_feats,
                                  const int* prev_kept, const uslam_feature* curr_feats, const int* curr_kept,
                                  uslam_match* out, uint32_t* out_counts, int out_cap_per_level, void* stream,

@@ -258,6 +258,17 @@ def ref_sampson():
     return run
 
 
+STAGED_MATCHER = os.path.join(os.path.dirname(HERE), "baseline", "_ref", "wslam", "src", "pose_estimate_cpu",
+                              "match_features_cpu.cpp")
+
+
+def ref_matcher_expected() -> bool:
+    """True where the reference's matcher source is at hand (its copy staged
+    in baseline/_ref travels with the repository), so oracle/_ref must hold
+    the compiled matcher and the live checks against it must run."""
+    return os.path.exists(STAGED_MATCHER)
+
+
 def ref_matcher_sizes():
     return sorted(os.path.basename(p)[len("libref_matcher_"):-3]
                   for p in glob.glob(os.path.join(REF_DIR, "libref_matcher_*.so")))

@@ -29,7 +29,8 @@ def _permute(rs, f, k):
 def test_match_independent_of_feature_order(flip_p):
     rs = np.random.RandomState(int(flip_p * 100) + 3)
     W, H = 752, 480
-    ref = oracle.ref_matcher(W, H)  # None without the reference checkout
+    ref = oracle.ref_matcher(W, H)  # None without a copy of the reference matcher source
+    assert ref is not None or not oracle.ref_matcher_expected()
     for trial in range(4):
         fa, ka, fb, kb = _random_sets(rs, W, H, per_level=150, flip_p=flip_p)
         base = _pairs(fa, ka, fb, kb, oracle.match(fa, ka, fb, kb, W, H))

@@ -60,7 +60,8 @@ def _random_sets(rs, W, H, per_level, flip_p):
 def test_matcher_against_compiled_reference_live(size):
     ref = oracle.ref_matcher(*size)
     if ref is None:
-        pytest.skip("reference checkout not present: compiled reference matcher unavailable (golden pins still run)")
+        assert not oracle.ref_matcher_expected(), "the staged reference matcher source exists but was not built"
+        pytest.skip("no copy of the reference matcher source: compiled reference unavailable (golden pins still run)")
     rs = np.random.RandomState(size[0])
     for trial in range(12):
         fa, ka, fb, kb = _random_sets(rs, size[0], size[1], per_level=120, flip_p=[0.0, 0.05, 0.2][trial % 3])
@@ -92,5 +93,6 @@ def test_matcher_ratio_boundary(d1, d2, expected):
     got = oracle.match(fa, k, fb, k, 752, 480)
     assert len(got) == expected
     ref = oracle.ref_matcher(752, 480)
+    assert ref is not None or not oracle.ref_matcher_expected()
     if ref is not None:
         assert np.array_equal(got, ref(fa, k, fb, k))

@@ -34,6 +34,7 @@ def test_noalloc_match_equals_batch_path(brief_pattern):
             b.close()
     stream = torch.cuda.current_stream().cuda_stream
     err = C.create_string_buffer(256)
+    free_before = None
     for call, (ia, ib) in enumerate([(0, 1), (2, 3)]):
         fa, ka, _ = feats[ia]
         fb, kb, _ = feats[ib]
@@ -45,10 +46,18 @@ def test_noalloc_match_equals_batch_path(brief_pattern):
         torch.cuda.synchronize()
         ka32 = np.ascontiguousarray(ka, np.int32)
         kb32 = np.ascontiguousarray(kb, np.int32)
+        if call == 1:
+            # the second call: every kernel it runs is loaded, so any change of
+            # the device's free memory would be an allocation by the call
+            free_before = torch.cuda.mem_get_info(0)[0]
+            torch_before = torch.cuda.memory_allocated(0)
         st = lib.uslam_match_noalloc(0, W, H, L, C.c_void_p(da.data_ptr()), capi.iptr(ka32),
                                      C.c_void_p(db.data_ptr()), capi.iptr(kb32), C.c_void_p(out.data_ptr()),
                                      C.c_void_p(counts.data_ptr()), cap_out, C.c_void_p(stream), err, len(err))
         assert st == capi.OK, err.value.decode()
+        if call == 1:
+            assert torch.cuda.mem_get_info(0)[0] == free_before, "the call allocated device memory"
+            assert torch.cuda.memory_allocated(0) == torch_before
         o = out.cpu().numpy().reshape(L, cap_out, 4)
         n = counts.cpu().numpy()
         got = np.concatenate([o[l, :n[l]] for l in range(L)]) if n.sum() else np.zeros((0, 4), np.int32)
@@ -57,16 +66,46 @@ def test_noalloc_match_equals_batch_path(brief_pattern):
 
 
 def test_noalloc_rejects_oversize_and_bad_args():
+    """Sizes beyond the fixed scratch and bad arguments are refused on the
+    host, with real device buffers in every pointer argument."""
+    import torch
+
     lib = capi.load()
     err = C.create_string_buffer(256)
+    feats = torch.zeros(48 * 64, dtype=torch.uint8, device="cuda")
+    out = torch.zeros(6 * 16, dtype=torch.int32, device="cuda")
+    counts = torch.zeros(6, dtype=torch.int32, device="cuda")
+    torch.cuda.synchronize()
+    fp, op, cp = C.c_void_p(feats.data_ptr()), C.c_void_p(out.data_ptr()), C.c_void_p(counts.data_ptr())
     big = np.full(6, 200000, np.int32)  # scratch need far beyond the fixed maximum
-    st = lib.uslam_match_noalloc(0, 752, 480, 6, C.c_void_p(1), capi.iptr(big), C.c_void_p(1), capi.iptr(big),
-                                 C.c_void_p(1), C.c_void_p(1), 200000, None, err, len(err))
+    st = lib.uslam_match_noalloc(0, 752, 480, 6, fp, capi.iptr(big), fp, capi.iptr(big), op, cp, 200000, None, err,
+                                 len(err))
     assert st == capi.CAPACITY and b"fixed maximum" in err.value
     small = np.zeros(6, np.int32)
-    st = lib.uslam_match_noalloc(0, 0, 480, 6, None, capi.iptr(small), None, capi.iptr(small), C.c_void_p(1),
-                                 C.c_void_p(1), 1, None, err, len(err))
+    st = lib.uslam_match_noalloc(0, 0, 480, 6, fp, capi.iptr(small), fp, capi.iptr(small), op, cp, 1, None, err,
+                                 len(err))
     assert st == capi.INVALID_ARG
+
+
+def test_noalloc_rejects_misaligned_records():
+    """A feature array that is not 16-byte aligned (a sub-pointer into a
+    caller's pool, here 4 bytes in) is refused before any device work."""
+    import torch
+
+    lib = capi.load()
+    err = C.create_string_buffer(256)
+    feats = torch.zeros(48 * 8 + 16, dtype=torch.uint8, device="cuda")
+    out = torch.zeros(6 * 4 * 4, dtype=torch.int32, device="cuda")
+    counts = torch.zeros(6, dtype=torch.int32, device="cuda")
+    torch.cuda.synchronize()
+    k = np.array([2, 0, 0, 0, 0, 0], np.int32)
+    base = feats.data_ptr()
+    assert base % 16 == 0
+    for pa, pb in ((base + 4, base), (base, base + 4)):
+        st = lib.uslam_match_noalloc(0, 752, 480, 6, C.c_void_p(pa), capi.iptr(k), C.c_void_p(pb), capi.iptr(k),
+                                     C.c_void_p(out.data_ptr()), C.c_void_p(counts.data_ptr()), 4, None, err,
+                                     len(err))
+        assert st == capi.INVALID_ARG and b"16-byte" in err.value, (st, err.value)
 
 
 def _flip(d: np.ndarray, n: int, rs) -> np.ndarray:

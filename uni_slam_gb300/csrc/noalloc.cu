@@ -41,7 +41,8 @@ constexpr int kMaxDevices = 64;
 
 // The no-alloc matcher's scratch.  Host code must not use this name as an
 // address: it is a host-side stand-in.  The device address comes from
-// cudaGetSymbolAddress once per device (see scratch_for_device).
+// cudaGetSymbolAddress once per device and CUDA context (see
+// scratch_for_device).
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoallocScratchBytes];
 
 // Everything the match kernels read besides the features, written into the
@@ -85,30 +86,68 @@ __global__ void k_noalloc_validate(const NoallocTables* t, uint32_t* bad) {
 struct DeviceScratch {
     unsigned char* ptr = nullptr;
     int num_sms = 0;
-    bool ready = false;
+    void* context = nullptr;  // the CUDA context the address belongs to
 };
 
 std::mutex g_setup_mutex;
 DeviceScratch g_scratch_by_device[kMaxDevices];
 
-// Set-up, once per device, with that device current: the scratch's device
-// address (cudaGetSymbolAddress) and the SM count.  Happens on the first call
-// on a device; that first call should therefore come before any stream capture.
+// The current CUDA context, read through the driver entry point (the runtime
+// has no call for it); a reset device gets a new context, and the module that
+// holds the scratch array is loaded again, possibly at another address.
+using CtxGetCurrentFn = int (*)(void**);
+CtxGetCurrentFn ctx_get_current() {
+    static CtxGetCurrentFn fn = [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 4000, cudaEnableDefault, &q) != cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            p = nullptr;
+        cudaGetLastError();
+        return reinterpret_cast<CtxGetCurrentFn>(p);
+    }();
+    return fn;
+}
+
+// Set-up, once per device and CUDA context, with that device current: the
+// scratch's device address (cudaGetSymbolAddress) and the SM count.  It runs
+// on the first call on a device, and again on the first call after the
+// device's context was reset.
 cudaError_t scratch_for_device(int device, DeviceScratch* out) {
+    void* cur = nullptr;
+    const CtxGetCurrentFn get = ctx_get_current();
+    if (!get || get(&cur) != 0 || !cur) return cudaErrorInitializationError;
     std::lock_guard<std::mutex> lock(g_setup_mutex);
     DeviceScratch& d = g_scratch_by_device[device];
-    if (!d.ready) {
+    if (d.context != cur) {
         void* p = nullptr;
         cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
         if (e != cudaSuccess) return e;
         e = cudaDeviceGetAttribute(&d.num_sms, cudaDevAttrMultiProcessorCount, device);
         if (e != cudaSuccess) return e;
         d.ptr = static_cast<unsigned char*>(p);
-        d.ready = true;
+        d.context = cur;
     }
     *out = d;
     return cudaSuccess;
 }
+
+// Makes `device` current for the call and puts the caller's device back.
+struct DeviceGuard {
+    int prev = -1;
+    cudaError_t set(int device) {
+        cudaError_t e = cudaGetDevice(&prev);
+        if (e != cudaSuccess) {
+            prev = -1;
+            return e;
+        }
+        return prev == device ? cudaSuccess : cudaSetDevice(device);
+    }
+    ~DeviceGuard() {
+        int now = -1;
+        if (prev >= 0 && cudaGetDevice(&now) == cudaSuccess && now != prev) cudaSetDevice(prev);
+    }
+};
 
 uslam_status fail(char* err, size_t err_len, uslam_status s, const char* msg) {
     if (err && err_len > 0) std::snprintf(err, err_len, "%s", msg);
@@ -144,7 +183,12 @@ extern "C" uslam_status uslam_match_noalloc(int device, int width, int height, i
             total[f] += kept[f][l];
         }
         if (total[f] > 0 && !feats[f]) return fail(err, err_len, USLAM_INVALID_ARG, "match_noalloc: null features");
+        // the matcher reads each record's descriptor as two 16-byte vectors
+        if (total[f] > 0 && reinterpret_cast<uintptr_t>(feats[f]) % 16u != 0u)
+            return fail(err, err_len, USLAM_INVALID_ARG, "match_noalloc: feature records not 16-byte aligned");
     }
+    if (reinterpret_cast<uintptr_t>(out) % 4u != 0u || reinterpret_cast<uintptr_t>(out_counts) % 4u != 0u)
+        return fail(err, err_len, USLAM_INVALID_ARG, "match_noalloc: output buffers not 4-byte aligned");
     if (out_cap_per_level < cap[0])
         return fail(err, err_len, USLAM_INVALID_ARG, "match_noalloc: out_cap_per_level below the previous set's largest level");
 
@@ -178,7 +222,8 @@ extern "C" uslam_status uslam_match_noalloc(int device, int width, int height, i
         return fail(err, err_len, USLAM_CAPACITY, msg);
     }
 
-    cudaError_t e = cudaSetDevice(device);
+    DeviceGuard guard;
+    cudaError_t e = guard.set(device);
     DeviceScratch ds;
     if (e == cudaSuccess) e = scratch_for_device(device, &ds);
     if (e != cudaSuccess) return fail(err, err_len, USLAM_CUDA_ERROR, cudaGetErrorString(e));
