@@ -20,10 +20,11 @@ sizes (640x480 .. 3840x2160) each matched against its warp in one graph,
 per-32x32-cell caps, detect tiles autotuned per size; ``cfg`` = the main
 workload in the cfg profile (FAST 9-of-16 at 20/255, 3x3 NMS, brute-force
 ratio 0.8); ``stress`` = 3840x2160 frames,
-8 levels, 2500 features per level (20000 per frame), brute-force top-2
-matching of every frame against a seeded warp of itself, 8 such pairs per
-batch.  ``--impl reference`` times the CPU restatement of the reference's
-path (oracle port) on all host cores, on the same workload.
+8 levels, 20000 features per frame (levels filled in order), brute-force
+top-2 matching of every frame against a seeded warp of itself, 8 such pairs
+per batch.  ``--impl reference`` times the reference's CPU path on all host
+cores, on the same workload: its own matcher (match_features_cpu.cpp compiled
+unmodified) beside the CPU restatement of its WGSL passes.
 """
 from __future__ import annotations
 
@@ -41,7 +42,9 @@ REPO = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, REPO)
 
 W, H, LEVELS = 752, 480, 6
-STRESS_W, STRESS_H, STRESS_LEVELS, STRESS_CAP = 3840, 2160, 8, 2500
+# the stress config's cap of 20000 keypoints per frame: levels filled in order
+# (the first 20000 in (level, y, x) order), each level's buffer able to hold all
+STRESS_W, STRESS_H, STRESS_LEVELS, STRESS_FRAME_CAP = 3840, 2160, 8, 20000
 POPC_PER_SM_CLK = 16  # 32-bit population count results per SM per clock (documented issue rate)
 POPC_PER_DISTANCE = 4  # carry-save-adder Hamming distance of 256 bits
 # kernels of one graph replay of the uniform batch (one tile shape), which the
@@ -817,7 +820,7 @@ def _stress_pair(seed: int):
 
 
 def stress_run(pat, local: int, pair_frames, steps: int, warmup: int, seed: int, matcher: int = 1) -> dict:
-    """3840x2160 frames, 8 levels, 2500 kept per level, brute-force top-2
+    """3840x2160 frames, 8 levels, 20000 kept per frame, brute-force top-2
     matching (ratio 0.8) of each frame against its warp, all pairs in one
     batch; matcher 1 computes the distances on the integer pipes (XOR +
     popcount), matcher 2 on the tensor cores (FP8 dot products, tcgen05)."""
@@ -827,8 +830,8 @@ def stress_run(pat, local: int, pair_frames, steps: int, warmup: int, seed: int,
 
     frames = [f for pr in pair_frames for f in pr]
     npairs = len(pair_frames)
-    ctx = Context(pat, levels=STRESS_LEVELS, max_width=STRESS_W, max_height=STRESS_H, cap_per_level=STRESS_CAP,
-                  device=local, matcher=matcher, ratio=0.8)
+    ctx = Context(pat, levels=STRESS_LEVELS, max_width=STRESS_W, max_height=STRESS_H,
+                  cap_per_level=STRESS_FRAME_CAP, frame_cap=STRESS_FRAME_CAP, device=local, matcher=matcher, ratio=0.8)
     batch = Batch(ctx, [(STRESS_W, STRESS_H)] * len(frames), [(2 * k, 2 * k + 1) for k in range(npairs)])
     try:
         for i, f in enumerate(frames):
@@ -867,7 +870,8 @@ def stress_run(pat, local: int, pair_frames, steps: int, warmup: int, seed: int,
         bf_s = prof["k_bruteforce"] / 1e3
         return {
             "workload": f"stress: {npairs} pairs of 3840x2160 u8 frames (5000 rectangles, 500 checker patches) and "
-                        f"their seeded warps, {STRESS_LEVELS} levels, {STRESS_CAP} kept per level, brute-force "
+                        f"their seeded warps, {STRESS_LEVELS} levels, {STRESS_FRAME_CAP} kept per frame (the first in "
+                        "(level, y, x) order), brute-force "
                         "top-2 Hamming matching of every feature against every feature, ratio 0.8",
             "frames": len(frames), "pairs": npairs, "ms_per_step": step_ms,
             "frames_per_s": len(frames) / (step_ms / 1e3), "pairs_per_s": npairs / (step_ms / 1e3),

@@ -99,6 +99,12 @@ typedef struct uslam_params {
      *    circle order; 3x3 non-maximum suppression on the score, a tie going
      *    to the first pixel in raster order; strength = the arc length. */
     int detector;
+    /* 0: no per-frame cap (the reference caps per level only, common.hpp:47).
+     * > 0: the levels are filled in order, level l keeping the first
+     * min(cap_per_level, frame_cap - features kept by levels 0..l-1) of its
+     * order, so a frame keeps the first frame_cap features in (level, y, x)
+     * order (or (level, cell, y, x) with cell_cap).  No reference counterpart. */
+    int frame_cap;
 } uslam_params;
 
 /* ---- context ---------------------------------------------------------- */

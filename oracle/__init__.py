@@ -46,6 +46,9 @@ def lib():
         L.orc_detect_cfg.argtypes = [vp, C.c_uint32, C.c_uint32, vp]
         L.orc_detect_cfg.restype = None
         L.orc_frame_ex.restype = C.c_int
+        L.orc_frame_fc.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, vp, vp,
+                                   C.c_int, vp, vp]
+        L.orc_frame_fc.restype = C.c_int
         L.orc_match.argtypes = [vp, vp, vp, vp, C.c_int, C.c_int, C.c_int, vp, C.c_int]
         L.orc_match.restype = C.c_int
         L.orc_match_bruteforce.argtypes = [vp, C.c_int, vp, C.c_int, C.c_float, vp]
@@ -129,10 +132,12 @@ def describe(lvl: np.ndarray, x: int, y: int, pattern: np.ndarray):
 
 
 def frame(img: np.ndarray, pattern: np.ndarray, levels: int = 6, cap: int | None = None, cell_cap: int = 0,
-          detector: int = 0):
+          detector: int = 0, frame_cap: int = 0):
     """Features of one frame: (features[FEATURE_DTYPE], kept[levels], raw[levels]).
     cell_cap > 0 keeps at most cell_cap keypoints per 32x32 cell, listed cell by cell;
-    detector = 1 selects the cfg detection profile (FAST 9-of-16 at 20/255, 3x3 NMS)."""
+    detector = 1 selects the cfg detection profile (FAST 9-of-16 at 20/255, 3x3 NMS);
+    frame_cap > 0 keeps the first frame_cap features of the frame in (level, order
+    within the level) order, on top of the per-level cap."""
     img = np.ascontiguousarray(img, np.uint8)
     H0, W0 = img.shape
     if cap is None:
@@ -143,8 +148,8 @@ def frame(img: np.ndarray, pattern: np.ndarray, levels: int = 6, cap: int | None
     feats = np.zeros(max_feats, FEATURE_DTYPE)
     kept = np.zeros(levels, np.int32)
     raw = np.zeros(levels, np.int32)
-    n = lib().orc_frame_ex(_p(img), W0, H0, W0, levels, cap, cell_cap, detector, _p(pat), _p(feats), max_feats,
-                           _p(kept), _p(raw))
+    n = lib().orc_frame_fc(_p(img), W0, H0, W0, levels, cap, cell_cap, detector, frame_cap, _p(pat), _p(feats),
+                           max_feats, _p(kept), _p(raw))
     if n < 0:
         raise RuntimeError("orc_frame: feature buffer too small")
     return feats[:n].copy(), kept, raw

@@ -336,13 +336,18 @@ static int emit(const float* lvl, uint32_t w, uint32_t h, int x, int y, uint32_t
     return 1;
 }
 
-int orc_frame_ex(const uint8_t* img, int W0, int H0, int pitch, int levels, int cap, int cell_cap, int detector,
-                 const int32_t* pattern, orc_feature* feats, int max_feats, int* kept, int* raw) {
+int orc_frame_fc(const uint8_t* img, int W0, int H0, int pitch, int levels, int cap, int cell_cap, int detector,
+                 int frame_cap, const int32_t* pattern, orc_feature* feats, int max_feats, int* kept, int* raw) {
     uint32_t ws[32], hs[32];
     orc_level_dims(W0, H0, levels, ws, hs);
     int total = 0, ok = 1;
+    const int level_cap = cap;
     for (int l = 0; l < levels && ok; ++l) {
         const uint32_t w = ws[l], h = hs[l];
+        /* per-frame cap: the levels are filled in order, each level keeping at
+         * most what the earlier levels left of frame_cap */
+        cap = level_cap;
+        if (frame_cap > 0 && frame_cap - total < cap) cap = frame_cap - total > 0 ? frame_cap - total : 0;
         const size_t n = (size_t)w * h;
         float* lvl = (float*)malloc(n * sizeof(float));
         uint32_t* resp = (uint32_t*)malloc(n * sizeof(uint32_t));
@@ -389,6 +394,11 @@ int orc_frame_ex(const uint8_t* img, int W0, int H0, int pitch, int levels, int 
         free(culled);
     }
     return ok ? total : -1;
+}
+
+int orc_frame_ex(const uint8_t* img, int W0, int H0, int pitch, int levels, int cap, int cell_cap, int detector,
+                 const int32_t* pattern, orc_feature* feats, int max_feats, int* kept, int* raw) {
+    return orc_frame_fc(img, W0, H0, pitch, levels, cap, cell_cap, detector, 0, pattern, feats, max_feats, kept, raw);
 }
 
 int orc_frame(const uint8_t* img, int W0, int H0, int pitch, int levels, int cap,

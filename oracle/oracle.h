@@ -78,6 +78,14 @@ int orc_frame(const uint8_t* img, int W0, int H0, int pitch, int levels, int cap
  * are kept, and the level cap keeps the first `cap` of that sequence. */
 int orc_frame_ex(const uint8_t* img, int W0, int H0, int pitch, int levels, int cap, int cell_cap, int detector,
                  const int32_t* pattern, orc_feature* feats, int max_feats, int* kept, int* raw);
+/* As orc_frame_ex with a per-frame cap (no reference counterpart; the
+ * reference caps per level only, common.hpp:47): frame_cap > 0 fills the
+ * levels in order, level l keeping the first min(cap, frame_cap - features
+ * kept by levels 0..l-1) of its order, so the frame keeps the first
+ * frame_cap features in (level, y, x) order (or (level, cell, y, x) order
+ * with cell caps).  frame_cap = 0: no per-frame cap. */
+int orc_frame_fc(const uint8_t* img, int W0, int H0, int pitch, int levels, int cap, int cell_cap, int detector,
+                 int frame_cap, const int32_t* pattern, orc_feature* feats, int max_feats, int* kept, int* raw);
 /* The `cfg` detection profile on one level (detector = 1 of orc_frame_ex):
  * FAST 9-of-16 with wrap-around at 20/255, score = sum of (|p - c| - 20/255)
  * over the qualifying points, 3x3 NMS (ties to the first pixel in raster

@@ -52,3 +52,19 @@ def test_cell_cap_zero_is_the_yx_policy(brief_pattern):
     a = oracle.frame(img, brief_pattern, cell_cap=0)
     b = oracle.frame(img, brief_pattern)
     assert a[0].tobytes() == b[0].tobytes() and np.array_equal(a[1], b[1])
+
+
+@pytest.mark.parametrize("frame_cap,cell_cap", [(3000, 0), (1500, 2), (10, 0), (100000, 0)])
+def test_frame_cap_keeps_the_first_in_level_order(brief_pattern, frame_cap, cell_cap):
+    """The per-frame cap keeps the first frame_cap features of the uncapped
+    frame in (level, order within the level) order: the levels fill in order."""
+    img = synth.scene_frame(9, 752, 480)
+    full, fk, fr = oracle.frame(img, brief_pattern, cell_cap=cell_cap)
+    got, gk, gr = oracle.frame(img, brief_pattern, cell_cap=cell_cap, frame_cap=frame_cap)
+    assert np.array_equal(gr, fr)
+    n = min(frame_cap, int(fk.sum()))
+    assert int(gk.sum()) == n and got.tobytes() == full[:n].tobytes()
+    left = frame_cap
+    for l in range(len(fk)):
+        assert gk[l] == min(fk[l], max(left, 0))
+        left -= gk[l]

@@ -831,9 +831,24 @@ k_band_write(const FrameDev* __restrict__ frames, const BandItem* __restrict__ i
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int w = F.w[l], h = F.h[l], kpitch = F.kp_pitch[l];
     const uint8_t* kp = F.kpmap[l];
-    const uint32_t cap = (uint32_t)F.cap;
     const int nb = (h + 31) / 32;
     const uint32_t* bc = F.bands[l];
+    uint32_t cap = (uint32_t)F.cap;
+    if (F.frame_cap > 0) {
+        // per-frame cap: what the earlier levels left of it (their kept
+        // counts follow from their band counts, every level's being complete)
+        uint32_t left = (uint32_t)F.frame_cap;
+        for (int q = 0; q < l && left > 0u; ++q) {
+            const int nbq = (F.h[q] + 31) / 32;
+            uint32_t kq = 0;
+            for (int b2 = lane; b2 < nbq; b2 += 32) kq += F.bands[q][2 * b2 + 1];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) kq += __shfl_xor_sync(0xffffffffu, kq, o);
+            kq = min(kq, (uint32_t)F.cap);
+            left -= min(kq, left);
+        }
+        cap = min(cap, left);
+    }
     // prefix of the earlier bands' kept counts (band 0: also the level totals)
     uint32_t pk = 0, tr = 0, tk = 0;
     for (int q = threadIdx.x; q < nb; q += KBAND_THREADS) {

@@ -326,6 +326,7 @@ uslam_status create_batch(uslam_ctx* ctx, int n_frames, const int* widths, const
         F.levels = L;
         F.margin = ctx->margin;
         F.cell_cap = ctx->cell_cap;
+        F.frame_cap = ctx->frame_cap;
         F.img_pitch = static_cast<int>(round_up(static_cast<size_t>(W0), 16));
         level_dims(W0, H0, L, F.w, F.h);
         for (int l = 0; l < L; ++l) {
@@ -359,7 +360,7 @@ uslam_status create_batch(uslam_ctx* ctx, int n_frames, const int* widths, const
         }
         Ly.tmaps = take(&scratch, static_cast<size_t>(L) * kNumTileShapes * USLAM_TMAP_BYTES);
         if (ctx->matcher == 2) {
-            const size_t rows = round_up(static_cast<size_t>(L) * capa, 256);
+            const size_t rows = tc_rows(F);
             Ly.bf8 = take(&scratch, rows * 256);
             Ly.bfext = take(&scratch, rows * 32);
             Ly.bfpop = take(&scratch, rows * 4);
@@ -753,7 +754,8 @@ uslam_status uslam_create(const uslam_params* params, uslam_ctx** out) {
         params->max_width > kMaxWidth || params->max_height < 1 || params->max_height > 65535 ||
         params->cap_per_level < 0 || params->cap_per_level >= (1 << 24) || !params->brief_pattern ||
         (params->matcher < 0 || params->matcher > 2) || (params->matcher != 0 && !(params->ratio > 0.0f)) ||
-        params->cell_cap < 0 || params->cell_cap > 1024 || (params->detector != 0 && params->detector != 1))
+        params->cell_cap < 0 || params->cell_cap > 1024 || (params->detector != 0 && params->detector != 1) ||
+        params->frame_cap < 0)
         return USLAM_INVALID_ARG;
     auto* c = new uslam_ctx();
     c->device = params->device;
@@ -764,6 +766,7 @@ uslam_status uslam_create(const uslam_params* params, uslam_ctx** out) {
     c->matcher = params->matcher;
     c->ratio = params->ratio;
     c->cell_cap = params->cell_cap;
+    c->frame_cap = params->frame_cap;
     c->detector = params->detector;
     // blur-cache margin: a rotated test point lies within ceil(radius) + 1 of
     // its keypoint (rounding of the rotation), so radius + 2 covers it.
@@ -1247,7 +1250,7 @@ cudaError_t copy_frame_state(const uslam_batch* src, uslam_batch* dst, int slot,
         if (e == cudaSuccess) e = cudaMemcpyAsync(B.qorder[l], A.qorder[l], capa * 4, cudaMemcpyDeviceToDevice, st);
     }
     if (A.bf8 && B.bf8 && e == cudaSuccess) {
-        const size_t rows = round_up(static_cast<size_t>(A.levels) * capa, 256);
+        const size_t rows = tc_rows(A);
         e = cudaMemcpyAsync(B.bf8, A.bf8, rows * 256, cudaMemcpyDeviceToDevice, st);
         if (e == cudaSuccess) e = cudaMemcpyAsync(B.bfext, A.bfext, rows * 32, cudaMemcpyDeviceToDevice, st);
         if (e == cudaSuccess) e = cudaMemcpyAsync(B.bfpop, A.bfpop, rows * 4, cudaMemcpyDeviceToDevice, st);

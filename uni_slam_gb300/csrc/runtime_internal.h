@@ -54,6 +54,14 @@ namespace uslam_rt {
 
 inline size_t round_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
 
+// Operand rows of a frame for the tensor-core matcher: every kept feature of
+// the frame (at most levels x cap, or frame_cap), rounded up to 256.
+inline size_t tc_rows(const FrameDev& F) {
+    size_t n = static_cast<size_t>(F.levels) * static_cast<size_t>(F.cap > 0 ? F.cap : 1);
+    if (F.frame_cap > 0) n = std::min(n, static_cast<size_t>(F.frame_cap));
+    return round_up(n, 256);
+}
+
 // A context's last error message.  Calls on one server may fail on several
 // host threads at once (submitting threads, result readers), so a write and
 // a reader's copy each take the lock.
@@ -213,6 +221,7 @@ struct uslam_ctx {
     int margin = 0;  // blur-cache margin: BRIEF pattern radius + 2
     int matcher = 0;      // 0 windowed mutual (reference), 1 brute-force top-2
     float ratio = 0.8f;   // Lowe ratio of the brute-force matcher
+    int frame_cap = 0;    // > 0: features kept per frame, levels filled in order
     int cell_cap = 0;     // > 0: keypoints kept per 32x32 cell of a level, cell order
     int detector = 0;     // 0 reference FAST + cull, 1 cfg profile (FAST 9-of-16 at 20/255 + 3x3 NMS)
     std::map<std::pair<int, int>, int> tile_shape;  // per resolution class (autotuned or set)

@@ -50,6 +50,7 @@ struct FrameDev {
     int lvl_pitch[USLAM_MAX_LEVELS]; // pyramid level row pitch (floats): w rounded up to 4
     int margin;                      // blur cache margin M beyond the level
     int cell_cap;                    // > 0: keypoints kept per 32x32 cell (cell order); 0: (y, x) order
+    int frame_cap;                   // > 0: features kept per frame, levels filled in order; 0: none
     float* lvl[USLAM_MAX_LEVELS];
     const void* tmaps;  // CUtensorMap [levels][USLAM_NUM_TILE_SHAPES] over lvl (device, 64-byte aligned)
     float* blur[USLAM_MAX_LEVELS];
