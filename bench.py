@@ -67,7 +67,7 @@ def _args():
     ap.add_argument("--frames", type=int, default=64)
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="bounded CPU-baseline sample")
-    ap.add_argument("--serve-seconds", type=float, default=10.0, help="served-form simulation length (0: skip)")
+    ap.add_argument("--serve-seconds", type=float, default=60.0, help="served-form simulation length (0: skip)")
     ap.add_argument("--serve-streams", type=int, default=32)
     ap.add_argument("--stress-pairs", type=int, default=8, help="3840x2160 frame/warp pairs (0: skip)")
     ap.add_argument("--stress-steps", type=int, default=5)
@@ -393,44 +393,106 @@ def _config(frames: int, seed: int, world: int) -> dict:
 # ------------------------------------------------------------------ served form
 
 SERVE_SIZES = [(640, 480), (752, 480), (1280, 720)]
+SERVE_TRAJECTORY = 64  # frames of each stream's own trajectory (the batched-uniform sequence length)
+_SERVE_TEX = None
 
 
-def serve_simulation(ctx, seconds: float, n_streams: int = 32, rate_hz: float = 20.0, promote_every: int = 10,
-                     seed: int = 0, frames_per_stream: int = 6) -> dict:
-    """Camera streams of sizes drawn from 640x480 / 752x480 / 1280x720, each
-    sending plane-trajectory frames at rate_hz with exponential inter-arrival
-    times (mean 1/rate_hz), a new keyframe every promote_every frames,
-    through the server (HBM-budget admission, continuous batching).  Latency
-    runs from a frame's scheduled arrival to its completion, so admission
-    waits count."""
+def _serve_pool_init(seed: int):
+    global _SERVE_TEX
+    import numpy as np
+
+    from uni_slam_gb300 import synth
+
+    _SERVE_TEX = synth.plane_texture(np.random.RandomState(seed + 11), 4096)
+
+
+def _serve_trajectory(args):
+    k, w, h, n = args
+    from uni_slam_gb300 import synth
+
+    return synth.plane_sequence(1000 + k, n, w, h, texture=_SERVE_TEX)
+
+
+def serve_streams(n_streams: int, seed: int, n_frames: int = SERVE_TRAJECTORY):
+    """Each camera stream's size (drawn from 640x480 / 752x480 / 1280x720) and
+    its own plane trajectory of n_frames frames at that size (rendered on a
+    spawn pool, before any serving run)."""
+    import numpy as np
+
+    rs = np.random.RandomState(seed + 7)
+    sizes = [SERVE_SIZES[rs.randint(len(SERVE_SIZES))] for _ in range(n_streams)]
+    with mp.get_context("spawn").Pool(min(16, os.cpu_count() or 1), initializer=_serve_pool_init,
+                                      initargs=(seed,)) as pool:
+        frames = pool.map(_serve_trajectory, [(k, w, h, n_frames) for k, (w, h) in enumerate(sizes)])
+    return sizes, frames
+
+
+def _walk(count: int, n: int) -> int:
+    """Frame index of a stream's count-th frame: its trajectory forwards, then
+    backwards, and so on (consecutive frames stay neighbours on the path)."""
+    if n < 2:
+        return 0
+    period = 2 * (n - 1)
+    c = count % period
+    return c if c < n else period - c
+
+
+class _ResultBuffers:
+    """Host buffers a client reads one request's results into (one ABI call
+    per request; sized for the largest frame of the served context)."""
+
+    def __init__(self, ctx):
+        import numpy as np
+
+        from uni_slam_gb300.capi import FEATURE_DTYPE, MATCH_DTYPE
+
+        cap = 333 * ctx.levels
+        self.feats = np.zeros(cap, FEATURE_DTYPE)
+        self.matches = np.zeros(cap, MATCH_DTYPE)
+        self.kept = np.zeros(ctx.levels, np.int32)
+        self.raw = np.zeros(ctx.levels, np.int32)
+
+
+def serve_simulation(ctx, sizes, frames, seconds: float, rate_hz: float = 20.0, promote_every: int = 10,
+                     seed: int = 0) -> dict:
+    """Camera streams each walking their own trajectory at rate_hz with
+    exponential inter-arrival times (mean 1/rate_hz), a new keyframe every
+    promote_every frames, through the server (HBM-budget admission,
+    continuous batching).  Latency runs from a frame's scheduled arrival until
+    the client holds its features and matches in host memory, so admission
+    waits and the result copy count."""
     import heapq
     import queue
 
     import numpy as np
 
-    from uni_slam_gb300 import Server, synth
+    from uni_slam_gb300 import Server
 
-    rs = np.random.RandomState(seed + 7)
-    tex = synth.plane_texture(np.random.RandomState(seed + 11), 4096)
-    sizes = [SERVE_SIZES[rs.randint(len(SERVE_SIZES))] for _ in range(n_streams)]
-    frames = [synth.plane_sequence(1000 + k, frames_per_stream, w, h, texture=tex) for k, (w, h) in enumerate(sizes)]
+    n_streams = len(sizes)
+    rs = np.random.RandomState(seed + 13)
     srv = Server(ctx, SERVE_SIZES, hbm_budget_bytes=8 << 30, max_batch=64)
     ids = [srv.open_stream(w, h) for (w, h) in sizes]
     count = [0] * n_streams
     done_q: queue.Queue = queue.Queue()
     lat: list[float] = []
-    parts: list[tuple[float, float, float]] = []  # (time since start, admission delay, server latency) in ms
+    parts: list[tuple[float, float, float, float]] = []  # (t since start, admission, server, result copy) in ms
+    bufs = _ResultBuffers(ctx)
+    copied = [0, 0]  # features, matches handed to the client
 
     def completer():
         while True:
             item = done_q.get()
             if item is None:
                 return
-            tk, admit_delay_ms, t_rel = item
+            tk, t_sched, admit_delay_ms, t_rel = item
             srv.wait(tk, 0)
-            server_ms = srv.latency_ms(tk)
-            lat.append(admit_delay_ms + server_ms)
-            parts.append((t_rel, admit_delay_ms, server_ms))
+            t0 = time.perf_counter()
+            nf, nm, server_ms = srv.result_into(tk, bufs.feats, bufs.matches, bufs.kept, bufs.raw)
+            t_have = time.perf_counter()
+            lat.append((t_have - t_sched) * 1e3)
+            parts.append((t_rel, admit_delay_ms, server_ms, (t_have - t0) * 1e3))
+            copied[0] += nf
+            copied[1] += nm
             srv.release(tk)
 
     th = threading.Thread(target=completer, daemon=True)
@@ -445,14 +507,14 @@ def serve_simulation(ctx, seconds: float, n_streams: int = 32, rate_hz: float = 
         now = time.perf_counter()
         if t_sched > now:
             time.sleep(t_sched - now)
-        img = frames[k][count[k] % frames_per_stream]
+        img = frames[k][_walk(count[k], len(frames[k]))]
         while True:
             tk = srv.submit(ids[k], img, promote=(count[k] % promote_every == 0))
             if tk is not None:
                 break
             refused += 1
             time.sleep(50e-6)
-        done_q.put((tk, (time.perf_counter() - t_sched) * 1e3, (t_sched - start) * 1e3))
+        done_q.put((tk, t_sched, (time.perf_counter() - t_sched) * 1e3, (t_sched - start) * 1e3))
         count[k] += 1
         heapq.heappush(heap, (t_sched + rs.exponential(1.0 / rate_hz), k))
     done_q.put(None)
@@ -465,34 +527,38 @@ def serve_simulation(ctx, seconds: float, n_streams: int = 32, rate_hz: float = 
         "streams": n_streams, "rate_hz_per_stream": rate_hz, "seconds": seconds, "frames": int(arr.size),
         "fps": arr.size / elapsed, "p50_ms": float(np.percentile(arr, 50)), "p99_ms": float(np.percentile(arr, 99)),
         "max_ms": float(arr.max()),
+        "latency": "scheduled arrival -> features and matches in the client's host buffers",
+        "results_copied": True, "features_copied": copied[0], "matches_copied": copied[1],
+        "trajectory": f"each stream walks its own {len(frames[0])}-frame plane trajectory at its size, forwards then "
+                      "backwards",
         # the five slowest frames: when, and how the latency splits between the
-        # client's admission (the frame waited to be submitted) and the server
-        "slowest": [{"t_ms": round(t, 1), "admission_ms": round(a, 3), "server_ms": round(b, 3)}
-                    for t, a, b in sorted(parts, key=lambda x: -(x[1] + x[2]))[:5]],
+        # client's admission (the frame waited to be submitted), the server, and
+        # the result copy into the client's buffers
+        "slowest": [{"t_ms": round(t, 1), "admission_ms": round(a, 3), "server_ms": round(b, 3),
+                     "result_copy_ms": round(c, 3)}
+                    for t, a, b, c in sorted(parts, key=lambda x: -(x[1] + x[2] + x[3]))[:5]],
         "admission_retries": refused, "launches": st["launches"],
         "max_batch_seen": st["max_batch_seen"], "slots": st["slots"],
         "sizes": {f"{w}x{h}": sizes.count((w, h)) for (w, h) in SERVE_SIZES},
     }
 
 
-def serve_saturation(ctx, seconds: float, n_streams: int = 32, inflight: int = 4, promote_every: int = 10,
-                     seed: int = 0, frames_per_stream: int = 6, submitters: int = 4) -> dict:
+def serve_saturation(ctx, sizes, frames, seconds: float, inflight: int = 4, promote_every: int = 10,
+                     submitters: int = 4) -> dict:
     """Closed-loop capacity of the serving loop: the same streams as
     serve_simulation, each keeping `inflight` frames outstanding (a new frame
-    is submitted as soon as one completes), so the dispatcher always finds
-    queued requests and batches them.  `submitters` host threads each feed a
-    share of the streams (frame copies into pinned staging run in parallel).
-    Latency runs from submit to completion."""
+    is submitted as soon as one's results are in the client's buffers), so
+    the dispatcher always finds queued requests and batches them.
+    `submitters` host threads each feed a share of the streams (frame copies
+    into pinned staging run in parallel).  Latency runs from submit until the
+    client holds the results."""
     import queue
 
     import numpy as np
 
-    from uni_slam_gb300 import Server, synth
+    from uni_slam_gb300 import Server
 
-    rs = np.random.RandomState(seed + 7)
-    tex = synth.plane_texture(np.random.RandomState(seed + 11), 4096)
-    sizes = [SERVE_SIZES[rs.randint(len(SERVE_SIZES))] for _ in range(n_streams)]
-    frames = [synth.plane_sequence(1000 + k, frames_per_stream, w, h, texture=tex) for k, (w, h) in enumerate(sizes)]
+    n_streams = len(sizes)
     srv = Server(ctx, SERVE_SIZES, hbm_budget_bytes=8 << 30, max_batch=64)
     ids = [srv.open_stream(w, h) for (w, h) in sizes]
     count = [0] * n_streams
@@ -500,15 +566,17 @@ def serve_saturation(ctx, seconds: float, n_streams: int = 32, inflight: int = 4
     lock = threading.Lock()
     done_q: queue.Queue = queue.Queue()
     lat: list[float] = []
+    bufs = _ResultBuffers(ctx)
 
     def completer():
         while True:
             item = done_q.get()
             if item is None:
                 return
-            tk, k = item
+            tk, k, t_submit = item
             srv.wait(tk, 0)
-            lat.append(srv.latency_ms(tk))
+            srv.result_into(tk, bufs.feats, bufs.matches, bufs.kept, bufs.raw)
+            lat.append((time.perf_counter() - t_submit) * 1e3)
             srv.release(tk)
             with lock:
                 outstanding[k] -= 1
@@ -528,14 +596,15 @@ def serve_saturation(ctx, seconds: float, n_streams: int = 32, inflight: int = 4
                     free = outstanding[k] < inflight
                 if not free:
                     continue
-                tk = srv.submit(ids[k], frames[k][count[k] % frames_per_stream],
+                t_submit = time.perf_counter()
+                tk = srv.submit(ids[k], frames[k][_walk(count[k], len(frames[k]))],
                                 promote=(count[k] % promote_every == 0))
                 if tk is None:
                     refused[me] += 1
                     continue
                 with lock:
                     outstanding[k] += 1
-                done_q.put((tk, k))
+                done_q.put((tk, k, t_submit))
                 count[k] += 1
                 progressed = True
             if not progressed:
@@ -555,7 +624,7 @@ def serve_saturation(ctx, seconds: float, n_streams: int = 32, inflight: int = 4
     arr = np.array(lat)
     return {
         "streams": n_streams, "inflight_per_stream": inflight, "submit_threads": submitters, "seconds": seconds,
-        "frames": int(arr.size),
+        "frames": int(arr.size), "results_copied": True,
         "fps": arr.size / elapsed, "p50_ms": float(np.percentile(arr, 50)), "p99_ms": float(np.percentile(arr, 99)),
         "admission_retries": refused, "launches": st["launches"], "max_batch_seen": st["max_batch_seen"],
         "frames_per_launch": arr.size / max(1, st["launches"]),
@@ -935,6 +1004,8 @@ def run_ours(a):
     pat = patmod.load()
     frames = synth.plane_sequence(a.seed + rank, n=a.frames)
     n = len(frames)
+    # the served streams' trajectories, rendered before any GPU work
+    serve_sizes, serve_frames = serve_streams(a.serve_streams, a.seed + rank) if a.serve_seconds > 0 else (None, None)
     ctx = Context(pat, levels=LEVELS, max_width=W, max_height=H, device=local)
     batch = Batch(ctx, [(W, H)] * n, [(i, i + 1) for i in range(n - 1)])
     for i, f in enumerate(frames):
@@ -1104,9 +1175,9 @@ def run_ours(a):
         gc.collect()
         gc.disable()
         try:
-            served = serve_simulation(sctx, a.serve_seconds, n_streams=a.serve_streams, seed=a.seed + rank)
-            served["saturation"] = serve_saturation(sctx, min(a.serve_seconds, 5.0), n_streams=a.serve_streams,
-                                                    seed=a.seed + rank)
+            served = serve_simulation(sctx, serve_sizes, serve_frames, a.serve_seconds, seed=a.seed + rank)
+            served["saturation"] = serve_saturation(sctx, serve_sizes, serve_frames, min(a.serve_seconds, 5.0))
+            served["saturation"]["over_plain"] = served["saturation"]["fps"] / plain_fps
         finally:
             gc.enable()
         served["client_gc"] = "paused during the runs"

@@ -109,3 +109,16 @@ def test_reference_arm_nonzero_rank_exits_quietly():
     r = subprocess.run([sys.executable, os.path.join(REPO, "bench.py"), "--impl", "reference", "--steps", "1",
                         "--warmup", "0", "--frames", "2"], capture_output=True, text=True, env=env, timeout=300)
     assert r.returncode == 0 and r.stdout.strip() == ""
+
+
+def test_served_streams_walk_their_trajectory_back_and_forth():
+    """A served stream's frames follow its trajectory forwards, then
+    backwards: every step moves to a neighbouring frame, every frame is used."""
+    import bench
+
+    n = 64
+    idx = [bench._walk(c, n) for c in range(5 * n)]
+    assert idx[:n] == list(range(n)) and idx[n] == n - 2
+    assert all(abs(a - b) == 1 for a, b in zip(idx, idx[1:]))
+    assert set(idx) == set(range(n))
+    assert bench._walk(7, 1) == 0

@@ -53,6 +53,8 @@ struct SrvSlot {
     int32_t* b2a = nullptr;
     int32_t* matches = nullptr;
     uint32_t* match_count = nullptr;
+    uint32_t* h_res = nullptr;  // pinned, mapped: the frame's results as the emit kernel lays them out
+    uint32_t* d_res = nullptr;  // device address of h_res
 };
 
 struct SrvReq {
@@ -79,6 +81,65 @@ struct LaunchBuf {
     size_t bytes = 0;
     bool busy = false;
 };
+
+// One frame of a launch whose results the emit kernel writes to host memory.
+struct SrvEmitItem {
+    int slot;
+    int per;                      // match block stride (entries per level); 0: the frame has no pair
+    const int32_t* matches;       // the pair's match blocks
+    const uint32_t* match_count;  // the pair's per-level match counts
+    uint32_t* out;                // device address of the slot's mapped host result area
+};
+
+// Words of a result area before the feature records: kept[L], raw[L],
+// matches[L] (clamped to the block stride), padded to 16 bytes.
+__host__ __device__ inline int res_header_words(int L) { return (3 * L + 3) / 4 * 4; }
+
+// Result area of one frame (pinned host memory, written by the device):
+// header, then every kept feature (48 B) level by level, then every match
+// (16 B) level by level -- what uslam_server_result hands out, so the
+// results reach host memory with the launch and a result call reads no
+// device memory.
+__global__ void __launch_bounds__(256) k_server_emit(const FrameDev* __restrict__ frames,
+                                                      const SrvEmitItem* __restrict__ items, int L) {
+    __shared__ uint32_t s_cnt[2][USLAM_MAX_LEVELS];
+    __shared__ uint32_t s_off[2][USLAM_MAX_LEVELS + 1];
+    const SrvEmitItem it = items[blockIdx.x];
+    const FrameDev& F = frames[it.slot];
+    const int hw = res_header_words(L);
+    if (threadIdx.x == 0) {
+        uint32_t fo = 0, mo = 0;
+        for (int l = 0; l < L; ++l) {
+            const uint32_t k = F.kept[l];
+            const uint32_t m = it.per > 0 ? min(it.match_count[l], (uint32_t)it.per) : 0u;
+            s_cnt[0][l] = k;
+            s_cnt[1][l] = m;
+            s_off[0][l] = fo;
+            s_off[1][l] = mo;
+            fo += k;
+            mo += m;
+            it.out[l] = k;
+            it.out[L + l] = F.raw[l];
+            it.out[2 * L + l] = m;
+        }
+        s_off[0][L] = fo;
+        s_off[1][L] = mo;
+        for (int q = 3 * L; q < hw; ++q) it.out[q] = 0u;
+    }
+    __syncthreads();
+    uint4* fdst = reinterpret_cast<uint4*>(it.out + hw);
+    uint4* mdst = fdst + 3u * s_off[0][L];
+    for (int l = 0; l < L; ++l) {
+        const uint4* src = reinterpret_cast<const uint4*>(F.feats[l]);
+        uint4* dst = fdst + 3u * s_off[0][l];
+        for (uint32_t i = threadIdx.x; i < 3u * s_cnt[0][l]; i += blockDim.x) dst[i] = src[i];
+        if (it.per > 0) {
+            const uint4* msrc = reinterpret_cast<const uint4*>(it.matches) + (size_t)l * it.per;
+            uint4* md = mdst + s_off[1][l];
+            for (uint32_t i = threadIdx.x; i < s_cnt[1][l]; i += blockDim.x) md[i] = msrc[i];
+        }
+    }
+}
 
 }  // namespace
 
@@ -121,7 +182,8 @@ size_t tables_bytes(int max_batch, int max_tiles_per_frame, int max_bands_per_fr
     const size_t u = round_up(sizeof(SegDev) * static_cast<size_t>(max_batch) * levels, 256);
     const size_t p = round_up(sizeof(PairDev) * static_cast<size_t>(max_batch), 256);
     const size_t b = round_up(sizeof(BandItem) * static_cast<size_t>(max_batch) * max_bands_per_frame, 256);
-    return t + f + m + u + p + b;
+    const size_t x = round_up(sizeof(SrvEmitItem) * static_cast<size_t>(max_batch), 256);
+    return t + f + m + u + p + b + x;
 }
 
 void free_server(uslam_server* s) {
@@ -132,8 +194,10 @@ void free_server(uslam_server* s) {
     }
     for (auto& L : s->inflight)
         if (L.done) cudaEventDestroy(L.done);
-    for (auto& sl : s->slots)
+    for (auto& sl : s->slots) {
         if (sl.h_in) cudaFreeHost(sl.h_in);
+        if (sl.h_res) cudaFreeHost(sl.h_res);
+    }
     for (auto& c : s->cs)
         if (c) cudaStreamDestroy(c);
     if (s->arena) cudaFree(s->arena);
@@ -156,11 +220,21 @@ cudaError_t launch_batch(uslam_server* s, const std::vector<uint64_t>& tickets, 
     std::vector<MatchSegDev> msegs;
     std::vector<PairDev> pairs;
     std::vector<BandItem> bands;
+    std::vector<SrvEmitItem> emits;
     cudaError_t e = cudaSuccess;
     for (uint64_t tk : tickets) {
         SrvReq& r = s->reqs[tk];
         SrvSlot& sl = s->slots[r.slot];
         const SrvClass& C = s->classes[sl.cls];
+        SrvEmitItem em{};
+        em.slot = r.slot;
+        em.out = sl.d_res;
+        if (r.ref >= 0) {
+            em.per = std::max(s->frames[r.ref].cap, 1);
+            em.matches = sl.matches;
+            em.match_count = sl.match_count;
+        }
+        emits.push_back(em);
         for (TileItem t : C.tiles) {
             t.frame = static_cast<uint16_t>(r.slot);
             shaped.by_shape[C.shape].push_back(t);
@@ -212,7 +286,8 @@ cudaError_t launch_batch(uslam_server* s, const std::vector<uint64_t>& tickets, 
     const size_t u_b = round_up(usegs.size() * sizeof(SegDev), 256);
     const size_t p_b = round_up(pairs.size() * sizeof(PairDev), 256);
     const size_t b_b = round_up(bands.size() * sizeof(BandItem), 256);
-    if (t_b + f_b + m_b + u_b + p_b + b_b > B.bytes) return cudaErrorInvalidValue;
+    const size_t x_b = round_up(emits.size() * sizeof(SrvEmitItem), 256);
+    if (t_b + f_b + m_b + u_b + p_b + b_b + x_b > B.bytes) return cudaErrorInvalidValue;
     char* h = B.h;
     std::memcpy(h, tiles.data(), tiles.size() * sizeof(TileItem));
     std::memcpy(h + t_b, fsegs.data(), fsegs.size() * sizeof(SegDev));
@@ -220,7 +295,8 @@ cudaError_t launch_batch(uslam_server* s, const std::vector<uint64_t>& tickets, 
     std::memcpy(h + t_b + f_b + m_b, usegs.data(), usegs.size() * sizeof(SegDev));
     std::memcpy(h + t_b + f_b + m_b + u_b, pairs.data(), pairs.size() * sizeof(PairDev));
     std::memcpy(h + t_b + f_b + m_b + u_b + p_b, bands.data(), bands.size() * sizeof(BandItem));
-    const size_t total = t_b + f_b + m_b + u_b + p_b + b_b;
+    std::memcpy(h + t_b + f_b + m_b + u_b + p_b + b_b, emits.data(), emits.size() * sizeof(SrvEmitItem));
+    const size_t total = t_b + f_b + m_b + u_b + p_b + b_b + x_b;
     e = cudaMemcpyAsync(B.d, h, total, cudaMemcpyHostToDevice, st);
     if (e != cudaSuccess) return e;
     const auto* d_tiles = reinterpret_cast<const TileItem*>(B.d);
@@ -229,6 +305,7 @@ cudaError_t launch_batch(uslam_server* s, const std::vector<uint64_t>& tickets, 
     const auto* d_usegs = reinterpret_cast<const SegDev*>(B.d + t_b + f_b + m_b);
     const auto* d_pairs = reinterpret_cast<const PairDev*>(B.d + t_b + f_b + m_b + u_b);
     const auto* d_bands = reinterpret_cast<const BandItem*>(B.d + t_b + f_b + m_b + u_b + p_b);
+    const auto* d_emits = reinterpret_cast<const SrvEmitItem*>(B.d + t_b + f_b + m_b + u_b + p_b + b_b);
     const int grid = c->num_sms * 4;
     const int nf = static_cast<int>(fsegs.size());
     if ((e = launch_detect_shaped(s->d_frames, d_tiles, shaped.begin, c->detector, s->d_err, st)) != cudaSuccess) return e;
@@ -244,6 +321,9 @@ cudaError_t launch_batch(uslam_server* s, const std::vector<uint64_t>& tickets, 
             cudaSuccess)
             return e;
     }
+    // every frame's features and matches to its slot's host result area
+    k_server_emit<<<static_cast<int>(emits.size()), 256, 0, st>>>(s->d_frames, d_emits, lv);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
     // the error word (kernel bounds checks, tile-load wait limits) travels
     // with the launch and is read when the launch completes
     if ((e = cudaMemcpyAsync(&s->h_err[bufi], s->d_err, sizeof(uint32_t), cudaMemcpyDeviceToHost, st)) != cudaSuccess)
@@ -494,6 +574,13 @@ uslam_status uslam_server_create(uslam_ctx* ctx, const uslam_server_params* p, u
             sl.matches = reinterpret_cast<int32_t*>(base + Y.matches);
             sl.match_count = reinterpret_cast<uint32_t*>(base + Y.mcount);
             if (e == cudaSuccess) e = cudaHostAlloc(&sl.h_in, static_cast<size_t>(F.H0) * F.img_pitch, cudaHostAllocDefault);
+            // results: header, every feature the slot can keep, every match of its
+            // pair (a keyframe of the same size class has the same cap)
+            const size_t capr = static_cast<size_t>(std::max(F.cap, 1)) * L;
+            const size_t res_bytes = 4 * static_cast<size_t>(res_header_words(L)) + 48 * capr + 16 * capr;
+            if (e == cudaSuccess)
+                e = cudaHostAlloc(&sl.h_res, res_bytes, cudaHostAllocMapped | cudaHostAllocPortable);
+            if (e == cudaSuccess) e = cudaHostGetDevicePointer(&sl.d_res, sl.h_res, 0);
         }
     }
     if (e == cudaSuccess) e = cudaMalloc(&s->d_frames, sizeof(FrameDev) * nslots);
@@ -624,43 +711,28 @@ uslam_status uslam_server_result(uslam_server* s, uint64_t ticket, uslam_feature
     lk.unlock();
     const int L = s->levels;
     if (latency_ms) *latency_ms = std::chrono::duration<double, std::milli>(r.t_done - r.t_submit).count();
-    std::vector<uint32_t> counts(2 * L);
-    cudaError_t e = cudaMemcpy(counts.data(), F.kept, sizeof(uint32_t) * 2 * L, cudaMemcpyDeviceToHost);
-    if (e != cudaSuccess) return s->ctx->cuda_fail(e, "result");
-    int total = 0;
+    // the launch wrote everything to the slot's host result area before its
+    // completion event (k_server_emit): no device access here
+    (void)F;
+    const uint32_t* res = sl.h_res;
+    int total = 0, nm = 0;
     for (int l = 0; l < L; ++l) {
-        if (kept) kept[l] = static_cast<int>(counts[l]);
-        if (raw) raw[l] = static_cast<int>(counts[L + l]);
-        total += static_cast<int>(counts[l]);
+        if (kept) kept[l] = static_cast<int>(res[l]);
+        if (raw) raw[l] = static_cast<int>(res[L + l]);
+        total += static_cast<int>(res[l]);
+        nm += static_cast<int>(res[2 * L + l]);
     }
+    const uint32_t* frec = res + res_header_words(L);
     if (feats) {
         if (total > max_feats) return set_err(&s->ctx->err, USLAM_CAPACITY, "result: feature buffer too small");
-        int n = 0;
-        for (int l = 0; l < L && e == cudaSuccess; ++l) {
-            e = cudaMemcpy(feats + n, F.feats[l], sizeof(uslam_feature) * counts[l], cudaMemcpyDeviceToHost);
-            n += static_cast<int>(counts[l]);
-        }
-        if (e != cudaSuccess) return s->ctx->cuda_fail(e, "result");
+        std::memcpy(feats, frec, sizeof(uslam_feature) * static_cast<size_t>(total));
     }
     if (n_matches) *n_matches = 0;
     if (r.ref < 0) return USLAM_NOT_READY;  // no keyframe to match against (the stream's first frame)
-    std::vector<uint32_t> mc(L);
-    e = cudaMemcpy(mc.data(), sl.match_count, sizeof(uint32_t) * L, cudaMemcpyDeviceToHost);
-    if (e != cudaSuccess) return s->ctx->cuda_fail(e, "result");
-    const int per = std::max(s->frames[r.ref].cap, 1);
-    int nm = 0;
-    for (int l = 0; l < L; ++l) nm += static_cast<int>(std::min<uint32_t>(mc[l], per));
     if (n_matches) *n_matches = nm;
     if (matches) {
         if (nm > max_matches) return set_err(&s->ctx->err, USLAM_CAPACITY, "result: match buffer too small");
-        int n = 0;
-        for (int l = 0; l < L && e == cudaSuccess; ++l) {
-            const int cnt = static_cast<int>(std::min<uint32_t>(mc[l], per));
-            e = cudaMemcpy(matches + n, sl.matches + static_cast<size_t>(l) * per * 4, sizeof(uslam_match) * cnt,
-                           cudaMemcpyDeviceToHost);
-            n += cnt;
-        }
-        if (e != cudaSuccess) return s->ctx->cuda_fail(e, "result");
+        std::memcpy(matches, frec + 12 * static_cast<size_t>(total), sizeof(uslam_match) * static_cast<size_t>(nm));
     }
     return USLAM_OK;
 }

@@ -400,6 +400,18 @@ class Server:
         self.ctx.check(st, "result", ok=(capi.OK, capi.NOT_READY))
         return feats, kept, raw, (m if st == capi.OK else None), lat.value
 
+    def result_into(self, ticket: int, feats: np.ndarray, matches: np.ndarray, kept: np.ndarray,
+                    raw: np.ndarray) -> tuple[int, int, float]:
+        """Results of a finished request into caller buffers (one call; the
+        server already holds them in host memory): (features, matches,
+        server latency in ms); the counts per level land in kept / raw."""
+        nm = C.c_int()
+        lat = C.c_double()
+        st = self.lib.uslam_server_result(self.h, ticket, ptr(feats), feats.size, iptr(kept), iptr(raw), ptr(matches),
+                                          matches.size, C.byref(nm), C.byref(lat))
+        self.ctx.check(st, "result", ok=(capi.OK, capi.NOT_READY))
+        return int(kept.sum()), (nm.value if st == capi.OK else 0), lat.value
+
     def latency_ms(self, ticket: int) -> float:
         """Submit-to-completion time of a finished request (no data copied)."""
         lat = C.c_double()
