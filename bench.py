@@ -631,6 +631,54 @@ def serve_saturation(ctx, sizes, frames, seconds: float, inflight: int = 4, prom
     }
 
 
+# ------------------------------------------------------------------ plugin path
+
+def plugin_run(pat, frames, warmup: int = 8, timed: int = 256, advance_every: int = 1) -> dict:
+    """The drop-in passes as the reference's pipeline runs them: per frame a
+    FrameBW of f32 pixels in AnyBag, CudaFeatureDetectPass (pinned staging of
+    the u8 bytes, asynchronous upload, the frame's work, its feature set and
+    matches copied back) and CudaMatchPass, with FeatureSet and MatchResult
+    built in AnyBag (include/uslam_wslam.hpp, compiled against stand-ins of
+    the reference's headers in tests/adapter/stubs).  Wall clock per frame
+    around the two passes."""
+    import struct
+    import subprocess
+    import tempfile
+
+    import numpy as np
+
+    from uni_slam_gb300 import level_dims
+
+    here = os.path.join(REPO, "tests", "adapter")
+    lib = os.path.join(REPO, "uni_slam_gb300")
+    with tempfile.TemporaryDirectory() as td:
+        exe = os.path.join(td, "adapter_bench")
+        subprocess.run(["g++", "-std=c++20", "-O2", "-I", os.path.join(here, "stubs"), "-I",
+                        os.path.join(REPO, "include"), os.path.join(here, "adapter_bench.cpp"), "-o", exe, "-L", lib,
+                        "-luslam", f"-Wl,-rpath,{lib}"], check=True, capture_output=True)
+        with open(os.path.join(td, "pattern.bin"), "wb") as f:
+            f.write(np.ascontiguousarray(pat, "<i4").tobytes())
+        with open(os.path.join(td, "frames.bin"), "wb") as f:
+            f.write(struct.pack("<3i", len(frames), W, H))
+            for img in frames:
+                f.write(struct.pack("<i", 0))
+                f.write(np.ascontiguousarray(img, np.uint8).tobytes())
+        r = subprocess.run([exe, os.path.join(td, "pattern.bin"), os.path.join(td, "frames.bin"), str(warmup),
+                            str(timed), str(advance_every)], capture_output=True, text=True, timeout=600)
+        if r.returncode != 0:
+            return {"error": f"adapter_bench rc={r.returncode}: {r.stderr[-300:]}"}
+        out = json.loads(r.stdout.strip().splitlines()[-1])
+    cap = W * H // 250
+    # per frame: the u8 frame up; the frame's counts + feature blocks and the
+    # pair's counts + match blocks down (uslam_frontend_process)
+    d2h = 8 * LEVELS + LEVELS * cap * 48 + ((4 * LEVELS + 15) // 16 * 16) + LEVELS * cap * 16
+    return {"value": out["frames_per_s"], "unit": "frames/s", "h2d_bytes_per_step": W * H,
+            "d2h_bytes_per_step": d2h, "step": "one frame", "frames": out["frames"],
+            "features_per_frame": out["features"] / out["frames"], "matches_per_frame": out["matches"] / out["frames"],
+            "method": "CudaFeatureDetectPass + CudaMatchPass on FrameBW f32 host frames, one frame per call "
+                      "(keyframe advanced every frame), outputs as FeatureSet / MatchResult in AnyBag"}
+
+
 # ------------------------------------------------------------------ GPU side
 
 UNEVEN_MIX = [(640, 480, 16), (752, 480, 16), (1280, 720, 8), (1920, 1080, 4), (3840, 2160, 2)]
@@ -754,7 +802,6 @@ def cfg_run(pat, local: int, frames, steps: int, warmup: int, matcher: int = 1) 
                         "with 3x3 NMS, brute-force top-2 Hamming matching at ratio 0.8 against the previous frame",
             "frames": n, "ms_per_step": step_ms, "frames_per_s": n / (step_ms / 1e3),
             "features_per_frame": sum(kept) / n, "matches_per_pair": sum(nmatch) / max(1, n - 1),
-            "reference_match_check": ref_check,
             "kernel_ms": prof, "l2": "flushed (256 MiB write) between timed steps",
             "match_lists": [_mm_digest(batch.matches(k)) for k in range(n - 1)],
         }
@@ -1162,6 +1209,9 @@ def run_ours(a):
     plain_fps = n / plain_s
     fe.close()
 
+    # ---- the drop-in passes on FrameBW host frames (the reference's call path)
+    plugin = plugin_run(pat, frames) if rank == 0 else None
+
     served = None
     if a.serve_seconds > 0:
         # keyframes hold up to 2000 descriptors: 333 per level x 6 levels
@@ -1223,7 +1273,7 @@ def run_ours(a):
             "warmup": a.warmup, "ms_per_step": step_ms_max, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32+u32", "data": "synthetic (seeded plane trajectory; EuRoC absent)",
             "config": _config(n, a.seed, world),
-            "plain_fps": plain_fps, "batched_over_plain": value / world / plain_fps,
+            "plain_fps": plain_fps, "batched_over_plain": value / world / plain_fps, "plugin_e2e": plugin,
             "e2e": {"value": n * world / e2e_s, "unit": "frames/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h,
                     "method": f"{E2E_DEPTH} batches in flight, each on its own stream: per step pinned H2D of the "

@@ -309,10 +309,23 @@ void uslam_frontend_destroy(uslam_frontend* fe);
  * FeatureSet(0).  advance_reference mirrors the "gen:feat:refadv" marker:
  * the previous current set becomes the reference before this frame is
  * stored.  Returns USLAM_NOT_READY (features computed, no matching) when no
- * reference exists yet.  Synchronous. */
+ * reference exists yet.  The frame is copied into a pinned staging buffer
+ * and uploaded by an asynchronous copy on the frontend's stream (the u8
+ * upload of FillPyramidPass::writeBaseLayer, fill_pyramid.cpp:221-269); the
+ * new feature set and matches are copied back behind the work, so the
+ * feature and match getters below read host memory.  Synchronous: returns
+ * when the frame's work and copies are complete. */
 uslam_status uslam_frontend_process(uslam_frontend* fe, const uint8_t* img, int pitch, int advance_reference);
+/* The same for the reference's f32 FrameBW pixels in [0, 1] (pitch in
+ * floats): each pixel becomes lrintf(p * 255) clamped to [0, 255] while it is
+ * written into the pinned staging -- exact for the u8 / 255 values
+ * data::getLocalFrame stores (data/src/provider_base.cpp:121-124) -- and the
+ * u8 frame is uploaded, a quarter of the f32 bytes. */
+uslam_status uslam_frontend_process_f32(uslam_frontend* fe, const float* img, int pitch, int advance_reference);
 uslam_status uslam_frontend_input_device(uslam_frontend* fe, uint8_t** dev_ptr, int* pitch);
-/* which = 0: current set, 1: reference set. */
+/* which = 0: current set, 1: reference set.  After uslam_frontend_process
+ * these read the copies that came back with the frame; after
+ * uslam_frontend_enqueue they first copy the outputs back (synchronous). */
 uslam_status uslam_frontend_features(uslam_frontend* fe, int which, uslam_feature* out, int max_out, int* kept,
                                      int* raw);
 uslam_status uslam_frontend_matches(uslam_frontend* fe, uslam_match* out, int max_out, int* n_out);

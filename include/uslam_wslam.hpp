@@ -103,13 +103,11 @@ class CudaFeatureDetectPass : public compute::Pass {
         if (!frame) return std::string("no frame under ") + ResourceIdentifier::GetFrameName(0);
         const data::FrameBW& f = **frame;
         if (auto err = gpu_->ensure(f.width, f.height)) return err;
-        // provider_base.cpp:121-124 stored u8 / 255; recover the byte exactly
-        u8_.resize(f.pixels.size());
-        for (size_t i = 0; i < f.pixels.size(); ++i)
-            u8_[i] = static_cast<uint8_t>(std::clamp(std::lrintf(f.pixels[i] * 255.0f), 0L, 255L));
         // consume-once marker (common.hpp:134-142), as LoadDataCPUPass does
         const bool advance = storage_.take<bool>(ResourceIdentifier::FeatureReferenceAdvanceName).value_or(false);
-        const uslam_status s = uslam_frontend_process(gpu_->frontend(), u8_.data(), f.width, advance ? 1 : 0);
+        // provider_base.cpp:121-124 stored u8 / 255: the library recovers each
+        // byte exactly while staging the frame in pinned memory and uploads u8
+        const uslam_status s = uslam_frontend_process_f32(gpu_->frontend(), f.pixels.data(), f.width, advance ? 1 : 0);
         if (s != USLAM_OK && s != USLAM_NOT_READY)
             return std::string("uslam_frontend_process: ") + uslam_last_error(gpu_->ctx());
         auto current = download(0);
@@ -157,7 +155,6 @@ class CudaFeatureDetectPass : public compute::Pass {
 
     std::shared_ptr<CudaFrontend> gpu_;
     AnyBag& storage_;
-    std::vector<uint8_t> u8_;
 };
 
 class CudaMatchPass : public compute::Pass {

@@ -74,6 +74,21 @@ def test_padded_rows_every_entry_point(brief_pattern):
             assert np.array_equal(_mm(fe.matches()), em)
         finally:
             fe.close()
+        # frontend on the reference's f32 FrameBW pixels, padded rows (pitch in
+        # floats): the bytes are recovered while staging, the results come back
+        # with the frame (the reference set's too)
+        fe = Frontend(c, W, H)
+        try:
+            q0 = (p0.astype(np.float32) / np.float32(255.0)).astype(np.float32)
+            q1 = (p1.astype(np.float32) / np.float32(255.0)).astype(np.float32)
+            assert not fe.process_f32(q0, pitch=PITCH)
+            _same(fe.features(0), e0)
+            assert fe.process_f32(q1, pitch=PITCH)
+            _same(fe.features(0), e1)
+            _same(fe.features(1), e0)
+            assert np.array_equal(_mm(fe.matches()), em)
+        finally:
+            fe.close()
         # single-frame sets: u8 (pitch in bytes) and f32 (pitch in floats)
         with FeatureSet(c, W, H) as a, FeatureSet(c, W, H) as bset:
             c.check(lib.uslam_detect_describe(c.h, capi.ptr(p0), W, H, PITCH, a.h), "detect_describe")

@@ -100,6 +100,7 @@ SIGNATURES = {
     "uslam_frontend_create": (C.c_int, [_vp, C.c_int, C.c_int, C.POINTER(_vp)]),
     "uslam_frontend_destroy": (None, [_vp]),
     "uslam_frontend_process": (C.c_int, [_vp, _vp, C.c_int, C.c_int]),
+    "uslam_frontend_process_f32": (C.c_int, [_vp, _vp, C.c_int, C.c_int]),
     "uslam_frontend_input_device": (C.c_int, [_vp, _u8pp, _ip]),
     "uslam_frontend_features": (C.c_int, [_vp, C.c_int, _vp, C.c_int, _ip, _ip]),
     "uslam_frontend_matches": (C.c_int, [_vp, _vp, C.c_int, _ip]),

@@ -1088,23 +1088,58 @@ uslam_status uslam_batch_io_bytes(uslam_batch* b, size_t* h2d, size_t* d2h) {
 struct uslam_frontend {
     uslam_batch* b = nullptr;
     uint8_t* incoming = nullptr;  // device buffer for caller-written frames
+    uint8_t* h_stage = nullptr;   // pinned u8 staging of the next host frame (H0 rows of img_pitch)
     int cur = -1;                 // slot holding FeatureSet(0)
     int ref = -1;                 // slot holding FeatureSet(1)
     bool matched = false;
+    // the batch's pinned output staging holds this slot's feature set / this
+    // pair's matches as of their last computation (downloaded with the frame)
+    bool host_frame[2] = {false, false};
+    bool host_pair[2] = {false, false};
 };
 
 namespace {
 
+// Byte range of a frame's outputs (counts + feature blocks) and of a pair's
+// outputs (counts + match blocks) in the batch's outputs region.
+std::pair<size_t, size_t> frame_out_range(const uslam_batch* b, int f) {
+    const FrameDev& F = b->frames[f];
+    const char* out0 = b->arena + b->in_bytes;
+    const size_t end = static_cast<size_t>(reinterpret_cast<const char*>(F.feats[F.levels - 1]) - out0) +
+                       static_cast<size_t>(std::max(F.cap, 1)) * 48;
+    return {b->feat_off[f], end - b->feat_off[f]};
+}
+std::pair<size_t, size_t> pair_out_range(const uslam_batch* b, int p) {
+    const PairDev& P = b->pairs[p];
+    const char* out0 = b->arena + b->in_bytes;
+    const size_t end = static_cast<size_t>(reinterpret_cast<const char*>(P.matches) - out0) +
+                       static_cast<size_t>(b->levels) * std::max(P.max_matches_per_level, 1) * 16;
+    return {b->pair_off[p], end - b->pair_off[p]};
+}
+
+// The reference's f32 pixel rule (data/src/provider_base.cpp:121-124 stores
+// u8 / 255): the byte back, exact for those values, nearest 1/255 otherwise.
+inline uint8_t f32_to_u8(float v) {
+    const long r = std::lrintf(v * 255.0f);
+    return static_cast<uint8_t>(r < 0 ? 0 : (r > 255 ? 255 : r));
+}
+
 // Choose the slot of the next frame and enqueue its copy and work.
-// src_host != NULL: H2D from caller memory; else src_dev != NULL: D2D from
-// caller device memory; else D2D from `incoming`.
-uslam_status frontend_enqueue(uslam_frontend* fe, const uint8_t* src_host, const uint8_t* src_dev, int pitch,
-                              int advance_reference, int* matched) {
+// src_host (u8) or src_f32 (f32 in [0, 1]) != NULL: the frame goes through
+// the pinned staging (an asynchronous H2D copy); else src_dev != NULL: D2D
+// from caller device memory; else D2D from `incoming`.  download: the new
+// feature set and matches are copied back into the pinned output staging
+// behind the work, for the feature / match getters.
+uslam_status frontend_enqueue(uslam_frontend* fe, const uint8_t* src_host, const float* src_f32,
+                              const uint8_t* src_dev, int pitch, int advance_reference, bool download,
+                              int* matched) {
     uslam_batch* b = fe->b;
     const FrameDev& F0 = b->frames[0];
     // LoadDataCPUPass::shiftFeatureSets (load_features_cpu.cpp:111-142): the
     // current set becomes the reference when asked or when none exists yet;
     // otherwise the reference is kept and the current set is replaced.
+    if ((src_host || src_f32 || src_dev) && pitch < F0.W0)
+        return set_err(b->err(), USLAM_INVALID_ARG, "process: pitch smaller than the frame width");
     int slot;
     if (fe->cur < 0) {
         slot = 0;
@@ -1113,28 +1148,73 @@ uslam_status frontend_enqueue(uslam_frontend* fe, const uint8_t* src_host, const
         slot = 1 - fe->ref;
     }
     uint8_t* dst = const_cast<uint8_t*>(b->frames[slot].img);
+    const size_t frame_bytes = static_cast<size_t>(F0.H0) * F0.img_pitch;
     cudaError_t e;
-    if (src_host) {
-        if (pitch < F0.W0) return set_err(b->err(), USLAM_INVALID_ARG, "process: pitch smaller than the frame width");
-        e = cudaMemcpy2DAsync(dst, F0.img_pitch, src_host, pitch, F0.W0, F0.H0, cudaMemcpyHostToDevice, b->stream);
+    if (src_host || src_f32) {
+        // the previous frame's upload from the staging has completed: every
+        // host-frame call returns after its work (and its copies) finished
+        for (int y = 0; y < F0.H0; ++y) {
+            uint8_t* row = fe->h_stage + static_cast<size_t>(y) * F0.img_pitch;
+            if (src_host) {
+                std::memcpy(row, src_host + static_cast<size_t>(y) * pitch, F0.W0);
+            } else {
+                const float* in = src_f32 + static_cast<size_t>(y) * pitch;
+                for (int x = 0; x < F0.W0; ++x) row[x] = f32_to_u8(in[x]);
+            }
+        }
+        e = cudaMemcpyAsync(dst, fe->h_stage, frame_bytes, cudaMemcpyHostToDevice, b->stream);
     } else if (src_dev) {
-        if (pitch < F0.W0) return set_err(b->err(), USLAM_INVALID_ARG, "enqueue: pitch smaller than the frame width");
         e = cudaMemcpy2DAsync(dst, F0.img_pitch, src_dev, pitch, F0.W0, F0.H0, cudaMemcpyDeviceToDevice, b->stream);
     } else {
-        e = cudaMemcpyAsync(dst, fe->incoming, static_cast<size_t>(F0.H0) * F0.img_pitch, cudaMemcpyDeviceToDevice,
-                            b->stream);
+        e = cudaMemcpyAsync(dst, fe->incoming, frame_bytes, cudaMemcpyDeviceToDevice, b->stream);
     }
     if (e == cudaSuccess) e = cudaMemsetAsync(b->d_err, 0, sizeof(uint32_t), b->stream);
     if (e == cudaSuccess) e = enqueue_program(b, b->frame_prog[slot]);
     fe->cur = slot;
     fe->matched = false;
+    fe->host_frame[slot] = false;
+    const int pair = slot == 0 ? 0 : 1;  // pair 0 = slot1 -> slot0, pair 1 = slot0 -> slot1
     if (e == cudaSuccess && fe->ref >= 0) {
-        const int pair = slot == 0 ? 0 : 1;  // pair 0 = slot1 -> slot0, pair 1 = slot0 -> slot1
+        fe->host_pair[pair] = false;
         e = enqueue_program(b, b->pair_prog[pair]);
         fe->matched = true;
     }
+    if (e == cudaSuccess && download) {
+        const auto fr = frame_out_range(b, slot);
+        e = cudaMemcpyAsync(b->h_out + fr.first, b->arena + b->in_bytes + fr.first, fr.second,
+                            cudaMemcpyDeviceToHost, b->stream);
+        if (e == cudaSuccess && fe->matched) {
+            const auto pr = pair_out_range(b, pair);
+            e = cudaMemcpyAsync(b->h_out + pr.first, b->arena + b->in_bytes + pr.first, pr.second,
+                                cudaMemcpyDeviceToHost, b->stream);
+        }
+    }
     if (e != cudaSuccess) return b->ctx->cuda_fail(e, "frontend launch");
     if (matched) *matched = fe->matched ? 1 : 0;
+    return USLAM_OK;
+}
+
+// A synchronous host-frame call: enqueue with the download, wait, and mark
+// the downloaded outputs current.
+uslam_status frontend_process_host(uslam_frontend* fe, const uint8_t* img, const float* img_f32, int pitch,
+                                   int advance_reference) {
+    int matched = 0;
+    uslam_status s = frontend_enqueue(fe, img, img_f32, nullptr, pitch, advance_reference, true, &matched);
+    if (s != USLAM_OK) return s;
+    s = sync_stream(fe->b, 0);
+    if (s != USLAM_OK) return s;
+    fe->host_frame[fe->cur] = true;
+    if (matched) fe->host_pair[fe->cur == 0 ? 0 : 1] = true;
+    return matched ? USLAM_OK : USLAM_NOT_READY;
+}
+
+// Bring the whole outputs region to the pinned staging (after asynchronous
+// enqueues, whose outputs were not downloaded).
+uslam_status frontend_refresh(uslam_frontend* fe) {
+    uslam_batch* b = fe->b;
+    cudaError_t e = cudaMemcpy(b->h_out, b->arena + b->in_bytes, b->out_bytes, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return b->ctx->cuda_fail(e, "outputs readback");
+    fe->host_frame[0] = fe->host_frame[1] = fe->host_pair[0] = fe->host_pair[1] = true;
     return USLAM_OK;
 }
 
@@ -1151,13 +1231,17 @@ uslam_status uslam_frontend_create(uslam_ctx* ctx, int width, int height, uslam_
     if (s != USLAM_OK) return s;
     auto* fe = new uslam_frontend();
     fe->b = b;
-    cudaError_t e = cudaMalloc(&fe->incoming, static_cast<size_t>(b->frames[0].H0) * b->frames[0].img_pitch);
+    const size_t frame_bytes = static_cast<size_t>(b->frames[0].H0) * b->frames[0].img_pitch;
+    cudaError_t e = cudaMalloc(&fe->incoming, frame_bytes);
+    if (e == cudaSuccess) e = cudaHostAlloc(&fe->h_stage, frame_bytes, cudaHostAllocDefault);
     if (e != cudaSuccess) {
         cudaGetLastError();
+        if (fe->incoming) cudaFree(fe->incoming);
         uslam_batch_destroy(b);
         delete fe;
         return set_err(&ctx->err, USLAM_OOM, "frontend input buffer allocation refused");
     }
+    std::memset(fe->h_stage, 0, frame_bytes);
     *out = fe;
     return USLAM_OK;
 }
@@ -1166,6 +1250,7 @@ void uslam_frontend_destroy(uslam_frontend* fe) {
     if (!fe) return;
     cudaSetDevice(fe->b->ctx->device);
     if (fe->incoming) cudaFree(fe->incoming);
+    if (fe->h_stage) cudaFreeHost(fe->h_stage);
     uslam_batch_destroy(fe->b);
     delete fe;
 }
@@ -1180,7 +1265,7 @@ uslam_status uslam_frontend_input_device(uslam_frontend* fe, uint8_t** dev_ptr, 
 uslam_status uslam_frontend_enqueue(uslam_frontend* fe, const uint8_t* dev_img, int pitch, int advance_reference,
                                     int* matched) {
     if (!fe) return USLAM_INVALID_ARG;
-    return frontend_enqueue(fe, nullptr, dev_img, pitch, advance_reference, matched);
+    return frontend_enqueue(fe, nullptr, nullptr, dev_img, pitch, advance_reference, false, matched);
 }
 
 uslam_status uslam_frontend_sync(uslam_frontend* fe) {
@@ -1190,12 +1275,23 @@ uslam_status uslam_frontend_sync(uslam_frontend* fe) {
 
 uslam_status uslam_frontend_process(uslam_frontend* fe, const uint8_t* img, int pitch, int advance_reference) {
     if (!fe) return USLAM_INVALID_ARG;
-    int matched = 0;
-    uslam_status s = frontend_enqueue(fe, img, nullptr, pitch, advance_reference, &matched);
-    if (s != USLAM_OK) return s;
-    s = sync_stream(fe->b, 0);
-    if (s != USLAM_OK) return s;
-    return matched ? USLAM_OK : USLAM_NOT_READY;
+    if (!img) {
+        // the frame is already in the frontend's device input buffer
+        int matched = 0;
+        uslam_status s = frontend_enqueue(fe, nullptr, nullptr, nullptr, pitch, advance_reference, true, &matched);
+        if (s != USLAM_OK) return s;
+        s = sync_stream(fe->b, 0);
+        if (s != USLAM_OK) return s;
+        fe->host_frame[fe->cur] = true;
+        if (matched) fe->host_pair[fe->cur == 0 ? 0 : 1] = true;
+        return matched ? USLAM_OK : USLAM_NOT_READY;
+    }
+    return frontend_process_host(fe, img, nullptr, pitch, advance_reference);
+}
+
+uslam_status uslam_frontend_process_f32(uslam_frontend* fe, const float* img, int pitch, int advance_reference) {
+    if (!fe || !img) return USLAM_INVALID_ARG;
+    return frontend_process_host(fe, nullptr, img, pitch, advance_reference);
 }
 
 uslam_status uslam_frontend_features(uslam_frontend* fe, int which, uslam_feature* out, int max_out, int* kept,
@@ -1203,20 +1299,22 @@ uslam_status uslam_frontend_features(uslam_frontend* fe, int which, uslam_featur
     if (!fe || (which != 0 && which != 1)) return USLAM_INVALID_ARG;
     const int slot = which == 0 ? fe->cur : fe->ref;
     if (slot < 0) return set_err(fe->b->err(), USLAM_NOT_READY, "features: that feature set does not exist yet");
-    uslam_batch* b = fe->b;
-    cudaError_t e = cudaMemcpy(b->h_out, b->arena + b->in_bytes, b->out_bytes, cudaMemcpyDeviceToHost);
-    if (e != cudaSuccess) return b->ctx->cuda_fail(e, "features readback");
-    return copy_features(b, b->h_out, slot, out, max_out, kept, raw);
+    if (!fe->host_frame[slot]) {
+        const uslam_status s = frontend_refresh(fe);
+        if (s != USLAM_OK) return s;
+    }
+    return copy_features(fe->b, fe->b->h_out, slot, out, max_out, kept, raw);
 }
 
 uslam_status uslam_frontend_matches(uslam_frontend* fe, uslam_match* out, int max_out, int* n_out) {
     if (!fe) return USLAM_INVALID_ARG;
     if (!fe->matched) return set_err(fe->b->err(), USLAM_NOT_READY, "matches: no reference feature set yet");
-    uslam_batch* b = fe->b;
-    cudaError_t e = cudaMemcpy(b->h_out, b->arena + b->in_bytes, b->out_bytes, cudaMemcpyDeviceToHost);
-    if (e != cudaSuccess) return b->ctx->cuda_fail(e, "matches readback");
     const int pair = fe->cur == 0 ? 0 : 1;
-    return copy_matches(b, b->h_out, pair, out, max_out, n_out);
+    if (!fe->host_pair[pair]) {
+        const uslam_status s = frontend_refresh(fe);
+        if (s != USLAM_OK) return s;
+    }
+    return copy_matches(fe->b, fe->b->h_out, pair, out, max_out, n_out);
 }
 
 }  // extern "C"

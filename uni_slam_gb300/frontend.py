@@ -312,6 +312,14 @@ class Frontend:
         self.ctx.check(st, "frontend_process", ok=(capi.OK, capi.NOT_READY))
         return st == capi.OK
 
+    def process_f32(self, img: np.ndarray, advance_reference: bool = False, pitch: int | None = None) -> bool:
+        """The reference's f32 FrameBW pixels (u8 / 255) of shape (H, pitch >= W);
+        returns True when the frame was matched against a reference set."""
+        img = np.ascontiguousarray(img, dtype=np.float32)
+        st = self.lib.uslam_frontend_process_f32(self.h, ptr(img), pitch or img.shape[1], int(advance_reference))
+        self.ctx.check(st, "frontend_process_f32", ok=(capi.OK, capi.NOT_READY))
+        return st == capi.OK
+
     def input_device(self) -> tuple[int, int]:
         p = C.POINTER(C.c_uint8)()
         pitch = C.c_int()
