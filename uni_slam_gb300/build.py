@@ -24,7 +24,8 @@ NVCC_FLAGS = ARCH + [
     "-Xcompiler", "-fPIC,-ffp-contract=off",
     "-I", os.path.join(REPO, "include"),
 ]
-SOURCES = ["kernels.cu", "runtime.cu", "server.cu", "noalloc.cu", "ransac.cu", "triangulate.cu", "bf_tc.cu"]
+SOURCES = ["kernels.cu", "runtime.cu", "server.cu", "noalloc.cu", "ransac.cu", "triangulate.cu", "bf_tc.cu",
+           "win_tc.cu"]
 
 
 def _nvcc() -> str:

@@ -57,6 +57,8 @@ struct Program {
     MatchSegDev* msegs = nullptr;
     SegDev* usegs = nullptr;
     SegDev* psegs = nullptr;  // one (pair, 0) entry per pair (brute-force matcher)
+    void* units = nullptr;    // the windowed tensor-core matcher's unit slots (device scratch)
+    size_t units_bytes = 0;
     std::vector<char> host;  // host image of the tables
     cudaGraphExec_t graph = nullptr;
 };
@@ -92,6 +94,10 @@ struct uslam_batch {
     cudaEvent_t lane_fork[kLanes] = {}, lane_join[kLanes] = {}, lane_desc[kLanes] = {}, lane_end[kLanes] = {};
     cudaEvent_t ev_start = nullptr;
     Program full;
+    // the windowed matcher on the tensor cores (k_win_pack / k_win_plan /
+    // k_win_mma; else k_match): matcher 0 with list positions within 16 bits
+    bool win_tc = false;
+    int win_umax = 0;  // unit slots per (pair, direction, level)
     std::vector<Program> frame_prog;  // per frame: detect+describe only
     std::vector<Program> pair_prog;   // per pair: match only
     ErrText* err() { return &ctx->err; }
@@ -151,6 +157,9 @@ uslam_status build_program(uslam_batch* b, const std::vector<int>& fr, const std
     std::memcpy(P->host.data() + t_bytes + f_bytes + m_bytes + u_bytes, psegs.data(), psegs.size() * sizeof(SegDev));
     std::memcpy(P->host.data() + t_bytes + f_bytes + m_bytes + u_bytes + p_bytes, bands.data(),
                 bands.size() * sizeof(BandItem));
+    // unit slots of the windowed tensor-core matcher: written on the device
+    P->units_bytes = b->win_tc ? round_up(msegs.size() * static_cast<size_t>(b->win_umax) * win_unit_bytes(), 256) : 0;
+    P->host.resize(P->host.size() + P->units_bytes, 0);
     return USLAM_OK;
 }
 
@@ -184,7 +193,9 @@ cudaError_t enqueue_frames(uslam_batch* b, const Program& P, const Lane& ln) {
         cudaSuccess)
         return e;
     if ((e = cudaStreamWaitEvent(ln.st, ln.join, 0)) != cudaSuccess) return e;
-    return launch_describe(b->d_frames, P.fsegs, P.nfsegs, c->d_pattern, grid, c->matcher == 2, ln.st);
+    if ((e = launch_describe(b->d_frames, P.fsegs, P.nfsegs, c->d_pattern, grid, c->matcher == 2, ln.st)) != cudaSuccess)
+        return e;
+    return b->win_tc ? launch_win_pack(b->d_frames, P.fsegs, P.nfsegs, c->num_sms, ln.st) : cudaSuccess;
 }
 
 // The pair stages of a program: match and the mutual check / emit.
@@ -200,6 +211,12 @@ cudaError_t enqueue_pairs(uslam_batch* b, const Program& P, const Lane& ln) {
             e = launch_bf_mma(b->d_frames, b->d_pairs, P.psegs, P.npsegs, c->ratio, c->num_sms, b->d_err, ln.st);
         if (e != cudaSuccess) return e;
         return launch_emit(b->d_frames, b->d_pairs, P.usegs, P.nusegs, b->d_err, ln.st);
+    }
+    if (b->win_tc) {
+        if ((e = launch_win_match(b->d_frames, b->d_pairs, P.msegs, P.nmsegs, b->win_umax, P.units, c->num_sms,
+                                  b->d_err, ln.st)) != cudaSuccess)
+            return e;
+        return launch_mutual(b->d_frames, b->d_pairs, P.usegs, P.nusegs, b->d_err, ln.st);
     }
     if ((e = launch_match_dyn(b->d_frames, b->d_pairs, P.msegs, P.nmsegs, c->num_sms * kMatchCtasPerSm,
                               ln.next_group, ln.st)) != cudaSuccess)
@@ -307,8 +324,17 @@ uslam_status create_batch(uslam_ctx* ctx, int n_frames, const int* widths, const
     struct FrameLayout {
         size_t lvl[USLAM_MAX_LEVELS], blur[USLAM_MAX_LEVELS], kpmap[USLAM_MAX_LEVELS], feats[USLAM_MAX_LEVELS],
             xorder[USLAM_MAX_LEVELS], colstart[USLAM_MAX_LEVELS], qorder[USLAM_MAX_LEVELS], bands[USLAM_MAX_LEVELS], counts,
-            tmaps, bf8, bfext, bfpop, bfid;
+            tmaps, bf8, bfext, bfpop, bfid, wq8, wc8, wcext, wcy, wcid;
     };
+    // the windowed tensor-core matcher: matcher 0, every list position and
+    // candidate row within 16 bits
+    int max_cap = 1;
+    for (int f = 0; f < n_frames; ++f) {
+        const long long c = ctx->cap_override > 0 ? ctx->cap_override : static_cast<long long>(widths[f]) * heights[f] / 250;
+        max_cap = static_cast<int>(std::max<long long>(max_cap, c));
+    }
+    b->win_tc = ctx->matcher == 0 && max_cap <= kWinMaxCap && ctx->max_h < 65535;
+    b->win_umax = b->win_tc ? win_units_per_seg(max_cap) : 0;
     std::vector<FrameLayout> fl(n_frames);
     for (int f = 0; f < n_frames; ++f) {
         const int W0 = widths[f], H0 = heights[f];
@@ -365,6 +391,19 @@ uslam_status create_batch(uslam_ctx* ctx, int n_frames, const int* widths, const
             Ly.bfext = take(&scratch, rows * 32);
             Ly.bfpop = take(&scratch, rows * 4);
             Ly.bfid = take(&scratch, rows * 4);
+        }
+        if (b->win_tc) {
+            // queries: each band from a multiple of 128 rows; lists: room for a
+            // last 128-row tile that starts below the list's end
+            F.wq_rows = static_cast<int>(round_up(capa, 128) + USLAM_MATCH_BANDS * 128);
+            F.wc_rows = static_cast<int>(round_up(capa, 32) + 128);
+            const size_t qrows = static_cast<size_t>(L) * F.wq_rows;
+            const size_t crows = static_cast<size_t>(L) * USLAM_MATCH_BANDS * F.wc_rows;
+            Ly.wq8 = take(&scratch, qrows * 256);
+            Ly.wc8 = take(&scratch, crows * 256);
+            Ly.wcext = take(&scratch, crows * 32);
+            Ly.wcy = take(&scratch, crows * 2);
+            Ly.wcid = take(&scratch, crows * 4);
         }
         b->max_w = std::max(b->max_w, F.w[0]);
     }
@@ -505,6 +544,13 @@ uslam_status create_batch(uslam_ctx* ctx, int n_frames, const int* widths, const
             F.bfpop = reinterpret_cast<uint32_t*>(sc_base + Ly.bfpop);
             F.bfid = reinterpret_cast<int32_t*>(sc_base + Ly.bfid);
         }
+        if (b->win_tc) {
+            F.wq8 = reinterpret_cast<uint8_t*>(sc_base + Ly.wq8);
+            F.wc8 = reinterpret_cast<uint8_t*>(sc_base + Ly.wc8);
+            F.wcext = reinterpret_cast<uint8_t*>(sc_base + Ly.wcext);
+            F.wcy = reinterpret_cast<uint16_t*>(sc_base + Ly.wcy);
+            F.wcid = reinterpret_cast<int32_t*>(sc_base + Ly.wcid);
+        }
         std::vector<char> maps(static_cast<size_t>(L) * kNumTileShapes * USLAM_TMAP_BYTES);
         s = encode_tile_maps(F, ctx->detector, maps.data(), &ctx->err);
         if (s == USLAM_OK) {
@@ -536,6 +582,7 @@ uslam_status create_batch(uslam_ctx* ctx, int n_frames, const int* widths, const
     }
     e = set_compact_smem(b->max_w);
     if (e == cudaSuccess && ctx->matcher == 2) e = set_bf_mma_smem();
+    if (e == cudaSuccess && b->win_tc) e = set_win_mma_smem();
     if (e != cudaSuccess) {
         free_batch(b);
         return ctx->cuda_fail(e, "shared memory attribute");
@@ -618,6 +665,7 @@ uslam_status create_batch(uslam_ctx* ctx, int n_frames, const int* widths, const
         P->psegs = reinterpret_cast<SegDev*>(base + t_bytes + f_bytes + m_bytes + u_bytes);
         const size_t p_bytes = round_up(P->npsegs * sizeof(SegDev), 256);
         P->bands = reinterpret_cast<BandItem*>(base + t_bytes + f_bytes + m_bytes + u_bytes + p_bytes);
+        P->units = P->units_bytes ? base + (P->host.size() - P->units_bytes) : nullptr;
         P->tiles = reinterpret_cast<TileItem*>(base);
         P->fsegs = reinterpret_cast<SegDev*>(base + t_bytes);
         P->msegs = reinterpret_cast<MatchSegDev*>(base + t_bytes + f_bytes);
@@ -958,11 +1006,14 @@ uslam_status uslam_batch_profile(uslam_batch* b, int iters, float* kernel_ms) {
             e = launch_compact_banded(b->d_frames, P.bands, P.nbands, P.fsegs, P.nfsegs, b->max_w, b->stream);
         mark();
         if (e == cudaSuccess) e = launch_describe(b->d_frames, P.fsegs, P.nfsegs, c->d_pattern, grid, c->matcher == 2, b->stream);
+        if (e == cudaSuccess && b->win_tc) e = launch_win_pack(b->d_frames, P.fsegs, P.nfsegs, c->num_sms, b->stream);
         mark();
         if (e == cudaSuccess)
             e = c->matcher == 1 ? launch_bruteforce(b->d_frames, b->d_pairs, P.psegs, P.npsegs, c->ratio, grid, b->stream)
                 : c->matcher == 2
                     ? launch_bf_mma(b->d_frames, b->d_pairs, P.psegs, P.npsegs, c->ratio, c->num_sms, b->d_err, b->stream)
+                : b->win_tc ? launch_win_match(b->d_frames, b->d_pairs, P.msegs, P.nmsegs, b->win_umax, P.units,
+                                               c->num_sms, b->d_err, b->stream)
                     : launch_match_dyn(b->d_frames, b->d_pairs, P.msegs, P.nmsegs, c->num_sms * kMatchCtasPerSm,
                                        b->d_err + 1, b->stream);
         mark();
@@ -1353,6 +1404,17 @@ cudaError_t copy_frame_state(const uslam_batch* src, uslam_batch* dst, int slot,
         if (e == cudaSuccess) e = cudaMemcpyAsync(B.bfext, A.bfext, rows * 32, cudaMemcpyDeviceToDevice, st);
         if (e == cudaSuccess) e = cudaMemcpyAsync(B.bfpop, A.bfpop, rows * 4, cudaMemcpyDeviceToDevice, st);
         if (e == cudaSuccess) e = cudaMemcpyAsync(B.bfid, A.bfid, rows * 4, cudaMemcpyDeviceToDevice, st);
+    }
+    if (A.wq8 && B.wq8 && e == cudaSuccess) {
+        // the windowed tensor-core matcher's operand rows (same frame size,
+        // so the same row strides)
+        const size_t qrows = static_cast<size_t>(A.levels) * A.wq_rows;
+        const size_t crows = static_cast<size_t>(A.levels) * USLAM_MATCH_BANDS * A.wc_rows;
+        e = cudaMemcpyAsync(B.wq8, A.wq8, qrows * 256, cudaMemcpyDeviceToDevice, st);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(B.wc8, A.wc8, crows * 256, cudaMemcpyDeviceToDevice, st);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(B.wcext, A.wcext, crows * 32, cudaMemcpyDeviceToDevice, st);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(B.wcy, A.wcy, crows * 2, cudaMemcpyDeviceToDevice, st);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(B.wcid, A.wcid, crows * 4, cudaMemcpyDeviceToDevice, st);
     }
     return e;
 }

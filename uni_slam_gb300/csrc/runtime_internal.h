@@ -39,6 +39,14 @@ cudaError_t launch_bruteforce(const FrameDev*, const PairDev*, const SegDev*, in
 cudaError_t launch_bf_mma(const FrameDev*, const PairDev*, const SegDev*, int, float, int, uint32_t*, cudaStream_t);
 cudaError_t set_compact_smem(int max_w);
 cudaError_t set_bf_mma_smem();
+// the windowed matcher on the tensor cores (win_tc.cu)
+cudaError_t set_win_mma_smem();
+int win_units_per_seg(int cap);
+size_t win_unit_bytes();
+cudaError_t launch_win_pack(const FrameDev*, const SegDev*, int, int, cudaStream_t);
+cudaError_t launch_win_match(const FrameDev*, const PairDev*, const void*, int, int, void*, int, uint32_t*,
+                             cudaStream_t);
+constexpr int kWinMaxCap = 60000;  // list positions and tile columns stay within 16 bits
 // Tile shapes (width, height) that k_detect is instantiated for; the index
 // is the `shape` argument of launch_detect.  Every shape computes the same
 // values (the arithmetic is per pixel), so the choice affects speed only.

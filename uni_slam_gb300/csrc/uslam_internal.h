@@ -77,6 +77,20 @@ struct FrameDev {
     uint8_t* bfext;
     uint32_t* bfpop;
     int32_t* bfid;
+    // windowed matcher on the tensor cores (the batch path of matcher 0; null
+    // otherwise): the frame's descriptors as operand rows in the bf8 layout.
+    // wq8: the query order of each level (level l from row l * wq_rows), each
+    // band's queries starting at a multiple of 128 rows; wc8 / wcext: the
+    // candidate lists (list b of level l from row (USLAM_MATCH_BANDS l + b) *
+    // wc_rows), with the extension rows of the bfext layout (row index within
+    // its 32-row group = list position % 32); wcy: the candidate's y in its
+    // level; wcid: packed (level, index).
+    uint8_t* wq8;
+    uint8_t* wc8;
+    uint8_t* wcext;
+    uint16_t* wcy;
+    int32_t* wcid;
+    int wq_rows, wc_rows;
 };
 
 // One frame pair to match: prev = reference set (a), curr = current set (b).
