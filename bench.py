@@ -635,9 +635,10 @@ def serve_saturation(ctx, sizes, frames, seconds: float, inflight: int = 4, prom
 
 def plugin_run(pat, frames, warmup: int = 8, timed: int = 256, advance_every: int = 1) -> dict:
     """The drop-in passes as the reference's pipeline runs them: per frame a
-    FrameBW of f32 pixels in AnyBag, CudaFeatureDetectPass (pinned staging of
-    the u8 bytes, asynchronous upload, the frame's work, its feature set and
-    matches copied back) and CudaMatchPass, with FeatureSet and MatchResult
+    FrameBW of f32 pixels in AnyBag, CudaFeatureDetectPass (pinned f32 staging,
+    asynchronous upload, the bytes recovered on the device, the frame's work,
+    its feature set and matches copied back) and CudaMatchPass, with
+    FeatureSet and MatchResult
     built in AnyBag (include/uslam_wslam.hpp, compiled against stand-ins of
     the reference's headers in tests/adapter/stubs).  Wall clock per frame
     around the two passes."""
@@ -669,11 +670,12 @@ def plugin_run(pat, frames, warmup: int = 8, timed: int = 256, advance_every: in
             return {"error": f"adapter_bench rc={r.returncode}: {r.stderr[-300:]}"}
         out = json.loads(r.stdout.strip().splitlines()[-1])
     cap = W * H // 250
-    # per frame: the u8 frame up; the frame's counts + feature blocks and the
-    # pair's counts + match blocks down (uslam_frontend_process)
+    # per frame: the f32 frame up (as the reference uploads it); the frame's
+    # counts + feature blocks and the pair's counts + match blocks down
     d2h = 8 * LEVELS + LEVELS * cap * 48 + ((4 * LEVELS + 15) // 16 * 16) + LEVELS * cap * 16
-    return {"value": out["frames_per_s"], "unit": "frames/s", "h2d_bytes_per_step": W * H,
+    return {"value": out["frames_per_s"], "unit": "frames/s", "h2d_bytes_per_step": 4 * W * H,
             "d2h_bytes_per_step": d2h, "step": "one frame", "frames": out["frames"],
+            "detect_pass_ms": out["detect_pass_ms"], "match_pass_ms": out["match_pass_ms"],
             "features_per_frame": out["features"] / out["frames"], "matches_per_frame": out["matches"] / out["frames"],
             "method": "CudaFeatureDetectPass + CudaMatchPass on FrameBW f32 host frames, one frame per call "
                       "(keyframe advanced every frame), outputs as FeatureSet / MatchResult in AnyBag"}

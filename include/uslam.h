@@ -293,6 +293,15 @@ uslam_status uslam_batch_set_stream(uslam_batch* b, void* cuda_stream);
  * describe (k_describe), match (k_match, k_bruteforce with matcher 1, k_bf_mma with matcher 2) and
  * mutual check / emit (k_mutual).  Synchronous. */
 uslam_status uslam_batch_profile(uslam_batch* b, int iters, float* kernel_ms);
+/* Test hook for the kernels' bounded waits (no reference counterpart): the
+ * number of polls of the first mbarrier wait of k_detect's tile load
+ * (detect_polls) and of the tensor-core brute-force matcher's first
+ * query-tile load (match_polls, matcher 2); -1 restores a kernel's own limit.
+ * A wait that runs out records USLAM_ERR_TMA_TIMEOUT in the batch's error word
+ * (uslam_batch_sync then returns USLAM_KERNEL_CHECK) after the copy in flight
+ * has landed (that drain keeps the full limit); the batch stays usable.  Takes
+ * effect from the next run. */
+uslam_status uslam_batch_set_first_wait(uslam_batch* b, int detect_polls, int match_polls);
 /* Bytes moved by upload and download per call (for end-to-end accounting). */
 uslam_status uslam_batch_io_bytes(uslam_batch* b, size_t* h2d, size_t* d2h);
 
@@ -317,10 +326,12 @@ void uslam_frontend_destroy(uslam_frontend* fe);
  * when the frame's work and copies are complete. */
 uslam_status uslam_frontend_process(uslam_frontend* fe, const uint8_t* img, int pitch, int advance_reference);
 /* The same for the reference's f32 FrameBW pixels in [0, 1] (pitch in
- * floats): each pixel becomes lrintf(p * 255) clamped to [0, 255] while it is
- * written into the pinned staging -- exact for the u8 / 255 values
- * data::getLocalFrame stores (data/src/provider_base.cpp:121-124) -- and the
- * u8 frame is uploaded, a quarter of the f32 bytes. */
+ * floats), uploaded as f32 the way FillPyramidPass::writeBaseLayer uploads
+ * them: the rows are copied into a pinned f32 staging buffer, one
+ * asynchronous copy takes them to the device, and a kernel recovers each byte
+ * as p * 255 clamped to [0, 255] (NaN to 0), rounded half to even -- exact
+ * for the u8 / 255 values data::getLocalFrame stores
+ * (data/src/provider_base.cpp:121-124). */
 uslam_status uslam_frontend_process_f32(uslam_frontend* fe, const float* img, int pitch, int advance_reference);
 uslam_status uslam_frontend_input_device(uslam_frontend* fe, uint8_t** dev_ptr, int* pitch);
 /* which = 0: current set, 1: reference set.  After uslam_frontend_process

@@ -138,6 +138,7 @@ class CudaFeatureDetectPass : public compute::Pass {
         FeatureSet set;
         size_t n = 0;
         for (int l = 0; l < L; ++l) {
+            set.at(l).reserve(static_cast<size_t>(kept[l]));
             for (int i = 0; i < kept[l]; ++i, ++n) {
                 const uslam_feature& g = buf[n];
                 Feature c{};

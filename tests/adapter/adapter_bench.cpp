@@ -38,7 +38,7 @@ int main(int argc, char** argv) {
     wslam::CudaMatchPass match(gpu, storage);
     if (detect.initialize() || match.initialize()) return 3;
     long long feats = 0, matches = 0;
-    double seconds = 0.0;
+    double seconds = 0.0, detect_s = 0.0;
     for (int i = 0; i < warmup + timed; ++i) {
         // the frame's pixels are copied into the FrameBW outside the time, as
         // the sensor loader pass would have stored them before this stage
@@ -52,6 +52,7 @@ int main(int argc, char** argv) {
             std::cerr << "detect: " << *e << "\n";
             return 4;
         }
+        const auto td = std::chrono::steady_clock::now();
         const auto me = match.execute();
         const auto t1 = std::chrono::steady_clock::now();
         const bool stop = me && *me == wslam::compute::kStageStopExecution;
@@ -61,6 +62,7 @@ int main(int argc, char** argv) {
         }
         if (i >= warmup) {
             seconds += std::chrono::duration<double>(t1 - t0).count();
+            detect_s += std::chrono::duration<double>(td - t0).count();
             const auto& cur = **storage.getPtr<wslam::FeatureSet>(wslam::ResourceIdentifier::GetFeatureSetName(0));
             for (const auto& lv : cur) feats += static_cast<long long>(lv.size());
             if (!stop) {
@@ -69,7 +71,9 @@ int main(int argc, char** argv) {
             }
         }
     }
-    std::printf("{\"frames\": %d, \"seconds\": %.6f, \"frames_per_s\": %.3f, \"features\": %lld, \"matches\": %lld}\n",
-                timed, seconds, timed / seconds, feats, matches);
+    std::printf(
+        "{\"frames\": %d, \"seconds\": %.6f, \"frames_per_s\": %.3f, \"detect_pass_ms\": %.4f, "
+        "\"match_pass_ms\": %.4f, \"features\": %lld, \"matches\": %lld}\n",
+        timed, seconds, timed / seconds, 1e3 * detect_s / timed, 1e3 * (seconds - detect_s) / timed, feats, matches);
     return 0;
 }

@@ -92,6 +92,7 @@ SIGNATURES = {
     "uslam_batch_set_stream": (C.c_int, [_vp, _vp]),
     "uslam_batch_profile": (C.c_int, [_vp, C.c_int, _vp]),
     "uslam_blur_margin": (C.c_int, [_vp, _ip]),
+    "uslam_batch_set_first_wait": (C.c_int, [_vp, C.c_int, C.c_int]),
     "uslam_batch_io_bytes": (C.c_int, [_vp, _szp, _szp]),
     "uslam_tile_shapes": (C.c_int, [_ip, _ip, _ip]),
     "uslam_set_tile_shape": (C.c_int, [_vp, C.c_int, C.c_int, C.c_int]),

@@ -79,9 +79,9 @@ __device__ __forceinline__ void bar_arrive(uint64_t* b) {
 __device__ __forceinline__ void bar_expect(uint64_t* b, uint32_t bytes) {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(saddr(b)), "r"(bytes) : "memory");
 }
-__device__ __forceinline__ bool bar_wait(uint64_t* b, uint32_t parity) {
+__device__ __forceinline__ bool bar_wait(uint64_t* b, uint32_t parity, uint32_t limit = kWaitLimit) {
     const uint32_t a = saddr(b);
-    for (uint32_t i = 0; i < kWaitLimit; ++i) {
+    for (uint32_t i = 0; i < limit; ++i) {
         uint32_t done;
         asm volatile(
             "{\n\t.reg .pred p;\n\t"
@@ -304,6 +304,7 @@ k_bf_mma(const FrameDev* __restrict__ frames, const PairDev* __restrict__ pairs,
             const uint64_t desc_b = smem_desc(saddr(sB), 128u, 2048u);
             const uint64_t desc_bx = smem_desc(saddr(sBx), 128u, 256u);
             uint32_t kk = 0, units_loaded = 0;
+            bool a_pending = false;  // a query tile in flight whose wait gave up
             int64_t last_mma = -1;  // tile index of the last MMA group committed
             int64_t loaded_to = 0;  // tiles [.., loaded_to) have had their loads issued
             auto load_b = [&](const TcUnit& u, uint32_t tile_kk, uint32_t n) -> bool {
@@ -326,7 +327,10 @@ k_bf_mma(const FrameDev* __restrict__ frames, const PairDev* __restrict__ pairs,
                 if (ok) {
                     bar_expect(&bar_a, TC_A_BYTES);
                     bulk_load(sA, u.A->bf8 + (size_t)u.qbase * TC_ROW_BYTES, TC_A_BYTES, &bar_a);
-                    ok = bar_wait(&bar_a, units_loaded & 1u);
+                    // the launch's first query-tile wait may be shortened (a test hook)
+                    const int fw = u.A->match_first_wait;
+                    ok = bar_wait(&bar_a, units_loaded & 1u, units_loaded == 0 && fw >= 0 ? (uint32_t)fw : kWaitLimit);
+                    a_pending = !ok;
                     ++units_loaded;
                 }
                 for (int n = 0; n < TC_STAGES - 1 && n < u.NT && ok; ++n) ok = load_b(u, kk + (uint32_t)n, (uint32_t)n);
@@ -363,6 +367,8 @@ k_bf_mma(const FrameDev* __restrict__ frames, const PairDev* __restrict__ pairs,
                 if (last_mma >= 0) bar_wait(&acc_full[last_mma & 1], (uint32_t)(last_mma >> 1) & 1u);
                 for (int64_t i = max(last_mma + 1, loaded_to - TC_STAGES); i < loaded_to; ++i)
                     bar_wait(&b_full[i % TC_STAGES], (uint32_t)(i / TC_STAGES) & 1u);
+                // the query tile whose wait gave up lands before the CTA leaves
+                if (a_pending) bar_wait(&bar_a, (units_loaded - 1u) & 1u);
             }
         }
         __syncwarp();

@@ -411,10 +411,11 @@ k_detect(const FrameDev* __restrict__ frames, const TileItem* __restrict__ tiles
         s_by1[k][ty] = min(max(r1, 0), SH - 1);
     }
     __syncthreads();  // the barrier is initialised before anyone polls it
-    const bool landed = mbar_wait(&s_bar, 0u, kTmaWaitLimit);
+    const uint32_t first_limit = F.detect_first_wait < 0 ? kTmaWaitLimit : (uint32_t)F.detect_first_wait;
+    const bool landed = mbar_wait(&s_bar, 0u, first_limit);
     if (__syncthreads_or(!landed)) {
         if (t == 0) atomicOr(err, USLAM_ERR_TMA_TIMEOUT);
-        mbar_wait(&s_bar, 0u, kTmaWaitLimit);  // the copy in flight, again bounded
+        mbar_wait(&s_bar, 0u, kTmaWaitLimit);  // the copy in flight lands before the tile is left (full limit)
         return;
     }
 
@@ -1677,6 +1678,33 @@ k_mutual(const FrameDev* __restrict__ frames, const PairDev* __restrict__ pairs,
     if (threadIdx.x == 0) P.match_count[l] = base;
 }
 
+// ------------------------------------------------------- frame ingest ----
+// The reference's f32 pixel rule (data/src/provider_base.cpp:121-124 stores
+// u8 / 255): the byte back, exact for those values; others become p * 255
+// clamped to [0, 255] (NaN to 0) and rounded half to even.  One thread per 4
+// pixels of a row.
+__global__ void __launch_bounds__(128) k_frame_from_f32(const float* __restrict__ src, int W, int H, uint8_t* __restrict__ dst, int dpitch) {
+    const int x4 = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y;
+    if (4 * x4 >= W || y >= H) return;
+    const float* row = src + (size_t)y * W;
+    uint32_t packed = 0;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const int x = 4 * x4 + k;
+        if (x >= W) break;
+        float t = row[x] * 255.0f;
+        t = t > 0.0f ? (t < 255.0f ? t : 255.0f) : 0.0f;
+        packed |= (uint32_t)__float2int_rn(t) << (8 * k);
+    }
+    uint8_t* out = dst + (size_t)y * dpitch + 4 * x4;
+    if (4 * x4 + 4 <= W) {
+        *reinterpret_cast<uint32_t*>(out) = packed;  // dpitch and the row start are multiples of 16
+    } else {
+        for (int k = 0; 4 * x4 + k < W; ++k) out[k] = (uint8_t)(packed >> (8 * k));
+    }
+}
+
 }  // namespace uslam
 
 // ------------------------------------------------------------ launch ----
@@ -1789,6 +1817,13 @@ cudaError_t launch_bruteforce(const FrameDev* frames, const PairDev* pairs, cons
                               float ratio, int grid, cudaStream_t st) {
     if (npairs <= 0) return cudaSuccess;
     k_bruteforce<<<grid, KB_THREADS, 0, st>>>(frames, pairs, psegs, npairs, ratio);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_frame_from_f32(const float* src, int W, int H, uint8_t* dst, int dpitch, cudaStream_t st) {
+    if (W <= 0 || H <= 0) return cudaSuccess;
+    const dim3 grid((W / 4 + 127) / 128 + 1, H);
+    k_frame_from_f32<<<grid, 128, 0, st>>>(src, W, H, dst, dpitch);
     return cudaGetLastError();
 }
 

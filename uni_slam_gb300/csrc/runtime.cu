@@ -353,6 +353,7 @@ uslam_status create_batch(uslam_ctx* ctx, int n_frames, const int* widths, const
         F.margin = ctx->margin;
         F.cell_cap = ctx->cell_cap;
         F.frame_cap = ctx->frame_cap;
+        F.detect_first_wait = F.match_first_wait = -1;
         F.img_pitch = static_cast<int>(round_up(static_cast<size_t>(W0), 16));
         level_dims(W0, H0, L, F.w, F.h);
         for (int l = 0; l < L; ++l) {
@@ -1125,6 +1126,19 @@ uslam_status uslam_autotune(uslam_ctx* ctx, int width, int height, const uint8_t
     return USLAM_OK;
 }
 
+uslam_status uslam_batch_set_first_wait(uslam_batch* b, int detect_polls, int match_polls) {
+    if (!b || detect_polls < -1 || match_polls < -1)
+        return set_err(b ? b->err() : nullptr, USLAM_INVALID_ARG, "set_first_wait: bad arguments");
+    for (FrameDev& F : b->frames) {
+        F.detect_first_wait = detect_polls;
+        F.match_first_wait = match_polls;
+    }
+    // the kernels read the frame table at run time: no new graph is needed
+    cudaError_t e = cudaMemcpy(b->d_frames, b->frames.data(), sizeof(FrameDev) * b->frames.size(), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return b->ctx->cuda_fail(e, "frame table upload");
+    return USLAM_OK;
+}
+
 uslam_status uslam_batch_io_bytes(uslam_batch* b, size_t* h2d, size_t* d2h) {
     if (!b) return USLAM_INVALID_ARG;
     if (h2d) *h2d = b->in_bytes;
@@ -1140,6 +1154,8 @@ struct uslam_frontend {
     uslam_batch* b = nullptr;
     uint8_t* incoming = nullptr;  // device buffer for caller-written frames
     uint8_t* h_stage = nullptr;   // pinned u8 staging of the next host frame (H0 rows of img_pitch)
+    float* h_stage_f32 = nullptr; // pinned f32 staging of the next f32 host frame (H0 rows of W0)
+    float* d_f32 = nullptr;       // its device copy
     int cur = -1;                 // slot holding FeatureSet(0)
     int ref = -1;                 // slot holding FeatureSet(1)
     bool matched = false;
@@ -1168,13 +1184,6 @@ std::pair<size_t, size_t> pair_out_range(const uslam_batch* b, int p) {
     return {b->pair_off[p], end - b->pair_off[p]};
 }
 
-// The reference's f32 pixel rule (data/src/provider_base.cpp:121-124 stores
-// u8 / 255): the byte back, exact for those values, nearest 1/255 otherwise.
-inline uint8_t f32_to_u8(float v) {
-    const long r = std::lrintf(v * 255.0f);
-    return static_cast<uint8_t>(r < 0 ? 0 : (r > 255 ? 255 : r));
-}
-
 // Choose the slot of the next frame and enqueue its copy and work.
 // src_host (u8) or src_f32 (f32 in [0, 1]) != NULL: the frame goes through
 // the pinned staging (an asynchronous H2D copy); else src_dev != NULL: D2D
@@ -1201,19 +1210,22 @@ uslam_status frontend_enqueue(uslam_frontend* fe, const uint8_t* src_host, const
     uint8_t* dst = const_cast<uint8_t*>(b->frames[slot].img);
     const size_t frame_bytes = static_cast<size_t>(F0.H0) * F0.img_pitch;
     cudaError_t e;
-    if (src_host || src_f32) {
+    if (src_host) {
         // the previous frame's upload from the staging has completed: every
         // host-frame call returns after its work (and its copies) finished
-        for (int y = 0; y < F0.H0; ++y) {
-            uint8_t* row = fe->h_stage + static_cast<size_t>(y) * F0.img_pitch;
-            if (src_host) {
-                std::memcpy(row, src_host + static_cast<size_t>(y) * pitch, F0.W0);
-            } else {
-                const float* in = src_f32 + static_cast<size_t>(y) * pitch;
-                for (int x = 0; x < F0.W0; ++x) row[x] = f32_to_u8(in[x]);
-            }
-        }
+        for (int y = 0; y < F0.H0; ++y)
+            std::memcpy(fe->h_stage + static_cast<size_t>(y) * F0.img_pitch, src_host + static_cast<size_t>(y) * pitch,
+                        F0.W0);
         e = cudaMemcpyAsync(dst, fe->h_stage, frame_bytes, cudaMemcpyHostToDevice, b->stream);
+    } else if (src_f32) {
+        // f32 rows into the pinned f32 staging, one asynchronous copy, the
+        // bytes recovered on the device
+        const size_t row_bytes = sizeof(float) * F0.W0;
+        for (int y = 0; y < F0.H0; ++y)
+            std::memcpy(fe->h_stage_f32 + static_cast<size_t>(y) * F0.W0, src_f32 + static_cast<size_t>(y) * pitch,
+                        row_bytes);
+        e = cudaMemcpyAsync(fe->d_f32, fe->h_stage_f32, row_bytes * F0.H0, cudaMemcpyHostToDevice, b->stream);
+        if (e == cudaSuccess) e = launch_frame_from_f32(fe->d_f32, F0.W0, F0.H0, dst, F0.img_pitch, b->stream);
     } else if (src_dev) {
         e = cudaMemcpy2DAsync(dst, F0.img_pitch, src_dev, pitch, F0.W0, F0.H0, cudaMemcpyDeviceToDevice, b->stream);
     } else {
@@ -1283,11 +1295,17 @@ uslam_status uslam_frontend_create(uslam_ctx* ctx, int width, int height, uslam_
     auto* fe = new uslam_frontend();
     fe->b = b;
     const size_t frame_bytes = static_cast<size_t>(b->frames[0].H0) * b->frames[0].img_pitch;
+    const size_t f32_bytes = sizeof(float) * static_cast<size_t>(b->frames[0].H0) * b->frames[0].W0;
     cudaError_t e = cudaMalloc(&fe->incoming, frame_bytes);
     if (e == cudaSuccess) e = cudaHostAlloc(&fe->h_stage, frame_bytes, cudaHostAllocDefault);
+    if (e == cudaSuccess) e = cudaHostAlloc(&fe->h_stage_f32, f32_bytes, cudaHostAllocDefault);
+    if (e == cudaSuccess) e = cudaMalloc(&fe->d_f32, f32_bytes);
     if (e != cudaSuccess) {
         cudaGetLastError();
         if (fe->incoming) cudaFree(fe->incoming);
+        if (fe->h_stage) cudaFreeHost(fe->h_stage);
+        if (fe->h_stage_f32) cudaFreeHost(fe->h_stage_f32);
+        if (fe->d_f32) cudaFree(fe->d_f32);
         uslam_batch_destroy(b);
         delete fe;
         return set_err(&ctx->err, USLAM_OOM, "frontend input buffer allocation refused");
@@ -1302,6 +1320,8 @@ void uslam_frontend_destroy(uslam_frontend* fe) {
     cudaSetDevice(fe->b->ctx->device);
     if (fe->incoming) cudaFree(fe->incoming);
     if (fe->h_stage) cudaFreeHost(fe->h_stage);
+    if (fe->h_stage_f32) cudaFreeHost(fe->h_stage_f32);
+    if (fe->d_f32) cudaFree(fe->d_f32);
     uslam_batch_destroy(fe->b);
     delete fe;
 }

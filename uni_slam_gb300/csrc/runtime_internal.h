@@ -39,6 +39,7 @@ cudaError_t launch_bruteforce(const FrameDev*, const PairDev*, const SegDev*, in
 cudaError_t launch_bf_mma(const FrameDev*, const PairDev*, const SegDev*, int, float, int, uint32_t*, cudaStream_t);
 cudaError_t set_compact_smem(int max_w);
 cudaError_t set_bf_mma_smem();
+cudaError_t launch_frame_from_f32(const float* src, int W, int H, uint8_t* dst, int dpitch, cudaStream_t st);
 // the windowed matcher on the tensor cores (win_tc.cu)
 cudaError_t set_win_mma_smem();
 int win_units_per_seg(int cap);

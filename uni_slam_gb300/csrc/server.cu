@@ -452,6 +452,7 @@ uslam_status uslam_server_create(uslam_ctx* ctx, const uslam_server_params* p, u
         F.margin = ctx->margin;
         F.cell_cap = ctx->cell_cap;
         F.frame_cap = ctx->frame_cap;
+        F.detect_first_wait = F.match_first_wait = -1;
         F.img_pitch = static_cast<int>(round_up(static_cast<size_t>(W0), 16));
         level_dims(W0, H0, L, F.w, F.h);
         for (int l = 0; l < L; ++l)

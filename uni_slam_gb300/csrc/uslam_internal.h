@@ -51,6 +51,10 @@ struct FrameDev {
     int margin;                      // blur cache margin M beyond the level
     int cell_cap;                    // > 0: keypoints kept per 32x32 cell (cell order); 0: (y, x) order
     int frame_cap;                   // > 0: features kept per frame, levels filled in order; 0: none
+    // polls of the first mbarrier wait of k_detect's tile load and of the
+    // tensor-core brute-force matcher's first query-tile load (-1: the
+    // kernels' own limits); a test hook of uslam_batch_set_first_wait
+    int detect_first_wait, match_first_wait;
     float* lvl[USLAM_MAX_LEVELS];
     const void* tmaps;  // CUtensorMap [levels][USLAM_NUM_TILE_SHAPES] over lvl (device, 64-byte aligned)
     float* blur[USLAM_MAX_LEVELS];
