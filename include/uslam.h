@@ -79,9 +79,13 @@ typedef struct uslam_params {
      *    best < ratio * second, no window and no cross-check (XOR + popcount
      *    on the integer pipes);
      * 2: the same brute-force top-2 with the distances from the tensor cores
-     *    (popc(a & b) as an FP8 0/1 dot product, exact): identical results. */
+     *    (popc(a & b) as an FP8 0/1 dot product, exact): identical results;
+     * 3: matcher 0 (the same match lists) with the in-window distances of
+     *    the batch path taken from tensor-core tiles (k_win_mma) where every
+     *    level holds at most 60000 features; slower than matcher 0 on the
+     *    752x480 workload, kept as an option. */
     int matcher;
-    float ratio;  /* Lowe ratio of matchers 1 and 2 (the windowed matcher uses the reference's 0.85) */
+    float ratio;  /* Lowe ratio of matchers 1 and 2 (the windowed matchers 0 and 3 use the reference's 0.85) */
     /* 0: a level's keypoints in (y, x) order, the first cap_per_level kept.
      * 1..1024: per-cell caps -- each level is cut into 32x32 cells from its
      * origin; the first cell_cap keypoints of each cell in (y, x) order are

@@ -18,6 +18,15 @@ def ctx(brief_pattern):
     c.close()
 
 
+@pytest.fixture(scope="module", params=[0, 3], ids=["k_match", "k_win_mma"])
+def wctx(request, brief_pattern):
+    """The windowed matcher with its distances from k_match (matcher 0) and
+    from the tensor cores (matcher 3): the same lists."""
+    c = Context(brief_pattern, levels=6, max_width=1280, max_height=720, matcher=request.param)
+    yield c
+    c.close()
+
+
 def _run(ctx, frames, pairs=()):
     b = Batch(ctx, [(f.shape[1], f.shape[0]) for f in frames], list(pairs))
     b.process(frames)
@@ -129,13 +138,14 @@ def test_features_and_matches_bit_exact(ctx, brief_pattern, seed):
         b.close()
 
 
-def test_uneven_batch_equals_oracle_and_alone(ctx, brief_pattern):
+def test_uneven_batch_equals_oracle_and_alone(wctx, brief_pattern):
     sizes = [(640, 480), (752, 480), (1280, 720), (97, 61), (333, 211)]
     frames, pairs = [], []
     for k, (w, h) in enumerate(sizes):
         a, c = synth.warped_pair(100 + k, w, h)
         frames += [a, c]
         pairs.append((2 * k, 2 * k + 1))
+    ctx = wctx
     b = _run(ctx, frames, pairs)
     try:
         for k, (w, h) in enumerate(sizes):
@@ -245,12 +255,12 @@ def test_frontend_rotation_matches_reference_rule(ctx, brief_pattern):
         fe.close()
 
 
-def test_large_batch_bit_exact(ctx, brief_pattern):
+def test_large_batch_bit_exact(wctx, brief_pattern):
     """22 frames (~170k keypoints, larger describe groups than the small
     tests), captured as two halves on two streams: every frame's features and
     a pair within the second half equal the oracle."""
     frames = synth.plane_sequence(77, n=22)
-    b = _run(ctx, frames, [(i, i + 1) for i in range(len(frames) - 1)])
+    b = _run(wctx, frames, [(i, i + 1) for i in range(len(frames) - 1)])
     try:
         total = 0
         for i, f in enumerate(frames):
@@ -265,7 +275,7 @@ def test_large_batch_bit_exact(ctx, brief_pattern):
         b.close()
 
 
-@pytest.mark.parametrize("matcher", [0, 2])
+@pytest.mark.parametrize("matcher", [0, 2, 3])
 def test_split_batch_pairs_across_halves(brief_pattern, matcher):
     """A batch of 20 frames is captured as two halves (frames 0-9 and 10-19)
     on two streams.  Pairs within either half, from the first half into the
@@ -282,7 +292,7 @@ def test_split_batch_pairs_across_halves(brief_pattern, matcher):
             for i in range(len(frames)):
                 _assert_features_equal(b.features(i), exp[i])
             for k, (p, q) in enumerate(pairs):
-                if matcher == 0:
+                if matcher in (0, 3):
                     em = oracle.match(exp[p][0], exp[p][1], exp[q][0], exp[q][1], W, H)
                 else:
                     em = oracle.match_bruteforce(exp[p][0], exp[p][1], exp[q][0], exp[q][1], 0.8)

@@ -662,9 +662,12 @@ __device__ void xsort_level(const FrameDev& F, int l, uint32_t kept, uint32_t* s
 // s_hist of w + 1 counters): the indices of the features with pick(i) true,
 // sorted by x, go to order_out; colstart_out (if given) receives the first
 // slot of each column.  Returns the number of features picked.
+// inv_out (if given) receives for every picked feature i its position plus
+// inv_base, and with inv_miss set ~0 for the others.
 template <typename Pick>
 __device__ uint32_t xsort_pass(const uint32_t* feats, uint32_t kept, int w, Pick pick, uint32_t* order_out,
-                               uint32_t* colstart_out, uint32_t* s_hist, uint32_t* s_warp) {
+                               uint32_t* colstart_out, uint32_t* s_hist, uint32_t* s_warp, uint32_t* inv_out = nullptr,
+                               uint32_t inv_base = 0u, bool inv_miss = false) {
     for (int i = threadIdx.x; i <= w; i += blockDim.x) s_hist[i] = 0u;
     __syncthreads();
     for (uint32_t i = threadIdx.x; i < kept; i += blockDim.x)
@@ -689,8 +692,15 @@ __device__ uint32_t xsort_pass(const uint32_t* feats, uint32_t kept, int w, Pick
         }
     }
     __syncthreads();
-    for (uint32_t i = threadIdx.x; i < kept; i += blockDim.x)
-        if (pick(i)) order_out[atomicAdd(&s_hist[(int)__uint_as_float(feats[(size_t)i * 12u])], 1u)] = i;
+    for (uint32_t i = threadIdx.x; i < kept; i += blockDim.x) {
+        if (pick(i)) {
+            const uint32_t pos = atomicAdd(&s_hist[(int)__uint_as_float(feats[(size_t)i * 12u])], 1u);
+            order_out[pos] = i;
+            if (inv_out) inv_out[i] = inv_base + pos;
+        } else if (inv_out && inv_miss) {
+            inv_out[i] = 0xffffffffu;
+        }
+    }
     __syncthreads();
     return tot;
 }
@@ -718,6 +728,7 @@ __device__ void xsort_level(const FrameDev& F, int l, uint32_t kept, uint32_t* s
     const float margin = 0.1f * H + 2.0f;
     const size_t cap = (size_t)(F.cap > 0 ? F.cap : 1);
     uint32_t* qband = F.colstart[l] + (size_t)NB * (size_t)(w + 1);
+    uint32_t* inv = F.winv[l];  // the tensor-core matcher's positions (null without it)
     for (int b = 0; b < NB; ++b) {
         const float lo = (float)b * H / (float)NB - margin, hi = (float)(b + 1) * H / (float)NB + margin;
         xsort_pass(
@@ -726,13 +737,14 @@ __device__ void xsort_level(const FrameDev& F, int l, uint32_t kept, uint32_t* s
                 const float y = lod0_y(feats, i, scale);
                 return y >= lo && y <= hi;
             },
-            F.xorder[l] + (size_t)b * cap, F.colstart[l] + (size_t)b * (size_t)(w + 1), s_hist, s_warp);
+            F.xorder[l] + (size_t)b * cap, F.colstart[l] + (size_t)b * (size_t)(w + 1), s_hist, s_warp,
+            inv ? inv + cap * (size_t)(1 + b) : nullptr, 0u, true);
     }
     uint32_t base = 0;
     for (int b = 0; b < NB; ++b) {
         const uint32_t n = xsort_pass(
             feats, kept, w, [&](uint32_t i) { return match_band(lod0_y(feats, i, scale), H) == b; },
-            F.qorder[l] + base, nullptr, s_hist, s_warp);
+            F.qorder[l] + base, nullptr, s_hist, s_warp, inv, base, false);
         if (threadIdx.x == 0) qband[b] = base;
         base += n;
     }
@@ -1099,9 +1111,55 @@ __device__ __forceinline__ uint32_t e4m3_small_int(int v) {
     return (uint32_t)(((k + 7) << 3) | (((v - (1 << k)) << 3) >> k));
 }
 
-// PACK: also write the tensor-core matcher's operand rows of every feature
-// (FrameDev::bf8 / bfext / bfpop / bfid).
-template <bool PACK>
+// FP8 operand row of a descriptor (bit k -> 0x50 = 8.0 or 0x00) at row R of
+// a K-major no-swizzle operand array: lane j writes bits 8 j .. 8 j + 7 (K
+// chunk j / 2, half j % 2); wj = the descriptor word holding them.
+__device__ __forceinline__ void write_fp8_row(uint8_t* base, uint32_t R, uint32_t wj, int lane) {
+    const uint32_t bits = (wj >> (8 * (lane & 3))) & 0xffu;
+    uint32_t lo = 0u, hi = 0u;
+#pragma unroll
+    for (int b = 0; b < 4; ++b) {
+        lo |= ((bits >> b) & 1u) * (0x50u << (8 * b));
+        hi |= ((bits >> (b + 4)) & 1u) * (0x50u << (8 * b));
+    }
+    *reinterpret_cast<uint2*>(base + (size_t)(R >> 3) * 2048u + (lane >> 1) * 128u + (R & 7u) * 16u + (lane & 1) * 8u) =
+        make_uint2(lo, hi);
+}
+// Extension row (32 E4M3 values) at row R, lanes 0-3: the popcount pc split
+// into 16 integers <= 16, then 256, grp split into two integers <= 16, then 1.
+__device__ __forceinline__ void write_ext_row(uint8_t* base, uint32_t R, uint32_t pc, int grp, int lane) {
+    uint32_t ext[2] = {0u, 0u};
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        const int e = 8 * lane + k;  // extension value index 0..31
+        uint32_t code = 0u;
+        if (e < 16) code = e4m3_small_int(min(16, max(0, (int)pc - 16 * e)));
+        else if (e == 16) code = 0x78u;  // 256
+        else if (e == 17) code = e4m3_small_int(min(grp, 16));
+        else if (e == 18) code = e4m3_small_int(max(grp - 16, 0));
+        else if (e == 19) code = 0x38u;  // 1
+        ext[k >> 2] |= code << (8 * (k & 3));
+    }
+    *reinterpret_cast<uint2*>(base + (size_t)(R >> 3) * 256u + (lane >> 1) * 128u + (R & 7u) * 16u + (lane & 1) * 8u) =
+        make_uint2(ext[0], ext[1]);
+}
+// Query-order position k of level l -> its operand row (each band's queries
+// from a multiple of 128 rows).
+__device__ __forceinline__ uint32_t win_query_row(const uint32_t* qband, int l, int wq_rows, uint32_t k) {
+    uint32_t off = (uint32_t)l * (uint32_t)wq_rows, b = 0;
+    while (b + 1 < (uint32_t)USLAM_MATCH_BANDS && k >= qband[b + 1]) {
+        off += (qband[b + 1] - qband[b] + 127u) / 128u * 128u;
+        ++b;
+    }
+    return off + (k - qband[b]);
+}
+
+// PACK: also write the brute-force tensor-core matcher's operand rows of
+// every feature (FrameDev::bf8 / bfext / bfpop / bfid).  WIN: the windowed
+// tensor-core matcher's rows: the feature's query row (wq8) and its row in
+// every candidate list that holds it (wc8, wcext, wcy, wcid), at the
+// positions k_xsort recorded (winv).
+template <bool PACK, bool WIN>
 __global__ void __launch_bounds__(KD_THREADS)
 k_describe(const FrameDev* __restrict__ frames, const SegDev* __restrict__ segs, int nseg,
            const int32_t* __restrict__ pattern) {
@@ -1207,6 +1265,29 @@ k_describe(const FrameDev* __restrict__ frames, const SegDev* __restrict__ segs,
             for (int k = 0; k < 8; ++k)
                 if (lane == 4 + k) out = words[k];
             if (lane >= 3 && lane < 12) rec[lane] = out;
+            if constexpr (WIN) {
+                uint32_t wj = words[0];
+                uint32_t pc = 0;
+#pragma unroll
+                for (int k = 0; k < 8; ++k) {
+                    if ((lane >> 2) == k) wj = words[k];
+                    pc += (uint32_t)__popc(words[k]);
+                }
+                const uint32_t* inv = F.winv[l];
+                const size_t cap = (size_t)(F.cap > 0 ? F.cap : 1);
+                const uint32_t* qband = F.colstart[l] + (size_t)USLAM_MATCH_BANDS * (size_t)(w + 1);
+                write_fp8_row(F.wq8, win_query_row(qband, l, F.wq_rows, __ldg(inv + i)), wj, lane);
+#pragma unroll
+                for (int b = 0; b < USLAM_MATCH_BANDS; ++b) {
+                    const uint32_t pos = __ldg(inv + cap * (size_t)(1 + b) + i);
+                    if (pos == 0xffffffffu) continue;
+                    const uint32_t R = (uint32_t)(USLAM_MATCH_BANDS * l + b) * (uint32_t)F.wc_rows + pos;
+                    write_fp8_row(F.wc8, R, wj, lane);
+                    if (lane < 4) write_ext_row(F.wcext, R, pc, (int)(pos & 31u), lane);
+                    else if (lane == 4) F.wcy[R] = (uint16_t)y;
+                    else if (lane == 5) F.wcid[R] = USLAM_PACK(l, i);
+                }
+            }
             if constexpr (PACK) {
                 // tensor-core operand rows of this feature (flat index f over
                 // the levels): lane j writes the FP8 values of descriptor bits
@@ -1770,10 +1851,11 @@ cudaError_t launch_blur_border(const FrameDev* frames, const SegDev* segs, int n
 }
 
 cudaError_t launch_describe(const FrameDev* frames, const SegDev* segs, int nseg, const int32_t* pattern,
-                            int grid, bool pack, cudaStream_t st) {
+                            int grid, bool pack, bool win, cudaStream_t st) {
     if (nseg <= 0) return cudaSuccess;
-    if (pack) k_describe<true><<<grid, KD_THREADS, 0, st>>>(frames, segs, nseg, pattern);
-    else k_describe<false><<<grid, KD_THREADS, 0, st>>>(frames, segs, nseg, pattern);
+    if (pack) k_describe<true, false><<<grid, KD_THREADS, 0, st>>>(frames, segs, nseg, pattern);
+    else if (win) k_describe<false, true><<<grid, KD_THREADS, 0, st>>>(frames, segs, nseg, pattern);
+    else k_describe<false, false><<<grid, KD_THREADS, 0, st>>>(frames, segs, nseg, pattern);
     return cudaGetLastError();
 }
 

@@ -94,7 +94,7 @@ struct uslam_batch {
     cudaEvent_t lane_fork[kLanes] = {}, lane_join[kLanes] = {}, lane_desc[kLanes] = {}, lane_end[kLanes] = {};
     cudaEvent_t ev_start = nullptr;
     Program full;
-    // the windowed matcher on the tensor cores (k_win_pack / k_win_plan /
+    // the windowed matcher on the tensor cores (k_describe<WIN> / k_win_plan /
     // k_win_mma; else k_match): matcher 0 with list positions within 16 bits
     bool win_tc = false;
     int win_umax = 0;  // unit slots per (pair, direction, level)
@@ -193,9 +193,7 @@ cudaError_t enqueue_frames(uslam_batch* b, const Program& P, const Lane& ln) {
         cudaSuccess)
         return e;
     if ((e = cudaStreamWaitEvent(ln.st, ln.join, 0)) != cudaSuccess) return e;
-    if ((e = launch_describe(b->d_frames, P.fsegs, P.nfsegs, c->d_pattern, grid, c->matcher == 2, ln.st)) != cudaSuccess)
-        return e;
-    return b->win_tc ? launch_win_pack(b->d_frames, P.fsegs, P.nfsegs, c->num_sms, ln.st) : cudaSuccess;
+    return launch_describe(b->d_frames, P.fsegs, P.nfsegs, c->d_pattern, grid, c->matcher == 2, b->win_tc, ln.st);
 }
 
 // The pair stages of a program: match and the mutual check / emit.
@@ -324,16 +322,16 @@ uslam_status create_batch(uslam_ctx* ctx, int n_frames, const int* widths, const
     struct FrameLayout {
         size_t lvl[USLAM_MAX_LEVELS], blur[USLAM_MAX_LEVELS], kpmap[USLAM_MAX_LEVELS], feats[USLAM_MAX_LEVELS],
             xorder[USLAM_MAX_LEVELS], colstart[USLAM_MAX_LEVELS], qorder[USLAM_MAX_LEVELS], bands[USLAM_MAX_LEVELS], counts,
-            tmaps, bf8, bfext, bfpop, bfid, wq8, wc8, wcext, wcy, wcid;
+            tmaps, bf8, bfext, bfpop, bfid, wq8, wc8, wcext, wcy, wcid, winv[USLAM_MAX_LEVELS];
     };
-    // the windowed tensor-core matcher: matcher 0, every list position and
-    // candidate row within 16 bits
+    // the windowed tensor-core matcher (asked for as matcher 3): every list
+    // position and candidate row within 16 bits, else k_match
     int max_cap = 1;
     for (int f = 0; f < n_frames; ++f) {
         const long long c = ctx->cap_override > 0 ? ctx->cap_override : static_cast<long long>(widths[f]) * heights[f] / 250;
         max_cap = static_cast<int>(std::max<long long>(max_cap, c));
     }
-    b->win_tc = ctx->matcher == 0 && max_cap <= kWinMaxCap && ctx->max_h < 65535;
+    b->win_tc = ctx->win_tc && max_cap <= kWinMaxCap && ctx->max_h < 65535;
     b->win_umax = b->win_tc ? win_units_per_seg(max_cap) : 0;
     std::vector<FrameLayout> fl(n_frames);
     for (int f = 0; f < n_frames; ++f) {
@@ -405,6 +403,7 @@ uslam_status create_batch(uslam_ctx* ctx, int n_frames, const int* widths, const
             Ly.wcext = take(&scratch, crows * 32);
             Ly.wcy = take(&scratch, crows * 2);
             Ly.wcid = take(&scratch, crows * 4);
+            for (int l = 0; l < L; ++l) Ly.winv[l] = take(&scratch, (1 + USLAM_MATCH_BANDS) * capa * 4);
         }
         b->max_w = std::max(b->max_w, F.w[0]);
     }
@@ -551,6 +550,7 @@ uslam_status create_batch(uslam_ctx* ctx, int n_frames, const int* widths, const
             F.wcext = reinterpret_cast<uint8_t*>(sc_base + Ly.wcext);
             F.wcy = reinterpret_cast<uint16_t*>(sc_base + Ly.wcy);
             F.wcid = reinterpret_cast<int32_t*>(sc_base + Ly.wcid);
+            for (int l = 0; l < L; ++l) F.winv[l] = reinterpret_cast<uint32_t*>(sc_base + Ly.winv[l]);
         }
         std::vector<char> maps(static_cast<size_t>(L) * kNumTileShapes * USLAM_TMAP_BYTES);
         s = encode_tile_maps(F, ctx->detector, maps.data(), &ctx->err);
@@ -802,7 +802,8 @@ uslam_status uslam_create(const uslam_params* params, uslam_ctx** out) {
     if (params->levels < 1 || params->levels > USLAM_MAX_LEVELS || params->max_width < 1 ||
         params->max_width > kMaxWidth || params->max_height < 1 || params->max_height > 65535 ||
         params->cap_per_level < 0 || params->cap_per_level >= (1 << 24) || !params->brief_pattern ||
-        (params->matcher < 0 || params->matcher > 2) || (params->matcher != 0 && !(params->ratio > 0.0f)) ||
+        (params->matcher < 0 || params->matcher > 3) ||
+        ((params->matcher == 1 || params->matcher == 2) && !(params->ratio > 0.0f)) ||
         params->cell_cap < 0 || params->cell_cap > 1024 || (params->detector != 0 && params->detector != 1) ||
         params->frame_cap < 0)
         return USLAM_INVALID_ARG;
@@ -812,7 +813,9 @@ uslam_status uslam_create(const uslam_params* params, uslam_ctx** out) {
     c->max_w = params->max_width;
     c->max_h = params->max_height;
     c->cap_override = params->cap_per_level;
-    c->matcher = params->matcher;
+    // matcher 3 is matcher 0 (the same lists) with the distances from the tensor cores
+    c->matcher = params->matcher == 3 ? 0 : params->matcher;
+    c->win_tc = params->matcher == 3;
     c->ratio = params->ratio;
     c->cell_cap = params->cell_cap;
     c->frame_cap = params->frame_cap;
@@ -1006,8 +1009,8 @@ uslam_status uslam_batch_profile(uslam_batch* b, int iters, float* kernel_ms) {
         if (e == cudaSuccess)
             e = launch_compact_banded(b->d_frames, P.bands, P.nbands, P.fsegs, P.nfsegs, b->max_w, b->stream);
         mark();
-        if (e == cudaSuccess) e = launch_describe(b->d_frames, P.fsegs, P.nfsegs, c->d_pattern, grid, c->matcher == 2, b->stream);
-        if (e == cudaSuccess && b->win_tc) e = launch_win_pack(b->d_frames, P.fsegs, P.nfsegs, c->num_sms, b->stream);
+        if (e == cudaSuccess)
+            e = launch_describe(b->d_frames, P.fsegs, P.nfsegs, c->d_pattern, grid, c->matcher == 2, b->win_tc, b->stream);
         mark();
         if (e == cudaSuccess)
             e = c->matcher == 1 ? launch_bruteforce(b->d_frames, b->d_pairs, P.psegs, P.npsegs, c->ratio, grid, b->stream)

@@ -28,7 +28,7 @@ cudaError_t launch_detect(const FrameDev*, const TileItem*, int, int, int, uint3
 cudaError_t launch_pyramid(const FrameDev*, const TileItem*, int, int, cudaStream_t);
 cudaError_t launch_compact_banded(const FrameDev*, const BandItem*, int, const SegDev*, int, int, cudaStream_t);
 cudaError_t launch_blur_border(const FrameDev*, const SegDev*, int, int, cudaStream_t);
-cudaError_t launch_describe(const FrameDev*, const SegDev*, int, const int32_t*, int, bool, cudaStream_t);
+cudaError_t launch_describe(const FrameDev*, const SegDev*, int, const int32_t*, int, bool, bool, cudaStream_t);
 cudaError_t launch_match(const FrameDev*, const PairDev*, const void*, int, int, cudaStream_t);
 cudaError_t launch_match_dyn(const FrameDev*, const PairDev*, const void*, int, int, uint32_t*, cudaStream_t);
 cudaError_t launch_mutual(const FrameDev*, const PairDev*, const SegDev*, int, uint32_t*, cudaStream_t);
@@ -44,7 +44,6 @@ cudaError_t launch_frame_from_f32(const float* src, int W, int H, uint8_t* dst, 
 cudaError_t set_win_mma_smem();
 int win_units_per_seg(int cap);
 size_t win_unit_bytes();
-cudaError_t launch_win_pack(const FrameDev*, const SegDev*, int, int, cudaStream_t);
 cudaError_t launch_win_match(const FrameDev*, const PairDev*, const void*, int, int, void*, int, uint32_t*,
                              cudaStream_t);
 constexpr int kWinMaxCap = 60000;  // list positions and tile columns stay within 16 bits
@@ -229,6 +228,7 @@ struct uslam_ctx {
     int num_sms = 0;
     int margin = 0;  // blur-cache margin: BRIEF pattern radius + 2
     int matcher = 0;      // 0 windowed mutual (reference), 1 brute-force top-2
+    bool win_tc = false;  // matcher 0 asked for with the distances from the tensor cores (matcher 3)
     float ratio = 0.8f;   // Lowe ratio of the brute-force matcher
     int frame_cap = 0;    // > 0: features kept per frame, levels filled in order
     int cell_cap = 0;     // > 0: keypoints kept per 32x32 cell of a level, cell order

@@ -313,7 +313,7 @@ cudaError_t launch_batch(uslam_server* s, const std::vector<uint64_t>& tickets, 
     if ((e = launch_compact_banded(s->d_frames, d_bands, static_cast<int>(bands.size()), d_fsegs, nf, s->max_w,
                                    st)) != cudaSuccess)
         return e;
-    if ((e = launch_describe(s->d_frames, d_fsegs, nf, c->d_pattern, grid, false, st)) != cudaSuccess) return e;
+    if ((e = launch_describe(s->d_frames, d_fsegs, nf, c->d_pattern, grid, false, false, st)) != cudaSuccess) return e;
     if (!pairs.empty()) {
         if ((e = launch_match(s->d_frames, d_pairs, d_msegs, static_cast<int>(msegs.size()), grid, st)) != cudaSuccess)
             return e;

@@ -89,6 +89,8 @@ struct FrameDev {
     // wc_rows), with the extension rows of the bfext layout (row index within
     // its 32-row group = list position % 32); wcy: the candidate's y in its
     // level; wcid: packed (level, index).
+    uint32_t* winv[USLAM_MAX_LEVELS];  // per level: query-order position of feature i at [i], its position
+                                       // in candidate list b (or ~0) at [cap (1 + b) + i] (written by k_xsort)
     uint8_t* wq8;
     uint8_t* wc8;
     uint8_t* wcext;

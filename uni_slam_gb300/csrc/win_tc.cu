@@ -16,7 +16,7 @@
 //     list rows (k_win_plan writes the units);
 //   * the operands are the descriptors as FP8 rows (bit = 8.0 or 0, so a 0/1
 //     dot product times 64) with the popcount / row extension of k_bf_mma,
-//     written by k_win_pack in query order and in list order; nine
+//     written by k_describe in query order and in list order; nine
 //     tcgen05.mma (K = 32) per tile leave in TMEM the exact integer key
 //       key = 32 (2 dot - popc(b) + 257) + s,   32 <= key <= 16447,
 //     (s = the candidate's list position mod 32), a larger key a smaller
@@ -255,111 +255,7 @@ __device__ void y_rows(float cy, float dy, float s, int h, int* lo, int* hi) {
     *hi = e;
 }
 
-__device__ __forceinline__ uint32_t e4m3_small_int(int v) {
-    if (v <= 0) return 0u;
-    const int k = 31 - __clz(v);
-    return (uint32_t)(((k + 7) << 3) | (((v - (1 << k)) << 3) >> k));
-}
-// Bits 0..3 of n as four bytes of 0x50 (E4M3 8.0) or 0.
-__device__ __forceinline__ uint32_t nibble_fp8(uint32_t n) { return ((n * 0x204081u) & 0x01010101u) * 0x50u; }
-
-// Query-order row of position k of level l: each band's queries start at a
-// multiple of 128 rows.
-__device__ __forceinline__ uint32_t query_row(const uint32_t* qband, int l, int wq_rows, uint32_t k) {
-    uint32_t off = (uint32_t)l * (uint32_t)wq_rows, b = 0;
-    while (b + 1 < (uint32_t)NB && k >= qband[b + 1]) {
-        off += (qband[b + 1] - qband[b] + 127u) / 128u * 128u;
-        ++b;
-    }
-    return off + (k - qband[b]);
-}
-
 }  // namespace
-
-// ------------------------------------------------------------------ pack ----
-// Operand rows of one (frame, level) per CTA-stride: the queries (wq8) and
-// the NB candidate lists (wc8, wcext, wcy, wcid), one warp per row.  Lane j <
-// 16 writes descriptor bits 16 j .. 16 j + 15 as 16 FP8 values (K chunk j of
-// the core-matrix layout); lanes 16, 17 the two halves of a candidate's
-// extension row; lane 18 its y, lane 19 its id.
-__global__ void __launch_bounds__(256) k_win_pack(const FrameDev* __restrict__ frames,
-                                                  const SegDev* __restrict__ segs) {
-    const SegDev sg = segs[blockIdx.y];
-    const FrameDev& F = frames[sg.frame];
-    const int l = sg.level;
-    const uint32_t kept = F.kept[l];
-    const int w = F.w[l];
-    const uint32_t* cs = F.colstart[l];
-    const uint32_t* qband = cs + (size_t)NB * (size_t)(w + 1);
-    uint32_t len[NB];
-    uint32_t total = kept;
-    for (int b = 0; b < NB; ++b) {
-        len[b] = cs[(size_t)b * (size_t)(w + 1) + w];
-        total += len[b];
-    }
-    const int lane = threadIdx.x & 31;
-    const uint32_t warps = gridDim.x * (blockDim.x >> 5);
-    const size_t cap = (size_t)(F.cap > 0 ? F.cap : 1);
-    for (uint32_t r = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); r < total; r += warps) {
-        uint32_t i, R;
-        bool cand = false;
-        uint32_t pos = 0;
-        if (r < kept) {
-            i = __ldg(F.qorder[l] + r);
-            R = query_row(qband, l, F.wq_rows, r);
-        } else {
-            uint32_t k = r - kept;
-            int b = 0;
-            while (b + 1 < NB && k >= len[b]) {
-                k -= len[b];
-                ++b;
-            }
-            i = __ldg(F.xorder[l] + (size_t)b * cap + k);
-            R = (uint32_t)(NB * l + b) * (uint32_t)F.wc_rows + k;
-            cand = true;
-            pos = k;
-        }
-        const uint32_t* rec = F.feats[l] + (size_t)i * 12u;
-        const uint4 d0 = *reinterpret_cast<const uint4*>(rec + 4);
-        const uint4 d1 = *reinterpret_cast<const uint4*>(rec + 8);
-        uint8_t* dst = cand ? F.wc8 : F.wq8;
-        if (lane < 16) {
-            const uint32_t wd[8] = {d0.x, d0.y, d0.z, d0.w, d1.x, d1.y, d1.z, d1.w};
-            uint32_t word = wd[0];
-#pragma unroll
-            for (int k = 1; k < 8; ++k)
-                if ((lane >> 1) == k) word = wd[k];
-            const uint32_t bits = (word >> (16 * (lane & 1))) & 0xffffu;
-            const uint4 v = make_uint4(nibble_fp8(bits & 15u), nibble_fp8((bits >> 4) & 15u),
-                                       nibble_fp8((bits >> 8) & 15u), nibble_fp8(bits >> 12));
-            *reinterpret_cast<uint4*>(dst + (size_t)(R >> 3) * 2048u + (uint32_t)lane * 128u + (R & 7u) * 16u) = v;
-        } else if (cand && lane < 18) {
-            // popcount split into 16 integers <= 16, 256, the list position's
-            // index within its 32-row group split into two integers <= 16, 1
-            const uint32_t pc = (uint32_t)(__popc(d0.x) + __popc(d0.y) + __popc(d0.z) + __popc(d0.w) + __popc(d1.x) +
-                                           __popc(d1.y) + __popc(d1.z) + __popc(d1.w));
-            const int grp = (int)(pos & 31u);
-            uint32_t ext[4] = {0u, 0u, 0u, 0u};
-#pragma unroll
-            for (int k = 0; k < 16; ++k) {
-                const int e = 16 * (lane - 16) + k;  // extension value index 0..31
-                uint32_t code = 0u;
-                if (e < 16) code = e4m3_small_int(min(16, max(0, (int)pc - 16 * e)));
-                else if (e == 16) code = 0x78u;  // 256
-                else if (e == 17) code = e4m3_small_int(min(grp, 16));
-                else if (e == 18) code = e4m3_small_int(max(grp - 16, 0));
-                else if (e == 19) code = 0x38u;  // 1
-                ext[k >> 2] |= code << (8 * (k & 3));
-            }
-            *reinterpret_cast<uint4*>(F.wcext + (size_t)(R >> 3) * 256u + (uint32_t)(lane - 16) * 128u + (R & 7u) * 16u) =
-                make_uint4(ext[0], ext[1], ext[2], ext[3]);
-        } else if (cand && lane == 18) {
-            F.wcy[R] = (uint16_t)(uint32_t)__uint_as_float(rec[1]);
-        } else if (cand && lane == 19) {
-            F.wcid[R] = USLAM_PACK(l, i);
-        }
-    }
-}
 
 // ------------------------------------------------------------------ plan ----
 // The units of one (pair, direction, level) per CTA: for band b, query tile
@@ -808,13 +704,6 @@ cudaError_t set_win_mma_smem() {
 
 // Unit slots per (pair, direction, level) for levels of at most `cap` features.
 int win_units_per_seg(int cap) { return (cap + WN_M - 1) / WN_M + NB; }
-
-cudaError_t launch_win_pack(const FrameDev* frames, const SegDev* fsegs, int nfsegs, int num_sms, cudaStream_t st) {
-    if (nfsegs <= 0) return cudaSuccess;
-    const int gx = max(1, (4 * num_sms + nfsegs - 1) / nfsegs);
-    k_win_pack<<<dim3(gx, nfsegs), 256, 0, st>>>(frames, fsegs);
-    return cudaGetLastError();
-}
 
 cudaError_t launch_win_match(const FrameDev* frames, const PairDev* pairs, const void* msegs, int nmsegs, int umax,
                              void* units, int num_sms, uint32_t* err, cudaStream_t st) {

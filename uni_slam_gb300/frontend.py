@@ -30,7 +30,8 @@ class Context:
     """Device context: BRIEF table, level count, caps (per level and, with
     cell_cap > 0, per 32x32 cell), size limits, matcher (0: the reference's
     windowed mutual matcher, 1: brute-force top-2 with Lowe ``ratio`` on the
-    integer pipes, 2: the same brute-force top-2 on the tensor cores) and
+    integer pipes, 2: the same brute-force top-2 on the tensor cores, 3: the
+    windowed matcher with its distances from tensor-core tiles) and
     detector (0: the reference's FAST + cull, 1: the cfg profile, FAST
     9-of-16 at 20/255 with 3x3 NMS); frame_cap > 0 keeps the first frame_cap
     features of a frame in (level, order within the level) order."""
