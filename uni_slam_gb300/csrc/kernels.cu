@@ -249,8 +249,8 @@ __device__ __forceinline__ void tma_load_2d(void* dst, const void* tmap, int x, 
 
 // ----------------------------------------------------------- pyramid ----
 // Level l of one TW x TH tile into lvl[l] (row pitch lvl_pitch): l = 0 is
-// f32(u8) / 255 (provider_base.cpp:121-124), read 8 pixels per 8-byte load
-// and stored as two 16-byte vectors; l >= 1 is one canonical bilinear tap of
+// f32(u8) / 255 (provider_base.cpp:121-124), read 16 pixels per 16-byte load
+// and stored as four 16-byte vectors; l >= 1 is one canonical bilinear tap of
 // LOD0 at the texel centre (create_pyramid.wgsl:11-12).  Sampling
 // coordinates depend only on the row or only on the column, so they are
 // computed once per tile row / column (the per-pixel operations, so the same
@@ -259,7 +259,7 @@ __device__ __forceinline__ void tma_load_2d(void* dst, const void* tmap, int x, 
 template <int TW, int TH>
 __global__ void __launch_bounds__(K1_THREADS)
 k_pyramid(const FrameDev* __restrict__ frames, const TileItem* __restrict__ tiles) {
-    static_assert(K1_THREADS % TW == 0 && TW % 8 == 0, "tile shape");
+    static_assert(K1_THREADS % TW == 0 && TW % 16 == 0, "tile shape");
     __shared__ float s_lut[256];  // f32(u8) / 255
     __shared__ int2 s_fx[TW];     // LOD0 source columns (x0, x1) per tile column
     __shared__ float2 s_fa[TW];   // (1 - a, a)
@@ -278,27 +278,26 @@ k_pyramid(const FrameDev* __restrict__ frames, const TileItem* __restrict__ tile
     s_lut[t] = (float)t / 255.0f;
     if (l == 0) {
         __syncthreads();
-        constexpr int SEGS = TW / 8;
+        constexpr int SEGS = TW / 16;
         for (int u = t; u < SEGS * TH; u += K1_THREADS) {
             const int r = u / SEGS;
-            const int x = X0 + (u - r * SEGS) * 8, y = Y0 + r;
+            const int x = X0 + (u - r * SEGS) * 16, y = Y0 + r;
             if (y >= h || x >= w) continue;
-            // x is a multiple of 8 below w, so x + 8 <= the 16-byte image pitch
-            const uint2 q = *reinterpret_cast<const uint2*>(img + (size_t)y * pitch + x);
-            float v[8];
-#pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                v[k] = s_lut[(q.x >> (8 * k)) & 255u];
-                v[4 + k] = s_lut[(q.y >> (8 * k)) & 255u];
-            }
+            // x is a multiple of 16 below w, so x + 16 <= the 16-byte image pitch
+            const uint4 q = *reinterpret_cast<const uint4*>(img + (size_t)y * pitch + x);
+            const uint32_t qw[4] = {q.x, q.y, q.z, q.w};
             float* o = out + (size_t)y * lp + x;
-            if (x + 8 <= lp) {
-                reinterpret_cast<float4*>(o)[0] = make_float4(v[0], v[1], v[2], v[3]);
-                reinterpret_cast<float4*>(o)[1] = make_float4(v[4], v[5], v[6], v[7]);
-            } else {
 #pragma unroll
-                for (int k = 0; k < 8; ++k)
-                    if (x + k < w) o[k] = v[k];
+            for (int g = 0; g < 4; ++g) {
+                const float4 v = make_float4(s_lut[qw[g] & 255u], s_lut[(qw[g] >> 8) & 255u],
+                                             s_lut[(qw[g] >> 16) & 255u], s_lut[qw[g] >> 24]);
+                // rows of 16-byte pitch: a group of 4 inside the row is stored whole
+                if (x + 4 * g + 4 <= lp) reinterpret_cast<float4*>(o)[g] = v;
+                else if (x + 4 * g < w) {
+                    const float vv[4] = {v.x, v.y, v.z, v.w};
+                    for (int k = 0; k < 4; ++k)
+                        if (x + 4 * g + k < w) o[4 * g + k] = vv[k];
+                }
             }
         }
         return;
@@ -370,6 +369,7 @@ k_detect(const FrameDev* __restrict__ frames, const TileItem* __restrict__ tiles
     __shared__ float2 s_b01[TH], s_nb01[TH], s_b22[TH], s_nb22[TH];
     __shared__ float s_score[CFG ? TH + 2 : 1][CFG ? TW + 2 : 1];  // cfg: FAST score, tile + 1 ring
     __shared__ uint8_t s_arc[CFG ? TH + 2 : 1][CFG ? TW + 2 : 1];
+    __shared__ uint8_t s_rowfast[TH];  // row taps at fixed offsets (no edge clamp)
     const TileItem it = tiles[blockIdx.x];
     const FrameDev& F = frames[it.frame];
     const int l = it.level;
@@ -390,6 +390,8 @@ k_detect(const FrameDev* __restrict__ frames, const TileItem* __restrict__ tiles
         mbar_expect_tx(&s_bar, (uint32_t)(SH * BW * 4));
         tma_load_2d(&sbox[0][0], tmap, X0 - USLAM_TILE_XPAD, Y0 - HY, &s_bar);
     }
+    for (int i = t; i < TH; i += K1_THREADS) s_rowfast[i] = 1;
+    __syncthreads();
     for (int i = t; i < 3 * TH; i += K1_THREADS) {
         // generate_features.wgsl:153-169, y part of the 9 taps
         const int ty = i / 3, k = i % 3;
@@ -409,6 +411,11 @@ k_detect(const FrameDev* __restrict__ frames, const TileItem* __restrict__ tiles
         }
         s_by0[k][ty] = min(max(r0, 0), SH - 1);
         s_by1[k][ty] = min(max(r1, 0), SH - 1);
+        // the row taps of an interior row sit at rows -2, -1 | d, d + 1 | 1, 2
+        // around the pixel (d = -1 or 0): no edge clamp
+        const int rr = ty + HY, e = k == 0 ? -2 : (k == 1 ? r0 - rr : 1);
+        const bool ok = r1 == r0 + 1 && r0 == rr + e && (k != 1 || e == -1 || e == 0);
+        if (!ok) s_rowfast[ty] = 0;
     }
     __syncthreads();  // the barrier is initialised before anyone polls it
     const uint32_t first_limit = F.detect_first_wait < 0 ? kTmaWaitLimit : (uint32_t)F.detect_first_wait;
@@ -421,13 +428,26 @@ k_detect(const FrameDev* __restrict__ frames, const TileItem* __restrict__ tiles
 
     // 1. halo cells outside the level follow the Tint clamp min(u32(c), n - 1)
     //    (a negative coordinate reads the far edge)
+    //    Only those cells are visited: whole rows above and below the level,
+    //    then the columns left and right of it in the rows between.
     if (X0 < HX || X0 + TW + HX > w || Y0 < HY || Y0 + TH + HY > h) {
         const float* lv = F.lvl[l];
         const int lp = F.lvl_pitch[l];
-        for (int idx = t; idx < SH * SW; idx += K1_THREADS) {
-            const int r = idx / SW, c = idx - r * SW;
+        const int top = min(max(HY - Y0, 0), SH), bot = min(max(Y0 - HY + SH - h, 0), SH - top);
+        const int left = min(max(HX - X0, 0), SW), right = min(max(X0 - HX + SW - w, 0), SW - left);
+        const int nrow = (top + bot) * SW, nside = (SH - top - bot) * (left + right);
+        for (int idx = t; idx < nrow + nside; idx += K1_THREADS) {
+            int r, c;
+            if (idx < nrow) {
+                const int k = idx / SW;
+                r = k < top ? k : SH - bot + (k - top);
+                c = idx - k * SW;
+            } else {
+                const int k = idx - nrow, rr = k / (left + right), cc = k - rr * (left + right);
+                r = top + rr;
+                c = cc < left ? cc : SW - right + (cc - left);
+            }
             const int gy = Y0 - HY + r, gx = X0 - HX + c;
-            if ((unsigned)gy < (unsigned)h && (unsigned)gx < (unsigned)w) continue;
             sbox[r][c + CX] = __ldg(lv + (size_t)tint_clamp(gy, h) * lp + tint_clamp(gx, w));
         }
         __syncthreads();
@@ -469,6 +489,11 @@ k_detect(const FrameDev* __restrict__ frames, const TileItem* __restrict__ tiles
             ix1[k] = min(max(c1, 0), SW - 1);
         }
     }
+    // the column taps of an interior column sit at -2, -1 | d, d + 1 | 1, 2
+    // around the pixel (d = dcx = -1 or 0): no edge clamp (warp-uniform flag)
+    const int cc = tx + HX, dcx = ix0[1] - cc;
+    const bool colfast = __all_sync(__activemask(), ix0[0] == cc - 2 && ix1[0] == cc - 1 && (dcx == -1 || dcx == 0) &&
+                                                        ix1[1] == ix0[1] + 1 && ix0[2] == cc + 1 && ix1[2] == cc + 2);
     const uint32_t* mask = F.mask[l];
     uint8_t* const kpmap = F.kpmap[l];
     float* const blur = F.blur[l];
@@ -536,52 +561,77 @@ k_detect(const FrameDev* __restrict__ frames, const TileItem* __restrict__ tiles
         // i-minor from 0.  The products of two taps run as packed pairs
         // ((i, 0) with (i, 1), and (0, 2) with (1, 2)); every lane is the scalar
         // product, and the sums are scalar in the written order.
-        const float* row0[3];
-        const float* row1[3];
+        // texel(i, j, e, f): T of tap (i, j), e = row 0 / 1, f = column 0 / 1.
+        const auto blur_value = [&](auto texel) -> float {
+            float q[3][3];
+            {
+                const float2 b01 = s_b01[ty], nb01 = s_nb01[ty];
 #pragma unroll
-        for (int j = 0; j < 3; ++j) {
-            row0[j] = sm[s_by0[j][ty]];
-            row1[j] = sm[s_by1[j][ty]];
-        }
-        float q[3][3];
-        {
-            const float2 b01 = s_b01[ty], nb01 = s_nb01[ty];
-#pragma unroll
-            for (int i = 0; i < 3; ++i) {
-                const float2 t00 = make_float2(row0[0][ix0[i]], row0[1][ix0[i]]);
-                const float2 t10 = make_float2(row0[0][ix1[i]], row0[1][ix1[i]]);
-                const float2 t01 = make_float2(row1[0][ix0[i]], row1[1][ix0[i]]);
-                const float2 t11 = make_float2(row1[0][ix1[i]], row1[1][ix1[i]]);
-                const float2 sv = sum4(mul2_rn(mul2_rn(pna[i], nb01), t00), mul2_rn(mul2_rn(pa[i], nb01), t10),
-                                       mul2_rn(mul2_rn(pna[i], b01), t01), mul2_rn(mul2_rn(pa[i], b01), t11));
-                const float2 qq = mul2_rn(mul2_rn(sv, wt_same[i]), wt01);
-                q[0][i] = qq.x;
-                q[1][i] = qq.y;
+                for (int i = 0; i < 3; ++i) {
+                    const float2 t00 = make_float2(texel(i, 0, 0, 0), texel(i, 1, 0, 0));
+                    const float2 t10 = make_float2(texel(i, 0, 0, 1), texel(i, 1, 0, 1));
+                    const float2 t01 = make_float2(texel(i, 0, 1, 0), texel(i, 1, 1, 0));
+                    const float2 t11 = make_float2(texel(i, 0, 1, 1), texel(i, 1, 1, 1));
+                    const float2 sv = sum4(mul2_rn(mul2_rn(pna[i], nb01), t00), mul2_rn(mul2_rn(pa[i], nb01), t10),
+                                           mul2_rn(mul2_rn(pna[i], b01), t01), mul2_rn(mul2_rn(pa[i], b01), t11));
+                    const float2 qq = mul2_rn(mul2_rn(sv, wt_same[i]), wt01);
+                    q[0][i] = qq.x;
+                    q[1][i] = qq.y;
+                }
             }
-        }
-        {
-            const float2 b22 = s_b22[ty], nb22 = s_nb22[ty];
-            const float2 t00 = make_float2(row0[2][ix0[0]], row0[2][ix0[1]]);
-            const float2 t10 = make_float2(row0[2][ix1[0]], row0[2][ix1[1]]);
-            const float2 t01 = make_float2(row1[2][ix0[0]], row1[2][ix0[1]]);
-            const float2 t11 = make_float2(row1[2][ix1[0]], row1[2][ix1[1]]);
-            const float2 sv = sum4(mul2_rn(mul2_rn(pna01, nb22), t00), mul2_rn(mul2_rn(pa01, nb22), t10),
-                                   mul2_rn(mul2_rn(pna01, b22), t01), mul2_rn(mul2_rn(pa01, b22), t11));
-            const float2 qq = mul2_rn(mul2_rn(sv, wt01), wt_same[2]);
-            q[2][0] = qq.x;
-            q[2][1] = qq.y;
-            const float a = ax[2], na = pna[2].x, b = b22.x, nb = nb22.x;
-            float s2 = (na * nb) * row0[2][ix0[2]];
-            s2 = s2 + (a * nb) * row0[2][ix1[2]];
-            s2 = s2 + (na * b) * row1[2][ix0[2]];
-            s2 = s2 + (a * b) * row1[2][ix1[2]];
-            q[2][2] = (s2 * 0.3125f) * 0.3125f;
-        }
-        float sum = 0.0f;
+            {
+                const float2 b22 = s_b22[ty], nb22 = s_nb22[ty];
+                const float2 t00 = make_float2(texel(0, 2, 0, 0), texel(1, 2, 0, 0));
+                const float2 t10 = make_float2(texel(0, 2, 0, 1), texel(1, 2, 0, 1));
+                const float2 t01 = make_float2(texel(0, 2, 1, 0), texel(1, 2, 1, 0));
+                const float2 t11 = make_float2(texel(0, 2, 1, 1), texel(1, 2, 1, 1));
+                const float2 sv = sum4(mul2_rn(mul2_rn(pna01, nb22), t00), mul2_rn(mul2_rn(pa01, nb22), t10),
+                                       mul2_rn(mul2_rn(pna01, b22), t01), mul2_rn(mul2_rn(pa01, b22), t11));
+                const float2 qq = mul2_rn(mul2_rn(sv, wt01), wt_same[2]);
+                q[2][0] = qq.x;
+                q[2][1] = qq.y;
+                const float a = ax[2], na = pna[2].x, b = b22.x, nb = nb22.x;
+                float s2 = (na * nb) * texel(2, 2, 0, 0);
+                s2 = s2 + (a * nb) * texel(2, 2, 0, 1);
+                s2 = s2 + (na * b) * texel(2, 2, 1, 0);
+                s2 = s2 + (a * b) * texel(2, 2, 1, 1);
+                q[2][2] = (s2 * 0.3125f) * 0.3125f;
+            }
+            float sum = 0.0f;
 #pragma unroll
-        for (int j = 0; j < 3; ++j)
+            for (int j = 0; j < 3; ++j)
 #pragma unroll
-            for (int i = 0; i < 3; ++i) sum = sum + q[j][i];
+                for (int i = 0; i < 3; ++i) sum = sum + q[j][i];
+            return sum;
+        };
+        float sum;
+        if (colfast && s_rowfast[ty]) {
+            // interior: the taps sit at rows / columns -2, -1 | d, d + 1 | 1, 2
+            // around the pixel (d = -1 or 0, per column dcx, per row dry), so
+            // every load is one of four base pointers plus a constant
+            const float* P = &sm[r][c];
+            const int dry = s_by0[1][ty] - r;
+            const float* Px = P + dcx;
+            const float* Py = P + dry * BW;
+            const float* Pxy = Py + dcx;
+            sum = blur_value([&](int i, int j, int e, int f) -> float {
+                const float* base = i == 1 ? (j == 1 ? Pxy : Px) : (j == 1 ? Py : P);
+                const int ro = (j == 0 ? -2 : (j == 1 ? 0 : 1)) + e;
+                const int co = (i == 0 ? -2 : (i == 1 ? 0 : 1)) + f;
+                return base[ro * BW + co];
+            });
+        } else {
+            const float* row0[3];
+            const float* row1[3];
+#pragma unroll
+            for (int j = 0; j < 3; ++j) {
+                row0[j] = sm[s_by0[j][ty]];
+                row1[j] = sm[s_by1[j][ty]];
+            }
+            sum = blur_value([&](int i, int j, int e, int f) -> float {
+                return (e ? row1[j] : row0[j])[f ? ix1[i] : ix0[i]];
+            });
+        }
         blur[(size_t)y * bl_pitch + x] = sum;
     }
 }

@@ -298,8 +298,14 @@ void free_batch(uslam_batch* b) {
     delete b;
 }
 
+// per_frame_form: the batch serves the one-frame forms (the frontend, feature
+// sets and their matches), where the windowed matcher takes its distances
+// from the tensor cores: for one pair k_match leaves most of the GPU idle and
+// its latency is that of its slowest query group (measured: the one-frame
+// form ran 4,109 frames/s with k_match, 5,497 with k_win_mma).
 uslam_status create_batch(uslam_ctx* ctx, int n_frames, const int* widths, const int* heights, int n_pairs,
-                          const int* pair_prev, const int* pair_curr, bool per_item_programs, uslam_batch** out) {
+                          const int* pair_prev, const int* pair_curr, bool per_item_programs, uslam_batch** out,
+                          bool per_frame_form = false) {
     if (!ctx || !out || n_frames <= 0 || !widths || !heights || n_pairs < 0 || (n_pairs > 0 && (!pair_prev || !pair_curr)))
         return set_err(ctx ? &ctx->err : nullptr, USLAM_INVALID_ARG, "batch_create: bad arguments");
     if (n_frames > 65535) return set_err(&ctx->err, USLAM_INVALID_ARG, "batch_create: more than 65535 frames");
@@ -324,14 +330,15 @@ uslam_status create_batch(uslam_ctx* ctx, int n_frames, const int* widths, const
             xorder[USLAM_MAX_LEVELS], colstart[USLAM_MAX_LEVELS], qorder[USLAM_MAX_LEVELS], bands[USLAM_MAX_LEVELS], counts,
             tmaps, bf8, bfext, bfpop, bfid, wq8, wc8, wcext, wcy, wcid, winv[USLAM_MAX_LEVELS];
     };
-    // the windowed tensor-core matcher (asked for as matcher 3): every list
-    // position and candidate row within 16 bits, else k_match
+    // the windowed tensor-core matcher (matcher 3, or matcher 0 in the
+    // one-frame forms): every list position and candidate row within 16 bits,
+    // else k_match
     int max_cap = 1;
     for (int f = 0; f < n_frames; ++f) {
         const long long c = ctx->cap_override > 0 ? ctx->cap_override : static_cast<long long>(widths[f]) * heights[f] / 250;
         max_cap = static_cast<int>(std::max<long long>(max_cap, c));
     }
-    b->win_tc = ctx->win_tc && max_cap <= kWinMaxCap && ctx->max_h < 65535;
+    b->win_tc = (ctx->win_tc || (ctx->matcher == 0 && per_frame_form)) && max_cap <= kWinMaxCap && ctx->max_h < 65535;
     b->win_umax = b->win_tc ? win_units_per_seg(max_cap) : 0;
     std::vector<FrameLayout> fl(n_frames);
     for (int f = 0; f < n_frames; ++f) {
@@ -1293,7 +1300,7 @@ uslam_status uslam_frontend_create(uslam_ctx* ctx, int width, int height, uslam_
     const int ws[2] = {width, width}, hs[2] = {height, height};
     const int prev[2] = {1, 0}, curr[2] = {0, 1};  // pair 0: slot1 -> slot0, pair 1: slot0 -> slot1
     uslam_batch* b = nullptr;
-    uslam_status s = create_batch(ctx, 2, ws, hs, 2, prev, curr, true, &b);
+    uslam_status s = create_batch(ctx, 2, ws, hs, 2, prev, curr, true, &b, true);
     if (s != USLAM_OK) return s;
     auto* fe = new uslam_frontend();
     fe->b = b;
@@ -1449,7 +1456,7 @@ extern "C" {
 uslam_status uslam_featset_create(uslam_ctx* ctx, int width, int height, uslam_featset** out) {
     if (!ctx || !out) return USLAM_INVALID_ARG;
     uslam_batch* b = nullptr;
-    uslam_status s = create_batch(ctx, 1, &width, &height, 0, nullptr, nullptr, false, &b);
+    uslam_status s = create_batch(ctx, 1, &width, &height, 0, nullptr, nullptr, false, &b, true);
     if (s != USLAM_OK) return s;
     auto* fs = new uslam_featset();
     fs->ctx = ctx;
@@ -1524,7 +1531,7 @@ uslam_status uslam_match_sets(uslam_ctx* ctx, const uslam_featset* prev, const u
         const int ws[2] = {prev->W, prev->W}, hs[2] = {prev->H, prev->H};
         const int pp = 0, pc = 1;
         uslam_batch* mb = nullptr;
-        uslam_status s = create_batch(ctx, 2, ws, hs, 1, &pp, &pc, true, &mb);
+        uslam_status s = create_batch(ctx, 2, ws, hs, 1, &pp, &pc, true, &mb, true);
         if (s != USLAM_OK) return s;
         it = ctx->match_batches.emplace(key, mb).first;
     }
