@@ -217,6 +217,32 @@ def test_widest_tallest_frames_and_most_levels(brief_pattern):
             b.close()
 
 
+def test_tiled_describe_edge_frames(brief_pattern):
+    """Batches of 8 frames or more describe over blur-cache boxes staged in
+    shared memory (k_describe_tiled).  The edge cases in one such batch: the
+    widest and tallest frames (8192 x 96, 96 x 8192, 12 levels: 64 column
+    chunks, 256 bands), tiny and odd frames whose boxes reach past every
+    edge (tests at negative coordinates read the sentinels), and a constant
+    frame; all bit-exact against the oracle."""
+    with Context(brief_pattern, levels=12, max_width=8192, max_height=8192) as c:
+        frames = list(synth.warped_pair(21, 8192, 96)) + list(synth.warped_pair(22, 96, 8192))
+        frames += [synth.scene_frame(9, 10, 10), synth.scene_frame(11, 37, 23), synth.scene_frame(12, 61, 45),
+                   np.full((48, 64), 77, np.uint8)]
+        assert len(frames) >= 8
+        b = _run(c, frames, [(0, 1), (2, 3)])
+        try:
+            exp = [oracle.frame(f, brief_pattern, levels=12) for f in frames]
+            for i in range(len(frames)):
+                _assert_features_equal(b.features(i), exp[i])
+            for k, (w, h) in enumerate([(8192, 96), (96, 8192)]):
+                em = oracle.match(exp[2 * k][0], exp[2 * k][1], exp[2 * k + 1][0], exp[2 * k + 1][1], w, h)
+                assert len(em) > 0
+                assert np.array_equal(_mm(b.matches(k)), em), f"pair {k} {w}x{h}"
+            assert sum(int(e[1].sum()) for e in exp[4:7]) > 0
+        finally:
+            b.close()
+
+
 def test_cap_keeps_first_in_yx_order(brief_pattern):
     f1, _ = synth.warped_pair(4)
     with Context(brief_pattern, levels=6, max_width=752, max_height=480, cap_per_level=100) as c:

@@ -385,7 +385,7 @@ k_detect(const FrameDev* __restrict__ frames, const TileItem* __restrict__ tiles
     //    replaced below.
     if (t == 0) {
         const void* tmap = static_cast<const char*>(F.tmaps) +
-                           (size_t)(l * USLAM_NUM_TILE_SHAPES + shape) * USLAM_TMAP_BYTES;
+                           (size_t)(l * USLAM_TMAPS_PER_LEVEL + shape) * USLAM_TMAP_BYTES;
         mbar_init(&s_bar, 1u);
         mbar_expect_tx(&s_bar, (uint32_t)(SH * BW * 4));
         tma_load_2d(&sbox[0][0], tmap, X0 - USLAM_TILE_XPAD, Y0 - HY, &s_bar);
@@ -1052,7 +1052,7 @@ __device__ __forceinline__ int find_segment(const uint32_t* s_pref, int nseg, ui
 // (columns w .. w + M) and runs of 32 columns of the bottom margin (rows
 // h .. h + M, all columns including the corner and the sentinel column).
 __device__ __forceinline__ uint32_t border_units(const FrameDev& F, int l) {
-    return (uint32_t)((F.h[l] + 31) / 32 + (F.bl_pitch[l] + 31) / 32);
+    return (uint32_t)((F.h[l] + 31) / 32 + (F.w[l] + F.margin + 1 + 31) / 32);
 }
 
 // The blur cache beyond the level edges: G(P) of generate_features.wgsl:149-172
@@ -1091,7 +1091,7 @@ k_blur_border(const FrameDev* __restrict__ frames, const SegDev* __restrict__ se
             ey1 = min(h, ey0 + 32);
         } else {
             ex = (unit - nr) * 32 + lane;
-            active = ex < bp;
+            active = ex <= w + M;
             ey0 = h;
             ey1 = h + M + 1;
         }
@@ -1204,6 +1204,91 @@ __device__ __forceinline__ uint32_t win_query_row(const uint32_t* qband, int l, 
     return off + (k - qband[b]);
 }
 
+// Finish one keypoint's record (the warp holds its 8 descriptor words, lane
+// k the word k of every lane): orientation and descriptor into the record
+// (generate_features.wgsl:170-172), plus the tensor-core operand rows (PACK,
+// WIN) of the matchers that take them.
+template <bool PACK, bool WIN>
+__device__ __forceinline__ void emit_feature(const FrameDev& F, int l, uint32_t i, int w, int y, float theta,
+                                             const uint32_t (&words)[8], int lane) {
+    uint32_t* rec = F.feats[l] + (size_t)i * 12u;
+    uint32_t out = __float_as_uint(theta);
+#pragma unroll
+    for (int k = 0; k < 8; ++k)
+        if (lane == 4 + k) out = words[k];
+    if (lane >= 3 && lane < 12) rec[lane] = out;
+    if constexpr (WIN) {
+        uint32_t wj = words[0];
+        uint32_t pc = 0;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            if ((lane >> 2) == k) wj = words[k];
+            pc += (uint32_t)__popc(words[k]);
+        }
+        const uint32_t* inv = F.winv[l];
+        const size_t cap = (size_t)(F.cap > 0 ? F.cap : 1);
+        const uint32_t* qband = F.colstart[l] + (size_t)USLAM_MATCH_BANDS * (size_t)(w + 1);
+        write_fp8_row(F.wq8, win_query_row(qband, l, F.wq_rows, __ldg(inv + i)), wj, lane);
+#pragma unroll
+        for (int b = 0; b < USLAM_MATCH_BANDS; ++b) {
+            const uint32_t pos = __ldg(inv + cap * (size_t)(1 + b) + i);
+            if (pos == 0xffffffffu) continue;
+            const uint32_t R = (uint32_t)(USLAM_MATCH_BANDS * l + b) * (uint32_t)F.wc_rows + pos;
+            write_fp8_row(F.wc8, R, wj, lane);
+            if (lane < 4) write_ext_row(F.wcext, R, pc, (int)(pos & 31u), lane);
+            else if (lane == 4) F.wcy[R] = (uint16_t)y;
+            else if (lane == 5) F.wcid[R] = USLAM_PACK(l, i);
+        }
+    }
+    if constexpr (PACK) {
+        // tensor-core operand rows of this feature (flat index f over
+        // the levels): lane j writes the FP8 values of descriptor bits
+        // 8j .. 8j + 7 (8.0 or 0; K chunk j / 2, half j % 2); lanes 0-3
+        // write the 32-value extension row: the popcount split into 16
+        // integers <= 16, then 256, the row's index within its 32-row
+        // group split into two integers <= 16, then 1, then zeros
+        uint32_t f = i;
+        for (int q = 0; q < l; ++q) f += F.kept[q];
+        uint32_t wj = words[0];
+        uint32_t pc = 0;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            if ((lane >> 2) == k) wj = words[k];
+            pc += (uint32_t)__popc(words[k]);
+        }
+        const uint32_t bits = (wj >> (8 * (lane & 3))) & 0xffu;
+        uint32_t lo = 0u, hi = 0u;
+#pragma unroll
+        for (int b = 0; b < 4; ++b) {
+            lo |= ((bits >> b) & 1u) * (0x50u << (8 * b));
+            hi |= ((bits >> (b + 4)) & 1u) * (0x50u << (8 * b));
+        }
+        *reinterpret_cast<uint2*>(F.bf8 + (size_t)(f >> 3) * 2048u + (lane >> 1) * 128u + (f & 7u) * 16u +
+                                  (lane & 1) * 8u) = make_uint2(lo, hi);
+        if (lane < 4) {
+            uint32_t ext[2] = {0u, 0u};
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+                const int e = 8 * lane + k;  // extension value index 0..31
+                const int grp = (int)(f & 31u);
+                uint32_t code = 0u;
+                if (e < 16) code = e4m3_small_int(min(16, max(0, (int)pc - 16 * e)));
+                else if (e == 16) code = 0x78u;  // 256
+                else if (e == 17) code = e4m3_small_int(min(grp, 16));
+                else if (e == 18) code = e4m3_small_int(max(grp - 16, 0));
+                else if (e == 19) code = 0x38u;  // 1
+                ext[k >> 2] |= code << (8 * (k & 3));
+            }
+            *reinterpret_cast<uint2*>(F.bfext + (size_t)(f >> 3) * 256u + (lane >> 1) * 128u + (f & 7u) * 16u +
+                                      (lane & 1) * 8u) = make_uint2(ext[0], ext[1]);
+        }
+        if (lane == 0) {
+            F.bfpop[f] = pc;
+            F.bfid[f] = USLAM_PACK(l, i);
+        }
+    }
+}
+
 // PACK: also write the brute-force tensor-core matcher's operand rows of
 // every feature (FrameDev::bf8 / bfext / bfpop / bfid).  WIN: the windowed
 // tensor-core matcher's rows: the feature's query row (wq8) and its row in
@@ -1310,83 +1395,188 @@ k_describe(const FrameDev* __restrict__ frames, const SegDev* __restrict__ segs,
             uint32_t words[8];
 #pragma unroll
             for (int k = 0; k < 8; ++k) words[k] = __ballot_sync(0xffffffffu, ga[k] > gb[k]);
-            uint32_t out = __float_as_uint(theta);
-#pragma unroll
-            for (int k = 0; k < 8; ++k)
-                if (lane == 4 + k) out = words[k];
-            if (lane >= 3 && lane < 12) rec[lane] = out;
-            if constexpr (WIN) {
-                uint32_t wj = words[0];
-                uint32_t pc = 0;
-#pragma unroll
-                for (int k = 0; k < 8; ++k) {
-                    if ((lane >> 2) == k) wj = words[k];
-                    pc += (uint32_t)__popc(words[k]);
-                }
-                const uint32_t* inv = F.winv[l];
-                const size_t cap = (size_t)(F.cap > 0 ? F.cap : 1);
-                const uint32_t* qband = F.colstart[l] + (size_t)USLAM_MATCH_BANDS * (size_t)(w + 1);
-                write_fp8_row(F.wq8, win_query_row(qband, l, F.wq_rows, __ldg(inv + i)), wj, lane);
-#pragma unroll
-                for (int b = 0; b < USLAM_MATCH_BANDS; ++b) {
-                    const uint32_t pos = __ldg(inv + cap * (size_t)(1 + b) + i);
-                    if (pos == 0xffffffffu) continue;
-                    const uint32_t R = (uint32_t)(USLAM_MATCH_BANDS * l + b) * (uint32_t)F.wc_rows + pos;
-                    write_fp8_row(F.wc8, R, wj, lane);
-                    if (lane < 4) write_ext_row(F.wcext, R, pc, (int)(pos & 31u), lane);
-                    else if (lane == 4) F.wcy[R] = (uint16_t)y;
-                    else if (lane == 5) F.wcid[R] = USLAM_PACK(l, i);
-                }
-            }
-            if constexpr (PACK) {
-                // tensor-core operand rows of this feature (flat index f over
-                // the levels): lane j writes the FP8 values of descriptor bits
-                // 8j .. 8j + 7 (8.0 or 0; K chunk j / 2, half j % 2); lanes 0-3
-                // write the 32-value extension row: the popcount split into 16
-                // integers <= 16, then 256, the row's index within its 32-row
-                // group split into two integers <= 16, then 1, then zeros
-                uint32_t f = i;
-                for (int q = 0; q < l; ++q) f += F.kept[q];
-                uint32_t wj = words[0];
-                uint32_t pc = 0;
-#pragma unroll
-                for (int k = 0; k < 8; ++k) {
-                    if ((lane >> 2) == k) wj = words[k];
-                    pc += (uint32_t)__popc(words[k]);
-                }
-                const uint32_t bits = (wj >> (8 * (lane & 3))) & 0xffu;
-                uint32_t lo = 0u, hi = 0u;
-#pragma unroll
-                for (int b = 0; b < 4; ++b) {
-                    lo |= ((bits >> b) & 1u) * (0x50u << (8 * b));
-                    hi |= ((bits >> (b + 4)) & 1u) * (0x50u << (8 * b));
-                }
-                *reinterpret_cast<uint2*>(F.bf8 + (size_t)(f >> 3) * 2048u + (lane >> 1) * 128u + (f & 7u) * 16u +
-                                          (lane & 1) * 8u) = make_uint2(lo, hi);
-                if (lane < 4) {
-                    uint32_t ext[2] = {0u, 0u};
-#pragma unroll
-                    for (int k = 0; k < 8; ++k) {
-                        const int e = 8 * lane + k;  // extension value index 0..31
-                        const int grp = (int)(f & 31u);
-                        uint32_t code = 0u;
-                        if (e < 16) code = e4m3_small_int(min(16, max(0, (int)pc - 16 * e)));
-                        else if (e == 16) code = 0x78u;  // 256
-                        else if (e == 17) code = e4m3_small_int(min(grp, 16));
-                        else if (e == 18) code = e4m3_small_int(max(grp - 16, 0));
-                        else if (e == 19) code = 0x38u;  // 1
-                        ext[k >> 2] |= code << (8 * (k & 3));
-                    }
-                    *reinterpret_cast<uint2*>(F.bfext + (size_t)(f >> 3) * 256u + (lane >> 1) * 128u + (f & 7u) * 16u +
-                                              (lane & 1) * 8u) = make_uint2(ext[0], ext[1]);
-                }
-                if (lane == 0) {
-                    F.bfpop[f] = pc;
-                    F.bfid[f] = USLAM_PACK(l, i);
-                }
-            }
+            emit_feature<PACK, WIN>(F, l, i, w, y, theta, words, lane);
         }
     }
+}
+
+// --------------------------------------------- K2 over staged tiles ----
+// The same orientation and descriptor as k_describe, with the blur-cache
+// samples read from shared memory: one CTA per item = (frame, level, 32-row
+// band, chunk of KDT_CW columns).  One 2D TMA load stages the box of the
+// blur cache that every test of the item's keypoints can reach (rows
+// y0 - R .. y0 + 31 + R, columns x0 - RX .. x0 + KDT_CW - 1 + RX, R = margin
+// - 1 >= the largest rotated test offset, RX = R rounded up to 4 so the box
+// starts on a 16-byte boundary); cells at negative coordinates get the
+// sentinel values the gather path reads for them.  The item's keypoints are
+// those of the band's list range (the band order of the compaction) with x
+// in the chunk, taken in rounds of up to KDT_THREADS.
+constexpr int KDT_THREADS = 256;
+constexpr int KDT_WARPS = KDT_THREADS / 32;
+
+template <bool PACK, bool WIN>
+__global__ void __launch_bounds__(KDT_THREADS)
+k_describe_tiled(const FrameDev* __restrict__ frames, const BandItem* __restrict__ items,
+                 const int32_t* __restrict__ pattern, uint32_t* err) {
+    extern __shared__ __align__(128) float s_box[];  // [BH][BW] blur-cache box
+    __shared__ float4 s_pat[256];
+    __shared__ float s_lut[256];
+    __shared__ uint32_t s_list[KDT_THREADS];
+    __shared__ uint32_t s_wcount[KDT_WARPS];
+    __shared__ uint32_t s_pos[2];
+    __shared__ __align__(8) uint64_t s_bar;
+    constexpr int8_t kdx[29] = {0, -2, -1, 0, 1, 2, -2, -1, 0, 1, 2, -3, -2, -1, 0, 1, 2, 3, -2, -1, 0, 1, 2, -2, -1, 0, 1, 2, 0};
+    constexpr int8_t kdy[29] = {-3, -2, -2, -2, -2, -2, -1, -1, -1, -1, -1, 0, 0, 0, 0, 0, 0, 0, 1, 1, 1, 1, 1, 2, 2, 2, 2, 2, 3};
+    const BandItem it = items[blockIdx.x];
+    const FrameDev& F = frames[it.frame];
+    const int l = it.level, band = it.band;
+    const int w = F.w[l], h = F.h[l], M = F.margin;
+    const int R = M - 1, RX = (R + 3) & ~3;
+    const int BW = KDT_CW + 2 * RX, BH = 32 + 2 * R;
+    const int x0 = (int)it.pad2 * KDT_CW, y0 = band * 32;
+    const int xs = x0 - RX, ys = y0 - R;
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    if (t == 0) {
+        const void* tmap = static_cast<const char*>(F.tmaps) +
+                           (size_t)(l * USLAM_TMAPS_PER_LEVEL + USLAM_NUM_TILE_SHAPES) * USLAM_TMAP_BYTES;
+        mbar_init(&s_bar, 1u);
+        mbar_expect_tx(&s_bar, (uint32_t)(BW * BH * 4));
+        tma_load_2d(s_box, tmap, xs, ys, &s_bar);
+    }
+    for (int i = t; i < 256; i += KDT_THREADS) {
+        s_pat[i] = make_float4((float)pattern[4 * i], (float)pattern[4 * i + 1], (float)pattern[4 * i + 2],
+                               (float)pattern[4 * i + 3]);
+        s_lut[i] = (float)i / 255.0f;
+    }
+    // the band's range of the level's list: after the kept counts of the
+    // earlier bands, clipped by the level's kept count (the cap)
+    if (warp == 0) {
+        uint32_t pk = 0;
+        for (int q = lane; q < band; q += 32) pk += F.bands[l][2 * q + 1];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) pk += __shfl_xor_sync(0xffffffffu, pk, o);
+        if (lane == 0) {
+            const uint32_t kept = F.kept[l];
+            const uint32_t b0 = min(pk, kept);
+            s_pos[0] = b0;
+            s_pos[1] = min(pk + F.bands[l][2 * band + 1], kept);
+        }
+    }
+    __syncthreads();  // barrier initialised, pattern, range
+    const bool landed = mbar_wait(&s_bar, 0u, kTmaWaitLimit);
+    if (__syncthreads_or(!landed)) {
+        if (t == 0) atomicOr(err, USLAM_ERR_TMA_TIMEOUT);
+        mbar_wait(&s_bar, 0u, kTmaWaitLimit);  // the copy in flight lands before the box is left
+        return;
+    }
+    // cells at negative coordinates: the sentinel column (x = w + M) / row
+    // (y = h + M) that every negative coordinate reads
+    if (xs < 0 || ys < 0) {
+        const float* blur = F.blur[l];
+        const int bp = F.bl_pitch[l];
+        const int nx = max(-xs, 0), ny = max(-ys, 0);
+        const int n = ny * BW + (BH - ny) * nx;
+        for (int k = t; k < n; k += KDT_THREADS) {
+            int r, c;
+            if (k < ny * BW) {
+                r = k / BW;
+                c = k - r * BW;
+            } else {
+                const int q = k - ny * BW;
+                r = ny + q / nx;
+                c = q - (q / nx) * nx;
+            }
+            const int gy = ys + r, gx = xs + c;
+            if (gy > h + M || gx > w + M) continue;  // past the cache: never read by a test
+            s_box[r * BW + c] = blur[(size_t)(gy < 0 ? h + M : gy) * bp + (gx < 0 ? w + M : gx)];
+        }
+        __syncthreads();
+    }
+    const uint32_t pos0 = s_pos[0], pos1 = s_pos[1];
+    const uint32_t* feats = F.feats[l];
+    for (uint32_t base = pos0; base < pos1; base += KDT_THREADS) {
+        // this round's keypoints with x in the chunk, in list order
+        const uint32_t i = base + (uint32_t)t;
+        bool sel = false;
+        if (i < pos1) {
+            const int x = (int)__uint_as_float(__ldg(feats + (size_t)i * 12u));
+            sel = x >= x0 && x < x0 + KDT_CW;
+        }
+        const uint32_t bal = __ballot_sync(0xffffffffu, sel);
+        if (lane == 0) s_wcount[warp] = (uint32_t)__popc(bal);
+        __syncthreads();
+        uint32_t off = 0, nsel = 0;
+        for (int q = 0; q < KDT_WARPS; ++q) {
+            off += q < warp ? s_wcount[q] : 0u;
+            nsel += s_wcount[q];
+        }
+        if (sel) s_list[off + (uint32_t)__popc(bal & ((1u << lane) - 1u))] = i;
+        __syncthreads();
+        // warp q takes G consecutive keypoints of the list (G <= 32); lane j
+        // first computes the orientation of keypoint j
+        const uint32_t G = (nsel + KDT_WARPS - 1) / KDT_WARPS;
+        const uint32_t g0 = (uint32_t)warp * G;
+        const int nk = (int)min(G, nsel > g0 ? nsel - g0 : 0u);
+        float my_theta = 0.0f, my_s = 0.0f, my_c = 0.0f;
+        if (lane < nk) {
+            // orientation (generate_features.wgsl:80-99): intensity moments over
+            // the r = 3 disc, summed in the reference's order, then atan2
+            const uint32_t* rec = feats + (size_t)s_list[g0 + lane] * 12u;
+            const int x = (int)__uint_as_float(rec[0]);
+            const int y = (int)__uint_as_float(rec[1]);
+            const float* lvl = F.lvl[l];
+            const int lp = F.lvl_pitch[l];
+            float m10 = 0.0f, m01 = 0.0f;
+#pragma unroll
+            for (int k = 0; k < 29; ++k) {
+                const int cx = tint_clamp(x + kdx[k], w);
+                const int cy = tint_clamp(y + kdy[k], h);
+                const float v = l == 0 ? s_lut[__ldg(F.img + (size_t)cy * F.img_pitch + cx)]
+                                       : __ldg(lvl + (size_t)cy * (size_t)lp + cx);
+                m10 = m10 + (float)kdx[k] * v;
+                m01 = m01 + (float)kdy[k] * v;
+            }
+            my_theta = uslam_atan2f(m01, m10);
+            uslam_sincosf(my_theta, &my_s, &my_c);
+        }
+        for (int kp = 0; kp < nk; ++kp) {
+            const uint32_t i2 = s_list[g0 + kp];
+            const float theta = __shfl_sync(0xffffffffu, my_theta, kp);
+            const float sn = __shfl_sync(0xffffffffu, my_s, kp);
+            const float cs = __shfl_sync(0xffffffffu, my_c, kp);
+            const uint32_t* rec = feats + (size_t)i2 * 12u;
+            const int x = (int)__uint_as_float(rec[0]);
+            const int y = (int)__uint_as_float(rec[1]);
+            // 256 tests, lane j owns tests j, j + 32, ..., j + 224: 16 reads of
+            // the staged box at (y + dy - ys, x + dx - xs)
+            const float* org = s_box + (y - ys) * BW + (x - xs);
+            float ga[8], gb[8];
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+                const float4 tp = s_pat[lane + 32 * k];
+                const int xa = (int)rintf(tp.x * cs - tp.y * sn);
+                const int ya = (int)rintf(tp.x * sn + tp.y * cs);
+                const int xb = (int)rintf(tp.z * cs - tp.w * sn);
+                const int yb = (int)rintf(tp.z * sn + tp.w * cs);
+                ga[k] = org[ya * BW + xa];
+                gb[k] = org[yb * BW + xb];
+            }
+            uint32_t words[8];
+#pragma unroll
+            for (int k = 0; k < 8; ++k) words[k] = __ballot_sync(0xffffffffu, ga[k] > gb[k]);
+            emit_feature<PACK, WIN>(F, l, i2, w, y, theta, words, lane);
+        }
+        __syncthreads();  // s_list / s_wcount reused by the next round
+    }
+}
+
+// Dynamic shared memory of k_describe_tiled for a blur-cache margin M (0 if
+// the box would exceed a TMA box's 256 cells per dimension).
+size_t describe_tiled_smem(int margin) {
+    const int R = margin - 1, RX = (R + 3) & ~3;
+    const int BW = KDT_CW + 2 * RX, BH = 32 + 2 * R;
+    if (R < 0 || BW > 256 || BH > 256) return 0;
+    return (size_t)BW * (size_t)BH * 4u;
 }
 
 // ------------------------------------------------- Hamming distance ----
@@ -1907,6 +2097,26 @@ cudaError_t launch_describe(const FrameDev* frames, const SegDev* segs, int nseg
     else if (win) k_describe<false, true><<<grid, KD_THREADS, 0, st>>>(frames, segs, nseg, pattern);
     else k_describe<false, false><<<grid, KD_THREADS, 0, st>>>(frames, segs, nseg, pattern);
     return cudaGetLastError();
+}
+
+cudaError_t launch_describe_tiled(const FrameDev* frames, const BandItem* items, int nitems, const int32_t* pattern,
+                                  bool pack, bool win, int margin, uint32_t* err, cudaStream_t st) {
+    if (nitems <= 0) return cudaSuccess;
+    const size_t smem = describe_tiled_smem(margin);
+    if (pack) k_describe_tiled<true, false><<<nitems, KDT_THREADS, smem, st>>>(frames, items, pattern, err);
+    else if (win) k_describe_tiled<false, true><<<nitems, KDT_THREADS, smem, st>>>(frames, items, pattern, err);
+    else k_describe_tiled<false, false><<<nitems, KDT_THREADS, smem, st>>>(frames, items, pattern, err);
+    return cudaGetLastError();
+}
+
+cudaError_t set_describe_tiled_smem(int margin) {
+    const int smem = (int)describe_tiled_smem(margin);
+    cudaError_t e = cudaFuncSetAttribute(k_describe_tiled<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_describe_tiled<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_describe_tiled<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    return e;
 }
 
 cudaError_t launch_match(const FrameDev* frames, const PairDev* pairs, const void* segs, int nseg, int grid,

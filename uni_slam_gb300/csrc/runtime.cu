@@ -49,8 +49,9 @@ constexpr int kSplitFrames = 16;
 
 // Launch tables of one program (a subset of the batch's frames and pairs).
 struct Program {
-    int ntiles = 0, nfsegs = 0, nmsegs = 0, nusegs = 0, npsegs = 0, nbands = 0;
+    int ntiles = 0, nfsegs = 0, nmsegs = 0, nusegs = 0, npsegs = 0, nbands = 0, ndesc = 0;
     BandItem* bands = nullptr;  // compaction work items: one per 32-row band of every (frame, level)
+    BandItem* desc = nullptr;   // describe items: every KDT_CW-column chunk of every band
     int tile_begin[kNumTileShapes + 1] = {0};  // tiles grouped by shape
     TileItem* tiles = nullptr;
     SegDev* fsegs = nullptr;
@@ -109,7 +110,7 @@ uslam_status build_program(uslam_batch* b, const std::vector<int>& fr, const std
     ShapedTiles st;
     std::vector<SegDev> fsegs, usegs, psegs;
     std::vector<MatchSegDev> msegs;
-    std::vector<BandItem> bands;
+    std::vector<BandItem> bands, desc;
     for (int f : fr) {
         const FrameDev& F = b->frames[f];
         append_tiles(&st.by_shape[b->ctx->shape_for(F.W0, F.H0)], f, F, b->ctx->shape_for(F.W0, F.H0));
@@ -121,6 +122,10 @@ uslam_status build_program(uslam_batch* b, const std::vector<int>& fr, const std
                 bi.level = static_cast<uint8_t>(l);
                 bi.band = static_cast<uint16_t>(q);
                 bands.push_back(bi);
+                for (int c = 0; c < (F.w[l] + KDT_CW - 1) / KDT_CW; ++c) {
+                    bi.pad2 = static_cast<uint16_t>(c);
+                    desc.push_back(bi);
+                }
             }
         }
     }
@@ -143,13 +148,15 @@ uslam_status build_program(uslam_batch* b, const std::vector<int>& fr, const std
     P->nusegs = static_cast<int>(usegs.size());
     P->npsegs = static_cast<int>(psegs.size());
     P->nbands = static_cast<int>(bands.size());
+    P->ndesc = static_cast<int>(desc.size());
     const size_t t_bytes = round_up(tiles.size() * sizeof(TileItem), 256);
     const size_t f_bytes = round_up(fsegs.size() * sizeof(SegDev), 256);
     const size_t m_bytes = round_up(msegs.size() * sizeof(MatchSegDev), 256);
     const size_t u_bytes = round_up(usegs.size() * sizeof(SegDev), 256);
     const size_t p_bytes = round_up(psegs.size() * sizeof(SegDev), 256);
     const size_t b_bytes = round_up(bands.size() * sizeof(BandItem), 256);
-    P->host.assign(t_bytes + f_bytes + m_bytes + u_bytes + p_bytes + b_bytes, 0);
+    const size_t d_bytes = round_up(desc.size() * sizeof(BandItem), 256);
+    P->host.assign(t_bytes + f_bytes + m_bytes + u_bytes + p_bytes + b_bytes + d_bytes, 0);
     std::memcpy(P->host.data(), tiles.data(), tiles.size() * sizeof(TileItem));
     std::memcpy(P->host.data() + t_bytes, fsegs.data(), fsegs.size() * sizeof(SegDev));
     std::memcpy(P->host.data() + t_bytes + f_bytes, msegs.data(), msegs.size() * sizeof(MatchSegDev));
@@ -157,6 +164,8 @@ uslam_status build_program(uslam_batch* b, const std::vector<int>& fr, const std
     std::memcpy(P->host.data() + t_bytes + f_bytes + m_bytes + u_bytes, psegs.data(), psegs.size() * sizeof(SegDev));
     std::memcpy(P->host.data() + t_bytes + f_bytes + m_bytes + u_bytes + p_bytes, bands.data(),
                 bands.size() * sizeof(BandItem));
+    std::memcpy(P->host.data() + t_bytes + f_bytes + m_bytes + u_bytes + p_bytes + b_bytes, desc.data(),
+                desc.size() * sizeof(BandItem));
     // unit slots of the windowed tensor-core matcher: written on the device
     P->units_bytes = b->win_tc ? round_up(msegs.size() * static_cast<size_t>(b->win_umax) * win_unit_bytes(), 256) : 0;
     P->host.resize(P->host.size() + P->units_bytes, 0);
@@ -172,6 +181,19 @@ struct Lane {
 };
 
 Lane lane0(uslam_batch* b) { return Lane{b->stream, b->aux_stream, b->ev_fork, b->ev_join, b->d_err + 1}; }
+
+// Describe of a program: in batches of kTiledDescribeFrames frames or more,
+// k_describe_tiled over the describe items (the blur cache staged per chunk
+// by TMA) where the pattern's reach fits a TMA box; else the gather form
+// k_describe over (frame, level) segments, whose warps take fewer keypoints
+// each and so finish a few frames sooner.
+cudaError_t describe_stage(uslam_batch* b, const Program& P, cudaStream_t st) {
+    uslam_ctx* c = b->ctx;
+    if (static_cast<int>(b->frames.size()) >= kTiledDescribeFrames && describe_tiled_smem(c->margin) > 0)
+        return launch_describe_tiled(b->d_frames, P.desc, P.ndesc, c->d_pattern, c->matcher == 2, b->win_tc, c->margin,
+                                     b->d_err, st);
+    return launch_describe(b->d_frames, P.fsegs, P.nfsegs, c->d_pattern, c->num_sms * 4, c->matcher == 2, b->win_tc, st);
+}
 
 // The frame stages of a program: pyramid, detect, blur border, compaction, describe.
 cudaError_t enqueue_frames(uslam_batch* b, const Program& P, const Lane& ln) {
@@ -193,7 +215,7 @@ cudaError_t enqueue_frames(uslam_batch* b, const Program& P, const Lane& ln) {
         cudaSuccess)
         return e;
     if ((e = cudaStreamWaitEvent(ln.st, ln.join, 0)) != cudaSuccess) return e;
-    return launch_describe(b->d_frames, P.fsegs, P.nfsegs, c->d_pattern, grid, c->matcher == 2, b->win_tc, ln.st);
+    return describe_stage(b, P, ln.st);
 }
 
 // The pair stages of a program: match and the mutual check / emit.
@@ -382,7 +404,7 @@ uslam_status create_batch(uslam_ctx* ctx, int n_frames, const int* widths, const
             Ly.feats[l] = take(&out_bytes, capa * 48);
             F.lvl_pitch[l] = lvl_pitch_of(F.w[l]);
             Ly.lvl[l] = take(&scratch, static_cast<size_t>(F.h[l]) * F.lvl_pitch[l] * 4);
-            F.bl_pitch[l] = F.w[l] + ctx->margin + 1;
+            F.bl_pitch[l] = lvl_pitch_of(F.w[l] + ctx->margin + 1);  // 16-byte rows (TMA)
             Ly.blur[l] = take(&scratch, static_cast<size_t>(F.h[l] + ctx->margin + 1) * F.bl_pitch[l] * 4);
             Ly.kpmap[l] = take(&scratch, static_cast<size_t>(F.h[l]) * F.kp_pitch[l]);
             Ly.xorder[l] = take(&scratch, USLAM_MATCH_BANDS * capa * 4);
@@ -390,7 +412,7 @@ uslam_status create_batch(uslam_ctx* ctx, int n_frames, const int* widths, const
             Ly.qorder[l] = take(&scratch, capa * 4);
             Ly.bands[l] = take(&scratch, static_cast<size_t>((F.h[l] + 31) / 32) * 8);
         }
-        Ly.tmaps = take(&scratch, static_cast<size_t>(L) * kNumTileShapes * USLAM_TMAP_BYTES);
+        Ly.tmaps = take(&scratch, static_cast<size_t>(L) * USLAM_TMAPS_PER_LEVEL * USLAM_TMAP_BYTES);
         if (ctx->matcher == 2) {
             const size_t rows = tc_rows(F);
             Ly.bf8 = take(&scratch, rows * 256);
@@ -559,7 +581,7 @@ uslam_status create_batch(uslam_ctx* ctx, int n_frames, const int* widths, const
             F.wcid = reinterpret_cast<int32_t*>(sc_base + Ly.wcid);
             for (int l = 0; l < L; ++l) F.winv[l] = reinterpret_cast<uint32_t*>(sc_base + Ly.winv[l]);
         }
-        std::vector<char> maps(static_cast<size_t>(L) * kNumTileShapes * USLAM_TMAP_BYTES);
+        std::vector<char> maps(static_cast<size_t>(L) * USLAM_TMAPS_PER_LEVEL * USLAM_TMAP_BYTES);
         s = encode_tile_maps(F, ctx->detector, maps.data(), &ctx->err);
         if (s == USLAM_OK) {
             e = cudaMemcpy(sc_base + Ly.tmaps, maps.data(), maps.size(), cudaMemcpyHostToDevice);
@@ -589,6 +611,8 @@ uslam_status create_batch(uslam_ctx* ctx, int n_frames, const int* widths, const
         return ctx->cuda_fail(e, "frame table upload");
     }
     e = set_compact_smem(b->max_w);
+    if (e == cudaSuccess && n_frames >= kTiledDescribeFrames && describe_tiled_smem(ctx->margin) > 0)
+        e = set_describe_tiled_smem(ctx->margin);
     if (e == cudaSuccess && ctx->matcher == 2) e = set_bf_mma_smem();
     if (e == cudaSuccess && b->win_tc) e = set_win_mma_smem();
     if (e != cudaSuccess) {
@@ -673,6 +697,8 @@ uslam_status create_batch(uslam_ctx* ctx, int n_frames, const int* widths, const
         P->psegs = reinterpret_cast<SegDev*>(base + t_bytes + f_bytes + m_bytes + u_bytes);
         const size_t p_bytes = round_up(P->npsegs * sizeof(SegDev), 256);
         P->bands = reinterpret_cast<BandItem*>(base + t_bytes + f_bytes + m_bytes + u_bytes + p_bytes);
+        const size_t b_bytes = round_up(P->nbands * sizeof(BandItem), 256);
+        P->desc = reinterpret_cast<BandItem*>(base + t_bytes + f_bytes + m_bytes + u_bytes + p_bytes + b_bytes);
         P->units = P->units_bytes ? base + (P->host.size() - P->units_bytes) : nullptr;
         P->tiles = reinterpret_cast<TileItem*>(base);
         P->fsegs = reinterpret_cast<SegDev*>(base + t_bytes);
@@ -958,8 +984,10 @@ uslam_status uslam_batch_blur_level(uslam_batch* b, int frame, int level, float*
     if (!b || !out || frame < 0 || frame >= static_cast<int>(b->frames.size()) || level < 0 || level >= b->levels)
         return USLAM_INVALID_ARG;
     const FrameDev& F = b->frames[frame];
-    const size_t n = static_cast<size_t>(F.h[level] + F.margin + 1) * F.bl_pitch[level];
-    cudaError_t e = cudaMemcpy(out, F.blur[level], sizeof(float) * n, cudaMemcpyDeviceToHost);
+    const size_t cols = static_cast<size_t>(F.w[level] + F.margin + 1);
+    cudaError_t e = cudaMemcpy2D(out, sizeof(float) * cols, F.blur[level], sizeof(float) * F.bl_pitch[level],
+                                 sizeof(float) * cols, static_cast<size_t>(F.h[level] + F.margin + 1),
+                                 cudaMemcpyDeviceToHost);
     if (e != cudaSuccess) return b->ctx->cuda_fail(e, "blur readback");
     return USLAM_OK;
 }
@@ -1017,7 +1045,7 @@ uslam_status uslam_batch_profile(uslam_batch* b, int iters, float* kernel_ms) {
             e = launch_compact_banded(b->d_frames, P.bands, P.nbands, P.fsegs, P.nfsegs, b->max_w, b->stream);
         mark();
         if (e == cudaSuccess)
-            e = launch_describe(b->d_frames, P.fsegs, P.nfsegs, c->d_pattern, grid, c->matcher == 2, b->win_tc, b->stream);
+            e = describe_stage(b, P, b->stream);
         mark();
         if (e == cudaSuccess)
             e = c->matcher == 1 ? launch_bruteforce(b->d_frames, b->d_pairs, P.psegs, P.npsegs, c->ratio, grid, b->stream)
@@ -1582,8 +1610,8 @@ uslam_status encode_tile_maps(const FrameDev& F, int detector, void* out, ErrTex
     for (int l = 0; l < F.levels; ++l)
         for (int sh = 0; sh < kNumTileShapes; ++sh) {
             CUtensorMap* m =
-                reinterpret_cast<CUtensorMap*>(static_cast<char*>(out) + (static_cast<size_t>(l) * kNumTileShapes + sh) *
-                                                                             USLAM_TMAP_BYTES);
+                reinterpret_cast<CUtensorMap*>(static_cast<char*>(out) +
+                                               (static_cast<size_t>(l) * USLAM_TMAPS_PER_LEVEL + sh) * USLAM_TMAP_BYTES);
             const cuuint64_t dims[2] = {static_cast<cuuint64_t>(F.w[l]), static_cast<cuuint64_t>(F.h[l])};
             const cuuint64_t strides[1] = {static_cast<cuuint64_t>(F.lvl_pitch[l]) * 4u};
             const cuuint32_t box[2] = {static_cast<cuuint32_t>(kTileShapes[sh][0] + 2 * USLAM_TILE_XPAD),
@@ -1597,6 +1625,26 @@ uslam_status encode_tile_maps(const FrameDev& F, int detector, void* out, ErrTex
                                "tensor map encode failed (level " + std::to_string(l) + ", shape " + std::to_string(sh) +
                                    ", code " + std::to_string(static_cast<int>(r)) + ")");
         }
+    // the blur caches, for k_describe_tiled: box = a describe item's chunk
+    // (KDT_CW columns, 32 rows) widened by RX columns and R rows each side
+    if (uslam::describe_tiled_smem(F.margin) == 0) return USLAM_OK;
+    const int R = F.margin - 1, RX = (R + 3) & ~3;
+    for (int l = 0; l < F.levels; ++l) {
+        CUtensorMap* m = reinterpret_cast<CUtensorMap*>(
+            static_cast<char*>(out) + (static_cast<size_t>(l) * USLAM_TMAPS_PER_LEVEL + kNumTileShapes) * USLAM_TMAP_BYTES);
+        const cuuint64_t dims[2] = {static_cast<cuuint64_t>(F.w[l] + F.margin + 1),
+                                    static_cast<cuuint64_t>(F.h[l] + F.margin + 1)};
+        const cuuint64_t strides[1] = {static_cast<cuuint64_t>(F.bl_pitch[l]) * 4u};
+        const cuuint32_t box[2] = {static_cast<cuuint32_t>(KDT_CW + 2 * RX), static_cast<cuuint32_t>(32 + 2 * R)};
+        const cuuint32_t estr[2] = {1u, 1u};
+        const CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, F.blur[l], dims, strides, box, estr,
+                              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                              CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        if (r != CUDA_SUCCESS)
+            return set_err(err, USLAM_CUDA_ERROR,
+                           "blur-cache tensor map encode failed (level " + std::to_string(l) + ", code " +
+                               std::to_string(static_cast<int>(r)) + ")");
+    }
     return USLAM_OK;
 }
 

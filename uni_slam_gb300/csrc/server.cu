@@ -40,6 +40,7 @@ struct SrvClass {
     int shape = 0;                // detect tile shape (index into kTileShapes)
     std::vector<TileItem> tiles;  // one frame's tile list (frame field patched per launch)
     std::vector<BandItem> bands;  // one frame's compaction bands (frame field patched per launch)
+    std::vector<BandItem> desc;   // one frame's describe items (chunks of the bands)
 };
 
 struct SrvSlot {
@@ -175,7 +176,8 @@ struct uslam_server {
 
 namespace {
 
-size_t tables_bytes(int max_batch, int max_tiles_per_frame, int max_bands_per_frame, int levels) {
+size_t tables_bytes(int max_batch, int max_tiles_per_frame, int max_bands_per_frame, int max_desc_per_frame,
+                    int levels) {
     const size_t t = round_up(sizeof(TileItem) * static_cast<size_t>(max_batch) * max_tiles_per_frame, 256);
     const size_t f = round_up(sizeof(SegDev) * static_cast<size_t>(max_batch) * levels, 256);
     const size_t m = round_up(sizeof(MatchSegDev) * static_cast<size_t>(max_batch) * 2 * levels, 256);
@@ -183,7 +185,8 @@ size_t tables_bytes(int max_batch, int max_tiles_per_frame, int max_bands_per_fr
     const size_t p = round_up(sizeof(PairDev) * static_cast<size_t>(max_batch), 256);
     const size_t b = round_up(sizeof(BandItem) * static_cast<size_t>(max_batch) * max_bands_per_frame, 256);
     const size_t x = round_up(sizeof(SrvEmitItem) * static_cast<size_t>(max_batch), 256);
-    return t + f + m + u + p + b + x;
+    const size_t d = round_up(sizeof(BandItem) * static_cast<size_t>(max_batch) * max_desc_per_frame, 256);
+    return t + f + m + u + p + b + x + d;
 }
 
 void free_server(uslam_server* s) {
@@ -219,7 +222,7 @@ cudaError_t launch_batch(uslam_server* s, const std::vector<uint64_t>& tickets, 
     std::vector<SegDev> fsegs, usegs;
     std::vector<MatchSegDev> msegs;
     std::vector<PairDev> pairs;
-    std::vector<BandItem> bands;
+    std::vector<BandItem> bands, desc;
     std::vector<SrvEmitItem> emits;
     cudaError_t e = cudaSuccess;
     for (uint64_t tk : tickets) {
@@ -243,6 +246,10 @@ cudaError_t launch_batch(uslam_server* s, const std::vector<uint64_t>& tickets, 
         for (BandItem bi : C.bands) {
             bi.frame = static_cast<uint16_t>(r.slot);
             bands.push_back(bi);
+        }
+        for (BandItem bi : C.desc) {
+            bi.frame = static_cast<uint16_t>(r.slot);
+            desc.push_back(bi);
         }
         const FrameDev& F = s->frames[r.slot];
         e = cudaMemcpyAsync(const_cast<uint8_t*>(F.img), sl.h_in, static_cast<size_t>(F.H0) * F.img_pitch,
@@ -279,7 +286,7 @@ cudaError_t launch_batch(uslam_server* s, const std::vector<uint64_t>& tickets, 
     }
     shaped.finish();
     const std::vector<TileItem>& tiles = shaped.flat;
-    // table image: tiles | fsegs | msegs | usegs | pairs | bands
+    // table image: tiles | fsegs | msegs | usegs | pairs | bands | emits | describe items
     const size_t t_b = round_up(tiles.size() * sizeof(TileItem), 256);
     const size_t f_b = round_up(fsegs.size() * sizeof(SegDev), 256);
     const size_t m_b = round_up(msegs.size() * sizeof(MatchSegDev), 256);
@@ -287,7 +294,8 @@ cudaError_t launch_batch(uslam_server* s, const std::vector<uint64_t>& tickets, 
     const size_t p_b = round_up(pairs.size() * sizeof(PairDev), 256);
     const size_t b_b = round_up(bands.size() * sizeof(BandItem), 256);
     const size_t x_b = round_up(emits.size() * sizeof(SrvEmitItem), 256);
-    if (t_b + f_b + m_b + u_b + p_b + b_b + x_b > B.bytes) return cudaErrorInvalidValue;
+    const size_t d_b = round_up(desc.size() * sizeof(BandItem), 256);
+    if (t_b + f_b + m_b + u_b + p_b + b_b + x_b + d_b > B.bytes) return cudaErrorInvalidValue;
     char* h = B.h;
     std::memcpy(h, tiles.data(), tiles.size() * sizeof(TileItem));
     std::memcpy(h + t_b, fsegs.data(), fsegs.size() * sizeof(SegDev));
@@ -296,7 +304,8 @@ cudaError_t launch_batch(uslam_server* s, const std::vector<uint64_t>& tickets, 
     std::memcpy(h + t_b + f_b + m_b + u_b, pairs.data(), pairs.size() * sizeof(PairDev));
     std::memcpy(h + t_b + f_b + m_b + u_b + p_b, bands.data(), bands.size() * sizeof(BandItem));
     std::memcpy(h + t_b + f_b + m_b + u_b + p_b + b_b, emits.data(), emits.size() * sizeof(SrvEmitItem));
-    const size_t total = t_b + f_b + m_b + u_b + p_b + b_b + x_b;
+    std::memcpy(h + t_b + f_b + m_b + u_b + p_b + b_b + x_b, desc.data(), desc.size() * sizeof(BandItem));
+    const size_t total = t_b + f_b + m_b + u_b + p_b + b_b + x_b + d_b;
     e = cudaMemcpyAsync(B.d, h, total, cudaMemcpyHostToDevice, st);
     if (e != cudaSuccess) return e;
     const auto* d_tiles = reinterpret_cast<const TileItem*>(B.d);
@@ -306,6 +315,7 @@ cudaError_t launch_batch(uslam_server* s, const std::vector<uint64_t>& tickets, 
     const auto* d_pairs = reinterpret_cast<const PairDev*>(B.d + t_b + f_b + m_b + u_b);
     const auto* d_bands = reinterpret_cast<const BandItem*>(B.d + t_b + f_b + m_b + u_b + p_b);
     const auto* d_emits = reinterpret_cast<const SrvEmitItem*>(B.d + t_b + f_b + m_b + u_b + p_b + b_b);
+    const auto* d_desc = reinterpret_cast<const BandItem*>(B.d + t_b + f_b + m_b + u_b + p_b + b_b + x_b);
     const int grid = c->num_sms * 4;
     const int nf = static_cast<int>(fsegs.size());
     if ((e = launch_detect_shaped(s->d_frames, d_tiles, shaped.begin, c->detector, s->d_err, st)) != cudaSuccess) return e;
@@ -313,7 +323,11 @@ cudaError_t launch_batch(uslam_server* s, const std::vector<uint64_t>& tickets, 
     if ((e = launch_compact_banded(s->d_frames, d_bands, static_cast<int>(bands.size()), d_fsegs, nf, s->max_w,
                                    st)) != cudaSuccess)
         return e;
-    if ((e = launch_describe(s->d_frames, d_fsegs, nf, c->d_pattern, grid, false, false, st)) != cudaSuccess) return e;
+    e = static_cast<int>(emits.size()) >= kTiledDescribeFrames && describe_tiled_smem(c->margin) > 0
+            ? launch_describe_tiled(s->d_frames, d_desc, static_cast<int>(desc.size()), c->d_pattern, false, false,
+                                    c->margin, s->d_err, st)
+            : launch_describe(s->d_frames, d_fsegs, nf, c->d_pattern, grid, false, false, st);
+    if (e != cudaSuccess) return e;
     if (!pairs.empty()) {
         if ((e = launch_match(s->d_frames, d_pairs, d_msegs, static_cast<int>(msegs.size()), grid, st)) != cudaSuccess)
             return e;
@@ -437,7 +451,7 @@ uslam_status uslam_server_create(uslam_ctx* ctx, const uslam_server_params* p, u
     };
     std::vector<SlotLayout> lay(p->n_sizes);
     std::vector<FrameDev> proto(p->n_sizes);
-    int max_tiles = 1, max_bands = 1;
+    int max_tiles = 1, max_bands = 1, max_desc = 1;
     for (int k = 0; k < p->n_sizes; ++k) {
         const int W0 = p->widths[k], H0 = p->heights[k];
         if (W0 < 1 || H0 < 1 || W0 > ctx->max_w || H0 > ctx->max_h) {
@@ -476,7 +490,7 @@ uslam_status uslam_server_create(uslam_ctx* ctx, const uslam_server_params* p, u
         C.H0 = H0;
         for (int l = 0; l < L; ++l) {
             F.kp_pitch[l] = static_cast<int>(round_up(static_cast<size_t>(F.w[l]), 16));
-            F.bl_pitch[l] = F.w[l] + ctx->margin + 1;
+            F.bl_pitch[l] = lvl_pitch_of(F.w[l] + ctx->margin + 1);  // 16-byte rows (TMA)
             F.lvl_pitch[l] = lvl_pitch_of(F.w[l]);
             Y.feats[l] = take(capa * 48);
             Y.lvl[l] = take(static_cast<size_t>(F.h[l]) * F.lvl_pitch[l] * 4);
@@ -495,16 +509,21 @@ uslam_status uslam_server_create(uslam_ctx* ctx, const uslam_server_params* p, u
                 bi.level = static_cast<uint8_t>(l);
                 bi.band = static_cast<uint16_t>(q);
                 C.bands.push_back(bi);
+                for (int ch = 0; ch < (F.w[l] + KDT_CW - 1) / KDT_CW; ++ch) {
+                    bi.pad2 = static_cast<uint16_t>(ch);
+                    C.desc.push_back(bi);
+                }
             }
         Y.a2b = take(static_cast<size_t>(L) * capa * 4);
         Y.b2a = take(static_cast<size_t>(L) * capa * 4);
         Y.matches = take(static_cast<size_t>(L) * capa * 16);
         Y.mcount = take(sizeof(uint32_t) * L);
-        Y.tmaps = take(static_cast<size_t>(L) * kNumTileShapes * USLAM_TMAP_BYTES);
+        Y.tmaps = take(static_cast<size_t>(L) * USLAM_TMAPS_PER_LEVEL * USLAM_TMAP_BYTES);
         Y.bytes = round_up(cur, 256);
         C.tiles_per_frame = static_cast<int>(C.tiles.size());
         max_tiles = std::max(max_tiles, C.tiles_per_frame);
         max_bands = std::max(max_bands, static_cast<int>(C.bands.size()));
+        max_desc = std::max(max_desc, static_cast<int>(C.desc.size()));
         s->max_w = std::max(s->max_w, F.w[0]);
         s->classes.push_back(std::move(C));
     }
@@ -560,7 +579,7 @@ uslam_status uslam_server_create(uslam_ctx* ctx, const uslam_server_params* p, u
                 F.mask[l] = masks[l];
             }
             F.tmaps = base + Y.tmaps;
-            std::vector<char> maps(static_cast<size_t>(L) * kNumTileShapes * USLAM_TMAP_BYTES);
+            std::vector<char> maps(static_cast<size_t>(L) * USLAM_TMAPS_PER_LEVEL * USLAM_TMAP_BYTES);
             const uslam_status ts = encode_tile_maps(F, ctx->detector, maps.data(), &ctx->err);
             if (ts != USLAM_OK) {
                 free_server(s);
@@ -590,12 +609,13 @@ uslam_status uslam_server_create(uslam_ctx* ctx, const uslam_server_params* p, u
     if (e == cudaSuccess) e = cudaHostAlloc(&s->h_err, 2 * sizeof(uint32_t), cudaHostAllocDefault);
     if (e == cudaSuccess) s->h_err[0] = s->h_err[1] = 0u;
     for (int b = 0; b < 2 && e == cudaSuccess; ++b) {
-        s->bufs[b].bytes = tables_bytes(s->max_batch, max_tiles, max_bands, L);
+        s->bufs[b].bytes = tables_bytes(s->max_batch, max_tiles, max_bands, max_desc, L);
         e = cudaHostAlloc(&s->bufs[b].h, s->bufs[b].bytes, cudaHostAllocDefault);
         if (e == cudaSuccess) e = cudaMalloc(&s->bufs[b].d, s->bufs[b].bytes);
         if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->cs[b], cudaStreamNonBlocking);
     }
     if (e == cudaSuccess) e = set_compact_smem(s->max_w);
+    if (e == cudaSuccess && describe_tiled_smem(ctx->margin) > 0) e = set_describe_tiled_smem(ctx->margin);
     if (e != cudaSuccess) {
         const std::string m = std::string("server_create: ") + cudaGetErrorString(e);
         cudaGetLastError();

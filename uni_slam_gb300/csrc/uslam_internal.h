@@ -132,6 +132,8 @@ struct SegDev {
 };
 
 // Compaction work item: one 32-row band (a row of 32x32 cells) of one level.
+// As a describe item (k_describe_tiled) pad2 is the chunk: columns
+// pad2 * KDT_CW .. + KDT_CW - 1 of the band.
 struct BandItem {
     uint16_t frame;
     uint8_t level;
@@ -154,6 +156,11 @@ struct BandItem {
 #define USLAM_TILE_XPAD 8
 #define USLAM_TMAP_BYTES 128
 #define USLAM_NUM_TILE_SHAPES 5  // k_detect tile shapes (kTileShapes of the runtime)
+// Tensor maps per level of a frame: one per k_detect tile shape over the
+// level, then one over the level's blur cache (k_describe_tiled's box).
+#define USLAM_TMAPS_PER_LEVEL (USLAM_NUM_TILE_SHAPES + 1)
+// k_describe_tiled: columns of a describe item (a chunk of a 32-row band).
+#define KDT_CW 128
 
 // Packed match-partner encoding: level in the top 8 bits, index in the low 24.
 #define USLAM_PACK(l, i) (((int32_t)(l) << 24) | (int32_t)(i))
