@@ -7,13 +7,16 @@ previous one (63 pairs).  A step is one pass over the 64-frame batch.
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
 Prints one JSON line (rank 0).  ``value`` = frames/s with inputs resident in
-HBM (graph replay of the 5-kernel batch, L2 flushed between steps);
+HBM (graph replay of the batch's kernels, L2 flushed between steps);
 ``e2e`` = the same through the C ABI with pinned-host H2D of the frames and
-D2H of every feature record and match list inside the timed region (two
-batches in flight, so one step's copies overlap the next step's kernels;
+D2H of every feature record and match list inside the timed region (three
+batches in flight, so one step's copies overlap the others' kernels;
 ``e2e.unpipelined_value`` is one batch with a sync after every step);
 ``plain_fps`` = the plain per-frame form (one frame per launch sequence,
-synchronous per frame); ``served`` = 32 camera streams at 20 Hz through the
+synchronous per frame); ``plugin_e2e`` = the reference-facing C++ passes on
+f32 host frames, one frame per call; ``windowed_tensor_core`` = the main
+workload with matcher 3 (the windowed matcher's distances from tensor-core
+tiles); ``served`` = 32 camera streams at 20 Hz through the
 serving loop (p50/p99 latency, frames/s), and ``served.saturation`` = the
 same streams closed-loop with 4 frames in flight each (capacity); ``uneven`` = 46 frames of five
 sizes (640x480 .. 3840x2160) each matched against its warp in one graph,
@@ -73,6 +76,8 @@ def _args():
     ap.add_argument("--stress-steps", type=int, default=5)
     ap.add_argument("--uneven", type=int, default=1, help="batched-uneven workload (0: skip)")
     ap.add_argument("--cfg", type=int, default=1, help="cfg detection/matching profile on the main workload (0: skip)")
+    ap.add_argument("--wintc", type=int, default=1,
+                    help="the main workload with the tensor-core windowed matcher, matcher 3 (0: skip)")
     ap.add_argument("--ransac", type=int, default=1, help="RANSAC hypothesis scoring on the workload's matches (0: skip)")
     ap.add_argument("--triangulate", type=int, default=1, help="batched two-view triangulation section (0: skip)")
     return ap.parse_args()
@@ -812,6 +817,54 @@ def cfg_run(pat, local: int, frames, steps: int, warmup: int, matcher: int = 1) 
         ctx.close()
 
 
+def wintc_run(pat, local: int, frames, steps: int, warmup: int, base_lists: list[str]) -> dict:
+    """The batched-uniform workload with matcher 3: the windowed matcher with
+    its distances from tensor-core tiles (k_describe writes the FP8 operand
+    rows, k_win_plan / k_win_mma match), beside matcher 0 (k_match) of the
+    main run: step time, per-kernel time and whether the lists are equal."""
+    import torch
+
+    from uni_slam_gb300 import Batch, Context
+
+    n = len(frames)
+    ctx = Context(pat, levels=LEVELS, max_width=W, max_height=H, device=local, matcher=3)
+    batch = Batch(ctx, [(W, H)] * n, [(i, i + 1) for i in range(n - 1)])
+    try:
+        for i, f in enumerate(frames):
+            batch.set_frame(i, f)
+        batch.upload()
+        batch.sync()
+        stream = torch.cuda.Stream()
+        batch.set_stream(stream.cuda_stream)
+        l2_flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+        for _ in range(warmup):
+            batch.run()
+        stream.synchronize()
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+        with torch.cuda.stream(stream):
+            for e0, e1 in evs:
+                l2_flush.zero_()
+                e0.record(stream)
+                batch.run()
+                e1.record(stream)
+        stream.synchronize()
+        step_ms = sum(e0.elapsed_time(e1) for e0, e1 in evs) / steps
+        batch.download()
+        batch.sync()
+        prof = batch.profile(iters=3)
+        prof = {("k_win_plan+k_win_mma" if k == "k_match" else k): v for k, v in prof.items()}
+        lists = [_mm_digest(batch.matches(k)) for k in range(n - 1)]
+        return {
+            "matcher": "3: the windowed mutual matcher with its distances from tensor-core tiles (tcgen05), "
+                       "FP8 operand rows written by k_describe",
+            "frames": n, "ms_per_step": step_ms, "frames_per_s": n / (step_ms / 1e3), "kernel_ms": prof,
+            "l2": "flushed (256 MiB write) between timed steps", "match_lists_equal": lists == base_lists,
+        }
+    finally:
+        batch.close()
+        ctx.close()
+
+
 def ransac_run(ctx, batch, pairs: int, n_hyp: int = 500, reps: int = 20) -> dict:
     """Batched RANSAC hypothesis scoring (the stage after matching) on the
     matches of the workload's first pairs: n_hyp fundamental matrices fitted on
@@ -1106,6 +1159,7 @@ def run_ours(a):
     kept = [int(batch.features(i)[1].sum()) for i in range(n)]
     nmatch = [len(batch.matches(p)) for p in range(n - 1)]
     nbytes = algorithmic_bytes(kept, nmatch, n)
+    main_lists = [_mm_digest(batch.matches(p)) for p in range(n - 1)]
     ref_check = reference_match_check(batch, n) if rank == 0 else None
 
     # ---- per-kernel timing for the roofline (events on the launching stream)
@@ -1242,6 +1296,7 @@ def run_ours(a):
     # serving loop runs in the same host state as in a stand-alone service
     stress_frames, uneven_frames = side_workload_frames(a, rank)
 
+    wintc = wintc_run(pat, local, frames, a.stress_steps, 2, main_lists) if a.wintc else None
     cfg = cfg_run(pat, local, frames, a.stress_steps, 2) if a.cfg else None
     if cfg:
         cfg["tensor_core"] = _tensor_core_leg(cfg_run(pat, local, frames, a.stress_steps, 2, matcher=2), cfg, "frames")
@@ -1282,7 +1337,8 @@ def run_ours(a):
                               "frames, graph, D2H of every feature record and match block",
                     "unpipelined_value": n * world / e2e_serial_s},
             "gpu_launches": KERNELS_PER_STEP * a.steps, "roofline": roofline, "cpu_baseline": cpu, "clocks": clk,
-            "served": served, "uneven": uneven, "stress": stress, "cfg": cfg, "ransac": ransac,
+            "served": served, "uneven": uneven, "stress": stress, "cfg": cfg, "windowed_tensor_core": wintc,
+            "ransac": ransac,
             "triangulate": tri,
             "features_per_frame": sum(kept) / n, "matches_per_pair": sum(nmatch) / max(1, n - 1),
             "reference_match_check": ref_check,

@@ -249,8 +249,8 @@ __device__ __forceinline__ void tma_load_2d(void* dst, const void* tmap, int x, 
 
 // ----------------------------------------------------------- pyramid ----
 // Level l of one TW x TH tile into lvl[l] (row pitch lvl_pitch): l = 0 is
-// f32(u8) / 255 (provider_base.cpp:121-124), read 16 pixels per 16-byte load
-// and stored as four 16-byte vectors; l >= 1 is one canonical bilinear tap of
+// f32(u8) / 255 (provider_base.cpp:121-124), read 8 pixels per 8-byte load
+// and stored as two 16-byte vectors; l >= 1 is one canonical bilinear tap of
 // LOD0 at the texel centre (create_pyramid.wgsl:11-12).  Sampling
 // coordinates depend only on the row or only on the column, so they are
 // computed once per tile row / column (the per-pixel operations, so the same
@@ -259,7 +259,7 @@ __device__ __forceinline__ void tma_load_2d(void* dst, const void* tmap, int x, 
 template <int TW, int TH>
 __global__ void __launch_bounds__(K1_THREADS)
 k_pyramid(const FrameDev* __restrict__ frames, const TileItem* __restrict__ tiles) {
-    static_assert(K1_THREADS % TW == 0 && TW % 16 == 0, "tile shape");
+    static_assert(K1_THREADS % TW == 0 && TW % 8 == 0, "tile shape");
     __shared__ float s_lut[256];  // f32(u8) / 255
     __shared__ int2 s_fx[TW];     // LOD0 source columns (x0, x1) per tile column
     __shared__ float2 s_fa[TW];   // (1 - a, a)
@@ -277,27 +277,32 @@ k_pyramid(const FrameDev* __restrict__ frames, const TileItem* __restrict__ tile
     const int pitch = F.img_pitch;
     s_lut[t] = (float)t / 255.0f;
     if (l == 0) {
+        // 8 pixels per thread (8-byte loads): a 64-wide tile of 32 rows is
+        // 256 segments, one per thread.  16-byte loads left half the threads
+        // without a segment and measured slower (0.151 against 0.144 ms on 64
+        // frames of 752x480).
         __syncthreads();
-        constexpr int SEGS = TW / 16;
+        constexpr int SEGS = TW / 8;
         for (int u = t; u < SEGS * TH; u += K1_THREADS) {
             const int r = u / SEGS;
-            const int x = X0 + (u - r * SEGS) * 16, y = Y0 + r;
+            const int x = X0 + (u - r * SEGS) * 8, y = Y0 + r;
             if (y >= h || x >= w) continue;
-            // x is a multiple of 16 below w, so x + 16 <= the 16-byte image pitch
-            const uint4 q = *reinterpret_cast<const uint4*>(img + (size_t)y * pitch + x);
-            const uint32_t qw[4] = {q.x, q.y, q.z, q.w};
-            float* o = out + (size_t)y * lp + x;
+            // x is a multiple of 8 below w, so x + 8 <= the 16-byte image pitch
+            const uint2 q = *reinterpret_cast<const uint2*>(img + (size_t)y * pitch + x);
+            float v[8];
 #pragma unroll
-            for (int g = 0; g < 4; ++g) {
-                const float4 v = make_float4(s_lut[qw[g] & 255u], s_lut[(qw[g] >> 8) & 255u],
-                                             s_lut[(qw[g] >> 16) & 255u], s_lut[qw[g] >> 24]);
-                // rows of 16-byte pitch: a group of 4 inside the row is stored whole
-                if (x + 4 * g + 4 <= lp) reinterpret_cast<float4*>(o)[g] = v;
-                else if (x + 4 * g < w) {
-                    const float vv[4] = {v.x, v.y, v.z, v.w};
-                    for (int k = 0; k < 4; ++k)
-                        if (x + 4 * g + k < w) o[4 * g + k] = vv[k];
-                }
+            for (int k = 0; k < 4; ++k) {
+                v[k] = s_lut[(q.x >> (8 * k)) & 255u];
+                v[4 + k] = s_lut[(q.y >> (8 * k)) & 255u];
+            }
+            float* o = out + (size_t)y * lp + x;
+            if (x + 8 <= lp) {
+                reinterpret_cast<float4*>(o)[0] = make_float4(v[0], v[1], v[2], v[3]);
+                reinterpret_cast<float4*>(o)[1] = make_float4(v[4], v[5], v[6], v[7]);
+            } else {
+#pragma unroll
+                for (int k = 0; k < 8; ++k)
+                    if (x + k < w) o[k] = v[k];
             }
         }
         return;
@@ -1436,20 +1441,9 @@ k_describe_tiled(const FrameDev* __restrict__ frames, const BandItem* __restrict
     const int x0 = (int)it.pad2 * KDT_CW, y0 = band * 32;
     const int xs = x0 - RX, ys = y0 - R;
     const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
-    if (t == 0) {
-        const void* tmap = static_cast<const char*>(F.tmaps) +
-                           (size_t)(l * USLAM_TMAPS_PER_LEVEL + USLAM_NUM_TILE_SHAPES) * USLAM_TMAP_BYTES;
-        mbar_init(&s_bar, 1u);
-        mbar_expect_tx(&s_bar, (uint32_t)(BW * BH * 4));
-        tma_load_2d(s_box, tmap, xs, ys, &s_bar);
-    }
-    for (int i = t; i < 256; i += KDT_THREADS) {
-        s_pat[i] = make_float4((float)pattern[4 * i], (float)pattern[4 * i + 1], (float)pattern[4 * i + 2],
-                               (float)pattern[4 * i + 3]);
-        s_lut[i] = (float)i / 255.0f;
-    }
     // the band's range of the level's list: after the kept counts of the
-    // earlier bands, clipped by the level's kept count (the cap)
+    // earlier bands, clipped by the level's kept count (the cap); the box is
+    // loaded only for a band that keeps keypoints
     if (warp == 0) {
         uint32_t pk = 0;
         for (int q = lane; q < band; q += 32) pk += F.bands[l][2 * q + 1];
@@ -1457,43 +1451,30 @@ k_describe_tiled(const FrameDev* __restrict__ frames, const BandItem* __restrict
         for (int o = 16; o > 0; o >>= 1) pk += __shfl_xor_sync(0xffffffffu, pk, o);
         if (lane == 0) {
             const uint32_t kept = F.kept[l];
-            const uint32_t b0 = min(pk, kept);
+            const uint32_t b0 = min(pk, kept), b1 = min(pk + F.bands[l][2 * band + 1], kept);
             s_pos[0] = b0;
-            s_pos[1] = min(pk + F.bands[l][2 * band + 1], kept);
-        }
-    }
-    __syncthreads();  // barrier initialised, pattern, range
-    const bool landed = mbar_wait(&s_bar, 0u, kTmaWaitLimit);
-    if (__syncthreads_or(!landed)) {
-        if (t == 0) atomicOr(err, USLAM_ERR_TMA_TIMEOUT);
-        mbar_wait(&s_bar, 0u, kTmaWaitLimit);  // the copy in flight lands before the box is left
-        return;
-    }
-    // cells at negative coordinates: the sentinel column (x = w + M) / row
-    // (y = h + M) that every negative coordinate reads
-    if (xs < 0 || ys < 0) {
-        const float* blur = F.blur[l];
-        const int bp = F.bl_pitch[l];
-        const int nx = max(-xs, 0), ny = max(-ys, 0);
-        const int n = ny * BW + (BH - ny) * nx;
-        for (int k = t; k < n; k += KDT_THREADS) {
-            int r, c;
-            if (k < ny * BW) {
-                r = k / BW;
-                c = k - r * BW;
-            } else {
-                const int q = k - ny * BW;
-                r = ny + q / nx;
-                c = q - (q / nx) * nx;
+            s_pos[1] = b1;
+            if (b1 > b0) {
+                const void* tmap = static_cast<const char*>(F.tmaps) +
+                                   (size_t)(l * USLAM_TMAPS_PER_LEVEL + USLAM_NUM_TILE_SHAPES) * USLAM_TMAP_BYTES;
+                mbar_init(&s_bar, 1u);
+                mbar_expect_tx(&s_bar, (uint32_t)(BW * BH * 4));
+                tma_load_2d(s_box, tmap, xs, ys, &s_bar);
             }
-            const int gy = ys + r, gx = xs + c;
-            if (gy > h + M || gx > w + M) continue;  // past the cache: never read by a test
-            s_box[r * BW + c] = blur[(size_t)(gy < 0 ? h + M : gy) * bp + (gx < 0 ? w + M : gx)];
         }
-        __syncthreads();
+    }
+    __syncthreads();  // range, barrier initialised
+    if (s_pos[1] <= s_pos[0]) return;  // no keypoint in the band: nothing loaded
+    // while the box is in flight: the pattern, the selection and the
+    // orientations of the first round (they read the level, not the box)
+    for (int i = t; i < 256; i += KDT_THREADS) {
+        s_pat[i] = make_float4((float)pattern[4 * i], (float)pattern[4 * i + 1], (float)pattern[4 * i + 2],
+                               (float)pattern[4 * i + 3]);
+        s_lut[i] = (float)i / 255.0f;
     }
     const uint32_t pos0 = s_pos[0], pos1 = s_pos[1];
     const uint32_t* feats = F.feats[l];
+    bool box_ready = false;
     for (uint32_t base = pos0; base < pos1; base += KDT_THREADS) {
         // this round's keypoints with x in the chunk, in list order
         const uint32_t i = base + (uint32_t)t;
@@ -1504,7 +1485,7 @@ k_describe_tiled(const FrameDev* __restrict__ frames, const BandItem* __restrict
         }
         const uint32_t bal = __ballot_sync(0xffffffffu, sel);
         if (lane == 0) s_wcount[warp] = (uint32_t)__popc(bal);
-        __syncthreads();
+        __syncthreads();  // also the pattern and the lookup table of the first round
         uint32_t off = 0, nsel = 0;
         for (int q = 0; q < KDT_WARPS; ++q) {
             off += q < warp ? s_wcount[q] : 0u;
@@ -1539,6 +1520,39 @@ k_describe_tiled(const FrameDev* __restrict__ frames, const BandItem* __restrict
             my_theta = uslam_atan2f(m01, m10);
             uslam_sincosf(my_theta, &my_s, &my_c);
         }
+        if (!box_ready) {
+            // the box has landed; cells at negative coordinates get the
+            // sentinel column (x = w + M) / row (y = h + M) that every
+            // negative coordinate reads
+            const bool landed = mbar_wait(&s_bar, 0u, kTmaWaitLimit);
+            if (__syncthreads_or(!landed)) {
+                if (t == 0) atomicOr(err, USLAM_ERR_TMA_TIMEOUT);
+                mbar_wait(&s_bar, 0u, kTmaWaitLimit);  // the copy in flight lands before the box is left
+                return;
+            }
+            if (xs < 0 || ys < 0) {
+                const float* blur = F.blur[l];
+                const int bp = F.bl_pitch[l];
+                const int nx = max(-xs, 0), ny = max(-ys, 0);
+                const int n = ny * BW + (BH - ny) * nx;
+                for (int k = t; k < n; k += KDT_THREADS) {
+                    int r, c;
+                    if (k < ny * BW) {
+                        r = k / BW;
+                        c = k - r * BW;
+                    } else {
+                        const int q = k - ny * BW;
+                        r = ny + q / nx;
+                        c = q - (q / nx) * nx;
+                    }
+                    const int gy = ys + r, gx = xs + c;
+                    if (gy > h + M || gx > w + M) continue;  // past the cache: never read by a test
+                    s_box[r * BW + c] = blur[(size_t)(gy < 0 ? h + M : gy) * bp + (gx < 0 ? w + M : gx)];
+                }
+                __syncthreads();
+            }
+            box_ready = true;
+        }
         for (int kp = 0; kp < nk; ++kp) {
             const uint32_t i2 = s_list[g0 + kp];
             const float theta = __shfl_sync(0xffffffffu, my_theta, kp);
@@ -1568,6 +1582,7 @@ k_describe_tiled(const FrameDev* __restrict__ frames, const BandItem* __restrict
         }
         __syncthreads();  // s_list / s_wcount reused by the next round
     }
+    if (!box_ready) mbar_wait(&s_bar, 0u, kTmaWaitLimit);  // no keypoint in the chunk: the load lands first
 }
 
 // Dynamic shared memory of k_describe_tiled for a blur-cache margin M (0 if
