@@ -109,6 +109,13 @@ typedef struct uslam_params {
      * order, so a frame keeps the first frame_cap features in (level, y, x)
      * order (or (level, cell, y, x) with cell_cap).  No reference counterpart. */
     int frame_cap;
+    /* How the describe stage reads the blur cache (identical records):
+     * 0: per-test gathers from global memory (k_describe);
+     * 1: batches of 8 frames or more stage the cache box of every 32-row x
+     *    128-column chunk in shared memory by one TMA load and read the tests
+     *    from there (k_describe_tiled); measured no faster on 752x480 frames
+     *    and slower on sparse 4K levels, so not the default. */
+    int describe_form;
 } uslam_params;
 
 /* ---- context ---------------------------------------------------------- */

@@ -18,11 +18,14 @@ def ctx(brief_pattern):
     c.close()
 
 
-@pytest.fixture(scope="module", params=[0, 3], ids=["k_match", "k_win_mma"])
+@pytest.fixture(scope="module", params=[(0, 0), (3, 0), (0, 1)], ids=["k_match", "k_win_mma", "k_describe_tiled"])
 def wctx(request, brief_pattern):
     """The windowed matcher with its distances from k_match (matcher 0) and
-    from the tensor cores (matcher 3): the same lists."""
-    c = Context(brief_pattern, levels=6, max_width=1280, max_height=720, matcher=request.param)
+    from the tensor cores (matcher 3), and the describe stage reading its
+    tests from TMA-staged shared-memory boxes (describe_form 1): the same
+    features and lists."""
+    matcher, form = request.param
+    c = Context(brief_pattern, levels=6, max_width=1280, max_height=720, matcher=matcher, describe_form=form)
     yield c
     c.close()
 
@@ -218,13 +221,13 @@ def test_widest_tallest_frames_and_most_levels(brief_pattern):
 
 
 def test_tiled_describe_edge_frames(brief_pattern):
-    """Batches of 8 frames or more describe over blur-cache boxes staged in
-    shared memory (k_describe_tiled).  The edge cases in one such batch: the
+    """With describe_form 1, batches of 8 frames or more describe over
+    blur-cache boxes staged in shared memory (k_describe_tiled).  The edge cases in one such batch: the
     widest and tallest frames (8192 x 96, 96 x 8192, 12 levels: 64 column
     chunks, 256 bands), tiny and odd frames whose boxes reach past every
     edge (tests at negative coordinates read the sentinels), and a constant
     frame; all bit-exact against the oracle."""
-    with Context(brief_pattern, levels=12, max_width=8192, max_height=8192) as c:
+    with Context(brief_pattern, levels=12, max_width=8192, max_height=8192, describe_form=1) as c:
         frames = list(synth.warped_pair(21, 8192, 96)) + list(synth.warped_pair(22, 96, 8192))
         frames += [synth.scene_frame(9, 10, 10), synth.scene_frame(11, 37, 23), synth.scene_frame(12, 61, 45),
                    np.full((48, 64), 77, np.uint8)]
@@ -301,16 +304,20 @@ def test_large_batch_bit_exact(wctx, brief_pattern):
         b.close()
 
 
+@pytest.mark.parametrize("form", [0, 1])
 @pytest.mark.parametrize("matcher", [0, 2, 3])
-def test_split_batch_pairs_across_halves(brief_pattern, matcher):
+def test_split_batch_pairs_across_halves(brief_pattern, matcher, form):
     """A batch of 20 frames is captured as two halves (frames 0-9 and 10-19)
     on two streams.  Pairs within either half, from the first half into the
     second and from the second back into the first all equal the oracle, with
-    the windowed matcher and with the tensor-core brute-force matcher."""
+    the windowed matcher (distances from k_match or from the tensor cores) and
+    with the tensor-core brute-force matcher, each with either describe form
+    (the tiled form also writing the matchers' operand rows)."""
     W, H = 320, 240
     frames = [synth.scene_frame(300 + k, W, H) for k in range(20)]
     pairs = [(0, 1), (3, 12), (15, 2), (10, 11), (19, 0), (9, 10), (8, 9), (12, 19)]
-    with Context(brief_pattern, levels=6, max_width=W, max_height=H, matcher=matcher, ratio=0.8) as c:
+    with Context(brief_pattern, levels=6, max_width=W, max_height=H, matcher=matcher, ratio=0.8,
+                 describe_form=form) as c:
         b = Batch(c, [(W, H)] * len(frames), pairs)
         try:
             b.process(frames)

@@ -39,6 +39,7 @@ class Params(C.Structure):
         ("device", C.c_int), ("levels", C.c_int), ("max_width", C.c_int), ("max_height", C.c_int),
         ("cap_per_level", C.c_int), ("brief_pattern", C.POINTER(C.c_int32)), ("matcher", C.c_int),
         ("ratio", C.c_float), ("cell_cap", C.c_int), ("detector", C.c_int), ("frame_cap", C.c_int),
+        ("describe_form", C.c_int),
     ]
 
 

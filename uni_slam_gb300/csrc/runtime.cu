@@ -182,14 +182,17 @@ struct Lane {
 
 Lane lane0(uslam_batch* b) { return Lane{b->stream, b->aux_stream, b->ev_fork, b->ev_join, b->d_err + 1}; }
 
-// Describe of a program: in batches of kTiledDescribeFrames frames or more,
-// k_describe_tiled over the describe items (the blur cache staged per chunk
-// by TMA) where the pattern's reach fits a TMA box; else the gather form
-// k_describe over (frame, level) segments, whose warps take fewer keypoints
-// each and so finish a few frames sooner.
+// Describe of a program: the gather form k_describe over (frame, level)
+// segments; with describe_form 1, in batches of kTiledDescribeFrames frames
+// or more, k_describe_tiled over the describe items (the blur cache staged
+// per chunk by TMA) where the pattern's reach fits a TMA box.
+bool tiled_describe(const uslam_ctx* c, int n_frames) {
+    return c->describe_form == 1 && n_frames >= kTiledDescribeFrames && describe_tiled_smem(c->margin) > 0;
+}
+
 cudaError_t describe_stage(uslam_batch* b, const Program& P, cudaStream_t st) {
     uslam_ctx* c = b->ctx;
-    if (static_cast<int>(b->frames.size()) >= kTiledDescribeFrames && describe_tiled_smem(c->margin) > 0)
+    if (tiled_describe(c, static_cast<int>(b->frames.size())))
         return launch_describe_tiled(b->d_frames, P.desc, P.ndesc, c->d_pattern, c->matcher == 2, b->win_tc, c->margin,
                                      b->d_err, st);
     return launch_describe(b->d_frames, P.fsegs, P.nfsegs, c->d_pattern, c->num_sms * 4, c->matcher == 2, b->win_tc, st);
@@ -611,8 +614,7 @@ uslam_status create_batch(uslam_ctx* ctx, int n_frames, const int* widths, const
         return ctx->cuda_fail(e, "frame table upload");
     }
     e = set_compact_smem(b->max_w);
-    if (e == cudaSuccess && n_frames >= kTiledDescribeFrames && describe_tiled_smem(ctx->margin) > 0)
-        e = set_describe_tiled_smem(ctx->margin);
+    if (e == cudaSuccess && tiled_describe(ctx, n_frames)) e = set_describe_tiled_smem(ctx->margin);
     if (e == cudaSuccess && ctx->matcher == 2) e = set_bf_mma_smem();
     if (e == cudaSuccess && b->win_tc) e = set_win_mma_smem();
     if (e != cudaSuccess) {
@@ -838,7 +840,7 @@ uslam_status uslam_create(const uslam_params* params, uslam_ctx** out) {
         (params->matcher < 0 || params->matcher > 3) ||
         ((params->matcher == 1 || params->matcher == 2) && !(params->ratio > 0.0f)) ||
         params->cell_cap < 0 || params->cell_cap > 1024 || (params->detector != 0 && params->detector != 1) ||
-        params->frame_cap < 0)
+        params->frame_cap < 0 || params->describe_form < 0 || params->describe_form > 1)
         return USLAM_INVALID_ARG;
     auto* c = new uslam_ctx();
     c->device = params->device;
@@ -852,6 +854,7 @@ uslam_status uslam_create(const uslam_params* params, uslam_ctx** out) {
     c->ratio = params->ratio;
     c->cell_cap = params->cell_cap;
     c->frame_cap = params->frame_cap;
+    c->describe_form = params->describe_form;
     c->detector = params->detector;
     // blur-cache margin: a rotated test point lies within ceil(radius) + 1 of
     // its keypoint (rounding of the rotation), so radius + 2 covers it.

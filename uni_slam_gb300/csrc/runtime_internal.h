@@ -35,9 +35,8 @@ cudaError_t launch_describe(const FrameDev*, const SegDev*, int, const int32_t*,
 cudaError_t launch_describe_tiled(const FrameDev*, const BandItem*, int, const int32_t*, bool, bool, int, uint32_t*,
                                   cudaStream_t);
 size_t describe_tiled_smem(int margin);
-// Frames of a batch (or server launch) from which the describe stage runs
-// k_describe_tiled (measured: 0.357 against 0.371 ms for k_describe on 64
-// frames of 752x480, while one frame ran 0.09 ms longer).
+// Frames of a batch (or server launch) from which describe_form 1 runs
+// k_describe_tiled (one frame measured 0.09 ms longer than with k_describe).
 constexpr int kTiledDescribeFrames = 8;
 cudaError_t set_describe_tiled_smem(int margin);
 cudaError_t launch_match(const FrameDev*, const PairDev*, const void*, int, int, cudaStream_t);
@@ -242,6 +241,7 @@ struct uslam_ctx {
     bool win_tc = false;  // matcher 0 asked for with the distances from the tensor cores (matcher 3)
     float ratio = 0.8f;   // Lowe ratio of the brute-force matcher
     int frame_cap = 0;    // > 0: features kept per frame, levels filled in order
+    int describe_form = 0;  // 1: k_describe_tiled in batches of kTiledDescribeFrames frames or more
     int cell_cap = 0;     // > 0: keypoints kept per 32x32 cell of a level, cell order
     int detector = 0;     // 0 reference FAST + cull, 1 cfg profile (FAST 9-of-16 at 20/255 + 3x3 NMS)
     std::map<std::pair<int, int>, int> tile_shape;  // per resolution class (autotuned or set)

@@ -323,7 +323,8 @@ cudaError_t launch_batch(uslam_server* s, const std::vector<uint64_t>& tickets, 
     if ((e = launch_compact_banded(s->d_frames, d_bands, static_cast<int>(bands.size()), d_fsegs, nf, s->max_w,
                                    st)) != cudaSuccess)
         return e;
-    e = static_cast<int>(emits.size()) >= kTiledDescribeFrames && describe_tiled_smem(c->margin) > 0
+    e = c->describe_form == 1 && static_cast<int>(emits.size()) >= kTiledDescribeFrames &&
+                describe_tiled_smem(c->margin) > 0
             ? launch_describe_tiled(s->d_frames, d_desc, static_cast<int>(desc.size()), c->d_pattern, false, false,
                                     c->margin, s->d_err, st)
             : launch_describe(s->d_frames, d_fsegs, nf, c->d_pattern, grid, false, false, st);
@@ -615,7 +616,8 @@ uslam_status uslam_server_create(uslam_ctx* ctx, const uslam_server_params* p, u
         if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->cs[b], cudaStreamNonBlocking);
     }
     if (e == cudaSuccess) e = set_compact_smem(s->max_w);
-    if (e == cudaSuccess && describe_tiled_smem(ctx->margin) > 0) e = set_describe_tiled_smem(ctx->margin);
+    if (e == cudaSuccess && ctx->describe_form == 1 && describe_tiled_smem(ctx->margin) > 0)
+        e = set_describe_tiled_smem(ctx->margin);
     if (e != cudaSuccess) {
         const std::string m = std::string("server_create: ") + cudaGetErrorString(e);
         cudaGetLastError();

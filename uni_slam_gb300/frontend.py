@@ -34,18 +34,20 @@ class Context:
     windowed matcher with its distances from tensor-core tiles) and
     detector (0: the reference's FAST + cull, 1: the cfg profile, FAST
     9-of-16 at 20/255 with 3x3 NMS); frame_cap > 0 keeps the first frame_cap
-    features of a frame in (level, order within the level) order."""
+    features of a frame in (level, order within the level) order;
+    describe_form 1 reads the describe tests from TMA-staged shared-memory
+    boxes in batches of 8+ frames (0: per-test gathers, the default)."""
 
     def __init__(self, pattern: np.ndarray, levels: int = 6, max_width: int = 4096, max_height: int = 4096,
                  cap_per_level: int = 0, device: int = 0, matcher: int = 0, ratio: float = 0.8,
-                 cell_cap: int = 0, detector: int = 0, frame_cap: int = 0):
+                 cell_cap: int = 0, detector: int = 0, frame_cap: int = 0, describe_form: int = 0):
         self.lib = capi.load()
         self._pattern = np.ascontiguousarray(pattern, dtype=np.int32).reshape(-1)
         if self._pattern.size != 1024:
             raise ValueError("pattern must hold 256 x (ax, ay, bx, by)")
         p = capi.Params(device, levels, max_width, max_height, cap_per_level,
                         self._pattern.ctypes.data_as(C.POINTER(C.c_int32)), matcher, ratio, cell_cap,
-                        detector, frame_cap)
+                        detector, frame_cap, describe_form)
         h = C.c_void_p()
         st = self.lib.uslam_create(C.byref(p), C.byref(h))
         if st != capi.OK:
