@@ -76,6 +76,8 @@ def _args():
     ap.add_argument("--stress-steps", type=int, default=5)
     ap.add_argument("--uneven", type=int, default=1, help="batched-uneven workload (0: skip)")
     ap.add_argument("--cfg", type=int, default=1, help="cfg detection/matching profile on the main workload (0: skip)")
+    ap.add_argument("--describe-form", type=int, default=0,
+                    help="describe stage of the main workload: 0 gathers, 1 TMA-staged shared-memory boxes")
     ap.add_argument("--wintc", type=int, default=1,
                     help="the main workload with the tensor-core windowed matcher, matcher 3 (0: skip)")
     ap.add_argument("--ransac", type=int, default=1, help="RANSAC hypothesis scoring on the workload's matches (0: skip)")
@@ -1108,7 +1110,7 @@ def run_ours(a):
     n = len(frames)
     # the served streams' trajectories, rendered before any GPU work
     serve_sizes, serve_frames = serve_streams(a.serve_streams, a.seed + rank) if a.serve_seconds > 0 else (None, None)
-    ctx = Context(pat, levels=LEVELS, max_width=W, max_height=H, device=local)
+    ctx = Context(pat, levels=LEVELS, max_width=W, max_height=H, device=local, describe_form=a.describe_form)
     batch = Batch(ctx, [(W, H)] * n, [(i, i + 1) for i in range(n - 1)])
     for i, f in enumerate(frames):
         batch.set_frame(i, f)
