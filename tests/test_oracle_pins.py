@@ -96,3 +96,20 @@ def test_matcher_ratio_boundary(d1, d2, expected):
     assert ref is not None or not oracle.ref_matcher_expected()
     if ref is not None:
         assert np.array_equal(got, ref(fa, k, fb, k))
+
+
+@pytest.mark.parametrize("case", [0, 1])
+def test_window_edge_pair_is_one_sided(case):
+    """At the window's x edge the two directions of FindMatches disagree in
+    f32 (tests/planted.py): the edge pair is not a match, the far pair is,
+    in the oracle and in the compiled reference."""
+    import planted
+
+    fa, ka, fb, kb = planted.window_edge_sets(case)
+    got = oracle.match(fa, ka, fb, kb, planted.W, planted.H)
+    far = [0, 1, 0, 0] if case == 0 else [0, 0, 0, 1]
+    assert got.tolist() == [far]
+    ref = oracle.ref_matcher(planted.W, planted.H)
+    assert ref is not None or not oracle.ref_matcher_expected()
+    if ref is not None:
+        assert np.array_equal(got, ref(fa, ka, fb, kb))

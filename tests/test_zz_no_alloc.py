@@ -157,6 +157,39 @@ def test_noalloc_ratio_boundary(d1, d2, expected):
     assert np.array_equal(got, em)
 
 
+@pytest.mark.parametrize("case", [0, 1])
+def test_noalloc_window_edge_pair(case):
+    """The symmetric matcher computes each pair's distance once for both
+    directions, and at the window's x edge the directions see different
+    candidates (tests/planted.py): only the far pair may match, as in the
+    oracle and the compiled reference."""
+    import torch
+
+    import oracle
+    import planted
+
+    lib = capi.load()
+    fa, ka, fb, kb = planted.window_edge_sets(case)
+    em = oracle.match(fa, ka, fb, kb, planted.W, planted.H)
+    assert len(em) == 1
+    L = planted.L
+    da = torch.from_numpy(fa.view(np.uint8).copy()).cuda()
+    db = torch.from_numpy(fb.view(np.uint8).copy()).cuda()
+    out = torch.full((L * 2 * 4,), -7, dtype=torch.int32, device="cuda")
+    counts = torch.zeros(L, dtype=torch.int32, device="cuda")
+    torch.cuda.synchronize()
+    err = C.create_string_buffer(256)
+    st = lib.uslam_match_noalloc(0, planted.W, planted.H, L, C.c_void_p(da.data_ptr()), capi.iptr(ka),
+                                 C.c_void_p(db.data_ptr()), capi.iptr(kb), C.c_void_p(out.data_ptr()),
+                                 C.c_void_p(counts.data_ptr()), 2, C.c_void_p(torch.cuda.current_stream().cuda_stream),
+                                 err, len(err))
+    assert st == capi.OK, err.value.decode()
+    o = out.cpu().numpy().reshape(L, 2, 4)
+    n = counts.cpu().numpy()
+    got = np.concatenate([o[l, :n[l]] for l in range(L)]) if n.sum() else np.zeros((0, 4), np.int32)
+    assert np.array_equal(got, em)
+
+
 def test_noalloc_rejects_records_outside_level():
     """Records whose x is not an integer inside its level are refused with
     USLAM_INVALID_ARG before any kernel indexes by them (the planted values,

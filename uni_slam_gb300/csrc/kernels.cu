@@ -1617,7 +1617,8 @@ constexpr int KM_THREADS = 256;
 
 struct MatchSegDev {
     int pair;
-    int dir;    // 0: queries = curr (b), pool = prev (a); 1: the reverse
+    int dir;    // tensor-core form: 0 queries = curr (b), pool = prev (a); 1 the reverse.
+                // k_match searches both directions from the prev queries and ignores it.
     int level;
 };
 
@@ -1643,34 +1644,92 @@ __device__ int last_col_le(float hi, float s, int w) {
     return xb;
 }
 
-// Candidates staged in shared memory per warp (32 at a time): LOD-0 y,
-// packed (level, index) and descriptor halves.
+// First xb in [0, w] with fl(fl(xb * s) + d) >= c (w if none): the first
+// column of a list whose features have LOD-0 x = c inside their own window
+// (the b -> a test of match_features_cpu.cpp:106-115 seen from a).
+__device__ int first_col_reach(float c, float d, float s, int w) {
+    int xb = (int)fminf(fmaxf(floorf((c - d) / s) - 1.0f, 0.0f), (float)w);
+    while (xb > 0 && (float)(xb - 1) * s + d >= c) --xb;
+    while (xb < w && !((float)xb * s + d >= c)) ++xb;
+    return xb;
+}
+
+// Last xb in [-1, w - 1] with fl(fl(xb * s) - d) <= c (-1 if none).
+__device__ int last_col_reach(float c, float d, float s, int w) {
+    int xb = (int)fminf(fmaxf(floorf((c + d) / s) + 1.0f, -1.0f), (float)(w - 1));
+    while (xb < w - 1 && (float)(xb + 1) * s - d <= c) ++xb;
+    while (xb >= 0 && !((float)xb * s - d <= c)) --xb;
+    return xb;
+}
+
+// Lane-wise minimum / maximum of two 16-bit keys per word.
+__device__ __forceinline__ uint32_t min_u16x2(uint32_t a, uint32_t b) {
+    uint32_t r;
+    asm("min.u16x2 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(b));
+    return r;
+}
+__device__ __forceinline__ uint32_t max_u16x2(uint32_t a, uint32_t b) {
+    uint32_t r;
+    asm("max.u16x2 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(b));
+    return r;
+}
+
+// Bits [lo, hi) of a staged batch that starts at list position base.
+__device__ __forceinline__ uint32_t range_bits(uint32_t lo, uint32_t hi, uint32_t base) {
+    const int a = (int)(max(lo, base) - base);
+    const int b = (int)(min(hi, base + 32u) > base ? min(hi, base + 32u) - base : 0u);
+    const uint32_t lo_mask = a >= 32 ? 0u : (0xffffffffu << a);
+    const uint32_t hi_mask = b >= 32 ? 0xffffffffu : ((1u << b) - 1u);
+    return lo_mask & hi_mask;
+}
+
+// One warp's staging area: 32 candidates (LOD-0 y, packed (level, index),
+// descriptor halves), the packed (level, index) of each lane's query, and the
+// batch's column keys: col[t * 32 + lane] = distance << 5 | lane for a hit of
+// slot t by lane, all ones otherwise.
 struct CandStage {
     float py[32];
     int32_t idx[32];
     uint4 d0[32], d1[32];
+    uint32_t qid[32];
+    uint16_t col[32 * 32];
 };
 
-// A warp takes 32 queries that are consecutive in x (from the query level's
-// x order) and streams the union of their spatial windows, level by level of
-// the pool, through shared memory.  Each lane's own x-window is an exact
-// index range of the x-ordered pool ([colstart[first col >= lo],
-// colstart[last col <= hi + 1])), so per staged batch a lane tests the y
-// condition only inside its range, collects the hits in a bit mask and
-// computes Hamming distances for those hits alone
-// (match_features_cpu.cpp:108-148).  The result does not depend on the
-// candidate order: a tied best always fails the ratio test.
+// The windowed mutual matcher (match_features_cpu.cpp:66-207), one Hamming
+// distance per pair of features.  Both directions of FindMatches compare the
+// same pairs: b in the window of a (a -> b, pool = the levels l - 1 .. l + 1
+// of the current set) and a in the window of b (b -> a).  So the queries of a
+// launch are the previous set's features alone, and every distance feeds
+// both searches:
+//  * a warp takes 32 queries a of one band that are consecutive in x (from
+//    the query level's x order) and streams the union of their windows, level
+//    by level of the pool, through shared memory, 32 candidates at a time;
+//  * per lane two exact index ranges of the x-ordered list: [m0, m1), the b
+//    inside a's window, and [n0, n1), the b whose window holds a (the same
+//    features except where f32 rounding at the window's x edge differs);
+//    the y test |ya - yb| <= 0.1 H0 is the same both ways;
+//  * a lane keeps a's two smallest keys (distance << 5 | slot) in registers,
+//    and writes the key distance << 5 | lane of each hit into the column of
+//    its slot; after the batch lane t folds column t into b's two smallest
+//    and merges them into b's accumulator in HBM (atomic minimum of
+//    (distance, packed a), then of the second distance), where the batches
+//    of every query group that meets b meet;
+//  * a2b is written per query group; k_mutual reads b's accumulator.
+// A tied best leaves the second distance equal to the best, which fails the
+// ratio test, so no result depends on the order of the candidates or of the
+// merges.  The pool rule (fewer than two candidates: no match) is applied to
+// a here and to b in k_mutual.
 __global__ void __launch_bounds__(KM_THREADS)
 k_match(const FrameDev* __restrict__ frames, const PairDev* __restrict__ pairs,
         const MatchSegDev* __restrict__ segs, int nseg, uint32_t* next_group) {
     __shared__ uint32_t s_pref[MAX_SEGS + 1];
     __shared__ uint32_t s_warp[33];
-    __shared__ CandStage s_stage[KM_THREADS / 32];
+    __shared__ __align__(16) CandStage s_stage[KM_THREADS / 32];
     // work units: groups of 32 queries of one band (band offsets follow the
     // query level's column tables)
     const uint32_t total = segment_prefix(nseg, s_pref, s_warp, [&](int s) {
         const PairDev& P = pairs[segs[s].pair];
-        const FrameDev& Qf = frames[segs[s].dir == 0 ? P.curr : P.prev];
+        const FrameDev& Qf = frames[P.prev];
         const int ql = segs[s].level;
         const uint32_t* qb = Qf.colstart[ql] + (size_t)USLAM_MATCH_BANDS * (size_t)(Qf.w[ql] + 1);
         uint32_t n = 0;
@@ -1682,11 +1741,18 @@ k_match(const FrameDev* __restrict__ frames, const PairDev* __restrict__ pairs,
     const int gw = blockIdx.x * (KM_THREADS / 32) + warp;
     const int nw = gridDim.x * (KM_THREADS / 32);
     CandStage& S = s_stage[warp];
+    {
+        // the column keys start empty; each column pass empties its column again
+        uint4* c = reinterpret_cast<uint4*>(S.col);
+        for (int k = lane; k < (int)(sizeof(S.col) / 16); k += 32) c[k] = make_uint4(~0u, ~0u, ~0u, ~0u);
+        __syncwarp();
+    }
     // Query groups cost very different amounts (the hits in their windows).
     // With next_group (a counter zeroed before the launch) a warp claims the
     // next group when it finishes one; without it warps take every nw-th
-    // group.  Each group writes only its own queries' results, so the order
-    // does not change them.
+    // group.  Each group writes only its own queries' a2b entries and merges
+    // into b's accumulators by atomic minima, so the order does not change
+    // the result.
     auto claim = [&](uint32_t g) -> uint32_t {
         if (!next_group) return g + (uint32_t)nw;
         uint32_t n = 0;
@@ -1698,8 +1764,8 @@ k_match(const FrameDev* __restrict__ frames, const PairDev* __restrict__ pairs,
         uint32_t grp = g - s_pref[sidx];
         const MatchSegDev sg = segs[sidx];
         const PairDev& P = pairs[sg.pair];
-        const FrameDev& Q = frames[sg.dir == 0 ? P.curr : P.prev];
-        const FrameDev& B = frames[sg.dir == 0 ? P.prev : P.curr];
+        const FrameDev& Q = frames[P.prev];
+        const FrameDev& B = frames[P.curr];
         const int l = sg.level;
         const uint32_t* qband = Q.colstart[l] + (size_t)USLAM_MATCH_BANDS * (size_t)(Q.w[l] + 1);
         int band = 0;
@@ -1716,97 +1782,164 @@ k_match(const FrameDev* __restrict__ frames, const PairDev* __restrict__ pairs,
         const float cy = (float)(uint32_t)__uint_as_float(qrec[1]) * ql;
         const uint4 qd0 = *reinterpret_cast<const uint4*>(qrec + 4);
         const uint4 qd1 = *reinterpret_cast<const uint4*>(qrec + 8);
-        const float lo = cx - P.max_dx, hi = cx + P.max_dx;
-        const float dy = P.max_dy;
+        const float dx = P.max_dx, dy = P.max_dy;
+        const float lo = cx - dx, hi = cx + dx;
+        S.qid[lane] = (uint32_t)USLAM_PACK(l, qi);
+        __syncwarp();
 
-        // best / second-best as keys (distance << 5 | slot); a tie on the best
-        // distance leaves second >> 5 == best >> 5, which fails the ratio test
+        // a's best / second-best as keys (distance << 5 | slot); a tie on the
+        // best distance leaves second >> 5 == best >> 5, which fails the test
         uint32_t bestk = 0xffffffffu, secondk = 0xffffffffu;
         int32_t bidx = -1;
         const int L = B.levels;
-        uint32_t pool = B.kept[l];
-        if (l > 0) pool += B.kept[l - 1];
-        if (l + 1 < L) pool += B.kept[l + 1];
-        if (pool >= 2u) {
-            for (int k = 0; k < 3; ++k) {
-                const int pl = k == 0 ? l : (k == 1 ? l - 1 : l + 1);
-                if (pl < 0 || pl >= L) continue;
-                const float ps = lod_scale(pl);
-                const int wpl = B.w[pl];
-                // the pool's candidate list of this band
-                const uint32_t* colstart = B.colstart[pl] + (size_t)band * (size_t)(wpl + 1);
-                // this lane's exact candidate range
-                uint32_t m0 = 0u, m1 = 0u;
-                if (valid) {
-                    const int xlo = first_col_ge(lo, ps, wpl);
-                    const int xhi = last_col_le(hi, ps, wpl);
-                    if (xlo <= xhi) {
-                        m0 = __ldg(colstart + xlo);
-                        m1 = __ldg(colstart + xhi + 1);
-                    }
+        uint4* const bacc = P.bacc;
+        const size_t capb = (size_t)(B.cap > 0 ? B.cap : 1);
+        uint16_t* const colq = S.col + lane;  // this lane's key of slot t at colq[32 t]
+        for (int k = 0; k < 3; ++k) {
+            const int pl = k == 0 ? l : (k == 1 ? l - 1 : l + 1);
+            if (pl < 0 || pl >= L) continue;
+            const float ps = lod_scale(pl);
+            const int wpl = B.w[pl];
+            // the pool's candidate list of this band
+            const uint32_t* colstart = B.colstart[pl] + (size_t)band * (size_t)(wpl + 1);
+            uint32_t m0 = 0u, m1 = 0u, n0 = 0u, n1 = 0u;
+            if (valid) {
+                int xlo = first_col_ge(lo, ps, wpl), xhi = last_col_le(hi, ps, wpl);
+                if (xlo <= xhi) {
+                    m0 = __ldg(colstart + xlo);
+                    m1 = __ldg(colstart + xhi + 1);
                 }
-                // union over the warp (lanes are x-sorted, so this is contiguous)
-                uint32_t c0 = m0 < m1 ? m0 : 0xffffffffu, c1 = m1;
-#pragma unroll
-                for (int o = 16; o > 0; o >>= 1) {
-                    c0 = min(c0, __shfl_xor_sync(0xffffffffu, c0, o));
-                    c1 = max(c1, __shfl_xor_sync(0xffffffffu, c1, o));
+                xlo = first_col_reach(cx, dx, ps, wpl);
+                xhi = last_col_reach(cx, dx, ps, wpl);
+                if (xlo <= xhi) {
+                    n0 = __ldg(colstart + xlo);
+                    n1 = __ldg(colstart + xhi + 1);
                 }
-                if (c0 >= c1) continue;
-                const uint32_t* xorder = B.xorder[pl] + (size_t)band * (size_t)(B.cap > 0 ? B.cap : 1);
-                const uint32_t* feats = B.feats[pl];
-                for (uint32_t base = c0; base < c1; base += 32u) {
-                    const uint32_t kk = base + (uint32_t)lane;
-                    if (kk < c1) {
-                        const uint32_t j = __ldg(xorder + kk);
-                        const uint32_t* rec = feats + (size_t)j * 12u;
-                        S.py[lane] = (float)(uint32_t)__uint_as_float(__ldg(rec + 1)) * ps;
-                        S.idx[lane] = USLAM_PACK(pl, j);
-                        S.d0[lane] = __ldg(reinterpret_cast<const uint4*>(rec + 4));
-                        S.d1[lane] = __ldg(reinterpret_cast<const uint4*>(rec + 8));
-                    }
-                    __syncwarp();
-                    const int a = (int)(max(m0, base) - base);
-                    const int b = (int)(min(m1, base + 32u) > base ? min(m1, base + 32u) - base : 0u);
-                    // y test of all 32 staged candidates (unrolled, float4 loads),
-                    // masked by this lane's slots [a, b)
-                    uint32_t ymask = 0u;
-                    const float4* py4 = reinterpret_cast<const float4*>(S.py);
+            }
+            // union over both ranges and the warp (lanes are x-sorted, so it is contiguous)
+            uint32_t c0 = min(m0 < m1 ? m0 : 0xffffffffu, n0 < n1 ? n0 : 0xffffffffu);
+            uint32_t c1 = max(m0 < m1 ? m1 : 0u, n0 < n1 ? n1 : 0u);
 #pragma unroll
-                    for (int q = 0; q < 8; ++q) {
-                        const float4 v = py4[q];
-                        ymask |= (!(fabsf(cy - v.x) > dy) ? 1u : 0u) << (4 * q);
-                        ymask |= (!(fabsf(cy - v.y) > dy) ? 1u : 0u) << (4 * q + 1);
-                        ymask |= (!(fabsf(cy - v.z) > dy) ? 1u : 0u) << (4 * q + 2);
-                        ymask |= (!(fabsf(cy - v.w) > dy) ? 1u : 0u) << (4 * q + 3);
-                    }
-                    const uint32_t lo_mask = a >= 32 ? 0u : (0xffffffffu << a);
-                    const uint32_t hi_mask = b >= 32 ? 0xffffffffu : ((1u << b) - 1u);
-                    uint32_t hits = ymask & lo_mask & hi_mask;
-                    // keys (distance << 5 | batch slot): min/max keep the two
-                    // smallest distances without branches; the slot of the best
-                    // is resolved to its candidate once per batch
-                    const uint32_t prev = bestk;
-                    while (hits) {
-                        const int t = 31 - __clz(hits);
-                        hits ^= 1u << t;
+            for (int o = 16; o > 0; o >>= 1) {
+                c0 = min(c0, __shfl_xor_sync(0xffffffffu, c0, o));
+                c1 = max(c1, __shfl_xor_sync(0xffffffffu, c1, o));
+            }
+            if (c0 >= c1) continue;
+            const uint32_t* xorder = B.xorder[pl] + (size_t)band * (size_t)(B.cap > 0 ? B.cap : 1);
+            const uint32_t* feats = B.feats[pl];
+            for (uint32_t base = c0; base < c1; base += 32u) {
+                const uint32_t kk = base + (uint32_t)lane;
+                if (kk < c1) {
+                    const uint32_t j = __ldg(xorder + kk);
+                    const uint32_t* rec = feats + (size_t)j * 12u;
+                    S.py[lane] = (float)(uint32_t)__uint_as_float(__ldg(rec + 1)) * ps;
+                    S.idx[lane] = USLAM_PACK(pl, j);
+                    S.d0[lane] = __ldg(reinterpret_cast<const uint4*>(rec + 4));
+                    S.d1[lane] = __ldg(reinterpret_cast<const uint4*>(rec + 8));
+                }
+                __syncwarp();
+                // y test of all 32 staged candidates (unrolled, float4 loads);
+                // slots past the list's end lie outside both ranges
+                uint32_t ymask = 0u;
+                const float4* py4 = reinterpret_cast<const float4*>(S.py);
+#pragma unroll
+                for (int q = 0; q < 8; ++q) {
+                    const float4 v = py4[q];
+                    ymask |= (!(fabsf(cy - v.x) > dy) ? 1u : 0u) << (4 * q);
+                    ymask |= (!(fabsf(cy - v.y) > dy) ? 1u : 0u) << (4 * q + 1);
+                    ymask |= (!(fabsf(cy - v.z) > dy) ? 1u : 0u) << (4 * q + 2);
+                    ymask |= (!(fabsf(cy - v.w) > dy) ? 1u : 0u) << (4 * q + 3);
+                }
+                const uint32_t h1 = ymask & range_bits(m0, m1, base);  // b in a's window
+                const uint32_t h0 = ymask & range_bits(n0, n1, base);  // a in b's window
+                const uint32_t prev = bestk;
+                uint32_t hb = h1 & h0;
+                while (hb) {
+                    const int t = 31 - __clz(hb);
+                    hb ^= 1u << t;
+                    const uint32_t d = hamming256(S.d0[t], S.d1[t], qd0, qd1);
+                    const uint32_t key = (d << 5) | (uint32_t)t;
+                    secondk = min(secondk, max(bestk, key));
+                    bestk = min(bestk, key);
+                    colq[32 * t] = (uint16_t)((d << 5) | (uint32_t)lane);
+                }
+                // pairs inside one direction's window only (rare)
+                uint32_t o1 = h1 & ~h0, o0 = h0 & ~h1;
+                if (__any_sync(0xffffffffu, (o1 | o0) != 0u)) {
+                    while (o1) {
+                        const int t = 31 - __clz(o1);
+                        o1 ^= 1u << t;
                         const uint32_t key = (hamming256(S.d0[t], S.d1[t], qd0, qd1) << 5) | (uint32_t)t;
                         secondk = min(secondk, max(bestk, key));
                         bestk = min(bestk, key);
                     }
-                    if (bestk != prev) bidx = S.idx[bestk & 31u];
-                    __syncwarp();
+                    while (o0) {
+                        const int t = 31 - __clz(o0);
+                        o0 ^= 1u << t;
+                        colq[32 * t] = (uint16_t)((hamming256(S.d0[t], S.d1[t], qd0, qd1) << 5) | (uint32_t)lane);
+                    }
                 }
+                if (bestk != prev) bidx = S.idx[bestk & 31u];
+                __syncwarp();
+                // column pass: lane t folds the keys of slot t into the two
+                // smallest (two 16-bit lanes at a time), empties the column
+                // and merges the pair into b's accumulator
+                if (kk < c1) {
+                    uint4* colt = reinterpret_cast<uint4*>(S.col + 32 * lane);
+                    uint32_t b2 = 0xffffffffu, s2 = 0xffffffffu;
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) {
+                        const uint4 v = colt[q];
+                        colt[q] = make_uint4(~0u, ~0u, ~0u, ~0u);
+                        s2 = min_u16x2(s2, max_u16x2(b2, v.x));
+                        b2 = min_u16x2(b2, v.x);
+                        s2 = min_u16x2(s2, max_u16x2(b2, v.y));
+                        b2 = min_u16x2(b2, v.y);
+                        s2 = min_u16x2(s2, max_u16x2(b2, v.z));
+                        b2 = min_u16x2(b2, v.z);
+                        s2 = min_u16x2(s2, max_u16x2(b2, v.w));
+                        b2 = min_u16x2(b2, v.w);
+                    }
+                    const uint32_t bl = b2 & 0xffffu, bh = b2 >> 16;
+                    const uint32_t cb = min(bl, bh);
+                    const uint32_t cs = min(max(bl, bh), min(s2 & 0xffffu, s2 >> 16));
+                    if (cb != 0xffffu) {
+                        const unsigned long long key =
+                            ((unsigned long long)(cb >> 5) << 32) | (unsigned long long)S.qid[cb & 31u];
+                        const int32_t id = S.idx[lane];
+                        uint4* acc = bacc + (size_t)USLAM_PACK_LEVEL(id) * capb + (size_t)USLAM_PACK_INDEX(id);
+                        const unsigned long long old = atomicMin(reinterpret_cast<unsigned long long*>(acc), key);
+                        // the larger of the old best and this best joins the
+                        // second-best candidates
+                        const uint32_t lose = (uint32_t)((old > key ? old : key) >> 32);
+                        atomicMin(&acc->z, min(lose, cs == 0xffffu ? 0xffffffffu : cs >> 5));
+                    }
+                }
+                __syncwarp();
             }
         }
         if (valid) {
+            uint32_t pool = B.kept[l];
+            if (l > 0) pool += B.kept[l - 1];
+            if (l + 1 < L) pool += B.kept[l + 1];
             int32_t res = -1;
-            if (bidx >= 0 && (float)(bestk >> 5) < 0.85f * (float)(secondk >> 5)) res = bidx;
-            const int capq = Q.cap;
-            if (sg.dir == 0) P.b2a[(size_t)l * capq + qi] = res;
-            else P.a2b[(size_t)l * capq + qi] = res;
+            if (pool >= 2u && bidx >= 0 && (float)(bestk >> 5) < 0.85f * (float)(secondk >> 5)) res = bidx;
+            P.a2b[(size_t)l * Q.cap + qi] = res;
         }
     }
+}
+
+// b's accumulators start empty (all ones) before every k_match launch: one
+// CTA per (pair, level of b).
+__global__ void __launch_bounds__(256)
+k_bacc_init(const FrameDev* __restrict__ frames, const PairDev* __restrict__ pairs, const SegDev* __restrict__ segs) {
+    const int pi = segs[blockIdx.x].frame;  // pair index
+    const int l = segs[blockIdx.x].level;
+    const PairDev& P = pairs[pi];
+    const FrameDev& B = frames[P.curr];
+    const uint32_t n = B.kept[l];
+    uint4* acc = P.bacc + (size_t)l * (size_t)(B.cap > 0 ? B.cap : 1);
+    for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) acc[i] = make_uint4(~0u, ~0u, ~0u, ~0u);
 }
 
 // ----------------------------------------------------- brute force ----
@@ -1993,7 +2126,21 @@ k_mutual(const FrameDev* __restrict__ frames, const PairDev* __restrict__ pairs,
             }
             if (m >= 0) {
                 const int bl = USLAM_PACK_LEVEL(m), bi = USLAM_PACK_INDEX(m);
-                ok = !MUTUAL || P.b2a[(size_t)bl * B.cap + bi] == USLAM_PACK(l, i);
+                if (!MUTUAL) {
+                    ok = true;
+                } else if (P.bacc) {
+                    // b's search from its accumulator (k_match): the pool rule
+                    // over a's levels bl - 1 .. bl + 1, the ratio test, and
+                    // its nearest a is this a
+                    const uint4 e = P.bacc[(size_t)bl * B.cap + bi];
+                    uint32_t pool = A.kept[bl];
+                    if (bl > 0) pool += A.kept[bl - 1];
+                    if (bl + 1 < A.levels) pool += A.kept[bl + 1];
+                    ok = pool >= 2u && e.y != 0xffffffffu && (float)e.y < 0.85f * (float)e.z &&
+                         e.x == (uint32_t)USLAM_PACK(l, i);
+                } else {
+                    ok = P.b2a[(size_t)bl * B.cap + bi] == USLAM_PACK(l, i);
+                }
             }
         }
         uint32_t tot;
@@ -2147,6 +2294,13 @@ cudaError_t launch_match_dyn(const FrameDev* frames, const PairDev* pairs, const
                              uint32_t* next_group, cudaStream_t st) {
     if (nseg <= 0) return cudaSuccess;
     k_match<<<grid, KM_THREADS, 0, st>>>(frames, pairs, static_cast<const MatchSegDev*>(segs), nseg, next_group);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_bacc_init(const FrameDev* frames, const PairDev* pairs, const SegDev* segs, int nseg,
+                             cudaStream_t st) {
+    if (nseg <= 0) return cudaSuccess;
+    k_bacc_init<<<nseg, 256, 0, st>>>(frames, pairs, segs);
     return cudaGetLastError();
 }
 

@@ -28,6 +28,7 @@ struct MatchSegDev {
 };
 cudaError_t launch_match(const FrameDev*, const PairDev*, const void*, int, int, cudaStream_t);
 cudaError_t launch_mutual(const FrameDev*, const PairDev*, const SegDev*, int, uint32_t*, cudaStream_t);
+cudaError_t launch_bacc_init(const FrameDev*, const PairDev*, const SegDev*, int, cudaStream_t);
 cudaError_t launch_xsort(const FrameDev*, const SegDev*, int, int, cudaStream_t);
 cudaError_t set_compact_smem(int max_w);
 }  // namespace uslam
@@ -50,7 +51,7 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoallocScratch
 struct NoallocTables {
     FrameDev frames[2];
     PairDev pair;
-    MatchSegDev msegs[2 * USLAM_MAX_LEVELS];
+    MatchSegDev msegs[USLAM_MAX_LEVELS];
     SegDev usegs[USLAM_MAX_LEVELS];
     SegDev xsegs[2 * USLAM_MAX_LEVELS];
     uint32_t counts[2][2 * USLAM_MAX_LEVELS];  // per frame: kept[levels], raw[levels]
@@ -192,7 +193,8 @@ extern "C" uslam_status uslam_match_noalloc(int device, int width, int height, i
     if (out_cap_per_level < cap[0])
         return fail(err, err_len, USLAM_INVALID_ARG, "match_noalloc: out_cap_per_level below the previous set's largest level");
 
-    // scratch layout: [tables][xorder, qorder f0][xorder, qorder f1][colstart f0][colstart f1][a2b][b2a][error]
+    // scratch layout: [tables][xorder, qorder f0][xorder, qorder f1][colstart f0][colstart f1][a2b][b -> a
+    // accumulators][error]
     // (per level: USLAM_MATCH_BANDS candidate lists of cap entries, the query order, and per band
     // the column table, then the band offsets)
     size_t cur = align256(sizeof(NoallocTables));
@@ -211,8 +213,8 @@ extern "C" uslam_status uslam_match_noalloc(int device, int width, int height, i
     }
     const size_t a2b_off = cur;
     cur = align256(cur + sizeof(int32_t) * static_cast<size_t>(levels) * cap[0]);
-    const size_t b2a_off = cur;
-    cur = align256(cur + sizeof(int32_t) * static_cast<size_t>(levels) * cap[1]);
+    const size_t bacc_off = cur;
+    cur = align256(cur + 16u * static_cast<size_t>(levels) * cap[1]);
     const size_t err_off = cur;
     cur += 256;
     if (cur > kNoallocScratchBytes) {
@@ -260,7 +262,7 @@ extern "C" uslam_status uslam_match_noalloc(int device, int width, int height, i
     P.prev = 0;
     P.curr = 1;
     P.a2b = reinterpret_cast<int32_t*>(base + a2b_off);
-    P.b2a = reinterpret_cast<int32_t*>(base + b2a_off);
+    P.bacc = reinterpret_cast<uint4*>(base + bacc_off);
     P.matches = reinterpret_cast<int32_t*>(out);
     P.match_count = out_counts;
     P.max_matches_per_level = out_cap_per_level;
@@ -268,8 +270,7 @@ extern "C" uslam_status uslam_match_noalloc(int device, int width, int height, i
     P.max_dx = 0.1f * static_cast<float>(static_cast<uint32_t>(width));
     P.max_dy = 0.1f * static_cast<float>(static_cast<uint32_t>(height));
     for (int l = 0; l < levels; ++l) {
-        t.msegs[2 * l] = MatchSegDev{0, 0, l};
-        t.msegs[2 * l + 1] = MatchSegDev{0, 1, l};
+        t.msegs[l] = MatchSegDev{0, 1, l};  // both directions from the previous set's queries
         t.usegs[l] = SegDev{0, l};
     }
 
@@ -294,7 +295,8 @@ extern "C" uslam_status uslam_match_noalloc(int device, int width, int height, i
         e = set_compact_smem(max_w);  // a function attribute, not an allocation
         if (e == cudaSuccess) e = launch_xsort(dtab->frames, dtab->xsegs, 2 * levels, max_w, st);
     }
-    if (e == cudaSuccess) e = launch_match(dtab->frames, &dtab->pair, dtab->msegs, 2 * levels, ds.num_sms * 4, st);
+    if (e == cudaSuccess) e = launch_bacc_init(dtab->frames, &dtab->pair, dtab->usegs, levels, st);
+    if (e == cudaSuccess) e = launch_match(dtab->frames, &dtab->pair, dtab->msegs, levels, ds.num_sms * 4, st);
     if (e == cudaSuccess) e = launch_mutual(dtab->frames, &dtab->pair, dtab->usegs, levels, derr, st);
     uint32_t word = 0;
     if (e == cudaSuccess) e = cudaMemcpyAsync(&word, derr, sizeof word, cudaMemcpyDeviceToHost, st);

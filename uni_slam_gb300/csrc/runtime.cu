@@ -135,7 +135,9 @@ uslam_status build_program(uslam_batch* b, const std::vector<int>& fr, const std
     for (int p : pr) {
         psegs.push_back(SegDev{p, 0});
         for (int l = 0; l < b->levels; ++l) {
-            msegs.push_back(MatchSegDev{p, 0, l});
+            // k_match searches both directions from the prev set's queries;
+            // the tensor-core form takes each direction as its own segment
+            if (b->win_tc) msegs.push_back(MatchSegDev{p, 0, l});
             msegs.push_back(MatchSegDev{p, 1, l});
             usegs.push_back(SegDev{p, l});
         }
@@ -241,6 +243,7 @@ cudaError_t enqueue_pairs(uslam_batch* b, const Program& P, const Lane& ln) {
             return e;
         return launch_mutual(b->d_frames, b->d_pairs, P.usegs, P.nusegs, b->d_err, ln.st);
     }
+    if ((e = launch_bacc_init(b->d_frames, b->d_pairs, P.usegs, P.nusegs, ln.st)) != cudaSuccess) return e;
     if ((e = launch_match_dyn(b->d_frames, b->d_pairs, P.msegs, P.nmsegs, c->num_sms * kMatchCtasPerSm,
                               ln.next_group, ln.st)) != cudaSuccess)
         return e;
@@ -442,6 +445,10 @@ uslam_status create_batch(uslam_ctx* ctx, int n_frames, const int* widths, const
     b->pairs.resize(n_pairs);
     b->pair_off.resize(n_pairs);
     std::vector<std::pair<size_t, size_t>> dirs(n_pairs);
+    // k_match (matcher 0 without the tensor-core form) searches b -> a into
+    // per-feature accumulators instead of b2a
+    const bool sym_match = ctx->matcher == 0 && !b->win_tc;
+    std::vector<size_t> bacc_off(n_pairs, 0);
     for (int p = 0; p < n_pairs; ++p) {
         const int a = pair_prev[p], c = pair_curr[p];
         if (a < 0 || a >= n_frames || c < 0 || c >= n_frames || a == c) {
@@ -464,6 +471,7 @@ uslam_status create_batch(uslam_ctx* ctx, int n_frames, const int* widths, const
         b->pair_off[p] = take(&out_bytes, round_up(sizeof(uint32_t) * L, 16) + static_cast<size_t>(L) * capa * 16);
         dirs[p].first = take(&scratch, static_cast<size_t>(L) * capa * 4);
         dirs[p].second = take(&scratch, static_cast<size_t>(L) * capc * 4);
+        if (sym_match) bacc_off[p] = take(&scratch, static_cast<size_t>(L) * capc * 16);
         P.bf_splits = 1;
         P.bf_ratio = ctx->ratio;
     }
@@ -601,6 +609,7 @@ uslam_status create_batch(uslam_ctx* ctx, int n_frames, const int* widths, const
         P.matches = reinterpret_cast<int32_t*>(out_base + b->pair_off[p] + round_up(sizeof(uint32_t) * L, 16));
         P.a2b = reinterpret_cast<int32_t*>(sc_base + dirs[p].first);
         P.b2a = reinterpret_cast<int32_t*>(sc_base + dirs[p].second);
+        P.bacc = sym_match ? reinterpret_cast<uint4*>(sc_base + bacc_off[p]) : nullptr;
         P.bf_part = P.bf_splits > 1 ? reinterpret_cast<uint32_t*>(sc_base + bf_off[p]) : nullptr;
     }
     b->d_err = reinterpret_cast<uint32_t*>(sc_base + err_off);
@@ -1050,6 +1059,8 @@ uslam_status uslam_batch_profile(uslam_batch* b, int iters, float* kernel_ms) {
         if (e == cudaSuccess)
             e = describe_stage(b, P, b->stream);
         mark();
+        if (e == cudaSuccess && c->matcher == 0 && !b->win_tc)
+            e = launch_bacc_init(b->d_frames, b->d_pairs, P.usegs, P.nusegs, b->stream);
         if (e == cudaSuccess)
             e = c->matcher == 1 ? launch_bruteforce(b->d_frames, b->d_pairs, P.psegs, P.npsegs, c->ratio, grid, b->stream)
                 : c->matcher == 2

@@ -42,6 +42,7 @@ cudaError_t set_describe_tiled_smem(int margin);
 cudaError_t launch_match(const FrameDev*, const PairDev*, const void*, int, int, cudaStream_t);
 cudaError_t launch_match_dyn(const FrameDev*, const PairDev*, const void*, int, int, uint32_t*, cudaStream_t);
 cudaError_t launch_mutual(const FrameDev*, const PairDev*, const SegDev*, int, uint32_t*, cudaStream_t);
+cudaError_t launch_bacc_init(const FrameDev*, const PairDev*, const SegDev*, int, cudaStream_t);
 cudaError_t launch_mutual_reset(const FrameDev*, const PairDev*, const SegDev*, int, uint32_t*, uint32_t*,
                                 cudaStream_t);
 cudaError_t launch_emit(const FrameDev*, const PairDev*, const SegDev*, int, uint32_t*, cudaStream_t);

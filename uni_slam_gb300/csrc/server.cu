@@ -51,7 +51,7 @@ struct SrvSlot {
     int producer_launch = -1;  // in-flight launch that writes its features, or -1
     uint8_t* h_in = nullptr;   // pinned staging of the frame
     int32_t* a2b = nullptr;    // pair scratch when this slot is the current frame
-    int32_t* b2a = nullptr;
+    uint4* bacc = nullptr;     // k_match's b -> a accumulators when this slot is the current frame
     int32_t* matches = nullptr;
     uint32_t* match_count = nullptr;
     uint32_t* h_res = nullptr;  // pinned, mapped: the frame's results as the emit kernel lays them out
@@ -269,7 +269,7 @@ cudaError_t launch_batch(uslam_server* s, const std::vector<uint64_t>& tickets, 
             P.prev = r.ref;
             P.curr = r.slot;
             P.a2b = sl.a2b;
-            P.b2a = sl.b2a;
+            P.bacc = sl.bacc;
             P.matches = sl.matches;
             P.match_count = sl.match_count;
             P.max_matches_per_level = std::max(s->frames[r.ref].cap, 1);
@@ -278,8 +278,7 @@ cudaError_t launch_batch(uslam_server* s, const std::vector<uint64_t>& tickets, 
             const int pi = static_cast<int>(pairs.size());
             pairs.push_back(P);
             for (int l = 0; l < lv; ++l) {
-                msegs.push_back(MatchSegDev{pi, 0, l});
-                msegs.push_back(MatchSegDev{pi, 1, l});
+                msegs.push_back(MatchSegDev{pi, 1, l});  // both directions from the keyframe's queries
                 usegs.push_back(SegDev{pi, l});
             }
         }
@@ -330,6 +329,8 @@ cudaError_t launch_batch(uslam_server* s, const std::vector<uint64_t>& tickets, 
             : launch_describe(s->d_frames, d_fsegs, nf, c->d_pattern, grid, false, false, st);
     if (e != cudaSuccess) return e;
     if (!pairs.empty()) {
+        if ((e = launch_bacc_init(s->d_frames, d_pairs, d_usegs, static_cast<int>(usegs.size()), st)) != cudaSuccess)
+            return e;
         if ((e = launch_match(s->d_frames, d_pairs, d_msegs, static_cast<int>(msegs.size()), grid, st)) != cudaSuccess)
             return e;
         if ((e = launch_mutual(s->d_frames, d_pairs, d_usegs, static_cast<int>(usegs.size()), s->d_err, st)) !=
@@ -447,7 +448,7 @@ uslam_status uslam_server_create(uslam_ctx* ctx, const uslam_server_params* p, u
     // slot bytes per class, then slots per class from an equal share of the budget
     struct SlotLayout {
         size_t bytes, in, counts, lvl[USLAM_MAX_LEVELS], blur[USLAM_MAX_LEVELS], kpmap[USLAM_MAX_LEVELS],
-            feats[USLAM_MAX_LEVELS], xorder[USLAM_MAX_LEVELS], colstart[USLAM_MAX_LEVELS], qorder[USLAM_MAX_LEVELS], bands[USLAM_MAX_LEVELS], a2b, b2a, matches, mcount,
+            feats[USLAM_MAX_LEVELS], xorder[USLAM_MAX_LEVELS], colstart[USLAM_MAX_LEVELS], qorder[USLAM_MAX_LEVELS], bands[USLAM_MAX_LEVELS], a2b, bacc, matches, mcount,
             tmaps;
     };
     std::vector<SlotLayout> lay(p->n_sizes);
@@ -516,7 +517,7 @@ uslam_status uslam_server_create(uslam_ctx* ctx, const uslam_server_params* p, u
                 }
             }
         Y.a2b = take(static_cast<size_t>(L) * capa * 4);
-        Y.b2a = take(static_cast<size_t>(L) * capa * 4);
+        Y.bacc = take(static_cast<size_t>(L) * capa * 16);
         Y.matches = take(static_cast<size_t>(L) * capa * 16);
         Y.mcount = take(sizeof(uint32_t) * L);
         Y.tmaps = take(static_cast<size_t>(L) * USLAM_TMAPS_PER_LEVEL * USLAM_TMAP_BYTES);
@@ -591,7 +592,7 @@ uslam_status uslam_server_create(uslam_ctx* ctx, const uslam_server_params* p, u
             SrvSlot& sl = s->slots[g];
             sl.cls = k;
             sl.a2b = reinterpret_cast<int32_t*>(base + Y.a2b);
-            sl.b2a = reinterpret_cast<int32_t*>(base + Y.b2a);
+            sl.bacc = reinterpret_cast<uint4*>(base + Y.bacc);
             sl.matches = reinterpret_cast<int32_t*>(base + Y.matches);
             sl.match_count = reinterpret_cast<uint32_t*>(base + Y.mcount);
             if (e == cudaSuccess) e = cudaHostAlloc(&sl.h_in, static_cast<size_t>(F.H0) * F.img_pitch, cudaHostAllocDefault);

@@ -35,6 +35,7 @@
 #pragma once
 
 #include <stdint.h>
+#include <vector_types.h>
 
 #define USLAM_MAX_LEVELS 12
 #define USLAM_MATCH_BANDS 3  // horizontal bands of the frame for the matcher's lists
@@ -103,7 +104,13 @@ struct FrameDev {
 struct PairDev {
     int prev, curr;         // frame indices in the batch
     int32_t* a2b;           // [levels * cap_prev]: prev feature -> packed curr feature or -1
-    int32_t* b2a;           // [levels * cap_curr]
+    int32_t* b2a;           // [levels * cap_curr] (the tensor-core windowed matcher)
+    // k_match's search of each curr feature b (levels * cap_curr entries of
+    // 16 bytes): .x = packed (level, index) and .y = distance of its nearest
+    // prev feature, .z = its second-smallest distance; all ones = none.
+    // Merged by atomic minima (.x/.y as one 64-bit word); null with the
+    // other matchers.
+    uint4* bacc;
     int32_t* matches;       // 4 ints per match (lod_a, idx_a, lod_b, idx_b)
     uint32_t* match_count;  // [levels] matches whose a lies in that level
     int max_matches_per_level;
