@@ -296,7 +296,7 @@ extern "C" uslam_status uslam_match_noalloc(int device, int width, int height, i
         if (e == cudaSuccess) e = launch_xsort(dtab->frames, dtab->xsegs, 2 * levels, max_w, st);
     }
     if (e == cudaSuccess) e = launch_bacc_init(dtab->frames, &dtab->pair, dtab->usegs, levels, st);
-    if (e == cudaSuccess) e = launch_match(dtab->frames, &dtab->pair, dtab->msegs, levels, ds.num_sms * 4, st);
+    if (e == cudaSuccess) e = launch_match(dtab->frames, &dtab->pair, dtab->msegs, levels, ds.num_sms, st);
     if (e == cudaSuccess) e = launch_mutual(dtab->frames, &dtab->pair, dtab->usegs, levels, derr, st);
     uint32_t word = 0;
     if (e == cudaSuccess) e = cudaMemcpyAsync(&word, derr, sizeof word, cudaMemcpyDeviceToHost, st);

@@ -39,8 +39,10 @@ size_t describe_tiled_smem(int margin);
 // k_describe_tiled (one frame measured 0.09 ms longer than with k_describe).
 constexpr int kTiledDescribeFrames = 8;
 cudaError_t set_describe_tiled_smem(int margin);
-cudaError_t launch_match(const FrameDev*, const PairDev*, const void*, int, int, cudaStream_t);
-cudaError_t launch_match_dyn(const FrameDev*, const PairDev*, const void*, int, int, uint32_t*, cudaStream_t);
+// k_match over num_sms x its resident CTAs; _dyn: its warps claim query groups from next_group
+cudaError_t launch_match(const FrameDev*, const PairDev*, const void* segs, int nseg, int num_sms, cudaStream_t);
+cudaError_t launch_match_dyn(const FrameDev*, const PairDev*, const void* segs, int nseg, int num_sms,
+                             uint32_t* next_group, cudaStream_t);
 cudaError_t launch_mutual(const FrameDev*, const PairDev*, const SegDev*, int, uint32_t*, cudaStream_t);
 cudaError_t launch_bacc_init(const FrameDev*, const PairDev*, const SegDev*, int, cudaStream_t);
 cudaError_t launch_mutual_reset(const FrameDev*, const PairDev*, const SegDev*, int, uint32_t*, uint32_t*,

@@ -331,7 +331,8 @@ cudaError_t launch_batch(uslam_server* s, const std::vector<uint64_t>& tickets, 
     if (!pairs.empty()) {
         if ((e = launch_bacc_init(s->d_frames, d_pairs, d_usegs, static_cast<int>(usegs.size()), st)) != cudaSuccess)
             return e;
-        if ((e = launch_match(s->d_frames, d_pairs, d_msegs, static_cast<int>(msegs.size()), grid, st)) != cudaSuccess)
+        if ((e = launch_match(s->d_frames, d_pairs, d_msegs, static_cast<int>(msegs.size()), c->num_sms, st)) !=
+            cudaSuccess)
             return e;
         if ((e = launch_mutual(s->d_frames, d_pairs, d_usegs, static_cast<int>(usegs.size()), s->d_err, st)) !=
             cudaSuccess)
