@@ -368,7 +368,7 @@ typedef struct uslam_server_params {
     const int* widths;        /* [n_sizes] */
     const int* heights;       /* [n_sizes] */
     size_t hbm_budget_bytes;  /* device memory for frame slots, shared equally by the size classes */
-    int max_batch;            /* most frames one launch takes */
+    int max_batch;            /* most frames one launch takes (max_batch x levels <= 2048) */
 } uslam_server_params;
 
 /* Frame slots (pyramid, features, keyframe pair scratch) are carved from the

@@ -1691,13 +1691,30 @@ __device__ __forceinline__ uint32_t range_bits(uint32_t lo, uint32_t hi, uint32_
 // descriptor halves), the packed (level, index) of each lane's query, and the
 // batch's column keys: col[t * 32 + lane] = distance << 5 | lane for a hit of
 // slot t by lane, all ones otherwise.
-struct CandStage {
+struct CandBuf {
     float py[32];
     int32_t idx[32];
     uint4 d0[32], d1[32];
+};
+struct CandStage {
+    CandBuf buf[2];
     uint32_t qid[32];
     uint16_t col[32 * 32];
 };
+constexpr int KM_MAX_SEGS = USLAM_MAX_MATCH_SEGS;
+
+__device__ __forceinline__ void cp_async4(void* smem, const void* gmem) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"((uint32_t)__cvta_generic_to_shared(smem)), "l"(gmem)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"((uint32_t)__cvta_generic_to_shared(smem)),
+                 "l"(gmem)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
 
 // The windowed mutual matcher (match_features_cpu.cpp:66-207), one Hamming
 // distance per pair of features.  Both directions of FindMatches compare the
@@ -1707,7 +1724,8 @@ struct CandStage {
 // both searches:
 //  * a warp takes 32 queries a of one band that are consecutive in x (from
 //    the query level's x order) and streams the union of their windows, level
-//    by level of the pool, through shared memory, 32 candidates at a time;
+//    by level of the pool, through shared memory, 32 candidates at a time
+//    (asynchronous copies, one batch ahead);
 //  * per lane two exact index ranges of the x-ordered list: [m0, m1), the b
 //    inside a's window, and [n0, n1), the b whose window holds a (the same
 //    features except where f32 rounding at the window's x edge differs);
@@ -1726,7 +1744,7 @@ struct CandStage {
 __global__ void __launch_bounds__(KM_THREADS, KM_CTAS_PER_SM)
 k_match(const FrameDev* __restrict__ frames, const PairDev* __restrict__ pairs,
         const MatchSegDev* __restrict__ segs, int nseg, uint32_t* next_group) {
-    __shared__ uint32_t s_pref[MAX_SEGS + 1];
+    __shared__ uint32_t s_pref[KM_MAX_SEGS + 1];
     __shared__ uint32_t s_warp[33];
     __shared__ __align__(16) CandStage s_stage[KM_THREADS / 32];
     // work units: groups of 32 queries of one band (band offsets follow the
@@ -1831,21 +1849,52 @@ k_match(const FrameDev* __restrict__ frames, const PairDev* __restrict__ pairs,
             if (c0 >= c1) continue;
             const uint32_t* xorder = B.xorder[pl] + (size_t)band * (size_t)(B.cap > 0 ? B.cap : 1);
             const uint32_t* feats = B.feats[pl];
-            for (uint32_t base = c0; base < c1; base += 32u) {
-                const uint32_t kk = base + (uint32_t)lane;
-                if (kk < c1) {
-                    const uint32_t j = __ldg(xorder + kk);
+            // Candidates are staged by asynchronous copies one batch ahead,
+            // into two buffers: batch i + 1's copies are issued before batch i
+            // is used, and batch i + 2's list entry is loaded meanwhile.
+            uint32_t jn = 0u;  // list entry of this lane's slot in the next batch
+            {
+                // prologue: batch 0 in flight, batch 1's list entry in hand
+                const uint32_t k0 = c0 + (uint32_t)lane;
+                if (k0 < c1) {
+                    const uint32_t j = __ldg(xorder + k0);
                     const uint32_t* rec = feats + (size_t)j * 12u;
-                    S.py[lane] = (float)(uint32_t)__uint_as_float(__ldg(rec + 1)) * ps;
-                    S.idx[lane] = USLAM_PACK(pl, j);
-                    S.d0[lane] = __ldg(reinterpret_cast<const uint4*>(rec + 4));
-                    S.d1[lane] = __ldg(reinterpret_cast<const uint4*>(rec + 8));
+                    CandBuf& N = S.buf[0];
+                    cp_async4(&N.py[lane], rec + 1);
+                    cp_async16(&N.d0[lane], rec + 4);
+                    cp_async16(&N.d1[lane], rec + 8);
+                    N.idx[lane] = USLAM_PACK(pl, j);
+                }
+                cp_async_commit();
+                if (k0 + 32u < c1) jn = __ldg(xorder + k0 + 32u);
+            }
+            int cur = 0;
+            for (uint32_t base = c0; base < c1; base += 32u, cur ^= 1) {
+                const uint32_t kk = base + (uint32_t)lane;
+                CandBuf& SB = S.buf[cur];
+                {
+                    // the next batch's copies go out before this batch is used
+                    const uint32_t kn = kk + 32u;
+                    if (kn < c1) {
+                        const uint32_t* rec = feats + (size_t)jn * 12u;
+                        CandBuf& N = S.buf[cur ^ 1];
+                        cp_async4(&N.py[lane], rec + 1);
+                        cp_async16(&N.d0[lane], rec + 4);
+                        cp_async16(&N.d1[lane], rec + 8);
+                        N.idx[lane] = USLAM_PACK(pl, jn);
+                    }
+                    cp_async_commit();
+                    if (kn + 32u < c1) jn = __ldg(xorder + kn + 32u);
+                    cp_async_wait<1>();
+                    // the staged word is the record's f32 y; the LOD-0 y as in
+                    // match_features_cpu.cpp:58-64
+                    if (kk < c1) SB.py[lane] = (float)(uint32_t)SB.py[lane] * ps;
                 }
                 __syncwarp();
                 // y test of all 32 staged candidates (unrolled, float4 loads);
                 // slots past the list's end lie outside both ranges
                 uint32_t ymask = 0u;
-                const float4* py4 = reinterpret_cast<const float4*>(S.py);
+                const float4* py4 = reinterpret_cast<const float4*>(SB.py);
 #pragma unroll
                 for (int q = 0; q < 8; ++q) {
                     const float4 v = py4[q];
@@ -1863,10 +1912,10 @@ k_match(const FrameDev* __restrict__ frames, const PairDev* __restrict__ pairs,
                     // distance is computed
                     int t = 31 - __clz(hb);
                     hb ^= 1u << t;
-                    uint4 c0d = S.d0[t], c1d = S.d1[t];
+                    uint4 c0d = SB.d0[t], c1d = SB.d1[t];
                     while (true) {
                         const int tn = hb ? 31 - __clz(hb) : t;
-                        const uint4 n0d = S.d0[tn], n1d = S.d1[tn];
+                        const uint4 n0d = SB.d0[tn], n1d = SB.d1[tn];
                         const uint32_t d = hamming256(c0d, c1d, qd0, qd1);
                         const uint32_t key = (d << 5) | (uint32_t)t;
                         secondk = min(secondk, max(bestk, key));
@@ -1885,17 +1934,17 @@ k_match(const FrameDev* __restrict__ frames, const PairDev* __restrict__ pairs,
                     while (o1) {
                         const int t = 31 - __clz(o1);
                         o1 ^= 1u << t;
-                        const uint32_t key = (hamming256(S.d0[t], S.d1[t], qd0, qd1) << 5) | (uint32_t)t;
+                        const uint32_t key = (hamming256(SB.d0[t], SB.d1[t], qd0, qd1) << 5) | (uint32_t)t;
                         secondk = min(secondk, max(bestk, key));
                         bestk = min(bestk, key);
                     }
                     while (o0) {
                         const int t = 31 - __clz(o0);
                         o0 ^= 1u << t;
-                        colq[32 * t] = (uint16_t)((hamming256(S.d0[t], S.d1[t], qd0, qd1) << 5) | (uint32_t)lane);
+                        colq[32 * t] = (uint16_t)((hamming256(SB.d0[t], SB.d1[t], qd0, qd1) << 5) | (uint32_t)lane);
                     }
                 }
-                if (bestk != prev) bidx = S.idx[bestk & 31u];
+                if (bestk != prev) bidx = SB.idx[bestk & 31u];
                 __syncwarp();
                 // column pass: lane t folds the keys of slot t into the two
                 // smallest (two 16-bit lanes at a time), empties the column
@@ -1922,7 +1971,7 @@ k_match(const FrameDev* __restrict__ frames, const PairDev* __restrict__ pairs,
                     if (cb != 0xffffu) {
                         const unsigned long long key =
                             ((unsigned long long)(cb >> 5) << 32) | (unsigned long long)S.qid[cb & 31u];
-                        const int32_t id = S.idx[lane];
+                        const int32_t id = SB.idx[lane];
                         uint4* acc = bacc + (size_t)USLAM_PACK_LEVEL(id) * capb + (size_t)USLAM_PACK_INDEX(id);
                         const unsigned long long old = atomicMin(reinterpret_cast<unsigned long long*>(acc), key);
                         // the larger of the old best and this best joins the
@@ -2301,16 +2350,15 @@ cudaError_t set_describe_tiled_smem(int margin) {
 cudaError_t launch_match(const FrameDev* frames, const PairDev* pairs, const void* segs, int nseg, int num_sms,
                          cudaStream_t st) {
     if (nseg <= 0) return cudaSuccess;
-    k_match<<<num_sms * KM_CTAS_PER_SM, KM_THREADS, 0, st>>>(frames, pairs, static_cast<const MatchSegDev*>(segs), nseg, nullptr);
+    k_match<<<num_sms * KM_CTAS_PER_SM, KM_THREADS, 0, st>>>(frames, pairs, static_cast<const MatchSegDev*>(segs), nseg,
+                                                              nullptr);
     return cudaGetLastError();
 }
-// Dynamic distribution of the query groups: next_group (device, 4 bytes)
-// holds 0 at the launch: zero when allocated, and zeroed again by the
-// k_mutual launch that follows every k_match launch (launch_mutual_reset).
 cudaError_t launch_match_dyn(const FrameDev* frames, const PairDev* pairs, const void* segs, int nseg, int num_sms,
                              uint32_t* next_group, cudaStream_t st) {
     if (nseg <= 0) return cudaSuccess;
-    k_match<<<num_sms * KM_CTAS_PER_SM, KM_THREADS, 0, st>>>(frames, pairs, static_cast<const MatchSegDev*>(segs), nseg, next_group);
+    k_match<<<num_sms * KM_CTAS_PER_SM, KM_THREADS, 0, st>>>(frames, pairs, static_cast<const MatchSegDev*>(segs), nseg,
+                                                              next_group);
     return cudaGetLastError();
 }
 

@@ -151,6 +151,8 @@ uslam_status build_program(uslam_batch* b, const std::vector<int>& fr, const std
     }
     if (static_cast<int>(fsegs.size()) > kMaxSegs || static_cast<int>(msegs.size()) > kMaxSegs)
         return set_err(b->err(), USLAM_CAPACITY, "batch exceeds 4096 (frame, level) or (pair, dir, level) segments");
+    if (!b->win_tc && static_cast<int>(msegs.size()) > USLAM_MAX_MATCH_SEGS)
+        return set_err(b->err(), USLAM_CAPACITY, "batch exceeds 2048 (pair, level) match segments");
     P->ntiles = static_cast<int>(tiles.size());
     P->nfsegs = static_cast<int>(fsegs.size());
     P->nmsegs = static_cast<int>(msegs.size());

@@ -180,7 +180,7 @@ size_t tables_bytes(int max_batch, int max_tiles_per_frame, int max_bands_per_fr
                     int levels) {
     const size_t t = round_up(sizeof(TileItem) * static_cast<size_t>(max_batch) * max_tiles_per_frame, 256);
     const size_t f = round_up(sizeof(SegDev) * static_cast<size_t>(max_batch) * levels, 256);
-    const size_t m = round_up(sizeof(MatchSegDev) * static_cast<size_t>(max_batch) * 2 * levels, 256);
+    const size_t m = round_up(sizeof(MatchSegDev) * static_cast<size_t>(max_batch) * levels, 256);
     const size_t u = round_up(sizeof(SegDev) * static_cast<size_t>(max_batch) * levels, 256);
     const size_t p = round_up(sizeof(PairDev) * static_cast<size_t>(max_batch), 256);
     const size_t b = round_up(sizeof(BandItem) * static_cast<size_t>(max_batch) * max_bands_per_frame, 256);
@@ -439,6 +439,10 @@ uslam_status uslam_server_create(uslam_ctx* ctx, const uslam_server_params* p, u
         return set_err(ctx ? &ctx->err : nullptr, USLAM_INVALID_ARG, "server_create: bad arguments");
     if (ctx->matcher != 0)
         return set_err(&ctx->err, USLAM_INVALID_ARG, "server_create: the served form runs the windowed matcher only");
+    // one launch holds max_batch frames: its (frame, level) and (pair, level)
+    // segment tables must fit the persistent kernels' shared prefix tables
+    if (static_cast<long long>(p->max_batch) * ctx->levels > USLAM_MAX_MATCH_SEGS)
+        return set_err(&ctx->err, USLAM_INVALID_ARG, "server_create: max_batch x levels exceeds 2048");
     cudaError_t e = cudaSetDevice(ctx->device);
     if (e != cudaSuccess) return ctx->cuda_fail(e, "cudaSetDevice");
     auto* s = new uslam_server();

@@ -39,6 +39,7 @@
 
 #define USLAM_MAX_LEVELS 12
 #define USLAM_MATCH_BANDS 3  // horizontal bands of the frame for the matcher's lists
+#define USLAM_MAX_MATCH_SEGS 2048  // (pair, level) segments of one k_match launch
 
 // Device copy of one frame's geometry and buffer addresses.
 struct FrameDev {
