@@ -426,7 +426,8 @@ uslam_status uslam_server_stats(uslam_server* server, uint64_t* launches, uint64
  * (0 <= x < w_l, 0 <= y < h_l), as every detector of this library and of the
  * reference produces them.  The counts and sizes are checked on the host and
  * the records by a kernel before anything indexes by them: a record outside
- * its level returns USLAM_INVALID_ARG.
+ * its level empties both sets for the rest of the call (nothing indexes by
+ * it) and the call returns USLAM_INVALID_ARG.
  *
  * Scratch comes from a file-scope device array of 4 MiB that every GPU which
  * loads the library holds until the process exits; a call whose scratch need
@@ -437,8 +438,8 @@ uslam_status uslam_server_stats(uslam_server* server, uint64_t* launches, uint64
  * (different streams or threads at the same time) race and must not be
  * issued.  The call makes `device` current while it runs and restores the
  * caller's current device before it returns.  It enqueues on `stream` (a
- * cudaStream_t; NULL = the default stream), waits once after the record
- * check and once at the end, and returns after the work is complete.  err
+ * cudaStream_t; NULL = the default stream), waits once at the end, and
+ * returns after the work is complete.  err
  * (optional, err_len bytes) receives a message on failure. */
 uslam_status uslam_match_noalloc(int device, int width, int height, int levels, const uslam_feature* prev_feats,
                                  const int* prev_kept, const uslam_feature* curr_feats, const int* curr_kept,

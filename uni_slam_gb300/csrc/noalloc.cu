@@ -66,7 +66,11 @@ __global__ void k_noalloc_tables(const NoallocTables t, NoallocTables* dst) {
 // The caller's feature records are device memory the host cannot check, and
 // the x-sort indexes its shared histogram by x: every record's x and y must be
 // integers (as f32) inside its level.  A record that is not (NaN included)
-// sets *bad, and the host returns USLAM_INVALID_ARG before the sort runs.
+// sets USLAM_ERR_BAD_RECORD in *bad; k_noalloc_gate then empties both sets, so
+// the sort and the match that follow on the stream see no features, and the
+// host returns USLAM_INVALID_ARG after its one synchronisation.
+constexpr uint32_t USLAM_ERR_BAD_RECORD = 1u << 16;
+
 __global__ void k_noalloc_validate(const NoallocTables* t, uint32_t* bad) {
     for (int f = 0; f < 2; ++f) {
         const FrameDev& F = t->frames[f];
@@ -78,10 +82,16 @@ __global__ void k_noalloc_validate(const NoallocTables* t, uint32_t* bad) {
                 const float x = __uint_as_float(rec[(size_t)i * 12u]);
                 const float y = __uint_as_float(rec[(size_t)i * 12u + 1u]);
                 const bool ok = x >= 0.0f && x < w && y >= 0.0f && y < h && x == truncf(x) && y == truncf(y);
-                if (!ok) atomicOr(bad, 1u);
+                if (!ok) atomicOr(bad, USLAM_ERR_BAD_RECORD);
             }
         }
     }
+}
+
+// After k_noalloc_validate: a bad record empties both feature sets.
+__global__ void k_noalloc_gate(NoallocTables* t, const uint32_t* err) {
+    if (!(*err & USLAM_ERR_BAD_RECORD)) return;
+    for (int i = threadIdx.x; i < 2 * 2 * USLAM_MAX_LEVELS; i += blockDim.x) (&t->counts[0][0])[i] = 0u;
 }
 
 struct DeviceScratch {
@@ -281,15 +291,13 @@ extern "C" uslam_status uslam_match_noalloc(int device, int width, int height, i
     k_noalloc_tables<<<1, 256, 0, st>>>(t, dtab);
     e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaMemsetAsync(derr, 0, sizeof(uint32_t), st);  // the error word must start at zero
-    uint32_t bad = 0;
     if (e == cudaSuccess && (total[0] > 0 || total[1] > 0)) {
         k_noalloc_validate<<<ds.num_sms, 256, 0, st>>>(dtab, derr);
         e = cudaGetLastError();
-        if (e == cudaSuccess) e = cudaMemcpyAsync(&bad, derr, sizeof bad, cudaMemcpyDeviceToHost, st);
-        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-        if (e == cudaSuccess && bad != 0u)
-            return fail(err, err_len, USLAM_INVALID_ARG,
-                        "match_noalloc: a feature record's x or y is not an integer inside its level");
+        if (e == cudaSuccess) {
+            k_noalloc_gate<<<1, 64, 0, st>>>(dtab, derr);
+            e = cudaGetLastError();
+        }
     }
     if (e == cudaSuccess) {
         e = set_compact_smem(max_w);  // a function attribute, not an allocation
@@ -302,6 +310,9 @@ extern "C" uslam_status uslam_match_noalloc(int device, int width, int height, i
     if (e == cudaSuccess) e = cudaMemcpyAsync(&word, derr, sizeof word, cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return fail(err, err_len, USLAM_CUDA_ERROR, cudaGetErrorString(e));
+    if (word & USLAM_ERR_BAD_RECORD)
+        return fail(err, err_len, USLAM_INVALID_ARG,
+                    "match_noalloc: a feature record's x or y is not an integer inside its level");
     if (word != 0u) return fail(err, err_len, USLAM_KERNEL_CHECK, "match_noalloc: match list overflow");
     if (err && err_len > 0) err[0] = '\0';
     return USLAM_OK;
