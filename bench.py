@@ -1197,6 +1197,18 @@ def run_ours(a):
         "path_achieved": nbytes["total_per_step"] / (step_ms / 1e3) / 1e9,
         "path_frac": nbytes["total_per_step"] / (step_ms / 1e3) / 1e9 / peak,
     }
+    # every kernel's own line: its algorithmic bytes / its event-timed launch,
+    # its DRAM traffic per launch from the committed captures, its SM side
+    pipes = measured_pipes()
+    roofline["per_kernel"] = {
+        k: {"ms": prof[k], "algorithmic_bytes": kernel_bytes[k],
+            "achieved": kernel_bytes[k] / (prof[k] / 1e3) / 1e9,
+            "frac": kernel_bytes[k] / (prof[k] / 1e3) / 1e9 / peak,
+            "traffic": (traffic_per_unit[k] * traffic_units[k]) if k in traffic_per_unit and k in traffic_units
+            else None,
+            "sm_bound": pipes.get(k)}
+        for k in prof if k in kernel_bytes and prof[k] > 0
+    }
 
     # ---- end to end through the C ABI: pinned H2D + graph + D2H every step
     batch.set_stream(None)  # the batch's own stream from here on
