@@ -638,6 +638,48 @@ def serve_saturation(ctx, sizes, frames, seconds: float, inflight: int = 4, prom
     }
 
 
+def serve_saturation_native(pat, sizes, frames, seconds: float, inflight: int = 4, threads: int = 8,
+                            promote_every: int = 10, cap_per_level: int = 333, per_stream: int = 16) -> dict:
+    """The closed-loop capacity of serve_saturation with native client threads
+    (tests/adapter/server_load.cpp against the C ABI): the same streams, sizes,
+    keyframe policy and per-level cap, the first `per_stream` frames of each
+    stream's trajectory walked forwards and backwards, results copied into
+    each client thread's host buffers.  The Python client's own submit and
+    result path (ctypes, one completer thread) does not limit it."""
+    import struct
+    import subprocess
+    import tempfile
+
+    import numpy as np
+
+    here = os.path.join(REPO, "tests", "adapter")
+    lib = os.path.join(REPO, "uni_slam_gb300")
+    with tempfile.TemporaryDirectory() as td:
+        exe = os.path.join(td, "server_load")
+        subprocess.run(["g++", "-std=c++17", "-O2", "-I", os.path.join(REPO, "include"),
+                        os.path.join(here, "server_load.cpp"), "-o", exe, "-L", lib, "-luslam",
+                        f"-Wl,-rpath,{lib}", "-lpthread"], check=True, capture_output=True)
+        with open(os.path.join(td, "pattern.bin"), "wb") as f:
+            f.write(np.ascontiguousarray(pat, "<i4").tobytes())
+        with open(os.path.join(td, "frames.bin"), "wb") as f:
+            f.write(struct.pack("<i", len(sizes)))
+            for (w, h), fr in zip(sizes, frames):
+                sub = fr[:per_stream]
+                f.write(struct.pack("<3i", w, h, len(sub)))
+                for img in sub:
+                    f.write(np.ascontiguousarray(img, np.uint8).tobytes())
+        r = subprocess.run([exe, os.path.join(td, "pattern.bin"), os.path.join(td, "frames.bin"), str(seconds),
+                            str(inflight), str(threads), str(promote_every), str(cap_per_level)],
+                           capture_output=True, text=True, timeout=600)
+        if r.returncode != 0:
+            return {"error": f"server_load rc={r.returncode}: {r.stderr[-300:]}"}
+        out = json.loads(r.stdout.strip().splitlines()[-1])
+    out.update({"streams": len(sizes), "inflight_per_stream": inflight, "client_threads": threads,
+                "results_copied": True, "client": "native (tests/adapter/server_load.cpp)",
+                "latency": "submit -> features and matches in the client thread's host buffers"})
+    return out
+
+
 # ------------------------------------------------------------------ plugin path
 
 def plugin_run(pat, frames, warmup: int = 8, timed: int = 256, advance_every: int = 1) -> dict:
@@ -1298,6 +1340,11 @@ def run_ours(a):
             served = serve_simulation(sctx, serve_sizes, serve_frames, a.serve_seconds, seed=a.seed + rank)
             served["saturation"] = serve_saturation(sctx, serve_sizes, serve_frames, min(a.serve_seconds, 5.0))
             served["saturation"]["over_plain"] = served["saturation"]["fps"] / plain_fps
+            if rank == 0:
+                nat = serve_saturation_native(pat, serve_sizes, serve_frames, min(a.serve_seconds, 5.0))
+                if "frames_per_s" in nat:
+                    nat["over_plain"] = nat["frames_per_s"] / plain_fps
+                served["saturation_native"] = nat
         finally:
             gc.enable()
         served["client_gc"] = "paused during the runs"
