@@ -13,9 +13,12 @@
 //                   candidate list, and the band-grouped query order
 //   k_describe (K2) orientation (one lane per keypoint of a warp's group) +
 //                   256-bit rotated BRIEF (the warp's lanes take 8 tests each)
-//   k_match    (K3) windowed top-2 Hamming search; a warp claims groups of 32
-//                   x-adjacent queries of one band
-//   k_mutual        mutual cross-check and ordered match output
+//   k_bacc_init     empties the b -> a accumulators before each k_match
+//   k_match    (K3) windowed top-2 Hamming search of both directions, one
+//                   distance per pair; a warp claims groups of 32 x-adjacent
+//                   queries of the previous set in one band
+//   k_mutual        mutual cross-check (b's search read from its accumulator)
+//                   and ordered match output
 //   k_bruteforce    brute-force top-2 matching (no window, no cross-check) on
 //                   the integer pipes; the tensor-core form is k_bf_mma
 //                   (bf_tc.cu)
