@@ -176,11 +176,24 @@ class CudaMatchPass : public compute::Pass {
         std::vector<uslam_match> buf(static_cast<size_t>(std::max(n, 1)));
         if (uslam_frontend_matches(gpu_->frontend(), buf.data(), n, &n) != USLAM_OK)
             return std::string("uslam_frontend_matches: ") + uslam_last_error(gpu_->ctx());
-        // result[lod of a]: key = current-frame feature (b), value = previous (a)
+        // result[lod of a]: key = current-frame feature (b), value = previous (a).
+        // Each level's pairs go in by ascending key with an end hint: the
+        // reference's flat_map then appends instead of shifting its tail on
+        // every insert, and an ordered map finds the place at once.  The
+        // mutual check leaves each b at most one a, so the keys are unique
+        // and the map holds the same entries as one emplace per match.
         MatchResult result;
+        std::vector<std::vector<std::pair<const Feature*, const Feature*>>> by_level(result.size());
         for (int i = 0; i < n; ++i) {
             const uslam_match& m = buf[i];
-            result.at(m.lod_a).emplace((**curr).at(m.lod_b).at(m.idx_b), (**prev).at(m.lod_a).at(m.idx_a));
+            by_level.at(static_cast<size_t>(m.lod_a))
+                .emplace_back(&(**curr).at(m.lod_b).at(m.idx_b), &(**prev).at(m.lod_a).at(m.idx_a));
+        }
+        for (size_t l = 0; l < by_level.size(); ++l) {
+            auto& pairs = by_level[l];
+            std::sort(pairs.begin(), pairs.end(), [](const auto& u, const auto& v) { return *u.first < *v.first; });
+            auto& level = result.at(l);
+            for (const auto& [b, a] : pairs) level.emplace_hint(level.end(), *b, *a);
         }
         storage_.set(ResourceIdentifier::MatchedFeaturesName, std::move(result));
         return std::nullopt;
