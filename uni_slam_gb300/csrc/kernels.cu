@@ -360,8 +360,11 @@ k_pyramid(const FrameDev* __restrict__ frames, const TileItem* __restrict__ tile
 // taps' sampling coordinates depend only on the row or only on the column,
 // so they are computed once per tile row / column (same operations as the
 // per-pixel formula, hence the same bits).
+// Six CTAs per SM (40 registers, no spills): 0.700 against 0.718 ms at five
+// (48 registers) and 0.712 at four on the 64-frame step; seven spill.  The
+// cfg profile's form spills at 40 and keeps five.
 template <int TW, int TH, bool CFG>
-__global__ void __launch_bounds__(K1_THREADS, 5)
+__global__ void __launch_bounds__(K1_THREADS, CFG ? 5 : 6)
 k_detect(const FrameDev* __restrict__ frames, const TileItem* __restrict__ tiles, int shape, uint32_t* err) {
     constexpr int HY = CFG ? HY_CFG : uslam::HY;
     constexpr int SW = TW + 2 * HX;                   // staged columns [X0 - HX, X0 + TW + HX)
