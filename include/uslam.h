@@ -256,7 +256,9 @@ uslam_status uslam_triangulate(uslam_ctx* ctx, const uslam_camera* cam, const us
 
 /* Plan a batch of n_frames frames (any mix of sizes) and n_pairs matches
  * (pair k matches frame pair_prev[k] (reference set) against frame
- * pair_curr[k]).  Allocates every device buffer up front. */
+ * pair_curr[k]).  Allocates every device buffer up front.  At most 4096
+ * (frame, level) segments and, with the windowed matcher, 2048 (pair, level)
+ * segments: USLAM_CAPACITY beyond. */
 uslam_status uslam_batch_create(uslam_ctx* ctx, int n_frames, const int* widths, const int* heights,
                                 int n_pairs, const int* pair_prev, const int* pair_curr, uslam_batch** out);
 void uslam_batch_destroy(uslam_batch* b);
