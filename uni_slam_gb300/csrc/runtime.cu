@@ -138,16 +138,29 @@ uslam_status build_program(uslam_batch* b, const std::vector<int>& fr, const std
     }
     if (!b->win_tc) {
         // k_match searches both directions from the prev set's queries.  Its
-        // warps claim query groups in segment order, so the groups of the
-        // first and last level (two pool levels instead of three, the
-        // cheapest) come last and shorten the launch's tail (0.594 -> 0.570 ms
-        // on the 64-frame step).
+        // warps claim query groups in segment order, so the costliest groups
+        // go first and the launch's tail is short: a group's windows cover a
+        // fixed share of its frame at about the same feature density, so its
+        // cost grows with the frame's area (larger frames first); within one
+        // size the groups of the first and last level (two pool levels
+        // instead of three) come last (0.594 -> 0.570 ms on the 64-frame step).
         std::vector<int> order;
         for (int l = 1; l + 1 < b->levels; ++l) order.push_back(l);
         order.push_back(0);
         if (b->levels > 1) order.push_back(b->levels - 1);
-        for (int l : order)
-            for (int p : pr) msegs.push_back(MatchSegDev{p, 1, l});
+        std::vector<int> by_area(pr.begin(), pr.end());
+        auto area = [&](int p) {
+            const FrameDev& F = b->frames[b->pairs[p].curr];
+            return static_cast<long long>(F.W0) * F.H0;
+        };
+        std::stable_sort(by_area.begin(), by_area.end(), [&](int x, int y) { return area(x) > area(y); });
+        for (size_t i = 0; i < by_area.size();) {
+            size_t j = i;
+            while (j < by_area.size() && area(by_area[j]) == area(by_area[i])) ++j;
+            for (int l : order)
+                for (size_t k = i; k < j; ++k) msegs.push_back(MatchSegDev{by_area[k], 1, l});
+            i = j;
+        }
     }
     if (static_cast<int>(fsegs.size()) > kMaxSegs || static_cast<int>(msegs.size()) > kMaxSegs)
         return set_err(b->err(), USLAM_CAPACITY, "batch exceeds 4096 (frame, level) or (pair, dir, level) segments");
