@@ -53,8 +53,8 @@ POPC_PER_DISTANCE = 4  # carry-save-adder Hamming distance of 256 bits
 # kernels of one graph replay of the uniform batch (one tile shape), which the
 # runtime captures as two halves of the frames on two streams: per half
 # k_pyramid, k_detect, k_blur_border, k_band_count, k_band_write, k_xsort,
-# k_describe, k_bacc_init, k_match, k_mutual
-KERNELS_PER_STEP = 20
+# k_describe, k_bacc_init, k_match_rank, k_match_order, k_match, k_mutual
+KERNELS_PER_STEP = 24
 # batches in flight in the pipelined end-to-end measurement
 E2E_DEPTH = 3
 METRIC = "frames/s detect+describe+match @752x480 (batched, 64-frame graph)"

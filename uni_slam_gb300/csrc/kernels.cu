@@ -14,6 +14,8 @@
 //   k_describe (K2) orientation (one lane per keypoint of a warp's group) +
 //                   256-bit rotated BRIEF (the warp's lanes take 8 tests each)
 //   k_bacc_init     empties the b -> a accumulators before each k_match
+//   k_match_rank, k_match_order
+//                   k_match's claim order: query groups by estimated cost
 //   k_match    (K3) windowed top-2 Hamming search of both directions, one
 //                   distance per pair; a warp claims groups of 32 x-adjacent
 //                   queries of the previous set in one band
@@ -1722,6 +1724,102 @@ __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commi
 template <int N>
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
 
+// Query groups of one (pair, level) segment: groups of 32 queries of the
+// previous set, per band of its query order.
+__device__ __forceinline__ uint32_t match_groups(const FrameDev* frames, const PairDev* pairs, const MatchSegDev& sg) {
+    const FrameDev& Qf = frames[pairs[sg.pair].prev];
+    const int ql = sg.level;
+    const uint32_t* qb = Qf.colstart[ql] + (size_t)USLAM_MATCH_BANDS * (size_t)(Qf.w[ql] + 1);
+    uint32_t n = 0;
+    for (int b = 0; b < USLAM_MATCH_BANDS; ++b) n += (qb[b + 1] - qb[b] + 31u) / 32u;
+    return n;
+}
+
+// Band of group grp of a segment (grp becomes the group within the band).
+__device__ __forceinline__ int match_group_band(const uint32_t* qband, uint32_t* grp) {
+    int band = 0;
+    while (band + 1 < USLAM_MATCH_BANDS && *grp >= (qband[band + 1] - qband[band] + 31u) / 32u) {
+        *grp -= (qband[band + 1] - qband[band] + 31u) / 32u;
+        ++band;
+    }
+    return band;
+}
+
+// The claim order of k_match: query groups by estimated cost, costliest
+// first, so that the launch does not end on a few long groups.  A group's
+// cost follows the candidates it stages: the union of its x-windows in the
+// band lists of its pool levels, bounded by its first and last query (the
+// group is x-sorted).  KM_BUCKETS cost buckets of 64 candidates.  The claim
+// block of a launch: [0] the claim counter, [1, 1 + KM_BUCKETS) the groups
+// per bucket, then the buckets' write cursors, then the order; k_mutual
+// zeroes the first KM_CLAIM_WORDS words after the launch.
+constexpr int KM_BUCKETS = 64;
+constexpr int KM_CLAIM_WORDS = 1 + 2 * KM_BUCKETS;
+
+__device__ uint32_t match_group_cost(const FrameDev* frames, const PairDev* pairs, const MatchSegDev& sg,
+                                     uint32_t grp) {
+    const PairDev& P = pairs[sg.pair];
+    const FrameDev& Q = frames[P.prev];
+    const FrameDev& B = frames[P.curr];
+    const int l = sg.level;
+    const uint32_t* qband = Q.colstart[l] + (size_t)USLAM_MATCH_BANDS * (size_t)(Q.w[l] + 1);
+    const int band = match_group_band(qband, &grp);
+    const uint32_t k0 = qband[band] + grp * 32u, k1 = min(k0 + 31u, qband[band + 1] - 1u);
+    const float ql = lod_scale(l);
+    const float x0 = (float)(uint32_t)__uint_as_float(Q.feats[l][(size_t)__ldg(Q.qorder[l] + k0) * 12u]) * ql;
+    const float x1 = (float)(uint32_t)__uint_as_float(Q.feats[l][(size_t)__ldg(Q.qorder[l] + k1) * 12u]) * ql;
+    const float lo = x0 - P.max_dx, hi = x1 + P.max_dx;
+    uint32_t n = 0;
+    for (int k = 0; k < 3; ++k) {
+        const int pl = k == 0 ? l : (k == 1 ? l - 1 : l + 1);
+        if (pl < 0 || pl >= B.levels) continue;
+        const float ps = lod_scale(pl);
+        const int wpl = B.w[pl];
+        const uint32_t* colstart = B.colstart[pl] + (size_t)band * (size_t)(wpl + 1);
+        const int xlo = first_col_ge(lo, ps, wpl), xhi = last_col_le(hi, ps, wpl);
+        if (xlo <= xhi) n += __ldg(colstart + xhi + 1) - __ldg(colstart + xlo);
+    }
+    return n;
+}
+
+// Pass 1: every group's cost bucket and the bucket sizes.
+__global__ void __launch_bounds__(256)
+k_match_rank(const FrameDev* __restrict__ frames, const PairDev* __restrict__ pairs,
+             const MatchSegDev* __restrict__ segs, int nseg, uint32_t* claim, uint8_t* gbucket) {
+    __shared__ uint32_t s_pref[KM_MAX_SEGS + 1];
+    __shared__ uint32_t s_warp[33];
+    const uint32_t total =
+        segment_prefix(nseg, s_pref, s_warp, [&](int s) { return match_groups(frames, pairs, segs[s]); });
+    for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < total; g += gridDim.x * blockDim.x) {
+        const int sidx = find_segment(s_pref, nseg, g);
+        const uint32_t c = match_group_cost(frames, pairs, segs[sidx], g - s_pref[sidx]);
+        const int b = KM_BUCKETS - 1 - (int)min(c >> 6, (uint32_t)(KM_BUCKETS - 1));
+        gbucket[g] = (uint8_t)b;
+        atomicAdd(claim + 1 + b, 1u);
+    }
+}
+
+// Pass 2: the order, bucket by bucket (within a bucket in arrival order).
+__global__ void __launch_bounds__(256) k_match_order(uint32_t* claim, const uint8_t* __restrict__ gbucket) {
+    __shared__ uint32_t s_start[KM_BUCKETS + 1];
+    if (threadIdx.x == 0) {
+        uint32_t run = 0;
+        for (int b = 0; b < KM_BUCKETS; ++b) {
+            s_start[b] = run;
+            run += claim[1 + b];
+        }
+        s_start[KM_BUCKETS] = run;
+    }
+    __syncthreads();
+    const uint32_t total = s_start[KM_BUCKETS];
+    uint32_t* cursor = claim + 1 + KM_BUCKETS;
+    uint32_t* order = claim + KM_CLAIM_WORDS;
+    for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < total; g += gridDim.x * blockDim.x) {
+        const int b = gbucket[g];
+        order[s_start[b] + atomicAdd(cursor + b, 1u)] = g;
+    }
+}
+
 // The windowed mutual matcher (match_features_cpu.cpp:66-207), one Hamming
 // distance per pair of features.  Both directions of FindMatches compare the
 // same pairs: b in the window of a (a -> b, pool = the levels l - 1 .. l + 1
@@ -1749,21 +1847,16 @@ __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_gr
 // a here and to b in k_mutual.
 __global__ void __launch_bounds__(KM_THREADS, KM_CTAS_PER_SM)
 k_match(const FrameDev* __restrict__ frames, const PairDev* __restrict__ pairs,
-        const MatchSegDev* __restrict__ segs, int nseg, uint32_t* next_group) {
+        const MatchSegDev* __restrict__ segs, int nseg, uint32_t* claim_block) {
     __shared__ uint32_t s_pref[KM_MAX_SEGS + 1];
     __shared__ uint32_t s_warp[33];
     __shared__ __align__(16) CandStage s_stage[KM_THREADS / 32];
     // work units: groups of 32 queries of one band (band offsets follow the
     // query level's column tables)
-    const uint32_t total = segment_prefix(nseg, s_pref, s_warp, [&](int s) {
-        const PairDev& P = pairs[segs[s].pair];
-        const FrameDev& Qf = frames[P.prev];
-        const int ql = segs[s].level;
-        const uint32_t* qb = Qf.colstart[ql] + (size_t)USLAM_MATCH_BANDS * (size_t)(Qf.w[ql] + 1);
-        uint32_t n = 0;
-        for (int b = 0; b < USLAM_MATCH_BANDS; ++b) n += (qb[b + 1] - qb[b] + 31u) / 32u;
-        return n;
-    });
+    const uint32_t total =
+        segment_prefix(nseg, s_pref, s_warp, [&](int s) { return match_groups(frames, pairs, segs[s]); });
+    uint32_t* const next_group = claim_block;
+    const uint32_t* const order = claim_block ? claim_block + KM_CLAIM_WORDS : nullptr;
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
     const int gw = blockIdx.x * (KM_THREADS / 32) + warp;
@@ -1776,9 +1869,10 @@ k_match(const FrameDev* __restrict__ frames, const PairDev* __restrict__ pairs,
         __syncwarp();
     }
     // Query groups cost very different amounts (the hits in their windows).
-    // With next_group (a counter zeroed before the launch) a warp claims the
-    // next group when it finishes one; without it warps take every nw-th
-    // group.  Each group writes only its own queries' a2b entries and merges
+    // With a claim block (its counter zeroed before the launch, its order
+    // written by k_match_rank / k_match_order) a warp claims the next group of
+    // the order, costliest first, when it finishes one; without it warps take
+    // every nw-th group.  Each group writes only its own queries' a2b entries and merges
     // into b's accumulators by atomic minima, so the order does not change
     // the result.
     auto claim = [&](uint32_t g) -> uint32_t {
@@ -1787,7 +1881,8 @@ k_match(const FrameDev* __restrict__ frames, const PairDev* __restrict__ pairs,
         if (lane == 0) n = atomicAdd(next_group, 1u);
         return __shfl_sync(0xffffffffu, n, 0);
     };
-    for (uint32_t g = next_group ? claim(0u) : (uint32_t)gw; g < total; g = claim(g)) {
+    for (uint32_t c = next_group ? claim(0u) : (uint32_t)gw; c < total; c = claim(c)) {
+        const uint32_t g = order ? __ldg(order + c) : c;
         const int sidx = find_segment(s_pref, nseg, g);
         uint32_t grp = g - s_pref[sidx];
         const MatchSegDev sg = segs[sidx];
@@ -1796,11 +1891,7 @@ k_match(const FrameDev* __restrict__ frames, const PairDev* __restrict__ pairs,
         const FrameDev& B = frames[P.curr];
         const int l = sg.level;
         const uint32_t* qband = Q.colstart[l] + (size_t)USLAM_MATCH_BANDS * (size_t)(Q.w[l] + 1);
-        int band = 0;
-        while (band + 1 < USLAM_MATCH_BANDS && grp >= (qband[band + 1] - qband[band] + 31u) / 32u) {
-            grp -= (qband[band + 1] - qband[band] + 31u) / 32u;
-            ++band;
-        }
+        const int band = match_group_band(qband, &grp);
         const uint32_t qk = qband[band] + grp * 32u + (uint32_t)lane;
         const bool valid = qk < qband[band + 1];
         const uint32_t qi = valid ? __ldg(Q.qorder[l] + qk) : 0u;
@@ -2153,9 +2244,10 @@ template <bool MUTUAL>
 __global__ void __launch_bounds__(KU_THREADS)
 k_mutual(const FrameDev* __restrict__ frames, const PairDev* __restrict__ pairs, const SegDev* __restrict__ segs,
          uint32_t* err, uint32_t* reset_word) {
-    // k_match's group counter for its next launch on this stream (k_mutual
-    // always follows k_match, which has finished with it)
-    if (reset_word && blockIdx.x == 0 && threadIdx.x == 0) *reset_word = 0u;
+    // k_match's claim counters for its next launch on this stream (k_mutual
+    // always follows k_match, which has finished with them)
+    if (reset_word && blockIdx.x == 0)
+        for (int i = threadIdx.x; i < KM_CLAIM_WORDS; i += blockDim.x) reset_word[i] = 0u;
     __shared__ uint32_t s_warp[33];
     const int pi = segs[blockIdx.x].frame;  // pair index
     const int l = segs[blockIdx.x].level;
@@ -2360,11 +2452,21 @@ cudaError_t launch_match(const FrameDev* frames, const PairDev* pairs, const voi
                                                               nullptr);
     return cudaGetLastError();
 }
+// The claim order (k_match_rank, k_match_order), then k_match claiming from
+// it.  claim: a block of match_claim_words(max groups) words, its first
+// KM_CLAIM_WORDS zero (k_mutual_reset zeroes them again after each launch);
+// gbucket: max groups bytes.
+size_t match_claim_words(size_t max_groups) { return KM_CLAIM_WORDS + max_groups; }
 cudaError_t launch_match_dyn(const FrameDev* frames, const PairDev* pairs, const void* segs, int nseg, int num_sms,
-                             uint32_t* next_group, cudaStream_t st) {
+                             uint32_t* claim, uint8_t* gbucket, cudaStream_t st) {
     if (nseg <= 0) return cudaSuccess;
-    k_match<<<num_sms * KM_CTAS_PER_SM, KM_THREADS, 0, st>>>(frames, pairs, static_cast<const MatchSegDev*>(segs), nseg,
-                                                              next_group);
+    const MatchSegDev* ms = static_cast<const MatchSegDev*>(segs);
+    k_match_rank<<<num_sms * 4, 256, 0, st>>>(frames, pairs, ms, nseg, claim, gbucket);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    k_match_order<<<num_sms, 256, 0, st>>>(claim, gbucket);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    k_match<<<num_sms * KM_CTAS_PER_SM, KM_THREADS, 0, st>>>(frames, pairs, ms, nseg, claim);
     return cudaGetLastError();
 }
 

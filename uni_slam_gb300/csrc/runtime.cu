@@ -76,6 +76,10 @@ struct uslam_batch {
     PairDev* d_pairs = nullptr;
     uint32_t* d_err = nullptr;
     char* d_tables = nullptr;
+    // k_match's claim blocks, one per lane (its counters and claim order),
+    // and each lane's group cost buckets
+    char* d_claim = nullptr;
+    size_t claim_stride = 0, claim_words = 0;
     cudaStream_t stream = nullptr;      // stream in use (own or caller's)
     cudaStream_t own_stream = nullptr;  // created with the batch
     cudaStream_t aux_stream = nullptr;  // k_blur_border's branch beside the compaction
@@ -197,14 +201,25 @@ uslam_status build_program(uslam_batch* b, const std::vector<int>& fr, const std
 }
 
 // A lane of launches: a stream, the stream k_blur_border forks to, their
-// fork/join events, and the word k_match claims its query groups from.
+// fork/join events, and the block k_match claims its query groups from (with
+// the group cost buckets its order is built from).
 struct Lane {
     cudaStream_t st, aux;
     cudaEvent_t fork, join;
-    uint32_t* next_group;
+    uint32_t* claim;
+    uint8_t* gbucket;
 };
 
-Lane lane0(uslam_batch* b) { return Lane{b->stream, b->aux_stream, b->ev_fork, b->ev_join, b->d_err + 1}; }
+uint32_t* lane_claim(uslam_batch* b, int j) {
+    return reinterpret_cast<uint32_t*>(b->d_claim + static_cast<size_t>(j) * b->claim_stride);
+}
+uint8_t* lane_gbucket(uslam_batch* b, int j) {
+    return reinterpret_cast<uint8_t*>(b->d_claim + static_cast<size_t>(j) * b->claim_stride) +
+           round_up(b->claim_words * sizeof(uint32_t), 256);
+}
+Lane lane0(uslam_batch* b) {
+    return Lane{b->stream, b->aux_stream, b->ev_fork, b->ev_join, lane_claim(b, 0), lane_gbucket(b, 0)};
+}
 
 // Describe of a program: the gather form k_describe over (frame, level)
 // segments; with describe_form 1, in batches of kTiledDescribeFrames frames
@@ -266,10 +281,10 @@ cudaError_t enqueue_pairs(uslam_batch* b, const Program& P, const Lane& ln) {
         return launch_mutual(b->d_frames, b->d_pairs, P.usegs, P.nusegs, b->d_err, ln.st);
     }
     if ((e = launch_bacc_init(b->d_frames, b->d_pairs, P.usegs, P.nusegs, ln.st)) != cudaSuccess) return e;
-    if ((e = launch_match_dyn(b->d_frames, b->d_pairs, P.msegs, P.nmsegs, c->num_sms,
-                              ln.next_group, ln.st)) != cudaSuccess)
+    if ((e = launch_match_dyn(b->d_frames, b->d_pairs, P.msegs, P.nmsegs, c->num_sms, ln.claim, ln.gbucket,
+                              ln.st)) != cudaSuccess)
         return e;
-    return launch_mutual_reset(b->d_frames, b->d_pairs, P.usegs, P.nusegs, b->d_err, ln.next_group, ln.st);
+    return launch_mutual_reset(b->d_frames, b->d_pairs, P.usegs, P.nusegs, b->d_err, ln.claim, ln.st);
 }
 
 // Enqueue a program's launch sequence on the batch stream.
@@ -287,7 +302,8 @@ cudaError_t enqueue_split(uslam_batch* b) {
     Lane ln[kLanes];
     for (int j = 0; j < K; ++j)
         ln[j] = j == 0 ? lane0(b)
-                       : Lane{b->lane_st[j], b->lane_aux[j], b->lane_fork[j], b->lane_join[j], b->d_err + 1 + j};
+                       : Lane{b->lane_st[j], b->lane_aux[j], b->lane_fork[j], b->lane_join[j], lane_claim(b, j),
+                              lane_gbucket(b, j)};
     cudaError_t e = cudaEventRecord(b->ev_start, b->stream);
     for (int j = 1; j < K && e == cudaSuccess; ++j) e = cudaStreamWaitEvent(ln[j].st, b->ev_start, 0);
     for (int j = 0; j < K && e == cudaSuccess; ++j) {
@@ -343,6 +359,7 @@ void free_batch(uslam_batch* b) {
     if (b->ev_start) cudaEventDestroy(b->ev_start);
     if (b->arena) cudaFree(b->arena);
     if (b->d_tables) cudaFree(b->d_tables);
+    if (b->d_claim) cudaFree(b->d_claim);
     if (b->h_in) cudaFreeHost(b->h_in);
     if (b->h_out) cudaFreeHost(b->h_out);
     delete b;
@@ -534,7 +551,7 @@ uslam_status create_batch(uslam_ctx* ctx, int n_frames, const int* widths, const
                                                std::max(b->frames[pair_prev[p]].cap, 1) * 16);
             }
     }
-    const size_t err_off = take(&scratch, 256);  // error word, then k_match's group counter
+    const size_t err_off = take(&scratch, 256);  // error word
     const size_t frames_off = take(&scratch, sizeof(FrameDev) * n_frames);
     const size_t pairs_off = take(&scratch, sizeof(PairDev) * std::max(n_pairs, 1));
     in_bytes = round_up(in_bytes, 256);
@@ -710,6 +727,24 @@ uslam_status create_batch(uslam_ctx* ctx, int n_frames, const int* widths, const
                 return s;
             }
             progs.push_back(&b->pair_prog[p]);
+        }
+    }
+    // k_match's claim blocks: per lane the counters and an order of up to
+    // max_groups query groups (every program's groups are at most the full
+    // program's), zeroed once here and by k_mutual after every launch
+    {
+        size_t max_groups = 0;
+        for (int p = 0; p < n_pairs; ++p)
+            max_groups += static_cast<size_t>(L) *
+                          (static_cast<size_t>(std::max(b->frames[pair_prev[p]].cap, 1)) / 32 + USLAM_MATCH_BANDS + 1);
+        b->claim_words = match_claim_words(max_groups);
+        b->claim_stride = round_up(b->claim_words * sizeof(uint32_t), 256) + round_up(std::max<size_t>(max_groups, 1), 256);
+        e = cudaMalloc(&b->d_claim, b->claim_stride * kLanes);
+        if (e == cudaSuccess) e = cudaMemset(b->d_claim, 0, b->claim_stride * kLanes);
+        if (e != cudaSuccess) {
+            free_batch(b);
+            cudaGetLastError();
+            return set_err(&ctx->err, USLAM_OOM, "match claim blocks: allocation refused");
         }
     }
     size_t tbytes = 0;
@@ -1090,12 +1125,12 @@ uslam_status uslam_batch_profile(uslam_batch* b, int iters, float* kernel_ms) {
                 : b->win_tc ? launch_win_match(b->d_frames, b->d_pairs, P.msegs, P.nmsegs, b->win_umax, P.units,
                                                c->num_sms, b->d_err, b->stream)
                     : launch_match_dyn(b->d_frames, b->d_pairs, P.msegs, P.nmsegs, c->num_sms,
-                                       b->d_err + 1, b->stream);
+                                       lane_claim(b, 0), lane_gbucket(b, 0), b->stream);
         mark();
         if (e == cudaSuccess)
             e = c->matcher != 0 ? launch_emit(b->d_frames, b->d_pairs, P.usegs, P.nusegs, b->d_err, b->stream)
                                 : launch_mutual_reset(b->d_frames, b->d_pairs, P.usegs, P.nusegs, b->d_err,
-                                                      b->d_err + 1, b->stream);
+                                                      lane_claim(b, 0), b->stream);
         mark();
         if (e == cudaSuccess) e = cudaEventSynchronize(ev[K]);
         for (int q = 0; q < K && e == cudaSuccess; ++q) {

@@ -42,7 +42,8 @@ cudaError_t set_describe_tiled_smem(int margin);
 // k_match over num_sms x its resident CTAs; _dyn: its warps claim query groups from next_group
 cudaError_t launch_match(const FrameDev*, const PairDev*, const void* segs, int nseg, int num_sms, cudaStream_t);
 cudaError_t launch_match_dyn(const FrameDev*, const PairDev*, const void* segs, int nseg, int num_sms,
-                             uint32_t* next_group, cudaStream_t);
+                             uint32_t* claim, uint8_t* gbucket, cudaStream_t);
+size_t match_claim_words(size_t max_groups);  // u32 words of one claim block
 cudaError_t launch_mutual(const FrameDev*, const PairDev*, const SegDev*, int, uint32_t*, cudaStream_t);
 cudaError_t launch_bacc_init(const FrameDev*, const PairDev*, const SegDev*, int, cudaStream_t);
 cudaError_t launch_mutual_reset(const FrameDev*, const PairDev*, const SegDev*, int, uint32_t*, uint32_t*,
