@@ -242,17 +242,19 @@ cudaError_t enqueue_frames(uslam_batch* b, const Program& P, const Lane& ln) {
     uslam_ctx* c = b->ctx;
     cudaError_t e = cudaSuccess;
     if (P.ntiles <= 0) return e;
-    if ((e = launch_detect_shaped(b->d_frames, P.tiles, P.tile_begin, c->detector, b->d_err, ln.st)) != cudaSuccess)
-        return e;
+    if ((e = launch_pyramid_shaped(b->d_frames, P.tiles, P.tile_begin, ln.st)) != cudaSuccess) return e;
     const int grid = c->num_sms * 4;
-    // k_blur_border (the blur cache's border) and the compaction (the
-    // keypoint lists) both read only what k_detect wrote: the border runs on a
-    // forked stream beside the compaction and joins before k_describe,
-    // which needs both (in a captured graph this is a fork/join).
+    // k_blur_border (the blur cache beyond the level edges) reads only the
+    // pyramid and the frame, and writes cells k_detect does not: it runs on a
+    // forked stream beside k_detect and the compaction and joins before
+    // k_describe, which needs both (in a captured graph this is a fork/join).
     if ((e = cudaEventRecord(ln.fork, ln.st)) != cudaSuccess) return e;
     if ((e = cudaStreamWaitEvent(ln.aux, ln.fork, 0)) != cudaSuccess) return e;
     if ((e = launch_blur_border(b->d_frames, P.fsegs, P.nfsegs, grid, ln.aux)) != cudaSuccess) return e;
     if ((e = cudaEventRecord(ln.join, ln.aux)) != cudaSuccess) return e;
+    if ((e = launch_detect_only_shaped(b->d_frames, P.tiles, P.tile_begin, c->detector, b->d_err, ln.st)) !=
+        cudaSuccess)
+        return e;
     if ((e = launch_compact_banded(b->d_frames, P.bands, P.nbands, P.fsegs, P.nfsegs, b->max_w, ln.st)) !=
         cudaSuccess)
         return e;

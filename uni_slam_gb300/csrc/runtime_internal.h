@@ -197,16 +197,34 @@ struct ShapedTiles {
     }
 };
 
-// One k_pyramid launch, then one k_detect launch, per tile shape present
-// (every pyramid level is written before any tile of that shape reads it).
-inline cudaError_t launch_detect_shaped(const FrameDev* frames, const TileItem* d_tiles, const int* begin,
-                                        int detector, uint32_t* err, cudaStream_t st) {
+// One k_pyramid launch per tile shape present.
+inline cudaError_t launch_pyramid_shaped(const FrameDev* frames, const TileItem* d_tiles, const int* begin,
+                                         cudaStream_t st) {
     for (int s = 0; s < kNumTileShapes; ++s) {
         const int n = begin[s + 1] - begin[s];
         if (n <= 0) continue;
         const cudaError_t e = launch_pyramid(frames, d_tiles + begin[s], n, s, st);
         if (e != cudaSuccess) return e;
     }
+    return cudaSuccess;
+}
+// One k_detect launch per tile shape present (after every pyramid level is written).
+inline cudaError_t launch_detect_only_shaped(const FrameDev* frames, const TileItem* d_tiles, const int* begin,
+                                             int detector, uint32_t* err, cudaStream_t st) {
+    for (int s = 0; s < kNumTileShapes; ++s) {
+        const int n = begin[s + 1] - begin[s];
+        if (n <= 0) continue;
+        const cudaError_t e = launch_detect(frames, d_tiles + begin[s], n, s, detector, err, st);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+// One k_pyramid launch, then one k_detect launch, per tile shape present
+// (every pyramid level is written before any tile of that shape reads it).
+inline cudaError_t launch_detect_shaped(const FrameDev* frames, const TileItem* d_tiles, const int* begin,
+                                        int detector, uint32_t* err, cudaStream_t st) {
+    const cudaError_t e = launch_pyramid_shaped(frames, d_tiles, begin, st);
+    if (e != cudaSuccess) return e;
     for (int s = 0; s < kNumTileShapes; ++s) {
         const int n = begin[s + 1] - begin[s];
         if (n <= 0) continue;
