@@ -1484,7 +1484,7 @@ k_describe_tiled(const FrameDev* __restrict__ frames, const BandItem* __restrict
     const uint32_t* feats = F.feats[l];
     bool box_ready = false;
     for (uint32_t base = pos0; base < pos1; base += KDT_THREADS) {
-        // this round's keypoints with x in the chunk, in list order
+        // this pass's keypoints with x in the chunk, in list order
         const uint32_t i = base + (uint32_t)t;
         bool sel = false;
         if (i < pos1) {
@@ -1588,7 +1588,7 @@ k_describe_tiled(const FrameDev* __restrict__ frames, const BandItem* __restrict
             for (int k = 0; k < 8; ++k) words[k] = __ballot_sync(0xffffffffu, ga[k] > gb[k]);
             emit_feature<PACK, WIN>(F, l, i2, w, y, theta, words, lane);
         }
-        __syncthreads();  // s_list / s_wcount reused by the next round
+        __syncthreads();  // s_list / s_wcount reused by the next pass
     }
     if (!box_ready) mbar_wait(&s_bar, 0u, kTmaWaitLimit);  // no keypoint in the chunk: the load lands first
 }
