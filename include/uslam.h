@@ -391,6 +391,10 @@ uslam_status uslam_server_open_stream(uslam_server* server, int width, int heigh
  * at a time, in order. */
 uslam_status uslam_server_submit(uslam_server* server, int stream, const uint8_t* img, int pitch,
                                  int promote_keyframe, uint64_t* ticket);
+/* Wait until the request has finished (timeout_ms <= 0: no limit).  After a
+ * failed launch or a tripped kernel check the server launches nothing more:
+ * requests in flight and queued finish with that status (USLAM_CUDA_ERROR or
+ * USLAM_KERNEL_CHECK), and submit refuses new frames with it. */
 uslam_status uslam_server_wait(uslam_server* server, uint64_t ticket, int timeout_ms);
 /* Features of the frame (as uslam_batch_features) and its mutual matches
  * against the keyframe it was submitted against (lod_a/idx_a = keyframe).
@@ -402,6 +406,12 @@ uslam_status uslam_server_result(uslam_server* server, uint64_t ticket, uslam_fe
 uslam_status uslam_server_release(uslam_server* server, uint64_t ticket);
 uslam_status uslam_server_stats(uslam_server* server, uint64_t* launches, uint64_t* frames, int* max_batch_seen,
                                 int* slots_total);
+/* Test hook for the served form's failure path (no reference counterpart),
+ * as uslam_batch_set_first_wait: the polls of the first mbarrier wait of
+ * k_detect's tile load in every slot (-1 restores the kernel's own limit).
+ * A wait that runs out trips the launch's kernel check without any fault.
+ * Call with no request in flight. */
+uslam_status uslam_server_set_first_wait(uslam_server* server, int detect_polls);
 
 /* ---- matcher for callers that cannot allocate ---------------------------- */
 

@@ -98,3 +98,43 @@ def test_admission_refuses_without_a_free_slot(brief_pattern):
             srv.close()
     finally:
         ctx.close()
+
+
+def test_failure_finishes_queued_requests(brief_pattern):
+    """The served form's failure path, without any GPU fault: with 0 polls for
+    the first wait of k_detect's tile load, every launch trips its kernel check
+    (USLAM_ERR_TMA_TIMEOUT, recorded once the copy in flight has landed).  With
+    one frame per launch, at most two launches are in flight and the rest of
+    the frames queue; the launches in flight and the queued requests all
+    finish with USLAM_KERNEL_CHECK (bounded waits: a request left unfinished
+    would time out instead), and the server refuses new frames with it."""
+    from uni_slam_gb300 import USlamError, capi
+
+    ctx = Context(brief_pattern, levels=6, max_width=752, max_height=480)
+    try:
+        frames = synth.plane_sequence(9, n=8)
+        srv = Server(ctx, [(752, 480)], hbm_budget_bytes=256 << 20, max_batch=1)
+        try:
+            sid = srv.open_stream(752, 480)
+            ctx.check(ctx.lib.uslam_server_set_first_wait(srv.h, 0), "set_first_wait")
+            tickets = []
+            for f in frames:
+                try:
+                    t = srv.submit(sid, f)
+                except USlamError as e:  # the first launch already failed
+                    assert e.status == capi.KERNEL_CHECK
+                    break
+                assert t is not None
+                tickets.append(t)
+            assert tickets
+            for t in tickets:
+                with pytest.raises(USlamError) as ei:
+                    srv.wait(t, 10000)
+                assert ei.value.status == capi.KERNEL_CHECK, str(ei.value)
+            with pytest.raises(USlamError) as ei:
+                srv.submit(sid, frames[0])
+            assert ei.value.status == capi.KERNEL_CHECK
+        finally:
+            srv.close()
+    finally:
+        ctx.close()

@@ -117,6 +117,7 @@ SIGNATURES = {
                                       C.POINTER(C.c_double)]),
     "uslam_server_release": (C.c_int, [_vp, C.c_uint64]),
     "uslam_server_stats": (C.c_int, [_vp, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64), _ip, _ip]),
+    "uslam_server_set_first_wait": (C.c_int, [_vp, C.c_int]),
     "uslam_featset_create": (C.c_int, [_vp, C.c_int, C.c_int, C.POINTER(_vp)]),
     "uslam_featset_destroy": (None, [_vp]),
     "uslam_detect_describe": (C.c_int, [_vp, _vp, C.c_int, C.c_int, C.c_int, _vp]),

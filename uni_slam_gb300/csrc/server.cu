@@ -380,6 +380,20 @@ void dispatcher(uslam_server* s) {
             progressed = true;
         }
         if (progressed) s->cv_done.notify_all();
+        if (!s->fatal.empty() && !s->pending.empty()) {
+            // after a failure nothing more is launched: what is queued
+            // finishes now, and its waiters see the failure
+            const auto now = Clock::now();
+            while (!s->pending.empty()) {
+                const auto it = s->reqs.find(s->pending.front());
+                s->pending.pop_front();
+                if (it == s->reqs.end()) continue;
+                it->second.done = true;
+                it->second.t_done = now;
+                if (it->second.ref >= 0) --s->slots[it->second.ref].refs;
+            }
+            s->cv_done.notify_all();
+        }
         // launch whatever is queued on a free table buffer
         int bufi = !s->bufs[0].busy ? 0 : (!s->bufs[1].busy ? 1 : -1);
         if (!s->pending.empty() && bufi >= 0 && s->fatal.empty()) {
@@ -673,8 +687,7 @@ uslam_status uslam_server_submit(uslam_server* s, int stream, const uint8_t* img
     if (stream < 0 || stream >= static_cast<int>(s->streams.size()))
         return set_err(&s->ctx->err, USLAM_INVALID_ARG, "submit: unknown stream");
     if (!s->fatal.empty()) return set_err(&s->ctx->err, s->fatal_status, s->fatal);
-    SrvStream& S = s->streams[stream];
-    const SrvClass& C = s->classes[S.cls];
+    const SrvClass& C = s->classes[s->streams[stream].cls];
     if (pitch < C.W0) return set_err(&s->ctx->err, USLAM_INVALID_ARG, "submit: pitch smaller than the frame width");
     int slot = -1;
     for (int i = 0; i < C.n_slots; ++i)
@@ -692,6 +705,8 @@ uslam_status uslam_server_submit(uslam_server* s, int stream, const uint8_t* img
     for (int y = 0; y < F.H0; ++y)
         std::memcpy(sl.h_in + static_cast<size_t>(y) * F.img_pitch, img + static_cast<size_t>(y) * pitch, F.W0);
     lk.lock();
+    // taken after the copy: open_stream may have grown the stream table meanwhile
+    SrvStream& S = s->streams[stream];
     SrvReq r;
     r.stream = stream;
     r.slot = slot;
@@ -716,14 +731,19 @@ uslam_status uslam_server_submit(uslam_server* s, int stream, const uint8_t* img
 uslam_status uslam_server_wait(uslam_server* s, uint64_t ticket, int timeout_ms) {
     if (!s) return USLAM_INVALID_ARG;
     std::unique_lock<std::mutex> lk(s->mu);
-    auto it = s->reqs.find(ticket);
-    if (it == s->reqs.end()) return set_err(&s->ctx->err, USLAM_INVALID_ARG, "wait: unknown ticket");
-    auto ready = [&] { return s->reqs[ticket].done; };
+    if (s->reqs.find(ticket) == s->reqs.end()) return set_err(&s->ctx->err, USLAM_INVALID_ARG, "wait: unknown ticket");
+    // looked up on every wake-up: another thread may release the ticket meanwhile
+    auto ready = [&] {
+        const auto i = s->reqs.find(ticket);
+        return i == s->reqs.end() || i->second.done;
+    };
     if (timeout_ms <= 0) {
         s->cv_done.wait(lk, ready);
     } else if (!s->cv_done.wait_for(lk, std::chrono::milliseconds(timeout_ms), ready)) {
         return set_err(&s->ctx->err, USLAM_TIMEOUT, "wait: request not finished in time");
     }
+    if (s->reqs.find(ticket) == s->reqs.end())
+        return set_err(&s->ctx->err, USLAM_INVALID_ARG, "wait: ticket released while waiting");
     if (!s->fatal.empty()) return set_err(&s->ctx->err, s->fatal_status, s->fatal);
     return USLAM_OK;
 }
@@ -785,6 +805,24 @@ uslam_status uslam_server_stats(uslam_server* s, uint64_t* launches, uint64_t* f
     if (frames) *frames = s->n_frames;
     if (max_batch_seen) *max_batch_seen = s->max_batch_seen;
     if (slots_total) *slots_total = static_cast<int>(s->slots.size());
+    return USLAM_OK;
+}
+
+uslam_status uslam_server_set_first_wait(uslam_server* s, int detect_polls) {
+    if (!s) return USLAM_INVALID_ARG;
+    if (detect_polls < -1) return set_err(&s->ctx->err, USLAM_INVALID_ARG, "set_first_wait: bad arguments");
+    std::lock_guard<std::mutex> lk(s->mu);
+    if (!s->inflight.empty() || !s->pending.empty())
+        return set_err(&s->ctx->err, USLAM_NOT_READY, "set_first_wait: requests in flight");
+    for (FrameDev& F : s->frames) F.detect_first_wait = detect_polls;
+    // the kernels read the slot table at run time
+    cudaSetDevice(s->ctx->device);
+    const cudaError_t e =
+        cudaMemcpy(s->d_frames, s->frames.data(), sizeof(FrameDev) * s->frames.size(), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return set_err(&s->ctx->err, USLAM_CUDA_ERROR, "set_first_wait: slot table upload");
+    }
     return USLAM_OK;
 }
 
