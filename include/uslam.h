@@ -394,7 +394,8 @@ uslam_status uslam_server_submit(uslam_server* server, int stream, const uint8_t
 /* Wait until the request has finished (timeout_ms <= 0: no limit).  After a
  * failed launch or a tripped kernel check the server launches nothing more:
  * requests in flight and queued finish with that status (USLAM_CUDA_ERROR or
- * USLAM_KERNEL_CHECK), and submit refuses new frames with it. */
+ * USLAM_KERNEL_CHECK), uslam_server_result returns it for them (they have no
+ * results; release them as usual), and submit refuses new frames with it. */
 uslam_status uslam_server_wait(uslam_server* server, uint64_t ticket, int timeout_ms);
 /* Features of the frame (as uslam_batch_features) and its mutual matches
  * against the keyframe it was submitted against (lod_a/idx_a = keyframe).

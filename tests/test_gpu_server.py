@@ -131,6 +131,11 @@ def test_failure_finishes_queued_requests(brief_pattern):
                 with pytest.raises(USlamError) as ei:
                     srv.wait(t, 10000)
                 assert ei.value.status == capi.KERNEL_CHECK, str(ei.value)
+                # no results for a failed request
+                with pytest.raises(USlamError) as ei:
+                    srv.result(t)
+                assert ei.value.status == capi.KERNEL_CHECK, str(ei.value)
+                srv.release(t)
             with pytest.raises(USlamError) as ei:
                 srv.submit(sid, frames[0])
             assert ei.value.status == capi.KERNEL_CHECK

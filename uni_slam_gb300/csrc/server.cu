@@ -61,6 +61,7 @@ struct SrvSlot {
 struct SrvReq {
     int stream = 0, slot = 0, ref = -1;
     bool promote = false, done = false;
+    bool failed = false;  // finished without results (a failed launch, or queued at a failure)
     Clock::time_point t_submit, t_done;
 };
 
@@ -367,9 +368,11 @@ void dispatcher(uslam_server* s) {
                 s->fatal_status = USLAM_KERNEL_CHECK;
             }
             const auto now = Clock::now();
+            const bool failed = q != cudaSuccess || s->h_err[L.buf] != 0u;
             for (uint64_t tk : L.tickets) {
                 SrvReq& r = s->reqs[tk];
                 r.done = true;
+                r.failed = failed;
                 r.t_done = now;
                 if (s->slots[r.slot].producer_launch == L.id) s->slots[r.slot].producer_launch = -1;
                 if (r.ref >= 0) --s->slots[r.ref].refs;
@@ -389,6 +392,7 @@ void dispatcher(uslam_server* s) {
                 s->pending.pop_front();
                 if (it == s->reqs.end()) continue;
                 it->second.done = true;
+                it->second.failed = true;
                 it->second.t_done = now;
                 if (it->second.ref >= 0) --s->slots[it->second.ref].refs;
             }
@@ -419,6 +423,7 @@ void dispatcher(uslam_server* s) {
                 for (uint64_t tk : batch) {
                     SrvReq& r = s->reqs[tk];
                     r.done = true;
+                    r.failed = true;
                     r.t_done = now;
                     s->slots[r.slot].producer_launch = -1;
                     if (r.ref >= 0) --s->slots[r.ref].refs;
@@ -754,6 +759,7 @@ uslam_status uslam_server_result(uslam_server* s, uint64_t ticket, uslam_feature
     std::unique_lock<std::mutex> lk(s->mu);
     auto it = s->reqs.find(ticket);
     if (it == s->reqs.end() || !it->second.done) return set_err(&s->ctx->err, USLAM_NOT_READY, "result: not finished");
+    if (it->second.failed) return set_err(&s->ctx->err, s->fatal_status, "result: request failed: " + s->fatal);
     const SrvReq r = it->second;
     const FrameDev F = s->frames[r.slot];
     const SrvSlot sl = s->slots[r.slot];
