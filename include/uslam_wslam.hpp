@@ -71,8 +71,13 @@ class CudaFrontend {
         p.brief_pattern = pattern_.data();
         if (uslam_status s = uslam_create(&p, &ctx_); s != USLAM_OK)
             return std::string("uslam_create: ") + uslam_status_string(s);
-        if (uslam_status s = uslam_frontend_create(ctx_, width, height, &fe_); s != USLAM_OK)
-            return std::string("uslam_frontend_create: ") + uslam_last_error(ctx_);
+        if (uslam_status s = uslam_frontend_create(ctx_, width, height, &fe_); s != USLAM_OK) {
+            std::string msg = std::string("uslam_frontend_create: ") + uslam_last_error(ctx_);
+            uslam_destroy(ctx_);  // the next frame starts over
+            ctx_ = nullptr;
+            fe_ = nullptr;
+            return msg;
+        }
         width_ = width;
         height_ = height;
         return std::nullopt;
@@ -105,8 +110,10 @@ class CudaFeatureDetectPass : public compute::Pass {
         if (auto err = gpu_->ensure(f.width, f.height)) return err;
         // consume-once marker (common.hpp:134-142), as LoadDataCPUPass does
         const bool advance = storage_.take<bool>(ResourceIdentifier::FeatureReferenceAdvanceName).value_or(false);
-        // provider_base.cpp:121-124 stored u8 / 255: the library recovers each
-        // byte exactly while staging the frame in pinned memory and uploads u8
+        // provider_base.cpp:121-124 stored u8 / 255: the library copies the f32
+        // pixels into pinned staging, uploads them as f32 (as
+        // FillPyramidPass::writeBaseLayer does) and recovers each byte exactly
+        // on the device
         const uslam_status s = uslam_frontend_process_f32(gpu_->frontend(), f.pixels.data(), f.width, advance ? 1 : 0);
         if (s != USLAM_OK && s != USLAM_NOT_READY)
             return std::string("uslam_frontend_process: ") + uslam_last_error(gpu_->ctx());
