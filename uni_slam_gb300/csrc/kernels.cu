@@ -65,7 +65,6 @@ __device__ __forceinline__ constexpr int circle_x(int i) {
 // A quarter turn maps point i to point i + 4 ((x, y) -> (-y, x)), so y_i = -x_(i+4).
 __device__ __forceinline__ constexpr int circle_y(int i) { return -circle_x((i + 4) & 15); }
 
-
 // Tint robustness clamp of textureLoad coordinates: min(u32(c), n - 1).
 __device__ __forceinline__ int tint_clamp(int c, int n) {
     const unsigned u = (unsigned)c;
@@ -77,34 +76,6 @@ __device__ __forceinline__ int edge_index(float f, int n) {
     if (f <= 0.0f) return 0;
     if (f >= (float)(n - 1)) return n - 1;
     return (int)f;
-}
-
-__device__ __forceinline__ float lod0_texel(const FrameDev& F, int x, int y) {
-    return (float)__ldg(F.img + (size_t)y * (size_t)F.img_pitch + x) / 255.0f;
-}
-
-// Level pixel (x, y) of level l: LOD0 = u8/255, l >= 1 = one canonical
-// bilinear tap of LOD0 at the texel centre (resources/create_pyramid.wgsl:11-12).
-__device__ float pyramid_pixel(const FrameDev& F, int l, int x, int y) {
-    if (l == 0) return lod0_texel(F, x, y);
-    const float uvx = ((float)x + 0.5f) / (float)F.w[l];
-    const float uvy = ((float)y + 0.5f) / (float)F.h[l];
-    const float u = uvx * (float)F.W0 - 0.5f;
-    const float v = uvy * (float)F.H0 - 0.5f;
-    const float fi = floorf(u);
-    const float fj = floorf(v);
-    const float a = u - fi;
-    const float b = v - fj;
-    const int i0 = edge_index(fi, F.W0), i1 = edge_index(fi + 1.0f, F.W0);
-    const int j0 = edge_index(fj, F.H0), j1 = edge_index(fj + 1.0f, F.H0);
-    const float t00 = lod0_texel(F, i0, j0), t10 = lod0_texel(F, i1, j0);
-    const float t01 = lod0_texel(F, i0, j1), t11 = lod0_texel(F, i1, j1);
-    const float na = 1.0f - a, nb = 1.0f - b;
-    float r = (na * nb) * t00;
-    r = r + (a * nb) * t10;
-    r = r + (na * b) * t01;
-    r = r + (a * b) * t11;
-    return r;
 }
 
 // FAST response at smem cell (r, c): 1 + longest non-wrapping run of
