@@ -8,7 +8,6 @@ pinned against the reference's own compiled source; WGSL stages unpinned).
 from __future__ import annotations
 
 import ctypes as C
-import glob
 import os
 
 import numpy as np
@@ -272,8 +271,3 @@ def ref_matcher_expected() -> bool:
     in baseline/_ref travels with the repository), so oracle/_ref must hold
     the compiled matcher and the live checks against it must run."""
     return os.path.exists(STAGED_MATCHER)
-
-
-def ref_matcher_sizes():
-    return sorted(os.path.basename(p)[len("libref_matcher_"):-3]
-                  for p in glob.glob(os.path.join(REF_DIR, "libref_matcher_*.so")))
