@@ -3,7 +3,6 @@
 and cannot run them (no Dawn, no graphics stack), so these known answers
 are the pins the oracle's detect / cull / describe logic rests on."""
 import numpy as np
-import pytest
 
 import oracle
 
